@@ -1,0 +1,16 @@
+"""comd_gb300: CoMD's force-and-integrate timestep on GB300 (sm_103a).
+
+The product is ``libcomdgb.so`` (C ABI in ``include/comdgb.h``): link-cell
+binning, LJ and EAM (table or Chebyshev) force kernels in FP64 or mixed
+precision, and the velocity-Verlet loop, driven from C as a drop-in for the
+reference's ``simflat_t`` / ``pot->force`` / ``nTimeSteps``.  This Python
+package only builds and binds the library for tests and benchmarks.
+"""
+from . import abi
+from .lib import (DISP_GAUSSIAN, DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY,
+                  POT_EAM_TABLE, POT_LJ, PREC_FP64, PREC_MIXED, ComdgbError, DeviceSim,
+                  eam_potential, fcc, free_host, lj_potential, load, opts, seed)
+
+__all__ = ["abi", "load", "opts", "DeviceSim", "ComdgbError", "eam_potential", "lj_potential",
+           "fcc", "seed", "free_host", "POT_DIR", "POT_EAM_TABLE", "POT_EAM_CHEBY", "POT_LJ",
+           "PREC_FP64", "PREC_MIXED", "DISP_NONE", "DISP_UNIFORM", "DISP_GAUSSIAN"]

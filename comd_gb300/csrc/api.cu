@@ -1,0 +1,985 @@
+// api.cu -- the C ABI of libcomdgb: device mirror of a simflat_t, the force
+// call, the velocity-Verlet loop (captured in CUDA graphs) and the drop-in
+// wrappers keyed by the caller's simflat_t pointer.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "comdgb.h"
+#include "internal.h"
+
+using namespace cg;
+
+namespace {
+
+thread_local char g_err[512] = "";
+std::mutex g_reg_mu;
+
+int set_err(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return set_err(COMDGB_ERR_CUDA, "%s failed: %s (%s:%d)", #call,                   \
+                     cudaGetErrorString(e_), __FILE__, __LINE__);                       \
+  } while (0)
+
+// bohr_per_atu_to_A_per_s (constants.h:61) and amu_to_m_e (constants.h:65)
+const double kBohrPerAtu = (double)0.529 / (double)2.418e-17;
+const double kAmuToMe = 1822.83;
+
+enum KernelGroup {
+  KG_ADV_POS = 0,
+  KG_REBIN1,
+  KG_COMPACT,
+  KG_NBR,
+  KG_PASS1,
+  KG_PASS2,
+  KG_ADV_VP,
+  KG_REBIN2,
+  KG_COUNT
+};
+const char *kGroupName[KG_COUNT] = {"advance_positions+classify", "rebin_plan_apply",
+                                    "compact_atoms",              "nbr_build",
+                                    "force_pass1",                "force_pass2",
+                                    "advance_velocity_positions+classify",
+                                    "rebin_plan_apply_2"};
+
+template <class T>
+T *dalloc(size_t n, int *err) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+    *err = 1;
+    return nullptr;
+  }
+  return (T *)p;
+}
+
+}  // namespace
+
+struct comdgb_sim {
+  int device = 0;
+  comdgb_opts opts{};
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  Geom g{};
+  int ntot = 0, nslots = 0;
+  double rmass = 1.0, cutoff = 0.0;
+  double volume = 1.0;
+  std::vector<void *> allocs;
+  Slots s{};
+  RebinWork w{};
+  EntryTab et{};
+  double *dcenter = nullptr;
+  int *box_start = nullptr, *atom_slot = nullptr, *cpart = nullptr;
+  int ncpart = 0;
+  uint16_t *nbr = nullptr;
+  int *nbr_n = nullptr;
+  int cap = 0;
+  double *atom_stress = nullptr;
+  double *rpart = nullptr;
+  long long *ripart = nullptr;
+  int nrpart = 0;
+  double *d_out = nullptr;     // [0] energy sum [1] stress sum [2] kinetic
+  long long *d_iout = nullptr; // [0] directed pair count
+  int *status = nullptr;
+  double *stage3 = nullptr;    // real3 staging for host transfers
+  int *bin_tmp = nullptr;
+  // potentials
+  EamPot<double, EVAL_TABLE> eam64t{};
+  EamPot<double, EVAL_CHEBY> eam64c{};
+  EamPot<float, EVAL_TABLE> eam32t{};
+  EamPot<float, EVAL_CHEBY> eam32c{};
+  LjPot<double> lj64{};
+  LjPot<float> lj32{};
+  double lj_eps = 0, lj_s6 = 0;
+  // graphs
+  cudaGraphExec_t step_exec = nullptr;
+  cudaGraphExec_t force_exec = nullptr;
+  double graph_dt = NAN;
+  // timing graph (event record nodes between kernel groups)
+  cudaGraphExec_t timed_exec = nullptr;
+  cudaGraph_t timed_graph = nullptr;
+  double timed_dt = NAN;
+  std::vector<cudaGraphNode_t> timed_nodes;  // event record nodes, group order
+  std::vector<cudaEvent_t> timed_cap_events;
+  // host last results
+  double e = 0.0, stress = 0.0;
+  simflat_t *host = nullptr;   // drop-in owner (attach)
+  bool host_pinned = false;
+};
+
+namespace {
+
+std::vector<comdgb_sim *> g_attached;
+
+ForceArgs force_args(comdgb_sim *h) {
+  ForceArgs A;
+  A.g = h->g;
+  A.s = h->s;
+  A.et = h->et;
+  A.atom_slot = h->atom_slot;
+  A.box_start = h->box_start;
+  A.ntot = h->ntot;
+  A.nbr = h->nbr;
+  A.nbr_n = h->nbr_n;
+  A.cap = h->cap;
+  A.atom_stress = h->atom_stress;
+  A.status = h->status;
+  return A;
+}
+
+template <class T>
+T *track(comdgb_sim *h, T *p) {
+  h->allocs.push_back((void *)p);
+  return p;
+}
+
+int alloc_slots(comdgb_sim *h, Slots &s, bool with_natoms, int *err) {
+  size_t ns = (size_t)h->nslots;
+  s.natoms = with_natoms ? track(h, dalloc<int>(h->g.nboxes, err)) : nullptr;
+  s.id = track(h, dalloc<int>(ns, err));
+  s.itype = track(h, dalloc<int>(ns, err));
+  s.mass = track(h, dalloc<double>(ns, err));
+  s.r = track(h, dalloc<d4>(ns, err));
+  s.p = track(h, dalloc<d4>(ns, err));
+  s.f = track(h, dalloc<d4>(ns, err));
+  s.rho = track(h, dalloc<double>(ns, err));
+  s.fi = track(h, dalloc<double>(ns, err));
+  s.pos32 = track(h, dalloc<float4>(ns, err));
+  s.fi32 = with_natoms ? track(h, dalloc<float>(ns, err)) : nullptr;
+  return *err;
+}
+
+void free_all(comdgb_sim *h) {
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+  if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
+  if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
+  if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
+  for (cudaEvent_t e : h->timed_cap_events) cudaEventDestroy(e);
+  for (void *p : h->allocs)
+    if (p) cudaFree(p);
+  h->allocs.clear();
+  if (h->stream) cudaStreamDestroy(h->stream);
+}
+
+int neighbor_capacity(const simflat_t *s, double rc) {
+  double vol = s->bounds[0] * s->bounds[1] * s->bounds[2];
+  double dens = vol > 0 ? (double)s->ntot / vol : 0.0;
+  double expect = 4.18879020478639 * rc * rc * rc * dens;
+  int cap = (int)(1.4 * expect) + 24;
+  cap = (cap + 7) & ~7;
+  if (cap < 32) cap = 32;
+  if (cap > CG_NNBR * CG_MAXATOMS) cap = CG_NNBR * CG_MAXATOMS;
+  return cap;
+}
+
+template <class T>
+Table<T> upload_table(comdgb_sim *h, const potentialarray_t *a, int *err) {
+  int n = a->n;
+  std::vector<T> v(n + 3);
+  for (int i = -1; i <= n + 1; i++) v[i + 1] = (T)a->values[i];
+  T *d = track(h, dalloc<T>(n + 3, err));
+  Table<T> t{};
+  if (*err) return t;
+  cudaMemcpy(d, v.data(), sizeof(T) * (n + 3), cudaMemcpyHostToDevice);
+  t.v = d + 1;
+  t.x0 = (T)a->x0;
+  t.xn = (T)a->xn;
+  t.invDx = (T)a->invDx;
+  t.n = n;
+  return t;
+}
+
+// series order: 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF
+void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, const double coef[6][CG_NCHEB],
+               const double a[6], const double b[6]) {
+  for (int s = 0; s < 6; s++) {
+    for (int j = 0; j < CG_NCHEB; j++) {
+      c64.c[s][j] = coef[s][j];
+      c32.c[s][j] = (float)coef[s][j];
+    }
+    c64.a[s] = a[s];
+    c64.b[s] = b[s];
+    c64.ys[s] = 2.0 / (b[s] - a[s]);
+    c64.yo[s] = -(a[s] + b[s]) / (b[s] - a[s]);
+    c32.a[s] = (float)a[s];
+    c32.b[s] = (float)b[s];
+    c32.ys[s] = (float)c64.ys[s];
+    c32.yo[s] = (float)c64.yo[s];
+  }
+}
+
+int fit_cheb_gpu(comdgb_sim *h, const eampotential_t *pot, double coef[6][CG_NCHEB],
+                 double a[6], double b[6]) {
+  int err = 0;
+  const potentialarray_t *tabs[3] = {pot->phi, pot->rho, pot->f};
+  double *d = dalloc<double>(2 * CG_NCHEB * 3, &err);
+  if (err) return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for Chebyshev fit");
+  std::vector<double *> tmp;
+  for (int q = 0; q < 3; q++) {
+    const potentialarray_t *t = tabs[q];
+    double *tv = dalloc<double>(t->n + 3, &err);
+    if (err) return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for Chebyshev fit");
+    tmp.push_back(tv);
+    cudaMemcpyAsync(tv, t->values - 1, sizeof(double) * (t->n + 3), cudaMemcpyHostToDevice,
+                    h->stream);
+    launch_cheb_fit(tv + 1, t->x0, t->xn, t->invDx, CG_NCHEB, d + q * CG_NCHEB,
+                    d + (3 + q) * CG_NCHEB, h->stream);
+    a[q] = a[q + 3] = t->x0;
+    b[q] = b[q + 3] = t->xn;
+  }
+  std::vector<double> hbuf(6 * CG_NCHEB);
+  CK(cudaMemcpyAsync(hbuf.data(), d, sizeof(double) * 6 * CG_NCHEB, cudaMemcpyDeviceToHost,
+                     h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int q = 0; q < 6; q++)
+    for (int j = 0; j < CG_NCHEB; j++) coef[q][j] = hbuf[q * CG_NCHEB + j];
+  cudaFree(d);
+  for (double *p : tmp) cudaFree(p);
+  return 0;
+}
+
+int setup_potential(comdgb_sim *h, const simflat_t *s) {
+  int err = 0;
+  const comdgb_opts &o = h->opts;
+  if (o.potential < 0) return 0;  // binning-only simulation
+  if (!s->pot) return set_err(COMDGB_ERR_ARG, "simflat_t has no potential");
+  h->cutoff = s->pot->cutoff;
+  h->rmass = (double)(kAmuToMe * (double)s->pot->mass);
+  if (o.potential == COMDGB_POT_LJ) {
+    const ljpotential_t *lp = (const ljpotential_t *)s->pot;
+    double sg = lp->sigma, s6 = sg * sg * sg * sg * sg * sg;
+    h->lj_eps = lp->epsilon;
+    h->lj_s6 = s6;
+    h->lj64 = LjPot<double>{s6, 12.0 * s6, 4.0 * lp->epsilon * s6, lp->cutoff * lp->cutoff};
+    h->lj32 = LjPot<float>{(float)s6, (float)(12.0 * s6), (float)(4.0 * lp->epsilon * s6),
+                           (float)(lp->cutoff * lp->cutoff)};
+    return 0;
+  }
+  const eampotential_t *ep = (const eampotential_t *)s->pot;
+  if (!ep->phi || !ep->rho || !ep->f) return set_err(COMDGB_ERR_ARG, "EAM tables missing");
+  double rc2 = h->cutoff * h->cutoff;
+  if (o.potential == COMDGB_POT_EAM_TABLE) {
+    h->eam64t.phi = upload_table<double>(h, ep->phi, &err);
+    h->eam64t.rho = upload_table<double>(h, ep->rho, &err);
+    h->eam64t.f = upload_table<double>(h, ep->f, &err);
+    h->eam64t.rc2 = rc2;
+    h->eam32t.phi = upload_table<float>(h, ep->phi, &err);
+    h->eam32t.rho = upload_table<float>(h, ep->rho, &err);
+    h->eam32t.f = upload_table<float>(h, ep->f, &err);
+    h->eam32t.rc2 = (float)rc2;
+    if (err) return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for EAM tables");
+    return 0;
+  }
+  if (o.potential != COMDGB_POT_EAM_CHEBY)
+    return set_err(COMDGB_ERR_ARG, "unknown potential kind %d", o.potential);
+  if (o.n_cheby != CG_NCHEB)
+    return set_err(COMDGB_ERR_UNSUPPORTED, "only %d Chebyshev terms are supported", CG_NCHEB);
+  double coef[6][CG_NCHEB], a[6], b[6];
+  if (o.cheby_from_host) {
+    const eam_cheby_t *ch = s->ch_pot;
+    if (!ch) return set_err(COMDGB_ERR_ARG, "cheby_from_host set but s->ch_pot is NULL");
+    const potentialarray_t *ser[6] = {ch->phi, ch->rho, ch->f, ch->dphi, ch->drho, ch->df};
+    for (int q = 0; q < 6; q++) {
+      if (!ser[q] || ser[q]->n != CG_NCHEB)
+        return set_err(COMDGB_ERR_UNSUPPORTED, "Chebyshev series %d must have %d terms", q,
+                       CG_NCHEB);
+      for (int j = 0; j < CG_NCHEB; j++) coef[q][j] = ser[q]->values[j];
+      a[q] = ser[q]->x0;
+      b[q] = ser[q]->xn;
+    }
+  } else {
+    int rc = fit_cheb_gpu(h, ep, coef, a, b);
+    if (rc) return rc;
+  }
+  fill_cheb(h->eam64c.ch, h->eam32c.ch, coef, a, b);
+  h->eam64c.rc2 = rc2;
+  h->eam32c.rc2 = (float)rc2;
+  return 0;
+}
+
+int read_status(comdgb_sim *h, int *st) {
+  CK(cudaMemcpyAsync(st, h->status, sizeof(int) * ST_COUNT, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int check_status(comdgb_sim *h) {
+  int st[ST_COUNT];
+  int rc = read_status(h, st);
+  if (rc) return rc;
+  if (st[ST_ERROR] == COMDGB_ERR_MAXATOMS)
+    return set_err(COMDGB_ERR_MAXATOMS, "Increase maxatoms: a box reached %d atoms",
+                   CG_MAXATOMS);
+  if (st[ST_ERROR] == COMDGB_ERR_BOXRANGE)
+    return set_err(COMDGB_ERR_BOXRANGE, "an atom's box index fell outside the grid");
+  if (st[ST_ERROR]) return set_err(st[ST_ERROR], "device error %d", st[ST_ERROR]);
+  return 0;
+}
+
+// ---- kernel groups of one step --------------------------------------------
+
+void enqueue_classify_finish(comdgb_sim *h) {
+  launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, h->stream);
+}
+
+void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
+  // ev (optional) records after each group: compact, nbr, pass1, pass2
+  ForceArgs A = force_args(h);
+  cudaStream_t st = h->stream;
+  launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
+                 st);
+  if (ev) cudaEventRecord(ev[evi++], st);
+  const int pot = h->opts.potential;
+  if (h->mixed) {
+    float rc2 = pot == COMDGB_POT_LJ ? h->lj32.rc2 : (float)(h->cutoff * h->cutoff);
+    launch_nbr_build<float>(A, rc2, st);
+  } else {
+    double rc2 = pot == COMDGB_POT_LJ ? h->lj64.rc2 : h->cutoff * h->cutoff;
+    launch_nbr_build<double>(A, rc2, st);
+  }
+  if (ev) cudaEventRecord(ev[evi++], st);
+  if (pot == COMDGB_POT_LJ) {
+    if (h->mixed) launch_lj<float>(A, h->lj32, st);
+    else launch_lj<double>(A, h->lj64, st);
+    if (ev) cudaEventRecord(ev[evi++], st);
+    if (ev) cudaEventRecord(ev[evi++], st);
+    return;
+  }
+  if (pot == COMDGB_POT_EAM_TABLE) {
+    if (h->mixed) launch_eam_pass1<float, EVAL_TABLE>(A, h->eam32t, st);
+    else launch_eam_pass1<double, EVAL_TABLE>(A, h->eam64t, st);
+    if (ev) cudaEventRecord(ev[evi++], st);
+    if (h->mixed) launch_eam_pass2<float, EVAL_TABLE>(A, h->eam32t, st);
+    else launch_eam_pass2<double, EVAL_TABLE>(A, h->eam64t, st);
+  } else {
+    if (h->mixed) launch_eam_pass1<float, EVAL_CHEBY>(A, h->eam32c, st);
+    else launch_eam_pass1<double, EVAL_CHEBY>(A, h->eam64c, st);
+    if (ev) cudaEventRecord(ev[evi++], st);
+    if (h->mixed) launch_eam_pass2<float, EVAL_CHEBY>(A, h->eam32c, st);
+    else launch_eam_pass2<double, EVAL_CHEBY>(A, h->eam64c, st);
+  }
+  if (ev) cudaEventRecord(ev[evi++], st);
+}
+
+void enqueue_reduce(comdgb_sim *h) {
+  ForceArgs A = force_args(h);
+  launch_reduce(A, h->rpart, h->ripart, h->nrpart, h->d_out, h->d_iout, h->stream);
+}
+
+void enqueue_rebox(comdgb_sim *h) {
+  cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), h->stream);
+  launch_classify(h->g, h->s, h->mixed, h->w, h->status, h->stream);
+  enqueue_classify_finish(h);
+}
+
+// one velocity-Verlet step (timestep.c:129-132); ev: optional group events
+void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev) {
+  int evi = 0;
+  cudaStream_t st = h->stream;
+  if (ev) cudaEventRecord(ev[evi++], st);
+  cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
+  launch_advance_positions(h->g, h->s, dt_atu / 2.0, h->rmass, h->mixed, true, h->w, h->status,
+                           st);
+  if (ev) cudaEventRecord(ev[evi++], st);
+  enqueue_classify_finish(h);
+  if (ev) cudaEventRecord(ev[evi++], st);
+  enqueue_force_parts(h, ev, evi);
+  cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
+  launch_advance_vp(h->g, h->s, dt_atu, dt_atu / 2.0, h->rmass, h->mixed, h->w, h->status, st);
+  if (ev) cudaEventRecord(ev[evi++], st);
+  enqueue_classify_finish(h);
+  if (ev) cudaEventRecord(ev[evi++], st);
+}
+
+int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool force) {
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  if (step) enqueue_step(h, dt_atu, nullptr);
+  if (force) {
+    int evi = 0;
+    enqueue_force_parts(h, nullptr, evi);
+    enqueue_reduce(h);
+  }
+  CK(cudaStreamEndCapture(h->stream, &graph));
+  if (*exec) cudaGraphExecDestroy(*exec);
+  cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess)
+    return set_err(COMDGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+int finish_force(comdgb_sim *h) {
+  double out[2];
+  long long iout;
+  CK(cudaMemcpyAsync(out, h->d_out, sizeof(double) * 2, cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaMemcpyAsync(&iout, h->d_iout, sizeof(long long), cudaMemcpyDeviceToHost, h->stream));
+  int rc = check_status(h);
+  if (rc) return rc;
+  (void)iout;
+  double esum = out[0];
+  if (h->opts.potential == COMDGB_POT_LJ) esum = esum * 4.0 * h->lj_eps * h->lj_s6;
+  h->e = esum;
+  h->stress = out[1] / h->volume;
+  if (!std::isfinite(h->e)) return set_err(COMDGB_ERR_NONFINITE, "total energy is %g", h->e);
+  return 0;
+}
+
+int do_force(comdgb_sim *h) {
+  if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
+  if (!h->force_exec) {
+    int rc = capture(h, &h->force_exec, 0.0, false, true);
+    if (rc) return rc;
+  }
+  CK(cudaGraphLaunch(h->force_exec, h->stream));
+  return finish_force(h);
+}
+
+int do_steps(comdgb_sim *h, int n, double dt) {
+  if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
+  double dt_atu = dt * kBohrPerAtu;  // timestep.c:126
+  if (n > 0 && (!h->step_exec || h->graph_dt != dt_atu)) {
+    int rc = capture(h, &h->step_exec, dt_atu, true, false);
+    if (rc) return rc;
+    h->graph_dt = dt_atu;
+  }
+  for (int i = 0; i < n; i++) CK(cudaGraphLaunch(h->step_exec, h->stream));
+  return do_force(h);
+}
+
+// ---- host transfers ---------------------------------------------------------
+
+int upload(comdgb_sim *h, const simflat_t *s) {
+  cudaStream_t st = h->stream;
+  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
+  if (s->nboxes != h->g.nboxes) return set_err(COMDGB_ERR_ARG, "box count changed");
+  if (s->ntot != h->ntot) return set_err(COMDGB_ERR_ARG, "atom count changed");
+  CK(cudaMemcpyAsync(h->s.natoms, s->natoms, nb * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.id, s->id, ns * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.itype, s->iType, ns * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.mass, s->mass, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->stage3, s->r, ns * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
+  launch_unpack3(h->stage3, h->s.r, (long)ns, st);
+  CK(cudaMemcpyAsync(h->stage3 + 3 * ns, s->p, ns * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                     st));
+  launch_unpack3(h->stage3 + 3 * ns, h->s.p, (long)ns, st);
+  CK(cudaMemcpyAsync(h->s.f, s->f, ns * 4 * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.rho, s->rho, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.fi, s->fi, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (h->mixed) launch_pos32(h->g, h->s, st);
+  CK(cudaMemsetAsync(h->status, 0, sizeof(int) * ST_COUNT, st));
+  CK(cudaGetLastError());
+  return 0;
+}
+
+int download_forces(comdgb_sim *h, simflat_t *s) {
+  cudaStream_t st = h->stream;
+  size_t ns = (size_t)h->nslots;
+  CK(cudaMemcpyAsync(s->f, h->s.f, ns * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->rho, h->s.rho, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->fi, h->s.fi, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  s->e = h->e;
+  s->stress = h->stress;
+  return 0;
+}
+
+int download(comdgb_sim *h, simflat_t *s) {
+  cudaStream_t st = h->stream;
+  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
+  CK(cudaMemcpyAsync(s->natoms, h->s.natoms, nb * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->id, h->s.id, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->iType, h->s.itype, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->mass, h->s.mass, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  launch_pack3(h->s.r, h->stage3, (long)ns, st);
+  CK(cudaMemcpyAsync(s->r, h->stage3, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  launch_pack3(h->s.p, h->stage3 + 3 * ns, (long)ns, st);
+  CK(cudaMemcpyAsync(s->p, h->stage3 + 3 * ns, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                     st));
+  return download_forces(h, s);
+}
+
+int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
+  *out = nullptr;
+  if (!s || !o) return set_err(COMDGB_ERR_ARG, "null argument");
+  if (s->nboxes < 1 || !s->natoms || !s->r)
+    return set_err(COMDGB_ERR_ARG, "simflat_t has no allocated domains");
+  if ((long)s->nboxes * CG_MAXATOMS >= (1L << 31))
+    return set_err(COMDGB_ERR_UNSUPPORTED, "too many boxes");
+  comdgb_sim *h = new comdgb_sim();
+  h->opts = *o;
+  h->device = o->device;
+  h->mixed = o->precision == COMDGB_PREC_MIXED;
+  cudaError_t ce = cudaSetDevice(o->device);
+  if (ce != cudaSuccess) {
+    delete h;
+    return set_err(COMDGB_ERR_CUDA, "cudaSetDevice(%d): %s", o->device, cudaGetErrorString(ce));
+  }
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return set_err(COMDGB_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  for (int j = 0; j < 3; j++) {
+    h->g.nbx[j] = s->nbx[j];
+    h->g.bounds[j] = s->bounds[j];
+    h->g.boxsize[j] = s->boxsize[j];
+  }
+  h->g.nboxes = s->nboxes;
+  h->g.periodic = o->periodic;
+  h->ntot = s->ntot;
+  h->nslots = s->nboxes * CG_MAXATOMS;
+  h->volume = s->bounds[0] * s->bounds[1] * s->bounds[2];
+  int err = 0;
+  size_t nb = (size_t)s->nboxes, ns = (size_t)h->nslots;
+  alloc_slots(h, h->s, true, &err);
+  alloc_slots(h, h->w.stage, false, &err);
+  h->w.dest = track(h, dalloc<int>(ns, &err));
+  h->w.depmask = track(h, dalloc<uint32_t>(2 * nb, &err));
+  h->w.n_lo = track(h, dalloc<int>(nb, &err));
+  h->w.n_dep = track(h, dalloc<int>(nb, &err));
+  h->w.final_len = track(h, dalloc<int>(nb, &err));
+  h->w.final_src = track(h, dalloc<uint8_t>(ns, &err));
+  h->w.dep_order = track(h, dalloc<uint8_t>(ns, &err));
+  h->et.n = track(h, dalloc<int>(nb, &err));
+  h->et.box = track(h, dalloc<int>(nb * CG_NNBR, &err));
+  h->et.dr64 = track(h, dalloc<d4>(nb * CG_NNBR, &err));
+  h->et.dr32 = track(h, dalloc<float4>(nb * CG_NNBR, &err));
+  h->dcenter = track(h, dalloc<double>(nb * 3, &err));
+  h->box_start = track(h, dalloc<int>(nb + 1, &err));
+  h->atom_slot = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
+  h->ncpart = compact_partials(s->nboxes);
+  h->cpart = track(h, dalloc<int>(h->ncpart, &err));
+  double rc = s->pot ? s->pot->cutoff : 1.0;
+  h->cap = neighbor_capacity(s, rc);
+  h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
+  h->nbr_n = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
+  h->atom_stress = track(h, dalloc<double>((size_t)h->ntot + 1, &err));
+  h->nrpart = reduce_partials(h->ntot);
+  h->rpart = track(h, dalloc<double>(2 * (size_t)h->nrpart, &err));
+  h->ripart = track(h, dalloc<long long>(h->nrpart, &err));
+  h->d_out = track(h, dalloc<double>(4, &err));
+  h->d_iout = track(h, dalloc<long long>(2, &err));
+  h->status = track(h, dalloc<int>(ST_COUNT, &err));
+  h->stage3 = track(h, dalloc<double>(ns * 6, &err));
+  if (err) {
+    free_all(h);
+    delete h;
+    return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed (%zu slots)", ns);
+  }
+  if (prepare_nbr_build<double>() != cudaSuccess || prepare_nbr_build<float>() != cudaSuccess)
+    err = 1;
+  cudaMemsetAsync(h->nbr_n, 0, sizeof(int) * ((size_t)h->ntot + 1), h->stream);
+  cudaMemsetAsync(h->atom_stress, 0, sizeof(double) * ((size_t)h->ntot + 1), h->stream);
+  cudaMemcpyAsync(h->dcenter, s->dcenter, nb * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                  h->stream);
+  launch_entry_table(h->g, h->dcenter, h->et, h->stream);
+  int rc2 = setup_potential(h, s);
+  if (!rc2) rc2 = upload(h, s);
+  if (!rc2) {
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) rc2 = set_err(COMDGB_ERR_CUDA, "setup: %s", cudaGetErrorString(e));
+  }
+  if (rc2) {
+    free_all(h);
+    delete h;
+    return rc2;
+  }
+  *out = h;
+  return 0;
+}
+
+comdgb_sim *find_attached(const void *s) {
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  for (comdgb_sim *h : g_attached)
+    if (h->host == s) return h;
+  return nullptr;
+}
+
+void pin_host(comdgb_sim *h, simflat_t *s) {
+  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
+  struct {
+    void *p;
+    size_t n;
+  } regs[] = {{s->natoms, nb * 4},     {s->id, ns * 4}, {s->iType, ns * 4}, {s->mass, ns * 8},
+              {s->r, ns * 24},         {s->p, ns * 24}, {s->f, ns * 32},    {s->rho, ns * 8},
+              {s->fi, ns * 8}};
+  bool ok = true;
+  for (auto &r : regs) ok &= cudaHostRegister(r.p, r.n, cudaHostRegisterDefault) == cudaSuccess;
+  cudaGetLastError();
+  h->host_pinned = ok;
+}
+
+void unpin_host(comdgb_sim *h, simflat_t *s) {
+  if (!h->host_pinned) return;
+  void *ptrs[] = {s->natoms, s->id, s->iType, s->mass, s->r, s->p, s->f, s->rho, s->fi};
+  for (void *p : ptrs) cudaHostUnregister(p);
+  cudaGetLastError();
+  h->host_pinned = false;
+}
+
+}  // namespace
+
+// ============================================================================
+// exported C ABI
+// ============================================================================
+extern "C" {
+
+void comdgb_default_opts(comdgb_opts *o) {
+  o->potential = COMDGB_POT_EAM_TABLE;
+  o->precision = COMDGB_PREC_FP64;
+  o->periodic = 1;
+  o->device = 0;
+  o->n_cheby = CG_NCHEB;
+  o->cheby_from_host = 0;
+}
+
+int comdgb_last_error(char *buf, int len) {
+  if (buf && len > 0) snprintf(buf, (size_t)len, "%s", g_err);
+  return (int)strlen(g_err);
+}
+
+const char *comdgb_version(void) { return "comdgb 0.1 sm_103a"; }
+
+int comdgb_sim_create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
+  return create(s, o, out);
+}
+
+void comdgb_sim_destroy(comdgb_sim *h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  cudaStreamSynchronize(h->stream);
+  free_all(h);
+  delete h;
+}
+
+int comdgb_sim_upload(comdgb_sim *h, const simflat_t *s) {
+  if (!h || !s) return set_err(COMDGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  int rc = upload(h, s);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int comdgb_sim_download(comdgb_sim *h, simflat_t *s) {
+  if (!h || !s) return set_err(COMDGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  return download(h, s);
+}
+
+int comdgb_sim_force(comdgb_sim *h) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  return do_force(h);
+}
+
+int comdgb_sim_steps(comdgb_sim *h, int n, double dt) {
+  if (!h || n < 0) return set_err(COMDGB_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  return do_steps(h, n, dt);
+}
+
+int comdgb_sim_rebox(comdgb_sim *h) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  enqueue_rebox(h);
+  CK(cudaGetLastError());
+  return check_status(h);
+}
+
+int comdgb_sim_energy(comdgb_sim *h, double *e, double *stress) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  if (e) *e = h->e;
+  if (stress) *stress = h->stress;
+  return 0;
+}
+
+int comdgb_sim_kinetic(comdgb_sim *h, double *ek) {
+  if (!h || !ek) return set_err(COMDGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
+                 h->stream);
+  launch_kinetic(h->g, h->s, h->atom_slot, h->ntot, h->rmass, h->rpart, h->nrpart, h->d_out + 2,
+                 h->stream);
+  CK(cudaMemcpyAsync(ek, h->d_out + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int comdgb_sim_pair_count(comdgb_sim *h, long long *pairs) {
+  if (!h || !pairs) return set_err(COMDGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(h->device));
+  long long v = 0;
+  CK(cudaMemcpyAsync(&v, h->d_iout, sizeof(long long), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  *pairs = v / 2;
+  return 0;
+}
+
+int comdgb_sim_synchronize(comdgb_sim *h) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+const char *comdgb_kernel_name(comdgb_sim *h, int k) {
+  (void)h;
+  if (k < 0 || k >= KG_COUNT) return "";
+  return kGroupName[k];
+}
+
+int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, float *kernel_ms,
+                           int max_kernels) {
+  if (!h || n <= 0) return set_err(COMDGB_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  double dt_atu = dt * kBohrPerAtu;
+  const int NE = KG_COUNT + 1;  // events around the groups
+  if (!h->timed_exec || h->timed_dt != dt_atu) {
+    for (cudaEvent_t e : h->timed_cap_events) cudaEventDestroy(e);
+    h->timed_cap_events.assign(NE, nullptr);
+    for (int i = 0; i < NE; i++) CK(cudaEventCreate(&h->timed_cap_events[i]));
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    enqueue_step(h, dt_atu, h->timed_cap_events.data());
+    CK(cudaStreamEndCapture(h->stream, &graph));
+    size_t nn = 0;
+    CK(cudaGraphGetNodes(graph, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+    if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
+    if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
+    h->timed_graph = graph;  // node handles below belong to it
+    CK(cudaGraphInstantiate(&h->timed_exec, graph, 0));
+    // map each capture event to its record node in the instantiated graph
+    h->timed_nodes.assign(NE, nullptr);
+    for (cudaGraphNode_t nd : nodes) {
+      cudaGraphNodeType t;
+      CK(cudaGraphNodeGetType(nd, &t));
+      if (t != cudaGraphNodeTypeEventRecord) continue;
+      cudaEvent_t ev;
+      CK(cudaGraphEventRecordNodeGetEvent(nd, &ev));
+      for (int i = 0; i < NE; i++)
+        if (h->timed_cap_events[i] == ev) h->timed_nodes[i] = nd;
+    }
+    h->timed_dt = dt_atu;
+  }
+  std::vector<cudaEvent_t> evs((size_t)n * NE);
+  for (auto &e : evs) CK(cudaEventCreate(&e));
+  CK(cudaStreamSynchronize(h->stream));
+  for (int s = 0; s < n; s++) {
+    for (int i = 0; i < NE; i++)
+      if (h->timed_nodes[i])
+        CK(cudaGraphExecEventRecordNodeSetEvent(h->timed_exec, h->timed_nodes[i],
+                                                evs[(size_t)s * NE + i]));
+    CK(cudaGraphLaunch(h->timed_exec, h->stream));
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  std::vector<double> ksum(KG_COUNT, 0.0);
+  for (int s = 0; s < n; s++) {
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, evs[(size_t)s * NE], evs[(size_t)s * NE + KG_COUNT]));
+    if (step_ms) step_ms[s] = ms;
+    for (int k = 0; k < KG_COUNT; k++) {
+      float km = 0.f;
+      CK(cudaEventElapsedTime(&km, evs[(size_t)s * NE + k], evs[(size_t)s * NE + k + 1]));
+      ksum[k] += km;
+    }
+  }
+  for (auto &e : evs) cudaEventDestroy(e);
+  if (kernel_ms)
+    for (int k = 0; k < KG_COUNT && k < max_kernels; k++) kernel_ms[k] = (float)(ksum[k] / n);
+  int rc = check_status(h);
+  if (rc) return rc;
+  return KG_COUNT;
+}
+
+// ---------------------------------------------------------------- drop-in
+
+int comdgb_attach(simflat_t *s, const comdgb_opts *o) {
+  if (!s || !o) return set_err(COMDGB_ERR_ARG, "null argument");
+  if (find_attached(s)) return set_err(COMDGB_ERR_ARG, "simflat_t already attached");
+  comdgb_sim *h = nullptr;
+  int rc = create(s, o, &h);
+  if (rc) return rc;
+  h->host = s;
+  pin_host(h, s);
+  std::lock_guard<std::mutex> lk(g_reg_mu);
+  g_attached.push_back(h);
+  return 0;
+}
+
+int comdgb_detach(simflat_t *s) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  {
+    std::lock_guard<std::mutex> lk(g_reg_mu);
+    for (size_t i = 0; i < g_attached.size(); i++)
+      if (g_attached[i] == h) {
+        g_attached.erase(g_attached.begin() + i);
+        break;
+      }
+  }
+  cudaSetDevice(h->device);
+  unpin_host(h, s);
+  comdgb_sim_destroy(h);
+  return 0;
+}
+
+int comdgb_force(void *sv) {
+  simflat_t *s = (simflat_t *)sv;
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  CK(cudaSetDevice(h->device));
+  int rc = upload(h, s);
+  if (!rc) rc = do_force(h);
+  if (!rc) rc = download_forces(h, s);
+  return rc;
+}
+
+double comdgb_nTimeSteps(int n, simflat_t *s, double dt) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) {
+    set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+    return NAN;
+  }
+  if (cudaSetDevice(h->device) != cudaSuccess) return NAN;
+  int rc = upload(h, s);
+  if (!rc) rc = do_steps(h, n, dt);
+  if (!rc) rc = download(h, s);
+  return rc ? NAN : s->e;
+}
+
+int comdgb_reBoxAll(simflat_t *s) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  CK(cudaSetDevice(h->device));
+  int rc = upload(h, s);
+  if (!rc) {
+    enqueue_rebox(h);
+    rc = check_status(h);
+  }
+  if (!rc) rc = download(h, s);
+  return rc;
+}
+
+int comdgb_rebox_host(simflat_t *s, int periodic, int device) {
+  comdgb_opts o;
+  comdgb_default_opts(&o);
+  o.potential = -1;
+  o.periodic = periodic;
+  o.device = device;
+  comdgb_sim *h = nullptr;
+  int rc = create(s, &o, &h);
+  if (rc) return rc;
+  enqueue_rebox(h);
+  rc = check_status(h);
+  if (!rc) rc = download(h, s);
+  comdgb_sim_destroy(h);
+  return rc;
+}
+
+int comdgb_put_atoms(simflat_t *s, int n, const double *xyz, const double *pxyz,
+                     const int *ids, const int *itypes, const double *masses, int device) {
+  if (!s || n < 0 || (n > 0 && (!xyz || !pxyz || !ids || !itypes || !masses)))
+    return set_err(COMDGB_ERR_ARG, "bad argument");
+  comdgb_opts o;
+  comdgb_default_opts(&o);
+  o.potential = -1;
+  o.device = device;
+  comdgb_sim *h = nullptr;
+  int saved = s->ntot;
+  s->ntot = 0;
+  int rc = create(s, &o, &h);
+  s->ntot = saved;
+  if (rc) return rc;
+  int err = 0;
+  double *dxyz = dalloc<double>((size_t)n * 3, &err), *dp = dalloc<double>((size_t)n * 3, &err);
+  double *dm = dalloc<double>(n, &err);
+  int *did = dalloc<int>(n, &err), *dty = dalloc<int>(n, &err);
+  int *tmp = dalloc<int>((size_t)h->nslots, &err);
+  if (err) rc = set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed");
+  cudaStream_t st = h->stream;
+  if (!rc && n > 0) {
+    cudaMemcpyAsync(dxyz, xyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dp, pxyz, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dm, masses, sizeof(double) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(did, ids, sizeof(int) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(dty, itypes, sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  }
+  if (!rc) {
+    launch_bin_atoms(h->g, h->dcenter, h->s, n, dxyz, dp, did, dty, dm, tmp, h->status, st);
+    rc = check_status(h);
+  }
+  if (!rc) {
+    h->ntot = n;
+    rc = download(h, s);
+    s->ntot = n;
+  }
+  cudaFree(dxyz);
+  cudaFree(dp);
+  cudaFree(dm);
+  cudaFree(did);
+  cudaFree(dty);
+  cudaFree(tmp);
+  comdgb_sim_destroy(h);
+  return rc;
+}
+
+eam_cheby_t *comdgb_cheb_make(const eampotential_t *p, int n, int device) {
+  if (!p || n != CG_NCHEB) {
+    set_err(COMDGB_ERR_UNSUPPORTED, "only %d Chebyshev terms are supported", CG_NCHEB);
+    return nullptr;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+  comdgb_sim tmp;
+  cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
+  double coef[6][CG_NCHEB], a[6], b[6];
+  int rc = fit_cheb_gpu(&tmp, p, coef, a, b);
+  cudaStreamDestroy(tmp.stream);
+  tmp.stream = nullptr;
+  if (rc) return nullptr;
+  eam_cheby_t *c = (eam_cheby_t *)calloc(1, sizeof(eam_cheby_t));
+  c->cutoff = p->cutoff;
+  c->mass = p->mass;
+  c->lat = p->lat;
+  potentialarray_t **ser[6] = {&c->phi, &c->rho, &c->f, &c->dphi, &c->drho, &c->df};
+  for (int q = 0; q < 6; q++) {
+    potentialarray_t *pa = (potentialarray_t *)calloc(1, sizeof(potentialarray_t));
+    pa->n = n;
+    pa->x0 = a[q];
+    pa->xn = b[q];
+    pa->invDx = q >= 3 ? 1.0 : 0.0;
+    pa->values = (double *)malloc(sizeof(double) * n);
+    for (int j = 0; j < n; j++) pa->values[j] = coef[q][j];
+    *ser[q] = pa;
+  }
+  return c;
+}
+
+void comdgb_cheb_free(eam_cheby_t *c) {
+  if (!c) return;
+  potentialarray_t *ser[6] = {c->phi, c->rho, c->f, c->dphi, c->drho, c->df};
+  for (potentialarray_t *pa : ser)
+    if (pa) {
+      free(pa->values);
+      free(pa);
+    }
+  free(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,173 @@
+// common.cuh -- device data layout and shared device helpers of libcomdgb.
+//
+// HBM layout (one GPU, structure of arrays over the reference's slots
+// slot = box*64 + k, src-flat/include/pmdTypes.h:100):
+//   r, p, f   double4 per slot (x, y, z, -) / (fx, fy, fz, e): one aligned
+//             32-byte access per atom for gathers and the Verlet kernel
+//   rho, fi, mass  double per slot;  id, itype  int per slot
+//   pos32     float4 per slot: FP32 copy of the box-relative position
+//             (mixed precision); fi32 float per slot: F'(rho) in FP32
+//   natoms    int per box
+// Per-box link-cell stencil ("entry table"), built once: for each box the
+// up to 27 neighbour box ids in getNeighborBoxes order (domains.c:391-430)
+// with multiplicity, and the minimum-image box offsets drbox
+// (eam.c:494-502) in FP64 and FP32.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define CG_MAXATOMS 64
+#define CG_NNBR 27
+#define CG_NCHEB 32
+
+namespace cg {
+
+// 32-byte aligned double4 (CUDA 13 deprecates the 16-byte aligned one)
+typedef double4_32a d4;
+
+struct Geom {
+  int nbx[3];
+  int nboxes;
+  int periodic;
+  double bounds[3];
+  double boxsize[3];
+};
+
+struct Slots {
+  int *natoms;
+  int *id;
+  int *itype;
+  double *mass;
+  d4 *r;
+  d4 *p;
+  d4 *f;
+  double *rho;
+  double *fi;
+  float4 *pos32;
+  float *fi32;
+};
+
+struct EntryTab {
+  int *n;          // [nboxes] number of valid entries
+  int *box;        // [nboxes*27] neighbour box id
+  d4 *dr64;     // [nboxes*27] drbox (x, y, z, 0)
+  float4 *dr32;    // [nboxes*27] drbox rounded to FP32
+};
+
+// device status words
+enum {
+  ST_ERROR = 0,       // first error code (COMDGB_ERR_*), 0 if none
+  ST_REBIN_SERIAL = 1,// set when the parallel rebin cannot reproduce reBoxAll
+  ST_NBR_OVERFLOW = 2,// atoms whose neighbour list overflowed (handled)
+  ST_SERIAL_RUNS = 3, // number of serial rebin fallbacks taken
+  ST_COUNT = 8
+};
+
+// tabulated function (potentialarray_t): v points at element 0, guards at
+// v[-1], v[n], v[n+1]
+template <class T>
+struct Table {
+  const T *v;
+  T x0, xn, invDx;
+  int n;
+};
+
+// Chebyshev series of the reference: 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF
+template <class T>
+struct Cheb {
+  T c[6][CG_NCHEB];
+  T a[6], b[6];
+  T ys[6], yo[6];  // y = x*ys + yo (FP32 path)
+};
+
+__host__ __device__ inline void box_ixyz(const Geom &g, int b, int *ix) {
+  ix[0] = b % g.nbx[0];
+  ix[1] = (b / g.nbx[0]) % g.nbx[1];
+  ix[2] = (b / g.nbx[0] / g.nbx[1]) % g.nbx[2];
+}
+
+// getIBoxFromIxyz3NP (domains.c:297-325): -1 outside a non-periodic grid,
+// else wrap by one period
+__host__ __device__ inline int box_from_ixyz(const Geom &g, int *ix) {
+  if (!g.periodic)
+    for (int j = 0; j < 3; j++)
+      if (ix[j] < 0 || ix[j] >= g.nbx[j]) return -1;
+  for (int j = 0; j < 3; j++) {
+    if (ix[j] < 0) ix[j] += g.nbx[j];
+    else if (ix[j] >= g.nbx[j]) ix[j] -= g.nbx[j];
+  }
+  return ix[0] + ix[1] * g.nbx[0] + ix[2] * g.nbx[0] * g.nbx[1];
+}
+
+// Kahan-compensated FP32 accumulator
+struct KSum {
+  float s, c;
+  __device__ __forceinline__ void zero() { s = 0.f; c = 0.f; }
+  __device__ __forceinline__ void add(float x) {
+    float y = __fsub_rn(x, c);
+    float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+struct DSum {
+  double s;
+  __device__ __forceinline__ void zero() { s = 0.0; }
+  __device__ __forceinline__ void add(double x) { s = __dadd_rn(s, x); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+
+// eamInterpolateDeriv (eam.c:401-434), same operation order
+template <class T>
+__device__ __forceinline__ void table_eval(const Table<T> &a, T r, T &value, T &deriv) {
+  if (r < a.x0) r = a.x0;
+  else if (r > a.xn) r = a.xn;
+  r = (r - a.x0) * a.invDx;
+  T fl = floor(r);
+  int i1 = (int)fl;
+  r = r - fl;
+  // a NaN argument must not index outside the table (valid r gives 0..n-1)
+  i1 = i1 < 0 ? 0 : (i1 > a.n - 1 ? a.n - 1 : i1);
+  const T *v = a.v;
+  T vm = __ldg(v + i1 - 1), v0 = __ldg(v + i1), v1 = __ldg(v + i1 + 1), v2 = __ldg(v + i1 + 2);
+  T gi = v1 - vm;
+  T gi1 = v2 - v0;
+  value = v0 + T(0.5) * r * (r * (v1 + vm - T(2.0) * v0) + gi);
+  deriv = (i1 <= 0) ? T(0) : T(0.5) * (gi + r * (gi1 - gi)) * a.invDx;
+}
+
+// eamCheb (cheby.c:276-310) in FP64: Clenshaw, lower clamp only
+__device__ __forceinline__ double cheb_eval64(const double *c, double a, double b, double x) {
+  if (x < a) x = a;
+  double d = 0.0, dd = 0.0, sv;
+  double y = __ddiv_rn(__dsub_rn(__dsub_rn(__dmul_rn(2.0, x), a), b), __dsub_rn(b, a));
+  double y2 = __dmul_rn(2.0, y);
+#pragma unroll
+  for (int j = CG_NCHEB - 1; j > 0; j--) {
+    sv = d;
+    d = __dadd_rn(__dsub_rn(__dmul_rn(y2, d), dd), c[j]);
+    dd = sv;
+  }
+  return __dadd_rn(__dsub_rn(__dmul_rn(y, d), dd), __dmul_rn(0.5, c[0]));
+}
+
+// the same series in FP32 with y from a fused multiply-add
+__device__ __forceinline__ float cheb_eval32(const float *c, float a, float ys, float yo,
+                                             float x) {
+  if (x < a) x = a;
+  float y = fmaf(x, ys, yo);
+  float y2 = 2.0f * y;
+  float d = 0.f, dd = 0.f;
+#pragma unroll
+  for (int j = CG_NCHEB - 1; j > 0; j--) {
+    float sv = d;
+    d = fmaf(y2, d, c[j] - dd);
+    dd = sv;
+  }
+  return fmaf(y, d, 0.5f * c[0] - dd);
+}
+
+}  // namespace cg

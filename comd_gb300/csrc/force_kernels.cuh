@@ -1,0 +1,392 @@
+// force_kernels.cuh -- link-cell force kernels, templated on the pair
+// arithmetic type T (double: the plain FP64 kernels; float: mixed precision).
+//
+// Work decomposition (full pairs: every atom sums over all its neighbours,
+// so per-atom sums need no atomics and are deterministic):
+//   nbr_build   one CTA per box.  The box's stencil entries (27 neighbour
+//               boxes with the reference's multiplicity) are staged from HBM
+//               into shared memory; each warp takes one atom of the box and
+//               tests 32 candidates per iteration, compacting hits with a
+//               ballot into the atom's neighbour list (uint16 codes: entry
+//               index << 6 | slot).  Cutoff test as pass 1 of eamForce:
+//               r2 <= rc2 (eam.c:521, ljForce.c:193).
+//   eam_pass1   one thread per atom over its list: pair phi, phi', rho
+//               (eam.c:484-549), then F(rho) and F'(rho) fused in
+//               (eam.c:576-594).
+//   eam_pass2   one thread per atom: (F'_i + F'_j) rho'(r) dr/r and the
+//               x-x stress (eam.c:595-653), r2 < rc2.
+//   lj_pass     one thread per atom: the 12-6 terms of ljForce.c:151-215.
+// Atoms whose neighbour count exceeds the list capacity fall back to a
+// direct scan of their stencil, so results never depend on the capacity.
+#pragma once
+
+#include "common.cuh"
+
+namespace cg {
+
+enum { EVAL_TABLE = 0, EVAL_CHEBY = 1 };
+
+struct ForceArgs {
+  Geom g;
+  Slots s;
+  EntryTab et;
+  const int *atom_slot;  // [ntot] slot of the a-th atom (box order)
+  const int *box_start;  // [nboxes+1] first atom index of each box
+  int ntot;
+  uint16_t *nbr;         // [ntot*cap]
+  int *nbr_n;            // [ntot] true neighbour count
+  int cap;
+  double *atom_stress;   // [ntot] per-atom share of the scalar stress
+  int *status;
+};
+
+template <class T>
+struct PrecT;
+
+template <>
+struct PrecT<double> {
+  typedef DSum Acc;
+  static __device__ __forceinline__ void pos(const Slots &s, int slot, double &x, double &y,
+                                             double &z) {
+    d4 v = s.r[slot];
+    x = v.x; y = v.y; z = v.z;
+  }
+  static __device__ __forceinline__ void drbox(const EntryTab &et, int idx, double &x,
+                                               double &y, double &z) {
+    d4 v = et.dr64[idx];
+    x = v.x; y = v.y; z = v.z;
+  }
+  static __device__ __forceinline__ double fi(const Slots &s, int slot) { return s.fi[slot]; }
+};
+
+template <>
+struct PrecT<float> {
+  typedef KSum Acc;
+  static __device__ __forceinline__ void pos(const Slots &s, int slot, float &x, float &y,
+                                             float &z) {
+    float4 v = __ldg(s.pos32 + slot);
+    x = v.x; y = v.y; z = v.z;
+  }
+  static __device__ __forceinline__ void drbox(const EntryTab &et, int idx, float &x, float &y,
+                                               float &z) {
+    float4 v = __ldg(et.dr32 + idx);
+    x = v.x; y = v.y; z = v.z;
+  }
+  static __device__ __forceinline__ float fi(const Slots &s, int slot) {
+    return __ldg(s.fi32 + slot);
+  }
+};
+
+// dr = drbox + r_i - r_j and r2 accumulated in the reference's order
+template <class T>
+__device__ __forceinline__ T pair_r2(T bx, T by, T bz, T xi, T yi, T zi, T xj, T yj, T zj,
+                                     T &dx, T &dy, T &dz) {
+  dx = (bx + xi) - xj;
+  dy = (by + yi) - yj;
+  dz = (bz + zi) - zj;
+  T r2 = dx * dx;
+  r2 = r2 + dy * dy;
+  r2 = r2 + dz * dz;
+  return r2;
+}
+
+// Visit every stencil candidate of atom (b, i) directly (overflow path).
+// fn(j_slot, dx, dy, dz, r2) is called for candidates with r2 <= rc2.
+template <class T, class F>
+__device__ void scan_stencil(const ForceArgs &A, int b, int i, T xi, T yi, T zi, T rc2, F &&fn) {
+  int ne = A.et.n[b];
+  for (int e = 0; e < ne; e++) {
+    int jb = A.et.box[b * CG_NNBR + e];
+    T bx, by, bz;
+    PrecT<T>::drbox(A.et, b * CG_NNBR + e, bx, by, bz);
+    int nj = A.s.natoms[jb];
+    for (int k = 0; k < nj; k++) {
+      if (jb == b && k == i) continue;
+      int js = jb * CG_MAXATOMS + k;
+      T xj, yj, zj, dx, dy, dz;
+      PrecT<T>::pos(A.s, js, xj, yj, zj);
+      T r2 = pair_r2(bx, by, bz, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+      if (r2 > rc2) continue;
+      fn(js, dx, dy, dz, r2);
+    }
+  }
+}
+
+// Visit the atom's neighbour list (or its stencil when the list overflowed).
+template <class T, class F>
+__device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int b, int i, T xi,
+                                                  T yi, T zi, T rc2, F &&fn) {
+  int n = A.nbr_n[a];
+  if (n > A.cap) {
+    scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
+    return;
+  }
+  const uint16_t *lst = A.nbr + (size_t)a * A.cap;
+  const int ebase = b * CG_NNBR;
+  for (int t0 = 0; t0 < n; t0 += 8) {
+    uint4 pk = *reinterpret_cast<const uint4 *>(lst + t0);
+    uint32_t w[4] = {pk.x, pk.y, pk.z, pk.w};
+#pragma unroll
+    for (int u = 0; u < 8; u++) {
+      if (t0 + u < n) {
+        uint32_t code = (w[u >> 1] >> ((u & 1) * 16)) & 0xffffu;
+        int e = code >> 6, k = code & 63;
+        int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
+        T bx, by, bz, xj, yj, zj, dx, dy, dz;
+        PrecT<T>::drbox(A.et, ebase + e, bx, by, bz);
+        PrecT<T>::pos(A.s, js, xj, yj, zj);
+        T r2 = pair_r2(bx, by, bz, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+        fn(js, dx, dy, dz, r2);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// neighbour-list build: one CTA per box, one warp per atom of the box
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(128) nbr_build_kernel(ForceArgs A, T rc2) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int b = blockIdx.x;
+  const int ni = A.s.natoms[b];
+  if (ni == 0) return;
+  const int maxc = CG_NNBR * CG_MAXATOMS;
+  T *cx = reinterpret_cast<T *>(smem_raw);
+  T *cy = cx + maxc;
+  T *cz = cy + maxc;
+  uint16_t *cc = reinterpret_cast<uint16_t *>(cz + maxc);
+  __shared__ int s_box[CG_NNBR];
+  __shared__ int s_off[CG_NNBR + 1];
+  __shared__ T s_dr[CG_NNBR][3];
+
+  const int ne = A.et.n[b];
+  if (threadIdx.x < ne) {
+    int e = threadIdx.x;
+    s_box[e] = A.et.box[b * CG_NNBR + e];
+    T bx, by, bz;
+    PrecT<T>::drbox(A.et, b * CG_NNBR + e, bx, by, bz);
+    s_dr[e][0] = bx; s_dr[e][1] = by; s_dr[e][2] = bz;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int off = 0;
+    for (int e = 0; e < ne; e++) {
+      s_off[e] = off;
+      off += A.s.natoms[s_box[e]];
+    }
+    s_off[ne] = off;
+  }
+  __syncthreads();
+  const int ncand = s_off[ne];
+  // stage candidates: entry-major, slot-minor
+  for (int e = 0; e < ne; e++) {
+    int jb = s_box[e], base = s_off[e], nj = s_off[e + 1] - base;
+    for (int k = threadIdx.x; k < nj; k += blockDim.x) {
+      T x, y, z;
+      PrecT<T>::pos(A.s, jb * CG_MAXATOMS + k, x, y, z);
+      cx[base + k] = x; cy[base + k] = y; cz[base + k] = z;
+      cc[base + k] = (uint16_t)((e << 6) | k);
+    }
+  }
+  __syncthreads();
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int i = warp; i < ni; i += nw) {
+    T xi, yi, zi;
+    PrecT<T>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
+    const int a = A.box_start[b] + i;
+    if (a >= A.ntot) break;  // only after a reported overflow
+    uint16_t *out = A.nbr + (size_t)a * A.cap;
+    int cnt = 0;
+    for (int c0 = 0; c0 < ncand; c0 += 32) {
+      int c = c0 + lane;
+      bool hit = false;
+      uint16_t code = 0;
+      if (c < ncand) {
+        code = cc[c];
+        int e = code >> 6, k = code & 63;
+        T dx, dy, dz;
+        T r2 = pair_r2(s_dr[e][0], s_dr[e][1], s_dr[e][2], xi, yi, zi, cx[c], cy[c], cz[c], dx,
+                       dy, dz);
+        hit = (r2 <= rc2) && !(s_box[e] == b && k == i);
+      }
+      unsigned m = __ballot_sync(0xffffffffu, hit);
+      int pos = cnt + __popc(m & lt);
+      if (hit && pos < A.cap) out[pos] = code;
+      cnt += __popc(m);
+    }
+    if (lane == 0) {
+      A.nbr_n[a] = cnt;
+      if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// EAM pass 1 (+ embedding): phi, phi', rho per pair; F, F' per atom
+// ---------------------------------------------------------------------------
+template <class T, int EVAL>
+struct EamPot {
+  Table<T> phi, rho, f;
+  Cheb<T> ch;
+  T rc2;
+};
+
+__device__ __forceinline__ double cheb_series(const Cheb<double> &c, int s, double x) {
+  return cheb_eval64(c.c[s], c.a[s], c.b[s], x);
+}
+__device__ __forceinline__ float cheb_series(const Cheb<float> &c, int s, float x) {
+  return cheb_eval32(c.c[s], c.a[s], c.ys[s], c.yo[s], x);
+}
+
+template <class T, int EVAL>
+__device__ __forceinline__ void eam_pair_terms(const EamPot<T, EVAL> &P, T r, T &phi, T &dphi,
+                                               T &rho) {
+  if (EVAL == EVAL_CHEBY) {
+    phi = cheb_series(P.ch, 0, r);
+    dphi = cheb_series(P.ch, 3, r);
+    rho = cheb_series(P.ch, 1, r);
+  } else {
+    T drho;
+    table_eval(P.phi, r, phi, dphi);
+    table_eval(P.rho, r, rho, drho);
+  }
+}
+
+template <class T, int EVAL>
+__device__ __forceinline__ void eam_embed(const EamPot<T, EVAL> &P, T rho, T &F, T &dF) {
+  if (EVAL == EVAL_CHEBY) {
+    F = cheb_series(P.ch, 2, rho);
+    dF = cheb_series(P.ch, 5, rho);
+  } else {
+    table_eval(P.f, rho, F, dF);
+  }
+}
+
+template <class T, int EVAL>
+__device__ __forceinline__ T eam_drho(const EamPot<T, EVAL> &P, T r) {
+  if (EVAL == EVAL_CHEBY) return cheb_series(P.ch, 4, r);
+  T v, d;
+  table_eval(P.rho, r, v, d);
+  return d;
+}
+
+template <class T, int EVAL>
+__global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, EVAL> P) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= A.ntot) return;
+  const int slot = A.atom_slot[a];
+  const int b = slot >> 6, i = slot & 63;
+  T xi, yi, zi;
+  PrecT<T>::pos(A.s, slot, xi, yi, zi);
+  typename PrecT<T>::Acc fx, fy, fz, ep, rh;
+  fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
+  auto fn = [&](int js, T dx, T dy, T dz, T r2) {
+    T r = sqrt(r2);
+    T phi, dphi, rho;
+    eam_pair_terms<T, EVAL>(P, r, phi, dphi, rho);
+    T w = dphi / r;
+    fx.add(w * dx);
+    fy.add(w * dy);
+    fz.add(w * dz);
+    ep.add(phi / T(2.0));
+    rh.add(rho);
+  };
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, P.rc2, fn);
+  double rho_i = rh.value();
+  T F, dF;
+  eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
+  d4 fo;
+  fo.x = fx.value();
+  fo.y = fy.value();
+  fo.z = fz.value();
+  fo.w = ep.value() + (double)F;
+  A.s.f[slot] = fo;
+  A.s.rho[slot] = rho_i;
+  A.s.fi[slot] = (double)dF;
+  if (sizeof(T) == 4) A.s.fi32[slot] = (float)dF;
+}
+
+// ---------------------------------------------------------------------------
+// EAM pass 2: embedding force and stress
+// ---------------------------------------------------------------------------
+template <class T, int EVAL>
+__global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, EVAL> P) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= A.ntot) return;
+  const int slot = A.atom_slot[a];
+  const int b = slot >> 6, i = slot & 63;
+  T xi, yi, zi;
+  PrecT<T>::pos(A.s, slot, xi, yi, zi);
+  const T fii = PrecT<T>::fi(A.s, slot);
+  typename PrecT<T>::Acc fx, fy, fz, sx;
+  fx.zero(); fy.zero(); fz.zero(); sx.zero();
+  const T rc2 = P.rc2;
+  auto fn = [&](int js, T dx, T dy, T dz, T r2) {
+    if (r2 >= rc2) return;
+    T r = sqrt(r2);
+    T drho = eam_drho<T, EVAL>(P, r);
+    T w = (fii + PrecT<T>::fi(A.s, js)) * drho;
+    T wr = w / r;
+    fx.add(wr * dx);
+    fy.add(wr * dy);
+    fz.add(wr * dz);
+    sx.add(wr * dx * dx);
+  };
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+  d4 fo = A.s.f[slot];
+  fo.x += fx.value();
+  fo.y += fy.value();
+  fo.z += fz.value();
+  A.s.f[slot] = fo;
+  A.atom_stress[a] = sx.value();
+}
+
+// ---------------------------------------------------------------------------
+// LJ: ljForce.c:151-215 as full pairs; the kinetic stress term is added once
+// per (atom, non-empty neighbour box) as at ljForce.c:175
+// ---------------------------------------------------------------------------
+template <class T>
+struct LjPot {
+  T s6, s6x12, eps4s6, rc2;  // sigma^6, 12*sigma^6, 4*eps*sigma^6, rc^2
+};
+
+template <class T>
+__global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= A.ntot) return;
+  const int slot = A.atom_slot[a];
+  const int b = slot >> 6, i = slot & 63;
+  T xi, yi, zi;
+  PrecT<T>::pos(A.s, slot, xi, yi, zi);
+  typename PrecT<T>::Acc fx, fy, fz, ep, sx;
+  fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
+  const T s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6;
+  auto fn = [&](int js, T dx, T dy, T dz, T r2) {
+    T ir2 = T(1.0) / r2;
+    T r6 = ir2 * ir2 * ir2;
+    ep.add(T(0.5) * r6 * (s6 * r6 - T(1.0)));
+    T fr = c4 * r6 * ir2 * (s12 * r6 - T(6.0));
+    fx.add(dx * fr);
+    fy.add(dy * fr);
+    fz.add(dz * fr);
+    sx.add(fr * dx * dx);
+  };
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, P.rc2, fn);
+  // kinetic term: -p_x^2/m per non-empty stencil entry
+  int ne = A.et.n[b], nonempty = 0;
+  for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
+  d4 p = A.s.p[slot];
+  double kin = __ddiv_rn(__dmul_rn(p.x, p.x), A.s.mass[slot]);
+  d4 fo;
+  fo.x = fx.value();
+  fo.y = fy.value();
+  fo.z = fz.value();
+  fo.w = ep.value();
+  A.s.f[slot] = fo;
+  A.atom_stress[a] = sx.value() - (double)nonempty * kin;
+}
+
+}  // namespace cg

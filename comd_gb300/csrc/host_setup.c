@@ -1,0 +1,236 @@
+/*
+ * host_setup.c -- host-side setup routines of libcomdgb (plain C): reading
+ * the EAM tables, the FCC lattice generator, seeded perturbation and the
+ * host simflat_t allocation.  They build the same structures as the
+ * reference's setup code so a caller without the reference can drive the
+ * GPU path; none of them is on the timed path.
+ */
+#define _POSIX_C_SOURCE 200112L
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "comdgb.h"
+#include "comdgb_seed.h"
+
+static void *zalloc(size_t n) {
+  void *p = NULL;
+  size_t padded = (n + 127) & ~(size_t)127;
+  if (padded == 0) padded = 128;
+  if (posix_memalign(&p, 128, padded)) return NULL;
+  memset(p, 0, padded);
+  return p;
+}
+
+static int read_be_or_le(FILE *fp, void *dst, int size, int swap) {
+  unsigned char b[8];
+  if (fread(b, (size_t)size, 1, fp) != 1) return 0;
+  unsigned char *d = (unsigned char *)dst;
+  for (int i = 0; i < size; i++) d[i] = swap ? b[size - 1 - i] : b[i];
+  return 1;
+}
+
+/* Fortran-record table file: [36][n x0 xn invDx iflo ifhi][36][8n][values][8n]
+ * (getPotentialArrayFromBinaryFile, eam.c:156-249).  Byte order is detected
+ * from the first record length.  Guard cells: values[-1] = iflo ? v[0] : 0,
+ * values[n] = values[n+1] = ifhi ? v[n-1] : 0; x0 is moved up one interval
+ * (allocPotentialArray, eam.c:130-153). */
+static potentialarray_t *read_table(const char *path) {
+  FILE *fp = fopen(path, "rb");
+  if (!fp) return NULL;
+  unsigned char head[4];
+  if (fread(head, 4, 1, fp) != 1) { fclose(fp); return NULL; }
+  int le = head[0] | (head[1] << 8) | (head[2] << 16) | (head[3] << 24);
+  int swap = le > 4096;
+  int n = 0, iflo = 0, ifhi = 0, rec = 0;
+  double x0 = 0, xn = 0, invdx = 0;
+  int ok = read_be_or_le(fp, &n, 4, swap) && read_be_or_le(fp, &x0, 8, swap) &&
+           read_be_or_le(fp, &xn, 8, swap) && read_be_or_le(fp, &invdx, 8, swap) &&
+           read_be_or_le(fp, &iflo, 4, swap) && read_be_or_le(fp, &ifhi, 4, swap) &&
+           read_be_or_le(fp, &rec, 4, swap) && read_be_or_le(fp, &rec, 4, swap);
+  if (!ok || n <= 0 || rec != n * 8) { fclose(fp); return NULL; }
+  potentialarray_t *a = (potentialarray_t *)zalloc(sizeof *a);
+  double *buf = (double *)zalloc((size_t)(n + 3) * sizeof(double));
+  if (!a || !buf) { free(a); free(buf); fclose(fp); return NULL; }
+  a->values = buf + 1;
+  for (int i = 0; i < n; i++)
+    if (!read_be_or_le(fp, a->values + i, 8, swap)) { free(buf); free(a); fclose(fp); return NULL; }
+  fclose(fp);
+  a->n = n;
+  a->invDx = invdx;
+  a->xn = xn;
+  a->x0 = x0 + (xn - x0) / (double)n;
+  a->values[-1] = iflo ? a->values[0] : 0.0;
+  a->values[n] = ifhi ? a->values[n - 1] : 0.0;
+  a->values[n + 1] = a->values[n];
+  return a;
+}
+
+static void free_table(potentialarray_t *a) {
+  if (!a) return;
+  free(a->values - 1);
+  free(a);
+}
+
+static double doc_line_value(const char *path, int line) {
+  FILE *fp = fopen(path, "r");
+  if (!fp) return -1.0;
+  char buf[4096];
+  double v = -1.0;
+  int l = 0;
+  while (l < line && fgets(buf, sizeof buf, fp)) l++;
+  if (l == line && sscanf(buf, "%lf", &v) != 1) v = -1.0;
+  fclose(fp);
+  return v;
+}
+
+eampotential_t *comdgb_eam_read(const char *dir, const char *name) {
+  char path[4096];
+  eampotential_t *p = (eampotential_t *)zalloc(sizeof *p);
+  if (!p) return NULL;
+  snprintf(path, sizeof path, "%s/%s.phi", dir, name);
+  p->phi = read_table(path);
+  snprintf(path, sizeof path, "%s/%s.rho", dir, name);
+  p->rho = read_table(path);
+  snprintf(path, sizeof path, "%s/%s.f", dir, name);
+  p->f = read_table(path);
+  snprintf(path, sizeof path, "%s/%s.doc", dir, name);
+  p->mass = doc_line_value(path, 2); /* mass in amu, second line */
+  p->lat = doc_line_value(path, 3);  /* lattice constant, third line */
+  if (!p->phi || !p->rho || !p->f || p->mass < 0.0) {
+    comdgb_eam_free(p);
+    return NULL;
+  }
+  p->cutoff = p->phi->xn; /* eam.c:392 */
+  return p;
+}
+
+void comdgb_eam_free(eampotential_t *p) {
+  if (!p) return;
+  free_table(p->phi);
+  free_table(p->rho);
+  free_table(p->f);
+  free(p);
+}
+
+ljpotential_t *comdgb_lj_make(double sigma, double epsilon, double cutoff, double mass) {
+  ljpotential_t *p = (ljpotential_t *)zalloc(sizeof *p);
+  if (!p) return NULL;
+  p->sigma = sigma;
+  p->epsilon = epsilon;
+  p->cutoff = cutoff;
+  p->mass = mass;
+  return p;
+}
+
+void comdgb_lj_free(ljpotential_t *p) { free(p); }
+
+void comdgb_sim_free_host(simflat_t *s) {
+  if (!s) return;
+  free(s->dcenter);
+  free(s->natoms);
+  free(s->id);
+  free(s->iType);
+  free(s->mass);
+  free(s->r);
+  free(s->p);
+  free(s->f);
+  free(s->rho);
+  free(s->fi);
+  free(s->comment);
+  free(s);
+}
+
+/* allocDomains (domains.c:155-200) */
+static int alloc_domains(simflat_t *s) {
+  double strain[3] = {s->defgrad == 0.0 ? 1.0 : s->defgrad, 1.0, 1.0};
+  double bf = s->bf == 0.0 ? 1.0 : s->bf;
+  s->nboxes = 1;
+  for (int j = 0; j < 3; j++) {
+    s->nbx[j] = (int)floor(s->bounds[j] / (s->pot->cutoff * bf * strain[j]));
+    if (s->nbx[j] < 1) return COMDGB_ERR_NOBOX;
+    s->nboxes *= s->nbx[j];
+    s->boxsize[j] = s->bounds[j] / (double)s->nbx[j];
+  }
+  size_t nb = (size_t)s->nboxes, ns = nb * COMDGB_MAXATOMS;
+  s->dcenter = (comdgb_real3 *)zalloc(nb * sizeof(comdgb_real3));
+  s->natoms = (int *)zalloc(nb * sizeof(int));
+  s->id = (int *)zalloc(ns * sizeof(int));
+  s->iType = (int *)zalloc(ns * sizeof(int));
+  s->mass = (double *)zalloc(ns * sizeof(double));
+  s->r = (comdgb_real3 *)zalloc(ns * sizeof(comdgb_real3));
+  s->p = (comdgb_real3 *)zalloc(ns * sizeof(comdgb_real3));
+  s->f = (comdgb_real4 *)zalloc(ns * sizeof(comdgb_real4));
+  s->rho = (double *)zalloc(ns * sizeof(double));
+  s->fi = (double *)zalloc(ns * sizeof(double));
+  if (!s->dcenter || !s->natoms || !s->id || !s->iType || !s->mass || !s->r || !s->p ||
+      !s->f || !s->rho || !s->fi)
+    return COMDGB_ERR_NOMEM;
+  s->stateflag = 1;
+  for (int b = 0; b < s->nboxes; b++) {
+    int ib[3] = {b % s->nbx[0], (b / s->nbx[0]) % s->nbx[1], b / s->nbx[0] / s->nbx[1]};
+    for (int j = 0; j < 3; j++) s->dcenter[b][j] = s->boxsize[j] * (double)ib[j];
+  }
+  return 0;
+}
+
+/* putAtomInBox (domains.c:237-291) for one atom at world position x */
+static int put_atom(simflat_t *s, int id, int itype, double mass, const double *x) {
+  double w[3];
+  int ib[3];
+  for (int m = 0; m < 3; m++) {
+    w[m] = x[m];
+    if (w[m] < 0.0) w[m] += s->bounds[m];
+    else if (w[m] >= s->bounds[m]) w[m] -= s->bounds[m];
+    ib[m] = (int)floor(w[m] / s->boxsize[m]);
+    if (ib[m] < 0 || ib[m] >= s->nbx[m]) return COMDGB_ERR_BOXRANGE;
+  }
+  int b = ib[0] + s->nbx[0] * ib[1] + s->nbx[0] * s->nbx[1] * ib[2];
+  if (s->natoms[b] >= COMDGB_MAXATOMS) return COMDGB_ERR_MAXATOMS;
+  int off = b * COMDGB_MAXATOMS + s->natoms[b]++;
+  s->ntot++;
+  s->id[off] = id;
+  s->iType[off] = itype;
+  s->mass[off] = mass;
+  for (int m = 0; m < 3; m++) s->r[off][m] = w[m] - s->dcenter[b][m];
+  return 0;
+}
+
+/* create_fcc_lattice (ic_fcc.c:63-141): walk the half-lattice points with
+ * running counters and keep those with odd index sum; ids in walk order */
+simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double bf,
+                      pmd_base_potential_t *pot, int *status) {
+  int st = 0;
+  simflat_t *s = (simflat_t *)zalloc(sizeof *s);
+  if (!s) { if (status) *status = COMDGB_ERR_NOMEM; return NULL; }
+  s->pot = pot;
+  s->comment = (char *)zalloc(1024);
+  s->defgrad = defgrad;
+  s->bf = bf;
+  s->bounds[0] = nx * lat * defgrad;
+  s->bounds[1] = ny * lat;
+  s->bounds[2] = nz * lat;
+  st = alloc_domains(s);
+  if (!st) {
+    double half = lat / 2.0, pt[3];
+    int ci = 0, cj = 0, ck = 0, nid = 0;
+    for (pt[2] = lat / 4.0; pt[2] < s->bounds[2] && !st; pt[2] += half, ck++)
+      for (pt[1] = lat / 4.0; pt[1] < s->bounds[1] && !st; pt[1] += half, cj++)
+        for (pt[0] = lat * defgrad / 4.0; pt[0] < s->bounds[0] && !st;
+             pt[0] += half * defgrad, ci++)
+          if ((ci + cj + ck) % 2) st = put_atom(s, nid++, 1, pot->mass, pt);
+  }
+  if (status) *status = st;
+  if (st) {
+    comdgb_sim_free_host(s);
+    return NULL;
+  }
+  return s;
+}
+
+void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,
+                 double mass_amu) {
+  comdgb_seed_apply(s, seed, disp_kind, amp, temp_k, mass_amu);
+}

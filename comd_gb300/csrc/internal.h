@@ -1,0 +1,65 @@
+// internal.h -- launchers shared between the kernel translation units and the
+// host API (api.cu).  All launches go to the caller's stream.
+#pragma once
+
+#include "common.cuh"
+#include "force_kernels.cuh"
+
+namespace cg {
+
+// rebin scratch (one set per simulation)
+struct RebinWork {
+  int *dest;            // [nslots] destination box of a departing atom
+  uint32_t *depmask;    // [2*nboxes] departure bits of slots 0-31 / 32-63
+  int *n_lo;            // [nboxes] arrivals from lower-index boxes
+  int *n_dep;           // [nboxes]
+  int *final_len;       // [nboxes] occupancy after the box's own scan
+  uint8_t *final_src;   // [nboxes*64] slot t <- old slot (<64) or placeholder 64+p
+  uint8_t *dep_order;   // [nboxes*64] departure order (old slots)
+  Slots stage;          // full records of departing atoms, indexed by old slot
+};
+
+// ---- md_kernels.cu ----
+void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, cudaStream_t st);
+// r += dt*p/rmass (and optionally the classify step of reBoxAll)
+void launch_advance_positions(const Geom &g, Slots s, double dt, double rmass, bool mixed,
+                              bool classify, const RebinWork &w, int *status, cudaStream_t st);
+// p -= dt_v*f; r += dt_r*p/rmass; classify
+void launch_advance_vp(const Geom &g, Slots s, double dt_v, double dt_r, double rmass,
+                       bool mixed, const RebinWork &w, int *status, cudaStream_t st);
+// classify only (reBoxAll without a position update)
+void launch_classify(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
+                     cudaStream_t st);
+// plan + apply + serial fallback; must follow a classify launch
+void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
+                         cudaStream_t st);
+void launch_compact(const Geom &g, const int *natoms, int *box_start, int *atom_slot, int ntot,
+                    int *partials, int npart, cudaStream_t st);
+int compact_partials(int nboxes);
+void launch_reduce(const ForceArgs &A, double *partials, long long *ipartials, int npart,
+                   double *out, long long *iout, cudaStream_t st);
+int reduce_partials(int ntot);
+void launch_kinetic(const Geom &g, Slots s, const int *atom_slot, int ntot, double rmass,
+                    double *partials, int npart, double *out, cudaStream_t st);
+void launch_unpack3(const double *src3, d4 *dst, long n, cudaStream_t st);
+void launch_pack3(const d4 *src, double *dst3, long n, cudaStream_t st);
+void launch_pos32(const Geom &g, Slots s, cudaStream_t st);
+void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, const double *xyz,
+                      const double *pxyz, const int *ids, const int *types, const double *masses,
+                      int *tmp_index, int *status, cudaStream_t st);
+void launch_cheb_fit(const double *table_v, double x0, double xn, double invdx, int n_terms,
+                     double *coef, double *dcoef, cudaStream_t st);
+
+// ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----
+template <class T>
+cudaError_t prepare_nbr_build();
+template <class T>
+void launch_nbr_build(const ForceArgs &A, T rc2, cudaStream_t st);
+template <class T, int EVAL>
+void launch_eam_pass1(const ForceArgs &A, const EamPot<T, EVAL> &P, cudaStream_t st);
+template <class T, int EVAL>
+void launch_eam_pass2(const ForceArgs &A, const EamPot<T, EVAL> &P, cudaStream_t st);
+template <class T>
+void launch_lj(const ForceArgs &A, const LjPot<T> &P, cudaStream_t st);
+
+}  // namespace cg

@@ -1,0 +1,787 @@
+// md_kernels.cu -- integration, link-cell rebinning, initial binning, stencil
+// table, atom compaction, reductions and the Chebyshev fit.
+//
+// Built with -fmad=false: the FP64 integrator must reproduce the
+// reference's separately rounded multiply and add (timestep.c:71,104) so
+// that, given the same forces, positions and momenta are bit-identical and
+// the rebinning decisions agree with reBoxAll.
+#include <cstdio>
+
+#include "internal.h"
+
+namespace cg {
+
+// ---------------------------------------------------------------------------
+// stencil table: getNeighborBoxes (domains.c:391-430) + min-image drbox
+// (eam.c:494-502), one thread per box
+// ---------------------------------------------------------------------------
+__global__ void entry_table_kernel(Geom g, const double *dcenter, EntryTab et) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nboxes) return;
+  int base = b * CG_NNBR;
+  int cnt = 0;
+  if (g.nboxes == 1) {
+    et.box[base] = 0;
+    et.dr64[base] = d4{0.0, 0.0, 0.0, 0.0};
+    et.dr32[base] = make_float4(0.f, 0.f, 0.f, 0.f);
+    et.n[b] = 1;
+    return;
+  }
+  int ix[3];
+  box_ixyz(g, b, ix);
+  for (int i = ix[0] - 1; i <= ix[0] + 1; i++)
+    for (int j = ix[1] - 1; j <= ix[1] + 1; j++)
+      for (int k = ix[2] - 1; k <= ix[2] + 1; k++) {
+        int t[3] = {i, j, k};
+        int nb = box_from_ixyz(g, t);
+        if (nb < 0) continue;
+        double dr[3];
+        for (int d = 0; d < 3; d++) {
+          dr[d] = dcenter[3 * b + d] - dcenter[3 * nb + d];
+          if (g.periodic) {
+            if (dr[d] < -0.5 * g.bounds[d]) dr[d] += g.bounds[d];
+            else if (dr[d] > 0.5 * g.bounds[d]) dr[d] -= g.bounds[d];
+          }
+        }
+        et.box[base + cnt] = nb;
+        et.dr64[base + cnt] = d4{dr[0], dr[1], dr[2], 0.0};
+        et.dr32[base + cnt] = make_float4((float)dr[0], (float)dr[1], (float)dr[2], 0.f);
+        cnt++;
+      }
+  for (int e = cnt; e < CG_NNBR; e++) et.box[base + e] = -1;
+  et.n[b] = cnt;
+}
+
+void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, cudaStream_t st) {
+  entry_table_kernel<<<(g.nboxes + 127) / 128, 128, 0, st>>>(g, dcenter, et);
+}
+
+// ---------------------------------------------------------------------------
+// reBoxAll, parallel form (domains.c:347-389).
+//
+// The reference scans boxes in ascending order with swap-remove.  Box j's
+// scan list is its own atoms followed by the arrivals from lower-index boxes
+// (in source order, then in each source's departure order); arrivals from
+// higher-index boxes are appended after the scan.  Which atoms leave a box,
+// and for where, depends only on each atom's own position, so:
+//   classify  per slot: destination (+-1 box per axis, periodic wrap) and
+//             the moved position; departing records copied to a stage.
+//   plan      per box: count lower arrivals, then replay the swap-remove
+//             scan with placeholders for them -> departure order and the
+//             box's arrangement after its scan.
+//   apply     per box: move stayers, place lower arrivals into their
+//             placeholders and append higher arrivals in source order.
+// If an arrival from a lower box would itself leave again when rescanned
+// (a move of more than one box per axis, or r+boxsize rounding to boxsize),
+// the plan is invalid and a serial replay of reBoxAll runs instead.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void copy_record(const Slots &dst, int ds, const Slots &src, int ss,
+                                            bool mixed) {
+  dst.id[ds] = src.id[ss];
+  dst.itype[ds] = src.itype[ss];
+  dst.mass[ds] = src.mass[ss];
+  dst.r[ds] = src.r[ss];
+  dst.p[ds] = src.p[ss];
+  dst.f[ds] = src.f[ss];
+  dst.rho[ds] = src.rho[ss];
+  dst.fi[ds] = src.fi[ss];
+  if (mixed) dst.pos32[ds] = src.pos32[ss];
+}
+
+// classify one slot; r is the (possibly just advanced) position
+__device__ __forceinline__ void classify_slot(const Geom &g, const Slots &s, int slot, bool valid,
+                                              d4 r, bool mixed, const RebinWork &w,
+                                              int *status) {
+  const int b = slot >> 6;
+  bool dep = false;
+  if (valid) {
+    int ixo[3], ixn[3];
+    box_ixyz(g, b, ixo);
+    double rn[3] = {r.x, r.y, r.z};
+    double rc[3] = {r.x, r.y, r.z};
+    for (int k = 0; k < 3; k++) {
+      if (rc[k] < 0.0) {
+        ixn[k] = ixo[k] - 1;
+        rn[k] += g.boxsize[k];
+      } else if (rc[k] >= g.boxsize[k]) {
+        ixn[k] = ixo[k] + 1;
+        rn[k] -= g.boxsize[k];
+      } else {
+        ixn[k] = ixo[k];
+      }
+    }
+    int jb = box_from_ixyz(g, ixn);
+    if (jb >= 0 && jb != b) {
+      dep = true;
+      w.dest[slot] = jb;
+      Slots st = w.stage;
+      st.id[slot] = s.id[slot];
+      st.itype[slot] = s.itype[slot];
+      st.mass[slot] = s.mass[slot];
+      st.r[slot] = d4{rn[0], rn[1], rn[2], 0.0};
+      st.p[slot] = s.p[slot];
+      st.f[slot] = s.f[slot];
+      st.rho[slot] = s.rho[slot];
+      st.fi[slot] = s.fi[slot];
+      if (mixed) st.pos32[slot] = make_float4((float)rn[0], (float)rn[1], (float)rn[2], 0.f);
+      if (jb > b) {
+        // re-examined in jb's scan: must stay there
+        int ix2[3], ix3[3];
+        box_ixyz(g, jb, ix2);
+        for (int k = 0; k < 3; k++) {
+          if (rn[k] < 0.0) ix3[k] = ix2[k] - 1;
+          else if (rn[k] >= g.boxsize[k]) ix3[k] = ix2[k] + 1;
+          else ix3[k] = ix2[k];
+        }
+        int jb2 = box_from_ixyz(g, ix3);
+        if (jb2 >= 0 && jb2 != jb) atomicExch(status + ST_REBIN_SERIAL, 1);
+      }
+    }
+  }
+  unsigned m = __ballot_sync(0xffffffffu, dep);
+  if ((threadIdx.x & 31) == 0) w.depmask[slot >> 5] = m;
+}
+
+template <bool UPDATE, bool VEL>
+__global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt_v, double dt_r,
+                                                      double rmass, bool mixed, bool classify,
+                                                      RebinWork w, int *status) {
+  const long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nslots = g.nboxes * CG_MAXATOMS;
+  if (slot >= nslots) return;  // nslots is a multiple of 64: whole warps exit
+  const int b = (int)(slot >> 6), k = (int)(slot & 63);
+  const bool valid = k < s.natoms[b];
+  d4 r = d4{0.0, 0.0, 0.0, 0.0};
+  if (valid) {
+    r = s.r[slot];
+    if (UPDATE) {
+      d4 p = s.p[slot];
+      if (VEL) {
+        // advanceVelocity, timestep.c:71
+        d4 f = s.f[slot];
+        p.x = p.x - dt_v * f.x;
+        p.y = p.y - dt_v * f.y;
+        p.z = p.z - dt_v * f.z;
+        s.p[slot] = p;
+      }
+      // advancePositions, timestep.c:104
+      r.x = r.x + dt_r * p.x / rmass;
+      r.y = r.y + dt_r * p.y / rmass;
+      r.z = r.z + dt_r * p.z / rmass;
+      s.r[slot] = r;
+      if (mixed) s.pos32[slot] = make_float4((float)r.x, (float)r.y, (float)r.z, 0.f);
+    }
+  }
+  if (classify) classify_slot(g, s, (int)slot, valid, r, mixed, w, status);
+}
+
+static unsigned slot_blocks(const Geom &g) {
+  long nslots = (long)g.nboxes * CG_MAXATOMS;
+  return (unsigned)((nslots + 255) / 256);
+}
+
+void launch_advance_positions(const Geom &g, Slots s, double dt, double rmass, bool mixed,
+                              bool classify, const RebinWork &w, int *status, cudaStream_t st) {
+  advance_kernel<true, false><<<slot_blocks(g), 256, 0, st>>>(g, s, 0.0, dt, rmass, mixed,
+                                                              classify, w, status);
+}
+
+void launch_advance_vp(const Geom &g, Slots s, double dt_v, double dt_r, double rmass,
+                       bool mixed, const RebinWork &w, int *status, cudaStream_t st) {
+  advance_kernel<true, true><<<slot_blocks(g), 256, 0, st>>>(g, s, dt_v, dt_r, rmass, mixed,
+                                                             true, w, status);
+}
+
+void launch_classify(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
+                     cudaStream_t st) {
+  advance_kernel<false, false><<<slot_blocks(g), 256, 0, st>>>(g, s, 0.0, 0.0, 1.0, mixed, true,
+                                                               w, status);
+}
+
+// distinct stencil boxes of b other than b, ascending
+__device__ int source_boxes(const Geom &g, int b, int *src) {
+  int n = 0;
+  if (g.nboxes == 1) return 0;
+  int ix[3];
+  box_ixyz(g, b, ix);
+  for (int i = -1; i <= 1; i++)
+    for (int j = -1; j <= 1; j++)
+      for (int k = -1; k <= 1; k++) {
+        int t[3] = {ix[0] + i, ix[1] + j, ix[2] + k};
+        int nb = box_from_ixyz(g, t);
+        if (nb < 0 || nb == b) continue;
+        bool dup = false;
+        for (int q = 0; q < n; q++) dup |= (src[q] == nb);
+        if (dup) continue;
+        int q = n++;
+        while (q > 0 && src[q - 1] > nb) {
+          src[q] = src[q - 1];
+          q--;
+        }
+        src[q] = nb;
+      }
+  return n;
+}
+
+__device__ __forceinline__ unsigned long long box_mask(const RebinWork &w, int b) {
+  return (unsigned long long)w.depmask[2 * b] | ((unsigned long long)w.depmask[2 * b + 1] << 32);
+}
+
+__device__ __forceinline__ void set_error(int *status, int code) {
+  atomicCAS(status + ST_ERROR, 0, code);
+}
+
+__global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nboxes) return;
+  if (*(volatile int *)(status + ST_REBIN_SERIAL)) return;
+  const unsigned long long mask = box_mask(w, b);
+  const int n = s.natoms[b];
+  int src[26];
+  const int ns = source_boxes(g, b, src);
+  int n_lo = 0;
+  for (int q = 0; q < ns && src[q] < b; q++) {
+    unsigned long long m = box_mask(w, src[q]);
+    while (m) {
+      int j = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      n_lo += (w.dest[src[q] * CG_MAXATOMS + j] == b);
+    }
+  }
+  w.n_lo[b] = n_lo;
+  if (mask == 0ull && n_lo == 0) {
+    w.n_dep[b] = 0;
+    w.final_len[b] = n;
+    return;
+  }
+  int L = n + n_lo;
+  if (n_lo > 0 && L >= CG_MAXATOMS) {  // moveAtom aborts at 64 (domains.c:229)
+    set_error(status, -11);
+    w.n_dep[b] = 0;
+    w.final_len[b] = 0;
+    return;
+  }
+  uint8_t arr[CG_MAXATOMS];
+  for (int t = 0; t < n; t++) arr[t] = (uint8_t)t;
+  for (int t = 0; t < n_lo; t++) arr[n + t] = (uint8_t)(CG_MAXATOMS + t);
+  int i = 0, d = 0;
+  uint8_t *order = w.dep_order + (size_t)b * CG_MAXATOMS;
+  while (i < L) {
+    int e = arr[i];
+    if (e < CG_MAXATOMS && ((mask >> e) & 1ull)) {
+      order[d++] = (uint8_t)e;
+      arr[i] = arr[--L];
+    } else {
+      i++;
+    }
+  }
+  uint8_t *fs = w.final_src + (size_t)b * CG_MAXATOMS;
+  for (int t = 0; t < L; t++) fs[t] = arr[t];
+  w.n_dep[b] = d;
+  w.final_len[b] = L;
+}
+
+__global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int *status) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nboxes) return;
+  if (*(volatile int *)(status + ST_REBIN_SERIAL)) return;
+  if (*(volatile int *)(status + ST_ERROR)) return;
+  const unsigned long long mask = box_mask(w, b);
+  const int n_lo = w.n_lo[b];
+  const int L = w.final_len[b];
+  int src[26];
+  const int ns = source_boxes(g, b, src);
+  // is anything arriving from a higher box?
+  int n_hi = 0;
+  for (int q = 0; q < ns; q++) {
+    if (src[q] < b) continue;
+    unsigned long long m = box_mask(w, src[q]);
+    while (m) {
+      int j = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      n_hi += (w.dest[src[q] * CG_MAXATOMS + j] == b);
+    }
+  }
+  if (mask == 0ull && n_lo == 0 && n_hi == 0) return;
+  if (n_hi > 0 && L + n_hi >= CG_MAXATOMS) {
+    set_error(status, -11);
+    return;
+  }
+  const int base = b * CG_MAXATOMS;
+  const uint8_t *fs = w.final_src + (size_t)b * CG_MAXATOMS;
+  // 1. stayers moved into holes (sources >= L, destinations < L)
+  if (mask != 0ull)
+    for (int t = 0; t < L; t++) {
+      int e = fs[t];
+      if (e < CG_MAXATOMS && e != t) copy_record(s, base + t, s, base + e, mixed);
+    }
+  // 2. lower arrivals into their placeholders, in (source, departure) order
+  if (n_lo > 0) {
+    int src_of[CG_MAXATOMS];
+    int p = 0;
+    for (int q = 0; q < ns && src[q] < b; q++) {
+      int sb = src[q];
+      int nd = w.n_dep[sb];
+      const uint8_t *ord = w.dep_order + (size_t)sb * CG_MAXATOMS;
+      for (int d = 0; d < nd; d++) {
+        int j = ord[d];
+        if (w.dest[sb * CG_MAXATOMS + j] == b) src_of[p++] = sb * CG_MAXATOMS + j;
+      }
+    }
+    for (int t = 0; t < L; t++) {
+      int e = fs[t];
+      if (e >= CG_MAXATOMS) copy_record(s, base + t, w.stage, src_of[e - CG_MAXATOMS], mixed);
+    }
+  }
+  // 3. higher arrivals appended
+  int h = 0;
+  for (int q = 0; q < ns; q++) {
+    int sb = src[q];
+    if (sb < b) continue;
+    int nd = w.n_dep[sb];
+    const uint8_t *ord = w.dep_order + (size_t)sb * CG_MAXATOMS;
+    for (int d = 0; d < nd; d++) {
+      int j = ord[d];
+      if (w.dest[sb * CG_MAXATOMS + j] == b) {
+        copy_record(s, base + L + h, w.stage, sb * CG_MAXATOMS + j, mixed);
+        h++;
+      }
+    }
+  }
+  s.natoms[b] = L + h;
+}
+
+// reBoxAll replayed serially on the device (used only when the parallel plan
+// cannot reproduce it); the reference algorithm, statement for statement
+__global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status) {
+  if (!*(volatile int *)(status + ST_REBIN_SERIAL)) return;
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  status[ST_SERIAL_RUNS] += 1;
+  for (int b = 0; b < g.nboxes; b++) {
+    int ixo[3];
+    box_ixyz(g, b, ixo);
+    int i = 0;
+    while (i < s.natoms[b]) {
+      int off = b * CG_MAXATOMS + i;
+      d4 r = s.r[off];
+      double rc[3] = {r.x, r.y, r.z}, rn[3] = {r.x, r.y, r.z};
+      int ixn[3];
+      for (int k = 0; k < 3; k++) {
+        if (rc[k] < 0.0) {
+          ixn[k] = ixo[k] - 1;
+          rn[k] += g.boxsize[k];
+        } else if (rc[k] >= g.boxsize[k]) {
+          ixn[k] = ixo[k] + 1;
+          rn[k] -= g.boxsize[k];
+        } else {
+          ixn[k] = ixo[k];
+        }
+      }
+      int jb = box_from_ixyz(g, ixn);
+      if (jb < 0 || jb == b) {
+        i++;
+        continue;
+      }
+      s.r[off] = d4{rn[0], rn[1], rn[2], 0.0};
+      if (mixed) s.pos32[off] = make_float4((float)rn[0], (float)rn[1], (float)rn[2], 0.f);
+      int nj = s.natoms[jb];
+      if (nj >= CG_MAXATOMS - 1) {  // reaching 64 aborts (domains.c:229)
+        set_error(status, -11);
+        return;
+      }
+      copy_record(s, jb * CG_MAXATOMS + nj, s, off, mixed);
+      s.natoms[jb] = nj + 1;
+      int ni = s.natoms[b] - 1;
+      s.natoms[b] = ni;
+      if (ni) copy_record(s, off, s, b * CG_MAXATOMS + ni, mixed);
+    }
+  }
+}
+
+void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
+                         cudaStream_t st) {
+  unsigned nb = (unsigned)((g.nboxes + 127) / 128);
+  rebin_plan_kernel<<<nb, 128, 0, st>>>(g, s, w, status);
+  rebin_apply_kernel<<<nb, 128, 0, st>>>(g, s, mixed, w, status);
+  rebin_serial_kernel<<<1, 32, 0, st>>>(g, s, mixed, status);
+}
+
+// ---------------------------------------------------------------------------
+// compaction: box_start = exclusive scan of natoms; atom_slot[a] = slot
+// ---------------------------------------------------------------------------
+#define CP_THREADS 256
+#define CP_PER 8
+#define CP_CHUNK (CP_THREADS * CP_PER)
+
+int compact_partials(int nboxes) { return (nboxes + CP_CHUNK - 1) / CP_CHUNK; }
+
+__device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total) {
+  // sh has CP_THREADS/32 ints
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int t = lane < CP_THREADS / 32 ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < CP_THREADS / 32) sh[lane] = t;
+  }
+  __syncthreads();
+  total = sh[CP_THREADS / 32 - 1];
+  int pre = wid > 0 ? sh[wid - 1] : 0;
+  __syncthreads();
+  return pre + x - v;
+}
+
+__global__ void __launch_bounds__(CP_THREADS) compact_sum_kernel(const int *natoms, int nboxes,
+                                                                 int *partials) {
+  __shared__ int sh[CP_THREADS / 32];
+  int base = blockIdx.x * CP_CHUNK + threadIdx.x * CP_PER;
+  int v = 0;
+  for (int q = 0; q < CP_PER; q++)
+    if (base + q < nboxes) v += natoms[base + q];
+  int total;
+  block_excl_scan(v, sh, total);
+  if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(CP_THREADS) compact_scan_partials_kernel(int *partials,
+                                                                           int npart) {
+  __shared__ int sh[CP_THREADS / 32];
+  int carry = 0;
+  for (int base = 0; base < npart; base += CP_THREADS) {
+    int idx = base + threadIdx.x;
+    int v = idx < npart ? partials[idx] : 0;
+    int total;
+    int ex = block_excl_scan(v, sh, total);
+    if (idx < npart) partials[idx] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(CP_THREADS) compact_write_kernel(const int *natoms, int nboxes,
+                                                                   const int *partials,
+                                                                   int *box_start,
+                                                                   int *atom_slot, int ntot) {
+  __shared__ int sh[CP_THREADS / 32];
+  int base = blockIdx.x * CP_CHUNK + threadIdx.x * CP_PER;
+  int loc[CP_PER];
+  int v = 0;
+  for (int q = 0; q < CP_PER; q++) {
+    loc[q] = (base + q < nboxes) ? natoms[base + q] : 0;
+    v += loc[q];
+  }
+  int total;
+  int off = block_excl_scan(v, sh, total) + partials[blockIdx.x];
+  for (int q = 0; q < CP_PER; q++) {
+    int b = base + q;
+    if (b < nboxes) {
+      box_start[b] = off;
+      // the counts sum to ntot unless a reported overflow left them inconsistent
+      for (int k = 0; k < loc[q]; k++)
+        if (off + k < ntot) atom_slot[off + k] = b * CG_MAXATOMS + k;
+      off += loc[q];
+      if (b == nboxes - 1) box_start[nboxes] = off;
+    }
+  }
+}
+
+void launch_compact(const Geom &g, const int *natoms, int *box_start, int *atom_slot, int ntot,
+                    int *partials, int npart, cudaStream_t st) {
+  compact_sum_kernel<<<npart, CP_THREADS, 0, st>>>(natoms, g.nboxes, partials);
+  compact_scan_partials_kernel<<<1, CP_THREADS, 0, st>>>(partials, npart);
+  compact_write_kernel<<<npart, CP_THREADS, 0, st>>>(natoms, g.nboxes, partials, box_start,
+                                                     atom_slot, ntot);
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reductions: energy (sum of f[3]), stress share, pair count
+// ---------------------------------------------------------------------------
+#define RD_THREADS 256
+#define RD_PER 16
+
+int reduce_partials(int ntot) {
+  int n = (ntot + RD_THREADS * RD_PER - 1) / (RD_THREADS * RD_PER);
+  return n < 1 ? 1 : n;
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+  __syncthreads();
+  return t;
+}
+
+__device__ __forceinline__ long long block_sum_l(long long v, long long *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  long long t = 0;
+  if (threadIdx.x == 0)
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q];
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(RD_THREADS) reduce_force_kernel(ForceArgs A, double *partials,
+                                                                  long long *ipartials) {
+  __shared__ double shd[RD_THREADS / 32];
+  __shared__ long long shl[RD_THREADS / 32];
+  int base = blockIdx.x * RD_THREADS * RD_PER;
+  double e = 0.0, sx = 0.0;
+  long long np = 0;
+  for (int q = 0; q < RD_PER; q++) {
+    int a = base + q * RD_THREADS + threadIdx.x;
+    if (a < A.ntot) {
+      e += A.s.f[A.atom_slot[a]].w;
+      sx += A.atom_stress[a];
+      np += A.nbr_n[a];
+    }
+  }
+  e = block_sum_d(e, shd);
+  sx = block_sum_d(sx, shd);
+  np = block_sum_l(np, shl);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = e;
+    partials[2 * blockIdx.x + 1] = sx;
+    ipartials[blockIdx.x] = np;
+  }
+}
+
+__global__ void reduce_final_kernel(const double *partials, const long long *ipartials, int npart,
+                                    double *out, long long *iout) {
+  if (threadIdx.x != 0) return;
+  double e = 0.0, sx = 0.0;
+  long long np = 0;
+  for (int q = 0; q < npart; q++) {
+    e += partials[2 * q];
+    sx += partials[2 * q + 1];
+    np += ipartials[q];
+  }
+  out[0] = e;
+  out[1] = sx;
+  iout[0] = np;
+}
+
+void launch_reduce(const ForceArgs &A, double *partials, long long *ipartials, int npart,
+                   double *out, long long *iout, cudaStream_t st) {
+  reduce_force_kernel<<<npart, RD_THREADS, 0, st>>>(A, partials, ipartials);
+  reduce_final_kernel<<<1, 32, 0, st>>>(partials, ipartials, npart, out, iout);
+}
+
+__global__ void __launch_bounds__(RD_THREADS) kinetic_kernel(Slots s, const int *atom_slot,
+                                                             int ntot, double *partials) {
+  __shared__ double shd[RD_THREADS / 32];
+  int base = blockIdx.x * RD_THREADS * RD_PER;
+  double ek = 0.0;
+  for (int q = 0; q < RD_PER; q++) {
+    int a = base + q * RD_THREADS + threadIdx.x;
+    if (a < ntot) {
+      d4 p = s.p[atom_slot[a]];
+      ek += p.x * p.x + p.y * p.y + p.z * p.z;
+    }
+  }
+  ek = block_sum_d(ek, shd);
+  if (threadIdx.x == 0) partials[blockIdx.x] = ek;
+}
+
+__global__ void kinetic_final_kernel(const double *partials, int npart, double rmass,
+                                     double *out) {
+  if (threadIdx.x != 0) return;
+  double ek = 0.0;
+  for (int q = 0; q < npart; q++) ek += partials[q];
+  out[0] = ek / (2.0 * rmass);
+}
+
+void launch_kinetic(const Geom &g, Slots s, const int *atom_slot, int ntot, double rmass,
+                    double *partials, int npart, double *out, cudaStream_t st) {
+  (void)g;
+  kinetic_kernel<<<npart, RD_THREADS, 0, st>>>(s, atom_slot, ntot, partials);
+  kinetic_final_kernel<<<1, 32, 0, st>>>(partials, npart, rmass, out);
+}
+
+// ---------------------------------------------------------------------------
+// host layout (real3, 24-byte stride) <-> device double4
+// ---------------------------------------------------------------------------
+__global__ void unpack3_kernel(const double *src3, d4 *dst, long n) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dst[i] = d4{src3[3 * i], src3[3 * i + 1], src3[3 * i + 2], 0.0};
+}
+
+__global__ void pack3_kernel(const d4 *src, double *dst3, long n) {
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  d4 v = src[i];
+  dst3[3 * i] = v.x;
+  dst3[3 * i + 1] = v.y;
+  dst3[3 * i + 2] = v.z;
+}
+
+void launch_unpack3(const double *src3, d4 *dst, long n, cudaStream_t st) {
+  if (n > 0) unpack3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src3, dst, n);
+}
+
+void launch_pack3(const d4 *src, double *dst3, long n, cudaStream_t st) {
+  if (n > 0) pack3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst3, n);
+}
+
+__global__ void pos32_kernel(Geom g, Slots s) {
+  long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
+  d4 r = s.r[slot];
+  s.pos32[slot] = make_float4((float)r.x, (float)r.y, (float)r.z, 0.f);
+}
+
+void launch_pos32(const Geom &g, Slots s, cudaStream_t st) {
+  pos32_kernel<<<slot_blocks(g), 256, 0, st>>>(g, s);
+}
+
+// ---------------------------------------------------------------------------
+// initial binning: n putAtomInBox calls (domains.c:237-291) as a counting
+// sort that keeps call order within each box
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int world_box(const Geom &g, const double *xyz_in, double *xyz,
+                                         bool &ok) {
+  int ib[3];
+  ok = true;
+  for (int m = 0; m < 3; m++) {
+    double x = xyz_in[m];
+    if (x < 0.0) x += g.bounds[m];
+    else if (x >= g.bounds[m]) x -= g.bounds[m];
+    xyz[m] = x;
+    ib[m] = (int)floor(x / g.boxsize[m]);
+    if (ib[m] < 0 || ib[m] >= g.nbx[m]) ok = false;
+  }
+  return ib[0] + g.nbx[0] * ib[1] + g.nbx[0] * g.nbx[1] * ib[2];
+}
+
+__global__ void bin_count_kernel(Geom g, Slots s, int n, const double *xyz, int *tmp_index,
+                                 int *status) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double w[3];
+  bool ok;
+  int b = world_box(g, xyz + 3 * (long)t, w, ok);
+  if (!ok) {
+    set_error(status, -12);
+    return;
+  }
+  int pos = atomicAdd(s.natoms + b, 1);
+  if (pos >= CG_MAXATOMS) {
+    set_error(status, -11);
+    return;
+  }
+  tmp_index[b * CG_MAXATOMS + pos] = t;
+}
+
+__global__ void bin_place_kernel(Geom g, const double *dcenter, Slots s, int n,
+                                 const double *xyz, const double *pxyz, const int *ids,
+                                 const int *types, const double *masses, int *tmp_index,
+                                 int *status) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nboxes) return;
+  if (*(volatile int *)(status + ST_ERROR)) return;
+  int nb = s.natoms[b];
+  if (nb > CG_MAXATOMS) return;  // reported by bin_count_kernel
+  int *ix = tmp_index + b * CG_MAXATOMS;
+  for (int i = 1; i < nb; i++) {  // insertion sort: call order
+    int v = ix[i], j = i - 1;
+    while (j >= 0 && ix[j] > v) {
+      ix[j + 1] = ix[j];
+      j--;
+    }
+    ix[j + 1] = v;
+  }
+  for (int k = 0; k < nb; k++) {
+    int t = ix[k];
+    int slot = b * CG_MAXATOMS + k;
+    double w[3];
+    bool ok;
+    world_box(g, xyz + 3 * (long)t, w, ok);
+    s.id[slot] = ids[t];
+    s.itype[slot] = types[t];
+    s.mass[slot] = masses[t];
+    s.r[slot] = d4{w[0] - dcenter[3 * b], w[1] - dcenter[3 * b + 1], w[2] - dcenter[3 * b + 2],
+                   0.0};
+    s.p[slot] = d4{pxyz[3 * (long)t], pxyz[3 * (long)t + 1], pxyz[3 * (long)t + 2], 0.0};
+    s.f[slot] = d4{0.0, 0.0, 0.0, 0.0};
+    s.rho[slot] = 0.0;
+    s.fi[slot] = 0.0;
+  }
+}
+
+void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, const double *xyz,
+                      const double *pxyz, const int *ids, const int *types, const double *masses,
+                      int *tmp_index, int *status, cudaStream_t st) {
+  cudaMemsetAsync(s.natoms, 0, sizeof(int) * g.nboxes, st);
+  if (n > 0) bin_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(g, s, n, xyz, tmp_index, status);
+  bin_place_kernel<<<(g.nboxes + 127) / 128, 128, 0, st>>>(g, dcenter, s, n, xyz, pxyz, ids,
+                                                           types, masses, tmp_index, status);
+}
+
+// ---------------------------------------------------------------------------
+// Chebyshev fit in FP64 (genCheb/genDer, cheby.c:125-179, 219-270), one
+// block of n threads per series
+// ---------------------------------------------------------------------------
+__global__ void cheb_fit_kernel(const double *v, double x0, double xn, double invdx, int n,
+                                double *coef, double *dcoef) {
+  __shared__ double fk[64];
+  __shared__ double c[64];
+  const double PI = 3.141592653589793;
+  int k = threadIdx.x;
+  double a = x0, b = xn;
+  double bma = 0.5 * (b - a), bpa = 0.5 * (b + a);
+  if (k < n) {
+    double y = cos(PI * (k + 0.5) / n);
+    // eamInterpolateDerivlocal (cheby.c:15-60): table value, >1e10 -> 0
+    double r = y * bma + bpa;
+    if (r < x0) r = x0;
+    else if (r > xn) r = xn;
+    r = (r - x0) * invdx;
+    double fl = floor(r);
+    int i1 = (int)fl;
+    r = r - fl;
+    double gi = v[i1 + 1] - v[i1 - 1];
+    double val = v[i1] + 0.5 * r * (r * (v[i1 + 1] + v[i1 - 1] - 2.0 * v[i1]) + gi);
+    if (val > 1.0e10) val = 0.0;
+    fk[k] = val;
+  }
+  __syncthreads();
+  if (k < n) {
+    double fac = 2.0 / n, sum = 0.0;
+    for (int q = 0; q < n; q++) sum += fk[q] * cos(PI * k * (q + 0.5) / n);
+    c[k] = fac * sum;
+    coef[k] = c[k];
+  }
+  __syncthreads();
+  if (k == 0) {
+    double cd[64];
+    cd[n - 1] = 0.0;
+    cd[n - 2] = 2.0 * (n - 1) * c[n - 1];
+    for (int j = n - 2; j > 0; j--) cd[j - 1] = cd[j + 1] + 2 * (j)*c[j];
+    double con = 2.0 / (b - a);
+    for (int j = 0; j < n; j++) dcoef[j] = cd[j] * con;
+  }
+}
+
+void launch_cheb_fit(const double *table_v, double x0, double xn, double invdx, int n_terms,
+                     double *coef, double *dcoef, cudaStream_t st) {
+  cheb_fit_kernel<<<1, 64, 0, st>>>(table_v, x0, xn, invdx, n_terms, coef, dcoef);
+}
+
+}  // namespace cg

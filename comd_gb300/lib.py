@@ -1,0 +1,244 @@
+"""ctypes bindings of libcomdgb.so (the C ABI declared in include/comdgb.h).
+
+Python is only the driver here: every computation runs in the library's
+CUDA kernels.  Loading fails loudly if the library is missing; there is no
+CPU fallback.
+"""
+import ctypes as C
+import os
+import threading
+
+from .abi import EamCheby, EamPotential, LjPotential, SimFlat
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libcomdgb.so")
+POT_DIR = os.path.join(HERE, "pots")
+
+POT_EAM_TABLE, POT_EAM_CHEBY, POT_LJ = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+DISP_NONE, DISP_UNIFORM, DISP_GAUSSIAN = 0, 1, 2
+ERR_MAXATOMS, ERR_BOXRANGE, ERR_NOBOX = -11, -12, -3
+
+# s -> t0 (src-flat/include/constants.h:61), amu -> m_e, k_B in Ha/K, eV in Ha
+BOHR_PER_ATU = 0.529 / 2.418e-17
+AMU_TO_ME = 1822.83
+KB_HA = 3.166811563e-6
+EV_TO_HA = 1.0 / 27.211386245988
+
+P_SIM = C.POINTER(SimFlat)
+
+
+class Opts(C.Structure):
+    _fields_ = [("potential", C.c_int), ("precision", C.c_int), ("periodic", C.c_int),
+                ("device", C.c_int), ("n_cheby", C.c_int), ("cheby_from_host", C.c_int)]
+
+
+class ComdgbError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"libcomdgb error {code}: {msg}")
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def _bind(lib):
+    L = lib
+    L.comdgb_default_opts.argtypes = [C.POINTER(Opts)]
+    L.comdgb_last_error.argtypes = [C.c_char_p, C.c_int]
+    L.comdgb_version.restype = C.c_char_p
+    L.comdgb_attach.argtypes = [P_SIM, C.POINTER(Opts)]
+    L.comdgb_force.argtypes = [C.c_void_p]
+    L.comdgb_nTimeSteps.restype = C.c_double
+    L.comdgb_nTimeSteps.argtypes = [C.c_int, P_SIM, C.c_double]
+    L.comdgb_reBoxAll.argtypes = [P_SIM]
+    L.comdgb_detach.argtypes = [P_SIM]
+    L.comdgb_sim_create.argtypes = [P_SIM, C.POINTER(Opts), C.POINTER(C.c_void_p)]
+    L.comdgb_sim_destroy.argtypes = [C.c_void_p]
+    L.comdgb_sim_upload.argtypes = [C.c_void_p, P_SIM]
+    L.comdgb_sim_download.argtypes = [C.c_void_p, P_SIM]
+    L.comdgb_sim_force.argtypes = [C.c_void_p]
+    L.comdgb_sim_steps.argtypes = [C.c_void_p, C.c_int, C.c_double]
+    L.comdgb_sim_rebox.argtypes = [C.c_void_p]
+    L.comdgb_sim_energy.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.comdgb_sim_kinetic.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    L.comdgb_sim_pair_count.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
+    L.comdgb_sim_synchronize.argtypes = [C.c_void_p]
+    L.comdgb_sim_timed_steps.argtypes = [C.c_void_p, C.c_int, C.c_double,
+                                         C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
+    L.comdgb_kernel_name.restype = C.c_char_p
+    L.comdgb_kernel_name.argtypes = [C.c_void_p, C.c_int]
+    L.comdgb_eam_read.restype = C.POINTER(EamPotential)
+    L.comdgb_eam_read.argtypes = [C.c_char_p, C.c_char_p]
+    L.comdgb_eam_free.argtypes = [C.c_void_p]
+    L.comdgb_cheb_make.restype = C.POINTER(EamCheby)
+    L.comdgb_cheb_make.argtypes = [C.c_void_p, C.c_int, C.c_int]
+    L.comdgb_cheb_free.argtypes = [C.c_void_p]
+    L.comdgb_lj_make.restype = C.POINTER(LjPotential)
+    L.comdgb_lj_make.argtypes = [C.c_double] * 4
+    L.comdgb_lj_free.argtypes = [C.c_void_p]
+    L.comdgb_fcc.restype = P_SIM
+    L.comdgb_fcc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                             C.c_void_p, C.POINTER(C.c_int)]
+    L.comdgb_seed.argtypes = [P_SIM, C.c_uint64, C.c_int, C.c_double, C.c_double, C.c_double]
+    L.comdgb_sim_free_host.argtypes = [P_SIM]
+    L.comdgb_rebox_host.argtypes = [P_SIM, C.c_int, C.c_int]
+    L.comdgb_put_atoms.argtypes = [P_SIM, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_int]
+    return lib
+
+
+def load(build_if_missing=True):
+    """The loaded libcomdgb.so (built in-tree on first use if absent)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH) and build_if_missing:
+                from .build import build
+                build()
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(f"libcomdgb.so not built at {LIB_PATH}")
+            _lib = _bind(C.CDLL(LIB_PATH))
+        return _lib
+
+
+def last_error():
+    buf = C.create_string_buffer(512)
+    load().comdgb_last_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+def check(rc):
+    if rc < 0:
+        raise ComdgbError(rc, last_error())
+    return rc
+
+
+def opts(potential=POT_EAM_TABLE, precision=PREC_FP64, periodic=True, device=0,
+         cheby_from_host=False):
+    o = Opts()
+    load().comdgb_default_opts(C.byref(o))
+    o.potential = potential
+    o.precision = precision
+    o.periodic = int(periodic)
+    o.device = device
+    o.cheby_from_host = int(cheby_from_host)
+    return o
+
+
+class Potential:
+    """Owns a host potential struct made by the library."""
+
+    def __init__(self, ptr, kind, free_fn):
+        self.ptr = ptr
+        self.kind = kind
+        self._free = free_fn
+
+    @property
+    def base(self):
+        return C.cast(self.ptr, C.c_void_p)
+
+    def close(self):
+        if self.ptr:
+            self._free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def eam_potential(name="cu", potdir=POT_DIR):
+    L = load()
+    p = L.comdgb_eam_read(potdir.encode(), name.encode())
+    if not p:
+        raise IOError(f"cannot read EAM potential {name} from {potdir}")
+    return Potential(p, "eam", L.comdgb_eam_free)
+
+
+def lj_potential(sigma, epsilon, cutoff, mass):
+    L = load()
+    return Potential(L.comdgb_lj_make(sigma, epsilon, cutoff, mass), "lj", L.comdgb_lj_free)
+
+
+def fcc(nx, ny, nz, lat, defgrad, bf, pot):
+    """create_fcc_lattice on the host; returns a SimFlat pointer (caller frees)."""
+    L = load()
+    st = C.c_int(0)
+    s = L.comdgb_fcc(nx, ny, nz, lat, defgrad, bf, pot.base, C.byref(st))
+    if not s:
+        raise ComdgbError(st.value, "comdgb_fcc failed")
+    return s
+
+
+def seed(s, seed_value, disp_kind, amp, temp_k, mass_amu):
+    load().comdgb_seed(s, seed_value, disp_kind, amp, temp_k, mass_amu)
+
+
+def free_host(s):
+    load().comdgb_sim_free_host(s)
+
+
+class DeviceSim:
+    """A device-resident simulation handle (comdgb_sim_*)."""
+
+    def __init__(self, host_sim, o):
+        self.L = load()
+        self.h = C.c_void_p()
+        check(self.L.comdgb_sim_create(host_sim, C.byref(o), C.byref(self.h)))
+
+    def close(self):
+        if self.h:
+            self.L.comdgb_sim_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, s):
+        check(self.L.comdgb_sim_upload(self.h, s))
+
+    def download(self, s):
+        check(self.L.comdgb_sim_download(self.h, s))
+
+    def force(self):
+        check(self.L.comdgb_sim_force(self.h))
+        return self.energy()
+
+    def steps(self, n, dt=1e-15):
+        check(self.L.comdgb_sim_steps(self.h, n, dt))
+        return self.energy()
+
+    def rebox(self):
+        check(self.L.comdgb_sim_rebox(self.h))
+
+    def energy(self):
+        e, st = C.c_double(), C.c_double()
+        check(self.L.comdgb_sim_energy(self.h, C.byref(e), C.byref(st)))
+        return e.value, st.value
+
+    def kinetic(self):
+        ek = C.c_double()
+        check(self.L.comdgb_sim_kinetic(self.h, C.byref(ek)))
+        return ek.value
+
+    def pair_count(self):
+        v = C.c_longlong()
+        check(self.L.comdgb_sim_pair_count(self.h, C.byref(v)))
+        return v.value
+
+    def synchronize(self):
+        check(self.L.comdgb_sim_synchronize(self.h))
+
+    def timed_steps(self, n, dt=1e-15, max_kernels=16):
+        step = (C.c_float * n)()
+        kern = (C.c_float * max_kernels)()
+        nk = check(self.L.comdgb_sim_timed_steps(self.h, n, dt, step, kern, max_kernels))
+        names = [self.L.comdgb_kernel_name(self.h, k).decode() for k in range(nk)]
+        return list(step), dict(zip(names, list(kern)[:nk]))

@@ -1,0 +1,160 @@
+/*
+ * comdgb.h -- C ABI of libcomdgb.so, the GB300 (sm_103a) implementation of
+ * CoMD's force-and-integrate timestep.
+ *
+ * Two ways in:
+ *  1. Drop-in on a host simflat_t (the reference's own data model,
+ *     include/comdgb_simflat.h).  comdgb_attach() mirrors the simulation
+ *     on the GPU; comdgb_force() has the signature of the potential's force
+ *     pointer (src-flat/include/pmdTypes.h:77) so `s->pot->force =
+ *     comdgb_force` makes the reference's computeForce
+ *     (src-flat/timestep.c:110-112) run on the GPU; comdgb_nTimeSteps()
+ *     replaces nTimeSteps (src-flat/timestep.c:114-140).  The host simflat_t
+ *     stays the source of truth: every such call copies the host state to
+ *     the GPU and the results back.
+ *  2. Device-resident handles (comdgb_sim_*) for callers that keep the
+ *     state on the GPU between calls and read it back only when asked.
+ *
+ * Every function returns 0 or a negative COMDGB_ERR_* code (the reference
+ * exit()s instead); comdgb_last_error() gives the message.  All functions
+ * are host functions; one library instance drives one GPU per handle.
+ */
+#ifndef COMDGB_H
+#define COMDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "comdgb_simflat.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* potential kinds */
+enum {
+  COMDGB_POT_EAM_TABLE = 0, /* eamForce with eamInterpolateDeriv, src-flat/eam.c:438-660 */
+  COMDGB_POT_EAM_CHEBY = 1, /* eamForce built with -DUSE_CHEBY, src-flat/cheby.c:276-310 */
+  COMDGB_POT_LJ = 2         /* LJ, src-flat/ljForce.c:89-224 */
+};
+
+/* arithmetic of the force kernels (integration is always FP64) */
+enum {
+  COMDGB_PREC_FP64 = 0,  /* every pair term in double precision */
+  COMDGB_PREC_MIXED = 1  /* FP32 pair terms on box-relative coordinates,
+                            Kahan-compensated FP32 per-atom sums, FP64 totals */
+};
+
+/* error codes; -11 and -3 keep the reference's abort codes */
+enum {
+  COMDGB_OK = 0,
+  COMDGB_ERR_ARG = -1,
+  COMDGB_ERR_NOBOX = -3,        /* "Need at least one cutoff wide domain" domains.c:180 */
+  COMDGB_ERR_MAXATOMS = -11,    /* "Increase maxatoms" domains.c:229 */
+  COMDGB_ERR_BOXRANGE = -12,    /* an atom's box index fell outside the grid */
+  COMDGB_ERR_CUDA = -30,
+  COMDGB_ERR_NOMEM = -31,
+  COMDGB_ERR_NOTATTACHED = -32,
+  COMDGB_ERR_IO = -33,
+  COMDGB_ERR_UNSUPPORTED = -34,
+  COMDGB_ERR_NONFINITE = -35    /* NaN/Inf in the total energy */
+};
+
+typedef struct comdgb_opts {
+  int potential;   /* COMDGB_POT_* */
+  int precision;   /* COMDGB_PREC_* */
+  int periodic;    /* 1: periodic boundaries (reference default PERIODIC=1) */
+  int device;      /* CUDA device ordinal */
+  int n_cheby;     /* Chebyshev terms; only 32 is supported (NUM_CHEBY, docompute.c:56) */
+  int cheby_from_host; /* 1: take the series from s->ch_pot; 0: fit them on the GPU */
+} comdgb_opts;
+
+/* fills o with the reference defaults (EAM table, FP64, periodic, device 0) */
+void comdgb_default_opts(comdgb_opts *o);
+
+/* ---------------- drop-in API on a host simflat_t ---------------- */
+
+/* Mirror s on the GPU.  s->pot must be an eampotential_t (EAM kinds) or an
+ * ljpotential_t (LJ); for COMDGB_POT_EAM_CHEBY with cheby_from_host, s->ch_pot
+ * must be set (setChebPot, src-flat/cheby.c:99-121). */
+int comdgb_attach(simflat_t *s, const comdgb_opts *o);
+/* Drop-in for the potential's force pointer (pmdTypes.h:77): copies the host
+ * slot arrays up, computes, writes f, rho, fi, e and stress back into s. */
+int comdgb_force(void *s);
+/* Drop-in for nTimeSteps (timestep.c:114-140): n velocity-Verlet steps and a
+ * final force call on the GPU; dt in seconds; returns s->e (NaN on error,
+ * see comdgb_last_error). */
+double comdgb_nTimeSteps(int n, simflat_t *s, double dt);
+/* Drop-in for reBoxAll (domains.c:347-389) on the GPU. */
+int comdgb_reBoxAll(simflat_t *s);
+int comdgb_detach(simflat_t *s);
+
+/* ---------------- device-resident handles ---------------- */
+
+typedef struct comdgb_sim comdgb_sim;
+
+/* Creates a GPU simulation from a host simflat_t (copied; s is not kept). */
+int comdgb_sim_create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out);
+void comdgb_sim_destroy(comdgb_sim *h);
+/* copy the host simulation's slot arrays to the GPU / the GPU's back */
+int comdgb_sim_upload(comdgb_sim *h, const simflat_t *s);
+int comdgb_sim_download(comdgb_sim *h, simflat_t *s);
+/* one force evaluation on the GPU state (results stay on the GPU) */
+int comdgb_sim_force(comdgb_sim *h);
+/* n steps + final force on the GPU state; dt in seconds; captured in a
+ * CUDA graph after the first call with the same dt */
+int comdgb_sim_steps(comdgb_sim *h, int n, double dt);
+int comdgb_sim_rebox(comdgb_sim *h);
+/* totals of the last force call: energy, stress (reference definitions) */
+int comdgb_sim_energy(comdgb_sim *h, double *e, double *stress);
+/* kinetic energy sum p^2/2M on the GPU */
+int comdgb_sim_kinetic(comdgb_sim *h, double *ek);
+/* device-side counters: unique in-cutoff pairs of the last force call */
+int comdgb_sim_pair_count(comdgb_sim *h, long long *pairs);
+int comdgb_sim_synchronize(comdgb_sim *h);
+
+/* Timed run for benchmarks: `n` steps (graph replays), events recorded on
+ * the library's stream; step_ms[n] gets each step's device time and
+ * kernel_ms[n_kernels] the average device time of each kernel of a step
+ * (names via comdgb_kernel_name).  Returns the number of kernels per step. */
+int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms,
+                           float *kernel_ms, int max_kernels);
+const char *comdgb_kernel_name(comdgb_sim *h, int k);
+
+/* ---------------- host-side setup (reference setup routines) ---------------- */
+
+/* setEamPot / eamReadASCII (eam.c:102-109, 347-398): reads <dir>/<name>.{phi,rho,f,doc} */
+eampotential_t *comdgb_eam_read(const char *dir, const char *name);
+void comdgb_eam_free(eampotential_t *p);
+/* setChebPot (cheby.c:99-121), the series fitted in FP64 on the GPU */
+eam_cheby_t *comdgb_cheb_make(const eampotential_t *p, int n, int device);
+void comdgb_cheb_free(eam_cheby_t *c);
+/* an LJ potential (getLJPot, ljForce.c:75-86, with caller parameters) */
+ljpotential_t *comdgb_lj_make(double sigma, double epsilon, double cutoff, double mass);
+void comdgb_lj_free(ljpotential_t *p);
+/* create_fcc_lattice (ic_fcc.c:63-141) into a new host simflat_t */
+simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double bf,
+                      pmd_base_potential_t *pot, int *status);
+/* seeded displacement / momenta (include/comdgb_seed.h) followed by nothing;
+ * the caller reboxes */
+void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,
+                 double mass_amu);
+void comdgb_sim_free_host(simflat_t *s);
+/* reBoxAll on the host simflat_t via the GPU (upload, rebox, download) */
+int comdgb_rebox_host(simflat_t *s, int periodic, int device);
+
+/* Bin atoms given in id order by their world coordinates on the GPU, with
+ * the slot order of n successive putAtomInBox calls (domains.c:237-291).
+ * s must have its domains allocated (nbx, boxsize, dcenter, arrays) and no
+ * atoms; fills natoms, id, iType, mass, r, p, ntot. */
+int comdgb_put_atoms(simflat_t *s, int n, const double *xyz, const double *pxyz,
+                     const int *ids, const int *itypes, const double *masses, int device);
+
+int comdgb_last_error(char *buf, int len);
+const char *comdgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* COMDGB_H */

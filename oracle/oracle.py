@@ -1,0 +1,164 @@
+"""TEST INFRASTRUCTURE ONLY: ctypes bindings of the CPU oracle and of the
+reference compiled from its sources (oracle/_ref).
+
+``Oracle`` wraps liboracle.so (the restatement in comd_oracle.c).
+``RefLib`` wraps oracle/_ref/libcomdref_{table,cheby}.so when they exist
+(they are built only where the reference sources are present).
+"""
+import ctypes as C
+import os
+import subprocess
+import threading
+
+from comd_gb300.abi import EamCheby, EamPotential, LjPotential, SimFlat
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KIND_EAM_TABLE, KIND_EAM_CHEBY, KIND_LJ = 0, 1, 2
+P_SIM = C.POINTER(SimFlat)
+
+_lock = threading.Lock()
+_oracle = None
+_refs = {}
+
+
+def build(with_ref=True):
+    """make the oracle (and oracle/_ref when the reference is present)."""
+    target = "all" if with_ref else os.path.join(HERE, "liboracle.so")
+    subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+
+
+def _bind(lib):
+    f = lib
+    f.orc_set_periodic.argtypes = [C.c_int]
+    f.orc_eam_read.restype = C.POINTER(EamPotential)
+    f.orc_eam_read.argtypes = [C.c_char_p, C.c_char_p]
+    f.orc_eam_free.argtypes = [C.c_void_p]
+    f.orc_cheb_make.restype = C.POINTER(EamCheby)
+    f.orc_cheb_make.argtypes = [C.c_void_p, C.c_int]
+    f.orc_cheb_free.argtypes = [C.c_void_p]
+    f.orc_cheb_eval.restype = C.c_double
+    f.orc_cheb_eval.argtypes = [C.c_void_p, C.c_double]
+    f.orc_table_eval.argtypes = [C.c_void_p, C.c_double, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double)]
+    f.orc_fcc.restype = P_SIM
+    f.orc_fcc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
+                          C.c_void_p, C.POINTER(C.c_int)]
+    f.orc_sim_clone.restype = P_SIM
+    f.orc_sim_clone.argtypes = [P_SIM]
+    f.orc_sim_free.argtypes = [P_SIM]
+    f.orc_alloc_domains.argtypes = [P_SIM]
+    f.orc_put_atom.argtypes = [P_SIM, C.c_int, C.c_int, C.c_double] + [C.c_double] * 6
+    f.orc_rebox_all.argtypes = [P_SIM]
+    f.orc_neighbor_boxes.argtypes = [P_SIM, C.c_int, C.POINTER(C.c_int)]
+    f.orc_eam_force.argtypes = [P_SIM, C.c_int]
+    f.orc_lj_force.argtypes = [P_SIM]
+    f.orc_force.argtypes = [P_SIM, C.c_int]
+    f.orc_ntimesteps.argtypes = [C.c_int, P_SIM, C.c_double, C.c_int]
+    f.orc_advance_velocity.argtypes = [P_SIM, C.c_double]
+    f.orc_advance_positions.argtypes = [P_SIM, C.c_double]
+    f.orc_seed_apply.argtypes = [P_SIM, C.c_uint64, C.c_int, C.c_double, C.c_double,
+                                 C.c_double]
+    f.orc_kinetic.restype = C.c_double
+    f.orc_kinetic.argtypes = [P_SIM]
+    f.orc_lj_make.restype = C.POINTER(LjPotential)
+    f.orc_lj_make.argtypes = [C.c_double] * 4
+    f.orc_free.argtypes = [C.c_void_p]
+    return lib
+
+
+def oracle_lib():
+    global _oracle
+    with _lock:
+        if _oracle is None:
+            path = os.path.join(HERE, "liboracle.so")
+            if not os.path.exists(path):
+                build(with_ref=False)
+            _oracle = _bind(C.CDLL(path))
+        return _oracle
+
+
+class Oracle:
+    """Thin OO helper over liboracle.so (all state is in C structs)."""
+
+    def __init__(self):
+        self.lib = oracle_lib()
+
+    def eam(self, potdir, name="cu"):
+        p = self.lib.orc_eam_read(potdir.encode(), name.encode())
+        if not p:
+            raise IOError(f"cannot read EAM potential {name} from {potdir}")
+        return p
+
+    def cheby(self, pot, n=32):
+        return self.lib.orc_cheb_make(pot, n)
+
+    def lj(self, sigma, epsilon, cutoff, mass):
+        return self.lib.orc_lj_make(sigma, epsilon, cutoff, mass)
+
+    def fcc(self, nx, ny, nz, lat, defgrad, bf, pot):
+        st = C.c_int(0)
+        s = self.lib.orc_fcc(nx, ny, nz, lat, defgrad, bf, C.cast(pot, C.c_void_p),
+                             C.byref(st))
+        if not s:
+            raise RuntimeError(f"orc_fcc failed with code {st.value}")
+        return s
+
+    def clone(self, s):
+        return self.lib.orc_sim_clone(s)
+
+    def free(self, s):
+        self.lib.orc_sim_free(s)
+
+    def rebox(self, s):
+        return self.lib.orc_rebox_all(s)
+
+    def force(self, s, kind):
+        return self.lib.orc_force(s, kind)
+
+    def steps(self, s, n, dt, kind):
+        return self.lib.orc_ntimesteps(n, s, dt, kind)
+
+    def seed(self, s, seed, kind, amp, temp_k, mass_amu):
+        self.lib.orc_seed_apply(s, seed, kind, amp, temp_k, mass_amu)
+
+    def set_periodic(self, p):
+        self.lib.orc_set_periodic(int(p))
+
+
+class RefLib:
+    """The reference src-flat compiled from its sources (FP64)."""
+
+    def __init__(self, cheby=False):
+        name = "libcomdref_cheby.so" if cheby else "libcomdref_table.so"
+        path = os.path.join(HERE, "_ref", name)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        lib = C.CDLL(path)
+        lib.refh_eam_load.restype = C.c_void_p
+        lib.refh_eam_load.argtypes = [C.c_char_p, C.c_char_p]
+        lib.refh_lj_make.restype = C.c_void_p
+        lib.refh_lj_make.argtypes = [C.c_double] * 4
+        lib.refh_fcc.restype = P_SIM
+        lib.refh_fcc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                 C.c_double, C.c_void_p, C.c_int]
+        lib.refh_seed_apply.argtypes = [P_SIM, C.c_uint64, C.c_int, C.c_double, C.c_double,
+                                        C.c_double]
+        lib.refh_rebox.argtypes = [P_SIM]
+        lib.refh_force.argtypes = [P_SIM]
+        lib.refh_ntimesteps.restype = C.c_double
+        lib.refh_ntimesteps.argtypes = [C.c_int, P_SIM, C.c_double]
+        lib.refh_set_periodic.argtypes = [C.c_int]
+        self.lib = lib
+        self.cheby = cheby
+
+
+def ref_lib(cheby=False):
+    """RefLib or None when oracle/_ref was not built on this machine."""
+    key = bool(cheby)
+    with _lock:
+        if key not in _refs:
+            try:
+                _refs[key] = RefLib(cheby)
+            except (FileNotFoundError, OSError):
+                _refs[key] = None
+        return _refs[key]

@@ -1,0 +1,303 @@
+"""GPU parity: the library's CUDA path against the CPU oracle on the same
+seeded inputs (all calls go through the C ABI of libcomdgb.so).
+
+Tolerances: the FP64 kernels differ from the oracle only in the order of the
+per-atom sums, so forces agree to 1e-11 of the largest component and energy
+to 1e-12 relative.  Integer work (box occupancy, slot order, ids) and the
+FP64 integrator are bit-exact.  Mixed precision must stay within the
+1e-5 relative RMS force error of the specification.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import comd_gb300 as cg
+from comd_gb300.abi import by_id, slot_views
+from helpers import Case, compare_forces, layout_equal, rel_rms, slots_equal
+
+pytestmark = pytest.mark.gpu
+
+FP64_F_TOL = 1e-11
+FP64_E_TOL = 1e-12
+MIXED_F_RMS_TOL = 1e-5
+
+
+def _force_case(oracle, potential, precision, **kw):
+    c = Case(oracle, potential, **kw)
+    try:
+        c.oracle_force()
+        d = c.device(precision)
+        e, stress = d.force()
+        d.download(c.s)
+        d.close()
+        cmp = compare_forces(c.s, c.o)
+        eo, so = c.o.contents.e, c.o.contents.stress
+        return cmp, (e, stress), (eo, so), c.s.contents.ntot
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("potential", [cg.POT_EAM_TABLE, cg.POT_EAM_CHEBY])
+def test_eam_force_fp64(oracle, potential):
+    cmp, (e, st), (eo, so), _ = _force_case(oracle, potential, cg.PREC_FP64)
+    assert cmp["f_max_rel"] < FP64_F_TOL, cmp
+    assert cmp["e_max_rel"] < FP64_F_TOL, cmp
+    assert cmp["rho_max_rel"] < FP64_E_TOL, cmp
+    assert cmp["fi_max_rel"] < FP64_E_TOL, cmp
+    assert abs(e - eo) <= FP64_E_TOL * abs(eo)
+    assert abs(st - so) <= 1e-10 * abs(so)
+
+
+def test_lj_force_fp64(oracle):
+    cmp, (e, st), (eo, so), _ = _force_case(oracle, cg.POT_LJ, cg.PREC_FP64, n=(8, 8, 8),
+                                            disp=cg.DISP_UNIFORM, amp=0.01 * 2.315, temp=300.0)
+    assert cmp["f_max_rel"] < FP64_F_TOL, cmp
+    assert cmp["e_max_rel"] < FP64_F_TOL, cmp
+    assert abs(e - eo) <= FP64_E_TOL * abs(eo)
+    assert abs(st - so) <= 1e-10 * abs(so)
+
+
+@pytest.mark.parametrize("n", [(3, 3, 3), (2, 2, 2), (2, 5, 4)])
+def test_eam_force_small_grids(oracle, n):
+    """nbx < 3 (duplicate stencil entries) and a single box, as the reference."""
+    cmp, (e, st), (eo, so), _ = _force_case(oracle, cg.POT_EAM_TABLE, cg.PREC_FP64, n=n)
+    assert cmp["f_max_rel"] < FP64_F_TOL, cmp
+    assert abs(e - eo) <= FP64_E_TOL * abs(eo)
+
+
+def test_eam_force_nonperiodic(oracle):
+    cmp, (e, st), (eo, so), _ = _force_case(oracle, cg.POT_EAM_TABLE, cg.PREC_FP64,
+                                            periodic=False)
+    assert cmp["f_max_rel"] < FP64_F_TOL, cmp
+    assert abs(e - eo) <= FP64_E_TOL * abs(eo)
+
+
+def test_eam_force_stretched_boxfactor(oracle):
+    cmp, (e, st), (eo, so), _ = _force_case(oracle, cg.POT_EAM_CHEBY, cg.PREC_FP64,
+                                            n=(10, 10, 10), defgrad=1.05, bf=1.5, temp=300.0,
+                                            amp=0.0, disp=cg.DISP_NONE)
+    assert cmp["f_max_rel"] < FP64_F_TOL, cmp
+    assert abs(e - eo) <= FP64_E_TOL * abs(eo)
+
+
+@pytest.mark.parametrize("potential", [cg.POT_EAM_TABLE, cg.POT_EAM_CHEBY])
+def test_eam_force_mixed(oracle, potential):
+    cmp, (e, st), (eo, so), ntot = _force_case(oracle, potential, cg.PREC_MIXED,
+                                               n=(10, 10, 10), defgrad=1.05, bf=1.5,
+                                               temp=300.0, amp=0.05)
+    assert cmp["f_rel_rms"] < MIXED_F_RMS_TOL, cmp
+    assert abs(e - eo) / ntot < 1e-7, (e, eo)
+
+
+def test_lj_force_mixed(oracle):
+    cmp, (e, st), (eo, so), ntot = _force_case(oracle, cg.POT_LJ, cg.PREC_MIXED, n=(8, 8, 8),
+                                               disp=cg.DISP_UNIFORM, amp=0.01 * 2.315)
+    assert cmp["f_rel_rms"] < MIXED_F_RMS_TOL, cmp
+    assert abs(e - eo) / ntot < 1e-7, (e, eo)
+
+
+def test_rebox_bitexact(oracle):
+    """GPU reBoxAll reproduces occupancy, slot order and every moved field."""
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(8, 8, 8), disp=cg.DISP_NONE, amp=0.0)
+    try:
+        v = slot_views(c.s)
+        rng = np.random.default_rng(5)
+        v["r"][:] += rng.uniform(-0.9, 0.9, size=v["r"].shape)
+        v["f"][:] = rng.normal(size=v["f"].shape)
+        v["rho"][:] = rng.normal(size=v["rho"].shape)
+        o2 = c.oracle.clone(c.s)
+        assert c.oracle.rebox(o2) == 0
+        d = c.device()
+        d.rebox()
+        d.download(c.s)
+        d.close()
+        assert slots_equal(c.s, o2, ("id", "iType", "mass", "r", "p", "f", "rho", "fi"))
+        c.oracle.free(o2)
+    finally:
+        c.close()
+
+
+def test_rebox_serial_fallback(oracle):
+    """Moves of more than one box per axis replay reBoxAll serially, still exact."""
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(8, 8, 8), disp=cg.DISP_NONE, amp=0.0)
+    try:
+        v = slot_views(c.s)
+        bs = c.s.contents.boxsize[0]
+        nb = c.s.contents.nboxes
+        # atoms of box 0 pushed 2.5 boxes up in x: they arrive at box 1 still out of range
+        v["r"][0:3, 0] += 2.5 * bs
+        v["r"][64 * (nb // 2) + 1, 1] -= 1.7 * c.s.contents.boxsize[1]
+        o2 = c.oracle.clone(c.s)
+        assert c.oracle.rebox(o2) == 0
+        d = c.device()
+        d.rebox()
+        d.download(c.s)
+        d.close()
+        assert slots_equal(c.s, o2)
+        c.oracle.free(o2)
+    finally:
+        c.close()
+
+
+def test_rebox_overflow_reported(oracle):
+    """A box reaching 64 atoms returns the reference's -11 instead of exiting."""
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(8, 8, 8), disp=cg.DISP_NONE, amp=0.0)
+    try:
+        v = slot_views(c.s)
+        nbx = list(c.s.contents.nbx)
+        bs = list(c.s.contents.boxsize)
+
+        def box(ix, iy, iz):
+            return ix + nbx[0] * (iy + nbx[1] * iz)
+
+        # every atom of four face neighbours of box 0 is pushed into box 0
+        for b, axis, target in ((box(1, 0, 0), 0, -0.5), (box(0, 1, 0), 1, -0.5),
+                                (box(0, 0, 1), 2, -0.5), (box(nbx[0] - 1, 0, 0), 0, 1.5)):
+            n = v["natoms"][b]
+            v["r"][64 * b:64 * b + n, axis] = target * bs[axis]
+        assert v["natoms"][[0, box(1, 0, 0), box(0, 1, 0), box(0, 0, 1),
+                            box(nbx[0] - 1, 0, 0)]].sum() >= 64
+        o2 = c.oracle.clone(c.s)
+        assert c.oracle.rebox(o2) == -11
+        d = c.device()
+        with pytest.raises(cg.ComdgbError) as ei:
+            d.rebox()
+        assert ei.value.code == -11
+        d.close()
+        c.oracle.free(o2)
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("potential", [cg.POT_EAM_TABLE, cg.POT_EAM_CHEBY, cg.POT_LJ])
+def test_steps_fp64(oracle, potential):
+    kw = {}
+    if potential == cg.POT_LJ:
+        kw = dict(n=(8, 8, 8), disp=cg.DISP_UNIFORM, amp=0.01 * 2.315, temp=0.0)
+    c = Case(oracle, potential, **kw)
+    try:
+        nsteps = 10
+        d = c.device()
+        e, _ = d.steps(nsteps, 1e-15)
+        d.download(c.s)
+        d.close()
+        assert c.oracle.steps(c.o, nsteps, 1e-15, c.kind) == 0
+        eo = c.o.contents.e
+        assert abs(e - eo) <= 1e-10 * abs(eo), (e, eo)
+        assert layout_equal(c.s, c.o)
+        rg, ro = by_id(c.s, "r"), by_id(c.o, "r")
+        assert np.max(np.abs(rg - ro)) < 1e-9
+        pg, po = by_id(c.s, "p"), by_id(c.o, "p")
+        assert rel_rms(pg, po) < 1e-8
+    finally:
+        c.close()
+
+
+def test_mixed_energy_drift(oracle):
+    """Mixed-precision EAM (Chebyshev) conserves H to 1e-4 eV/atom over 1000 steps."""
+    c = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), temp=600.0, amp=0.05)
+    try:
+        d = c.device(cg.PREC_MIXED)
+        n = c.s.contents.ntot
+        e0, _ = d.force()
+        h0 = e0 + d.kinetic()
+        hs = []
+        for _ in range(10):
+            e, _ = d.steps(100, 1e-15)
+            hs.append(e + d.kinetic())
+        d.close()
+        drift = max(abs(h - h0) for h in hs) / n
+        assert drift < 1e-4 * cg.lib.EV_TO_HA, drift
+    finally:
+        c.close()
+
+
+def test_cheb_fit_on_gpu(oracle, pots_dir):
+    L = cg.load()
+    pot = cg.eam_potential("cu")
+    cg_cheb = L.comdgb_cheb_make(pot.ptr, 32, 0)
+    assert cg_cheb
+    ref = oracle.cheby(oracle.eam(pots_dir, "cu"), 32)
+    for name in ("phi", "rho", "f", "dphi", "drho", "df"):
+        a = getattr(cg_cheb.contents, name).contents
+        b = getattr(ref.contents, name).contents
+        va = np.ctypeslib.as_array(a.values, (32,))
+        vb = np.ctypeslib.as_array(b.values, (32,))
+        assert a.x0 == b.x0 and a.xn == b.xn
+        assert np.max(np.abs(va - vb)) <= 1e-12 * np.max(np.abs(vb)), name
+    L.comdgb_cheb_free(cg_cheb)
+
+
+def test_gpu_fitted_cheby_force(oracle):
+    """EAM Chebyshev with the series fitted on the GPU instead of the host."""
+    c = Case(oracle, cg.POT_EAM_CHEBY)
+    try:
+        c.oracle_force()
+        d = c.device(cg.PREC_FP64, cheby_from_host=False)
+        e, _ = d.force()
+        d.download(c.s)
+        d.close()
+        cmp = compare_forces(c.s, c.o)
+        assert cmp["f_max_rel"] < 1e-10, cmp
+        assert abs(e - c.o.contents.e) <= 1e-11 * abs(c.o.contents.e)
+    finally:
+        c.close()
+
+
+def test_put_atoms_bitexact(oracle):
+    """Device counting-sort binning equals n sequential putAtomInBox calls."""
+    L = cg.load()
+    pot = cg.eam_potential("cu")
+    s = cg.fcc(6, 6, 6, 3.615, 1.0, 1.0, pot)
+    v = slot_views(s)
+    m = v["natoms"].sum()
+    rng = np.random.default_rng(3)
+    # world coordinates of the lattice atoms, shuffled ids, some outside [0, L)
+    dc = v["dcenter"]
+    occ = np.arange(64)[None, :] < v["natoms"][:, None]
+    boxes = np.nonzero(occ)[0]
+    xyz = v["r"][occ.reshape(-1)] + dc[boxes]
+    xyz += rng.normal(scale=0.2, size=xyz.shape)
+    order = rng.permutation(m)
+    xyz = np.ascontiguousarray(xyz[order])
+    pxyz = np.ascontiguousarray(rng.normal(size=xyz.shape))
+    ids = np.ascontiguousarray(np.arange(m, dtype=np.int32)[::-1])
+    types = np.ones(m, dtype=np.int32)
+    masses = np.full(m, 63.55)
+    o2 = oracle.clone(s)
+    # empty both
+    for sim in (s, o2):
+        vv = slot_views(sim)
+        vv["natoms"][:] = 0
+        sim.contents.ntot = 0
+    for t in range(m):
+        assert oracle.lib.orc_put_atom(o2, int(ids[t]), 1, 63.55, *xyz[t], *pxyz[t]) == 0
+    rc = L.comdgb_put_atoms(s, m, xyz.ctypes.data, pxyz.ctypes.data, ids.ctypes.data,
+                            types.ctypes.data, masses.ctypes.data, 0)
+    assert rc == 0, cg.lib.last_error()
+    assert s.contents.ntot == m
+    assert slots_equal(s, o2)
+    cg.free_host(s)
+    oracle.free(o2)
+
+
+def test_dropin_force_and_steps(oracle):
+    """attach + pot->force = comdgb_force + comdgb_nTimeSteps on a host simflat_t."""
+    L = cg.load()
+    c = Case(oracle, cg.POT_EAM_CHEBY)
+    try:
+        o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, cheby_from_host=True)
+        assert L.comdgb_attach(c.s, C.byref(o)) == 0, cg.lib.last_error()
+        assert L.comdgb_force(C.cast(c.s, C.c_void_p)) == 0
+        c.oracle_force()
+        cmp = compare_forces(c.s, c.o)
+        assert cmp["f_max_rel"] < FP64_F_TOL
+        assert abs(c.s.contents.e - c.o.contents.e) <= FP64_E_TOL * abs(c.o.contents.e)
+        e = L.comdgb_nTimeSteps(5, c.s, 1e-15)
+        assert c.oracle.steps(c.o, 5, 1e-15, c.kind) == 0
+        assert abs(e - c.o.contents.e) <= 1e-10 * abs(c.o.contents.e)
+        assert layout_equal(c.s, c.o)
+        assert L.comdgb_detach(c.s) == 0
+    finally:
+        c.close()
