@@ -1,0 +1,468 @@
+#!/usr/bin/env python3
+"""Benchmark of CoMD's force-and-integrate step on GB300.
+
+Metric: EAM atom-steps/s at 4M atoms on one GB300, mixed precision (FP32
+pair terms, compensated per-atom sums, FP64 integration) against the plain
+FP64 GPU kernel, with the force error of mixed vs FP64 stated.
+
+Workload (the configuration the metric is quoted on): EAM Cu, Chebyshev
+series (32 terms, fitted in FP64 on the GPU from the bundled Cu tables),
+FCC 100x100x100 unit cells = 4,000,000 atoms, x-stretch (deformation
+gradient) 1.05, box factor 1.5, seeded Maxwell-Boltzmann momenta at 300 K,
+dt = 1 fs.  One step = one velocity-Verlet timestep of the reference's
+nTimeSteps (advance positions dt/2, reBoxAll, force, advance momenta dt,
+advance positions dt/2, reBoxAll).  Inputs are synthetic and seeded.
+
+value: device-resident throughput, CUDA events over K graph replays.
+e2e:   the same metric through the drop-in C ABI (comdgb_attach +
+       comdgb_nTimeSteps(10) on a host simflat_t), host<->device copies of
+       the whole simulation inside every call.
+--impl reference: the reference's CPU path (oracle/_ref when it was built
+from the reference sources on this machine, else the CPU oracle port)
+with every host thread, each on an independent periodic sample.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = {"name": "eam_cu_chebyshev_fcc100_stretch1.05_bf1.5_300K", "nx": 100, "ny": 100,
+            "nz": 100, "defgrad": 1.05, "bf": 1.5, "temp_k": 300.0, "seed": 2026, "dt_s": 1e-15}
+METRIC = "EAM atom-steps/s @4M atoms, 1 GB300: mixed vs FP64 at <=1e-5 force err"
+UNIT = "atom-steps/s"
+# algorithmic work (counted per unique in-cutoff pair / per atom; FMA = 2)
+FLOPS_PASS1_PER_PAIR = 443    # phi, phi', rho by Clenshaw (+ r, dr)
+FLOPS_PASS2_PER_PAIR = 132    # rho' by Clenshaw + embedding force
+FLOPS_EMBED_PER_ATOM = 208    # F, F' per atom (fused into pass 1)
+BYTES_VERLET_PER_ATOM = 120   # read r, p, f; write r, p (FP64)
+BYTES_ADVPOS_PER_ATOM = 72    # read r, p; write r (FP64)
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class Dist:
+    """Barrier / max over ranks (gloo on CPU) when launched with N > 1."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def make_host_sim(cg, w, nx=None, ny=None, nz=None, disp=None, amp=0.0):
+    pot = cg.eam_potential("cu")
+    s = cg.fcc(nx or w["nx"], ny or w["ny"], nz or w["nz"], pot.ptr.contents.lat, w["defgrad"],
+               w["bf"], pot)
+    cg.seed(s, w["seed"], disp if disp is not None else cg.DISP_NONE, amp, w["temp_k"],
+            pot.ptr.contents.mass)
+    return pot, s
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def committed_traffic():
+    """per-launch DRAM bytes of the dominant kernel from the committed ncu summary"""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------------ CPU arms
+def _cpu_worker(barrier, queue, cells, steps, w, prefer_reference, index):
+    """One CPU sample in its own process (the reference keeps static state,
+    so samples never share an address space).  stdout is silenced because
+    the reference prints while it sets up."""
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    sys.path.insert(0, ROOT)
+    import oracle
+    ref = oracle.ref_lib(cheby=True) if prefer_reference else None
+    if ref is not None:
+        L = ref.lib
+        potdir = os.path.join(ROOT, "comd_gb300", "pots").encode()
+        rp = L.refh_eam_load(potdir, b"cu")
+        s = L.refh_fcc(cells, cells, cells, 3.615, w["defgrad"], w["bf"], rp, 1)
+        L.refh_seed_apply(s, w["seed"] + index, 0, 0.0, w["temp_k"], 63.55)
+        L.refh_rebox(s)
+
+        def run():
+            L.refh_ntimesteps(steps, s, w["dt_s"])
+        kind = "reference"
+    else:
+        O = oracle.Oracle()
+        pot = O.eam(os.path.join(ROOT, "comd_gb300", "pots"), "cu")
+        s = O.fcc(cells, cells, cells, pot.contents.lat, w["defgrad"], w["bf"], pot)
+        s.contents.ch_pot = O.cheby(pot, 32)
+        O.seed(s, w["seed"] + index, 0, 0.0, w["temp_k"], pot.contents.mass)
+        O.rebox(s)
+
+        def run():
+            O.steps(s, steps, w["dt_s"], oracle.KIND_EAM_CHEBY)
+        kind = "port"
+    natoms = s.contents.ntot
+    barrier.wait()
+    t0 = time.perf_counter()
+    run()
+    queue.put((natoms, time.perf_counter() - t0, kind))
+
+
+def cpu_sample(procs, cells, steps, w, prefer_reference):
+    """`procs` independent periodic samples (cells^3 FCC unit cells with the
+    workload's stretch, box factor and temperature), one spawned process per
+    host core, each running nTimeSteps(steps) of the reference's CPU path
+    concurrently.  Returns (atom-steps/s, kind, description); atom-steps are
+    counted as the reference counts them: N * (steps + 1) force calls."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(procs)
+    queue = ctx.Queue()
+    ps = [ctx.Process(target=_cpu_worker, args=(barrier, queue, cells, steps, w,
+                                                prefer_reference, i)) for i in range(procs)]
+    for p in ps:
+        p.start()
+    res = [queue.get(timeout=1800) for _ in ps]
+    for p in ps:
+        p.join()
+    natoms = res[0][0]
+    wall = max(r[1] for r in res)
+    kind = res[0][2]
+    value = sum(r[0] for r in res) * (steps + 1) / wall
+    desc = (f"{procs} concurrent processes, each an independent periodic sample of {natoms} "
+            f"atoms ({cells}^3 FCC cells, stretch {w['defgrad']}, box factor {w['bf']}, "
+            f"{w['temp_k']} K momenta), nTimeSteps({steps}) of EAM Chebyshev FP64; "
+            f"slowest sample {wall:.1f} s")
+    return value, kind, desc
+
+
+def cpu_threads():
+    return max(1, min(os.cpu_count() or 1, 72))
+
+
+def reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    threads = cpu_threads()
+    w = WORKLOAD
+    # each step: one nTimeSteps(1) per thread on an independent sample; the
+    # sample is sized so the whole run stays within a few minutes
+    total_steps = args.steps + args.warmup
+    per_step_s = min(12.0, 150.0 / max(total_steps, 1))
+    cells = int(round((per_step_s / 2 / 25e-6 / 4) ** (1 / 3)))
+    cells = max(8, min(cells, 40))
+    for _ in range(args.warmup):
+        cpu_sample(threads, cells, 1, w, True)
+    vals = []
+    kind = desc = None
+    for _ in range(args.steps):
+        v, kind, desc = cpu_sample(threads, cells, 1, w, True)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded FCC Cu lattice, 300 K momenta)",
+            "config": {"workload": w["name"], "atoms": 4_000_000, "potential": "EAM Cu Chebyshev",
+                       "sample": desc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                             "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+def gpu_arm(args):
+    import comd_gb300 as cg
+    from comd_gb300.abi import slot_views, occupied_mask
+
+    rank, world, local = env_rank()
+    dist = Dist(world)
+    dev = local
+    w = WORKLOAD
+    cg.load()
+    pot, s = make_host_sim(cg, w)
+    rc = cg.load().comdgb_rebox_host(s, 1, dev)  # initSimFromCmdLine's reBoxAll
+    if rc:
+        raise cg.ComdgbError(rc, cg.lib.last_error())
+    natoms = s.contents.ntot
+    dt = w["dt_s"]
+
+    mixed = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, device=dev,
+                                    cheby_from_host=False))
+    h0_e, _ = mixed.force()
+    h0 = h0_e + mixed.kinetic()
+    mixed.steps(args.warmup, dt)
+    mixed.synchronize()
+    per_step_kernels, _ = mixed.graph_kernels()
+
+    clocks = ClockSampler(dev)
+    clocks.start()
+    dist.barrier()
+    mixed.synchronize()
+    step_ms, span_ms, kern_ms = mixed.timed_steps(args.steps, dt)
+    mixed.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    elapsed_s = dist.max(span_ms / 1e3)
+    value = dist.sum(natoms * args.steps) / elapsed_s
+    pairs = mixed.pair_count()
+
+    # energy drift over 1000 steps (warmup + timed + the rest, untimed)
+    done = args.warmup + args.steps
+    drift = None
+    if args.drift_steps > done:
+        mixed.steps(args.drift_steps - done, dt)
+        e1, _ = mixed.force()
+        drift = abs(e1 + mixed.kinetic() - h0) / natoms
+
+    # force error of mixed vs the FP64 kernel on the same (thermalised) state
+    mixed.download(s)
+    f_mixed = slot_views(s)["f"][occupied_mask(s)][:, :3].copy()
+    fp64_value = fp64_ms = None
+    ferr = None
+    if not args.no_fp64:
+        fp64 = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, device=dev,
+                                       cheby_from_host=False))
+        fp64.force()
+        fp64.download(s)
+        f64 = slot_views(s)["f"][occupied_mask(s)][:, :3].copy()
+        ferr = float(np.sqrt(np.mean((f_mixed - f64) ** 2)) / np.sqrt(np.mean(f64 ** 2)))
+        fp64.steps(1, dt)
+        fp64.synchronize()
+        st64, span64, _ = fp64.timed_steps(args.fp64_steps, dt)
+        fp64_ms = span64 / args.fp64_steps
+        fp64_value = natoms / (fp64_ms / 1e3)
+        fp64.close()
+
+    # e2e through the drop-in C ABI on the host simflat_t
+    e2e = None
+    if not args.no_e2e:
+        import ctypes as C
+        L = cg.load()
+        o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, device=dev, cheby_from_host=False)
+        cg.lib.check(L.comdgb_attach(s, C.byref(o)))
+        calls, per_call = args.e2e_calls, 10
+        L.comdgb_nTimeSteps(per_call, s, dt)  # warm-up: graph capture, pinning
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            e = L.comdgb_nTimeSteps(per_call, s, dt)
+            if e != e:
+                raise cg.ComdgbError(-30, cg.lib.last_error())
+        t1 = time.perf_counter()
+        dist.barrier()
+        e2e_s = dist.max(t1 - t0)
+        L.comdgb_detach(s)
+        ns = s.contents.nboxes * 64
+        nb = s.contents.nboxes
+        # bytes copied per call: natoms, id, iType, mass, r, p, f, rho, fi
+        h2d = nb * 4 + ns * (4 + 4 + 8 + 24 + 24 + 32 + 8 + 8)
+        d2h = h2d
+        e2e = {"value": dist.sum(natoms * calls * per_call) / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": h2d // per_call, "d2h_bytes_per_step": d2h // per_call,
+               "call": f"comdgb_nTimeSteps({per_call}) on a host simflat_t (pinned), "
+                       "full state copied up and back every call"}
+
+    # roofline of the dominant kernel group
+    peaks = measured_peaks()
+    fp32_peak = cg.lib.fp32_peak_tflops(dev)
+    dom = max(kern_ms, key=kern_ms.get)
+    groups = {}
+    for name, ms in kern_ms.items():
+        g = {"ms": ms, "share": ms / sum(kern_ms.values())}
+        if name == "force_pass1":
+            fl = FLOPS_PASS1_PER_PAIR * pairs + FLOPS_EMBED_PER_ATOM * natoms
+            g.update(bound="fp32", achieved=fl / (ms / 1e3) / 1e12, unit="TFLOP/s")
+        elif name == "force_pass2":
+            fl = FLOPS_PASS2_PER_PAIR * pairs
+            g.update(bound="fp32", achieved=fl / (ms / 1e3) / 1e12, unit="TFLOP/s")
+        elif name.startswith("advance_velocity"):
+            g.update(bound="hbm", achieved=BYTES_VERLET_PER_ATOM * natoms / (ms / 1e3) / 1e9,
+                     unit="GB/s")
+        elif name.startswith("advance_positions"):
+            g.update(bound="hbm", achieved=BYTES_ADVPOS_PER_ATOM * natoms / (ms / 1e3) / 1e9,
+                     unit="GB/s")
+        if "bound" in g:
+            pk = fp32_peak if g["bound"] == "fp32" else peaks.get("hbm_gbs", 6800.0)
+            g["peak"] = pk
+            g["frac"] = g["achieved"] / pk
+        groups[name] = g
+    dg = groups[dom]
+    traffic = committed_traffic().get(dom)
+    roofline = {"kernel": dom, "bound": dg.get("bound"), "achieved": dg.get("achieved"),
+                "peak": dg.get("peak"), "unit": dg.get("unit"), "frac": dg.get("frac"),
+                "traffic": traffic,
+                "peak_source": ("FP32 FMA throughput measured on this GPU by "
+                                "comdgb_fp32_fma_peak (no FP32 figure in MEASURED_PEAKS.json)"
+                                if dg.get("bound") == "fp32" else "MEASURED_PEAKS.json hbm_gbs"),
+                "algorithmic": f"{FLOPS_PASS1_PER_PAIR} flops/unique pair + "
+                               f"{FLOPS_EMBED_PER_ATOM}/atom, {pairs} pairs"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, kind, desc = cpu_sample(cpu_threads(), args.cpu_cells, 1, w, True)
+        cpu = {"value": v, "unit": UNIT, "cores": cpu_threads(), "kind": kind, "sample": desc}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_s * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded FCC Cu lattice, 300 K momenta)",
+        "config": {"workload": w["name"], "atoms": natoms, "potential": "EAM Cu Chebyshev 32",
+                   "precision": "mixed (FP32 pairs, Kahan FP32 sums, FP64 integration)",
+                   "boxes": s.contents.nboxes, "nbx": list(s.contents.nbx),
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (~1.1 GB device state per step)",
+                   "dt_fs": 1.0},
+        "fp64_gpu": {"value": fp64_value, "ms_per_step": fp64_ms, "steps": args.fp64_steps},
+        "mixed_vs_fp64": (value / world / fp64_value) if fp64_value else None,
+        "force_rel_rms_mixed_vs_fp64": ferr,
+        "energy_drift_ha_per_atom": drift, "drift_steps": args.drift_steps,
+        "pairs_per_step": pairs, "pair_evals_per_s": pairs * args.steps / (span_ms / 1e3),
+        "kernel_groups": groups, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": per_step_kernels * args.steps, "clocks": clk,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    mixed.close()
+    cg.free_host(s)
+    dist.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--drift-steps", type=int, default=1000)
+    ap.add_argument("--e2e-calls", type=int, default=3)
+    ap.add_argument("--cpu-cells", type=int, default=30)
+    ap.add_argument("--cells", type=int, default=0,
+                    help="override the lattice to N^3 unit cells (profiling captures only)")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.cells:
+        WORKLOAD.update(nx=args.cells, ny=args.cells, nz=args.cells,
+                        name=WORKLOAD["name"].replace("fcc100", f"fcc{args.cells}"))
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gpu_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

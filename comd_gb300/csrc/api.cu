@@ -115,6 +115,7 @@ struct comdgb_sim {
   double timed_dt = NAN;
   std::vector<cudaGraphNode_t> timed_nodes;  // event record nodes, group order
   std::vector<cudaEvent_t> timed_cap_events;
+  int step_kernels = 0, force_kernels = 0;  // kernel nodes per captured graph
   // host last results
   double e = 0.0, stress = 0.0;
   simflat_t *host = nullptr;   // drop-in owner (attach)
@@ -200,25 +201,85 @@ Table<T> upload_table(comdgb_sim *h, const potentialarray_t *a, int *err) {
   t.xn = (T)a->xn;
   t.invDx = (T)a->invDx;
   t.n = n;
+  t.seg = nullptr;
+  if (sizeof(T) == 4) {
+    // per-interval coefficients of eamInterpolateDeriv (eam.c:422-431) in FP64
+    const double *w = a->values;
+    std::vector<float4> seg(2 * (size_t)n);
+    for (int i = 0; i < n; i++) {
+      double gi = w[i + 1] - w[i - 1], gi1 = w[i + 2] - w[i];
+      double c1 = 0.5 * gi, c2 = 0.5 * (w[i + 1] + w[i - 1] - 2.0 * w[i]);
+      double d0 = i <= 0 ? 0.0 : 0.5 * gi * a->invDx;
+      double d1 = i <= 0 ? 0.0 : 0.5 * (gi1 - gi) * a->invDx;
+      seg[2 * i] = make_float4((float)w[i], (float)c1, (float)c2, (float)d0);
+      seg[2 * i + 1] = make_float4((float)d1, 0.f, 0.f, 0.f);
+    }
+    float4 *ds = track(h, dalloc<float4>(2 * (size_t)n, err));
+    if (*err) return t;
+    cudaMemcpy(ds, seg.data(), sizeof(float4) * 2 * n, cudaMemcpyHostToDevice);
+    t.seg = ds;
+  }
   return t;
 }
 
-// series order: 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF
-void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, const double coef[6][CG_NCHEB],
-               const double a[6], const double b[6]) {
+// eamCheb (cheby.c:276-310) on the host, FP64
+double cheb_host(const double *c, double a, double b, double x) {
+  if (x < a) x = a;
+  double d = 0.0, dd = 0.0, y = (2.0 * x - a - b) / (b - a), y2 = 2.0 * y;
+  for (int j = CG_NCHEB - 1; j > 0; j--) {
+    double sv = d;
+    d = y2 * d - dd + c[j];
+    dd = sv;
+  }
+  return y * d - dd + 0.5 * c[0];
+}
+
+// The degree-31 polynomial of series c on [a, b] written in the Chebyshev
+// basis of [lo, b]: sampled at the 32 Chebyshev nodes of [lo, b] (exact for
+// a degree-31 polynomial) and transformed back.  Identical function to
+// ~1e-14 relative; in FP32 its Clenshaw sum no longer cancels the large
+// coefficients that the repulsive core near a puts into the series.
+void cheb_reexpand(const double *c, double a, double b, double lo, double *out) {
+  const double PI = 3.141592653589793;
+  double fk[CG_NCHEB];
+  for (int k = 0; k < CG_NCHEB; k++) {
+    double y = cos(PI * (k + 0.5) / CG_NCHEB);
+    fk[k] = cheb_host(c, a, b, y * 0.5 * (b - lo) + 0.5 * (b + lo));
+  }
+  for (int j = 0; j < CG_NCHEB; j++) {
+    double sum = 0.0;
+    for (int k = 0; k < CG_NCHEB; k++) sum += fk[k] * cos(PI * j * (k + 0.5) / CG_NCHEB);
+    out[j] = 2.0 / CG_NCHEB * sum;
+  }
+}
+
+// series order: 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF.  pair_lo: lower end
+// of the re-expansion interval of the pair series (FP32 path)
+void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
+               const double coef[6][CG_NCHEB], const double a[6], const double b[6],
+               double pair_lo) {
   for (int s = 0; s < 6; s++) {
     for (int j = 0; j < CG_NCHEB; j++) {
       c64.c[s][j] = coef[s][j];
-      c32.c[s][j] = (float)coef[s][j];
+      lo32.c[s][j] = (float)coef[s][j];
     }
     c64.a[s] = a[s];
     c64.b[s] = b[s];
     c64.ys[s] = 2.0 / (b[s] - a[s]);
     c64.yo[s] = -(a[s] + b[s]) / (b[s] - a[s]);
-    c32.a[s] = (float)a[s];
+    lo32.a[s] = (float)a[s];
+    lo32.ys[s] = (float)c64.ys[s];
+    lo32.yo[s] = (float)c64.yo[s];
+    bool pair = (s == 0 || s == 1 || s == 3 || s == 4);
+    double lo = (pair && pair_lo > a[s] && pair_lo < b[s]) ? pair_lo : a[s];
+    double re[CG_NCHEB];
+    if (lo > a[s]) cheb_reexpand(coef[s], a[s], b[s], lo, re);
+    for (int j = 0; j < CG_NCHEB; j++) c32.c[s][j] = (float)(lo > a[s] ? re[j] : coef[s][j]);
+    c32.a[s] = (float)lo;
     c32.b[s] = (float)b[s];
-    c32.ys[s] = (float)c64.ys[s];
-    c32.yo[s] = (float)c64.yo[s];
+    c32.ys[s] = (float)(2.0 / (b[s] - lo));
+    c32.yo[s] = (float)(-(lo + b[s]) / (b[s] - lo));
+    lo32.lo[s] = lo > a[s] ? (float)lo : -3.0e38f;
   }
 }
 
@@ -305,7 +366,10 @@ int setup_potential(comdgb_sim *h, const simflat_t *s) {
     int rc = fit_cheb_gpu(h, ep, coef, a, b);
     if (rc) return rc;
   }
-  fill_cheb(h->eam64c.ch, h->eam32c.ch, coef, a, b);
+  // pair distances below 0.75 of the nearest-neighbour distance of the
+  // potential's lattice take the reference coefficients (never in practice)
+  double pair_lo = ep->lat > 0 ? 0.75 * ep->lat / sqrt(2.0) : 0.0;
+  fill_cheb(h->eam64c.ch, h->eam32c.ch, h->eam32c.chlo, coef, a, b, pair_lo);
   h->eam64c.rc2 = rc2;
   h->eam32c.rc2 = (float)rc2;
   return 0;
@@ -405,6 +469,19 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev) {
   if (ev) cudaEventRecord(ev[evi++], st);
 }
 
+int count_kernel_nodes(cudaGraph_t graph) {
+  size_t nn = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nn) != cudaSuccess) return -1;
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (cudaGraphGetNodes(graph, nodes.data(), &nn) != cudaSuccess) return -1;
+  int k = 0;
+  for (cudaGraphNode_t nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+  }
+  return k;
+}
+
 int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool force) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -415,6 +492,8 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool
     enqueue_reduce(h);
   }
   CK(cudaStreamEndCapture(h->stream, &graph));
+  if (step) h->step_kernels = count_kernel_nodes(graph);
+  if (force) h->force_kernels = count_kernel_nodes(graph);
   if (*exec) cudaGraphExecDestroy(*exec);
   cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
   cudaGraphDestroy(graph);
@@ -557,7 +636,7 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   h->et.n = track(h, dalloc<int>(nb, &err));
   h->et.box = track(h, dalloc<int>(nb * CG_NNBR, &err));
   h->et.dr64 = track(h, dalloc<d4>(nb * CG_NNBR, &err));
-  h->et.dr32 = track(h, dalloc<float4>(nb * CG_NNBR, &err));
+  h->et.dr32 = track(h, dalloc<float4>(2 * nb * CG_NNBR, &err));
   h->dcenter = track(h, dalloc<double>(nb * 3, &err));
   h->box_start = track(h, dalloc<int>(nb + 1, &err));
   h->atom_slot = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
@@ -633,6 +712,21 @@ void unpin_host(comdgb_sim *h, simflat_t *s) {
 
 }  // namespace
 
+// FP32 FMA throughput probe: 8 independent FMA chains per thread
+__global__ void fma_probe_kernel(float *out, int iters, float a, float b) {
+  float x[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) x[q] = threadIdx.x * 1e-3f + q;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = fmaf(x[q], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int q = 0; q < 8; q++) s += x[q];
+  if (s == 1.2345f) out[0] = s;  // keeps the chains live; practically never stores
+}
+
 // ============================================================================
 // exported C ABI
 // ============================================================================
@@ -645,6 +739,36 @@ void comdgb_default_opts(comdgb_opts *o) {
   o->device = 0;
   o->n_cheby = CG_NCHEB;
   o->cheby_from_host = 0;
+}
+
+int comdgb_fp32_fma_peak(int device, double *tflops) {
+  if (!tflops) return set_err(COMDGB_ERR_ARG, "null argument");
+  CK(cudaSetDevice(device));
+  int nsm = 0;
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device));
+  float *out = nullptr;
+  CK(cudaMalloc(&out, sizeof(float)));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int threads = 512, blocks = nsm * 4, iters = 4096;
+  double best = 0.0;
+  for (int rep = 0; rep < 4; rep++) {
+    cudaEventRecord(e0);
+    fma_probe_kernel<<<blocks, threads>>>(out, iters, 0.9999f, 1e-6f);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    double flops = 2.0 * 8.0 * iters * (double)threads * blocks;
+    if (ms > 0 && rep > 0) best = fmax(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  CK(cudaGetLastError());
+  *tflops = best;
+  return 0;
 }
 
 int comdgb_last_error(char *buf, int len) {
@@ -737,6 +861,13 @@ int comdgb_sim_synchronize(comdgb_sim *h) {
   return 0;
 }
 
+int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  if (per_step) *per_step = h->step_kernels;
+  if (per_force) *per_force = h->force_kernels;
+  return 0;
+}
+
 const char *comdgb_kernel_name(comdgb_sim *h, int k) {
   (void)h;
   if (k < 0 || k >= KG_COUNT) return "";
@@ -790,6 +921,11 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
   }
   CK(cudaStreamSynchronize(h->stream));
   std::vector<double> ksum(KG_COUNT, 0.0);
+  if (step_ms) {
+    float span = 0.f;
+    CK(cudaEventElapsedTime(&span, evs[0], evs[(size_t)(n - 1) * NE + KG_COUNT]));
+    step_ms[n] = span;
+  }
   for (int s = 0; s < n; s++) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, evs[(size_t)s * NE], evs[(size_t)s * NE + KG_COUNT]));

@@ -71,6 +71,10 @@ struct Table {
   const T *v;
   T x0, xn, invDx;
   int n;
+  // FP32 path: per interval i, two float4 (c0, c1, c2, d0) (d1, 0, 0, 0)
+  // computed in FP64 from v[i-1..i+2] so no FP32 differences of nearby table
+  // values are formed: value = c0 + u(c1 + u c2), deriv = d0 + u d1
+  const float4 *seg;
 };
 
 // Chebyshev series of the reference: 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF
@@ -79,6 +83,16 @@ struct Cheb {
   T c[6][CG_NCHEB];
   T a[6], b[6];
   T ys[6], yo[6];  // y = x*ys + yo (FP32 path)
+};
+
+// FP32 path: the pair series (phi, rho, dphi, drho) are the same degree-31
+// polynomials re-expanded in FP64 on the sub-interval [lo, xn] where pair
+// distances occur (Cheb<float> then holds those coefficients); arguments
+// below lo use the reference's own coefficients kept here.
+struct ChebLow32 {
+  float c[6][CG_NCHEB];
+  float a[6], ys[6], yo[6];
+  float lo[6];
 };
 
 __host__ __device__ inline void box_ixyz(const Geom &g, int b, int *ix) {
@@ -137,6 +151,22 @@ __device__ __forceinline__ void table_eval(const Table<T> &a, T r, T &value, T &
   T gi1 = v2 - v0;
   value = v0 + T(0.5) * r * (r * (v1 + vm - T(2.0) * v0) + gi);
   deriv = (i1 <= 0) ? T(0) : T(0.5) * (gi + r * (gi1 - gi)) * a.invDx;
+}
+
+// FP32 table lookup from the per-interval coefficients (same function)
+__device__ __forceinline__ void table_eval(const Table<float> &a, float r, float &value,
+                                           float &deriv) {
+  if (r < a.x0) r = a.x0;
+  else if (r > a.xn) r = a.xn;
+  float t = (r - a.x0) * a.invDx;
+  float fl = floorf(t);
+  int i1 = (int)fl;
+  i1 = i1 < 0 ? 0 : (i1 > a.n - 1 ? a.n - 1 : i1);
+  float u = t - fl;
+  float4 s0 = __ldg(a.seg + 2 * i1);
+  float d1 = __ldg(reinterpret_cast<const float *>(a.seg + 2 * i1 + 1));
+  value = fmaf(u, fmaf(u, s0.z, s0.y), s0.x);
+  deriv = fmaf(u, d1, s0.w);
 }
 
 // eamCheb (cheby.c:276-310) in FP64: Clenshaw, lower clamp only

@@ -40,6 +40,18 @@ struct ForceArgs {
   int *status;
 };
 
+// Box offset of a stencil entry: FP64 value, or FP32 hi + lo parts.
+template <class T>
+struct BoxOff;
+template <>
+struct BoxOff<double> {
+  double x, y, z;
+};
+template <>
+struct BoxOff<float> {
+  float x, y, z, lx, ly, lz;
+};
+
 template <class T>
 struct PrecT;
 
@@ -51,10 +63,9 @@ struct PrecT<double> {
     d4 v = s.r[slot];
     x = v.x; y = v.y; z = v.z;
   }
-  static __device__ __forceinline__ void drbox(const EntryTab &et, int idx, double &x,
-                                               double &y, double &z) {
+  static __device__ __forceinline__ BoxOff<double> drbox(const EntryTab &et, int idx) {
     d4 v = et.dr64[idx];
-    x = v.x; y = v.y; z = v.z;
+    return BoxOff<double>{v.x, v.y, v.z};
   }
   static __device__ __forceinline__ double fi(const Slots &s, int slot) { return s.fi[slot]; }
 };
@@ -67,27 +78,37 @@ struct PrecT<float> {
     float4 v = __ldg(s.pos32 + slot);
     x = v.x; y = v.y; z = v.z;
   }
-  static __device__ __forceinline__ void drbox(const EntryTab &et, int idx, float &x, float &y,
-                                               float &z) {
-    float4 v = __ldg(et.dr32 + idx);
-    x = v.x; y = v.y; z = v.z;
+  static __device__ __forceinline__ BoxOff<float> drbox(const EntryTab &et, int idx) {
+    float4 h = __ldg(et.dr32 + 2 * idx), l = __ldg(et.dr32 + 2 * idx + 1);
+    return BoxOff<float>{h.x, h.y, h.z, l.x, l.y, l.z};
   }
   static __device__ __forceinline__ float fi(const Slots &s, int slot) {
     return __ldg(s.fi32 + slot);
   }
 };
 
-// dr = drbox + r_i - r_j and r2 accumulated in the reference's order
-template <class T>
-__device__ __forceinline__ T pair_r2(T bx, T by, T bz, T xi, T yi, T zi, T xj, T yj, T zj,
-                                     T &dx, T &dy, T &dz) {
-  dx = (bx + xi) - xj;
-  dy = (by + yi) - yj;
-  dz = (bz + zi) - zj;
-  T r2 = dx * dx;
+// FP64: dr = drbox + r_i - r_j and r2 accumulated in the reference's order
+__device__ __forceinline__ double pair_r2(const BoxOff<double> &o, double xi, double yi,
+                                          double zi, double xj, double yj, double zj, double &dx,
+                                          double &dy, double &dz) {
+  dx = (o.x + xi) - xj;
+  dy = (o.y + yi) - yj;
+  dz = (o.z + zi) - zj;
+  double r2 = dx * dx;
   r2 = r2 + dy * dy;
   r2 = r2 + dz * dz;
   return r2;
+}
+
+// FP32: coordinates are relative to the box centre (|x| <= boxsize/2) and
+// the box offset is added as hi + lo, so dr carries only its own rounding
+__device__ __forceinline__ float pair_r2(const BoxOff<float> &o, float xi, float yi, float zi,
+                                         float xj, float yj, float zj, float &dx, float &dy,
+                                         float &dz) {
+  dx = ((xi - xj) + o.x) + o.lx;
+  dy = ((yi - yj) + o.y) + o.ly;
+  dz = ((zi - zj) + o.z) + o.lz;
+  return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
 }
 
 // Visit every stencil candidate of atom (b, i) directly (overflow path).
@@ -97,15 +118,14 @@ __device__ void scan_stencil(const ForceArgs &A, int b, int i, T xi, T yi, T zi,
   int ne = A.et.n[b];
   for (int e = 0; e < ne; e++) {
     int jb = A.et.box[b * CG_NNBR + e];
-    T bx, by, bz;
-    PrecT<T>::drbox(A.et, b * CG_NNBR + e, bx, by, bz);
+    BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
     int nj = A.s.natoms[jb];
     for (int k = 0; k < nj; k++) {
       if (jb == b && k == i) continue;
       int js = jb * CG_MAXATOMS + k;
       T xj, yj, zj, dx, dy, dz;
       PrecT<T>::pos(A.s, js, xj, yj, zj);
-      T r2 = pair_r2(bx, by, bz, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+      T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
       if (r2 > rc2) continue;
       fn(js, dx, dy, dz, r2);
     }
@@ -132,10 +152,10 @@ __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int
         uint32_t code = (w[u >> 1] >> ((u & 1) * 16)) & 0xffffu;
         int e = code >> 6, k = code & 63;
         int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
-        T bx, by, bz, xj, yj, zj, dx, dy, dz;
-        PrecT<T>::drbox(A.et, ebase + e, bx, by, bz);
+        T xj, yj, zj, dx, dy, dz;
+        BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
         PrecT<T>::pos(A.s, js, xj, yj, zj);
-        T r2 = pair_r2(bx, by, bz, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+        T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
         fn(js, dx, dy, dz, r2);
       }
     }
@@ -158,15 +178,13 @@ __global__ void __launch_bounds__(128) nbr_build_kernel(ForceArgs A, T rc2) {
   uint16_t *cc = reinterpret_cast<uint16_t *>(cz + maxc);
   __shared__ int s_box[CG_NNBR];
   __shared__ int s_off[CG_NNBR + 1];
-  __shared__ T s_dr[CG_NNBR][3];
+  __shared__ BoxOff<T> s_dr[CG_NNBR];
 
   const int ne = A.et.n[b];
   if (threadIdx.x < ne) {
     int e = threadIdx.x;
     s_box[e] = A.et.box[b * CG_NNBR + e];
-    T bx, by, bz;
-    PrecT<T>::drbox(A.et, b * CG_NNBR + e, bx, by, bz);
-    s_dr[e][0] = bx; s_dr[e][1] = by; s_dr[e][2] = bz;
+    s_dr[e] = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -208,8 +226,7 @@ __global__ void __launch_bounds__(128) nbr_build_kernel(ForceArgs A, T rc2) {
         code = cc[c];
         int e = code >> 6, k = code & 63;
         T dx, dy, dz;
-        T r2 = pair_r2(s_dr[e][0], s_dr[e][1], s_dr[e][2], xi, yi, zi, cx[c], cy[c], cz[c], dx,
-                       dy, dz);
+        T r2 = pair_r2(s_dr[e], xi, yi, zi, cx[c], cy[c], cz[c], dx, dy, dz);
         hit = (r2 <= rc2) && !(s_box[e] == b && k == i);
       }
       unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -231,23 +248,27 @@ template <class T, int EVAL>
 struct EamPot {
   Table<T> phi, rho, f;
   Cheb<T> ch;
+  ChebLow32 chlo;  // FP32 only
   T rc2;
 };
 
-__device__ __forceinline__ double cheb_series(const Cheb<double> &c, int s, double x) {
-  return cheb_eval64(c.c[s], c.a[s], c.b[s], x);
+template <int EVAL>
+__device__ __forceinline__ double cheb_series(const EamPot<double, EVAL> &P, int s, double x) {
+  return cheb_eval64(P.ch.c[s], P.ch.a[s], P.ch.b[s], x);
 }
-__device__ __forceinline__ float cheb_series(const Cheb<float> &c, int s, float x) {
-  return cheb_eval32(c.c[s], c.a[s], c.ys[s], c.yo[s], x);
+template <int EVAL>
+__device__ __forceinline__ float cheb_series(const EamPot<float, EVAL> &P, int s, float x) {
+  if (x >= P.chlo.lo[s]) return cheb_eval32(P.ch.c[s], P.ch.a[s], P.ch.ys[s], P.ch.yo[s], x);
+  return cheb_eval32(P.chlo.c[s], P.chlo.a[s], P.chlo.ys[s], P.chlo.yo[s], x);
 }
 
 template <class T, int EVAL>
 __device__ __forceinline__ void eam_pair_terms(const EamPot<T, EVAL> &P, T r, T &phi, T &dphi,
                                                T &rho) {
   if (EVAL == EVAL_CHEBY) {
-    phi = cheb_series(P.ch, 0, r);
-    dphi = cheb_series(P.ch, 3, r);
-    rho = cheb_series(P.ch, 1, r);
+    phi = cheb_series(P, 0, r);
+    dphi = cheb_series(P, 3, r);
+    rho = cheb_series(P, 1, r);
   } else {
     T drho;
     table_eval(P.phi, r, phi, dphi);
@@ -258,8 +279,8 @@ __device__ __forceinline__ void eam_pair_terms(const EamPot<T, EVAL> &P, T r, T 
 template <class T, int EVAL>
 __device__ __forceinline__ void eam_embed(const EamPot<T, EVAL> &P, T rho, T &F, T &dF) {
   if (EVAL == EVAL_CHEBY) {
-    F = cheb_series(P.ch, 2, rho);
-    dF = cheb_series(P.ch, 5, rho);
+    F = cheb_series(P, 2, rho);
+    dF = cheb_series(P, 5, rho);
   } else {
     table_eval(P.f, rho, F, dF);
   }
@@ -267,7 +288,7 @@ __device__ __forceinline__ void eam_embed(const EamPot<T, EVAL> &P, T rho, T &F,
 
 template <class T, int EVAL>
 __device__ __forceinline__ T eam_drho(const EamPot<T, EVAL> &P, T r) {
-  if (EVAL == EVAL_CHEBY) return cheb_series(P.ch, 4, r);
+  if (EVAL == EVAL_CHEBY) return cheb_series(P, 4, r);
   T v, d;
   table_eval(P.rho, r, v, d);
   return d;

@@ -23,7 +23,8 @@ __global__ void entry_table_kernel(Geom g, const double *dcenter, EntryTab et) {
   if (g.nboxes == 1) {
     et.box[base] = 0;
     et.dr64[base] = d4{0.0, 0.0, 0.0, 0.0};
-    et.dr32[base] = make_float4(0.f, 0.f, 0.f, 0.f);
+    et.dr32[2 * base] = make_float4(0.f, 0.f, 0.f, 0.f);
+    et.dr32[2 * base + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     et.n[b] = 1;
     return;
   }
@@ -45,7 +46,12 @@ __global__ void entry_table_kernel(Geom g, const double *dcenter, EntryTab et) {
         }
         et.box[base + cnt] = nb;
         et.dr64[base + cnt] = d4{dr[0], dr[1], dr[2], 0.0};
-        et.dr32[base + cnt] = make_float4((float)dr[0], (float)dr[1], (float)dr[2], 0.f);
+        float hi[3];
+        for (int d = 0; d < 3; d++) hi[d] = (float)dr[d];
+        et.dr32[2 * (base + cnt)] = make_float4(hi[0], hi[1], hi[2], 0.f);
+        et.dr32[2 * (base + cnt) + 1] =
+            make_float4((float)(dr[0] - (double)hi[0]), (float)(dr[1] - (double)hi[1]),
+                        (float)(dr[2] - (double)hi[2]), 0.f);
         cnt++;
       }
   for (int e = cnt; e < CG_NNBR; e++) et.box[base + e] = -1;
@@ -75,6 +81,12 @@ void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, cudaS
 // (a move of more than one box per axis, or r+boxsize rounding to boxsize),
 // the plan is invalid and a serial replay of reBoxAll runs instead.
 // ---------------------------------------------------------------------------
+
+// FP32 position relative to the box centre (mixed precision)
+__device__ __forceinline__ float4 centred32(const Geom &g, double x, double y, double z) {
+  return make_float4((float)(x - 0.5 * g.boxsize[0]), (float)(y - 0.5 * g.boxsize[1]),
+                     (float)(z - 0.5 * g.boxsize[2]), 0.f);
+}
 
 __device__ __forceinline__ void copy_record(const Slots &dst, int ds, const Slots &src, int ss,
                                             bool mixed) {
@@ -124,7 +136,7 @@ __device__ __forceinline__ void classify_slot(const Geom &g, const Slots &s, int
       st.f[slot] = s.f[slot];
       st.rho[slot] = s.rho[slot];
       st.fi[slot] = s.fi[slot];
-      if (mixed) st.pos32[slot] = make_float4((float)rn[0], (float)rn[1], (float)rn[2], 0.f);
+      if (mixed) st.pos32[slot] = centred32(g, rn[0], rn[1], rn[2]);
       if (jb > b) {
         // re-examined in jb's scan: must stay there
         int ix2[3], ix3[3];
@@ -170,7 +182,7 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt
       r.y = r.y + dt_r * p.y / rmass;
       r.z = r.z + dt_r * p.z / rmass;
       s.r[slot] = r;
-      if (mixed) s.pos32[slot] = make_float4((float)r.x, (float)r.y, (float)r.z, 0.f);
+      if (mixed) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
     }
   }
   if (classify) classify_slot(g, s, (int)slot, valid, r, mixed, w, status);
@@ -384,7 +396,7 @@ __global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status) {
         continue;
       }
       s.r[off] = d4{rn[0], rn[1], rn[2], 0.0};
-      if (mixed) s.pos32[off] = make_float4((float)rn[0], (float)rn[1], (float)rn[2], 0.f);
+      if (mixed) s.pos32[off] = centred32(g, rn[0], rn[1], rn[2]);
       int nj = s.natoms[jb];
       if (nj >= CG_MAXATOMS - 1) {  // reaching 64 aborts (domains.c:229)
         set_error(status, -11);
@@ -644,7 +656,7 @@ __global__ void pos32_kernel(Geom g, Slots s) {
   long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
   d4 r = s.r[slot];
-  s.pos32[slot] = make_float4((float)r.x, (float)r.y, (float)r.z, 0.f);
+  s.pos32[slot] = centred32(g, r.x, r.y, r.z);
 }
 
 void launch_pos32(const Geom &g, Slots s, cudaStream_t st) {

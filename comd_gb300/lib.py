@@ -67,6 +67,8 @@ def _bind(lib):
     L.comdgb_sim_synchronize.argtypes = [C.c_void_p]
     L.comdgb_sim_timed_steps.argtypes = [C.c_void_p, C.c_int, C.c_double,
                                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
+    L.comdgb_sim_graph_kernels.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.comdgb_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.comdgb_kernel_name.restype = C.c_char_p
     L.comdgb_kernel_name.argtypes = [C.c_void_p, C.c_int]
     L.comdgb_eam_read.restype = C.POINTER(EamPotential)
@@ -101,6 +103,12 @@ def load(build_if_missing=True):
                 raise ImportError(f"libcomdgb.so not built at {LIB_PATH}")
             _lib = _bind(C.CDLL(LIB_PATH))
         return _lib
+
+
+def fp32_peak_tflops(device=0):
+    v = C.c_double()
+    check(load().comdgb_fp32_fma_peak(device, C.byref(v)))
+    return v.value
 
 
 def last_error():
@@ -236,9 +244,15 @@ class DeviceSim:
     def synchronize(self):
         check(self.L.comdgb_sim_synchronize(self.h))
 
+    def graph_kernels(self):
+        a, b = C.c_int(), C.c_int()
+        check(self.L.comdgb_sim_graph_kernels(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def timed_steps(self, n, dt=1e-15, max_kernels=16):
-        step = (C.c_float * n)()
+        """(per-step ms, span ms, {kernel group: mean ms per step})"""
+        step = (C.c_float * (n + 1))()
         kern = (C.c_float * max_kernels)()
         nk = check(self.L.comdgb_sim_timed_steps(self.h, n, dt, step, kern, max_kernels))
         names = [self.L.comdgb_kernel_name(self.h, k).decode() for k in range(nk)]
-        return list(step), dict(zip(names, list(kern)[:nk]))
+        return list(step)[:n], step[n], dict(zip(names, list(kern)[:nk]))

@@ -114,12 +114,18 @@ int comdgb_sim_pair_count(comdgb_sim *h, long long *pairs);
 int comdgb_sim_synchronize(comdgb_sim *h);
 
 /* Timed run for benchmarks: `n` steps (graph replays), events recorded on
- * the library's stream; step_ms[n] gets each step's device time and
- * kernel_ms[n_kernels] the average device time of each kernel of a step
- * (names via comdgb_kernel_name).  Returns the number of kernels per step. */
+ * the library's stream; step_ms[0..n-1] gets each step's device time,
+ * step_ms[n] the span from the first step's start to the last step's end,
+ * and kernel_ms[k] the average device time of kernel group k of a step
+ * (names via comdgb_kernel_name).  Returns the number of groups per step. */
 int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms,
                            float *kernel_ms, int max_kernels);
 const char *comdgb_kernel_name(comdgb_sim *h, int k);
+/* kernels launched per replay of the captured step graph / force graph */
+int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
+/* measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops); the
+ * peak the mixed-precision force kernels are compared against */
+int comdgb_fp32_fma_peak(int device, double *tflops);
 
 /* ---------------- host-side setup (reference setup routines) ---------------- */
 

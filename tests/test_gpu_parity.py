@@ -76,7 +76,7 @@ def test_eam_force_nonperiodic(oracle):
 def test_eam_force_stretched_boxfactor(oracle):
     cmp, (e, st), (eo, so), _ = _force_case(oracle, cg.POT_EAM_CHEBY, cg.PREC_FP64,
                                             n=(10, 10, 10), defgrad=1.05, bf=1.5, temp=300.0,
-                                            amp=0.0, disp=cg.DISP_NONE)
+                                            amp=0.05, disp=cg.DISP_GAUSSIAN)
     assert cmp["f_max_rel"] < FP64_F_TOL, cmp
     assert abs(e - eo) <= FP64_E_TOL * abs(eo)
 
