@@ -83,6 +83,7 @@ struct comdgb_sim {
   RebinWork w{};
   EntryTab et{};
   double *dcenter = nullptr;
+  int *boxc = nullptr;
   int *box_start = nullptr, *atom_slot = nullptr, *cpart = nullptr;
   int ncpart = 0;
   uint16_t *nbr = nullptr;
@@ -406,7 +407,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
   cudaStream_t st = h->stream;
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
                  st);
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   const int pot = h->opts.potential;
   if (h->mixed) {
     float rc2 = pot == COMDGB_POT_LJ ? h->lj32.rc2 : (float)(h->cutoff * h->cutoff);
@@ -415,28 +416,28 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
     double rc2 = pot == COMDGB_POT_LJ ? h->lj64.rc2 : h->cutoff * h->cutoff;
     launch_nbr_build<double>(A, rc2, st);
   }
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   if (pot == COMDGB_POT_LJ) {
     if (h->mixed) launch_lj<float>(A, h->lj32, st);
     else launch_lj<double>(A, h->lj64, st);
-    if (ev) cudaEventRecord(ev[evi++], st);
-    if (ev) cudaEventRecord(ev[evi++], st);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     return;
   }
   if (pot == COMDGB_POT_EAM_TABLE) {
     if (h->mixed) launch_eam_pass1<float, EVAL_TABLE>(A, h->eam32t, st);
     else launch_eam_pass1<double, EVAL_TABLE>(A, h->eam64t, st);
-    if (ev) cudaEventRecord(ev[evi++], st);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     if (h->mixed) launch_eam_pass2<float, EVAL_TABLE>(A, h->eam32t, st);
     else launch_eam_pass2<double, EVAL_TABLE>(A, h->eam64t, st);
   } else {
     if (h->mixed) launch_eam_pass1<float, EVAL_CHEBY>(A, h->eam32c, st);
     else launch_eam_pass1<double, EVAL_CHEBY>(A, h->eam64c, st);
-    if (ev) cudaEventRecord(ev[evi++], st);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     if (h->mixed) launch_eam_pass2<float, EVAL_CHEBY>(A, h->eam32c, st);
     else launch_eam_pass2<double, EVAL_CHEBY>(A, h->eam64c, st);
   }
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
 }
 
 void enqueue_reduce(comdgb_sim *h) {
@@ -454,19 +455,19 @@ void enqueue_rebox(comdgb_sim *h) {
 void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev) {
   int evi = 0;
   cudaStream_t st = h->stream;
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
   launch_advance_positions(h->g, h->s, dt_atu / 2.0, h->rmass, h->mixed, true, h->w, h->status,
                            st);
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_classify_finish(h);
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_force_parts(h, ev, evi);
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
   launch_advance_vp(h->g, h->s, dt_atu, dt_atu / 2.0, h->rmass, h->mixed, h->w, h->status, st);
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_classify_finish(h);
-  if (ev) cudaEventRecord(ev[evi++], st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
 }
 
 int count_kernel_nodes(cudaGraph_t graph) {
@@ -599,6 +600,8 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
     return set_err(COMDGB_ERR_ARG, "simflat_t has no allocated domains");
   if ((long)s->nboxes * CG_MAXATOMS >= (1L << 31))
     return set_err(COMDGB_ERR_UNSUPPORTED, "too many boxes");
+  for (int j = 0; j < 3; j++)
+    if (s->nbx[j] > 1023) return set_err(COMDGB_ERR_UNSUPPORTED, "more than 1023 boxes per axis");
   comdgb_sim *h = new comdgb_sim();
   h->opts = *o;
   h->device = o->device;
@@ -638,6 +641,8 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   h->et.dr64 = track(h, dalloc<d4>(nb * CG_NNBR, &err));
   h->et.dr32 = track(h, dalloc<float4>(2 * nb * CG_NNBR, &err));
   h->dcenter = track(h, dalloc<double>(nb * 3, &err));
+  h->boxc = track(h, dalloc<int>(nb, &err));
+  h->g.boxc = h->boxc;
   h->box_start = track(h, dalloc<int>(nb + 1, &err));
   h->atom_slot = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
   h->ncpart = compact_partials(s->nboxes);
@@ -665,7 +670,7 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   cudaMemsetAsync(h->atom_stress, 0, sizeof(double) * ((size_t)h->ntot + 1), h->stream);
   cudaMemcpyAsync(h->dcenter, s->dcenter, nb * 3 * sizeof(double), cudaMemcpyHostToDevice,
                   h->stream);
-  launch_entry_table(h->g, h->dcenter, h->et, h->stream);
+  launch_entry_table(h->g, h->dcenter, h->et, h->boxc, h->stream);
   int rc2 = setup_potential(h, s);
   if (!rc2) rc2 = upload(h, s);
   if (!rc2) {
@@ -821,6 +826,25 @@ int comdgb_sim_rebox(comdgb_sim *h) {
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   CK(cudaSetDevice(h->device));
   enqueue_rebox(h);
+  CK(cudaGetLastError());
+  return check_status(h);
+}
+
+int comdgb_sim_advance_velocity(comdgb_sim *h, double dt) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  launch_advance_velocity(h->g, h->s, dt, h->stream);
+  CK(cudaGetLastError());
+  return check_status(h);
+}
+
+int comdgb_sim_advance_positions(comdgb_sim *h, double dt) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  CK(cudaSetDevice(h->device));
+  cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), h->stream);
+  launch_advance_positions(h->g, h->s, dt, h->rmass, h->mixed, true, h->w, h->status,
+                           h->stream);
+  enqueue_classify_finish(h);
   CK(cudaGetLastError());
   return check_status(h);
 }

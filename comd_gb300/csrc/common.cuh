@@ -32,7 +32,26 @@ struct Geom {
   int periodic;
   double bounds[3];
   double boxsize[3];
+  const int *boxc;  // [nboxes] packed box coordinates ix | iy << 10 | iz << 20
 };
+
+// box coordinates from the packed table (avoids integer division)
+__device__ __forceinline__ void box_ixyz_tab(const Geom &g, int b, int *ix) {
+  int c = __ldg(g.boxc + b);
+  ix[0] = c & 1023;
+  ix[1] = (c >> 10) & 1023;
+  ix[2] = (c >> 20) & 1023;
+}
+
+// RN(a / b) from y = RN(1/b) with two fused multiply-adds (Markstein): the
+// residual a - b*q is exact and q + r*y rounds to the correctly rounded
+// quotient.  Used only when b's significand is not all ones (checked on
+// the host); the integrator's result equals a division a / b bit for bit.
+__device__ __forceinline__ double div_markstein(double a, double b, double y) {
+  double q = __dmul_rn(a, y);
+  double r = __fma_rn(-q, b, a);
+  return __fma_rn(r, y, q);
+}
 
 struct Slots {
   int *natoms;

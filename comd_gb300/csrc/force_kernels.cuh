@@ -165,72 +165,143 @@ __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int
 // ---------------------------------------------------------------------------
 // neighbour-list build: one CTA per box, one warp per atom of the box
 // ---------------------------------------------------------------------------
+#define NB_THREADS 128
+#define NB_MAXC (CG_NNBR * CG_MAXATOMS)
+
+// stencil entries of box b: boxes, box offsets and candidate offsets (warp 0)
 template <class T>
-__global__ void __launch_bounds__(128) nbr_build_kernel(ForceArgs A, T rc2) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ int stage_entries(const ForceArgs &A, int b, int *s_box, int *s_off,
+                                             BoxOff<T> *s_dr) {
+  const int ne = A.et.n[b];
+  if (threadIdx.x < 32) {
+    const int e = threadIdx.x;
+    int n = 0;
+    if (e < ne) {
+      int jb = A.et.box[b * CG_NNBR + e];
+      s_box[e] = jb;
+      s_dr[e] = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
+      n = A.s.natoms[jb];
+    }
+    int x = n;  // inclusive warp scan
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (e >= o) x += y;
+    }
+    if (e < ne) s_off[e + 1] = x;
+    if (e == 0) s_off[0] = 0;
+  }
+  __syncthreads();
+  return ne;
+}
+
+__device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
+  int lo = 0, hi = ne - 1;  // last e with s_off[e] <= c
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (s_off[mid] <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// FP32: candidates staged as (x - drbox, y - drbox, z - drbox, code) in the
+// centre box's frame; the cutoff of the build is widened by a hair so the
+// list is a superset of the pairs the passes accept with their exact dr.
+static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
+  __shared__ __align__(16) float4 cand[NB_MAXC];
+  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
+  __shared__ BoxOff<float> s_dr[CG_NNBR];
   const int b = blockIdx.x;
   const int ni = A.s.natoms[b];
   if (ni == 0) return;
-  const int maxc = CG_NNBR * CG_MAXATOMS;
-  T *cx = reinterpret_cast<T *>(smem_raw);
-  T *cy = cx + maxc;
-  T *cz = cy + maxc;
-  uint16_t *cc = reinterpret_cast<uint16_t *>(cz + maxc);
-  __shared__ int s_box[CG_NNBR];
-  __shared__ int s_off[CG_NNBR + 1];
-  __shared__ BoxOff<T> s_dr[CG_NNBR];
-
-  const int ne = A.et.n[b];
-  if (threadIdx.x < ne) {
-    int e = threadIdx.x;
-    s_box[e] = A.et.box[b * CG_NNBR + e];
-    s_dr[e] = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int off = 0;
-    for (int e = 0; e < ne; e++) {
-      s_off[e] = off;
-      off += A.s.natoms[s_box[e]];
-    }
-    s_off[ne] = off;
-  }
-  __syncthreads();
+  const int ne = stage_entries<float>(A, b, s_box, s_off, s_dr);
   const int ncand = s_off[ne];
-  // stage candidates: entry-major, slot-minor
-  for (int e = 0; e < ne; e++) {
-    int jb = s_box[e], base = s_off[e], nj = s_off[e + 1] - base;
-    for (int k = threadIdx.x; k < nj; k += blockDim.x) {
-      T x, y, z;
-      PrecT<T>::pos(A.s, jb * CG_MAXATOMS + k, x, y, z);
-      cx[base + k] = x; cy[base + k] = y; cz[base + k] = z;
-      cc[base + k] = (uint16_t)((e << 6) | k);
-    }
+  for (int c = threadIdx.x; c < ncand; c += NB_THREADS) {
+    int e = entry_of(s_off, ne, c);
+    int k = c - s_off[e];
+    float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
+    BoxOff<float> o = s_dr[e];
+    cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
+                          __int_as_float((e << 6) | k));
   }
   __syncthreads();
-
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const float rc2b = rc2 * (1.0f + 4e-6f);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
-  for (int i = warp; i < ni; i += nw) {
-    T xi, yi, zi;
-    PrecT<T>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
+  for (int i = warp; i < ni; i += NB_THREADS / 32) {
+    const float4 pi = __ldg(A.s.pos32 + b * CG_MAXATOMS + i);
     const int a = A.box_start[b] + i;
     if (a >= A.ntot) break;  // only after a reported overflow
     uint16_t *out = A.nbr + (size_t)a * A.cap;
     int cnt = 0;
     for (int c0 = 0; c0 < ncand; c0 += 32) {
-      int c = c0 + lane;
+      const int c = c0 + lane;
+      bool hit = false;
+      float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c < ncand) {
+        q = cand[c];
+        float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
+        float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        hit = (r2 <= rc2b) && (r2 > 0.f);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      const int pos = cnt + __popc(m & lt);
+      if (hit && pos < A.cap) out[pos] = (uint16_t)__float_as_int(q.w);
+      cnt += __popc(m);
+    }
+    if (lane == 0) {
+      A.nbr_n[a] = cnt;
+      if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+    }
+  }
+}
+
+// FP64: the reference's dr = (drbox + r_i) - r_j, operation by operation
+static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArgs A, double rc2) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double *cx = reinterpret_cast<double *>(smem_raw);
+  double *cy = cx + NB_MAXC;
+  double *cz = cy + NB_MAXC;
+  uint16_t *cc = reinterpret_cast<uint16_t *>(cz + NB_MAXC);
+  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
+  __shared__ BoxOff<double> s_dr[CG_NNBR];
+  const int b = blockIdx.x;
+  const int ni = A.s.natoms[b];
+  if (ni == 0) return;
+  const int ne = stage_entries<double>(A, b, s_box, s_off, s_dr);
+  const int ncand = s_off[ne];
+  for (int c = threadIdx.x; c < ncand; c += NB_THREADS) {
+    int e = entry_of(s_off, ne, c);
+    int k = c - s_off[e];
+    d4 q = A.s.r[s_box[e] * CG_MAXATOMS + k];
+    cx[c] = q.x;
+    cy[c] = q.y;
+    cz[c] = q.z;
+    cc[c] = (uint16_t)((e << 6) | k);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  for (int i = warp; i < ni; i += NB_THREADS / 32) {
+    double xi, yi, zi;
+    PrecT<double>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
+    const int a = A.box_start[b] + i;
+    if (a >= A.ntot) break;
+    uint16_t *out = A.nbr + (size_t)a * A.cap;
+    int cnt = 0;
+    for (int c0 = 0; c0 < ncand; c0 += 32) {
+      const int c = c0 + lane;
       bool hit = false;
       uint16_t code = 0;
       if (c < ncand) {
         code = cc[c];
         int e = code >> 6, k = code & 63;
-        T dx, dy, dz;
-        T r2 = pair_r2(s_dr[e], xi, yi, zi, cx[c], cy[c], cz[c], dx, dy, dz);
+        double dx, dy, dz;
+        double r2 = pair_r2(s_dr[e], xi, yi, zi, cx[c], cy[c], cz[c], dx, dy, dz);
         hit = (r2 <= rc2) && !(s_box[e] == b && k == i);
       }
-      unsigned m = __ballot_sync(0xffffffffu, hit);
-      int pos = cnt + __popc(m & lt);
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      const int pos = cnt + __popc(m & lt);
       if (hit && pos < A.cap) out[pos] = code;
       cnt += __popc(m);
     }
@@ -256,10 +327,29 @@ template <int EVAL>
 __device__ __forceinline__ double cheb_series(const EamPot<double, EVAL> &P, int s, double x) {
   return cheb_eval64(P.ch.c[s], P.ch.a[s], P.ch.b[s], x);
 }
+// the reference coefficients for arguments below the re-expansion interval
+// (never taken in practice; kept out of line so it costs no code in the loop)
+static __device__ __noinline__ float cheb_low32(const ChebLow32 &L, int s, float x) {
+  return cheb_eval32(L.c[s], L.a[s], L.ys[s], L.yo[s], x);
+}
+
 template <int EVAL>
 __device__ __forceinline__ float cheb_series(const EamPot<float, EVAL> &P, int s, float x) {
   if (x >= P.chlo.lo[s]) return cheb_eval32(P.ch.c[s], P.ch.a[s], P.ch.ys[s], P.ch.yo[s], x);
-  return cheb_eval32(P.chlo.c[s], P.chlo.a[s], P.chlo.ys[s], P.chlo.yo[s], x);
+  return cheb_low32(P.chlo, s, x);
+}
+
+// r and 1/r from r^2: FP64 as the reference (sqrt, then divide); FP32 from
+// rsqrt refined by one Newton step (about 1 ulp)
+__device__ __forceinline__ void r_and_inv(double r2, double &r, double &inv) {
+  r = sqrt(r2);
+  inv = 1.0 / r;
+}
+__device__ __forceinline__ void r_and_inv(float r2, float &r, float &inv) {
+  float y = rsqrtf(r2);
+  y = y * fmaf(-0.5f * r2, y * y, 1.5f);
+  inv = y;
+  r = r2 * y;
 }
 
 template <class T, int EVAL>
@@ -304,18 +394,21 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   PrecT<T>::pos(A.s, slot, xi, yi, zi);
   typename PrecT<T>::Acc fx, fy, fz, ep, rh;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
+  const T rc2 = P.rc2;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
-    T r = sqrt(r2);
+    if (r2 > rc2) return;
+    T r, inv_r;
+    r_and_inv(r2, r, inv_r);
     T phi, dphi, rho;
     eam_pair_terms<T, EVAL>(P, r, phi, dphi, rho);
-    T w = dphi / r;
+    T w = dphi * inv_r;
     fx.add(w * dx);
     fy.add(w * dy);
     fz.add(w * dz);
     ep.add(phi / T(2.0));
     rh.add(rho);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, P.rc2, fn);
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
   double rho_i = rh.value();
   T F, dF;
   eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
@@ -347,10 +440,11 @@ __global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, E
   const T rc2 = P.rc2;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 >= rc2) return;
-    T r = sqrt(r2);
+    T r, inv_r;
+    r_and_inv(r2, r, inv_r);
     T drho = eam_drho<T, EVAL>(P, r);
     T w = (fii + PrecT<T>::fi(A.s, js)) * drho;
-    T wr = w / r;
+    T wr = w * inv_r;
     fx.add(wr * dx);
     fy.add(wr * dy);
     fz.add(wr * dz);
@@ -385,7 +479,9 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
   typename PrecT<T>::Acc fx, fy, fz, ep, sx;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
   const T s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6;
+  const T rc2 = P.rc2;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
+    if (r2 > rc2) return;
     T ir2 = T(1.0) / r2;
     T r6 = ir2 * ir2 * ir2;
     ep.add(T(0.5) * r6 * (s6 * r6 - T(1.0)));
@@ -395,7 +491,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
     fz.add(dz * fr);
     sx.add(fr * dx * dx);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, P.rc2, fn);
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
   // kinetic term: -p_x^2/m per non-empty stencil entry
   int ne = A.et.n[b], nonempty = 0;
   for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;

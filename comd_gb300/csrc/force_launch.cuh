@@ -5,19 +5,23 @@
 namespace cg {
 
 static size_t nbr_build_smem() {
-  return (size_t)CG_NNBR * CG_MAXATOMS * (3 * sizeof(FT) + sizeof(uint16_t));
+  return sizeof(FT) == 8 ? (size_t)NB_MAXC * (3 * sizeof(double) + sizeof(uint16_t)) : 0;
 }
 
 // called on the current device before any launch or stream capture
 template <>
 cudaError_t prepare_nbr_build<FT>() {
-  return cudaFuncSetAttribute(nbr_build_kernel<FT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  if (sizeof(FT) == 4) return cudaSuccess;
+  return cudaFuncSetAttribute(nbr_build64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)nbr_build_smem());
 }
 
 template <>
 void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
-  nbr_build_kernel<FT><<<A.g.nboxes, 128, nbr_build_smem(), st>>>(A, rc2);
+  if (sizeof(FT) == 4)
+    nbr_build32_kernel<<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+  else
+    nbr_build64_kernel<<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
 }
 
 template <>

@@ -20,13 +20,18 @@ struct RebinWork {
 };
 
 // ---- md_kernels.cu ----
-void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, cudaStream_t st);
+// packed box coordinates (g.boxc must point at boxc) and the stencil table
+void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, int *boxc,
+                        cudaStream_t st);
+double mass_reciprocal(double rmass);
 // r += dt*p/rmass (and optionally the classify step of reBoxAll)
 void launch_advance_positions(const Geom &g, Slots s, double dt, double rmass, bool mixed,
                               bool classify, const RebinWork &w, int *status, cudaStream_t st);
 // p -= dt_v*f; r += dt_r*p/rmass; classify
 void launch_advance_vp(const Geom &g, Slots s, double dt_v, double dt_r, double rmass,
                        bool mixed, const RebinWork &w, int *status, cudaStream_t st);
+// p -= dt_v*f only (advanceVelocity)
+void launch_advance_velocity(const Geom &g, Slots s, double dt_v, cudaStream_t st);
 // classify only (reBoxAll without a position update)
 void launch_classify(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
                      cudaStream_t st);

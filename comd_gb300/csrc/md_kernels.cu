@@ -6,6 +6,7 @@
 // that, given the same forces, positions and momenta are bit-identical and
 // the rebinning decisions agree with reBoxAll.
 #include <cstdio>
+#include <cstring>
 
 #include "internal.h"
 
@@ -58,7 +59,17 @@ __global__ void entry_table_kernel(Geom g, const double *dcenter, EntryTab et) {
   et.n[b] = cnt;
 }
 
-void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, cudaStream_t st) {
+__global__ void box_coord_kernel(Geom g, int *boxc) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nboxes) return;
+  int ix[3];
+  box_ixyz(g, b, ix);
+  boxc[b] = ix[0] | (ix[1] << 10) | (ix[2] << 20);
+}
+
+void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, int *boxc,
+                        cudaStream_t st) {
+  box_coord_kernel<<<(g.nboxes + 127) / 128, 128, 0, st>>>(g, boxc);
   entry_table_kernel<<<(g.nboxes + 127) / 128, 128, 0, st>>>(g, dcenter, et);
 }
 
@@ -109,7 +120,7 @@ __device__ __forceinline__ void classify_slot(const Geom &g, const Slots &s, int
   bool dep = false;
   if (valid) {
     int ixo[3], ixn[3];
-    box_ixyz(g, b, ixo);
+    box_ixyz_tab(g, b, ixo);
     double rn[3] = {r.x, r.y, r.z};
     double rc[3] = {r.x, r.y, r.z};
     for (int k = 0; k < 3; k++) {
@@ -140,7 +151,7 @@ __device__ __forceinline__ void classify_slot(const Geom &g, const Slots &s, int
       if (jb > b) {
         // re-examined in jb's scan: must stay there
         int ix2[3], ix3[3];
-        box_ixyz(g, jb, ix2);
+        box_ixyz_tab(g, jb, ix2);
         for (int k = 0; k < 3; k++) {
           if (rn[k] < 0.0) ix3[k] = ix2[k] - 1;
           else if (rn[k] >= g.boxsize[k]) ix3[k] = ix2[k] + 1;
@@ -155,10 +166,15 @@ __device__ __forceinline__ void classify_slot(const Geom &g, const Slots &s, int
   if ((threadIdx.x & 31) == 0) w.depmask[slot >> 5] = m;
 }
 
-template <bool UPDATE, bool VEL>
+// division by the (constant) mass: Markstein when rinv != 0, else IEEE
+__device__ __forceinline__ double div_mass(double a, double rmass, double rinv) {
+  return rinv != 0.0 ? div_markstein(a, rmass, rinv) : a / rmass;
+}
+
+template <bool POS, bool VEL>
 __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt_v, double dt_r,
-                                                      double rmass, bool mixed, bool classify,
-                                                      RebinWork w, int *status) {
+                                                      double rmass, double rinv, bool mixed,
+                                                      bool classify, RebinWork w, int *status) {
   const long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int nslots = g.nboxes * CG_MAXATOMS;
   if (slot >= nslots) return;  // nslots is a multiple of 64: whole warps exit
@@ -167,7 +183,7 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt
   d4 r = d4{0.0, 0.0, 0.0, 0.0};
   if (valid) {
     r = s.r[slot];
-    if (UPDATE) {
+    if (POS || VEL) {
       d4 p = s.p[slot];
       if (VEL) {
         // advanceVelocity, timestep.c:71
@@ -177,12 +193,14 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt
         p.z = p.z - dt_v * f.z;
         s.p[slot] = p;
       }
-      // advancePositions, timestep.c:104
-      r.x = r.x + dt_r * p.x / rmass;
-      r.y = r.y + dt_r * p.y / rmass;
-      r.z = r.z + dt_r * p.z / rmass;
-      s.r[slot] = r;
-      if (mixed) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
+      if (POS) {
+        // advancePositions, timestep.c:104: r + (dt*p)/rmass
+        r.x = r.x + div_mass(dt_r * p.x, rmass, rinv);
+        r.y = r.y + div_mass(dt_r * p.y, rmass, rinv);
+        r.z = r.z + div_mass(dt_r * p.z, rmass, rinv);
+        s.r[slot] = r;
+        if (mixed) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
+      }
     }
   }
   if (classify) classify_slot(g, s, (int)slot, valid, r, mixed, w, status);
@@ -193,22 +211,37 @@ static unsigned slot_blocks(const Geom &g) {
   return (unsigned)((nslots + 255) / 256);
 }
 
+// y = RN(1/b) when Markstein's division is exact for b, else 0 (IEEE path)
+double mass_reciprocal(double rmass) {
+  uint64_t bits;
+  memcpy(&bits, &rmass, sizeof bits);
+  const uint64_t mant = bits & ((1ull << 52) - 1);
+  if (mant == (1ull << 52) - 1 || !(rmass > 0.0)) return 0.0;
+  return 1.0 / rmass;
+}
+
 void launch_advance_positions(const Geom &g, Slots s, double dt, double rmass, bool mixed,
                               bool classify, const RebinWork &w, int *status, cudaStream_t st) {
-  advance_kernel<true, false><<<slot_blocks(g), 256, 0, st>>>(g, s, 0.0, dt, rmass, mixed,
-                                                              classify, w, status);
+  advance_kernel<true, false><<<slot_blocks(g), 256, 0, st>>>(
+      g, s, 0.0, dt, rmass, mass_reciprocal(rmass), mixed, classify, w, status);
 }
 
 void launch_advance_vp(const Geom &g, Slots s, double dt_v, double dt_r, double rmass,
                        bool mixed, const RebinWork &w, int *status, cudaStream_t st) {
-  advance_kernel<true, true><<<slot_blocks(g), 256, 0, st>>>(g, s, dt_v, dt_r, rmass, mixed,
-                                                             true, w, status);
+  advance_kernel<true, true><<<slot_blocks(g), 256, 0, st>>>(
+      g, s, dt_v, dt_r, rmass, mass_reciprocal(rmass), mixed, true, w, status);
+}
+
+void launch_advance_velocity(const Geom &g, Slots s, double dt_v, cudaStream_t st) {
+  RebinWork none{};
+  advance_kernel<false, true><<<slot_blocks(g), 256, 0, st>>>(g, s, dt_v, 0.0, 1.0, 0.0, false,
+                                                              false, none, nullptr);
 }
 
 void launch_classify(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
                      cudaStream_t st) {
-  advance_kernel<false, false><<<slot_blocks(g), 256, 0, st>>>(g, s, 0.0, 0.0, 1.0, mixed, true,
-                                                               w, status);
+  advance_kernel<false, false><<<slot_blocks(g), 256, 0, st>>>(g, s, 0.0, 0.0, 1.0, 0.0, mixed,
+                                                               true, w, status);
 }
 
 // distinct stencil boxes of b other than b, ascending

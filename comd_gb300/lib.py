@@ -61,6 +61,8 @@ def _bind(lib):
     L.comdgb_sim_force.argtypes = [C.c_void_p]
     L.comdgb_sim_steps.argtypes = [C.c_void_p, C.c_int, C.c_double]
     L.comdgb_sim_rebox.argtypes = [C.c_void_p]
+    L.comdgb_sim_advance_velocity.argtypes = [C.c_void_p, C.c_double]
+    L.comdgb_sim_advance_positions.argtypes = [C.c_void_p, C.c_double]
     L.comdgb_sim_energy.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.comdgb_sim_kinetic.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     L.comdgb_sim_pair_count.argtypes = [C.c_void_p, C.POINTER(C.c_longlong)]
@@ -222,6 +224,12 @@ class DeviceSim:
     def steps(self, n, dt=1e-15):
         check(self.L.comdgb_sim_steps(self.h, n, dt))
         return self.energy()
+
+    def advance_velocity(self, dt):
+        check(self.L.comdgb_sim_advance_velocity(self.h, dt))
+
+    def advance_positions(self, dt):
+        check(self.L.comdgb_sim_advance_positions(self.h, dt))
 
     def rebox(self):
         check(self.L.comdgb_sim_rebox(self.h))

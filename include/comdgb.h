@@ -105,6 +105,11 @@ int comdgb_sim_force(comdgb_sim *h);
  * CUDA graph after the first call with the same dt */
 int comdgb_sim_steps(comdgb_sim *h, int n, double dt);
 int comdgb_sim_rebox(comdgb_sim *h);
+/* advanceVelocity (timestep.c:62-74): p -= dt f; dt in the reference's
+ * internal time unit (seconds * 0.529/2.418e-17, timestep.c:126) */
+int comdgb_sim_advance_velocity(comdgb_sim *h, double dt);
+/* advancePositions (timestep.c:76-108): r += dt p / (1822.83 m), then reBoxAll */
+int comdgb_sim_advance_positions(comdgb_sim *h, double dt);
 /* totals of the last force call: energy, stress (reference definitions) */
 int comdgb_sim_energy(comdgb_sim *h, double *e, double *stress);
 /* kinetic energy sum p^2/2M on the GPU */

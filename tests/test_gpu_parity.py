@@ -75,7 +75,7 @@ def test_eam_force_nonperiodic(oracle):
 
 def test_eam_force_stretched_boxfactor(oracle):
     cmp, (e, st), (eo, so), _ = _force_case(oracle, cg.POT_EAM_CHEBY, cg.PREC_FP64,
-                                            n=(10, 10, 10), defgrad=1.05, bf=1.5, temp=300.0,
+                                            n=(13, 13, 13), defgrad=1.05, bf=1.5, temp=300.0,
                                             amp=0.05, disp=cg.DISP_GAUSSIAN)
     assert cmp["f_max_rel"] < FP64_F_TOL, cmp
     assert abs(e - eo) <= FP64_E_TOL * abs(eo)
@@ -84,7 +84,7 @@ def test_eam_force_stretched_boxfactor(oracle):
 @pytest.mark.parametrize("potential", [cg.POT_EAM_TABLE, cg.POT_EAM_CHEBY])
 def test_eam_force_mixed(oracle, potential):
     cmp, (e, st), (eo, so), ntot = _force_case(oracle, potential, cg.PREC_MIXED,
-                                               n=(10, 10, 10), defgrad=1.05, bf=1.5,
+                                               n=(13, 13, 13), defgrad=1.05, bf=1.5,
                                                temp=300.0, amp=0.05)
     assert cmp["f_rel_rms"] < MIXED_F_RMS_TOL, cmp
     assert abs(e - eo) / ntot < 1e-7, (e, eo)
@@ -113,6 +113,32 @@ def test_rebox_bitexact(oracle):
         d.download(c.s)
         d.close()
         assert slots_equal(c.s, o2, ("id", "iType", "mass", "r", "p", "f", "rho", "fi"))
+        c.oracle.free(o2)
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("mass", [63.55, 107.9, 1.0])
+def test_integrator_bitexact(oracle, mass):
+    """advanceVelocity + advancePositions (+ reBoxAll) equal the oracle bit for bit."""
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(8, 8, 8), temp=900.0)
+    try:
+        c.pot.ptr.contents.mass = mass
+        v = slot_views(c.s)
+        rng = np.random.default_rng(9)
+        v["f"][:] = rng.normal(scale=0.05, size=v["f"].shape)
+        v["p"][:] *= 40.0  # large momenta so that atoms cross boxes
+        o2 = c.oracle.clone(c.s)
+        dt = 1e-15 * cg.lib.BOHR_PER_ATU
+        d = c.device()
+        d.advance_velocity(dt)
+        d.advance_positions(dt / 2.0)
+        d.download(c.s)
+        d.close()
+        c.oracle.lib.orc_advance_velocity(o2, dt)
+        c.oracle.lib.orc_advance_positions(o2, dt / 2.0)
+        assert c.oracle.rebox(o2) == 0
+        assert slots_equal(c.s, o2, ("id", "r", "p", "f"))
         c.oracle.free(o2)
     finally:
         c.close()

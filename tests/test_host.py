@@ -1,0 +1,129 @@
+"""CPU tests of the library's host side: the shared library loads and exports
+every entry point of include/comdgb.h, the host setup routines reproduce
+the oracle's byte for byte, GPU calls fail with an error code (never a CPU
+fallback) when no GPU is present, and the replica path of bench.py works
+across two gloo ranks."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import comd_gb300 as cg
+from comd_gb300.abi import slot_views
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "comdgb.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(comdgb_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = cg.load()
+    names = declared_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_tables_match_oracle(oracle, pots_dir):
+    pot = cg.eam_potential("cu")
+    opot = oracle.eam(pots_dir, "cu")
+    for name in ("phi", "rho", "f"):
+        a = getattr(pot.ptr.contents, name).contents
+        b = getattr(opot.contents, name).contents
+        assert (a.n, a.x0, a.xn, a.invDx) == (b.n, b.x0, b.xn, b.invDx)
+        va = np.ctypeslib.as_array(C.cast(C.addressof(a.values.contents) - 8,
+                                          C.POINTER(C.c_double)), (a.n + 3,))
+        vb = np.ctypeslib.as_array(C.cast(C.addressof(b.values.contents) - 8,
+                                          C.POINTER(C.c_double)), (b.n + 3,))
+        assert np.array_equal(va, vb)
+    assert pot.ptr.contents.mass == 63.55 and pot.ptr.contents.lat == 3.615
+    assert pot.ptr.contents.cutoff == 4.961
+
+
+@pytest.mark.parametrize("dims", [(10, 10, 10, 1.0, 1.0), (13, 13, 13, 1.05, 1.5),
+                                  (3, 5, 2, 1.0, 1.0)])
+def test_fcc_and_seed_match_oracle(oracle, pots_dir, dims):
+    nx, ny, nz, dg, bf = dims
+    pot = cg.eam_potential("cu")
+    opot = oracle.eam(pots_dir, "cu")
+    s = cg.fcc(nx, ny, nz, 3.615, dg, bf, pot)
+    so = oracle.fcc(nx, ny, nz, 3.615, dg, bf, opot)
+    cg.seed(s, 99, cg.DISP_GAUSSIAN, 0.05, 600.0, 63.55)
+    oracle.seed(so, 99, cg.DISP_GAUSSIAN, 0.05, 600.0, 63.55)
+    assert list(s.contents.nbx) == list(so.contents.nbx)
+    assert s.contents.ntot == so.contents.ntot == 4 * nx * ny * nz
+    va, vb = slot_views(s), slot_views(so)
+    for k in va:
+        assert np.array_equal(va[k], vb[k]), k
+    cg.free_host(s)
+    oracle.free(so)
+
+
+def test_seed_momenta_have_zero_total(oracle, pots_dir):
+    pot = oracle.eam(pots_dir, "cu")
+    s = oracle.fcc(6, 6, 6, 3.615, 1.0, 1.0, pot)
+    oracle.seed(s, 3, 0, 0.0, 300.0, 63.55)
+    v = slot_views(s)
+    m = np.arange(64)[None, :] < v["natoms"][:, None]
+    p = v["p"][m.reshape(-1)]
+    assert np.abs(p.sum(0)).max() < 1e-9 * np.abs(p).max()
+    # equipartition: <p^2/2M> = 3/2 kT within sampling error
+    ek = (p ** 2).sum() / (2 * 63.55 * 1822.83)
+    kt = 3.166811563e-6 * 300.0
+    assert abs(ek / (1.5 * kt * len(p)) - 1) < 0.1
+    oracle.free(s)
+
+
+def test_gpu_entry_points_fail_loudly_without_gpu():
+    """Without a usable GPU the library returns an error; it never computes on the CPU."""
+    import subprocess
+    import sys
+    code = (
+        "import os, sys; sys.path.insert(0, %r); os.environ['CUDA_VISIBLE_DEVICES'] = '';"
+        "import comd_gb300 as cg\n"
+        "pot = cg.eam_potential('cu'); s = cg.fcc(4, 4, 4, 3.615, 1, 1, pot)\n"
+        "try:\n    cg.DeviceSim(s, cg.opts()); print('CREATED')\n"
+        "except cg.ComdgbError as e:\n    print('ERR', e.code)\n" % ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                         env=dict(os.environ, CUDA_VISIBLE_DEVICES=""), timeout=120)
+    assert "ERR" in out.stdout, out.stdout + out.stderr
+    assert "CREATED" not in out.stdout
+
+
+def _replica_rank(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    d = bench.Dist(world)
+    d.barrier()
+    s = d.sum(rank + 1.0)
+    m = d.max(10.0 * rank)
+    d.close()
+    q.put((rank, s, m))
+
+
+def test_bench_replicas_over_gloo():
+    """bench.py's N>1 path (replicas): barrier, sum of work and max of time over 2 ranks."""
+    pytest.importorskip("torch")
+    import multiprocessing as mp
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    ps = [ctx.Process(target=_replica_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in ps:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in ps)
+    for p in ps:
+        p.join(timeout=60)
+    assert res == [(0, 3.0, 10.0), (1, 3.0, 10.0)]
