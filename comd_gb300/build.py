@@ -29,6 +29,7 @@ UNITS = [
     ("force_fp64.cu", ["-fmad=false"]),
     ("force_mixed.cu", []),
     ("api.cu", []),
+    ("noalloc.cu", ["-fmad=false"]),
 ]
 CUNITS = ["host_setup.c"]
 

@@ -90,6 +90,9 @@ def _bind(lib):
     L.comdgb_rebox_host.argtypes = [P_SIM, C.c_int, C.c_int]
     L.comdgb_put_atoms.argtypes = [P_SIM, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p, C.c_void_p, C.c_int]
+    L.comdgb_put_atoms_noalloc.argtypes = (
+        [C.POINTER(C.c_int), C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p, C.c_int]
+        + [C.c_void_p] * 5 + [C.c_void_p] * 6 + [C.c_int, C.c_void_p])
     return lib
 
 

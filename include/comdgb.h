@@ -161,6 +161,26 @@ int comdgb_rebox_host(simflat_t *s, int periodic, int device);
 int comdgb_put_atoms(simflat_t *s, int n, const double *xyz, const double *pxyz,
                      const int *ids, const int *itypes, const double *masses, int device);
 
+/* Allocation-free binning.  No counterpart in the reference: it is
+ * comdgb_put_atoms for callers that cannot allocate device memory while
+ * they run (an engine owning all GPU memory through its own arena, work
+ * issued during CUDA graph stream capture, latency-critical loops).  All
+ * arrays are device pointers in the reference's slot layout (r and p as
+ * real3 rows, slot = box*64 + k); dcenter is nbx product x 3 doubles.  The
+ * result equals comdgb_put_atoms: n putAtomInBox calls in array order.
+ * Scratch is a library-owned device array of COMDGB_NOALLOC_MAX_BOXES*64
+ * ints (4 MiB per device, held until the process exits); larger grids are
+ * rejected with COMDGB_ERR_ARG.  The first call on a device looks up that
+ * array's address (cudaGetSymbolAddress) -- make it before any stream
+ * capture.  Calls share the array: calls that overlap on the GPU race.
+ * Synchronises `stream` (a cudaStream_t, NULL = default) to report errors. */
+#define COMDGB_NOALLOC_MAX_BOXES 16384
+int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3], const double boxsize[3],
+                             const double *dcenter, int n, const double *xyz, const double *pxyz,
+                             const int *ids, const int *itypes, const double *masses,
+                             int *natoms, int *id, int *itype, double *mass, double *r, double *p,
+                             int device, void *stream);
+
 int comdgb_last_error(char *buf, int len);
 const char *comdgb_version(void);
 
