@@ -38,7 +38,11 @@ struct ForceArgs {
   int cap;
   double *atom_stress;   // [ntot] per-atom share of the scalar stress
   int *status;
+  uint32_t *mask;        // [ntot*NB_MASKW] FP32 path: hit bits per 32-candidate chunk
 };
+
+// candidates per box neighbourhood are at most 27*64, i.e. 54 chunks of 32
+#define NB_MASKW 54
 
 // Box offset of a stencil entry: FP64 value, or FP32 hi + lo parts.
 template <class T>
@@ -256,6 +260,94 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
   }
 }
 
+// FP32, bit-mask form: the same candidate test, but each warp takes two
+// atoms per candidate load and keeps only the 32-bit ballot of every chunk
+// (lane q % 32 holds chunk q); eam_pass1 decodes the bits into the list.
+static __global__ void __launch_bounds__(NB_THREADS) nbr_mask32_kernel(ForceArgs A, float rc2) {
+  __shared__ __align__(16) float4 cand[NB_MAXC];
+  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
+  __shared__ BoxOff<float> s_dr[CG_NNBR];
+  const int b = blockIdx.x;
+  const int ni = A.s.natoms[b];
+  if (ni == 0) return;
+  const int ne = stage_entries<float>(A, b, s_box, s_off, s_dr);
+  const int ncand = s_off[ne];
+  for (int c = threadIdx.x; c < ncand; c += NB_THREADS) {
+    int e = entry_of(s_off, ne, c);
+    int k = c - s_off[e];
+    float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
+    BoxOff<float> o = s_dr[e];
+    cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz, 0.f);
+  }
+  __syncthreads();
+  const float rc2b = rc2 * (1.0f + 4e-6f);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nchunk = (ncand + 31) >> 5;
+  for (int i0 = 2 * warp; i0 < ni; i0 += 2 * (NB_THREADS / 32)) {
+    const int i1 = (i0 + 1 < ni) ? i0 + 1 : i0;
+    const float4 p0 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0);
+    const float4 p1 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i1);
+    uint32_t k0a = 0, k0b = 0, k1a = 0, k1b = 0;  // kept masks, chunks lane and lane+32
+    for (int q = 0; q < nchunk; q++) {
+      const int c = (q << 5) + lane;
+      bool h0 = false, h1 = false;
+      if (c < ncand) {
+        const float4 cq = cand[c];
+        float dx = p0.x - cq.x, dy = p0.y - cq.y, dz = p0.z - cq.z;
+        float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        h0 = (r2 <= rc2b) && (r2 > 0.f);
+        dx = p1.x - cq.x; dy = p1.y - cq.y; dz = p1.z - cq.z;
+        r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        h1 = (r2 <= rc2b) && (r2 > 0.f);
+      }
+      const uint32_t m0 = __ballot_sync(0xffffffffu, h0);
+      const uint32_t m1 = __ballot_sync(0xffffffffu, h1);
+      if ((q & 31) == lane) {
+        if (q < 32) { k0a = m0; k1a = m1; }
+        else { k0b = m0; k1b = m1; }
+      }
+    }
+    const int a0 = A.box_start[b] + i0, a1 = A.box_start[b] + i1;
+    if (a0 < A.ntot) {
+      uint32_t *o0 = A.mask + (size_t)a0 * NB_MASKW;
+      if (lane < nchunk) o0[lane] = k0a;
+      if (lane + 32 < nchunk) o0[lane + 32] = k0b;
+    }
+    if (i1 != i0 && a1 < A.ntot) {
+      uint32_t *o1 = A.mask + (size_t)a1 * NB_MASKW;
+      if (lane < nchunk) o1[lane] = k1a;
+      if (lane + 32 < nchunk) o1[lane + 32] = k1b;
+    }
+  }
+}
+
+// Turn atom a's hit bits into its list of codes (entry << 6 | slot) in the
+// order of the candidates; returns the number of neighbours.  Offsets of the
+// stencil entries are rebuilt from the current box counts.
+__device__ __forceinline__ int decode_mask(const ForceArgs &A, int a, int b) {
+  const int ne = A.et.n[b];
+  int offs[CG_NNBR + 1];
+  offs[0] = 0;
+  for (int e = 0; e < ne; e++) offs[e + 1] = offs[e] + A.s.natoms[A.et.box[b * CG_NNBR + e]];
+  const int nchunk = (offs[ne] + 31) >> 5;
+  const uint32_t *m = A.mask + (size_t)a * NB_MASKW;
+  uint16_t *out = A.nbr + (size_t)a * A.cap;
+  int cnt = 0, e = 0;
+  for (int q = 0; q < nchunk; q++) {
+    uint32_t w = m[q];
+    while (w) {
+      const int c = (q << 5) + __ffs(w) - 1;
+      w &= w - 1;
+      while (c >= offs[e + 1]) e++;
+      if (cnt < A.cap) out[cnt] = (uint16_t)((e << 6) | (c - offs[e]));
+      cnt++;
+    }
+  }
+  A.nbr_n[a] = cnt;
+  if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+  return cnt;
+}
+
 // FP64: the reference's dr = (drbox + r_i) - r_j, operation by operation
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArgs A, double rc2) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -392,6 +484,7 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   const int b = slot >> 6, i = slot & 63;
   T xi, yi, zi;
   PrecT<T>::pos(A.s, slot, xi, yi, zi);
+  if (sizeof(T) == 4 && A.mask) decode_mask(A, a, b);
   typename PrecT<T>::Acc fx, fy, fz, ep, rh;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
   const T rc2 = P.rc2;
@@ -476,6 +569,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
   const int b = slot >> 6, i = slot & 63;
   T xi, yi, zi;
   PrecT<T>::pos(A.s, slot, xi, yi, zi);
+  if (sizeof(T) == 4 && A.mask) decode_mask(A, a, b);
   typename PrecT<T>::Acc fx, fy, fz, ep, sx;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
   const T s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6;
