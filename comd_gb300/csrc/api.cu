@@ -88,7 +88,6 @@ struct comdgb_sim {
   int ncpart = 0;
   uint16_t *nbr = nullptr;
   int *nbr_n = nullptr;
-  uint32_t *nbr_mask = nullptr;  // mixed precision: hit bits of the candidate scan
   int cap = 0;
   double *atom_stress = nullptr;
   double *rpart = nullptr;
@@ -141,7 +140,6 @@ ForceArgs force_args(comdgb_sim *h) {
   A.cap = h->cap;
   A.atom_stress = h->atom_stress;
   A.status = h->status;
-  A.mask = h->mixed ? h->nbr_mask : nullptr;
   return A;
 }
 
@@ -653,7 +651,6 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   h->cap = neighbor_capacity(s, rc);
   h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
   h->nbr_n = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
-  if (h->mixed) h->nbr_mask = track(h, dalloc<uint32_t>((size_t)h->ntot * NB_MASKW + 1, &err));
   h->atom_stress = track(h, dalloc<double>((size_t)h->ntot + 1, &err));
   h->nrpart = reduce_partials(h->ntot);
   h->rpart = track(h, dalloc<double>(2 * (size_t)h->nrpart, &err));

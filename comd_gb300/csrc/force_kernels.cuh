@@ -38,11 +38,7 @@ struct ForceArgs {
   int cap;
   double *atom_stress;   // [ntot] per-atom share of the scalar stress
   int *status;
-  uint32_t *mask;        // [ntot*NB_MASKW] FP32 path: hit bits per 32-candidate chunk
 };
-
-// candidates per box neighbourhood are at most 27*64, i.e. 54 chunks of 32
-#define NB_MASKW 54
 
 // Box offset of a stencil entry: FP64 value, or FP32 hi + lo parts.
 template <class T>
@@ -209,10 +205,17 @@ __device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
 }
 
 // FP32: candidates staged as (x - drbox, y - drbox, z - drbox, code) in the
-// centre box's frame; the cutoff of the build is widened by a hair so the
-// list is a superset of the pairs the passes accept with their exact dr.
+// centre box's frame, padded to whole 32-candidate chunks with far-away
+// sentinels.  Each warp takes two atoms per candidate load and parks every
+// chunk's ballot in warp-private shared memory; the warp then writes each
+// atom's list cooperatively (one mask word per lane, prefix sum of the
+// popcounts, each lane emits its own bits).  The cutoff of the build is
+// widened by a hair so the list is a superset of the pairs the passes accept
+// with their exact dr.
+#define NB_CHUNKS (NB_MAXC / 32)  // 54
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
   __shared__ __align__(16) float4 cand[NB_MAXC];
+  __shared__ uint32_t s_mask[NB_THREADS / 32][2][NB_CHUNKS];
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
   __shared__ BoxOff<float> s_dr[CG_NNBR];
   const int b = blockIdx.x;
@@ -220,132 +223,95 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
   if (ni == 0) return;
   const int ne = stage_entries<float>(A, b, s_box, s_off, s_dr);
   const int ncand = s_off[ne];
-  for (int c = threadIdx.x; c < ncand; c += NB_THREADS) {
-    int e = entry_of(s_off, ne, c);
-    int k = c - s_off[e];
-    float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
-    BoxOff<float> o = s_dr[e];
-    cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
-                          __int_as_float((e << 6) | k));
-  }
-  __syncthreads();
-  const float rc2b = rc2 * (1.0f + 4e-6f);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int i = warp; i < ni; i += NB_THREADS / 32) {
-    const float4 pi = __ldg(A.s.pos32 + b * CG_MAXATOMS + i);
-    const int a = A.box_start[b] + i;
-    if (a >= A.ntot) break;  // only after a reported overflow
-    uint16_t *out = A.nbr + (size_t)a * A.cap;
-    int cnt = 0;
-    for (int c0 = 0; c0 < ncand; c0 += 32) {
-      const int c = c0 + lane;
-      bool hit = false;
-      float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (c < ncand) {
-        q = cand[c];
-        float dx = pi.x - q.x, dy = pi.y - q.y, dz = pi.z - q.z;
-        float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        hit = (r2 <= rc2b) && (r2 > 0.f);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, hit);
-      const int pos = cnt + __popc(m & lt);
-      if (hit && pos < A.cap) out[pos] = (uint16_t)__float_as_int(q.w);
-      cnt += __popc(m);
-    }
-    if (lane == 0) {
-      A.nbr_n[a] = cnt;
-      if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
-    }
-  }
-}
-
-// FP32, bit-mask form: the same candidate test, but each warp takes two
-// atoms per candidate load and keeps only the 32-bit ballot of every chunk
-// (lane q % 32 holds chunk q); eam_pass1 decodes the bits into the list.
-static __global__ void __launch_bounds__(NB_THREADS) nbr_mask32_kernel(ForceArgs A, float rc2) {
-  __shared__ __align__(16) float4 cand[NB_MAXC];
-  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
-  __shared__ BoxOff<float> s_dr[CG_NNBR];
-  const int b = blockIdx.x;
-  const int ni = A.s.natoms[b];
-  if (ni == 0) return;
-  const int ne = stage_entries<float>(A, b, s_box, s_off, s_dr);
-  const int ncand = s_off[ne];
-  for (int c = threadIdx.x; c < ncand; c += NB_THREADS) {
-    int e = entry_of(s_off, ne, c);
-    int k = c - s_off[e];
-    float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
-    BoxOff<float> o = s_dr[e];
-    cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz, 0.f);
-  }
-  __syncthreads();
-  const float rc2b = rc2 * (1.0f + 4e-6f);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nchunk = (ncand + 31) >> 5;
+  for (int c = threadIdx.x; c < (nchunk << 5); c += NB_THREADS) {
+    if (c < ncand) {
+      int e = entry_of(s_off, ne, c);
+      int k = c - s_off[e];
+      float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
+      BoxOff<float> o = s_dr[e];
+      cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
+                            __int_as_float((e << 6) | k));
+    } else {
+      cand[c] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+    }
+  }
+  __syncthreads();
+  const float rc2b = rc2 * (1.0f + 4e-6f);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t *m0s = s_mask[warp][0], *m1s = s_mask[warp][1];
   for (int i0 = 2 * warp; i0 < ni; i0 += 2 * (NB_THREADS / 32)) {
-    const int i1 = (i0 + 1 < ni) ? i0 + 1 : i0;
+    const bool two = i0 + 1 < ni;
+    const int i1 = two ? i0 + 1 : i0;
     const float4 p0 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0);
     const float4 p1 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i1);
-    uint32_t k0a = 0, k0b = 0, k1a = 0, k1b = 0;  // kept masks, chunks lane and lane+32
     for (int q = 0; q < nchunk; q++) {
-      const int c = (q << 5) + lane;
-      bool h0 = false, h1 = false;
-      if (c < ncand) {
-        const float4 cq = cand[c];
-        float dx = p0.x - cq.x, dy = p0.y - cq.y, dz = p0.z - cq.z;
-        float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        h0 = (r2 <= rc2b) && (r2 > 0.f);
-        dx = p1.x - cq.x; dy = p1.y - cq.y; dz = p1.z - cq.z;
-        r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        h1 = (r2 <= rc2b) && (r2 > 0.f);
-      }
+      const float4 cq = cand[(q << 5) + lane];
+      float dx = p0.x - cq.x, dy = p0.y - cq.y, dz = p0.z - cq.z;
+      float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const bool h0 = (r2 <= rc2b) && (r2 > 0.f);
+      dx = p1.x - cq.x; dy = p1.y - cq.y; dz = p1.z - cq.z;
+      r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const bool h1 = (r2 <= rc2b) && (r2 > 0.f);
       const uint32_t m0 = __ballot_sync(0xffffffffu, h0);
       const uint32_t m1 = __ballot_sync(0xffffffffu, h1);
-      if ((q & 31) == lane) {
-        if (q < 32) { k0a = m0; k1a = m1; }
-        else { k0b = m0; k1b = m1; }
+      if (lane == 0) {
+        m0s[q] = m0;
+        m1s[q] = m1;
       }
     }
-    const int a0 = A.box_start[b] + i0, a1 = A.box_start[b] + i1;
-    if (a0 < A.ntot) {
-      uint32_t *o0 = A.mask + (size_t)a0 * NB_MASKW;
-      if (lane < nchunk) o0[lane] = k0a;
-      if (lane + 32 < nchunk) o0[lane + 32] = k0b;
+    __syncwarp();
+    for (int t = 0; t < (two ? 2 : 1); t++) {
+      const uint32_t *ms = t ? m1s : m0s;
+      const int a = A.box_start[b] + i0 + t;
+      if (a >= A.ntot) break;  // only after a reported overflow
+      // chunk words in candidate order: word w is held by lane w & 31 (w < 32
+      // in `lo`, w >= 32 in `hi`); inclusive prefix of the hit counts
+      const uint32_t lo = lane < nchunk ? ms[lane] : 0u;
+      const uint32_t hi = lane + 32 < nchunk ? ms[lane + 32] : 0u;
+      int xl = __popc(lo), xh = __popc(hi);
+      for (int o = 1; o < 32; o <<= 1) {
+        const int yl = __shfl_up_sync(0xffffffffu, xl, o);
+        const int yh = __shfl_up_sync(0xffffffffu, xh, o);
+        if (lane >= o) {
+          xl += yl;
+          xh += yh;
+        }
+      }
+      const int tot_lo = __shfl_sync(0xffffffffu, xl, 31);
+      const int total = tot_lo + __shfl_sync(0xffffffffu, xh, 31);
+      uint16_t *out = A.nbr + (size_t)a * A.cap;
+      // one hit per lane per round: find its word by binary search over the
+      // prefix, then its bit with fns
+      for (int h0 = 0; h0 < total; h0 += 32) {
+        const int h = h0 + lane;
+        const bool second = h >= tot_lo;
+        const int hh = second ? h - tot_lo : h;
+        int l = 0;
+        for (int step = 16; step > 0; step >>= 1) {
+          const int vl = __shfl_sync(0xffffffffu, xl, l + step - 1);
+          const int vh = __shfl_sync(0xffffffffu, xh, l + step - 1);
+          if ((second ? vh : vl) <= hh) l += step;
+        }
+        const int prev_l = __shfl_sync(0xffffffffu, xl, (l + 31) & 31);
+        const int prev_h = __shfl_sync(0xffffffffu, xh, (l + 31) & 31);
+        const uint32_t wl = __shfl_sync(0xffffffffu, lo, l);
+        const uint32_t wh = __shfl_sync(0xffffffffu, hi, l);
+        if (h < total && h < A.cap) {
+          const int before = l ? (second ? prev_h : prev_l) : 0;
+          const uint32_t word = second ? wh : wl;
+          const unsigned bit = __fns(word, 0, hh - before + 1);
+          const int c = ((second ? l + 32 : l) << 5) + (int)(bit & 31u);
+          if (bit < 32u && c < (nchunk << 5)) out[h] = (uint16_t)__float_as_int(cand[c].w);
+        }
+      }
+      if (lane == 0) {
+        A.nbr_n[a] = total;
+        if (total > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+      }
     }
-    if (i1 != i0 && a1 < A.ntot) {
-      uint32_t *o1 = A.mask + (size_t)a1 * NB_MASKW;
-      if (lane < nchunk) o1[lane] = k1a;
-      if (lane + 32 < nchunk) o1[lane + 32] = k1b;
-    }
+    __syncwarp();
   }
-}
-
-// Turn atom a's hit bits into its list of codes (entry << 6 | slot) in the
-// order of the candidates; returns the number of neighbours.  Offsets of the
-// stencil entries are rebuilt from the current box counts.
-__device__ __forceinline__ int decode_mask(const ForceArgs &A, int a, int b) {
-  const int ne = A.et.n[b];
-  int offs[CG_NNBR + 1];
-  offs[0] = 0;
-  for (int e = 0; e < ne; e++) offs[e + 1] = offs[e] + A.s.natoms[A.et.box[b * CG_NNBR + e]];
-  const int nchunk = (offs[ne] + 31) >> 5;
-  const uint32_t *m = A.mask + (size_t)a * NB_MASKW;
-  uint16_t *out = A.nbr + (size_t)a * A.cap;
-  int cnt = 0, e = 0;
-  for (int q = 0; q < nchunk; q++) {
-    uint32_t w = m[q];
-    while (w) {
-      const int c = (q << 5) + __ffs(w) - 1;
-      w &= w - 1;
-      while (c >= offs[e + 1]) e++;
-      if (cnt < A.cap) out[cnt] = (uint16_t)((e << 6) | (c - offs[e]));
-      cnt++;
-    }
-  }
-  A.nbr_n[a] = cnt;
-  if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
-  return cnt;
 }
 
 // FP64: the reference's dr = (drbox + r_i) - r_j, operation by operation
@@ -484,7 +450,6 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   const int b = slot >> 6, i = slot & 63;
   T xi, yi, zi;
   PrecT<T>::pos(A.s, slot, xi, yi, zi);
-  if (sizeof(T) == 4 && A.mask) decode_mask(A, a, b);
   typename PrecT<T>::Acc fx, fy, fz, ep, rh;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
   const T rc2 = P.rc2;
@@ -569,7 +534,6 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
   const int b = slot >> 6, i = slot & 63;
   T xi, yi, zi;
   PrecT<T>::pos(A.s, slot, xi, yi, zi);
-  if (sizeof(T) == 4 && A.mask) decode_mask(A, a, b);
   typename PrecT<T>::Acc fx, fy, fz, ep, sx;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
   const T s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6;

@@ -18,9 +18,7 @@ cudaError_t prepare_nbr_build<FT>() {
 
 template <>
 void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
-  if (sizeof(FT) == 4 && A.mask)
-    nbr_mask32_kernel<<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
-  else if (sizeof(FT) == 4)
+  if (sizeof(FT) == 4)
     nbr_build32_kernel<<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
   else
     nbr_build64_kernel<<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
