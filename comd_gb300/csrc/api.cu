@@ -282,6 +282,12 @@ void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
     c32.yo[s] = (float)(-(lo + b[s]) / (b[s] - lo));
     lo32.lo[s] = lo > a[s] ? (float)lo : -3.0e38f;
   }
+  // one recurrence serves phi, rho and dphi only if they share the interval
+  lo32.pair_shared = 1;
+  for (int s : {1, 3})
+    if (c32.a[s] != c32.a[0] || c32.ys[s] != c32.ys[0] || c32.yo[s] != c32.yo[0] ||
+        lo32.lo[s] != lo32.lo[0])
+      lo32.pair_shared = 0;
 }
 
 int fit_cheb_gpu(comdgb_sim *h, const eampotential_t *pot, double coef[6][CG_NCHEB],

@@ -112,6 +112,7 @@ struct ChebLow32 {
   float c[6][CG_NCHEB];
   float a[6], ys[6], yo[6];
   float lo[6];
+  int pair_shared;  // phi, rho, dphi re-expanded on one interval (same y)
 };
 
 __host__ __device__ inline void box_ixyz(const Geom &g, int b, int *ix) {
@@ -217,6 +218,32 @@ __device__ __forceinline__ float cheb_eval32(const float *c, float a, float ys, 
     dd = sv;
   }
   return fmaf(y, d, 0.5f * c[0] - dd);
+}
+
+// Three series on the same interval at one argument: the Chebyshev
+// polynomials T_k(y) from their three-term recurrence (shared by the three
+// sums), then sum c_k T_k with c_0 halved -- the same value as three
+// Clenshaw sums for two thirds of the FP32 operations.  Forward recurrence
+// and Clenshaw have the same FP32 accuracy for |y| <= 1 on these series.
+__device__ __forceinline__ void cheb3_eval32(const float *c0, const float *c1, const float *c2,
+                                             float a, float ys, float yo, float x, float &s0,
+                                             float &s1, float &s2) {
+  if (x < a) x = a;
+  const float y = fmaf(x, ys, yo);
+  const float y2 = 2.0f * y;
+  float tm = 1.0f, t = y;
+  s0 = fmaf(c0[1], y, 0.5f * c0[0]);
+  s1 = fmaf(c1[1], y, 0.5f * c1[0]);
+  s2 = fmaf(c2[1], y, 0.5f * c2[0]);
+#pragma unroll
+  for (int k = 2; k < CG_NCHEB; k++) {
+    const float tn = fmaf(y2, t, -tm);
+    tm = t;
+    t = tn;
+    s0 = fmaf(c0[k], t, s0);
+    s1 = fmaf(c1[k], t, s1);
+    s2 = fmaf(c2[k], t, s2);
+  }
 }
 
 }  // namespace cg

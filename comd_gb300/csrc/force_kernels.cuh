@@ -213,9 +213,10 @@ __device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
 // widened by a hair so the list is a superset of the pairs the passes accept
 // with their exact dr.
 #define NB_CHUNKS (NB_MAXC / 32)  // 54
+#define NB_ATOMS 4                 // atoms tested per candidate load
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
   __shared__ __align__(16) float4 cand[NB_MAXC];
-  __shared__ uint32_t s_mask[NB_THREADS / 32][2][NB_CHUNKS];
+  __shared__ uint32_t s_mask[NB_THREADS / 32][NB_ATOMS][NB_CHUNKS];
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
   __shared__ BoxOff<float> s_dr[CG_NNBR];
   const int b = blockIdx.x;
@@ -239,30 +240,34 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
   __syncthreads();
   const float rc2b = rc2 * (1.0f + 4e-6f);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t *m0s = s_mask[warp][0], *m1s = s_mask[warp][1];
-  for (int i0 = 2 * warp; i0 < ni; i0 += 2 * (NB_THREADS / 32)) {
-    const bool two = i0 + 1 < ni;
-    const int i1 = two ? i0 + 1 : i0;
-    const float4 p0 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0);
-    const float4 p1 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i1);
+  for (int i0 = NB_ATOMS * warp; i0 < ni; i0 += NB_ATOMS * (NB_THREADS / 32)) {
+    const int na = min(NB_ATOMS, ni - i0);
+    float4 pa[NB_ATOMS];
+#pragma unroll
+    for (int t = 0; t < NB_ATOMS; t++)
+      pa[t] = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0 + (t < na ? t : 0));
     for (int q = 0; q < nchunk; q++) {
       const float4 cq = cand[(q << 5) + lane];
-      float dx = p0.x - cq.x, dy = p0.y - cq.y, dz = p0.z - cq.z;
-      float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      const bool h0 = (r2 <= rc2b) && (r2 > 0.f);
-      dx = p1.x - cq.x; dy = p1.y - cq.y; dz = p1.z - cq.z;
-      r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      const bool h1 = (r2 <= rc2b) && (r2 > 0.f);
-      const uint32_t m0 = __ballot_sync(0xffffffffu, h0);
-      const uint32_t m1 = __ballot_sync(0xffffffffu, h1);
-      if (lane == 0) {
-        m0s[q] = m0;
-        m1s[q] = m1;
+#pragma unroll
+      for (int t = 0; t < NB_ATOMS; t++) {
+        const float dx = pa[t].x - cq.x, dy = pa[t].y - cq.y, dz = pa[t].z - cq.z;
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const uint32_t m = __ballot_sync(0xffffffffu, r2 <= rc2b);
+        if (lane == 0) s_mask[warp][t][q] = m;
       }
     }
     __syncwarp();
-    for (int t = 0; t < (two ? 2 : 1); t++) {
-      const uint32_t *ms = t ? m1s : m0s;
+    // the atom itself sits in every stencil entry of its own box (one entry
+    // unless nbx < 3): clear those bits
+    if (lane < na)
+      for (int e = 0; e < ne; e++)
+        if (s_box[e] == b) {
+          const int c = s_off[e] + i0 + lane;
+          s_mask[warp][lane][c >> 5] &= ~(1u << (c & 31));
+        }
+    __syncwarp();
+    for (int t = 0; t < na; t++) {
+      const uint32_t *ms = s_mask[warp][t];
       const int a = A.box_start[b] + i0 + t;
       if (a >= A.ntot) break;  // only after a reported overflow
       // chunk words in candidate order: word w is held by lane w & 31 (w < 32
@@ -410,10 +415,34 @@ __device__ __forceinline__ void r_and_inv(float r2, float &r, float &inv) {
   r = r2 * y;
 }
 
+// phi, phi' and rho of one pair distance from the FP32 series: the three
+// re-expanded series share the interval [lo, rc] and so one T_k recurrence
+template <int EVAL>
+__device__ __forceinline__ void cheb_pair32(const EamPot<float, EVAL> &P, float r, float &phi,
+                                            float &dphi, float &rho) {
+  if (P.chlo.pair_shared && r >= P.chlo.lo[0]) {
+    cheb3_eval32(P.ch.c[0], P.ch.c[3], P.ch.c[1], P.ch.a[0], P.ch.ys[0], P.ch.yo[0], r, phi,
+                 dphi, rho);
+  } else if (!P.chlo.pair_shared) {
+    phi = cheb_series(P, 0, r);
+    dphi = cheb_series(P, 3, r);
+    rho = cheb_series(P, 1, r);
+  } else {
+    phi = cheb_low32(P.chlo, 0, r);
+    dphi = cheb_low32(P.chlo, 3, r);
+    rho = cheb_low32(P.chlo, 1, r);
+  }
+}
+template <int EVAL>
+__device__ __forceinline__ void cheb_pair32(const EamPot<double, EVAL> &, double, double &,
+                                            double &, double &) {}
+
 template <class T, int EVAL>
 __device__ __forceinline__ void eam_pair_terms(const EamPot<T, EVAL> &P, T r, T &phi, T &dphi,
                                                T &rho) {
-  if (EVAL == EVAL_CHEBY) {
+  if (EVAL == EVAL_CHEBY && sizeof(T) == 4) {
+    cheb_pair32(P, r, phi, dphi, rho);
+  } else if (EVAL == EVAL_CHEBY) {
     phi = cheb_series(P, 0, r);
     dphi = cheb_series(P, 3, r);
     rho = cheb_series(P, 1, r);
