@@ -1,6 +1,7 @@
 // api.cu -- the C ABI of libcomdgb: device mirror of a simflat_t, the force
 // call, the velocity-Verlet loop (captured in CUDA graphs) and the drop-in
 // wrappers keyed by the caller's simflat_t pointer.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -81,6 +82,8 @@ struct comdgb_sim {
   std::vector<void *> allocs;
   Slots s{};
   RebinWork w{};
+  Persist pl{};        // persistent lists (all null when lists are rebuilt each step)
+  double skin = 0.0;
   EntryTab et{};
   double *dcenter = nullptr;
   int *boxc = nullptr;
@@ -140,6 +143,7 @@ ForceArgs force_args(comdgb_sim *h) {
   A.cap = h->cap;
   A.atom_stress = h->atom_stress;
   A.status = h->status;
+  A.pl = h->pl;
   return A;
 }
 
@@ -397,6 +401,8 @@ int check_status(comdgb_sim *h) {
                    CG_MAXATOMS);
   if (st[ST_ERROR] == COMDGB_ERR_BOXRANGE)
     return set_err(COMDGB_ERR_BOXRANGE, "an atom's box index fell outside the grid");
+  if (st[ST_ERROR] == COMDGB_ERR_ARG)
+    return set_err(COMDGB_ERR_ARG, "atom ids must be 0..ntot-1, each once (persistent lists)");
   if (st[ST_ERROR]) return set_err(st[ST_ERROR], "device error %d", st[ST_ERROR]);
   return 0;
 }
@@ -415,13 +421,18 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
                  st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   const int pot = h->opts.potential;
+  // persistent lists are built with rc + skin, and only when a rebuild is due
+  const double rcl = h->cutoff + h->skin;
   if (h->mixed) {
-    float rc2 = pot == COMDGB_POT_LJ ? h->lj32.rc2 : (float)(h->cutoff * h->cutoff);
+    float rc2 = h->pl.vlist ? (float)(rcl * rcl)
+                            : (pot == COMDGB_POT_LJ ? h->lj32.rc2 : (float)(h->cutoff * h->cutoff));
     launch_nbr_build<float>(A, rc2, st);
   } else {
-    double rc2 = pot == COMDGB_POT_LJ ? h->lj64.rc2 : h->cutoff * h->cutoff;
+    double rc2 = h->pl.vlist ? rcl * rcl
+                             : (pot == COMDGB_POT_LJ ? h->lj64.rc2 : h->cutoff * h->cutoff);
     launch_nbr_build<double>(A, rc2, st);
   }
+  if (h->pl.vlist) launch_rebuild_done(h->status, st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   if (pot == COMDGB_POT_LJ) {
     if (h->mixed) launch_lj<float>(A, h->lj32, st);
@@ -568,6 +579,10 @@ int upload(comdgb_sim *h, const simflat_t *s) {
   CK(cudaMemcpyAsync(h->s.fi, s->fi, ns * sizeof(double), cudaMemcpyHostToDevice, st));
   if (h->mixed) launch_pos32(h->g, h->s, st);
   CK(cudaMemsetAsync(h->status, 0, sizeof(int) * ST_COUNT, st));
+  if (h->pl.vlist) {  // new host state: map ids to slots and rebuild the lists
+    launch_slot_of(h->g, h->s, h->pl, h->ntot, h->status, st);
+    CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
+  }
   CK(cudaGetLastError());
   return 0;
 }
@@ -597,6 +612,30 @@ int download(comdgb_sim *h, simflat_t *s) {
   CK(cudaMemcpyAsync(s->p, h->stage3 + 3 * ns, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost,
                      st));
   return download_forces(h, s);
+}
+
+// Persistent lists need the full 27-box stencil of distinct boxes (periodic,
+// nbx >= 3), boxes at least rc + skin wide (so a list pair is always in
+// neighbouring boxes) and ids 0..ntot-1 (they key the lists).
+bool use_persistent_lists(comdgb_sim *h, const simflat_t *s, const comdgb_opts *o) {
+  if (o->potential < 0 || o->list_mode == COMDGB_LIST_PER_STEP || !o->periodic) return false;
+  double bmin = 1e300;
+  for (int j = 0; j < 3; j++) {
+    if (s->nbx[j] < 3) return false;
+    bmin = std::min(bmin, s->boxsize[j]);
+  }
+  double skin = o->skin > 0.0 ? o->skin : 0.3;
+  skin = std::min(skin, bmin - h->cutoff);
+  if (!(skin >= 0.1)) return false;
+  std::vector<char> seen((size_t)s->ntot, 0);
+  for (int b = 0; b < s->nboxes; b++)
+    for (int k = 0; k < s->natoms[b]; k++) {
+      int id = s->id[b * CG_MAXATOMS + k];
+      if (id < 0 || id >= s->ntot || seen[id]) return false;
+      seen[id] = 1;
+    }
+  h->skin = skin;
+  return true;
 }
 
 int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
@@ -655,7 +694,19 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   h->cpart = track(h, dalloc<int>(h->ncpart, &err));
   double rc = s->pot ? s->pot->cutoff : 1.0;
   h->cap = neighbor_capacity(s, rc);
-  h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
+  h->cutoff = rc;
+  if (use_persistent_lists(h, s, o)) {
+    h->pl.vcap = neighbor_capacity(s, rc + h->skin);
+    h->pl.vlist = track(h, dalloc<int>((size_t)h->ntot * h->pl.vcap + 4, &err));
+    h->pl.vcount = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
+    h->pl.slot_of = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
+    h->pl.rref = track(h, dalloc<d4>((size_t)h->ntot + 1, &err));
+    h->pl.half_skin2 = 0.25 * h->skin * h->skin;
+    h->w.pl = h->pl;
+    h->nbr = track(h, dalloc<uint16_t>(8, &err));  // per-step list unused
+  } else {
+    h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
+  }
   h->nbr_n = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
   h->atom_stress = track(h, dalloc<double>((size_t)h->ntot + 1, &err));
   h->nrpart = reduce_partials(h->ntot);
@@ -753,6 +804,8 @@ void comdgb_default_opts(comdgb_opts *o) {
   o->device = 0;
   o->n_cheby = CG_NCHEB;
   o->cheby_from_host = 0;
+  o->list_mode = COMDGB_LIST_AUTO;
+  o->skin = 0.3;
 }
 
 int comdgb_fp32_fma_peak(int device, double *tflops) {
@@ -874,6 +927,19 @@ int comdgb_sim_kinetic(comdgb_sim *h, double *ek) {
                  h->stream);
   CK(cudaMemcpyAsync(ek, h->d_out + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long *builds) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  if (persistent) *persistent = h->pl.vlist != nullptr;
+  if (skin) *skin = h->pl.vlist ? h->skin : 0.0;
+  if (builds) {
+    int st[ST_COUNT];
+    int rc = read_status(h, st);
+    if (rc) return rc;
+    *builds = st[ST_REBUILDS];
+  }
   return 0;
 }
 

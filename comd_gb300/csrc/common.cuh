@@ -43,6 +43,16 @@ __device__ __forceinline__ void box_ixyz_tab(const Geom &g, int b, int *ix) {
   ix[2] = (c >> 20) & 1023;
 }
 
+// world-frame position of a box-relative FP64 position: the box corner as
+// the reference computes dcenter (boxsize * index, domains.c:194-196) plus r
+__device__ __forceinline__ void world_pos(const Geom &g, int b, const d4 &r, double *w) {
+  int ix[3];
+  box_ixyz_tab(g, b, ix);
+  w[0] = g.boxsize[0] * (double)ix[0] + r.x;
+  w[1] = g.boxsize[1] * (double)ix[1] + r.y;
+  w[2] = g.boxsize[2] * (double)ix[2] + r.z;
+}
+
 // RN(a / b) from y = RN(1/b) with two fused multiply-adds (Markstein): the
 // residual a - b*q is exact and q + r*y rounds to the correctly rounded
 // quotient.  Used only when b's significand is not all ones (checked on
@@ -80,7 +90,21 @@ enum {
   ST_REBIN_SERIAL = 1,// set when the parallel rebin cannot reproduce reBoxAll
   ST_NBR_OVERFLOW = 2,// atoms whose neighbour list overflowed (handled)
   ST_SERIAL_RUNS = 3, // number of serial rebin fallbacks taken
+  ST_REBUILD = 4,     // persistent lists: an atom moved more than skin/2
+  ST_REBUILDS = 5,    // persistent lists: number of list builds
   ST_COUNT = 8
+};
+
+// Persistent (skin) neighbour lists, keyed by atom id: built with cutoff
+// rc + skin, rebuilt when an atom has moved more than skin/2 since the last
+// build.  Every member is null when lists are rebuilt each step.
+struct Persist {
+  int *vlist;        // [ntot*vcap] neighbour ids of atom id
+  int *vcount;       // [ntot] true neighbour count
+  int vcap;
+  int *slot_of;      // [ntot] current slot of atom id (kept by the rebin)
+  d4 *rref;          // [ntot] position (world frame, FP64) at the last build
+  double half_skin2; // (skin/2)^2
 };
 
 // tabulated function (potentialarray_t): v points at element 0, guards at

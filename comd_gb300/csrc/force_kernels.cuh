@@ -38,7 +38,27 @@ struct ForceArgs {
   int cap;
   double *atom_stress;   // [ntot] per-atom share of the scalar stress
   int *status;
+  Persist pl;            // persistent lists (pl.vlist == nullptr: per-step lists)
 };
+
+// Stencil entry of box jb seen from box b when both stencils are the full
+// 27 boxes in getNeighborBoxes order (periodic, nbx >= 3): (dx+1)*9 +
+// (dy+1)*3 + (dz+1) with the minimum-image box difference; -1 when the boxes
+// are not neighbours (then the atoms are farther apart than a box, i.e.
+// beyond the cutoff).
+__device__ __forceinline__ int stencil_entry(const Geom &g, int b, int jb) {
+  const int ci = __ldg(g.boxc + b), cj = __ldg(g.boxc + jb);
+  int e = 0;
+#pragma unroll
+  for (int ax = 0; ax < 3; ax++) {
+    int d = ((cj >> (10 * ax)) & 1023) - ((ci >> (10 * ax)) & 1023);
+    if (d > 1) d -= g.nbx[ax];
+    else if (d < -1) d += g.nbx[ax];
+    if (d > 1 || d < -1) return -1;
+    e = e * 3 + d + 1;
+  }
+  return e;
+}
 
 // Box offset of a stencil entry: FP64 value, or FP32 hi + lo parts.
 template <class T>
@@ -132,10 +152,46 @@ __device__ void scan_stencil(const ForceArgs &A, int b, int i, T xi, T yi, T zi,
   }
 }
 
+// Persistent list of atom (b, i): neighbour ids, looked up in their current
+// slots; the pair's box offset is the stencil entry of the two current boxes,
+// so dr is formed exactly as with the per-step list.
+template <class T, class F>
+__device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int b, int i, T xi, T yi,
+                                                    T zi, T rc2, F &&fn) {
+  const int idi = A.s.id[b * CG_MAXATOMS + i];
+  const int n = A.pl.vcount[idi];
+  if (n > A.pl.vcap) {
+    scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
+    return;
+  }
+  const int *lst = A.pl.vlist + (size_t)idi * A.pl.vcap;
+  for (int t0 = 0; t0 < n; t0 += 4) {
+    const int4 pk = *reinterpret_cast<const int4 *>(lst + t0);
+    const int w[4] = {pk.x, pk.y, pk.z, pk.w};
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      if (t0 + u < n) {
+        const int js = __ldg(A.pl.slot_of + w[u]);
+        const int e = stencil_entry(A.g, b, js >> 6);
+        if (e < 0) continue;
+        T xj, yj, zj, dx, dy, dz;
+        BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
+        PrecT<T>::pos(A.s, js, xj, yj, zj);
+        T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+        fn(js, dx, dy, dz, r2);
+      }
+    }
+  }
+}
+
 // Visit the atom's neighbour list (or its stencil when the list overflowed).
 template <class T, class F>
 __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int b, int i, T xi,
                                                   T yi, T zi, T rc2, F &&fn) {
+  if (A.pl.vlist) {
+    for_each_persistent<T>(A, b, i, xi, yi, zi, rc2, fn);
+    return;
+  }
   int n = A.nbr_n[a];
   if (n > A.cap) {
     scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
@@ -214,11 +270,48 @@ __device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
 // with their exact dr.
 #define NB_CHUNKS (NB_MAXC / 32)  // 54
 #define NB_ATOMS 4                 // atoms tested per candidate load
+// Persistent variant (PERSIST): runs only when a rebuild is due, writes
+// neighbour ids into the atom's id-keyed row and records its position.
+template <bool PERSIST>
+__device__ __forceinline__ bool build_skipped(const ForceArgs &A) {
+  return PERSIST && !*(volatile const int *)(A.status + ST_REBUILD);
+}
+
+// row of atom i of box b: list storage, count slot and capacity
+template <bool PERSIST>
+__device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i) {
+  if (PERSIST) {
+    const int slot = b * CG_MAXATOMS + i;
+    const int idi = A.s.id[slot];
+    double w[3];
+    world_pos(A.g, b, A.s.r[slot], w);
+    A.pl.rref[idi] = d4{w[0], w[1], w[2], 0.0};
+    return idi;
+  }
+  return A.box_start[b] + i;
+}
+
+template <bool PERSIST>
+__device__ __forceinline__ void build_store(const ForceArgs &A, int row, int h, int value) {
+  if (PERSIST) A.pl.vlist[(size_t)row * A.pl.vcap + h] = value;
+  else A.nbr[(size_t)row * A.cap + h] = (uint16_t)value;
+}
+
+template <bool PERSIST>
+__device__ __forceinline__ void build_count(const ForceArgs &A, int row, int total) {
+  const int cap = PERSIST ? A.pl.vcap : A.cap;
+  if (PERSIST) A.pl.vcount[row] = total;
+  else A.nbr_n[row] = total;
+  if (total > cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+}
+
+template <bool PERSIST>
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
   __shared__ __align__(16) float4 cand[NB_MAXC];
   __shared__ uint32_t s_mask[NB_THREADS / 32][NB_ATOMS][NB_CHUNKS];
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
   __shared__ BoxOff<float> s_dr[CG_NNBR];
+  if (build_skipped<PERSIST>(A)) return;
   const int b = blockIdx.x;
   const int ni = A.s.natoms[b];
   if (ni == 0) return;
@@ -231,8 +324,9 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
       int k = c - s_off[e];
       float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
       BoxOff<float> o = s_dr[e];
+      const int tag = PERSIST ? A.s.id[s_box[e] * CG_MAXATOMS + k] : ((e << 6) | k);
       cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
-                            __int_as_float((e << 6) | k));
+                            __int_as_float(tag));
     } else {
       cand[c] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
     }
@@ -268,8 +362,10 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
     __syncwarp();
     for (int t = 0; t < na; t++) {
       const uint32_t *ms = s_mask[warp][t];
-      const int a = A.box_start[b] + i0 + t;
-      if (a >= A.ntot) break;  // only after a reported overflow
+      if (!PERSIST && A.box_start[b] + i0 + t >= A.ntot) break;  // only after an overflow
+      const int row = (lane == 0) ? build_row<PERSIST>(A, b, i0 + t) : 0;
+      const int a = __shfl_sync(0xffffffffu, row, 0);
+      const int cap = PERSIST ? A.pl.vcap : A.cap;
       // chunk words in candidate order: word w is held by lane w & 31 (w < 32
       // in `lo`, w >= 32 in `hi`); inclusive prefix of the hit counts
       const uint32_t lo = lane < nchunk ? ms[lane] : 0u;
@@ -285,7 +381,6 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
       }
       const int tot_lo = __shfl_sync(0xffffffffu, xl, 31);
       const int total = tot_lo + __shfl_sync(0xffffffffu, xh, 31);
-      uint16_t *out = A.nbr + (size_t)a * A.cap;
       // one hit per lane per round: find its word by binary search over the
       // prefix, then its bit with fns
       for (int h0 = 0; h0 < total; h0 += 32) {
@@ -302,24 +397,23 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
         const int prev_h = __shfl_sync(0xffffffffu, xh, (l + 31) & 31);
         const uint32_t wl = __shfl_sync(0xffffffffu, lo, l);
         const uint32_t wh = __shfl_sync(0xffffffffu, hi, l);
-        if (h < total && h < A.cap) {
+        if (h < total && h < cap) {
           const int before = l ? (second ? prev_h : prev_l) : 0;
           const uint32_t word = second ? wh : wl;
           const unsigned bit = __fns(word, 0, hh - before + 1);
           const int c = ((second ? l + 32 : l) << 5) + (int)(bit & 31u);
-          if (bit < 32u && c < (nchunk << 5)) out[h] = (uint16_t)__float_as_int(cand[c].w);
+          if (bit < 32u && c < (nchunk << 5))
+            build_store<PERSIST>(A, a, h, __float_as_int(cand[c].w));
         }
       }
-      if (lane == 0) {
-        A.nbr_n[a] = total;
-        if (total > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
-      }
+      if (lane == 0) build_count<PERSIST>(A, a, total);
     }
     __syncwarp();
   }
 }
 
 // FP64: the reference's dr = (drbox + r_i) - r_j, operation by operation
+template <bool PERSIST>
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArgs A, double rc2) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double *cx = reinterpret_cast<double *>(smem_raw);
@@ -328,6 +422,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
   uint16_t *cc = reinterpret_cast<uint16_t *>(cz + NB_MAXC);
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
   __shared__ BoxOff<double> s_dr[CG_NNBR];
+  if (build_skipped<PERSIST>(A)) return;
   const int b = blockIdx.x;
   const int ni = A.s.natoms[b];
   if (ni == 0) return;
@@ -348,9 +443,10 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
   for (int i = warp; i < ni; i += NB_THREADS / 32) {
     double xi, yi, zi;
     PrecT<double>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
-    const int a = A.box_start[b] + i;
-    if (a >= A.ntot) break;
-    uint16_t *out = A.nbr + (size_t)a * A.cap;
+    if (!PERSIST && A.box_start[b] + i >= A.ntot) break;  // only after an overflow
+    const int row = (lane == 0) ? build_row<PERSIST>(A, b, i) : 0;
+    const int a = __shfl_sync(0xffffffffu, row, 0);
+    const int cap = PERSIST ? A.pl.vcap : A.cap;
     int cnt = 0;
     for (int c0 = 0; c0 < ncand; c0 += 32) {
       const int c = c0 + lane;
@@ -365,13 +461,13 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
       }
       const unsigned m = __ballot_sync(0xffffffffu, hit);
       const int pos = cnt + __popc(m & lt);
-      if (hit && pos < A.cap) out[pos] = code;
+      if (hit && pos < cap)
+        build_store<PERSIST>(A, a, pos,
+                             PERSIST ? A.s.id[s_box[code >> 6] * CG_MAXATOMS + (code & 63)]
+                                     : (int)code);
       cnt += __popc(m);
     }
-    if (lane == 0) {
-      A.nbr_n[a] = cnt;
-      if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
-    }
+    if (lane == 0) build_count<PERSIST>(A, a, cnt);
   }
 }
 
@@ -482,8 +578,10 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   typename PrecT<T>::Acc fx, fy, fz, ep, rh;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
   const T rc2 = P.rc2;
+  int npair = 0;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 > rc2) return;
+    npair++;
     T r, inv_r;
     r_and_inv(r2, r, inv_r);
     T phi, dphi, rho;
@@ -496,6 +594,7 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
     rh.add(rho);
   };
   for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+  if (A.pl.vlist) A.nbr_n[a] = npair;  // in-cutoff pairs (the skin list holds more)
   double rho_i = rh.value();
   T F, dF;
   eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
@@ -567,8 +666,10 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
   const T s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6;
   const T rc2 = P.rc2;
+  int npair = 0;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 > rc2) return;
+    npair++;
     T ir2 = T(1.0) / r2;
     T r6 = ir2 * ir2 * ir2;
     ep.add(T(0.5) * r6 * (s6 * r6 - T(1.0)));
@@ -579,6 +680,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
     sx.add(fr * dx * dx);
   };
   for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+  if (A.pl.vlist) A.nbr_n[a] = npair;
   // kinetic term: -p_x^2/m per non-empty stencil entry
   int ne = A.et.n[b], nonempty = 0;
   for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;

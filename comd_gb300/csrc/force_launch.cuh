@@ -12,16 +12,26 @@ static size_t nbr_build_smem() {
 template <>
 cudaError_t prepare_nbr_build<FT>() {
   if (sizeof(FT) == 4) return cudaSuccess;
-  return cudaFuncSetAttribute(nbr_build64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)nbr_build_smem());
+  cudaError_t e = cudaFuncSetAttribute(nbr_build64_kernel<false>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)nbr_build_smem());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(nbr_build64_kernel<true>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nbr_build_smem());
 }
 
 template <>
 void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
-  if (sizeof(FT) == 4)
-    nbr_build32_kernel<<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
-  else
-    nbr_build64_kernel<<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
+  const bool persist = A.pl.vlist != nullptr;
+  if (sizeof(FT) == 4) {
+    if (persist) nbr_build32_kernel<true><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+    else nbr_build32_kernel<false><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+  } else {
+    if (persist)
+      nbr_build64_kernel<true><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
+    else
+      nbr_build64_kernel<false><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
+  }
 }
 
 template <>

@@ -17,6 +17,7 @@ struct RebinWork {
   uint8_t *final_src;   // [nboxes*64] slot t <- old slot (<64) or placeholder 64+p
   uint8_t *dep_order;   // [nboxes*64] departure order (old slots)
   Slots stage;          // full records of departing atoms, indexed by old slot
+  Persist pl;           // persistent lists: id -> slot map to keep, displacement check
 };
 
 // ---- md_kernels.cu ----
@@ -54,6 +55,12 @@ void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, cons
                       int *tmp_index, int *status, cudaStream_t st);
 void launch_cheb_fit(const double *table_v, double x0, double xn, double invdx, int n_terms,
                      double *coef, double *dcoef, cudaStream_t st);
+
+// persistent lists: id -> slot map of the current layout (ids must be
+// 0..ntot-1; a duplicate or out-of-range id sets ST_ERROR to -1), and the
+// end of a (possible) rebuild
+void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, cudaStream_t st);
+void launch_rebuild_done(int *status, cudaStream_t st);
 
 // ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----
 template <class T>

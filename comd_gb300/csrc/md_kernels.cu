@@ -99,8 +99,10 @@ __device__ __forceinline__ float4 centred32(const Geom &g, double x, double y, d
                      (float)(z - 0.5 * g.boxsize[2]), 0.f);
 }
 
+// move one atom's record; with persistent lists also re-point its id
 __device__ __forceinline__ void copy_record(const Slots &dst, int ds, const Slots &src, int ss,
-                                            bool mixed) {
+                                            bool mixed, int *slot_of = nullptr) {
+  if (slot_of) slot_of[src.id[ss]] = ds;
   dst.id[ds] = src.id[ss];
   dst.itype[ds] = src.itype[ss];
   dst.mass[ds] = src.mass[ss];
@@ -200,6 +202,21 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt
         r.z = r.z + div_mass(dt_r * p.z, rmass, rinv);
         s.r[slot] = r;
         if (mixed) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
+        if (w.pl.rref) {
+          // persistent lists: rebuild once any atom moved more than skin/2
+          double wp[3];
+          world_pos(g, b, r, wp);
+          const d4 r0 = w.pl.rref[s.id[slot]];
+          const double r0v[3] = {r0.x, r0.y, r0.z};
+          double d2 = 0.0;
+          for (int k = 0; k < 3; k++) {
+            double d = wp[k] - r0v[k];
+            if (d > 0.5 * g.bounds[k]) d -= g.bounds[k];
+            else if (d < -0.5 * g.bounds[k]) d += g.bounds[k];
+            d2 += d * d;
+          }
+          if (d2 > w.pl.half_skin2) atomicExch(status + ST_REBUILD, 1);
+        }
       }
     }
   }
@@ -359,7 +376,8 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
   if (mask != 0ull)
     for (int t = 0; t < L; t++) {
       int e = fs[t];
-      if (e < CG_MAXATOMS && e != t) copy_record(s, base + t, s, base + e, mixed);
+      if (e < CG_MAXATOMS && e != t)
+        copy_record(s, base + t, s, base + e, mixed, w.pl.slot_of);
     }
   // 2. lower arrivals into their placeholders, in (source, departure) order
   if (n_lo > 0) {
@@ -376,7 +394,8 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
     }
     for (int t = 0; t < L; t++) {
       int e = fs[t];
-      if (e >= CG_MAXATOMS) copy_record(s, base + t, w.stage, src_of[e - CG_MAXATOMS], mixed);
+      if (e >= CG_MAXATOMS)
+        copy_record(s, base + t, w.stage, src_of[e - CG_MAXATOMS], mixed, w.pl.slot_of);
     }
   }
   // 3. higher arrivals appended
@@ -389,7 +408,7 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
     for (int d = 0; d < nd; d++) {
       int j = ord[d];
       if (w.dest[sb * CG_MAXATOMS + j] == b) {
-        copy_record(s, base + L + h, w.stage, sb * CG_MAXATOMS + j, mixed);
+        copy_record(s, base + L + h, w.stage, sb * CG_MAXATOMS + j, mixed, w.pl.slot_of);
         h++;
       }
     }
@@ -399,7 +418,7 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
 
 // reBoxAll replayed serially on the device (used only when the parallel plan
 // cannot reproduce it); the reference algorithm, statement for statement
-__global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status) {
+__global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, int *slot_of) {
   if (!*(volatile int *)(status + ST_REBIN_SERIAL)) return;
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   status[ST_SERIAL_RUNS] += 1;
@@ -435,11 +454,11 @@ __global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status) {
         set_error(status, -11);
         return;
       }
-      copy_record(s, jb * CG_MAXATOMS + nj, s, off, mixed);
+      copy_record(s, jb * CG_MAXATOMS + nj, s, off, mixed, slot_of);
       s.natoms[jb] = nj + 1;
       int ni = s.natoms[b] - 1;
       s.natoms[b] = ni;
-      if (ni) copy_record(s, off, s, b * CG_MAXATOMS + ni, mixed);
+      if (ni) copy_record(s, off, s, b * CG_MAXATOMS + ni, mixed, slot_of);
     }
   }
 }
@@ -449,7 +468,39 @@ void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w,
   unsigned nb = (unsigned)((g.nboxes + 127) / 128);
   rebin_plan_kernel<<<nb, 128, 0, st>>>(g, s, w, status);
   rebin_apply_kernel<<<nb, 128, 0, st>>>(g, s, mixed, w, status);
-  rebin_serial_kernel<<<1, 32, 0, st>>>(g, s, mixed, status);
+  rebin_serial_kernel<<<1, 32, 0, st>>>(g, s, mixed, status, w.pl.slot_of);
+}
+
+// ---------------------------------------------------------------------------
+// persistent lists: id -> slot map, end of a rebuild
+// ---------------------------------------------------------------------------
+__global__ void slot_of_kernel(Geom g, Slots s, Persist pl, int ntot, int *status) {
+  const long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
+  const int b = (int)(slot >> 6), k = (int)(slot & 63);
+  if (k >= s.natoms[b]) return;
+  const int id = s.id[slot];
+  if (id < 0 || id >= ntot) {
+    set_error(status, -1);
+    return;
+  }
+  if (atomicExch(pl.slot_of + id, (int)slot) != -1) set_error(status, -1);
+}
+
+void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, cudaStream_t st) {
+  cudaMemsetAsync(pl.slot_of, 0xff, sizeof(int) * (size_t)ntot, st);
+  slot_of_kernel<<<slot_blocks(g), 256, 0, st>>>(g, s, pl, ntot, status);
+}
+
+__global__ void rebuild_done_kernel(int *status) {
+  if (status[ST_REBUILD]) {
+    status[ST_REBUILDS] += 1;
+    status[ST_REBUILD] = 0;
+  }
+}
+
+void launch_rebuild_done(int *status, cudaStream_t st) {
+  rebuild_done_kernel<<<1, 1, 0, st>>>(status);
 }
 
 // ---------------------------------------------------------------------------

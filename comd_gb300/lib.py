@@ -30,7 +30,8 @@ P_SIM = C.POINTER(SimFlat)
 
 class Opts(C.Structure):
     _fields_ = [("potential", C.c_int), ("precision", C.c_int), ("periodic", C.c_int),
-                ("device", C.c_int), ("n_cheby", C.c_int), ("cheby_from_host", C.c_int)]
+                ("device", C.c_int), ("n_cheby", C.c_int), ("cheby_from_host", C.c_int),
+                ("list_mode", C.c_int), ("skin", C.c_double)]
 
 
 class ComdgbError(RuntimeError):
@@ -71,6 +72,8 @@ def _bind(lib):
                                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.comdgb_sim_graph_kernels.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.comdgb_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p
     L.comdgb_kernel_name.argtypes = [C.c_void_p, C.c_int]
     L.comdgb_eam_read.restype = C.POINTER(EamPotential)
@@ -129,9 +132,12 @@ def check(rc):
 
 
 def opts(potential=POT_EAM_TABLE, precision=PREC_FP64, periodic=True, device=0,
-         cheby_from_host=False):
+         cheby_from_host=False, per_step_lists=False, skin=None):
     o = Opts()
     load().comdgb_default_opts(C.byref(o))
+    o.list_mode = 1 if per_step_lists else 0
+    if skin is not None:
+        o.skin = skin
     o.potential = potential
     o.precision = precision
     o.periodic = int(periodic)
@@ -254,6 +260,12 @@ class DeviceSim:
 
     def synchronize(self):
         check(self.L.comdgb_sim_synchronize(self.h))
+
+    def list_info(self):
+        """(persistent lists in use, skin in A, persistent-list builds since upload)"""
+        p, sk, n = C.c_int(), C.c_double(), C.c_longlong()
+        check(self.L.comdgb_sim_list_info(self.h, C.byref(p), C.byref(sk), C.byref(n)))
+        return bool(p.value), sk.value, n.value
 
     def graph_kernels(self):
         a, b = C.c_int(), C.c_int()

@@ -67,7 +67,17 @@ typedef struct comdgb_opts {
   int device;      /* CUDA device ordinal */
   int n_cheby;     /* Chebyshev terms; only 32 is supported (NUM_CHEBY, docompute.c:56) */
   int cheby_from_host; /* 1: take the series from s->ch_pot; 0: fit them on the GPU */
+  int list_mode;       /* COMDGB_LIST_AUTO (default) or COMDGB_LIST_PER_STEP */
+  double skin;         /* persistent-list skin in Angstrom (default 0.3) */
 } comdgb_opts;
+
+/* Neighbour lists.  AUTO keeps lists across steps (cutoff rc + skin, keyed
+ * by atom id, rebuilt when an atom has moved more than skin/2) whenever the
+ * grid allows it: periodic, at least 3 boxes per axis, boxes at least
+ * rc + 0.1 A wide and ids 0..ntot-1; otherwise, and with PER_STEP, the list
+ * is rebuilt from the link cells at every force call.  Both give the same
+ * set of pairs within rc. */
+enum { COMDGB_LIST_AUTO = 0, COMDGB_LIST_PER_STEP = 1 };
 
 /* fills o with the reference defaults (EAM table, FP64, periodic, device 0) */
 void comdgb_default_opts(comdgb_opts *o);
@@ -128,6 +138,9 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms,
 const char *comdgb_kernel_name(comdgb_sim *h, int k);
 /* kernels launched per replay of the captured step graph / force graph */
 int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
+/* list mode in use (1 persistent, 0 per step), its skin, and the number of
+ * persistent-list builds since the last upload */
+int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long *builds);
 /* measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops); the
  * peak the mixed-precision force kernels are compared against */
 int comdgb_fp32_fma_peak(int device, double *tflops);

@@ -327,3 +327,37 @@ def test_dropin_force_and_steps(oracle):
         assert L.comdgb_detach(c.s) == 0
     finally:
         c.close()
+
+
+@pytest.mark.parametrize("precision", [cg.PREC_FP64, cg.PREC_MIXED])
+def test_persistent_lists_match_per_step_lists(oracle, precision):
+    """Lists kept across steps (skin) give the same forces as lists rebuilt
+    every step, and trajectories with several rebuilds track the oracle."""
+    c = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), temp=1200.0, amp=0.05)
+    try:
+        dp = cg.DeviceSim(c.s, cg.opts(cg.POT_EAM_CHEBY, precision, cheby_from_host=True,
+                                       skin=0.1))
+        ds = cg.DeviceSim(c.s, cg.opts(cg.POT_EAM_CHEBY, precision, cheby_from_host=True,
+                                       per_step_lists=True))
+        assert dp.list_info()[0] and not ds.list_info()[0]
+        ep, _ = dp.force()
+        es, _ = ds.force()
+        assert abs(ep - es) <= 1e-12 * abs(es)
+        n = 40
+        ep, _ = dp.steps(n, 1e-15)
+        es, _ = ds.steps(n, 1e-15)
+        persistent, skin, builds = dp.list_info()
+        assert builds >= 3, builds  # 1200 K with a 0.1 A skin rebuilds several times
+        assert dp.pair_count() == ds.pair_count()
+        if precision == cg.PREC_FP64:
+            assert c.oracle.steps(c.o, n, 1e-15, c.kind) == 0
+            assert abs(ep - c.o.contents.e) <= 1e-10 * abs(c.o.contents.e)
+            dp.download(c.s)
+            assert layout_equal(c.s, c.o)
+        else:
+            assert abs(ep - es) <= 1e-7 * abs(es)
+        dp.close()
+        ds.close()
+    finally:
+        c.close()
+
