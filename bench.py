@@ -303,6 +303,7 @@ def gpu_arm(args):
     mixed.synchronize()
     per_step_kernels, _ = mixed.graph_kernels()
 
+    persistent, skin, builds0 = mixed.list_info()
     clocks = ClockSampler(dev)
     clocks.start()
     dist.barrier()
@@ -311,6 +312,8 @@ def gpu_arm(args):
     mixed.synchronize()
     dist.barrier()
     clk = clocks.stop()
+    lists = {"persistent": persistent, "skin_A": skin,
+             "builds_in_timed_steps": mixed.list_info()[2] - builds0}
     elapsed_s = dist.max(span_ms / 1e3)
     value = dist.sum(natoms * args.steps) / elapsed_s
     pairs = mixed.pair_count()
@@ -426,7 +429,7 @@ def gpu_arm(args):
         "mixed_vs_fp64": (value / world / fp64_value) if fp64_value else None,
         "force_rel_rms_mixed_vs_fp64": ferr,
         "energy_drift_ha_per_atom": drift, "drift_steps": args.drift_steps,
-        "pairs_per_step": pairs, "pair_evals_per_s": pairs * args.steps / (span_ms / 1e3),
+        "neighbour_lists": lists, "pairs_per_step": pairs, "pair_evals_per_s": pairs * args.steps / (span_ms / 1e3),
         "kernel_groups": groups, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": per_step_kernels * args.steps, "clocks": clk,
     }

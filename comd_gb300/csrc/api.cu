@@ -506,6 +506,7 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool
   if (step) enqueue_step(h, dt_atu, nullptr);
   if (force) {
     int evi = 0;
+    if (h->pl.vlist) launch_skin_check(h->g, h->s, h->pl, h->mixed, h->status, h->stream);
     enqueue_force_parts(h, nullptr, evi);
     enqueue_reduce(h);
   }
@@ -700,13 +701,13 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
     h->pl.vlist = track(h, dalloc<int>((size_t)h->ntot * h->pl.vcap + 4, &err));
     h->pl.vcount = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
     h->pl.slot_of = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
-    h->pl.rref = track(h, dalloc<d4>((size_t)h->ntot + 1, &err));
-    h->pl.half_skin2 = 0.25 * h->skin * h->skin;
+    h->pl.rref = track(h, dalloc<float4>((size_t)h->ntot + 1, &err));
+    const double hs = 0.5 * h->skin - 2e-4;
+    h->pl.half_skin2 = (float)(hs * hs);
     h->w.pl = h->pl;
-    h->nbr = track(h, dalloc<uint16_t>(8, &err));  // per-step list unused
-  } else {
-    h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
   }
+  // per-step list: built each step, or (persistent lists) left by pass 1
+  h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
   h->nbr_n = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
   h->atom_stress = track(h, dalloc<double>((size_t)h->ntot + 1, &err));
   h->nrpart = reduce_partials(h->ntot);

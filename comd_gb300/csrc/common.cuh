@@ -43,16 +43,6 @@ __device__ __forceinline__ void box_ixyz_tab(const Geom &g, int b, int *ix) {
   ix[2] = (c >> 20) & 1023;
 }
 
-// world-frame position of a box-relative FP64 position: the box corner as
-// the reference computes dcenter (boxsize * index, domains.c:194-196) plus r
-__device__ __forceinline__ void world_pos(const Geom &g, int b, const d4 &r, double *w) {
-  int ix[3];
-  box_ixyz_tab(g, b, ix);
-  w[0] = g.boxsize[0] * (double)ix[0] + r.x;
-  w[1] = g.boxsize[1] * (double)ix[1] + r.y;
-  w[2] = g.boxsize[2] * (double)ix[2] + r.z;
-}
-
 // RN(a / b) from y = RN(1/b) with two fused multiply-adds (Markstein): the
 // residual a - b*q is exact and q + r*y rounds to the correctly rounded
 // quotient.  Used only when b's significand is not all ones (checked on
@@ -103,9 +93,40 @@ struct Persist {
   int *vcount;       // [ntot] true neighbour count
   int vcap;
   int *slot_of;      // [ntot] current slot of atom id (kept by the rebin)
-  d4 *rref;          // [ntot] position (world frame, FP64) at the last build
-  double half_skin2; // (skin/2)^2
+  float4 *rref;      // [ntot] position (world frame, FP32) at the last build
+  float half_skin2;  // (skin/2 - 2e-4 A)^2: FP32 world coordinates err by < 1e-4 A
 };
+
+// world-frame position in FP32 from the FP32 box-centred position (mixed
+// precision) or from the FP64 box-relative one; good to ~1e-4 A, used only
+// for the skin test
+__device__ __forceinline__ float4 world32(const Geom &g, int b, const float4 *pos32, long slot,
+                                          const d4 &r) {
+  int ix[3];
+  box_ixyz_tab(g, b, ix);
+  if (pos32) {
+    const float4 p = pos32[slot];
+    return make_float4(fmaf((float)ix[0] + 0.5f, (float)g.boxsize[0], p.x),
+                       fmaf((float)ix[1] + 0.5f, (float)g.boxsize[1], p.y),
+                       fmaf((float)ix[2] + 0.5f, (float)g.boxsize[2], p.z), 0.f);
+  }
+  return make_float4((float)(g.boxsize[0] * (double)ix[0] + r.x),
+                     (float)(g.boxsize[1] * (double)ix[1] + r.y),
+                     (float)(g.boxsize[2] * (double)ix[2] + r.z), 0.f);
+}
+
+// squared minimum-image distance between two FP32 world positions
+__device__ __forceinline__ float disp2(const Geom &g, float4 a, float4 b) {
+  float d[3] = {a.x - b.x, a.y - b.y, a.z - b.z};
+  float s = 0.f;
+  for (int k = 0; k < 3; k++) {
+    const float L = (float)g.bounds[k];
+    if (d[k] > 0.5f * L) d[k] -= L;
+    else if (d[k] < -0.5f * L) d[k] += L;
+    s = fmaf(d[k], d[k], s);
+  }
+  return s;
+}
 
 // tabulated function (potentialarray_t): v points at element 0, guards at
 // v[-1], v[n], v[n+1]

@@ -155,15 +155,20 @@ __device__ void scan_stencil(const ForceArgs &A, int b, int i, T xi, T yi, T zi,
 // Persistent list of atom (b, i): neighbour ids, looked up in their current
 // slots; the pair's box offset is the stencil entry of the two current boxes,
 // so dr is formed exactly as with the per-step list.
+// With `a` >= 0 the pairs within rc2 are also written, as slot codes, to the
+// per-step list of compact atom a (for the passes that follow).
 template <class T, class F>
-__device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int b, int i, T xi, T yi,
-                                                    T zi, T rc2, F &&fn) {
+__device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int a, int b, int i, T xi,
+                                                    T yi, T zi, T rc2, F &&fn) {
   const int idi = A.s.id[b * CG_MAXATOMS + i];
   const int n = A.pl.vcount[idi];
   if (n > A.pl.vcap) {
     scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
+    if (a >= 0) A.nbr_n[a] = A.cap + 1;  // later passes scan the stencil too
     return;
   }
+  uint16_t *emit = a >= 0 ? A.nbr + (size_t)a * A.cap : nullptr;
+  int cnt = 0;
   const int *lst = A.pl.vlist + (size_t)idi * A.pl.vcap;
   for (int t0 = 0; t0 < n; t0 += 4) {
     const int4 pk = *reinterpret_cast<const int4 *>(lst + t0);
@@ -178,18 +183,28 @@ __device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int b, i
         BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
         PrecT<T>::pos(A.s, js, xj, yj, zj);
         T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+        if (emit && r2 <= rc2) {
+          if (cnt < A.cap) emit[cnt] = (uint16_t)((e << 6) | (js & 63));
+          cnt++;
+        }
         fn(js, dx, dy, dz, r2);
       }
     }
   }
+  if (a >= 0) {
+    A.nbr_n[a] = cnt;
+    if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+  }
 }
 
 // Visit the atom's neighbour list (or its stencil when the list overflowed).
-template <class T, class F>
+// The first pass of a force call (PERSIST_FIRST) walks the persistent list
+// and leaves the exact per-step list for the passes after it.
+template <class T, bool PERSIST_FIRST = false, class F>
 __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int b, int i, T xi,
                                                   T yi, T zi, T rc2, F &&fn) {
-  if (A.pl.vlist) {
-    for_each_persistent<T>(A, b, i, xi, yi, zi, rc2, fn);
+  if (PERSIST_FIRST && A.pl.vlist) {
+    for_each_persistent<T>(A, a, b, i, xi, yi, zi, rc2, fn);
     return;
   }
   int n = A.nbr_n[a];
@@ -279,13 +294,11 @@ __device__ __forceinline__ bool build_skipped(const ForceArgs &A) {
 
 // row of atom i of box b: list storage, count slot and capacity
 template <bool PERSIST>
-__device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i) {
+__device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i, bool mixed) {
   if (PERSIST) {
     const int slot = b * CG_MAXATOMS + i;
     const int idi = A.s.id[slot];
-    double w[3];
-    world_pos(A.g, b, A.s.r[slot], w);
-    A.pl.rref[idi] = d4{w[0], w[1], w[2], 0.0};
+    A.pl.rref[idi] = world32(A.g, b, mixed ? A.s.pos32 : nullptr, slot, A.s.r[slot]);
     return idi;
   }
   return A.box_start[b] + i;
@@ -363,7 +376,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
     for (int t = 0; t < na; t++) {
       const uint32_t *ms = s_mask[warp][t];
       if (!PERSIST && A.box_start[b] + i0 + t >= A.ntot) break;  // only after an overflow
-      const int row = (lane == 0) ? build_row<PERSIST>(A, b, i0 + t) : 0;
+      const int row = (lane == 0) ? build_row<PERSIST>(A, b, i0 + t, true) : 0;
       const int a = __shfl_sync(0xffffffffu, row, 0);
       const int cap = PERSIST ? A.pl.vcap : A.cap;
       // chunk words in candidate order: word w is held by lane w & 31 (w < 32
@@ -444,7 +457,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
     double xi, yi, zi;
     PrecT<double>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
     if (!PERSIST && A.box_start[b] + i >= A.ntot) break;  // only after an overflow
-    const int row = (lane == 0) ? build_row<PERSIST>(A, b, i) : 0;
+    const int row = (lane == 0) ? build_row<PERSIST>(A, b, i, false) : 0;
     const int a = __shfl_sync(0xffffffffu, row, 0);
     const int cap = PERSIST ? A.pl.vcap : A.cap;
     int cnt = 0;
@@ -578,10 +591,8 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   typename PrecT<T>::Acc fx, fy, fz, ep, rh;
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
   const T rc2 = P.rc2;
-  int npair = 0;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 > rc2) return;
-    npair++;
     T r, inv_r;
     r_and_inv(r2, r, inv_r);
     T phi, dphi, rho;
@@ -593,8 +604,7 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
     ep.add(phi / T(2.0));
     rh.add(rho);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
-  if (A.pl.vlist) A.nbr_n[a] = npair;  // in-cutoff pairs (the skin list holds more)
+  for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, rc2, fn);
   double rho_i = rh.value();
   T F, dF;
   eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
@@ -666,10 +676,8 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
   fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
   const T s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6;
   const T rc2 = P.rc2;
-  int npair = 0;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 > rc2) return;
-    npair++;
     T ir2 = T(1.0) / r2;
     T r6 = ir2 * ir2 * ir2;
     ep.add(T(0.5) * r6 * (s6 * r6 - T(1.0)));
@@ -679,8 +687,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
     fz.add(dz * fr);
     sx.add(fr * dx * dx);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
-  if (A.pl.vlist) A.nbr_n[a] = npair;
+  for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, rc2, fn);
   // kinetic term: -p_x^2/m per non-empty stencil entry
   int ne = A.et.n[b], nonempty = 0;
   for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;

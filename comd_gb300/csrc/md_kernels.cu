@@ -202,20 +202,12 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt
         r.z = r.z + div_mass(dt_r * p.z, rmass, rinv);
         s.r[slot] = r;
         if (mixed) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
-        if (w.pl.rref) {
-          // persistent lists: rebuild once any atom moved more than skin/2
-          double wp[3];
-          world_pos(g, b, r, wp);
-          const d4 r0 = w.pl.rref[s.id[slot]];
-          const double r0v[3] = {r0.x, r0.y, r0.z};
-          double d2 = 0.0;
-          for (int k = 0; k < 3; k++) {
-            double d = wp[k] - r0v[k];
-            if (d > 0.5 * g.bounds[k]) d -= g.bounds[k];
-            else if (d < -0.5 * g.bounds[k]) d += g.bounds[k];
-            d2 += d * d;
-          }
-          if (d2 > w.pl.half_skin2) atomicExch(status + ST_REBUILD, 1);
+        if (!VEL && w.pl.rref) {
+          // persistent lists: the half step before a force call decides
+          // whether the lists are rebuilt (an atom moved more than skin/2)
+          const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
+          if (disp2(g, wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
+            atomicExch(status + ST_REBUILD, 1);
         }
       }
     }
@@ -497,6 +489,22 @@ __global__ void rebuild_done_kernel(int *status) {
     status[ST_REBUILDS] += 1;
     status[ST_REBUILD] = 0;
   }
+}
+
+// skin test of every atom (standalone force calls: positions may have moved
+// since the last half step that tested them)
+__global__ void skin_check_kernel(Geom g, Slots s, Persist pl, bool mixed, int *status) {
+  const long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
+  const int b = (int)(slot >> 6), k = (int)(slot & 63);
+  if (k >= s.natoms[b]) return;
+  const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, s.r[slot]);
+  if (disp2(g, wp, pl.rref[s.id[slot]]) > pl.half_skin2) atomicExch(status + ST_REBUILD, 1);
+}
+
+void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *status,
+                       cudaStream_t st) {
+  skin_check_kernel<<<slot_blocks(g), 256, 0, st>>>(g, s, pl, mixed, status);
 }
 
 void launch_rebuild_done(int *status, cudaStream_t st) {
