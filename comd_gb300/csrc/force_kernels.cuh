@@ -173,7 +173,7 @@ __device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int a, i
   for (int t0 = 0; t0 < n; t0 += 4) {
     const int4 pk = *reinterpret_cast<const int4 *>(lst + t0);
     const int w[4] = {pk.x, pk.y, pk.z, pk.w};
-#pragma unroll
+#pragma unroll 1
     for (int u = 0; u < 4; u++) {
       if (t0 + u < n) {
         const int js = __ldg(A.pl.slot_of + w[u]);
@@ -212,24 +212,20 @@ __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int
     scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
     return;
   }
-  const uint16_t *lst = A.nbr + (size_t)a * A.cap;
+  const uint32_t *lst = reinterpret_cast<const uint32_t *>(A.nbr + (size_t)a * A.cap);
   const int ebase = b * CG_NNBR;
-  for (int t0 = 0; t0 < n; t0 += 8) {
-    uint4 pk = *reinterpret_cast<const uint4 *>(lst + t0);
-    uint32_t w[4] = {pk.x, pk.y, pk.z, pk.w};
-#pragma unroll
-    for (int u = 0; u < 8; u++) {
-      if (t0 + u < n) {
-        uint32_t code = (w[u >> 1] >> ((u & 1) * 16)) & 0xffffu;
-        int e = code >> 6, k = code & 63;
-        int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
-        T xj, yj, zj, dx, dy, dz;
-        BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
-        PrecT<T>::pos(A.s, js, xj, yj, zj);
-        T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
-        fn(js, dx, dy, dz, r2);
-      }
-    }
+  // one copy of the pair code in the loop body: the list is read two codes
+  // per 32-bit word
+#pragma unroll 1
+  for (int t = 0; t < n; t++) {
+    const uint32_t code = (__ldg(lst + (t >> 1)) >> ((t & 1) * 16)) & 0xffffu;
+    const int e = code >> 6, k = code & 63;
+    const int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
+    T xj, yj, zj, dx, dy, dz;
+    BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
+    PrecT<T>::pos(A.s, js, xj, yj, zj);
+    T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+    fn(js, dx, dy, dz, r2);
   }
 }
 
@@ -485,6 +481,23 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
 }
 
 // ---------------------------------------------------------------------------
+// persistent lists: the exact per-step list of each atom (pairs within the
+// cutoff, as slot codes) from its skin list, so the force passes evaluate no
+// pair beyond the cutoff
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void __launch_bounds__(128) persist_filter_kernel(ForceArgs A, T rc2) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= A.ntot) return;
+  const int slot = A.atom_slot[a];
+  const int b = slot >> 6, i = slot & 63;
+  T xi, yi, zi;
+  PrecT<T>::pos(A.s, slot, xi, yi, zi);
+  auto none = [](int, T, T, T, T) {};
+  for_each_persistent<T>(A, a, b, i, xi, yi, zi, rc2, none);
+}
+
+// ---------------------------------------------------------------------------
 // EAM pass 1 (+ embedding): phi, phi', rho per pair; F, F' per atom
 // ---------------------------------------------------------------------------
 template <class T, int EVAL>
@@ -604,7 +617,7 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
     ep.add(phi / T(2.0));
     rh.add(rho);
   };
-  for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, rc2, fn);
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
   double rho_i = rh.value();
   T F, dF;
   eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
@@ -687,7 +700,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
     fz.add(dz * fr);
     sx.add(fr * dx * dx);
   };
-  for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, rc2, fn);
+  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
   // kinetic term: -p_x^2/m per non-empty stencil entry
   int ne = A.et.n[b], nonempty = 0;
   for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
