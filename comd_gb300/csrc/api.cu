@@ -470,10 +470,17 @@ void enqueue_reduce(comdgb_sim *h) {
   launch_reduce(A, h->rpart, h->ripart, h->nrpart, h->d_out, h->d_iout, h->stream);
 }
 
+// atom list (atom -> slot) of the current layout
+void enqueue_compact(comdgb_sim *h) {
+  launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
+                 h->stream);
+}
+
 void enqueue_rebox(comdgb_sim *h) {
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), h->stream);
-  launch_classify(h->g, h->s, h->mixed, h->w, h->status, h->stream);
+  launch_classify(h->g, h->s, h->atom_slot, h->ntot, h->mixed, h->w, h->status, h->stream);
   enqueue_classify_finish(h);
+  enqueue_compact(h);
 }
 
 // one velocity-Verlet step (timestep.c:129-132); ev: optional group events
@@ -481,17 +488,20 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev) {
   int evi = 0;
   cudaStream_t st = h->stream;
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+  // the atom list is the one made after the previous rebin
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
-  launch_advance_positions(h->g, h->s, dt_atu / 2.0, h->rmass, h->mixed, true, h->w, h->status,
-                           st);
+  launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass, h->mixed,
+                           true, h->w, h->status, st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_classify_finish(h);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-  enqueue_force_parts(h, ev, evi);
+  enqueue_force_parts(h, ev, evi);  // starts with the atom list of the new layout
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
-  launch_advance_vp(h->g, h->s, dt_atu, dt_atu / 2.0, h->rmass, h->mixed, h->w, h->status, st);
+  launch_advance_vp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass, h->mixed,
+                    h->w, h->status, st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_classify_finish(h);
+  enqueue_compact(h);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
 }
 
@@ -514,6 +524,8 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool
   if (step) enqueue_step(h, dt_atu, nullptr);
   if (force) {
     int evi = 0;
+    // the last half step of a step leaves the FP32 copy stale
+    if (h->mixed) launch_pos32(h->g, h->s, h->stream);
     if (h->pl.vlist) launch_skin_check(h->g, h->s, h->pl, h->mixed, h->status, h->stream);
     enqueue_force_parts(h, nullptr, evi);
     enqueue_reduce(h);
@@ -592,6 +604,7 @@ int upload(comdgb_sim *h, const simflat_t *s) {
     launch_slot_of(h->g, h->s, h->pl, h->ntot, h->status, st);
     CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
   }
+  enqueue_compact(h);
   CK(cudaGetLastError());
   return 0;
 }
@@ -904,7 +917,7 @@ int comdgb_sim_rebox(comdgb_sim *h) {
 int comdgb_sim_advance_velocity(comdgb_sim *h, double dt) {
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   CK(cudaSetDevice(h->device));
-  launch_advance_velocity(h->g, h->s, dt, h->stream);
+  launch_advance_velocity(h->g, h->s, h->atom_slot, h->ntot, dt, h->stream);
   CK(cudaGetLastError());
   return check_status(h);
 }
@@ -913,9 +926,10 @@ int comdgb_sim_advance_positions(comdgb_sim *h, double dt) {
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   CK(cudaSetDevice(h->device));
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), h->stream);
-  launch_advance_positions(h->g, h->s, dt, h->rmass, h->mixed, true, h->w, h->status,
-                           h->stream);
+  launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt, h->rmass, h->mixed, true, h->w,
+                           h->status, h->stream);
   enqueue_classify_finish(h);
+  enqueue_compact(h);
   CK(cudaGetLastError());
   return check_status(h);
 }

@@ -198,34 +198,34 @@ __device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int a, i
 }
 
 // Visit the atom's neighbour list (or its stencil when the list overflowed).
-// The first pass of a force call (PERSIST_FIRST) walks the persistent list
-// and leaves the exact per-step list for the passes after it.
-template <class T, bool PERSIST_FIRST = false, class F>
+// UNROLL copies of the pair code per loop trip: 1 for the heavy first pass
+// (code size), more for the light passes (independent gathers in flight).
+template <class T, int UNROLL = 1, class F>
 __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int b, int i, T xi,
                                                   T yi, T zi, T rc2, F &&fn) {
-  if (PERSIST_FIRST && A.pl.vlist) {
-    for_each_persistent<T>(A, a, b, i, xi, yi, zi, rc2, fn);
-    return;
-  }
   int n = A.nbr_n[a];
   if (n > A.cap) {
     scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
     return;
   }
-  const uint32_t *lst = reinterpret_cast<const uint32_t *>(A.nbr + (size_t)a * A.cap);
+  const uint16_t *lst = A.nbr + (size_t)a * A.cap;
   const int ebase = b * CG_NNBR;
-  // one copy of the pair code in the loop body: the list is read two codes
-  // per 32-bit word
 #pragma unroll 1
-  for (int t = 0; t < n; t++) {
-    const uint32_t code = (__ldg(lst + (t >> 1)) >> ((t & 1) * 16)) & 0xffffu;
-    const int e = code >> 6, k = code & 63;
-    const int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
-    T xj, yj, zj, dx, dy, dz;
-    BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
-    PrecT<T>::pos(A.s, js, xj, yj, zj);
-    T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
-    fn(js, dx, dy, dz, r2);
+  for (int t0 = 0; t0 < n; t0 += UNROLL) {
+#pragma unroll
+    for (int u = 0; u < UNROLL; u++) {
+      const int t = t0 + u;
+      if (t < n) {
+        const uint32_t code = __ldg(lst + t);
+        const int e = code >> 6, k = code & 63;
+        const int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
+        T xj, yj, zj, dx, dy, dz;
+        BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
+        PrecT<T>::pos(A.s, js, xj, yj, zj);
+        T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+        fn(js, dx, dy, dz, r2);
+      }
+    }
   }
 }
 
@@ -487,14 +487,49 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
 // ---------------------------------------------------------------------------
 template <class T>
 __global__ void __launch_bounds__(128) persist_filter_kernel(ForceArgs A, T rc2) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= A.ntot) return;
+  // one warp per atom, one skin-list entry per lane: the gathers of 32
+  // entries are in flight together; hits are compacted in list order
+  const int a = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (a >= A.ntot) return;  // whole warps
   const int slot = A.atom_slot[a];
   const int b = slot >> 6, i = slot & 63;
+  const int idi = A.s.id[slot];
+  const int n = A.pl.vcount[idi];
+  if (n > A.pl.vcap) {  // overflowed skin list: the passes scan the stencil
+    if (lane == 0) A.nbr_n[a] = A.cap + 1;
+    return;
+  }
   T xi, yi, zi;
   PrecT<T>::pos(A.s, slot, xi, yi, zi);
-  auto none = [](int, T, T, T, T) {};
-  for_each_persistent<T>(A, a, b, i, xi, yi, zi, rc2, none);
+  const int *lst = A.pl.vlist + (size_t)idi * A.pl.vcap;
+  uint16_t *out = A.nbr + (size_t)a * A.cap;
+  const unsigned lt = (1u << lane) - 1u;
+  int cnt = 0;
+  for (int t0 = 0; t0 < n; t0 += 32) {
+    const int t = t0 + lane;
+    bool hit = false;
+    int code = 0;
+    if (t < n) {
+      const int js = __ldg(A.pl.slot_of + __ldg(lst + t));
+      const int e = stencil_entry(A.g, b, js >> 6);
+      if (e >= 0) {
+        T xj, yj, zj, dx, dy, dz;
+        BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
+        PrecT<T>::pos(A.s, js, xj, yj, zj);
+        hit = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz) <= rc2;
+        code = (e << 6) | (js & 63);
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    const int pos = cnt + __popc(m & lt);
+    if (hit && pos < A.cap) out[pos] = (uint16_t)code;
+    cnt += __popc(m);
+  }
+  if (lane == 0) {
+    A.nbr_n[a] = cnt;
+    if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -659,7 +694,7 @@ __global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, E
     fz.add(wr * dz);
     sx.add(wr * dx * dx);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+  for_each_neighbor<T, 4>(A, a, b, i, xi, yi, zi, rc2, fn);
   d4 fo = A.s.f[slot];
   fo.x += fx.value();
   fo.y += fy.value();

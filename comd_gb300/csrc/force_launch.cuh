@@ -36,7 +36,8 @@ void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
 
 template <>
 void launch_persist_filter<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
-  if (A.ntot > 0) persist_filter_kernel<FT><<<(A.ntot + 127) / 128, 128, 0, st>>>(A, rc2);
+  if (A.ntot > 0)
+    persist_filter_kernel<FT><<<(unsigned)(((long)A.ntot * 32 + 127) / 128), 128, 0, st>>>(A, rc2);
 }
 
 template <>

@@ -25,17 +25,22 @@ struct RebinWork {
 void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, int *boxc,
                         cudaStream_t st);
 double mass_reciprocal(double rmass);
+// The Verlet and classify kernels run one thread per atom of the compacted
+// atom list atom_slot (which must match the current layout).
 // r += dt*p/rmass (and optionally the classify step of reBoxAll)
-void launch_advance_positions(const Geom &g, Slots s, double dt, double rmass, bool mixed,
-                              bool classify, const RebinWork &w, int *status, cudaStream_t st);
-// p -= dt_v*f; r += dt_r*p/rmass; classify
-void launch_advance_vp(const Geom &g, Slots s, double dt_v, double dt_r, double rmass,
-                       bool mixed, const RebinWork &w, int *status, cudaStream_t st);
+void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
+                              double rmass, bool mixed, bool classify, const RebinWork &w,
+                              int *status, cudaStream_t st);
+// p -= dt_v*f; r += dt_r*p/rmass; classify (the FP32 copy is not refreshed)
+void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                       double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
+                       cudaStream_t st);
 // p -= dt_v*f only (advanceVelocity)
-void launch_advance_velocity(const Geom &g, Slots s, double dt_v, cudaStream_t st);
+void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                             cudaStream_t st);
 // classify only (reBoxAll without a position update)
-void launch_classify(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
-                     cudaStream_t st);
+void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
+                     const RebinWork &w, int *status, cudaStream_t st);
 // plan + apply + serial fallback; must follow a classify launch
 void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
                          cudaStream_t st);

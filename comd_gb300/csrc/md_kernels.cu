@@ -114,58 +114,53 @@ __device__ __forceinline__ void copy_record(const Slots &dst, int ds, const Slot
   if (mixed) dst.pos32[ds] = src.pos32[ss];
 }
 
-// classify one slot; r is the (possibly just advanced) position
-__device__ __forceinline__ void classify_slot(const Geom &g, const Slots &s, int slot, bool valid,
-                                              d4 r, bool mixed, const RebinWork &w,
-                                              int *status) {
+// classify one atom; r is its (possibly just advanced) position.  A
+// departing atom sets its bit in depmask (cleared before the launch), records
+// its destination and copies its record, with the moved position, to the stage.
+__device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int slot, d4 r,
+                                              bool mixed, const RebinWork &w, int *status) {
   const int b = slot >> 6;
-  bool dep = false;
-  if (valid) {
-    int ixo[3], ixn[3];
-    box_ixyz_tab(g, b, ixo);
-    double rn[3] = {r.x, r.y, r.z};
-    double rc[3] = {r.x, r.y, r.z};
-    for (int k = 0; k < 3; k++) {
-      if (rc[k] < 0.0) {
-        ixn[k] = ixo[k] - 1;
-        rn[k] += g.boxsize[k];
-      } else if (rc[k] >= g.boxsize[k]) {
-        ixn[k] = ixo[k] + 1;
-        rn[k] -= g.boxsize[k];
-      } else {
-        ixn[k] = ixo[k];
-      }
-    }
-    int jb = box_from_ixyz(g, ixn);
-    if (jb >= 0 && jb != b) {
-      dep = true;
-      w.dest[slot] = jb;
-      Slots st = w.stage;
-      st.id[slot] = s.id[slot];
-      st.itype[slot] = s.itype[slot];
-      st.mass[slot] = s.mass[slot];
-      st.r[slot] = d4{rn[0], rn[1], rn[2], 0.0};
-      st.p[slot] = s.p[slot];
-      st.f[slot] = s.f[slot];
-      st.rho[slot] = s.rho[slot];
-      st.fi[slot] = s.fi[slot];
-      if (mixed) st.pos32[slot] = centred32(g, rn[0], rn[1], rn[2]);
-      if (jb > b) {
-        // re-examined in jb's scan: must stay there
-        int ix2[3], ix3[3];
-        box_ixyz_tab(g, jb, ix2);
-        for (int k = 0; k < 3; k++) {
-          if (rn[k] < 0.0) ix3[k] = ix2[k] - 1;
-          else if (rn[k] >= g.boxsize[k]) ix3[k] = ix2[k] + 1;
-          else ix3[k] = ix2[k];
-        }
-        int jb2 = box_from_ixyz(g, ix3);
-        if (jb2 >= 0 && jb2 != jb) atomicExch(status + ST_REBIN_SERIAL, 1);
-      }
+  int ixo[3], ixn[3];
+  box_ixyz_tab(g, b, ixo);
+  double rn[3] = {r.x, r.y, r.z};
+  const double rc[3] = {r.x, r.y, r.z};
+  for (int k = 0; k < 3; k++) {
+    if (rc[k] < 0.0) {
+      ixn[k] = ixo[k] - 1;
+      rn[k] += g.boxsize[k];
+    } else if (rc[k] >= g.boxsize[k]) {
+      ixn[k] = ixo[k] + 1;
+      rn[k] -= g.boxsize[k];
+    } else {
+      ixn[k] = ixo[k];
     }
   }
-  unsigned m = __ballot_sync(0xffffffffu, dep);
-  if ((threadIdx.x & 31) == 0) w.depmask[slot >> 5] = m;
+  const int jb = box_from_ixyz(g, ixn);
+  if (jb < 0 || jb == b) return;
+  atomicOr(w.depmask + (slot >> 5), 1u << (slot & 31));
+  w.dest[slot] = jb;
+  Slots st = w.stage;
+  st.id[slot] = s.id[slot];
+  st.itype[slot] = s.itype[slot];
+  st.mass[slot] = s.mass[slot];
+  st.r[slot] = d4{rn[0], rn[1], rn[2], 0.0};
+  st.p[slot] = s.p[slot];
+  st.f[slot] = s.f[slot];
+  st.rho[slot] = s.rho[slot];
+  st.fi[slot] = s.fi[slot];
+  if (mixed) st.pos32[slot] = centred32(g, rn[0], rn[1], rn[2]);
+  if (jb > b) {
+    // re-examined in jb's scan: must stay there
+    int ix2[3], ix3[3];
+    box_ixyz_tab(g, jb, ix2);
+    for (int k = 0; k < 3; k++) {
+      if (rn[k] < 0.0) ix3[k] = ix2[k] - 1;
+      else if (rn[k] >= g.boxsize[k]) ix3[k] = ix2[k] + 1;
+      else ix3[k] = ix2[k];
+    }
+    const int jb2 = box_from_ixyz(g, ix3);
+    if (jb2 >= 0 && jb2 != jb) atomicExch(status + ST_REBIN_SERIAL, 1);
+  }
 }
 
 // division by the (constant) mass: Markstein when rinv != 0, else IEEE
@@ -173,52 +168,56 @@ __device__ __forceinline__ double div_mass(double a, double rmass, double rinv) 
   return rinv != 0.0 ? div_markstein(a, rmass, rinv) : a / rmass;
 }
 
+// One thread per atom of the compacted atom list (every lane of every warp
+// holds an atom, so no FP64 instruction is issued for an empty slot).
+// write32: also refresh the FP32 copy of the position (mixed precision; the
+// half step that ends a step skips it, the next one rewrites it first).
 template <bool POS, bool VEL>
-__global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, double dt_v, double dt_r,
+__global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int *atom_slot,
+                                                      int ntot, double dt_v, double dt_r,
                                                       double rmass, double rinv, bool mixed,
-                                                      bool classify, RebinWork w, int *status) {
-  const long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int nslots = g.nboxes * CG_MAXATOMS;
-  if (slot >= nslots) return;  // nslots is a multiple of 64: whole warps exit
-  const int b = (int)(slot >> 6), k = (int)(slot & 63);
-  const bool valid = k < s.natoms[b];
-  d4 r = d4{0.0, 0.0, 0.0, 0.0};
-  if (valid) {
-    r = s.r[slot];
-    if (POS || VEL) {
-      d4 p = s.p[slot];
-      if (VEL) {
-        // advanceVelocity, timestep.c:71
-        d4 f = s.f[slot];
-        p.x = p.x - dt_v * f.x;
-        p.y = p.y - dt_v * f.y;
-        p.z = p.z - dt_v * f.z;
-        s.p[slot] = p;
-      }
-      if (POS) {
-        // advancePositions, timestep.c:104: r + (dt*p)/rmass
-        r.x = r.x + div_mass(dt_r * p.x, rmass, rinv);
-        r.y = r.y + div_mass(dt_r * p.y, rmass, rinv);
-        r.z = r.z + div_mass(dt_r * p.z, rmass, rinv);
-        s.r[slot] = r;
-        if (mixed) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
-        if (!VEL && w.pl.rref) {
-          // persistent lists: the half step before a force call decides
-          // whether the lists are rebuilt (an atom moved more than skin/2)
-          const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
-          if (disp2(g, wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
-            atomicExch(status + ST_REBUILD, 1);
-        }
+                                                      bool write32, bool classify, RebinWork w,
+                                                      int *status) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= ntot) return;
+  const int slot = atom_slot[a];
+  const int b = slot >> 6;
+  d4 r = s.r[slot];
+  if (POS || VEL) {
+    d4 p = s.p[slot];
+    if (VEL) {
+      // advanceVelocity, timestep.c:71
+      d4 f = s.f[slot];
+      p.x = p.x - dt_v * f.x;
+      p.y = p.y - dt_v * f.y;
+      p.z = p.z - dt_v * f.z;
+      s.p[slot] = p;
+    }
+    if (POS) {
+      // advancePositions, timestep.c:104: r + (dt*p)/rmass
+      r.x = r.x + div_mass(dt_r * p.x, rmass, rinv);
+      r.y = r.y + div_mass(dt_r * p.y, rmass, rinv);
+      r.z = r.z + div_mass(dt_r * p.z, rmass, rinv);
+      s.r[slot] = r;
+      if (mixed && write32) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
+      if (!VEL && w.pl.rref) {
+        // persistent lists: the half step before a force call decides
+        // whether the lists are rebuilt (an atom moved more than skin/2)
+        const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
+        if (disp2(g, wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
+          atomicExch(status + ST_REBUILD, 1);
       }
     }
   }
-  if (classify) classify_slot(g, s, (int)slot, valid, r, mixed, w, status);
+  if (classify) classify_atom(g, s, slot, r, mixed, w, status);
 }
 
 static unsigned slot_blocks(const Geom &g) {
   long nslots = (long)g.nboxes * CG_MAXATOMS;
   return (unsigned)((nslots + 255) / 256);
 }
+
+static unsigned atom_blocks(int ntot) { return (unsigned)((ntot + 255) / 256); }
 
 // y = RN(1/b) when Markstein's division is exact for b, else 0 (IEEE path)
 double mass_reciprocal(double rmass) {
@@ -229,28 +228,40 @@ double mass_reciprocal(double rmass) {
   return 1.0 / rmass;
 }
 
-void launch_advance_positions(const Geom &g, Slots s, double dt, double rmass, bool mixed,
-                              bool classify, const RebinWork &w, int *status, cudaStream_t st) {
-  advance_kernel<true, false><<<slot_blocks(g), 256, 0, st>>>(
-      g, s, 0.0, dt, rmass, mass_reciprocal(rmass), mixed, classify, w, status);
+void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
+                              double rmass, bool mixed, bool classify, const RebinWork &w,
+                              int *status, cudaStream_t st) {
+  if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
+  if (ntot > 0)
+    advance_kernel<true, false><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, 0.0, dt, rmass, mass_reciprocal(rmass), mixed, true, classify, w,
+        status);
 }
 
-void launch_advance_vp(const Geom &g, Slots s, double dt_v, double dt_r, double rmass,
-                       bool mixed, const RebinWork &w, int *status, cudaStream_t st) {
-  advance_kernel<true, true><<<slot_blocks(g), 256, 0, st>>>(
-      g, s, dt_v, dt_r, rmass, mass_reciprocal(rmass), mixed, true, w, status);
+void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                       double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
+                       cudaStream_t st) {
+  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
+  if (ntot > 0)
+    advance_kernel<true, true><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, dt_v, dt_r, rmass, mass_reciprocal(rmass), mixed, false, true, w,
+        status);
 }
 
-void launch_advance_velocity(const Geom &g, Slots s, double dt_v, cudaStream_t st) {
+void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                             cudaStream_t st) {
   RebinWork none{};
-  advance_kernel<false, true><<<slot_blocks(g), 256, 0, st>>>(g, s, dt_v, 0.0, 1.0, 0.0, false,
-                                                              false, none, nullptr);
+  if (ntot > 0)
+    advance_kernel<false, true><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, none, nullptr);
 }
 
-void launch_classify(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
-                     cudaStream_t st) {
-  advance_kernel<false, false><<<slot_blocks(g), 256, 0, st>>>(g, s, 0.0, 0.0, 1.0, 0.0, mixed,
-                                                               true, w, status);
+void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
+                     const RebinWork &w, int *status, cudaStream_t st) {
+  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
+  if (ntot > 0)
+    advance_kernel<false, false><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, w, status);
 }
 
 // distinct stencil boxes of b other than b, ascending
