@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(128) persist_filter_kernel(ForceArgs A, T rc2)
   const int lane = threadIdx.x & 31;
   if (a >= A.ntot) return;  // whole warps
   const int slot = A.atom_slot[a];
-  const int b = slot >> 6, i = slot & 63;
+  const int b = slot >> 6;
   const int idi = A.s.id[slot];
   const int n = A.pl.vcount[idi];
   if (n > A.pl.vcap) {  // overflowed skin list: the passes scan the stencil
