@@ -432,15 +432,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
                              : (pot == COMDGB_POT_LJ ? h->lj64.rc2 : h->cutoff * h->cutoff);
     launch_nbr_build<double>(A, rc2, st);
   }
-  if (h->pl.vlist) {
-    launch_rebuild_done(h->status, st);
-    const double rc = h->cutoff;
-    if (h->mixed)
-      launch_persist_filter<float>(
-          A, pot == COMDGB_POT_LJ ? h->lj32.rc2 : (float)(rc * rc), st);
-    else
-      launch_persist_filter<double>(A, pot == COMDGB_POT_LJ ? h->lj64.rc2 : rc * rc, st);
-  }
+  if (h->pl.vlist) launch_rebuild_done(h->status, st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   if (pot == COMDGB_POT_LJ) {
     if (h->mixed) launch_lj<float>(A, h->lj32, st);

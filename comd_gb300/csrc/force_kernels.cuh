@@ -170,26 +170,20 @@ __device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int a, i
   uint16_t *emit = a >= 0 ? A.nbr + (size_t)a * A.cap : nullptr;
   int cnt = 0;
   const int *lst = A.pl.vlist + (size_t)idi * A.pl.vcap;
-  for (int t0 = 0; t0 < n; t0 += 4) {
-    const int4 pk = *reinterpret_cast<const int4 *>(lst + t0);
-    const int w[4] = {pk.x, pk.y, pk.z, pk.w};
 #pragma unroll 1
-    for (int u = 0; u < 4; u++) {
-      if (t0 + u < n) {
-        const int js = __ldg(A.pl.slot_of + w[u]);
-        const int e = stencil_entry(A.g, b, js >> 6);
-        if (e < 0) continue;
-        T xj, yj, zj, dx, dy, dz;
-        BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
-        PrecT<T>::pos(A.s, js, xj, yj, zj);
-        T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
-        if (emit && r2 <= rc2) {
-          if (cnt < A.cap) emit[cnt] = (uint16_t)((e << 6) | (js & 63));
-          cnt++;
-        }
-        fn(js, dx, dy, dz, r2);
-      }
+  for (int t = 0; t < n; t++) {
+    const int js = __ldg(A.pl.slot_of + __ldg(lst + t));
+    const int e = stencil_entry(A.g, b, js >> 6);
+    if (e < 0) continue;
+    T xj, yj, zj, dx, dy, dz;
+    BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
+    PrecT<T>::pos(A.s, js, xj, yj, zj);
+    T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+    if (emit && r2 <= rc2) {
+      if (cnt < A.cap) emit[cnt] = (uint16_t)((e << 6) | (js & 63));
+      cnt++;
     }
+    fn(js, dx, dy, dz, r2);
   }
   if (a >= 0) {
     A.nbr_n[a] = cnt;
@@ -198,34 +192,46 @@ __device__ __forceinline__ void for_each_persistent(const ForceArgs &A, int a, i
 }
 
 // Visit the atom's neighbour list (or its stencil when the list overflowed).
-// UNROLL copies of the pair code per loop trip: 1 for the heavy first pass
-// (code size), more for the light passes (independent gathers in flight).
-template <class T, int UNROLL = 1, class F>
+// The first pass of a force call with persistent lists (PERSIST_FIRST)
+// walks the skin list instead and leaves the exact per-step list behind.
+// VEC: read eight codes per 16-byte load and unroll over them (light
+// passes: independent gathers in flight); otherwise one copy of the pair
+// code in the loop (heavy passes: instruction cache).
+template <class T, bool VEC = false, bool PERSIST_FIRST = false, class F>
 __device__ __forceinline__ void for_each_neighbor(const ForceArgs &A, int a, int b, int i, T xi,
                                                   T yi, T zi, T rc2, F &&fn) {
-  int n = A.nbr_n[a];
+  if (PERSIST_FIRST && A.pl.vlist) {
+    for_each_persistent<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+    return;
+  }
+  const int n = A.nbr_n[a];
   if (n > A.cap) {
     scan_stencil<T>(A, b, i, xi, yi, zi, rc2, fn);
     return;
   }
-  const uint16_t *lst = A.nbr + (size_t)a * A.cap;
   const int ebase = b * CG_NNBR;
-#pragma unroll 1
-  for (int t0 = 0; t0 < n; t0 += UNROLL) {
+  auto visit = [&](uint32_t code) {
+    const int e = code >> 6, k = code & 63;
+    const int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
+    T xj, yj, zj, dx, dy, dz;
+    BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
+    PrecT<T>::pos(A.s, js, xj, yj, zj);
+    T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
+    fn(js, dx, dy, dz, r2);
+  };
+  if (VEC) {
+    const uint16_t *lst = A.nbr + (size_t)a * A.cap;
+    for (int t0 = 0; t0 < n; t0 += 8) {
+      const uint4 pk = *reinterpret_cast<const uint4 *>(lst + t0);
+      const uint32_t w[4] = {pk.x, pk.y, pk.z, pk.w};
 #pragma unroll
-    for (int u = 0; u < UNROLL; u++) {
-      const int t = t0 + u;
-      if (t < n) {
-        const uint32_t code = __ldg(lst + t);
-        const int e = code >> 6, k = code & 63;
-        const int js = __ldg(A.et.box + ebase + e) * CG_MAXATOMS + k;
-        T xj, yj, zj, dx, dy, dz;
-        BoxOff<T> bo = PrecT<T>::drbox(A.et, ebase + e);
-        PrecT<T>::pos(A.s, js, xj, yj, zj);
-        T r2 = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz);
-        fn(js, dx, dy, dz, r2);
-      }
+      for (int u = 0; u < 8; u++)
+        if (t0 + u < n) visit((w[u >> 1] >> ((u & 1) * 16)) & 0xffffu);
     }
+  } else {
+    const uint32_t *lst = reinterpret_cast<const uint32_t *>(A.nbr + (size_t)a * A.cap);
+#pragma unroll 1
+    for (int t = 0; t < n; t++) visit((__ldg(lst + (t >> 1)) >> ((t & 1) * 16)) & 0xffffu);
   }
 }
 
@@ -481,58 +487,6 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
 }
 
 // ---------------------------------------------------------------------------
-// persistent lists: the exact per-step list of each atom (pairs within the
-// cutoff, as slot codes) from its skin list, so the force passes evaluate no
-// pair beyond the cutoff
-// ---------------------------------------------------------------------------
-template <class T>
-__global__ void __launch_bounds__(128) persist_filter_kernel(ForceArgs A, T rc2) {
-  // one warp per atom, one skin-list entry per lane: the gathers of 32
-  // entries are in flight together; hits are compacted in list order
-  const int a = (int)(((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (a >= A.ntot) return;  // whole warps
-  const int slot = A.atom_slot[a];
-  const int b = slot >> 6;
-  const int idi = A.s.id[slot];
-  const int n = A.pl.vcount[idi];
-  if (n > A.pl.vcap) {  // overflowed skin list: the passes scan the stencil
-    if (lane == 0) A.nbr_n[a] = A.cap + 1;
-    return;
-  }
-  T xi, yi, zi;
-  PrecT<T>::pos(A.s, slot, xi, yi, zi);
-  const int *lst = A.pl.vlist + (size_t)idi * A.pl.vcap;
-  uint16_t *out = A.nbr + (size_t)a * A.cap;
-  const unsigned lt = (1u << lane) - 1u;
-  int cnt = 0;
-  for (int t0 = 0; t0 < n; t0 += 32) {
-    const int t = t0 + lane;
-    bool hit = false;
-    int code = 0;
-    if (t < n) {
-      const int js = __ldg(A.pl.slot_of + __ldg(lst + t));
-      const int e = stencil_entry(A.g, b, js >> 6);
-      if (e >= 0) {
-        T xj, yj, zj, dx, dy, dz;
-        BoxOff<T> bo = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
-        PrecT<T>::pos(A.s, js, xj, yj, zj);
-        hit = pair_r2(bo, xi, yi, zi, xj, yj, zj, dx, dy, dz) <= rc2;
-        code = (e << 6) | (js & 63);
-      }
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, hit);
-    const int pos = cnt + __popc(m & lt);
-    if (hit && pos < A.cap) out[pos] = (uint16_t)code;
-    cnt += __popc(m);
-  }
-  if (lane == 0) {
-    A.nbr_n[a] = cnt;
-    if (cnt > A.cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // EAM pass 1 (+ embedding): phi, phi', rho per pair; F, F' per atom
 // ---------------------------------------------------------------------------
 template <class T, int EVAL>
@@ -652,7 +606,7 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
     ep.add(phi / T(2.0));
     rh.add(rho);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+  for_each_neighbor<T, false, true>(A, a, b, i, xi, yi, zi, rc2, fn);
   double rho_i = rh.value();
   T F, dF;
   eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
@@ -694,7 +648,7 @@ __global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, E
     fz.add(wr * dz);
     sx.add(wr * dx * dx);
   };
-  for_each_neighbor<T, 4>(A, a, b, i, xi, yi, zi, rc2, fn);
+  for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, rc2, fn);
   d4 fo = A.s.f[slot];
   fo.x += fx.value();
   fo.y += fy.value();
@@ -735,7 +689,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
     fz.add(dz * fr);
     sx.add(fr * dx * dx);
   };
-  for_each_neighbor<T>(A, a, b, i, xi, yi, zi, rc2, fn);
+  for_each_neighbor<T, false, true>(A, a, b, i, xi, yi, zi, rc2, fn);
   // kinetic term: -p_x^2/m per non-empty stencil entry
   int ne = A.et.n[b], nonempty = 0;
   for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;

@@ -35,12 +35,6 @@ void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
 }
 
 template <>
-void launch_persist_filter<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
-  if (A.ntot > 0)
-    persist_filter_kernel<FT><<<(unsigned)(((long)A.ntot * 32 + 127) / 128), 128, 0, st>>>(A, rc2);
-}
-
-template <>
 void launch_eam_pass1<FT, EVAL_TABLE>(const ForceArgs &A, const EamPot<FT, EVAL_TABLE> &P,
                                       cudaStream_t st) {
   if (A.ntot > 0) eam_pass1_kernel<FT, EVAL_TABLE><<<(A.ntot + 127) / 128, 128, 0, st>>>(A, P);

@@ -74,8 +74,6 @@ template <class T>
 cudaError_t prepare_nbr_build();
 template <class T>
 void launch_nbr_build(const ForceArgs &A, T rc2, cudaStream_t st);
-template <class T>
-void launch_persist_filter(const ForceArgs &A, T rc2, cudaStream_t st);
 template <class T, int EVAL>
 void launch_eam_pass1(const ForceArgs &A, const EamPot<T, EVAL> &P, cudaStream_t st);
 template <class T, int EVAL>
