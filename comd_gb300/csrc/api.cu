@@ -83,6 +83,7 @@ struct comdgb_sim {
   Slots s{};
   RebinWork w{};
   Persist pl{};        // persistent lists (all null when lists are rebuilt each step)
+  ForceOrder fo{};     // mixed precision: persistent lists in force order
   double skin = 0.0;
   EntryTab et{};
   double *dcenter = nullptr;
@@ -144,6 +145,7 @@ ForceArgs force_args(comdgb_sim *h) {
   A.atom_stress = h->atom_stress;
   A.status = h->status;
   A.pl = h->pl;
+  A.fo = h->fo;
   return A;
 }
 
@@ -294,6 +296,88 @@ void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
       lo32.pair_shared = 0;
 }
 
+// Segment table of the FP32 pair path (PairSeg): phi, phi'/r, rho, rho'/r
+// of the FP64 series as cubics in s = r^2 on [lo^2, rc^2], lo = max(pair_lo,
+// series lower ends).  Each cubic interpolates the function at the 4
+// Chebyshev nodes of its segment; the result is checked at 9 points per
+// segment and the table is dropped (series path) if any function errs by
+// more than 1e-7 of its largest magnitude on the interval.  Returns 0, or
+// -1 when device memory ran out.
+int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
+                   const double b[6], double pair_lo, double rc, PairSeg *out) {
+  *out = PairSeg{nullptr, nullptr, 3.0e38f, 1.0f, 0};
+  double lo = pair_lo;
+  for (int s : {0, 1, 3, 4}) lo = std::max(lo, a[s]);
+  if (!(lo > 0.0 && lo < rc)) return 0;
+  const int n = SEG_N;
+  const float s_lo = (float)(lo * lo);
+  const float inv_h = (float)(n / (rc * rc - (double)s_lo));
+  const double h_s = 1.0 / (double)inv_h;
+  auto fn = [&](int q, double s) {
+    double r = sqrt(s);
+    switch (q) {
+      case 0: return cheb_host(coef[0], a[0], b[0], r);
+      case 1: return cheb_host(coef[3], a[3], b[3], r) / r;
+      case 2: return cheb_host(coef[1], a[1], b[1], r);
+      default: return cheb_host(coef[4], a[4], b[4], r) / r;
+    }
+  };
+  const double PI = 3.141592653589793;
+  double tn[4], tj[4][4];  // nodes in t and T_j(2 t_m - 1)
+  for (int m = 0; m < 4; m++) {
+    tn[m] = 0.5 + 0.5 * cos(PI * (m + 0.5) / 4.0);
+    double y = 2.0 * tn[m] - 1.0;
+    tj[m][0] = 1.0;
+    tj[m][1] = y;
+    tj[m][2] = 2.0 * y * y - 1.0;
+    tj[m][3] = y * (4.0 * y * y - 3.0);
+  }
+  std::vector<double> mono((size_t)4 * n * 4);  // [q][k][4]
+  double fmax[4] = {0, 0, 0, 0}, emax[4] = {0, 0, 0, 0};
+  for (int q = 0; q < 4; q++) {
+    for (int k = 0; k < n; k++) {
+      double fv[4], c[4] = {0, 0, 0, 0};
+      for (int m = 0; m < 4; m++) fv[m] = fn(q, (double)s_lo + (k + tn[m]) * h_s);
+      for (int j = 0; j < 4; j++) {
+        for (int m = 0; m < 4; m++) c[j] += fv[m] * tj[m][j];
+        c[j] *= 0.5;  // 2/4; c0 enters halved below
+      }
+      // sum_j c_j T_j(2t-1) with c0 halved, in powers of t
+      double *mk = &mono[((size_t)q * n + k) * 4];
+      mk[0] = 0.5 * c[0] - c[1] + c[2] - c[3];
+      mk[1] = 2.0 * c[1] - 8.0 * c[2] + 18.0 * c[3];
+      mk[2] = 8.0 * c[2] - 48.0 * c[3];
+      mk[3] = 32.0 * c[3];
+      for (int e = 0; e <= 8; e++) {
+        double t = e / 8.0, ex = fn(q, (double)s_lo + (k + t) * h_s);
+        double p = ((mk[3] * t + mk[2]) * t + mk[1]) * t + mk[0];
+        fmax[q] = std::max(fmax[q], fabs(ex));
+        emax[q] = std::max(emax[q], fabs(p - ex));
+      }
+    }
+    if (!(emax[q] <= 1e-7 * fmax[q])) return 0;
+  }
+  std::vector<float4> p1((size_t)3 * n), p2((size_t)n);
+  for (int k = 0; k < n; k++)
+    for (int q = 0; q < 4; q++) {
+      const double *mk = &mono[((size_t)q * n + k) * 4];
+      float4 v = make_float4((float)mk[0], (float)mk[1], (float)mk[2], (float)mk[3]);
+      if (q < 3) p1[(size_t)3 * k + q] = v;
+      else p2[k] = v;
+    }
+  int err = 0;
+  float4 *d1 = track(h, dalloc<float4>(p1.size(), &err));
+  float4 *d2 = track(h, dalloc<float4>(p2.size(), &err));
+  if (err) return -1;
+  if (cudaMemcpy(d1, p1.data(), sizeof(float4) * p1.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess ||
+      cudaMemcpy(d2, p2.data(), sizeof(float4) * p2.size(), cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+    return -1;
+  *out = PairSeg{d1, d2, s_lo, inv_h, n};
+  return 0;
+}
+
 int fit_cheb_gpu(comdgb_sim *h, const eampotential_t *pot, double coef[6][CG_NCHEB],
                  double a[6], double b[6]) {
   int err = 0;
@@ -381,6 +465,8 @@ int setup_potential(comdgb_sim *h, const simflat_t *s) {
   // potential's lattice take the reference coefficients (never in practice)
   double pair_lo = ep->lat > 0 ? 0.75 * ep->lat / sqrt(2.0) : 0.0;
   fill_cheb(h->eam64c.ch, h->eam32c.ch, h->eam32c.chlo, coef, a, b, pair_lo);
+  if (build_pair_seg(h, coef, a, b, pair_lo, h->cutoff, &h->eam32c.seg))
+    return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for the pair segment table");
   h->eam64c.rc2 = rc2;
   h->eam32c.rc2 = (float)rc2;
   return 0;
@@ -423,6 +509,28 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
   const int pot = h->opts.potential;
   // persistent lists are built with rc + skin, and only when a rebuild is due
   const double rcl = h->cutoff + h->skin;
+  if (h->fo.list) {
+    // force order: positions of this step (and the rebuild test), then the
+    // list build if due, then the passes
+    launch_fo_refresh(h->g, h->s, h->fo, h->pl.slot_of, h->ntot, h->status, st);
+    launch_nbr_build<float>(A, (float)(rcl * rcl), st);
+    launch_rebuild_done(h->status, st);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    if (pot == COMDGB_POT_LJ) {
+      launch_fo_lj(A, h->lj32, st);
+      if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    } else if (pot == COMDGB_POT_EAM_TABLE) {
+      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 0, st);
+      if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 1, st);
+    } else {
+      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 0, st);
+      if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 1, st);
+    }
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    return;
+  }
   if (h->mixed) {
     float rc2 = h->pl.vlist ? (float)(rcl * rcl)
                             : (pot == COMDGB_POT_LJ ? h->lj32.rc2 : (float)(h->cutoff * h->cutoff));
@@ -592,7 +700,7 @@ int upload(comdgb_sim *h, const simflat_t *s) {
   CK(cudaMemcpyAsync(h->s.fi, s->fi, ns * sizeof(double), cudaMemcpyHostToDevice, st));
   if (h->mixed) launch_pos32(h->g, h->s, st);
   CK(cudaMemsetAsync(h->status, 0, sizeof(int) * ST_COUNT, st));
-  if (h->pl.vlist) {  // new host state: map ids to slots and rebuild the lists
+  if (h->pl.slot_of) {  // new host state: map ids to slots and rebuild the lists
     launch_slot_of(h->g, h->s, h->pl, h->ntot, h->status, st);
     CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
   }
@@ -710,13 +818,34 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   h->cap = neighbor_capacity(s, rc);
   h->cutoff = rc;
   if (use_persistent_lists(h, s, o)) {
-    h->pl.vcap = neighbor_capacity(s, rc + h->skin);
-    h->pl.vlist = track(h, dalloc<int>((size_t)h->ntot * h->pl.vcap + 4, &err));
-    h->pl.vcount = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
-    h->pl.slot_of = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
-    h->pl.rref = track(h, dalloc<float4>((size_t)h->ntot + 1, &err));
-    const double hs = 0.5 * h->skin - 2e-4;
-    h->pl.half_skin2 = (float)(hs * hs);
+    const int vcap = neighbor_capacity(s, rc + h->skin);
+    const size_t n1 = (size_t)h->ntot + 1;
+    h->pl.slot_of = track(h, dalloc<int>(n1, &err));
+    if (h->mixed && h->ntot < (1 << 27)) {
+      // force order: rows padded to whole warps of 32 atoms
+      const size_t rows = ((size_t)h->ntot + 31) / 32 * 32;
+      h->fo.vcap = vcap;
+      h->fo.list = track(h, dalloc<uint32_t>(rows * vcap, &err));
+      h->fo.n = track(h, dalloc<int>(n1, &err));
+      h->fo.id = track(h, dalloc<int>(n1, &err));
+      h->fo.ref = track(h, dalloc<d4>(n1, &err));
+      h->fo.pos = track(h, dalloc<float4>(n1, &err));
+      h->fo.slot = track(h, dalloc<int>(n1, &err));
+      h->fo.fi = track(h, dalloc<float>(n1, &err));
+      for (int k = 0; k < 3; k++) {
+        h->fo.hi[k] = (float)s->boxsize[k];
+        h->fo.lo[k] = (float)(s->boxsize[k] - (double)h->fo.hi[k]);
+      }
+      const double hs = 0.5 * h->skin - 1e-6;
+      h->fo.half_skin2 = hs * hs;
+    } else {
+      h->pl.vcap = vcap;
+      h->pl.vlist = track(h, dalloc<int>((size_t)h->ntot * vcap + 4, &err));
+      h->pl.vcount = track(h, dalloc<int>(n1, &err));
+      h->pl.rref = track(h, dalloc<float4>(n1, &err));
+      const double hs = 0.5 * h->skin - 2e-4;
+      h->pl.half_skin2 = (float)(hs * hs);
+    }
     h->w.pl = h->pl;
   }
   // per-step list: built each step, or (persistent lists) left by pass 1
@@ -735,7 +864,7 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
     delete h;
     return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed (%zu slots)", ns);
   }
-  if (prepare_nbr_build<double>() != cudaSuccess || prepare_nbr_build<float>() != cudaSuccess)
+  if (prepare_force_kernels<double>() != cudaSuccess || prepare_force_kernels<float>() != cudaSuccess)
     err = 1;
   cudaMemsetAsync(h->nbr_n, 0, sizeof(int) * ((size_t)h->ntot + 1), h->stream);
   cudaMemsetAsync(h->atom_stress, 0, sizeof(double) * ((size_t)h->ntot + 1), h->stream);
@@ -947,8 +1076,9 @@ int comdgb_sim_kinetic(comdgb_sim *h, double *ek) {
 
 int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long *builds) {
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
-  if (persistent) *persistent = h->pl.vlist != nullptr;
-  if (skin) *skin = h->pl.vlist ? h->skin : 0.0;
+  const bool pers = h->pl.vlist || h->fo.list;
+  if (persistent) *persistent = pers;
+  if (skin) *skin = pers ? h->skin : 0.0;
   if (builds) {
     int st[ST_COUNT];
     int rc = read_status(h, st);

@@ -97,6 +97,29 @@ struct Persist {
   float half_skin2;  // (skin/2 - 2e-4 A)^2: FP32 world coordinates err by < 1e-4 A
 };
 
+// Force order (mixed precision with persistent lists): each list build
+// numbers the atoms in the box order of that moment, a = box_start[b] + k,
+// and the passes work in that numbering until the next build.  The list of
+// atom a is stored transposed per warp of 32 atoms -- entry t of atom a at
+// ((a / 32) * vcap + t) * 32 + a % 32, so the 32 lanes of a warp read entry
+// t as one 128-byte line -- each entry (neighbour number << 5) | code, the
+// code (dx+1)*9 + (dy+1)*3 + (dz+1) of the neighbour's build box relative
+// to a's.  Positions are FP32 relative to the centre of the atom's build
+// box, refreshed every step from the FP64 slot data, so a pair's dr is
+// (pos_a - pos_j) - d * boxsize with d the code's box difference.
+struct ForceOrder {
+  uint32_t *list;
+  int *n;            // [ntot] list length (> vcap: overflowed, the stencil is scanned)
+  int vcap;
+  int *id;           // [ntot] atom id of a
+  d4 *ref;           // [ntot] FP64 box-relative position at the build; w = build box
+  float4 *pos;       // [ntot] FP32 position relative to the build box centre
+  int *slot;         // [ntot] current slot of a
+  float *fi;         // [ntot] F'(rho) of a, FP32 (EAM pass 2)
+  float hi[3], lo[3];  // box size as FP32 hi + lo
+  double half_skin2;   // rebuild when an atom moved more than this squared
+};
+
 // world-frame position in FP32 from the FP32 box-centred position (mixed
 // precision) or from the FP64 box-relative one; good to ~1e-4 A, used only
 // for the skin test
@@ -159,6 +182,25 @@ struct ChebLow32 {
   float lo[6];
   int pair_shared;  // phi, rho, dphi re-expanded on one interval (same y)
 };
+
+// The pair functions of an EAM Chebyshev potential as piecewise cubics in
+// s = r^2 for the FP32 path: n equal segments from s_lo, u = (s - s_lo) *
+// inv_h, segment k = floor(u), t = u - k.  Each float4 holds the monomial
+// coefficients (c0, c1, c2, c3) in t of one function on one segment, fitted
+// in FP64 to the FP64 series (interpolation at the segment's 4 Chebyshev
+// nodes).  p1[3k .. 3k+2]: phi(r), phi'(r)/r, rho(r); p2[k]: rho'(r)/r.
+// s < s_lo (and n == 0: no table) takes the series instead.
+constexpr int SEG_N = 512;  // segments of the table
+struct PairSeg {
+  const float4 *p1;
+  const float4 *p2;
+  float s_lo, inv_h;
+  int n;
+};
+
+__device__ __forceinline__ float seg_cubic(float4 c, float t) {
+  return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+}
 
 __host__ __device__ inline void box_ixyz(const Geom &g, int b, int *ix) {
   ix[0] = b % g.nbx[0];

@@ -25,6 +25,7 @@
 namespace cg {
 
 enum { EVAL_TABLE = 0, EVAL_CHEBY = 1 };
+constexpr int PASS_THREADS = 256;  // CTA size of the EAM passes
 
 struct ForceArgs {
   Geom g;
@@ -38,7 +39,8 @@ struct ForceArgs {
   int cap;
   double *atom_stress;   // [ntot] per-atom share of the scalar stress
   int *status;
-  Persist pl;            // persistent lists (pl.vlist == nullptr: per-step lists)
+  Persist pl;            // persistent lists keyed by id (FP64)
+  ForceOrder fo;         // persistent lists in force order (mixed; fo.list != nullptr)
 };
 
 // Stencil entry of box jb seen from box b when both stencils are the full
@@ -287,46 +289,70 @@ __device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
 // with their exact dr.
 #define NB_CHUNKS (NB_MAXC / 32)  // 54
 #define NB_ATOMS 4                 // atoms tested per candidate load
-// Persistent variant (PERSIST): runs only when a rebuild is due, writes
-// neighbour ids into the atom's id-keyed row and records its position.
-template <bool PERSIST>
+// Modes: LIST_STEP writes the per-step list (uint16 codes); LIST_ID (runs
+// only when a rebuild is due) writes neighbour ids into the atom's id-keyed
+// row and records its position; LIST_FO (also only when due) writes the
+// transposed force-order list and the atom's force-order record.
+enum { LIST_STEP = 0, LIST_ID = 1, LIST_FO = 2 };
+
+template <int MODE>
 __device__ __forceinline__ bool build_skipped(const ForceArgs &A) {
-  return PERSIST && !*(volatile const int *)(A.status + ST_REBUILD);
+  return MODE != LIST_STEP && !*(volatile const int *)(A.status + ST_REBUILD);
 }
 
 // row of atom i of box b: list storage, count slot and capacity
-template <bool PERSIST>
+template <int MODE>
 __device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i, bool mixed) {
-  if (PERSIST) {
-    const int slot = b * CG_MAXATOMS + i;
+  const int slot = b * CG_MAXATOMS + i;
+  if (MODE == LIST_ID) {
     const int idi = A.s.id[slot];
     A.pl.rref[idi] = world32(A.g, b, mixed ? A.s.pos32 : nullptr, slot, A.s.r[slot]);
     return idi;
   }
-  return A.box_start[b] + i;
+  const int a = A.box_start[b] + i;
+  if (MODE == LIST_FO) {
+    const d4 r = A.s.r[slot];
+    d4 q;
+    q.x = r.x;
+    q.y = r.y;
+    q.z = r.z;
+    q.w = (double)b;
+    A.fo.ref[a] = q;
+    A.fo.id[a] = A.s.id[slot];
+    A.fo.slot[a] = slot;
+    A.fo.pos[a] = A.s.pos32[slot];
+  }
+  return a;
 }
 
-template <bool PERSIST>
+template <int MODE>
 __device__ __forceinline__ void build_store(const ForceArgs &A, int row, int h, int value) {
-  if (PERSIST) A.pl.vlist[(size_t)row * A.pl.vcap + h] = value;
+  if (MODE == LIST_ID) A.pl.vlist[(size_t)row * A.pl.vcap + h] = value;
+  else if (MODE == LIST_FO)
+    A.fo.list[((size_t)(row >> 5) * A.fo.vcap + h) * 32 + (row & 31)] = (uint32_t)value;
   else A.nbr[(size_t)row * A.cap + h] = (uint16_t)value;
 }
 
-template <bool PERSIST>
-__device__ __forceinline__ void build_count(const ForceArgs &A, int row, int total) {
-  const int cap = PERSIST ? A.pl.vcap : A.cap;
-  if (PERSIST) A.pl.vcount[row] = total;
-  else A.nbr_n[row] = total;
-  if (total > cap) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+template <int MODE>
+__device__ __forceinline__ int build_cap(const ForceArgs &A) {
+  return MODE == LIST_ID ? A.pl.vcap : MODE == LIST_FO ? A.fo.vcap : A.cap;
 }
 
-template <bool PERSIST>
+template <int MODE>
+__device__ __forceinline__ void build_count(const ForceArgs &A, int row, int total) {
+  if (MODE == LIST_ID) A.pl.vcount[row] = total;
+  else if (MODE == LIST_FO) A.fo.n[row] = total;
+  else A.nbr_n[row] = total;
+  if (total > build_cap<MODE>(A)) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+}
+
+template <int MODE>
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
   __shared__ __align__(16) float4 cand[NB_MAXC];
   __shared__ uint32_t s_mask[NB_THREADS / 32][NB_ATOMS][NB_CHUNKS];
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
   __shared__ BoxOff<float> s_dr[CG_NNBR];
-  if (build_skipped<PERSIST>(A)) return;
+  if (build_skipped<MODE>(A)) return;
   const int b = blockIdx.x;
   const int ni = A.s.natoms[b];
   if (ni == 0) return;
@@ -339,7 +365,10 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
       int k = c - s_off[e];
       float4 q = __ldg(A.s.pos32 + s_box[e] * CG_MAXATOMS + k);
       BoxOff<float> o = s_dr[e];
-      const int tag = PERSIST ? A.s.id[s_box[e] * CG_MAXATOMS + k] : ((e << 6) | k);
+      // force order: with periodic nbx >= 3 the entry index is the code
+      const int tag = MODE == LIST_ID   ? A.s.id[s_box[e] * CG_MAXATOMS + k]
+                      : MODE == LIST_FO ? (int)(((unsigned)(A.box_start[s_box[e]] + k) << 5) | e)
+                                        : ((e << 6) | k);
       cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
                             __int_as_float(tag));
     } else {
@@ -377,10 +406,10 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
     __syncwarp();
     for (int t = 0; t < na; t++) {
       const uint32_t *ms = s_mask[warp][t];
-      if (!PERSIST && A.box_start[b] + i0 + t >= A.ntot) break;  // only after an overflow
-      const int row = (lane == 0) ? build_row<PERSIST>(A, b, i0 + t, true) : 0;
+      if (MODE != LIST_ID && A.box_start[b] + i0 + t >= A.ntot) break;  // only after an overflow
+      const int row = (lane == 0) ? build_row<MODE>(A, b, i0 + t, true) : 0;
       const int a = __shfl_sync(0xffffffffu, row, 0);
-      const int cap = PERSIST ? A.pl.vcap : A.cap;
+      const int cap = build_cap<MODE>(A);
       // chunk words in candidate order: word w is held by lane w & 31 (w < 32
       // in `lo`, w >= 32 in `hi`); inclusive prefix of the hit counts
       const uint32_t lo = lane < nchunk ? ms[lane] : 0u;
@@ -418,17 +447,17 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
           const unsigned bit = __fns(word, 0, hh - before + 1);
           const int c = ((second ? l + 32 : l) << 5) + (int)(bit & 31u);
           if (bit < 32u && c < (nchunk << 5))
-            build_store<PERSIST>(A, a, h, __float_as_int(cand[c].w));
+            build_store<MODE>(A, a, h, __float_as_int(cand[c].w));
         }
       }
-      if (lane == 0) build_count<PERSIST>(A, a, total);
+      if (lane == 0) build_count<MODE>(A, a, total);
     }
     __syncwarp();
   }
 }
 
 // FP64: the reference's dr = (drbox + r_i) - r_j, operation by operation
-template <bool PERSIST>
+template <int MODE>
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArgs A, double rc2) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double *cx = reinterpret_cast<double *>(smem_raw);
@@ -437,7 +466,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
   uint16_t *cc = reinterpret_cast<uint16_t *>(cz + NB_MAXC);
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
   __shared__ BoxOff<double> s_dr[CG_NNBR];
-  if (build_skipped<PERSIST>(A)) return;
+  if (build_skipped<MODE>(A)) return;
   const int b = blockIdx.x;
   const int ni = A.s.natoms[b];
   if (ni == 0) return;
@@ -458,10 +487,10 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
   for (int i = warp; i < ni; i += NB_THREADS / 32) {
     double xi, yi, zi;
     PrecT<double>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
-    if (!PERSIST && A.box_start[b] + i >= A.ntot) break;  // only after an overflow
-    const int row = (lane == 0) ? build_row<PERSIST>(A, b, i, false) : 0;
+    if (MODE != LIST_ID && A.box_start[b] + i >= A.ntot) break;  // only after an overflow
+    const int row = (lane == 0) ? build_row<MODE>(A, b, i, false) : 0;
     const int a = __shfl_sync(0xffffffffu, row, 0);
-    const int cap = PERSIST ? A.pl.vcap : A.cap;
+    const int cap = build_cap<MODE>(A);
     int cnt = 0;
     for (int c0 = 0; c0 < ncand; c0 += 32) {
       const int c = c0 + lane;
@@ -477,12 +506,12 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
       const unsigned m = __ballot_sync(0xffffffffu, hit);
       const int pos = cnt + __popc(m & lt);
       if (hit && pos < cap)
-        build_store<PERSIST>(A, a, pos,
-                             PERSIST ? A.s.id[s_box[code >> 6] * CG_MAXATOMS + (code & 63)]
+        build_store<MODE>(A, a, pos,
+                             MODE == LIST_ID ? A.s.id[s_box[code >> 6] * CG_MAXATOMS + (code & 63)]
                                      : (int)code);
       cnt += __popc(m);
     }
-    if (lane == 0) build_count<PERSIST>(A, a, cnt);
+    if (lane == 0) build_count<MODE>(A, a, cnt);
   }
 }
 
@@ -494,6 +523,7 @@ struct EamPot {
   Table<T> phi, rho, f;
   Cheb<T> ch;
   ChebLow32 chlo;  // FP32 only
+  PairSeg seg;     // FP32 Chebyshev only
   T rc2;
 };
 
@@ -582,10 +612,79 @@ __device__ __forceinline__ T eam_drho(const EamPot<T, EVAL> &P, T r) {
   return d;
 }
 
+// Pair terms of one distance: phi, w = phi'(r)/r and rho.  The FP32
+// Chebyshev path reads them from the segment table in shared memory (sm);
+// distances below the table, or no table, take the series out of line.
 template <class T, int EVAL>
-__global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, EVAL> P) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= A.ntot) return;
+__device__ __forceinline__ void eam_pair_w(const EamPot<T, EVAL> &P, const float4 *, T r2,
+                                           T &phi, T &w, T &rho) {
+  T r, inv_r, dphi;
+  r_and_inv(r2, r, inv_r);
+  eam_pair_terms<T, EVAL>(P, r, phi, dphi, rho);
+  w = dphi * inv_r;
+}
+static __device__ __noinline__ void seg_pair_series(const EamPot<float, EVAL_CHEBY> &P, float r2,
+                                                    float &phi, float &w, float &rho) {
+  float r, inv_r, dphi;
+  r_and_inv(r2, r, inv_r);
+  cheb_pair32(P, r, phi, dphi, rho);
+  w = dphi * inv_r;
+}
+static __device__ __forceinline__ void eam_pair_w(const EamPot<float, EVAL_CHEBY> &P,
+                                                  const float4 *sm, float r2, float &phi,
+                                                  float &w, float &rho) {
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  if (!(u >= 0.f)) {
+    seg_pair_series(P, r2, phi, w, rho);
+    return;
+  }
+  const int k = min((int)u, P.seg.n - 1);
+  const float t = u - (float)k;
+  const float4 *c = sm + 3 * k;
+  phi = seg_cubic(c[0], t);
+  w = seg_cubic(c[1], t);
+  rho = seg_cubic(c[2], t);
+}
+
+// (F'_i + F'_j) rho'(r) / r for one pair (fsum = F'_i + F'_j), as eam_pair_w
+template <class T, int EVAL>
+__device__ __forceinline__ T eam_embed_w(const EamPot<T, EVAL> &P, const float4 *, T r2,
+                                         T fsum) {
+  T r, inv_r;
+  r_and_inv(r2, r, inv_r);
+  return fsum * eam_drho<T, EVAL>(P, r) * inv_r;
+}
+static __device__ __noinline__ float seg_drho_series(const EamPot<float, EVAL_CHEBY> &P,
+                                                     float r2) {
+  float r, inv_r;
+  r_and_inv(r2, r, inv_r);
+  return cheb_series(P, 4, r) * inv_r;
+}
+static __device__ __forceinline__ float eam_embed_w(const EamPot<float, EVAL_CHEBY> &P,
+                                                    const float4 *sm, float r2, float fsum) {
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  if (!(u >= 0.f)) return fsum * seg_drho_series(P, r2);
+  const int k = min((int)u, P.seg.n - 1);
+  return fsum * seg_cubic(sm[k], u - (float)k);
+}
+
+template <class T, int EVAL>
+__device__ __forceinline__ bool uses_seg(const EamPot<T, EVAL> &P) {
+  return sizeof(T) == 4 && EVAL == EVAL_CHEBY && P.seg.n > 0;
+}
+
+// the segment table (nrec float4 from src) into shared memory, once per CTA
+__device__ __forceinline__ void stage_seg(float4 *sm, const float4 *src, int nrec) {
+  for (int q = threadIdx.x; q < nrec; q += blockDim.x) sm[q] = __ldg(src + q);
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// EAM pass 1: density, pair energy and pair force of one atom
+// ---------------------------------------------------------------------------
+template <class T, int EVAL>
+__device__ __forceinline__ void eam_pass1_atom(const ForceArgs &A, const EamPot<T, EVAL> &P,
+                                               const float4 *sm, int a) {
   const int slot = A.atom_slot[a];
   const int b = slot >> 6, i = slot & 63;
   T xi, yi, zi;
@@ -595,11 +694,8 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   const T rc2 = P.rc2;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 > rc2) return;
-    T r, inv_r;
-    r_and_inv(r2, r, inv_r);
-    T phi, dphi, rho;
-    eam_pair_terms<T, EVAL>(P, r, phi, dphi, rho);
-    T w = dphi * inv_r;
+    T phi, w, rho;
+    eam_pair_w(P, sm, r2, phi, w, rho);
     fx.add(w * dx);
     fy.add(w * dy);
     fz.add(w * dz);
@@ -621,13 +717,23 @@ __global__ void __launch_bounds__(128) eam_pass1_kernel(ForceArgs A, EamPot<T, E
   if (sizeof(T) == 4) A.s.fi32[slot] = (float)dF;
 }
 
+// grid-stride over the compact atoms; the grid is sized to the resident CTAs
+// so each CTA stages the segment table once
+template <class T, int EVAL>
+__global__ void __launch_bounds__(PASS_THREADS)
+    eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<T, EVAL> P) {
+  extern __shared__ float4 seg_sm[];
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 3 * P.seg.n);
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x)
+    eam_pass1_atom<T, EVAL>(A, P, seg_sm, a);
+}
+
 // ---------------------------------------------------------------------------
 // EAM pass 2: embedding force and stress
 // ---------------------------------------------------------------------------
 template <class T, int EVAL>
-__global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, EVAL> P) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= A.ntot) return;
+__device__ __forceinline__ void eam_pass2_atom(const ForceArgs &A, const EamPot<T, EVAL> &P,
+                                               const float4 *sm, int a) {
   const int slot = A.atom_slot[a];
   const int b = slot >> 6, i = slot & 63;
   T xi, yi, zi;
@@ -638,11 +744,7 @@ __global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, E
   const T rc2 = P.rc2;
   auto fn = [&](int js, T dx, T dy, T dz, T r2) {
     if (r2 >= rc2) return;
-    T r, inv_r;
-    r_and_inv(r2, r, inv_r);
-    T drho = eam_drho<T, EVAL>(P, r);
-    T w = (fii + PrecT<T>::fi(A.s, js)) * drho;
-    T wr = w * inv_r;
+    T wr = eam_embed_w(P, sm, r2, fii + PrecT<T>::fi(A.s, js));
     fx.add(wr * dx);
     fy.add(wr * dy);
     fz.add(wr * dz);
@@ -655,6 +757,128 @@ __global__ void __launch_bounds__(128) eam_pass2_kernel(ForceArgs A, EamPot<T, E
   fo.z += fz.value();
   A.s.f[slot] = fo;
   A.atom_stress[a] = sx.value();
+}
+
+template <class T, int EVAL>
+__global__ void __launch_bounds__(PASS_THREADS)
+    eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<T, EVAL> P) {
+  extern __shared__ float4 seg_sm[];
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p2, P.seg.n);
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x)
+    eam_pass2_atom<T, EVAL>(A, P, seg_sm, a);
+}
+
+// ---------------------------------------------------------------------------
+// Force-order passes (mixed precision, persistent lists)
+// ---------------------------------------------------------------------------
+// k - 1 as a float for 0 <= k < 2^22 (exponent-field trick: two instructions)
+__device__ __forceinline__ float small_int_minus1(int k) {
+  return __int_as_float(0x4B000000 | k) - 8388609.0f;
+}
+
+// Visit the list of force-order atom a at FP32 position (xi, yi, zi):
+// fn(fj, dx, dy, dz, r2) for every entry, fj = F'(rho_j) when NEED_FI.  An
+// overflowed list scans the stencil of the atom's current slot instead.
+template <bool NEED_FI, class F>
+__device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot, float4 pi,
+                                            float rc2, F &&fn) {
+  const int n = A.fo.n[a];
+  if (n > A.fo.vcap) {
+    const float4 p = __ldg(A.s.pos32 + slot);
+    scan_stencil<float>(A, slot >> 6, slot & 63, p.x, p.y, p.z, rc2,
+                        [&](int js, float dx, float dy, float dz, float r2) {
+                          fn(NEED_FI ? __ldg(A.s.fi32 + js) : 0.f, dx, dy, dz, r2);
+                        });
+    return;
+  }
+  const float hx = A.fo.hi[0], hy = A.fo.hi[1], hz = A.fo.hi[2];
+  const float lx = A.fo.lo[0], ly = A.fo.lo[1], lz = A.fo.lo[2];
+  const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
+#pragma unroll 2
+  for (int t = 0; t < n; t++) {
+    const uint32_t p = __ldg(lst + (size_t)t * 32);
+    const int j = (int)(p >> 5), c = (int)(p & 31u);
+    const float4 q = __ldg(A.fo.pos + j);
+    const float fj = NEED_FI ? __ldg(A.fo.fi + j) : 0.f;
+    // code = (dx+1)*9 + (dy+1)*3 + (dz+1); the pair offset is -d * boxsize
+    const int cx = (c * 57) >> 9, rem = c - 9 * cx;
+    const int cy = (rem * 11) >> 5, cz = rem - 3 * cy;
+    const float ex = -small_int_minus1(cx), ey = -small_int_minus1(cy),
+                ez = -small_int_minus1(cz);
+    const float dx = fmaf(ex, lx, fmaf(ex, hx, pi.x - q.x));
+    const float dy = fmaf(ey, ly, fmaf(ey, hy, pi.y - q.y));
+    const float dz = fmaf(ez, lz, fmaf(ez, hz, pi.z - q.z));
+    fn(fj, dx, dy, dz, fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+  }
+}
+
+template <int EVAL>
+__global__ void __launch_bounds__(PASS_THREADS)
+    fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
+  extern __shared__ float4 seg_sm[];
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 3 * P.seg.n);
+  const float rc2 = P.rc2;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
+    const int slot = A.fo.slot[a];
+    KSum fx, fy, fz, ep, rh;
+    fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
+    int cnt = 0;
+    auto fn = [&](float, float dx, float dy, float dz, float r2) {
+      if (r2 > rc2) return;
+      cnt++;
+      float phi, w, rho;
+      eam_pair_w(P, seg_sm, r2, phi, w, rho);
+      fx.add(w * dx);
+      fy.add(w * dy);
+      fz.add(w * dz);
+      ep.add(phi * 0.5f);
+      rh.add(rho);
+    };
+    fo_for_each<false>(A, a, slot, A.fo.pos[a], rc2, fn);
+    const double rho_i = rh.value();
+    float F, dF;
+    eam_embed<float, EVAL>(P, (float)rho_i, F, dF);
+    d4 fo;
+    fo.x = fx.value();
+    fo.y = fy.value();
+    fo.z = fz.value();
+    fo.w = ep.value() + (double)F;
+    A.s.f[slot] = fo;
+    A.s.rho[slot] = rho_i;
+    A.s.fi[slot] = (double)dF;
+    A.s.fi32[slot] = dF;
+    A.fo.fi[a] = dF;
+    A.nbr_n[a] = cnt;
+  }
+}
+
+template <int EVAL>
+__global__ void __launch_bounds__(PASS_THREADS)
+    fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
+  extern __shared__ float4 seg_sm[];
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p2, P.seg.n);
+  const float rc2 = P.rc2;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
+    const int slot = A.fo.slot[a];
+    const float fii = A.fo.fi[a];
+    KSum fx, fy, fz, sx;
+    fx.zero(); fy.zero(); fz.zero(); sx.zero();
+    auto fn = [&](float fj, float dx, float dy, float dz, float r2) {
+      if (r2 >= rc2) return;
+      const float wr = eam_embed_w(P, seg_sm, r2, fii + fj);
+      fx.add(wr * dx);
+      fy.add(wr * dy);
+      fz.add(wr * dz);
+      sx.add(wr * dx * dx);
+    };
+    fo_for_each<true>(A, a, slot, A.fo.pos[a], rc2, fn);
+    d4 fo = A.s.f[slot];
+    fo.x += fx.value();
+    fo.y += fy.value();
+    fo.z += fz.value();
+    A.s.f[slot] = fo;
+    A.atom_stress[a] = sx.value();
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -702,6 +926,43 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
   fo.w = ep.value();
   A.s.f[slot] = fo;
   A.atom_stress[a] = sx.value() - (double)nonempty * kin;
+}
+
+// LJ in force order (mixed precision, persistent lists)
+static __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<float> P) {
+  const float s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6, rc2 = P.rc2;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
+    const int slot = A.fo.slot[a];
+    const int b = slot >> 6;
+    KSum fx, fy, fz, ep, sx;
+    fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
+    int cnt = 0;
+    auto fn = [&](float, float dx, float dy, float dz, float r2) {
+      if (r2 > rc2) return;
+      cnt++;
+      float ir2 = 1.0f / r2;
+      float r6 = ir2 * ir2 * ir2;
+      ep.add(0.5f * r6 * (s6 * r6 - 1.0f));
+      float fr = c4 * r6 * ir2 * (s12 * r6 - 6.0f);
+      fx.add(dx * fr);
+      fy.add(dy * fr);
+      fz.add(dz * fr);
+      sx.add(fr * dx * dx);
+    };
+    fo_for_each<false>(A, a, slot, A.fo.pos[a], rc2, fn);
+    int ne = A.et.n[b], nonempty = 0;
+    for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
+    d4 p = A.s.p[slot];
+    double kin = __ddiv_rn(__dmul_rn(p.x, p.x), A.s.mass[slot]);
+    d4 fo;
+    fo.x = fx.value();
+    fo.y = fy.value();
+    fo.z = fz.value();
+    fo.w = ep.value();
+    A.s.f[slot] = fo;
+    A.atom_stress[a] = sx.value() - (double)nonempty * kin;
+    A.nbr_n[a] = cnt;
+  }
 }
 
 }  // namespace cg

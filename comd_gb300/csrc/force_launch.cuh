@@ -8,51 +8,137 @@ static size_t nbr_build_smem() {
   return sizeof(FT) == 8 ? (size_t)NB_MAXC * (3 * sizeof(double) + sizeof(uint16_t)) : 0;
 }
 
+// resident CTAs per SM of the EAM pass kernels ([pass][eval]) and the SM
+// count, found before any launch or stream capture
+static int g_pass_per_sm[2][2];
+static int g_fo_per_sm[3][2];  // force order: [pass 1, pass 2, LJ][eval]
+static int g_num_sms = 1;
+
+template <class K>
+static cudaError_t pass_occupancy(K kernel, size_t smem, int *out) {
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kernel, PASS_THREADS, smem);
+  if (*out < 1) *out = 1;
+  return e;
+}
+
+static size_t pass_smem(int pass, int eval) {
+  if (sizeof(FT) != 4 || eval != EVAL_CHEBY) return 0;
+  return sizeof(float4) * (pass == 0 ? 3 : 1) * SEG_N;
+}
+
 // called on the current device before any launch or stream capture
 template <>
-cudaError_t prepare_nbr_build<FT>() {
-  if (sizeof(FT) == 4) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(nbr_build64_kernel<false>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)nbr_build_smem());
+cudaError_t prepare_force_kernels<FT>() {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = pass_occupancy(eam_pass1_kernel<FT, EVAL_TABLE>, pass_smem(0, EVAL_TABLE),
+                       &g_pass_per_sm[0][EVAL_TABLE]);
+  if (e == cudaSuccess)
+    e = pass_occupancy(eam_pass1_kernel<FT, EVAL_CHEBY>, pass_smem(0, EVAL_CHEBY),
+                       &g_pass_per_sm[0][EVAL_CHEBY]);
+  if (e == cudaSuccess)
+    e = pass_occupancy(eam_pass2_kernel<FT, EVAL_TABLE>, pass_smem(1, EVAL_TABLE),
+                       &g_pass_per_sm[1][EVAL_TABLE]);
+  if (e == cudaSuccess)
+    e = pass_occupancy(eam_pass2_kernel<FT, EVAL_CHEBY>, pass_smem(1, EVAL_CHEBY),
+                       &g_pass_per_sm[1][EVAL_CHEBY]);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(nbr_build64_kernel<true>,
+#if COMDGB_FT_FLOAT
+  {
+    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[0][EVAL_TABLE]);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY>, pass_smem(0, EVAL_CHEBY),
+                         &g_fo_per_sm[0][EVAL_CHEBY]);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[1][EVAL_TABLE]);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY>, pass_smem(1, EVAL_CHEBY),
+                         &g_fo_per_sm[1][EVAL_CHEBY]);
+    if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel, 0, &g_fo_per_sm[2][0]);
+    return e;
+  }
+#endif
+  e = cudaFuncSetAttribute(nbr_build64_kernel<LIST_STEP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)nbr_build_smem());
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(nbr_build64_kernel<LIST_ID>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)nbr_build_smem());
+}
+
+// grid of a pass: every atom one thread, capped at the resident CTAs
+static int pass_grid(int pass, int eval, int ntot, bool fo = false) {
+  long need = (ntot + PASS_THREADS - 1) / PASS_THREADS;
+  long cap = (long)g_num_sms * (fo ? g_fo_per_sm[pass][eval] : g_pass_per_sm[pass][eval]);
+  return (int)(need < cap ? need : cap);
 }
 
 template <>
 void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
-  const bool persist = A.pl.vlist != nullptr;
   if (sizeof(FT) == 4) {
-    if (persist) nbr_build32_kernel<true><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
-    else nbr_build32_kernel<false><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+    if (A.fo.list) nbr_build32_kernel<LIST_FO><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+    else if (A.pl.vlist)
+      nbr_build32_kernel<LIST_ID><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+    else nbr_build32_kernel<LIST_STEP><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
   } else {
-    if (persist)
-      nbr_build64_kernel<true><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
+    if (A.pl.vlist)
+      nbr_build64_kernel<LIST_ID><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
     else
-      nbr_build64_kernel<false><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
+      nbr_build64_kernel<LIST_STEP><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A,
+                                                                                  (double)rc2);
   }
 }
+
+#if COMDGB_FT_FLOAT
+template <int EVAL>
+void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st) {
+  if (A.ntot <= 0) return;
+  const size_t smem = P.seg.n > 0 ? pass_smem(pass, EVAL) : 0;
+  const int grid = pass_grid(pass, EVAL, A.ntot, true);
+  if (pass == 0) fo_eam_pass1_kernel<EVAL><<<grid, PASS_THREADS, smem, st>>>(A, P);
+  else fo_eam_pass2_kernel<EVAL><<<grid, PASS_THREADS, smem, st>>>(A, P);
+}
+template void launch_fo_eam<EVAL_TABLE>(const ForceArgs &, const EamPot<float, EVAL_TABLE> &,
+                                        int, cudaStream_t);
+template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, EVAL_CHEBY> &,
+                                        int, cudaStream_t);
+
+void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st) {
+  if (A.ntot > 0) fo_lj_kernel<<<pass_grid(2, 0, A.ntot, true), PASS_THREADS, 0, st>>>(A, P);
+}
+#endif
 
 template <>
 void launch_eam_pass1<FT, EVAL_TABLE>(const ForceArgs &A, const EamPot<FT, EVAL_TABLE> &P,
                                       cudaStream_t st) {
-  if (A.ntot > 0) eam_pass1_kernel<FT, EVAL_TABLE><<<(A.ntot + 127) / 128, 128, 0, st>>>(A, P);
+  if (A.ntot <= 0) return;
+  const size_t smem = P.seg.n > 0 ? pass_smem(0, EVAL_TABLE) : 0;
+  eam_pass1_kernel<FT, EVAL_TABLE><<<pass_grid(0, EVAL_TABLE, A.ntot), PASS_THREADS, smem, st>>>(A, P);
 }
 template <>
 void launch_eam_pass1<FT, EVAL_CHEBY>(const ForceArgs &A, const EamPot<FT, EVAL_CHEBY> &P,
                                       cudaStream_t st) {
-  if (A.ntot > 0) eam_pass1_kernel<FT, EVAL_CHEBY><<<(A.ntot + 127) / 128, 128, 0, st>>>(A, P);
+  if (A.ntot <= 0) return;
+  const size_t smem = P.seg.n > 0 ? pass_smem(0, EVAL_CHEBY) : 0;
+  eam_pass1_kernel<FT, EVAL_CHEBY><<<pass_grid(0, EVAL_CHEBY, A.ntot), PASS_THREADS, smem, st>>>(A, P);
 }
 template <>
 void launch_eam_pass2<FT, EVAL_TABLE>(const ForceArgs &A, const EamPot<FT, EVAL_TABLE> &P,
                                       cudaStream_t st) {
-  if (A.ntot > 0) eam_pass2_kernel<FT, EVAL_TABLE><<<(A.ntot + 127) / 128, 128, 0, st>>>(A, P);
+  if (A.ntot <= 0) return;
+  const size_t smem = P.seg.n > 0 ? pass_smem(1, EVAL_TABLE) : 0;
+  eam_pass2_kernel<FT, EVAL_TABLE><<<pass_grid(1, EVAL_TABLE, A.ntot), PASS_THREADS, smem, st>>>(A, P);
 }
 template <>
 void launch_eam_pass2<FT, EVAL_CHEBY>(const ForceArgs &A, const EamPot<FT, EVAL_CHEBY> &P,
                                       cudaStream_t st) {
-  if (A.ntot > 0) eam_pass2_kernel<FT, EVAL_CHEBY><<<(A.ntot + 127) / 128, 128, 0, st>>>(A, P);
+  if (A.ntot <= 0) return;
+  const size_t smem = P.seg.n > 0 ? pass_smem(1, EVAL_CHEBY) : 0;
+  eam_pass2_kernel<FT, EVAL_CHEBY><<<pass_grid(1, EVAL_CHEBY, A.ntot), PASS_THREADS, smem, st>>>(A, P);
 }
 template <>
 void launch_lj<FT>(const ForceArgs &A, const LjPot<FT> &P, cudaStream_t st) {

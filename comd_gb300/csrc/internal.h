@@ -68,10 +68,12 @@ void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, c
 void launch_rebuild_done(int *status, cudaStream_t st);
 void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *status,
                        cudaStream_t st);
+void launch_fo_refresh(const Geom &g, Slots s, const ForceOrder &fo, const int *slot_of,
+                       int ntot, int *status, cudaStream_t st);
 
 // ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----
 template <class T>
-cudaError_t prepare_nbr_build();
+cudaError_t prepare_force_kernels();
 template <class T>
 void launch_nbr_build(const ForceArgs &A, T rc2, cudaStream_t st);
 template <class T, int EVAL>
@@ -80,5 +82,9 @@ template <class T, int EVAL>
 void launch_eam_pass2(const ForceArgs &A, const EamPot<T, EVAL> &P, cudaStream_t st);
 template <class T>
 void launch_lj(const ForceArgs &A, const LjPot<T> &P, cudaStream_t st);
+// force order (mixed precision only, force_mixed.cu); pass 0 or 1
+template <int EVAL>
+void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st);
+void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st);
 
 }  // namespace cg

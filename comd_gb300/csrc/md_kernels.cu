@@ -502,6 +502,46 @@ __global__ void rebuild_done_kernel(int *status) {
   }
 }
 
+// Force order, each force call before the list build: the current slot of
+// every force-order atom, its displacement since the build (FP64, box
+// difference taken minimum-image) and from it the FP32 position relative
+// to its build box centre.  A displacement beyond skin/2 flags a rebuild,
+// which then rewrites every record, so once the flag is up (set before this
+// launch, or by another thread) the remaining records are left alone.
+__global__ void __launch_bounds__(256) fo_refresh_kernel(Geom g, Slots s, ForceOrder fo,
+                                                         const int *slot_of, int ntot,
+                                                         int *status) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= ntot || *(volatile int *)(status + ST_REBUILD)) return;
+  const int slot = slot_of[fo.id[a]];
+  fo.slot[a] = slot;
+  const d4 r = s.r[slot], q = fo.ref[a];
+  int ixn[3], ixb[3];
+  box_ixyz_tab(g, slot >> 6, ixn);
+  box_ixyz_tab(g, (int)q.w, ixb);
+  const double rv[3] = {r.x, r.y, r.z}, qv[3] = {q.x, q.y, q.z};
+  double d[3], d2 = 0.0;
+  float pv[3];
+  for (int k = 0; k < 3; k++) {
+    int db = ixn[k] - ixb[k];
+    if (g.periodic) {
+      if (db > 1) db -= g.nbx[k];
+      else if (db < -1) db += g.nbx[k];
+    }
+    d[k] = (rv[k] - qv[k]) + (double)db * g.boxsize[k];
+    d2 = d2 + d[k] * d[k];
+    pv[k] = (float)((qv[k] - 0.5 * g.boxsize[k]) + d[k]);
+  }
+  if (!(d2 <= fo.half_skin2)) atomicExch(status + ST_REBUILD, 1);
+  fo.pos[a] = make_float4(pv[0], pv[1], pv[2], 0.f);
+}
+
+void launch_fo_refresh(const Geom &g, Slots s, const ForceOrder &fo, const int *slot_of,
+                       int ntot, int *status, cudaStream_t st) {
+  if (ntot > 0)
+    fo_refresh_kernel<<<atom_blocks(ntot), 256, 0, st>>>(g, s, fo, slot_of, ntot, status);
+}
+
 // skin test of every atom (standalone force calls: positions may have moved
 // since the last half step that tested them)
 __global__ void skin_check_kernel(Geom g, Slots s, Persist pl, bool mixed, int *status) {
