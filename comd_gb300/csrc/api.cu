@@ -296,85 +296,65 @@ void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
       lo32.pair_shared = 0;
 }
 
-// Segment table of the FP32 pair path (PairSeg): phi, phi'/r, rho, rho'/r
-// of the FP64 series as cubics in s = r^2 on [lo^2, rc^2], lo = max(pair_lo,
-// series lower ends).  Each cubic interpolates the function at the 4
-// Chebyshev nodes of its segment; the result is checked at 9 points per
-// segment and the table is dropped (series path) if any function errs by
-// more than 1e-7 of its largest magnitude on the interval.  Returns 0, or
-// -1 when device memory ran out.
+// Segment table of the FP32 pair path (PairSeg): phi and rho of the FP64
+// series as cubic Hermite interpolants in s = r^2 on [lo^2, rc^2], lo =
+// max(pair_lo, series lower ends); the end slopes come from the derivative
+// series (d/dt = h * D(r) / (2 r)).  Checked at 9 points per segment: values
+// to 1e-7 and slopes (dscale * d/dt against D(r)/r) to 1e-6 of the
+// function's largest magnitude on the interval -- so derivative series that
+// are not the derivatives of phi and rho drop the table (series path).
+// Returns 0, or -1 when device memory ran out.
 int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
                    const double b[6], double pair_lo, double rc, PairSeg *out) {
-  *out = PairSeg{nullptr, nullptr, 3.0e38f, 1.0f, 0};
+  *out = PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0};
   double lo = pair_lo;
   for (int s : {0, 1, 3, 4}) lo = std::max(lo, a[s]);
   if (!(lo > 0.0 && lo < rc)) return 0;
   const int n = SEG_N;
   const float s_lo = (float)(lo * lo);
   const float inv_h = (float)(n / (rc * rc - (double)s_lo));
-  const double h_s = 1.0 / (double)inv_h;
-  auto fn = [&](int q, double s) {
-    double r = sqrt(s);
-    switch (q) {
-      case 0: return cheb_host(coef[0], a[0], b[0], r);
-      case 1: return cheb_host(coef[3], a[3], b[3], r) / r;
-      case 2: return cheb_host(coef[1], a[1], b[1], r);
-      default: return cheb_host(coef[4], a[4], b[4], r) / r;
-    }
+  const float dscale = 2.0f * inv_h;
+  const double hs = 1.0 / (double)inv_h;
+  // q = 0: phi (series 0, derivative 3); q = 1: rho (series 1, derivative 4)
+  auto val = [&](int q, double s) {
+    return q == 0 ? cheb_host(coef[0], a[0], b[0], sqrt(s)) : cheb_host(coef[1], a[1], b[1], sqrt(s));
   };
-  const double PI = 3.141592653589793;
-  double tn[4], tj[4][4];  // nodes in t and T_j(2 t_m - 1)
-  for (int m = 0; m < 4; m++) {
-    tn[m] = 0.5 + 0.5 * cos(PI * (m + 0.5) / 4.0);
-    double y = 2.0 * tn[m] - 1.0;
-    tj[m][0] = 1.0;
-    tj[m][1] = y;
-    tj[m][2] = 2.0 * y * y - 1.0;
-    tj[m][3] = y * (4.0 * y * y - 3.0);
-  }
-  std::vector<double> mono((size_t)4 * n * 4);  // [q][k][4]
-  double fmax[4] = {0, 0, 0, 0}, emax[4] = {0, 0, 0, 0};
-  for (int q = 0; q < 4; q++) {
+  auto der = [&](int q, double s) {  // D(r) / r
+    double r = sqrt(s);
+    return (q == 0 ? cheb_host(coef[3], a[3], b[3], r) : cheb_host(coef[4], a[4], b[4], r)) / r;
+  };
+  std::vector<float4> p1((size_t)2 * n);
+  for (int q = 0; q < 2; q++) {
+    double fmax = 0, gmax = 0, ferr = 0, gerr = 0;
+    double f0 = val(q, (double)s_lo), m0 = 0.5 * hs * der(q, (double)s_lo);
     for (int k = 0; k < n; k++) {
-      double fv[4], c[4] = {0, 0, 0, 0};
-      for (int m = 0; m < 4; m++) fv[m] = fn(q, (double)s_lo + (k + tn[m]) * h_s);
-      for (int j = 0; j < 4; j++) {
-        for (int m = 0; m < 4; m++) c[j] += fv[m] * tj[m][j];
-        c[j] *= 0.5;  // 2/4; c0 enters halved below
-      }
-      // sum_j c_j T_j(2t-1) with c0 halved, in powers of t
-      double *mk = &mono[((size_t)q * n + k) * 4];
-      mk[0] = 0.5 * c[0] - c[1] + c[2] - c[3];
-      mk[1] = 2.0 * c[1] - 8.0 * c[2] + 18.0 * c[3];
-      mk[2] = 8.0 * c[2] - 48.0 * c[3];
-      mk[3] = 32.0 * c[3];
+      const double s1 = (double)s_lo + (k + 1) * hs;
+      const double f1 = val(q, s1), m1 = 0.5 * hs * der(q, s1);
+      const double c0 = f0, c1 = m0, c2 = 3.0 * (f1 - f0) - 2.0 * m0 - m1,
+                   c3 = 2.0 * (f0 - f1) + m0 + m1;
+      p1[(size_t)q * n + k] = make_float4((float)c0, (float)c1, (float)c2, (float)c3);
       for (int e = 0; e <= 8; e++) {
-        double t = e / 8.0, ex = fn(q, (double)s_lo + (k + t) * h_s);
-        double p = ((mk[3] * t + mk[2]) * t + mk[1]) * t + mk[0];
-        fmax[q] = std::max(fmax[q], fabs(ex));
-        emax[q] = std::max(emax[q], fabs(p - ex));
+        const double t = e / 8.0, s = (double)s_lo + (k + t) * hs;
+        const double fv = val(q, s), gv = der(q, s);
+        const double pv = ((c3 * t + c2) * t + c1) * t + c0;
+        const double pd = (double)dscale * ((3.0 * c3 * t + 2.0 * c2) * t + c1);
+        fmax = std::max(fmax, fabs(fv));
+        gmax = std::max(gmax, fabs(gv));
+        ferr = std::max(ferr, fabs(pv - fv));
+        gerr = std::max(gerr, fabs(pd - gv));
       }
+      f0 = f1;
+      m0 = m1;
     }
-    if (!(emax[q] <= 1e-7 * fmax[q])) return 0;
+    if (!(ferr <= 1e-7 * fmax) || !(gerr <= 1e-6 * gmax)) return 0;
   }
-  std::vector<float4> p1((size_t)3 * n), p2((size_t)n);
-  for (int k = 0; k < n; k++)
-    for (int q = 0; q < 4; q++) {
-      const double *mk = &mono[((size_t)q * n + k) * 4];
-      float4 v = make_float4((float)mk[0], (float)mk[1], (float)mk[2], (float)mk[3]);
-      if (q < 3) p1[(size_t)3 * k + q] = v;
-      else p2[k] = v;
-    }
   int err = 0;
   float4 *d1 = track(h, dalloc<float4>(p1.size(), &err));
-  float4 *d2 = track(h, dalloc<float4>(p2.size(), &err));
   if (err) return -1;
   if (cudaMemcpy(d1, p1.data(), sizeof(float4) * p1.size(), cudaMemcpyHostToDevice) !=
-          cudaSuccess ||
-      cudaMemcpy(d2, p2.data(), sizeof(float4) * p2.size(), cudaMemcpyHostToDevice) !=
-          cudaSuccess)
+      cudaSuccess)
     return -1;
-  *out = PairSeg{d1, d2, s_lo, inv_h, n};
+  *out = PairSeg{d1, s_lo, inv_h, dscale, n};
   return 0;
 }
 
@@ -831,7 +811,7 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
       h->fo.ref = track(h, dalloc<d4>(n1, &err));
       h->fo.pos = track(h, dalloc<float4>(n1, &err));
       h->fo.slot = track(h, dalloc<int>(n1, &err));
-      h->fo.fi = track(h, dalloc<float>(n1, &err));
+      h->fo.pf = track(h, dalloc<float4>(n1, &err));
       for (int k = 0; k < 3; k++) {
         h->fo.hi[k] = (float)s->boxsize[k];
         h->fo.lo[k] = (float)(s->boxsize[k] - (double)h->fo.hi[k]);

@@ -115,7 +115,7 @@ struct ForceOrder {
   d4 *ref;           // [ntot] FP64 box-relative position at the build; w = build box
   float4 *pos;       // [ntot] FP32 position relative to the build box centre
   int *slot;         // [ntot] current slot of a
-  float *fi;         // [ntot] F'(rho) of a, FP32 (EAM pass 2)
+  float4 *pf;        // [ntot] EAM: pos with w = F'(rho) of a (written by pass 1 for pass 2)
   float hi[3], lo[3];  // box size as FP32 hi + lo
   double half_skin2;   // rebuild when an atom moved more than this squared
 };
@@ -185,21 +185,26 @@ struct ChebLow32 {
 
 // The pair functions of an EAM Chebyshev potential as piecewise cubics in
 // s = r^2 for the FP32 path: n equal segments from s_lo, u = (s - s_lo) *
-// inv_h, segment k = floor(u), t = u - k.  Each float4 holds the monomial
-// coefficients (c0, c1, c2, c3) in t of one function on one segment, fitted
-// in FP64 to the FP64 series (interpolation at the segment's 4 Chebyshev
-// nodes).  p1[3k .. 3k+2]: phi(r), phi'(r)/r, rho(r); p2[k]: rho'(r)/r.
+// inv_h, segment k = floor(u), t = u - k.  p1[k] holds the monomial
+// coefficients (c0, c1, c2, c3) in t of phi on segment k, p1[n + k] those of
+// rho: cubic Hermite interpolants of the FP64 series (value and derivative
+// at both segment ends).  The reference's derivative series are the exact
+// derivatives of its phi and rho series (genDer), so phi'(r)/r = 2 dphi/ds
+// = dscale * dphi/dt with dscale = 2 * inv_h, and likewise rho'(r)/r.
 // s < s_lo (and n == 0: no table) takes the series instead.
-constexpr int SEG_N = 512;  // segments of the table
+constexpr int SEG_N = 2048;  // segments of the table
 struct PairSeg {
   const float4 *p1;
-  const float4 *p2;
-  float s_lo, inv_h;
+  float s_lo, inv_h, dscale;
   int n;
 };
 
 __device__ __forceinline__ float seg_cubic(float4 c, float t) {
   return fmaf(fmaf(fmaf(c.w, t, c.z), t, c.y), t, c.x);
+}
+// d/dt of the cubic
+__device__ __forceinline__ float seg_dcubic(float4 c, float t) {
+  return fmaf(fmaf(3.0f * c.w, t, 2.0f * c.z), t, c.y);
 }
 
 __host__ __device__ inline void box_ixyz(const Geom &g, int b, int *ix) {

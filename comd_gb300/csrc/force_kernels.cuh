@@ -613,59 +613,79 @@ __device__ __forceinline__ T eam_drho(const EamPot<T, EVAL> &P, T r) {
 }
 
 // Pair terms of one distance: phi, w = phi'(r)/r and rho.  The FP32
-// Chebyshev path reads them from the segment table in shared memory (sm);
-// distances below the table, or no table, take the series out of line.
+// Chebyshev path reads them from the segment table in shared memory (sm)
+// and returns false for a distance below the table (or with no table): the
+// caller then takes that pair from the series in a second, rare sweep, so
+// the pair loop itself holds no call.
 template <class T, int EVAL>
-__device__ __forceinline__ void eam_pair_w(const EamPot<T, EVAL> &P, const float4 *, T r2,
+__device__ __forceinline__ bool eam_pair_w(const EamPot<T, EVAL> &P, const float4 *, T r2,
                                            T &phi, T &w, T &rho) {
   T r, inv_r, dphi;
   r_and_inv(r2, r, inv_r);
   eam_pair_terms<T, EVAL>(P, r, phi, dphi, rho);
   w = dphi * inv_r;
+  return true;
 }
-static __device__ __noinline__ void seg_pair_series(const EamPot<float, EVAL_CHEBY> &P, float r2,
-                                                    float &phi, float &w, float &rho) {
+static __device__ __forceinline__ bool eam_pair_w(const EamPot<float, EVAL_CHEBY> &P,
+                                                  const float4 *sm, float r2, float &phi,
+                                                  float &w, float &rho) {
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  if (!(u >= 0.f)) return false;
+  const int k = min((int)u, P.seg.n - 1);
+  const float t = u - (float)k;
+  const float4 cp = sm[k], cr = sm[P.seg.n + k];
+  phi = seg_cubic(cp, t);
+  w = P.seg.dscale * seg_dcubic(cp, t);
+  rho = seg_cubic(cr, t);
+  return true;
+}
+// the series for a pair below the table (FP32 Chebyshev only)
+template <class T, int EVAL>
+__device__ __forceinline__ void pair_w_series(const EamPot<T, EVAL> &, T, T &, T &, T &) {}
+static __device__ __noinline__ void pair_w_series(const EamPot<float, EVAL_CHEBY> &P, float r2,
+                                                  float &phi, float &w, float &rho) {
   float r, inv_r, dphi;
   r_and_inv(r2, r, inv_r);
   cheb_pair32(P, r, phi, dphi, rho);
   w = dphi * inv_r;
 }
-static __device__ __forceinline__ void eam_pair_w(const EamPot<float, EVAL_CHEBY> &P,
-                                                  const float4 *sm, float r2, float &phi,
-                                                  float &w, float &rho) {
-  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
-  if (!(u >= 0.f)) {
-    seg_pair_series(P, r2, phi, w, rho);
-    return;
-  }
-  const int k = min((int)u, P.seg.n - 1);
-  const float t = u - (float)k;
-  const float4 *c = sm + 3 * k;
-  phi = seg_cubic(c[0], t);
-  w = seg_cubic(c[1], t);
-  rho = seg_cubic(c[2], t);
+template <class T, int EVAL>
+__device__ __forceinline__ bool below_seg(const EamPot<T, EVAL> &, T) {
+  return false;
+}
+static __device__ __forceinline__ bool below_seg(const EamPot<float, EVAL_CHEBY> &P, float r2) {
+  return !((r2 - P.seg.s_lo) * P.seg.inv_h >= 0.f);
 }
 
-// (F'_i + F'_j) rho'(r) / r for one pair (fsum = F'_i + F'_j), as eam_pair_w
+// wr = (F'_i + F'_j) rho'(r) / r for one pair (fsum = F'_i + F'_j); the FP32
+// Chebyshev path reads rho's cubic (sm holds the rho half of the table).
+// false: below the table, as eam_pair_w.
 template <class T, int EVAL>
-__device__ __forceinline__ T eam_embed_w(const EamPot<T, EVAL> &P, const float4 *, T r2,
-                                         T fsum) {
+__device__ __forceinline__ bool eam_embed_w(const EamPot<T, EVAL> &P, const float4 *, T r2,
+                                            T fsum, T &wr) {
   T r, inv_r;
   r_and_inv(r2, r, inv_r);
-  return fsum * eam_drho<T, EVAL>(P, r) * inv_r;
+  wr = fsum * eam_drho<T, EVAL>(P, r) * inv_r;
+  return true;
 }
-static __device__ __noinline__ float seg_drho_series(const EamPot<float, EVAL_CHEBY> &P,
-                                                     float r2) {
+static __device__ __forceinline__ bool eam_embed_w(const EamPot<float, EVAL_CHEBY> &P,
+                                                   const float4 *sm, float r2, float fsum,
+                                                   float &wr) {
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  if (!(u >= 0.f)) return false;
+  const int k = min((int)u, P.seg.n - 1);
+  wr = fsum * (P.seg.dscale * seg_dcubic(sm[k], u - (float)k));
+  return true;
+}
+template <class T, int EVAL>
+__device__ __forceinline__ T embed_w_series(const EamPot<T, EVAL> &, T, T) {
+  return T(0);
+}
+static __device__ __noinline__ float embed_w_series(const EamPot<float, EVAL_CHEBY> &P, float r2,
+                                                    float fsum) {
   float r, inv_r;
   r_and_inv(r2, r, inv_r);
-  return cheb_series(P, 4, r) * inv_r;
-}
-static __device__ __forceinline__ float eam_embed_w(const EamPot<float, EVAL_CHEBY> &P,
-                                                    const float4 *sm, float r2, float fsum) {
-  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
-  if (!(u >= 0.f)) return fsum * seg_drho_series(P, r2);
-  const int k = min((int)u, P.seg.n - 1);
-  return fsum * seg_cubic(sm[k], u - (float)k);
+  return fsum * (cheb_series(P, 4, r) * inv_r);
 }
 
 template <class T, int EVAL>
@@ -680,41 +700,67 @@ __device__ __forceinline__ void stage_seg(float4 *sm, const float4 *src, int nre
 }
 
 // ---------------------------------------------------------------------------
-// EAM pass 1: density, pair energy and pair force of one atom
+// EAM pass 1: density, pair energy and pair force of one atom.  `visit`
+// runs the atom's neighbour traversal with a pair functor.
 // ---------------------------------------------------------------------------
-template <class T, int EVAL>
-__device__ __forceinline__ void eam_pass1_atom(const ForceArgs &A, const EamPot<T, EVAL> &P,
-                                               const float4 *sm, int a) {
-  const int slot = A.atom_slot[a];
-  const int b = slot >> 6, i = slot & 63;
-  T xi, yi, zi;
-  PrecT<T>::pos(A.s, slot, xi, yi, zi);
+template <class T>
+struct Pass1Acc {
   typename PrecT<T>::Acc fx, fy, fz, ep, rh;
-  fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
-  const T rc2 = P.rc2;
-  auto fn = [&](int js, T dx, T dy, T dz, T r2) {
-    if (r2 > rc2) return;
-    T phi, w, rho;
-    eam_pair_w(P, sm, r2, phi, w, rho);
+  int cnt;
+  __device__ __forceinline__ void zero() {
+    fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
+    cnt = 0;
+  }
+  __device__ __forceinline__ void add(T phi, T w, T rho, T dx, T dy, T dz) {
     fx.add(w * dx);
     fy.add(w * dy);
     fz.add(w * dz);
     ep.add(phi / T(2.0));
     rh.add(rho);
-  };
-  for_each_neighbor<T, false, true>(A, a, b, i, xi, yi, zi, rc2, fn);
-  double rho_i = rh.value();
+  }
+};
+
+template <class T, int EVAL, class V>
+__device__ __forceinline__ void eam_pass1_sum(const EamPot<T, EVAL> &P, const float4 *sm,
+                                              Pass1Acc<T> &acc, V &&visit) {
+  const T rc2 = P.rc2;
+  bool low = false;
+  visit([&](T, T dx, T dy, T dz, T r2) {
+    if (r2 > rc2) return;
+    acc.cnt++;
+    T phi, w, rho;
+    if (!eam_pair_w(P, sm, r2, phi, w, rho)) {
+      low = true;
+      return;
+    }
+    acc.add(phi, w, rho, dx, dy, dz);
+  });
+  if (low)  // pairs below the table: the series, in a second sweep
+    visit([&](T, T dx, T dy, T dz, T r2) {
+      if (r2 > rc2 || !below_seg(P, r2)) return;
+      T phi, w, rho;
+      pair_w_series(P, r2, phi, w, rho);
+      acc.add(phi, w, rho, dx, dy, dz);
+    });
+}
+
+// per-atom results of pass 1: F and F' fused in (eam.c:576-594)
+template <class T, int EVAL>
+__device__ __forceinline__ float eam_pass1_store(const ForceArgs &A, const EamPot<T, EVAL> &P,
+                                                 Pass1Acc<T> &acc, int slot) {
+  double rho_i = acc.rh.value();
   T F, dF;
   eam_embed<T, EVAL>(P, (T)rho_i, F, dF);
   d4 fo;
-  fo.x = fx.value();
-  fo.y = fy.value();
-  fo.z = fz.value();
-  fo.w = ep.value() + (double)F;
+  fo.x = acc.fx.value();
+  fo.y = acc.fy.value();
+  fo.z = acc.fz.value();
+  fo.w = acc.ep.value() + (double)F;
   A.s.f[slot] = fo;
   A.s.rho[slot] = rho_i;
   A.s.fi[slot] = (double)dF;
   if (sizeof(T) == 4) A.s.fi32[slot] = (float)dF;
+  return (float)dF;
 }
 
 // grid-stride over the compact atoms; the grid is sized to the resident CTAs
@@ -723,62 +769,106 @@ template <class T, int EVAL>
 __global__ void __launch_bounds__(PASS_THREADS)
     eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<T, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 3 * P.seg.n);
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x)
-    eam_pass1_atom<T, EVAL>(A, P, seg_sm, a);
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
+    const int slot = A.atom_slot[a];
+    const int b = slot >> 6, i = slot & 63;
+    T xi, yi, zi;
+    PrecT<T>::pos(A.s, slot, xi, yi, zi);
+    Pass1Acc<T> acc;
+    acc.zero();
+    eam_pass1_sum(P, seg_sm, acc, [&](auto &&fn) {
+      for_each_neighbor<T, false, true>(A, a, b, i, xi, yi, zi, P.rc2,
+                                        [&](int, T dx, T dy, T dz, T r2) { fn(T(0), dx, dy, dz, r2); });
+    });
+    eam_pass1_store(A, P, acc, slot);
+  }
 }
 
 // ---------------------------------------------------------------------------
 // EAM pass 2: embedding force and stress
 // ---------------------------------------------------------------------------
-template <class T, int EVAL>
-__device__ __forceinline__ void eam_pass2_atom(const ForceArgs &A, const EamPot<T, EVAL> &P,
-                                               const float4 *sm, int a) {
-  const int slot = A.atom_slot[a];
-  const int b = slot >> 6, i = slot & 63;
-  T xi, yi, zi;
-  PrecT<T>::pos(A.s, slot, xi, yi, zi);
-  const T fii = PrecT<T>::fi(A.s, slot);
+template <class T>
+struct Pass2Acc {
   typename PrecT<T>::Acc fx, fy, fz, sx;
-  fx.zero(); fy.zero(); fz.zero(); sx.zero();
-  const T rc2 = P.rc2;
-  auto fn = [&](int js, T dx, T dy, T dz, T r2) {
-    if (r2 >= rc2) return;
-    T wr = eam_embed_w(P, sm, r2, fii + PrecT<T>::fi(A.s, js));
+  __device__ __forceinline__ void zero() { fx.zero(); fy.zero(); fz.zero(); sx.zero(); }
+  __device__ __forceinline__ void add(T wr, T dx, T dy, T dz) {
     fx.add(wr * dx);
     fy.add(wr * dy);
     fz.add(wr * dz);
     sx.add(wr * dx * dx);
-  };
-  for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, rc2, fn);
+  }
+};
+
+// visit(fn) calls fn(F'_j, dx, dy, dz, r2) per neighbour
+template <class T, int EVAL, class V>
+__device__ __forceinline__ void eam_pass2_sum(const EamPot<T, EVAL> &P, const float4 *sm, T fii,
+                                              Pass2Acc<T> &acc, V &&visit) {
+  const T rc2 = P.rc2;
+  bool low = false;
+  visit([&](T fj, T dx, T dy, T dz, T r2) {
+    if (r2 >= rc2) return;
+    T wr;
+    if (!eam_embed_w(P, sm, r2, fii + fj, wr)) {
+      low = true;
+      return;
+    }
+    acc.add(wr, dx, dy, dz);
+  });
+  if (low)
+    visit([&](T fj, T dx, T dy, T dz, T r2) {
+      if (r2 >= rc2 || !below_seg(P, r2)) return;
+      acc.add(embed_w_series(P, r2, fii + fj), dx, dy, dz);
+    });
+}
+
+template <class T>
+__device__ __forceinline__ void eam_pass2_store(const ForceArgs &A, Pass2Acc<T> &acc, int slot,
+                                                int a) {
   d4 fo = A.s.f[slot];
-  fo.x += fx.value();
-  fo.y += fy.value();
-  fo.z += fz.value();
+  fo.x += acc.fx.value();
+  fo.y += acc.fy.value();
+  fo.z += acc.fz.value();
   A.s.f[slot] = fo;
-  A.atom_stress[a] = sx.value();
+  A.atom_stress[a] = acc.sx.value();
 }
 
 template <class T, int EVAL>
 __global__ void __launch_bounds__(PASS_THREADS)
     eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<T, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p2, P.seg.n);
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x)
-    eam_pass2_atom<T, EVAL>(A, P, seg_sm, a);
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
+    const int slot = A.atom_slot[a];
+    const int b = slot >> 6, i = slot & 63;
+    T xi, yi, zi;
+    PrecT<T>::pos(A.s, slot, xi, yi, zi);
+    Pass2Acc<T> acc;
+    acc.zero();
+    eam_pass2_sum(P, seg_sm, PrecT<T>::fi(A.s, slot), acc, [&](auto &&fn) {
+      for_each_neighbor<T, true>(A, a, b, i, xi, yi, zi, P.rc2,
+                                 [&](int js, T dx, T dy, T dz, T r2) {
+                                   fn(PrecT<T>::fi(A.s, js), dx, dy, dz, r2);
+                                 });
+    });
+    eam_pass2_store(A, acc, slot, a);
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Force-order passes (mixed precision, persistent lists)
 // ---------------------------------------------------------------------------
+constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
+
 // k - 1 as a float for 0 <= k < 2^22 (exponent-field trick: two instructions)
 __device__ __forceinline__ float small_int_minus1(int k) {
   return __int_as_float(0x4B000000 | k) - 8388609.0f;
 }
 
-// Visit the list of force-order atom a at FP32 position (xi, yi, zi):
-// fn(fj, dx, dy, dz, r2) for every entry, fj = F'(rho_j) when NEED_FI.  An
-// overflowed list scans the stencil of the atom's current slot instead.
+// Visit the list of force-order atom a at FP32 position pi: fn(fj, dx, dy,
+// dz, r2) for every entry; with NEED_FI positions come from fo.pf and fj is
+// F'(rho_j) (its w), else fj is unspecified.  An overflowed list scans the
+// stencil of the atom's current slot instead.
 template <bool NEED_FI, class F>
 __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot, float4 pi,
                                             float rc2, F &&fn) {
@@ -794,12 +884,12 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   const float hx = A.fo.hi[0], hy = A.fo.hi[1], hz = A.fo.hi[2];
   const float lx = A.fo.lo[0], ly = A.fo.lo[1], lz = A.fo.lo[2];
   const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
+  const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
 #pragma unroll 2
   for (int t = 0; t < n; t++) {
     const uint32_t p = __ldg(lst + (size_t)t * 32);
     const int j = (int)(p >> 5), c = (int)(p & 31u);
-    const float4 q = __ldg(A.fo.pos + j);
-    const float fj = NEED_FI ? __ldg(A.fo.fi + j) : 0.f;
+    const float4 q = __ldg(pj + j);
     // code = (dx+1)*9 + (dy+1)*3 + (dz+1); the pair offset is -d * boxsize
     const int cx = (c * 57) >> 9, rem = c - 9 * cx;
     const int cy = (rem * 11) >> 5, cz = rem - 3 * cy;
@@ -808,47 +898,25 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
     const float dx = fmaf(ex, lx, fmaf(ex, hx, pi.x - q.x));
     const float dy = fmaf(ey, ly, fmaf(ey, hy, pi.y - q.y));
     const float dz = fmaf(ez, lz, fmaf(ez, hz, pi.z - q.z));
-    fn(fj, dx, dy, dz, fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+    fn(q.w, dx, dy, dz, fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
   }
 }
 
 template <int EVAL>
-__global__ void __launch_bounds__(PASS_THREADS)
+__global__ void __launch_bounds__(FO1_THREADS, 2)
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 3 * P.seg.n);
-  const float rc2 = P.rc2;
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
-    KSum fx, fy, fz, ep, rh;
-    fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
-    int cnt = 0;
-    auto fn = [&](float, float dx, float dy, float dz, float r2) {
-      if (r2 > rc2) return;
-      cnt++;
-      float phi, w, rho;
-      eam_pair_w(P, seg_sm, r2, phi, w, rho);
-      fx.add(w * dx);
-      fy.add(w * dy);
-      fz.add(w * dz);
-      ep.add(phi * 0.5f);
-      rh.add(rho);
-    };
-    fo_for_each<false>(A, a, slot, A.fo.pos[a], rc2, fn);
-    const double rho_i = rh.value();
-    float F, dF;
-    eam_embed<float, EVAL>(P, (float)rho_i, F, dF);
-    d4 fo;
-    fo.x = fx.value();
-    fo.y = fy.value();
-    fo.z = fz.value();
-    fo.w = ep.value() + (double)F;
-    A.s.f[slot] = fo;
-    A.s.rho[slot] = rho_i;
-    A.s.fi[slot] = (double)dF;
-    A.s.fi32[slot] = dF;
-    A.fo.fi[a] = dF;
-    A.nbr_n[a] = cnt;
+    const float4 pi = A.fo.pos[a];
+    Pass1Acc<float> acc;
+    acc.zero();
+    eam_pass1_sum(P, seg_sm, acc,
+                  [&](auto &&fn) { fo_for_each<false>(A, a, slot, pi, P.rc2, fn); });
+    const float dF = eam_pass1_store(A, P, acc, slot);
+    A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
+    A.nbr_n[a] = acc.cnt;
   }
 }
 
@@ -856,28 +924,15 @@ template <int EVAL>
 __global__ void __launch_bounds__(PASS_THREADS)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p2, P.seg.n);
-  const float rc2 = P.rc2;
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
-    const float fii = A.fo.fi[a];
-    KSum fx, fy, fz, sx;
-    fx.zero(); fy.zero(); fz.zero(); sx.zero();
-    auto fn = [&](float fj, float dx, float dy, float dz, float r2) {
-      if (r2 >= rc2) return;
-      const float wr = eam_embed_w(P, seg_sm, r2, fii + fj);
-      fx.add(wr * dx);
-      fy.add(wr * dy);
-      fz.add(wr * dz);
-      sx.add(wr * dx * dx);
-    };
-    fo_for_each<true>(A, a, slot, A.fo.pos[a], rc2, fn);
-    d4 fo = A.s.f[slot];
-    fo.x += fx.value();
-    fo.y += fy.value();
-    fo.z += fz.value();
-    A.s.f[slot] = fo;
-    A.atom_stress[a] = sx.value();
+    const float4 pi = A.fo.pf[a];
+    Pass2Acc<float> acc;
+    acc.zero();
+    eam_pass2_sum(P, seg_sm, pi.w, acc,
+                  [&](auto &&fn) { fo_for_each<true>(A, a, slot, pi, P.rc2, fn); });
+    eam_pass2_store(A, acc, slot, a);
   }
 }
 

@@ -15,18 +15,18 @@ static int g_fo_per_sm[3][2];  // force order: [pass 1, pass 2, LJ][eval]
 static int g_num_sms = 1;
 
 template <class K>
-static cudaError_t pass_occupancy(K kernel, size_t smem, int *out) {
+static cudaError_t pass_occupancy(K kernel, size_t smem, int *out, int threads = PASS_THREADS) {
   cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kernel, PASS_THREADS, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, kernel, threads, smem);
   if (*out < 1) *out = 1;
   return e;
 }
 
 static size_t pass_smem(int pass, int eval) {
   if (sizeof(FT) != 4 || eval != EVAL_CHEBY) return 0;
-  return sizeof(float4) * (pass == 0 ? 3 : 1) * SEG_N;
+  return sizeof(float4) * (pass == 0 ? 2 : 1) * SEG_N;
 }
 
 // called on the current device before any launch or stream capture
@@ -50,10 +50,11 @@ cudaError_t prepare_force_kernels<FT>() {
   if (e != cudaSuccess) return e;
 #if COMDGB_FT_FLOAT
   {
-    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[0][EVAL_TABLE]);
+    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[0][EVAL_TABLE],
+                       FO1_THREADS);
     if (e == cudaSuccess)
       e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY>, pass_smem(0, EVAL_CHEBY),
-                         &g_fo_per_sm[0][EVAL_CHEBY]);
+                         &g_fo_per_sm[0][EVAL_CHEBY], FO1_THREADS);
     if (e == cudaSuccess)
       e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[1][EVAL_TABLE]);
     if (e == cudaSuccess)
@@ -71,8 +72,9 @@ cudaError_t prepare_force_kernels<FT>() {
 }
 
 // grid of a pass: every atom one thread, capped at the resident CTAs
-static int pass_grid(int pass, int eval, int ntot, bool fo = false) {
-  long need = (ntot + PASS_THREADS - 1) / PASS_THREADS;
+static int pass_grid(int pass, int eval, int ntot, bool fo = false,
+                     int threads = PASS_THREADS) {
+  long need = (ntot + threads - 1) / threads;
   long cap = (long)g_num_sms * (fo ? g_fo_per_sm[pass][eval] : g_pass_per_sm[pass][eval]);
   return (int)(need < cap ? need : cap);
 }
@@ -98,9 +100,11 @@ template <int EVAL>
 void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st) {
   if (A.ntot <= 0) return;
   const size_t smem = P.seg.n > 0 ? pass_smem(pass, EVAL) : 0;
-  const int grid = pass_grid(pass, EVAL, A.ntot, true);
-  if (pass == 0) fo_eam_pass1_kernel<EVAL><<<grid, PASS_THREADS, smem, st>>>(A, P);
-  else fo_eam_pass2_kernel<EVAL><<<grid, PASS_THREADS, smem, st>>>(A, P);
+  if (pass == 0)
+    fo_eam_pass1_kernel<EVAL><<<pass_grid(0, EVAL, A.ntot, true, FO1_THREADS), FO1_THREADS, smem,
+                                st>>>(A, P);
+  else
+    fo_eam_pass2_kernel<EVAL><<<pass_grid(1, EVAL, A.ntot, true), PASS_THREADS, smem, st>>>(A, P);
 }
 template void launch_fo_eam<EVAL_TABLE>(const ForceArgs &, const EamPot<float, EVAL_TABLE> &,
                                         int, cudaStream_t);
