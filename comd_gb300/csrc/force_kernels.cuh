@@ -860,6 +860,12 @@ __global__ void __launch_bounds__(PASS_THREADS)
 // ---------------------------------------------------------------------------
 constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
 
+constexpr int FO_PREFETCH = 8;    // list lines fetched ahead
+
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
 // k - 1 as a float for 0 <= k < 2^22 (exponent-field trick: two instructions)
 __device__ __forceinline__ float small_int_minus1(int k) {
   return __int_as_float(0x4B000000 | k) - 8388609.0f;
@@ -885,8 +891,11 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   const float lx = A.fo.lo[0], ly = A.fo.lo[1], lz = A.fo.lo[2];
   const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
+  // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1
+  // while line t is used (within this atom's list only)
 #pragma unroll 2
   for (int t = 0; t < n; t++) {
+    if (t + FO_PREFETCH < n) prefetch_l1(lst + (size_t)(t + FO_PREFETCH) * 32);
     const uint32_t p = __ldg(lst + (size_t)t * 32);
     const int j = (int)(p >> 5), c = (int)(p & 31u);
     const float4 q = __ldg(pj + j);
