@@ -490,9 +490,8 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
   // persistent lists are built with rc + skin, and only when a rebuild is due
   const double rcl = h->cutoff + h->skin;
   if (h->fo.list) {
-    // force order: positions of this step (and the rebuild test), then the
-    // list build if due, then the passes
-    launch_fo_refresh(h->g, h->s, h->fo, h->pl.slot_of, h->ntot, h->status, st);
+    // force order (positions were placed by the half step before, or by
+    // fo_track): the list build if due, then the passes
     launch_nbr_build<float>(A, (float)(rcl * rcl), st);
     launch_rebuild_done(h->status, st);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
@@ -607,6 +606,8 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool
     // the last half step of a step leaves the FP32 copy stale
     if (h->mixed) launch_pos32(h->g, h->s, h->stream);
     if (h->pl.vlist) launch_skin_check(h->g, h->s, h->pl, h->mixed, h->status, h->stream);
+    if (h->fo.list)
+      launch_fo_track(h->g, h->s, h->fo, h->atom_slot, h->ntot, h->status, h->stream);
     enqueue_force_parts(h, nullptr, evi);
     enqueue_reduce(h);
   }
@@ -682,6 +683,8 @@ int upload(comdgb_sim *h, const simflat_t *s) {
   CK(cudaMemsetAsync(h->status, 0, sizeof(int) * ST_COUNT, st));
   if (h->pl.slot_of) {  // new host state: map ids to slots and rebuild the lists
     launch_slot_of(h->g, h->s, h->pl, h->ntot, h->status, st);
+    if (h->fo.of_id)
+      CK(cudaMemsetAsync(h->fo.of_id, 0xff, sizeof(int) * ((size_t)h->ntot + 1), st));
     CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
   }
   enqueue_compact(h);
@@ -766,6 +769,7 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
     h->g.nbx[j] = s->nbx[j];
     h->g.bounds[j] = s->bounds[j];
     h->g.boxsize[j] = s->boxsize[j];
+    h->g.half[j] = 0.5 * s->boxsize[j];
   }
   h->g.nboxes = s->nboxes;
   h->g.periodic = o->periodic;
@@ -808,7 +812,8 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
       h->fo.list = track(h, dalloc<uint32_t>(rows * vcap, &err));
       h->fo.n = track(h, dalloc<int>(n1, &err));
       h->fo.id = track(h, dalloc<int>(n1, &err));
-      h->fo.ref = track(h, dalloc<d4>(n1, &err));
+      h->fo.of_id = track(h, dalloc<int>(n1, &err));
+      h->fo.ref = track(h, dalloc<float4>(n1, &err));
       h->fo.pos = track(h, dalloc<float4>(n1, &err));
       h->fo.slot = track(h, dalloc<int>(n1, &err));
       h->fo.pf = track(h, dalloc<float4>(n1, &err));
@@ -816,8 +821,8 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
         h->fo.hi[k] = (float)s->boxsize[k];
         h->fo.lo[k] = (float)(s->boxsize[k] - (double)h->fo.hi[k]);
       }
-      const double hs = 0.5 * h->skin - 1e-6;
-      h->fo.half_skin2 = hs * hs;
+      const double hs = 0.5 * h->skin - 1e-5;  // FP32 displacements err by < 1e-6 A
+      h->fo.half_skin2 = (float)(hs * hs);
     } else {
       h->pl.vcap = vcap;
       h->pl.vlist = track(h, dalloc<int>((size_t)h->ntot * vcap + 4, &err));
@@ -827,6 +832,12 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
       h->pl.half_skin2 = (float)(hs * hs);
     }
     h->w.pl = h->pl;
+    if (h->fo.list) {
+      h->w.fo = h->fo;
+      h->w.map = SlotMap{nullptr, h->fo.of_id, h->fo.slot};
+    } else {
+      h->w.map = SlotMap{h->pl.slot_of, nullptr, nullptr};
+    }
   }
   // per-step list: built each step, or (persistent lists) left by pass 1
   h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
@@ -929,6 +940,12 @@ void comdgb_default_opts(comdgb_opts *o) {
   o->cheby_from_host = 0;
   o->list_mode = COMDGB_LIST_AUTO;
   o->skin = 0.3;
+}
+
+int comdgb_round_f32(const double *x, float *y, long n) {
+  if ((!x || !y) && n > 0) return set_err(COMDGB_ERR_ARG, "null argument");
+  for (long i = 0; i < n; i++) y[i] = d2f_rn(x[i]);
+  return 0;
 }
 
 int comdgb_fp32_fma_peak(int device, double *tflops) {

@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 #define CG_MAXATOMS 64
@@ -32,8 +33,50 @@ struct Geom {
   int periodic;
   double bounds[3];
   double boxsize[3];
+  double half[3];   // boxsize / 2: the box centre of the FP32 positions
   const int *boxc;  // [nboxes] packed box coordinates ix | iy << 10 | iz << 20
 };
+
+// RN(x) to FP32 from the IEEE bits with integer operations (the FP64 pipe of
+// this part issues two operations per SM per clock); results that are not
+// normal FP32 numbers take the hardware conversion.
+__host__ __device__ __forceinline__ float d2f_rn(double x) {
+#ifdef __CUDA_ARCH__
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long b;
+  memcpy(&b, &x, sizeof b);
+#endif
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)x;
+  const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);  // top 23 of 52 bits
+  const unsigned rest = lo & 0x1fffffffu;                    // the 29 dropped bits
+  unsigned f = (hi & 0x80000000u) | ((unsigned)e << 23) | m;
+  if (rest > 0x10000000u || (rest == 0x10000000u && (m & 1u))) f += 1u;  // ties to even
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(f);
+#else
+  float y;
+  memcpy(&y, &f, sizeof y);
+  return y;
+#endif
+}
+
+// FP32 position relative to the box centre, RN(x - boxsize/2): one FP64
+// subtraction and the integer rounding per coordinate
+__device__ __forceinline__ float4 centred32(const Geom &g, double x, double y, double z) {
+  return make_float4(d2f_rn(x - g.half[0]), d2f_rn(y - g.half[1]), d2f_rn(z - g.half[2]), 0.f);
+}
+
+// which side of [0, hi) x lies on (-1: x < 0, +1: x >= hi, 0: inside or NaN)
+// for a finite hi > 0, by integer compares of the IEEE bits
+__device__ __forceinline__ int side_of(double x, double hi) {
+  const long long b = __double_as_longlong(x);
+  const long long inf = 0x7ff0000000000000LL;
+  if (b < 0) return (b != (long long)0x8000000000000000ULL && (b & 0x7fffffffffffffffLL) <= inf) ? -1 : 0;
+  return (b >= __double_as_longlong(hi) && b <= inf) ? 1 : 0;
+}
 
 // box coordinates from the packed table (avoids integer division)
 __device__ __forceinline__ void box_ixyz_tab(const Geom &g, int b, int *ix) {
@@ -112,12 +155,27 @@ struct ForceOrder {
   int *n;            // [ntot] list length (> vcap: overflowed, the stencil is scanned)
   int vcap;
   int *id;           // [ntot] atom id of a
-  d4 *ref;           // [ntot] FP64 box-relative position at the build; w = build box
+  int *of_id;        // [ntot] force-order number of atom id (-1 before the first build)
+  float4 *ref;       // [ntot] FP32 position at the build (build-box centred); w = build box
   float4 *pos;       // [ntot] FP32 position relative to the build box centre
-  int *slot;         // [ntot] current slot of a
+  int *slot;         // [ntot] current slot of a (kept by the rebin)
   float4 *pf;        // [ntot] EAM: pos with w = F'(rho) of a (written by pass 1 for pass 2)
   float hi[3], lo[3];  // box size as FP32 hi + lo
-  double half_skin2;   // rebuild when an atom moved more than this squared
+  float half_skin2;    // rebuild when an atom moved more than this squared
+};
+
+// the slot of an atom moved by the rebin, in the maps the list mode keeps
+struct SlotMap {
+  int *slot_of;        // by id (id-keyed persistent lists) or null
+  const int *fo_of_id; // force order: id -> a, or null
+  int *fo_slot;        // force order: a -> slot
+  __device__ __forceinline__ void moved(int id, int ds) const {
+    if (slot_of) slot_of[id] = ds;
+    if (fo_slot) {
+      const int a = fo_of_id[id];
+      if (a >= 0) fo_slot[a] = ds;
+    }
+  }
 };
 
 // world-frame position in FP32 from the FP32 box-centred position (mixed

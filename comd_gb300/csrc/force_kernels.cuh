@@ -311,16 +311,13 @@ __device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i, bool 
   }
   const int a = A.box_start[b] + i;
   if (MODE == LIST_FO) {
-    const d4 r = A.s.r[slot];
-    d4 q;
-    q.x = r.x;
-    q.y = r.y;
-    q.z = r.z;
-    q.w = (double)b;
-    A.fo.ref[a] = q;
-    A.fo.id[a] = A.s.id[slot];
+    const float4 p = A.s.pos32[slot];
+    const int id = A.s.id[slot];
+    A.fo.ref[a] = make_float4(p.x, p.y, p.z, __int_as_float(b));
+    A.fo.id[a] = id;
+    A.fo.of_id[id] = a;
     A.fo.slot[a] = slot;
-    A.fo.pos[a] = A.s.pos32[slot];
+    A.fo.pos[a] = p;
   }
   return a;
 }

@@ -17,7 +17,9 @@ struct RebinWork {
   uint8_t *final_src;   // [nboxes*64] slot t <- old slot (<64) or placeholder 64+p
   uint8_t *dep_order;   // [nboxes*64] departure order (old slots)
   Slots stage;          // full records of departing atoms, indexed by old slot
-  Persist pl;           // persistent lists: id -> slot map to keep, displacement check
+  Persist pl;           // id-keyed persistent lists: displacement check
+  ForceOrder fo;        // force order: positions to track (fo.of_id null: none)
+  SlotMap map;          // slot maps the rebin keeps
 };
 
 // ---- md_kernels.cu ----
@@ -68,8 +70,8 @@ void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, c
 void launch_rebuild_done(int *status, cudaStream_t st);
 void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *status,
                        cudaStream_t st);
-void launch_fo_refresh(const Geom &g, Slots s, const ForceOrder &fo, const int *slot_of,
-                       int ntot, int *status, cudaStream_t st);
+void launch_fo_track(const Geom &g, Slots s, const ForceOrder &fo, const int *atom_slot,
+                     int ntot, int *status, cudaStream_t st);
 
 // ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----
 template <class T>

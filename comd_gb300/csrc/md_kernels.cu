@@ -93,16 +93,10 @@ void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, int *
 // the plan is invalid and a serial replay of reBoxAll runs instead.
 // ---------------------------------------------------------------------------
 
-// FP32 position relative to the box centre (mixed precision)
-__device__ __forceinline__ float4 centred32(const Geom &g, double x, double y, double z) {
-  return make_float4((float)(x - 0.5 * g.boxsize[0]), (float)(y - 0.5 * g.boxsize[1]),
-                     (float)(z - 0.5 * g.boxsize[2]), 0.f);
-}
-
 // move one atom's record; with persistent lists also re-point its id
 __device__ __forceinline__ void copy_record(const Slots &dst, int ds, const Slots &src, int ss,
-                                            bool mixed, int *slot_of = nullptr) {
-  if (slot_of) slot_of[src.id[ss]] = ds;
+                                            bool mixed, const SlotMap &map) {
+  map.moved(src.id[ss], ds);
   dst.id[ds] = src.id[ss];
   dst.itype[ds] = src.itype[ss];
   dst.mass[ds] = src.mass[ss];
@@ -122,18 +116,14 @@ __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int
   const int b = slot >> 6;
   int ixo[3], ixn[3];
   box_ixyz_tab(g, b, ixo);
+  const int sd[3] = {side_of(r.x, g.boxsize[0]), side_of(r.y, g.boxsize[1]),
+                      side_of(r.z, g.boxsize[2])};
+  if ((sd[0] | sd[1] | sd[2]) == 0) return;  // stays (the common case: no FP64 work)
   double rn[3] = {r.x, r.y, r.z};
-  const double rc[3] = {r.x, r.y, r.z};
   for (int k = 0; k < 3; k++) {
-    if (rc[k] < 0.0) {
-      ixn[k] = ixo[k] - 1;
-      rn[k] += g.boxsize[k];
-    } else if (rc[k] >= g.boxsize[k]) {
-      ixn[k] = ixo[k] + 1;
-      rn[k] -= g.boxsize[k];
-    } else {
-      ixn[k] = ixo[k];
-    }
+    ixn[k] = ixo[k] + sd[k];
+    if (sd[k] < 0) rn[k] += g.boxsize[k];
+    else if (sd[k] > 0) rn[k] -= g.boxsize[k];
   }
   const int jb = box_from_ixyz(g, ixn);
   if (jb < 0 || jb == b) return;
@@ -163,16 +153,46 @@ __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int
   }
 }
 
-// division by the (constant) mass: Markstein when rinv != 0, else IEEE
+// division by the (constant) mass: Markstein (MARK, rinv = RN(1/rmass)) or IEEE
+template <bool MARK>
 __device__ __forceinline__ double div_mass(double a, double rmass, double rinv) {
-  return rinv != 0.0 ? div_markstein(a, rmass, rinv) : a / rmass;
+  return MARK ? div_markstein(a, rmass, rinv) : a / rmass;
 }
 
-// One thread per atom of the compacted atom list (every lane of every warp
-// holds an atom, so no FP64 instruction is issued for an empty slot).
-// write32: also refresh the FP32 copy of the position (mixed precision; the
-// half step that ends a step skips it, the next one rewrites it first).
-template <bool POS, bool VEL>
+// Force order: the FP32 position of atom id (now in box b at box-relative
+// FP64 position r, FP32 centred position p32) relative to its build box
+// centre -- p32 itself while the atom is in its build box, else RN(r -
+// boxsize/2 + (b - build box) * boxsize), one rounding either way -- and the
+// rebuild test on its displacement since the build.  Before the first build
+// (no force-order number) a rebuild is due anyway.
+__device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, int b, int id,
+                                         const d4 &r, float4 p32, int *status) {
+  const int af = fo.of_id[id];
+  if (af < 0) return;
+  const float4 q = fo.ref[af];
+  int ixn[3], ixb[3];
+  box_ixyz_tab(g, b, ixn);
+  box_ixyz_tab(g, __float_as_int(q.w), ixb);
+  const double rv[3] = {r.x, r.y, r.z};
+  const float qv[3] = {q.x, q.y, q.z};
+  float pv[3] = {p32.x, p32.y, p32.z}, d2 = 0.f;
+  bool far = false;
+  for (int k = 0; k < 3; k++) {
+    int db = ixn[k] - ixb[k];
+    if (g.periodic) {
+      if (db > 1) db -= g.nbx[k];
+      else if (db < -1) db += g.nbx[k];
+    }
+    far |= db > 1 || db < -1;
+    if (db != 0) pv[k] = d2f_rn(fma((double)db, g.boxsize[k], rv[k] - g.half[k]));
+    const float d = pv[k] - qv[k];
+    d2 = fmaf(d, d, d2);
+  }
+  if (far || !(d2 <= fo.half_skin2)) atomicExch(status + ST_REBUILD, 1);
+  fo.pos[af] = make_float4(pv[0], pv[1], pv[2], 0.f);
+}
+
+template <bool POS, bool VEL, bool MARK>
 __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int *atom_slot,
                                                       int ntot, double dt_v, double dt_r,
                                                       double rmass, double rinv, bool mixed,
@@ -195,11 +215,15 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
     }
     if (POS) {
       // advancePositions, timestep.c:104: r + (dt*p)/rmass
-      r.x = r.x + div_mass(dt_r * p.x, rmass, rinv);
-      r.y = r.y + div_mass(dt_r * p.y, rmass, rinv);
-      r.z = r.z + div_mass(dt_r * p.z, rmass, rinv);
+      r.x = r.x + div_mass<MARK>(dt_r * p.x, rmass, rinv);
+      r.y = r.y + div_mass<MARK>(dt_r * p.y, rmass, rinv);
+      r.z = r.z + div_mass<MARK>(dt_r * p.z, rmass, rinv);
       s.r[slot] = r;
-      if (mixed && write32) s.pos32[slot] = centred32(g, r.x, r.y, r.z);
+      if (mixed && write32) {
+        const float4 p32 = centred32(g, r.x, r.y, r.z);
+        s.pos32[slot] = p32;
+        if (w.fo.of_id) fo_track(g, w.fo, b, s.id[slot], r, p32, status);
+      }
       if (!VEL && w.pl.rref) {
         // persistent lists: the half step before a force call decides
         // whether the lists are rebuilt (an atom moved more than skin/2)
@@ -232,27 +256,35 @@ void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int 
                               double rmass, bool mixed, bool classify, const RebinWork &w,
                               int *status, cudaStream_t st) {
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
-  if (ntot > 0)
-    advance_kernel<true, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, dt, rmass, mass_reciprocal(rmass), mixed, true, classify, w,
-        status);
+  if (ntot <= 0) return;
+  const double rinv = mass_reciprocal(rmass);
+  if (rinv != 0.0)
+    advance_kernel<true, false, true><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, w, status);
+  else
+    advance_kernel<true, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, w, status);
 }
 
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
                        cudaStream_t st) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
-  if (ntot > 0)
-    advance_kernel<true, true><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, dt_v, dt_r, rmass, mass_reciprocal(rmass), mixed, false, true, w,
-        status);
+  if (ntot <= 0) return;
+  const double rinv = mass_reciprocal(rmass);
+  if (rinv != 0.0)
+    advance_kernel<true, true, true><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, w, status);
+  else
+    advance_kernel<true, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, w, status);
 }
 
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                              cudaStream_t st) {
   RebinWork none{};
   if (ntot > 0)
-    advance_kernel<false, true><<<atom_blocks(ntot), 256, 0, st>>>(
+    advance_kernel<false, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
         g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, none, nullptr);
 }
 
@@ -260,7 +292,7 @@ void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, boo
                      const RebinWork &w, int *status, cudaStream_t st) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
   if (ntot > 0)
-    advance_kernel<false, false><<<atom_blocks(ntot), 256, 0, st>>>(
+    advance_kernel<false, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
         g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, w, status);
 }
 
@@ -380,7 +412,7 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
     for (int t = 0; t < L; t++) {
       int e = fs[t];
       if (e < CG_MAXATOMS && e != t)
-        copy_record(s, base + t, s, base + e, mixed, w.pl.slot_of);
+        copy_record(s, base + t, s, base + e, mixed, w.map);
     }
   // 2. lower arrivals into their placeholders, in (source, departure) order
   if (n_lo > 0) {
@@ -398,7 +430,7 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
     for (int t = 0; t < L; t++) {
       int e = fs[t];
       if (e >= CG_MAXATOMS)
-        copy_record(s, base + t, w.stage, src_of[e - CG_MAXATOMS], mixed, w.pl.slot_of);
+        copy_record(s, base + t, w.stage, src_of[e - CG_MAXATOMS], mixed, w.map);
     }
   }
   // 3. higher arrivals appended
@@ -411,7 +443,7 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
     for (int d = 0; d < nd; d++) {
       int j = ord[d];
       if (w.dest[sb * CG_MAXATOMS + j] == b) {
-        copy_record(s, base + L + h, w.stage, sb * CG_MAXATOMS + j, mixed, w.pl.slot_of);
+        copy_record(s, base + L + h, w.stage, sb * CG_MAXATOMS + j, mixed, w.map);
         h++;
       }
     }
@@ -421,7 +453,7 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
 
 // reBoxAll replayed serially on the device (used only when the parallel plan
 // cannot reproduce it); the reference algorithm, statement for statement
-__global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, int *slot_of) {
+__global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, SlotMap slot_of) {
   if (!*(volatile int *)(status + ST_REBIN_SERIAL)) return;
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   status[ST_SERIAL_RUNS] += 1;
@@ -471,7 +503,7 @@ void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w,
   unsigned nb = (unsigned)((g.nboxes + 127) / 128);
   rebin_plan_kernel<<<nb, 128, 0, st>>>(g, s, w, status);
   rebin_apply_kernel<<<nb, 128, 0, st>>>(g, s, mixed, w, status);
-  rebin_serial_kernel<<<1, 32, 0, st>>>(g, s, mixed, status, w.pl.slot_of);
+  rebin_serial_kernel<<<1, 32, 0, st>>>(g, s, mixed, status, w.map);
 }
 
 // ---------------------------------------------------------------------------
@@ -502,44 +534,21 @@ __global__ void rebuild_done_kernel(int *status) {
   }
 }
 
-// Force order, each force call before the list build: the current slot of
-// every force-order atom, its displacement since the build (FP64, box
-// difference taken minimum-image) and from it the FP32 position relative
-// to its build box centre.  A displacement beyond skin/2 flags a rebuild,
-// which then rewrites every record, so once the flag is up (set before this
-// launch, or by another thread) the remaining records are left alone.
-__global__ void __launch_bounds__(256) fo_refresh_kernel(Geom g, Slots s, ForceOrder fo,
-                                                         const int *slot_of, int ntot,
-                                                         int *status) {
+// Force order, standalone force calls: every atom's force-order position
+// from its refreshed FP32 position, and the rebuild test
+__global__ void __launch_bounds__(256) fo_track_kernel(Geom g, Slots s, ForceOrder fo,
+                                                       const int *atom_slot, int ntot,
+                                                       int *status) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= ntot || *(volatile int *)(status + ST_REBUILD)) return;
-  const int slot = slot_of[fo.id[a]];
-  fo.slot[a] = slot;
-  const d4 r = s.r[slot], q = fo.ref[a];
-  int ixn[3], ixb[3];
-  box_ixyz_tab(g, slot >> 6, ixn);
-  box_ixyz_tab(g, (int)q.w, ixb);
-  const double rv[3] = {r.x, r.y, r.z}, qv[3] = {q.x, q.y, q.z};
-  double d[3], d2 = 0.0;
-  float pv[3];
-  for (int k = 0; k < 3; k++) {
-    int db = ixn[k] - ixb[k];
-    if (g.periodic) {
-      if (db > 1) db -= g.nbx[k];
-      else if (db < -1) db += g.nbx[k];
-    }
-    d[k] = (rv[k] - qv[k]) + (double)db * g.boxsize[k];
-    d2 = d2 + d[k] * d[k];
-    pv[k] = (float)((qv[k] - 0.5 * g.boxsize[k]) + d[k]);
-  }
-  if (!(d2 <= fo.half_skin2)) atomicExch(status + ST_REBUILD, 1);
-  fo.pos[a] = make_float4(pv[0], pv[1], pv[2], 0.f);
+  if (a >= ntot) return;
+  const int slot = atom_slot[a];
+  fo_track(g, fo, slot >> 6, s.id[slot], s.r[slot], s.pos32[slot], status);
 }
 
-void launch_fo_refresh(const Geom &g, Slots s, const ForceOrder &fo, const int *slot_of,
-                       int ntot, int *status, cudaStream_t st) {
+void launch_fo_track(const Geom &g, Slots s, const ForceOrder &fo, const int *atom_slot,
+                     int ntot, int *status, cudaStream_t st) {
   if (ntot > 0)
-    fo_refresh_kernel<<<atom_blocks(ntot), 256, 0, st>>>(g, s, fo, slot_of, ntot, status);
+    fo_track_kernel<<<atom_blocks(ntot), 256, 0, st>>>(g, s, fo, atom_slot, ntot, status);
 }
 
 // skin test of every atom (standalone force calls: positions may have moved

@@ -8,6 +8,8 @@ import ctypes as C
 import os
 import threading
 
+import numpy as np
+
 from .abi import EamCheby, EamPotential, LjPotential, SimFlat
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -72,6 +74,7 @@ def _bind(lib):
                                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.comdgb_sim_graph_kernels.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.comdgb_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.comdgb_round_f32.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_long]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p
@@ -117,6 +120,15 @@ def fp32_peak_tflops(device=0):
     v = C.c_double()
     check(load().comdgb_fp32_fma_peak(device, C.byref(v)))
     return v.value
+
+
+def round_f32(x):
+    """FP64 -> FP32 (nearest, ties to even) by the library's integer routine."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    y = np.empty(x.shape, dtype=np.float32)
+    check(load().comdgb_round_f32(x.ctypes.data_as(C.POINTER(C.c_double)),
+                                  y.ctypes.data_as(C.POINTER(C.c_float)), x.size))
+    return y
 
 
 def last_error():

@@ -144,6 +144,9 @@ int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long
 /* measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops); the
  * peak the mixed-precision force kernels are compared against */
 int comdgb_fp32_fma_peak(int device, double *tflops);
+/* y[i] = x[i] rounded to FP32 (nearest, ties to even) by the integer routine
+ * the mixed-precision kernels use for positions; runs on the host */
+int comdgb_round_f32(const double *x, float *y, long n);
 
 /* ---------------- host-side setup (reference setup routines) ---------------- */
 

@@ -127,3 +127,22 @@ def test_bench_replicas_over_gloo():
     for p in ps:
         p.join(timeout=60)
     assert res == [(0, 3.0, 10.0), (1, 3.0, 10.0)]
+
+
+def test_round_f32_matches_ieee_nearest_even():
+    """The integer FP64 -> FP32 rounding of the mixed-precision positions
+    equals IEEE round-to-nearest-even (numpy's conversion), ties included."""
+    rng = np.random.default_rng(7)
+    x = np.concatenate([rng.uniform(-4.0, 4.0, 200000),
+                        rng.uniform(0.0, 1e-3, 1000), rng.normal(0.0, 1e3, 1000),
+                        [0.0, -0.0, 1.0, -1.0, 3.4e38, 1e-40, -1e-45, 1e300, np.inf, -np.inf]])
+    # exact ties: FP32 values plus half an FP32 ulp (representable in FP64)
+    f = rng.uniform(0.5, 4.0, 5000).astype(np.float32)
+    ulp = np.spacing(f).astype(np.float64)
+    x = np.concatenate([x, f.astype(np.float64) + 0.5 * ulp, f.astype(np.float64) - 0.5 * ulp])
+    with np.errstate(over="ignore"):
+        want = x.astype(np.float32)
+    got = cg.round_f32(x)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    nan = cg.round_f32(np.array([np.nan]))
+    assert np.isnan(nan[0])
