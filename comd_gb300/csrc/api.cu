@@ -483,6 +483,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
   // ev (optional) records after each group: compact, nbr, pass1, pass2
   ForceArgs A = force_args(h);
   cudaStream_t st = h->stream;
+  cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
                  st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
@@ -570,7 +571,7 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev) {
   // the atom list is the one made after the previous rebin
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
   launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass, h->mixed,
-                           true, h->w, h->status, st);
+                           true, h->w, h->status, st, true);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_classify_finish(h);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
@@ -1181,6 +1182,9 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
   if (kernel_ms)
     for (int k = 0; k < KG_COUNT && k < max_kernels; k++) kernel_ms[k] = (float)(ksum[k] / n);
   int rc = check_status(h);
+  if (rc) return rc;
+  // forces of the final positions, as nTimeSteps ends (timestep.c:137)
+  rc = do_force(h);
   if (rc) return rc;
   return KG_COUNT;
 }

@@ -125,6 +125,7 @@ enum {
   ST_SERIAL_RUNS = 3, // number of serial rebin fallbacks taken
   ST_REBUILD = 4,     // persistent lists: an atom moved more than skin/2
   ST_REBUILDS = 5,    // persistent lists: number of list builds
+  ST_DELTA = 6,       // f.xyz holds the half-step position increments (see advance_kernel)
   ST_COUNT = 8
 };
 

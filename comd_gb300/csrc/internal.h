@@ -30,10 +30,13 @@ double mass_reciprocal(double rmass);
 // The Verlet and classify kernels run one thread per atom of the compacted
 // atom list atom_slot (which must match the current layout).
 // r += dt*p/rmass (and optionally the classify step of reBoxAll)
+// use_delta: add the increments the previous step's last half step left in
+// f.xyz when the status word says they are there (step graphs only)
 void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
                               double rmass, bool mixed, bool classify, const RebinWork &w,
-                              int *status, cudaStream_t st);
-// p -= dt_v*f; r += dt_r*p/rmass; classify (the FP32 copy is not refreshed)
+                              int *status, cudaStream_t st, bool use_delta = false);
+// p -= dt_v*f; r += dt_r*p/rmass; classify (the FP32 copy is not refreshed);
+// leaves the position increments in f.xyz and says so in the status word
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
                        cudaStream_t st);

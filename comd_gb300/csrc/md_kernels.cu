@@ -192,22 +192,38 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
   fo.pos[af] = make_float4(pv[0], pv[1], pv[2], 0.f);
 }
 
+// delta: the two position half steps around a step boundary add the same
+// increment RN(RN(dt/2 * p) / rmass) -- p does not change in between -- so
+// the one that ends a step (DELTA_STORE) leaves it in f.xyz, which is dead
+// until the next force computation overwrites it, and the one that starts
+// the next step (DELTA_USE) adds it instead of recomputing it when the
+// status word ST_DELTA says f.xyz holds it (set after DELTA_STORE, cleared
+// by every force computation and upload).  Bit for bit the same positions.
+enum { DELTA_NONE = 0, DELTA_STORE = 1, DELTA_USE = 2 };
+
 template <bool POS, bool VEL, bool MARK>
 __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int *atom_slot,
                                                       int ntot, double dt_v, double dt_r,
                                                       double rmass, double rinv, bool mixed,
-                                                      bool write32, bool classify, RebinWork w,
-                                                      int *status) {
+                                                      bool write32, bool classify, int delta,
+                                                      RebinWork w, int *status) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= ntot) return;
   const int slot = atom_slot[a];
   const int b = slot >> 6;
   d4 r = s.r[slot];
-  if (POS || VEL) {
+  if (POS && !VEL && delta == DELTA_USE && *(volatile const int *)(status + ST_DELTA)) {
+    const d4 dl = s.f[slot];
+    r.x = r.x + dl.x;
+    r.y = r.y + dl.y;
+    r.z = r.z + dl.z;
+    s.r[slot] = r;
+  } else if (POS || VEL) {
     d4 p = s.p[slot];
+    d4 f;
     if (VEL) {
       // advanceVelocity, timestep.c:71
-      d4 f = s.f[slot];
+      f = s.f[slot];
       p.x = p.x - dt_v * f.x;
       p.y = p.y - dt_v * f.y;
       p.z = p.z - dt_v * f.z;
@@ -215,22 +231,33 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
     }
     if (POS) {
       // advancePositions, timestep.c:104: r + (dt*p)/rmass
-      r.x = r.x + div_mass<MARK>(dt_r * p.x, rmass, rinv);
-      r.y = r.y + div_mass<MARK>(dt_r * p.y, rmass, rinv);
-      r.z = r.z + div_mass<MARK>(dt_r * p.z, rmass, rinv);
+      const double ix = div_mass<MARK>(dt_r * p.x, rmass, rinv);
+      const double iy = div_mass<MARK>(dt_r * p.y, rmass, rinv);
+      const double iz = div_mass<MARK>(dt_r * p.z, rmass, rinv);
+      r.x = r.x + ix;
+      r.y = r.y + iy;
+      r.z = r.z + iz;
       s.r[slot] = r;
-      if (mixed && write32) {
-        const float4 p32 = centred32(g, r.x, r.y, r.z);
-        s.pos32[slot] = p32;
-        if (w.fo.of_id) fo_track(g, w.fo, b, s.id[slot], r, p32, status);
+      if (VEL && delta == DELTA_STORE) {
+        f.x = ix;
+        f.y = iy;
+        f.z = iz;
+        s.f[slot] = f;
       }
-      if (!VEL && w.pl.rref) {
-        // persistent lists: the half step before a force call decides
-        // whether the lists are rebuilt (an atom moved more than skin/2)
-        const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
-        if (disp2(g, wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
-          atomicExch(status + ST_REBUILD, 1);
-      }
+    }
+  }
+  if (POS) {
+    if (mixed && write32) {
+      const float4 p32 = centred32(g, r.x, r.y, r.z);
+      s.pos32[slot] = p32;
+      if (w.fo.of_id) fo_track(g, w.fo, b, s.id[slot], r, p32, status);
+    }
+    if (!VEL && w.pl.rref) {
+      // persistent lists: the half step before a force call decides
+      // whether the lists are rebuilt (an atom moved more than skin/2)
+      const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
+      if (disp2(g, wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
+        atomicExch(status + ST_REBUILD, 1);
     }
   }
   if (classify) classify_atom(g, s, slot, r, mixed, w, status);
@@ -254,30 +281,36 @@ double mass_reciprocal(double rmass) {
 
 void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
                               double rmass, bool mixed, bool classify, const RebinWork &w,
-                              int *status, cudaStream_t st) {
+                              int *status, cudaStream_t st, bool use_delta) {
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
   if (ntot <= 0) return;
   const double rinv = mass_reciprocal(rmass);
+  const int delta = use_delta ? DELTA_USE : DELTA_NONE;
   if (rinv != 0.0)
     advance_kernel<true, false, true><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, w, status);
+        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, delta, w, status);
   else
     advance_kernel<true, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, w, status);
+        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, delta, w, status);
 }
 
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
                        cudaStream_t st) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
-  if (ntot <= 0) return;
-  const double rinv = mass_reciprocal(rmass);
-  if (rinv != 0.0)
-    advance_kernel<true, true, true><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, w, status);
-  else
-    advance_kernel<true, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, w, status);
+  if (ntot > 0) {
+    const double rinv = mass_reciprocal(rmass);
+    if (rinv != 0.0)
+      advance_kernel<true, true, true><<<atom_blocks(ntot), 256, 0, st>>>(
+          g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, DELTA_STORE, w,
+          status);
+    else
+      advance_kernel<true, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
+          g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, DELTA_STORE, w,
+          status);
+  }
+  // f.xyz now holds the increments (the next position half step reuses them)
+  cudaMemsetAsync(status + ST_DELTA, 0x01, 1, st);
 }
 
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
@@ -285,7 +318,7 @@ void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int n
   RebinWork none{};
   if (ntot > 0)
     advance_kernel<false, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, none, nullptr);
+        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, DELTA_NONE, none, nullptr);
 }
 
 void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
@@ -293,7 +326,7 @@ void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, boo
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
   if (ntot > 0)
     advance_kernel<false, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, w, status);
+        g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, DELTA_NONE, w, status);
 }
 
 // distinct stencil boxes of b other than b, ascending
