@@ -782,7 +782,9 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   alloc_slots(h, h->s, true, &err);
   alloc_slots(h, h->w.stage, false, &err);
   h->w.dest = track(h, dalloc<int>(ns, &err));
-  h->w.depmask = track(h, dalloc<uint32_t>(2 * nb, &err));
+  h->w.depmask = track(h, dalloc<uint32_t>(4 * nb, &err));
+  h->w.arr_lo = reinterpret_cast<int *>(h->w.depmask + 2 * nb);
+  h->w.arr_hi = h->w.arr_lo + nb;
   h->w.n_lo = track(h, dalloc<int>(nb, &err));
   h->w.n_dep = track(h, dalloc<int>(nb, &err));
   h->w.final_len = track(h, dalloc<int>(nb, &err));

@@ -11,6 +11,8 @@ namespace cg {
 struct RebinWork {
   int *dest;            // [nslots] destination box of a departing atom
   uint32_t *depmask;    // [2*nboxes] departure bits of slots 0-31 / 32-63
+  int *arr_lo, *arr_hi; // [nboxes] arrivals from lower / higher boxes (same
+                        // allocation as depmask, cleared with it: 4*nboxes words)
   int *n_lo;            // [nboxes] arrivals from lower-index boxes
   int *n_dep;           // [nboxes]
   int *final_len;       // [nboxes] occupancy after the box's own scan

@@ -128,6 +128,7 @@ __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int
   const int jb = box_from_ixyz(g, ixn);
   if (jb < 0 || jb == b) return;
   atomicOr(w.depmask + (slot >> 5), 1u << (slot & 31));
+  atomicAdd(b < jb ? w.arr_lo + jb : w.arr_hi + jb, 1);
   w.dest[slot] = jb;
   Slots st = w.stage;
   st.id[slot] = s.id[slot];
@@ -282,7 +283,7 @@ double mass_reciprocal(double rmass) {
 void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
                               double rmass, bool mixed, bool classify, const RebinWork &w,
                               int *status, cudaStream_t st, bool use_delta) {
-  if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
+  if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   if (ntot <= 0) return;
   const double rinv = mass_reciprocal(rmass);
   const int delta = use_delta ? DELTA_USE : DELTA_NONE;
@@ -297,7 +298,7 @@ void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int 
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
                        cudaStream_t st) {
-  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
+  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   if (ntot > 0) {
     const double rinv = mass_reciprocal(rmass);
     if (rinv != 0.0)
@@ -323,7 +324,7 @@ void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int n
 
 void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
                      const RebinWork &w, int *status, cudaStream_t st) {
-  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 2 * (size_t)g.nboxes, st);
+  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   if (ntot > 0)
     advance_kernel<false, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
         g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, DELTA_NONE, w, status);
@@ -368,17 +369,7 @@ __global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status) {
   if (*(volatile int *)(status + ST_REBIN_SERIAL)) return;
   const unsigned long long mask = box_mask(w, b);
   const int n = s.natoms[b];
-  int src[26];
-  const int ns = source_boxes(g, b, src);
-  int n_lo = 0;
-  for (int q = 0; q < ns && src[q] < b; q++) {
-    unsigned long long m = box_mask(w, src[q]);
-    while (m) {
-      int j = __ffsll((long long)m) - 1;
-      m &= m - 1;
-      n_lo += (w.dest[src[q] * CG_MAXATOMS + j] == b);
-    }
-  }
+  const int n_lo = w.arr_lo[b];  // counted by the classify step
   w.n_lo[b] = n_lo;
   if (mask == 0ull && n_lo == 0) {
     w.n_dep[b] = 0;
@@ -419,21 +410,11 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
   if (*(volatile int *)(status + ST_ERROR)) return;
   const unsigned long long mask = box_mask(w, b);
   const int n_lo = w.n_lo[b];
+  const int n_hi = w.arr_hi[b];  // counted by the classify step
+  if (mask == 0ull && n_lo == 0 && n_hi == 0) return;
   const int L = w.final_len[b];
   int src[26];
   const int ns = source_boxes(g, b, src);
-  // is anything arriving from a higher box?
-  int n_hi = 0;
-  for (int q = 0; q < ns; q++) {
-    if (src[q] < b) continue;
-    unsigned long long m = box_mask(w, src[q]);
-    while (m) {
-      int j = __ffsll((long long)m) - 1;
-      m &= m - 1;
-      n_hi += (w.dest[src[q] * CG_MAXATOMS + j] == b);
-    }
-  }
-  if (mask == 0ull && n_lo == 0 && n_hi == 0) return;
   if (n_hi > 0 && L + n_hi >= CG_MAXATOMS) {
     set_error(status, -11);
     return;
@@ -608,7 +589,7 @@ void launch_rebuild_done(int *status, cudaStream_t st) {
 // compaction: box_start = exclusive scan of natoms; atom_slot[a] = slot
 // ---------------------------------------------------------------------------
 #define CP_THREADS 256
-#define CP_PER 8
+#define CP_PER 2
 #define CP_CHUNK (CP_THREADS * CP_PER)
 
 int compact_partials(int nboxes) { return (nboxes + CP_CHUNK - 1) / CP_CHUNK; }
@@ -664,30 +645,41 @@ __global__ void __launch_bounds__(CP_THREADS) compact_scan_partials_kernel(int *
   }
 }
 
+// box offsets from the block's scan, then each warp writes whole boxes'
+// atom entries (coalesced)
 __global__ void __launch_bounds__(CP_THREADS) compact_write_kernel(const int *natoms, int nboxes,
                                                                    const int *partials,
                                                                    int *box_start,
                                                                    int *atom_slot, int ntot) {
   __shared__ int sh[CP_THREADS / 32];
-  int base = blockIdx.x * CP_CHUNK + threadIdx.x * CP_PER;
+  __shared__ int s_off[CP_CHUNK], s_n[CP_CHUNK];
+  const int b0 = blockIdx.x * CP_CHUNK;
   int loc[CP_PER];
   int v = 0;
   for (int q = 0; q < CP_PER; q++) {
-    loc[q] = (base + q < nboxes) ? natoms[base + q] : 0;
+    const int b = b0 + threadIdx.x * CP_PER + q;
+    loc[q] = b < nboxes ? natoms[b] : 0;
     v += loc[q];
   }
   int total;
   int off = block_excl_scan(v, sh, total) + partials[blockIdx.x];
   for (int q = 0; q < CP_PER; q++) {
-    int b = base + q;
+    const int i = threadIdx.x * CP_PER + q, b = b0 + i;
+    s_off[i] = off;
+    s_n[i] = loc[q];
     if (b < nboxes) {
       box_start[b] = off;
-      // the counts sum to ntot unless a reported overflow left them inconsistent
-      for (int k = 0; k < loc[q]; k++)
-        if (off + k < ntot) atom_slot[off + k] = b * CG_MAXATOMS + k;
-      off += loc[q];
-      if (b == nboxes - 1) box_start[nboxes] = off;
+      if (b == nboxes - 1) box_start[nboxes] = off + loc[q];
     }
+    off += loc[q];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, nbk = min(CP_CHUNK, nboxes - b0);
+  for (int i = threadIdx.x >> 5; i < nbk; i += CP_THREADS / 32) {
+    const int o = s_off[i], n = s_n[i], base = (b0 + i) * CG_MAXATOMS;
+    // the counts sum to ntot unless a reported overflow left them inconsistent
+    for (int k = lane; k < n; k += 32)
+      if (o + k < ntot) atom_slot[o + k] = base + k;
   }
 }
 
