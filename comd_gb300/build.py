@@ -30,6 +30,7 @@ UNITS = [
     ("force_mixed.cu", []),
     ("api.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
+    ("adjoint.cu", []),
 ]
 CUNITS = ["host_setup.c"]
 

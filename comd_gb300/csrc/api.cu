@@ -10,12 +10,12 @@
 #include <mutex>
 #include <vector>
 
-#include "comdgb.h"
-#include "internal.h"
+#include "sim.h"
 
 using namespace cg;
+using namespace cgapi;
 
-namespace {
+namespace cgapi {
 
 thread_local char g_err[512] = "";
 std::mutex g_reg_mu;
@@ -27,18 +27,6 @@ int set_err(int code, const char *fmt, ...) {
   va_end(ap);
   return code;
 }
-
-#define CK(call)                                                                        \
-  do {                                                                                  \
-    cudaError_t e_ = (call);                                                            \
-    if (e_ != cudaSuccess)                                                              \
-      return set_err(COMDGB_ERR_CUDA, "%s failed: %s (%s:%d)", #call,                   \
-                     cudaGetErrorString(e_), __FILE__, __LINE__);                       \
-  } while (0)
-
-// bohr_per_atu_to_A_per_s (constants.h:61) and amu_to_m_e (constants.h:65)
-const double kBohrPerAtu = (double)0.529 / (double)2.418e-17;
-const double kAmuToMe = 1822.83;
 
 enum KernelGroup {
   KG_ADV_POS = 0,
@@ -57,77 +45,9 @@ const char *kGroupName[KG_COUNT] = {"advance_positions+classify", "rebin_plan_ap
                                     "advance_velocity_positions+classify",
                                     "rebin_plan_apply_2"};
 
-template <class T>
-T *dalloc(size_t n, int *err) {
-  void *p = nullptr;
-  if (n == 0) n = 1;
-  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
-    *err = 1;
-    return nullptr;
-  }
-  return (T *)p;
-}
-
 }  // namespace
 
-struct comdgb_sim {
-  int device = 0;
-  comdgb_opts opts{};
-  bool mixed = false;
-  cudaStream_t stream = nullptr;
-  Geom g{};
-  int ntot = 0, nslots = 0;
-  double rmass = 1.0, cutoff = 0.0;
-  double volume = 1.0;
-  std::vector<void *> allocs;
-  Slots s{};
-  RebinWork w{};
-  Persist pl{};        // persistent lists (all null when lists are rebuilt each step)
-  ForceOrder fo{};     // mixed precision: persistent lists in force order
-  double skin = 0.0;
-  EntryTab et{};
-  double *dcenter = nullptr;
-  int *boxc = nullptr;
-  int *box_start = nullptr, *atom_slot = nullptr, *cpart = nullptr;
-  int ncpart = 0;
-  uint16_t *nbr = nullptr;
-  int *nbr_n = nullptr;
-  int cap = 0;
-  double *atom_stress = nullptr;
-  double *rpart = nullptr;
-  long long *ripart = nullptr;
-  int nrpart = 0;
-  double *d_out = nullptr;     // [0] energy sum [1] stress sum [2] kinetic
-  long long *d_iout = nullptr; // [0] directed pair count
-  int *status = nullptr;
-  double *stage3 = nullptr;    // real3 staging for host transfers
-  int *bin_tmp = nullptr;
-  // potentials
-  EamPot<double, EVAL_TABLE> eam64t{};
-  EamPot<double, EVAL_CHEBY> eam64c{};
-  EamPot<float, EVAL_TABLE> eam32t{};
-  EamPot<float, EVAL_CHEBY> eam32c{};
-  LjPot<double> lj64{};
-  LjPot<float> lj32{};
-  double lj_eps = 0, lj_s6 = 0;
-  // graphs
-  cudaGraphExec_t step_exec = nullptr;
-  cudaGraphExec_t force_exec = nullptr;
-  double graph_dt = NAN;
-  // timing graph (event record nodes between kernel groups)
-  cudaGraphExec_t timed_exec = nullptr;
-  cudaGraph_t timed_graph = nullptr;
-  double timed_dt = NAN;
-  std::vector<cudaGraphNode_t> timed_nodes;  // event record nodes, group order
-  std::vector<cudaEvent_t> timed_cap_events;
-  int step_kernels = 0, force_kernels = 0;  // kernel nodes per captured graph
-  // host last results
-  double e = 0.0, stress = 0.0;
-  simflat_t *host = nullptr;   // drop-in owner (attach)
-  bool host_pinned = false;
-};
-
-namespace {
+namespace cgapi {
 
 std::vector<comdgb_sim *> g_attached;
 
@@ -147,12 +67,6 @@ ForceArgs force_args(comdgb_sim *h) {
   A.pl = h->pl;
   A.fo = h->fo;
   return A;
-}
-
-template <class T>
-T *track(comdgb_sim *h, T *p) {
-  h->allocs.push_back((void *)p);
-  return p;
 }
 
 int alloc_slots(comdgb_sim *h, Slots &s, bool with_natoms, int *err) {
@@ -180,6 +94,8 @@ void free_all(comdgb_sim *h) {
   for (void *p : h->allocs)
     if (p) cudaFree(p);
   h->allocs.clear();
+  for (void *q : h->adj.snaps) delete (Snapshot *)q;  // their device arrays were in allocs
+  h->adj.snaps.clear();
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -349,8 +265,9 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
     if (!(ferr <= 1e-7 * fmax) || !(gerr <= 1e-6 * gmax)) return 0;
   }
   int err = 0;
-  float4 *d1 = track(h, dalloc<float4>(p1.size(), &err));
+  float4 *d1 = h->seg_buf ? h->seg_buf : track(h, dalloc<float4>(p1.size(), &err));
   if (err) return -1;
+  h->seg_buf = d1;
   if (cudaMemcpy(d1, p1.data(), sizeof(float4) * p1.size(), cudaMemcpyHostToDevice) !=
       cudaSuccess)
     return -1;
@@ -397,12 +314,7 @@ int setup_potential(comdgb_sim *h, const simflat_t *s) {
   h->rmass = (double)(kAmuToMe * (double)s->pot->mass);
   if (o.potential == COMDGB_POT_LJ) {
     const ljpotential_t *lp = (const ljpotential_t *)s->pot;
-    double sg = lp->sigma, s6 = sg * sg * sg * sg * sg * sg;
-    h->lj_eps = lp->epsilon;
-    h->lj_s6 = s6;
-    h->lj64 = LjPot<double>{s6, 12.0 * s6, 4.0 * lp->epsilon * s6, lp->cutoff * lp->cutoff};
-    h->lj32 = LjPot<float>{(float)s6, (float)(12.0 * s6), (float)(4.0 * lp->epsilon * s6),
-                           (float)(lp->cutoff * lp->cutoff)};
+    install_lj(h, lp->epsilon, lp->sigma, lp->cutoff);
     return 0;
   }
   const eampotential_t *ep = (const eampotential_t *)s->pot;
@@ -441,16 +353,54 @@ int setup_potential(comdgb_sim *h, const simflat_t *s) {
     int rc = fit_cheb_gpu(h, ep, coef, a, b);
     if (rc) return rc;
   }
-  // pair distances below 0.75 of the nearest-neighbour distance of the
-  // potential's lattice take the reference coefficients (never in practice)
-  double pair_lo = ep->lat > 0 ? 0.75 * ep->lat / sqrt(2.0) : 0.0;
-  fill_cheb(h->eam64c.ch, h->eam32c.ch, h->eam32c.chlo, coef, a, b, pair_lo);
-  if (build_pair_seg(h, coef, a, b, pair_lo, h->cutoff, &h->eam32c.seg))
-    return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for the pair segment table");
+  h->pair_lo = ep->lat > 0 ? 0.75 * ep->lat / sqrt(2.0) : 0.0;
   h->eam64c.rc2 = rc2;
   h->eam32c.rc2 = (float)rc2;
+  return install_cheby(h, coef, a, b);
+}
+
+}  // namespace cgapi
+
+// the captured graphs hold the potentials by value
+void cgapi::drop_graphs(comdgb_sim *h) {
+  if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
+  if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
+  if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
+  if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
+  h->step_exec = h->force_exec = h->timed_exec = nullptr;
+  h->timed_graph = nullptr;
+}
+
+// ljForce.c:75-86 parameters (sigma^6 forms of the pair terms)
+void cgapi::install_lj(comdgb_sim *h, double eps, double sigma, double cutoff) {
+  const double s6 = sigma * sigma * sigma * sigma * sigma * sigma;
+  h->lj_eps = eps;
+  h->lj_sigma = sigma;
+  h->lj_s6 = s6;
+  h->lj64 = LjPot<double>{s6, 12.0 * s6, 4.0 * eps * s6, cutoff * cutoff};
+  h->lj32 = LjPot<float>{(float)s6, (float)(12.0 * s6), (float)(4.0 * eps * s6),
+                         (float)(cutoff * cutoff)};
+  drop_graphs(h);
+}
+
+// series order 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF.  Pair distances below
+// 0.75 of the nearest-neighbour distance of the potential's lattice
+// (h->pair_lo) take the reference coefficients in FP32 (never in practice).
+int cgapi::install_cheby(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
+                         const double b[6]) {
+  fill_cheb(h->eam64c.ch, h->eam32c.ch, h->eam32c.chlo, coef, a, b, h->pair_lo);
+  if (build_pair_seg(h, coef, a, b, h->pair_lo, h->cutoff, &h->eam32c.seg))
+    return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for the pair segment table");
+  for (int q = 0; q < 6; q++) {
+    for (int j = 0; j < CG_NCHEB; j++) h->cheb_coef[q][j] = coef[q][j];
+    h->cheb_a[q] = a[q];
+    h->cheb_b[q] = b[q];
+  }
+  drop_graphs(h);
   return 0;
 }
+
+namespace cgapi {
 
 int read_status(comdgb_sim *h, int *st) {
   CK(cudaMemcpyAsync(st, h->status, sizeof(int) * ST_COUNT, cudaMemcpyDeviceToHost, h->stream));
@@ -691,6 +641,77 @@ int upload(comdgb_sim *h, const simflat_t *s) {
   enqueue_compact(h);
   CK(cudaGetLastError());
   return 0;
+}
+
+// After the slot state was replaced on the device: id -> slot maps and a
+// list rebuild at the next force call; f holds no position increments.
+int relist(comdgb_sim *h) {
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st));
+  if (h->pl.slot_of) {
+    launch_slot_of(h->g, h->s, h->pl, h->ntot, h->status, st);
+    if (h->fo.of_id)
+      CK(cudaMemsetAsync(h->fo.of_id, 0xff, sizeof(int) * ((size_t)h->ntot + 1), st));
+    CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
+  }
+  enqueue_compact(h);
+  CK(cudaGetLastError());
+  return 0;
+}
+
+// a velocity-Verlet step (timestep.c:129-132) as separate launches: the first
+// position half step and its rebox, then (after the caller's force call) the
+// velocity step, the second position half step and its rebox
+int step_first_half(comdgb_sim *h, double dt_atu) {
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st));
+  launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass, h->mixed,
+                           true, h->w, h->status, st, false);
+  enqueue_classify_finish(h);
+  enqueue_compact(h);
+  CK(cudaGetLastError());
+  return check_status(h);
+}
+int step_second_half(comdgb_sim *h, double dt_atu) {
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st));
+  launch_advance_vp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass, h->mixed,
+                    h->w, h->status, st);
+  CK(cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st));  // not kept across calls
+  enqueue_classify_finish(h);
+  enqueue_compact(h);
+  CK(cudaGetLastError());
+  return check_status(h);
+}
+
+// a device copy of the slot state (natoms, id, itype, mass, r, p)
+int snapshot_alloc(comdgb_sim *h, Snapshot *q) {
+  int err = 0;
+  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
+  q->natoms = track(h, dalloc<int>(nb, &err));
+  q->id = track(h, dalloc<int>(ns, &err));
+  q->itype = track(h, dalloc<int>(ns, &err));
+  q->mass = track(h, dalloc<double>(ns, &err));
+  q->r = track(h, dalloc<d4>(ns, &err));
+  q->p = track(h, dalloc<d4>(ns, &err));
+  return err ? set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for a state snapshot") : 0;
+}
+int snapshot_copy(comdgb_sim *h, const Snapshot &q, bool save) {
+  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
+  cudaStream_t st = h->stream;
+  auto cp = [&](void *dev, void *snap, size_t bytes) {
+    return save ? cudaMemcpyAsync(snap, dev, bytes, cudaMemcpyDeviceToDevice, st)
+                : cudaMemcpyAsync(dev, snap, bytes, cudaMemcpyDeviceToDevice, st);
+  };
+  CK(cp(h->s.natoms, q.natoms, nb * sizeof(int)));
+  CK(cp(h->s.id, q.id, ns * sizeof(int)));
+  CK(cp(h->s.itype, q.itype, ns * sizeof(int)));
+  CK(cp(h->s.mass, q.mass, ns * sizeof(double)));
+  CK(cp(h->s.r, q.r, ns * sizeof(d4)));
+  CK(cp(h->s.p, q.p, ns * sizeof(d4)));
+  if (save) return 0;
+  if (h->mixed) launch_pos32(h->g, h->s, st);
+  return relist(h);
 }
 
 int download_forces(comdgb_sim *h, simflat_t *s) {

@@ -1,0 +1,148 @@
+// sim.h -- the device simulation object behind the C ABI handle and the
+// host helpers shared by the API translation units (api.cu, adjoint.cu).
+#pragma once
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <vector>
+
+#include "comdgb.h"
+#include "internal.h"
+
+namespace cgapi {
+
+// records the message for comdgb_last_error and returns code
+int set_err(int code, const char *fmt, ...);
+
+#define CK(call)                                                                        \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return set_err(COMDGB_ERR_CUDA, "%s failed: %s (%s:%d)", #call,                   \
+                     cudaGetErrorString(e_), __FILE__, __LINE__);                       \
+  } while (0)
+
+// bohr_per_atu_to_A_per_s (constants.h:61) and amu_to_m_e (constants.h:65)
+constexpr double kBohrPerAtu = (double)0.529 / (double)2.418e-17;
+constexpr double kAmuToMe = 1822.83;
+
+template <class T>
+T *dalloc(size_t n, int *err) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+    *err = 1;
+    return nullptr;
+  }
+  return (T *)p;
+}
+
+}  // namespace cgapi
+
+using cg::d4;
+
+struct comdgb_sim {
+  int device = 0;
+  comdgb_opts opts{};
+  bool mixed = false;
+  cudaStream_t stream = nullptr;
+  cg::Geom g{};
+  int ntot = 0, nslots = 0;
+  double rmass = 1.0, cutoff = 0.0;
+  double volume = 1.0;
+  std::vector<void *> allocs;
+  cg::Slots s{};
+  cg::RebinWork w{};
+  cg::Persist pl{};        // persistent lists (all null when lists are rebuilt each step)
+  cg::ForceOrder fo{};     // mixed precision: persistent lists in force order
+  double skin = 0.0;
+  cg::EntryTab et{};
+  double *dcenter = nullptr;
+  int *boxc = nullptr;
+  int *box_start = nullptr, *atom_slot = nullptr, *cpart = nullptr;
+  int ncpart = 0;
+  uint16_t *nbr = nullptr;
+  int *nbr_n = nullptr;
+  int cap = 0;
+  double *atom_stress = nullptr;
+  double *rpart = nullptr;
+  long long *ripart = nullptr;
+  int nrpart = 0;
+  double *d_out = nullptr;     // [0] energy sum [1] stress sum [2] kinetic
+  long long *d_iout = nullptr; // [0] directed pair count
+  int *status = nullptr;
+  double *stage3 = nullptr;    // real3 staging for host transfers
+  int *bin_tmp = nullptr;
+  // potentials
+  cg::EamPot<double, cg::EVAL_TABLE> eam64t{};
+  cg::EamPot<double, cg::EVAL_CHEBY> eam64c{};
+  cg::EamPot<float, cg::EVAL_TABLE> eam32t{};
+  cg::EamPot<float, cg::EVAL_CHEBY> eam32c{};
+  cg::LjPot<double> lj64{};
+  cg::LjPot<float> lj32{};
+  double lj_eps = 0, lj_s6 = 0, lj_sigma = 0;
+  // EAM Chebyshev: the installed FP64 series (0 phi, 1 rho, 2 F, 3-5 their
+  // derivatives) and the FP32 pair-table lower end
+  double cheb_coef[6][CG_NCHEB] = {};
+  double cheb_a[6] = {}, cheb_b[6] = {};
+  double pair_lo = 0.0;
+  float4 *seg_buf = nullptr;
+  // adjoint scratch, allocated on first use (adjoint.cu)
+  struct Adj {
+    d4 *lam = nullptr;
+    double *w = nullptr, *x = nullptr, *loss = nullptr, *partial = nullptr, *out = nullptr;
+    double *target = nullptr, *rb = nullptr, *pb = nullptr, *u = nullptr, *hv = nullptr;
+    int nblk = 0;
+    std::vector<void *> snaps;  // Snapshot* (checkpoints, mid-step states, final)
+  } adj;
+  // graphs
+  cudaGraphExec_t step_exec = nullptr;
+  cudaGraphExec_t force_exec = nullptr;
+  double graph_dt = NAN;
+  // timing graph (event record nodes between kernel groups)
+  cudaGraphExec_t timed_exec = nullptr;
+  cudaGraph_t timed_graph = nullptr;
+  double timed_dt = NAN;
+  std::vector<cudaGraphNode_t> timed_nodes;  // event record nodes, group order
+  std::vector<cudaEvent_t> timed_cap_events;
+  int step_kernels = 0, force_kernels = 0;  // kernel nodes per captured graph
+  // host last results
+  double e = 0.0, stress = 0.0;
+  simflat_t *host = nullptr;   // drop-in owner (attach)
+  bool host_pinned = false;
+};
+
+
+namespace cgapi {
+
+template <class T>
+T *track(comdgb_sim *h, T *p) {
+  h->allocs.push_back((void *)p);
+  return p;
+}
+cg::ForceArgs force_args(comdgb_sim *h);
+int do_force(comdgb_sim *h);       // force call (graph), energy and stress to the host
+int check_status(comdgb_sim *h);
+double cheb_host(const double *c, double a, double b, double x);  // eamCheb on the host
+void drop_graphs(comdgb_sim *h);  // after a change of potential parameters
+void install_lj(comdgb_sim *h, double eps, double sigma, double cutoff);
+// after a state replacement: id maps, list rebuild due, compacted atom list
+int relist(comdgb_sim *h);
+// a velocity-Verlet step as separate launches around the caller's force call
+int step_first_half(comdgb_sim *h, double dt_atu);
+int step_second_half(comdgb_sim *h, double dt_atu);
+// device copy of the slot state; snapshot_copy(save) stores, (!save) restores
+struct Snapshot {
+  int *natoms = nullptr, *id = nullptr, *itype = nullptr;
+  double *mass = nullptr;
+  d4 *r = nullptr, *p = nullptr;
+};
+int snapshot_alloc(comdgb_sim *h, Snapshot *q);
+int snapshot_copy(comdgb_sim *h, const Snapshot &q, bool save);
+// series order 0 phi, 1 rho, 2 F, 3 dphi, 4 drho, 5 dF: install on the device
+// (FP64 and FP32 forms, pair segment table) and drop the captured graphs
+int install_cheby(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
+                  const double b[6]);
+
+}  // namespace cgapi

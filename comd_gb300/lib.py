@@ -75,6 +75,13 @@ def _bind(lib):
     L.comdgb_sim_graph_kernels.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.comdgb_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.comdgb_round_f32.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_long]
+    D = C.POINTER(C.c_double)
+    L.comdgb_sim_set_cheby.argtypes = [C.c_void_p, D, D, D]
+    L.comdgb_sim_get_cheby.argtypes = [C.c_void_p, D, D, D]
+    L.comdgb_sim_set_lj.argtypes = [C.c_void_p, C.c_double, C.c_double]
+    L.comdgb_sim_energy_grad.argtypes = [C.c_void_p, D, D]
+    L.comdgb_sim_force_loss_grad.argtypes = [C.c_void_p, D, D, D]
+    L.comdgb_sim_traj_energy_grad.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, D, D]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p
@@ -219,6 +226,7 @@ class DeviceSim:
     def __init__(self, host_sim, o):
         self.L = load()
         self.h = C.c_void_p()
+        self._pot = o.potential
         check(self.L.comdgb_sim_create(host_sim, C.byref(o), C.byref(self.h)))
 
     def close(self):
@@ -245,6 +253,55 @@ class DeviceSim:
     def steps(self, n, dt=1e-15):
         check(self.L.comdgb_sim_steps(self.h, n, dt))
         return self.energy()
+
+    # ---- parameters and gradients (FP64 simulations) ----
+    def _np(self, n):
+        a = np.zeros(n, dtype=np.float64)
+        return a, a.ctypes.data_as(C.POINTER(C.c_double))
+
+    def nparams(self):
+        return 2 if self._pot == POT_LJ else 96
+
+    def get_cheby(self):
+        c, pc = self._np(96)
+        a, pa = self._np(3)
+        b, pb = self._np(3)
+        check(self.L.comdgb_sim_get_cheby(self.h, pc, pa, pb))
+        return c, a, b
+
+    def set_cheby(self, coef, x0, xn):
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        a = np.ascontiguousarray(x0, dtype=np.float64)
+        b = np.ascontiguousarray(xn, dtype=np.float64)
+        P = C.POINTER(C.c_double)
+        check(self.L.comdgb_sim_set_cheby(self.h, c.ctypes.data_as(P), a.ctypes.data_as(P),
+                                          b.ctypes.data_as(P)))
+
+    def set_lj(self, epsilon, sigma):
+        check(self.L.comdgb_sim_set_lj(self.h, epsilon, sigma))
+
+    def energy_grad(self):
+        """(U, dU/d(parameters))"""
+        g, pg = self._np(self.nparams())
+        e = C.c_double()
+        check(self.L.comdgb_sim_energy_grad(self.h, C.byref(e), pg))
+        return e.value, g
+
+    def force_loss_grad(self, target):
+        """(L, dL/d(parameters)) for L = sum |f_i - target[id_i]|^2"""
+        t = np.ascontiguousarray(target, dtype=np.float64)
+        g, pg = self._np(self.nparams())
+        loss = C.c_double()
+        check(self.L.comdgb_sim_force_loss_grad(self.h, t.ctypes.data_as(C.POINTER(C.c_double)),
+                                                C.byref(loss), pg))
+        return loss.value, g
+
+    def traj_energy_grad(self, n, dt=1e-15, every=20):
+        """(J, dJ/dc): J = potential energy after n steps"""
+        g, pg = self._np(self.nparams())
+        j = C.c_double()
+        check(self.L.comdgb_sim_traj_energy_grad(self.h, n, dt, every, C.byref(j), pg))
+        return j.value, g
 
     def advance_velocity(self, dt):
         check(self.L.comdgb_sim_advance_velocity(self.h, dt))

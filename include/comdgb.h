@@ -148,6 +148,27 @@ int comdgb_fp32_fma_peak(int device, double *tflops);
  * the mixed-precision kernels use for positions; runs on the host */
 int comdgb_round_f32(const double *x, float *y, long n);
 
+/* ---------------- gradients and adjoint (FP64 simulations) ---------------- */
+/* Parameters.  EAM Chebyshev: the base series phi, rho, F -- coef[32*q + k],
+ * q = 0 phi, 1 rho, 2 F, on [x0[q], xn[q]] -- whose derivative series follow
+ * as genDer derives them (cheby.c:219-270).  LJ: (epsilon, sigma) at the
+ * fixed cutoff.  The gradient calls compute the forces first (FP64). */
+int comdgb_sim_set_cheby(comdgb_sim *h, const double *coef, const double *x0, const double *xn);
+int comdgb_sim_get_cheby(comdgb_sim *h, double *coef, double *x0, double *xn);
+int comdgb_sim_set_lj(comdgb_sim *h, double epsilon, double sigma);
+/* total energy U at the current positions and dU/d(parameters): 96 values
+ * (EAM Chebyshev, coef order) or 2 (LJ: epsilon, sigma) */
+int comdgb_sim_energy_grad(comdgb_sim *h, double *energy, double *grad);
+/* force-matching loss L = sum_i |f_i - target[id_i]|^2 (target: 3 doubles per
+ * atom id, host memory; f as the reference defines it) and dL/d(parameters) */
+int comdgb_sim_force_loss_grad(comdgb_sim *h, const double *target, double *loss, double *grad);
+/* J = U after n velocity-Verlet steps of dt seconds from the current state and
+ * dJ/d(parameters) (EAM Chebyshev), by the reverse of the loop with the state
+ * checkpointed every `every` steps and the steps in between recomputed; the
+ * state is left as after the n steps */
+int comdgb_sim_traj_energy_grad(comdgb_sim *h, int n, double dt, int every, double *j,
+                                double *grad);
+
 /* ---------------- host-side setup (reference setup routines) ---------------- */
 
 /* setEamPot / eamReadASCII (eam.c:102-109, 347-398): reads <dir>/<name>.{phi,rho,f,doc} */

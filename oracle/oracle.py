@@ -6,6 +6,8 @@ reference compiled from its sources (oracle/_ref).
 (they are built only where the reference sources are present).
 """
 import ctypes as C
+
+import numpy as np
 import os
 import subprocess
 import threading
@@ -63,6 +65,10 @@ def _bind(lib):
     f.orc_lj_make.restype = C.POINTER(LjPotential)
     f.orc_lj_make.argtypes = [C.c_double] * 4
     f.orc_free.argtypes = [C.c_void_p]
+    D = C.POINTER(C.c_double)
+    f.orc_cheb_set.argtypes = [C.c_void_p, D, D, D]
+    f.orc_eam_cheb_grad.argtypes = [P_SIM, D, D, D, D, D]
+    f.orc_lj_grad.argtypes = [P_SIM, D, D, D, D, D]
     return lib
 
 
@@ -91,6 +97,29 @@ class Oracle:
 
     def cheby(self, pot, n=32):
         return self.lib.orc_cheb_make(pot, n)
+
+    def cheb_set(self, ch, coef, x0, xn):
+        """replace the base series (phi, rho, F) and derive the derivative series"""
+        P = C.POINTER(C.c_double)
+        c = np.ascontiguousarray(coef, dtype=np.float64)
+        a = np.ascontiguousarray(x0, dtype=np.float64)
+        b = np.ascontiguousarray(xn, dtype=np.float64)
+        self.lib.orc_cheb_set(ch, c.ctypes.data_as(P), a.ctypes.data_as(P), b.ctypes.data_as(P))
+
+    def grad(self, s, kind, target=None):
+        """(U, dU/dp, L, dL/dp) for EAM Chebyshev (96 parameters) or LJ (2)"""
+        P = C.POINTER(C.c_double)
+        n = 2 if kind == "lj" else 96
+        gu, gl = np.zeros(n), np.zeros(n)
+        e, loss = C.c_double(), C.c_double()
+        t = None if target is None else np.ascontiguousarray(target, dtype=np.float64)
+        tp = t.ctypes.data_as(P) if t is not None else None
+        fn = self.lib.orc_lj_grad if kind == "lj" else self.lib.orc_eam_cheb_grad
+        rc = fn(s, tp, C.byref(e), gu.ctypes.data_as(P), C.byref(loss),
+                gl.ctypes.data_as(P) if t is not None else None)
+        if rc:
+            raise RuntimeError(f"oracle gradient failed: {rc}")
+        return e.value, gu, loss.value, gl
 
     def lj(self, sigma, epsilon, cutoff, mass):
         return self.lib.orc_lj_make(sigma, epsilon, cutoff, mass)
