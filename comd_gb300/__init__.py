@@ -7,10 +7,10 @@ reference's ``simflat_t`` / ``pot->force`` / ``nTimeSteps``.  This Python
 package only builds and binds the library for tests and benchmarks.
 """
 from . import abi
-from .lib import (DISP_GAUSSIAN, DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY,
+from .lib import (Batch, DISP_GAUSSIAN, DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY,
                   POT_EAM_TABLE, POT_LJ, PREC_FP64, PREC_MIXED, ComdgbError, DeviceSim,
                   eam_potential, fcc, free_host, lj_potential, load, opts, round_f32, seed)
 
-__all__ = ["abi", "load", "opts", "DeviceSim", "ComdgbError", "eam_potential", "lj_potential",
+__all__ = ["abi", "load", "Batch", "opts", "DeviceSim", "ComdgbError", "eam_potential", "lj_potential",
            "fcc", "seed", "free_host", "round_f32", "POT_DIR", "POT_EAM_TABLE", "POT_EAM_CHEBY", "POT_LJ",
            "PREC_FP64", "PREC_MIXED", "DISP_NONE", "DISP_UNIFORM", "DISP_GAUSSIAN"]

@@ -498,6 +498,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
 void enqueue_reduce(comdgb_sim *h) {
   ForceArgs A = force_args(h);
   launch_reduce(A, h->rpart, h->ripart, h->nrpart, h->d_out, h->d_iout, h->stream);
+  if (h->nrep > 1) launch_rep_reduce(A, h->rep_out, h->stream);
 }
 
 // atom list (atom -> slot) of the current layout
@@ -581,10 +582,19 @@ int finish_force(comdgb_sim *h) {
   int rc = check_status(h);
   if (rc) return rc;
   (void)iout;
-  double esum = out[0];
-  if (h->opts.potential == COMDGB_POT_LJ) esum = esum * 4.0 * h->lj_eps * h->lj_s6;
-  h->e = esum;
+  const double escale = h->opts.potential == COMDGB_POT_LJ ? 4.0 * h->lj_eps * h->lj_s6 : 1.0;
+  h->e = h->opts.potential == COMDGB_POT_LJ ? out[0] * escale : out[0];
   h->stress = out[1] / h->volume;
+  if (h->nrep > 1) {
+    std::vector<double> ro(2 * (size_t)h->nrep);
+    CK(cudaMemcpy(ro.data(), h->rep_out, sizeof(double) * ro.size(), cudaMemcpyDeviceToHost));
+    h->rep_e.resize(h->nrep);
+    h->rep_stress.resize(h->nrep);
+    for (int r = 0; r < h->nrep; r++) {
+      h->rep_e[r] = h->opts.potential == COMDGB_POT_LJ ? ro[2 * r] * escale : ro[2 * r];
+      h->rep_stress[r] = ro[2 * r + 1] / h->volumes[r];
+    }
+  }
   if (!std::isfinite(h->e)) return set_err(COMDGB_ERR_NONFINITE, "total energy is %g", h->e);
   return 0;
 }
@@ -613,23 +623,35 @@ int do_steps(comdgb_sim *h, int n, double dt) {
 
 // ---- host transfers ---------------------------------------------------------
 
-int upload(comdgb_sim *h, const simflat_t *s) {
+// the host arrays of replica r into its box and slot range (ids offset by
+// the replica's first atom)
+int upload_rep(comdgb_sim *h, int r, const simflat_t *s) {
   cudaStream_t st = h->stream;
-  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
-  if (s->nboxes != h->g.nboxes) return set_err(COMDGB_ERR_ARG, "box count changed");
-  if (s->ntot != h->ntot) return set_err(COMDGB_ERR_ARG, "atom count changed");
-  CK(cudaMemcpyAsync(h->s.natoms, s->natoms, nb * sizeof(int), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.id, s->id, ns * sizeof(int), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.itype, s->iType, ns * sizeof(int), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.mass, s->mass, ns * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->stage3, s->r, ns * 3 * sizeof(double), cudaMemcpyHostToDevice, st));
-  launch_unpack3(h->stage3, h->s.r, (long)ns, st);
-  CK(cudaMemcpyAsync(h->stage3 + 3 * ns, s->p, ns * 3 * sizeof(double), cudaMemcpyHostToDevice,
+  const RepGeo &R = h->reps[r];
+  if (s->nboxes != R.nb) return set_err(COMDGB_ERR_ARG, "box count changed");
+  if (s->ntot != h->atom0[r + 1] - h->atom0[r]) return set_err(COMDGB_ERR_ARG, "atom count changed");
+  const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
+  const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
+  CK(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.id + s0, s->id, ns * sizeof(int), cudaMemcpyHostToDevice, st));
+  if (h->atom0[r]) launch_add_offset(h->s.id + s0, (long)ns, h->atom0[r], st);
+  CK(cudaMemcpyAsync(h->s.itype + s0, s->iType, ns * sizeof(int), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.mass + s0, s->mass, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->stage3 + 3 * s0, s->r, ns * 3 * sizeof(double), cudaMemcpyHostToDevice,
                      st));
-  launch_unpack3(h->stage3 + 3 * ns, h->s.p, (long)ns, st);
-  CK(cudaMemcpyAsync(h->s.f, s->f, ns * 4 * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.rho, s->rho, ns * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.fi, s->fi, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  launch_unpack3(h->stage3 + 3 * s0, h->s.r + s0, (long)ns, st);
+  CK(cudaMemcpyAsync(h->stage3 + 3 * (NS + s0), s->p, ns * 3 * sizeof(double),
+                     cudaMemcpyHostToDevice, st));
+  launch_unpack3(h->stage3 + 3 * (NS + s0), h->s.p + s0, (long)ns, st);
+  CK(cudaMemcpyAsync(h->s.f + s0, s->f, ns * 4 * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.rho + s0, s->rho, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(h->s.fi + s0, s->fi, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  return 0;
+}
+
+// after the uploads: FP32 copies, status, id maps and list rebuild, atom list
+int upload_done(comdgb_sim *h) {
+  cudaStream_t st = h->stream;
   if (h->mixed) launch_pos32(h->g, h->s, st);
   CK(cudaMemsetAsync(h->status, 0, sizeof(int) * ST_COUNT, st));
   if (h->pl.slot_of) {  // new host state: map ids to slots and rebuild the lists
@@ -641,6 +663,12 @@ int upload(comdgb_sim *h, const simflat_t *s) {
   enqueue_compact(h);
   CK(cudaGetLastError());
   return 0;
+}
+
+int upload(comdgb_sim *h, const simflat_t *s) {
+  if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_upload");
+  int rc = upload_rep(h, 0, s);
+  return rc ? rc : upload_done(h);
 }
 
 // After the slot state was replaced on the device: id -> slot maps and a
@@ -714,66 +742,109 @@ int snapshot_copy(comdgb_sim *h, const Snapshot &q, bool save) {
   return relist(h);
 }
 
-int download_forces(comdgb_sim *h, simflat_t *s) {
+// f, rho, fi (and e, stress) of replica r
+int download_forces_rep(comdgb_sim *h, int r, simflat_t *s) {
   cudaStream_t st = h->stream;
-  size_t ns = (size_t)h->nslots;
-  CK(cudaMemcpyAsync(s->f, h->s.f, ns * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->rho, h->s.rho, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->fi, h->s.fi, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const RepGeo &R = h->reps[r];
+  const size_t ns = (size_t)R.nb * CG_MAXATOMS, s0 = (size_t)R.box0 * CG_MAXATOMS;
+  CK(cudaMemcpyAsync(s->f, h->s.f + s0, ns * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->rho, h->s.rho + s0, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->fi, h->s.fi + s0, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
-  s->e = h->e;
-  s->stress = h->stress;
+  if (h->nrep == 1) {
+    s->e = h->e;
+    s->stress = h->stress;
+  } else {
+    s->e = r < (int)h->rep_e.size() ? h->rep_e[r] : 0.0;
+    s->stress = r < (int)h->rep_stress.size() ? h->rep_stress[r] : 0.0;
+  }
   return 0;
 }
 
-int download(comdgb_sim *h, simflat_t *s) {
+int download_rep(comdgb_sim *h, int r, simflat_t *s) {
   cudaStream_t st = h->stream;
-  size_t ns = (size_t)h->nslots, nb = (size_t)h->g.nboxes;
-  CK(cudaMemcpyAsync(s->natoms, h->s.natoms, nb * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->id, h->s.id, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->iType, h->s.itype, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->mass, h->s.mass, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
-  launch_pack3(h->s.r, h->stage3, (long)ns, st);
-  CK(cudaMemcpyAsync(s->r, h->stage3, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  launch_pack3(h->s.p, h->stage3 + 3 * ns, (long)ns, st);
-  CK(cudaMemcpyAsync(s->p, h->stage3 + 3 * ns, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost,
+  const RepGeo &R = h->reps[r];
+  if (s->nboxes != R.nb) return set_err(COMDGB_ERR_ARG, "box count differs");
+  const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
+  const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
+  CK(cudaMemcpyAsync(s->natoms, h->s.natoms + b0, nb * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->id, h->s.id + s0, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->iType, h->s.itype + s0, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(s->mass, h->s.mass + s0, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  launch_pack3(h->s.r + s0, h->stage3 + 3 * s0, (long)ns, st);
+  CK(cudaMemcpyAsync(s->r, h->stage3 + 3 * s0, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost,
                      st));
-  return download_forces(h, s);
+  launch_pack3(h->s.p + s0, h->stage3 + 3 * (NS + s0), (long)ns, st);
+  CK(cudaMemcpyAsync(s->p, h->stage3 + 3 * (NS + s0), ns * 3 * sizeof(double),
+                     cudaMemcpyDeviceToHost, st));
+  int rc = download_forces_rep(h, r, s);
+  if (rc) return rc;
+  const int off = h->atom0[r];
+  if (off)
+    for (size_t b = 0; b < nb; b++)
+      for (int k = 0; k < s->natoms[b]; k++) s->id[b * CG_MAXATOMS + k] -= off;
+  return 0;
+}
+
+int download_forces(comdgb_sim *h, simflat_t *s) { return download_forces_rep(h, 0, s); }
+int download(comdgb_sim *h, simflat_t *s) {
+  if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_download");
+  return download_rep(h, 0, s);
 }
 
 // Persistent lists need the full 27-box stencil of distinct boxes (periodic,
 // nbx >= 3), boxes at least rc + skin wide (so a list pair is always in
 // neighbouring boxes) and ids 0..ntot-1 (they key the lists).
-bool use_persistent_lists(comdgb_sim *h, const simflat_t *s, const comdgb_opts *o) {
+bool use_persistent_lists(comdgb_sim *h, const simflat_t *const *sims, int nrep,
+                          const comdgb_opts *o) {
   if (o->potential < 0 || o->list_mode == COMDGB_LIST_PER_STEP || !o->periodic) return false;
   double bmin = 1e300;
-  for (int j = 0; j < 3; j++) {
-    if (s->nbx[j] < 3) return false;
-    bmin = std::min(bmin, s->boxsize[j]);
+  for (int r = 0; r < nrep; r++) {
+    const simflat_t *s = sims[r];
+    for (int j = 0; j < 3; j++) {
+      if (s->nbx[j] < 3) return false;
+      bmin = std::min(bmin, s->boxsize[j]);
+    }
+    std::vector<char> seen((size_t)s->ntot, 0);
+    for (int b = 0; b < s->nboxes; b++)
+      for (int k = 0; k < s->natoms[b]; k++) {
+        int id = s->id[b * CG_MAXATOMS + k];
+        if (id < 0 || id >= s->ntot || seen[id]) return false;
+        seen[id] = 1;
+      }
   }
   double skin = o->skin > 0.0 ? o->skin : 0.3;
   skin = std::min(skin, bmin - h->cutoff);
   if (!(skin >= 0.1)) return false;
-  std::vector<char> seen((size_t)s->ntot, 0);
-  for (int b = 0; b < s->nboxes; b++)
-    for (int k = 0; k < s->natoms[b]; k++) {
-      int id = s->id[b * CG_MAXATOMS + k];
-      if (id < 0 || id >= s->ntot || seen[id]) return false;
-      seen[id] = 1;
-    }
   h->skin = skin;
   return true;
 }
 
-int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
+// One simulation of nrep replicas (nrep = 1: a plain simulation).  Replica r
+// owns global boxes [box0_r, box0_r + nboxes_r), the slots of those boxes and
+// atoms [atom0_r, atom0_r + ntot_r) of the compacted order; its ids are
+// offset by atom0_r on the device.  All replicas use the potential of the
+// first.
+int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_sim **out) {
   *out = nullptr;
-  if (!s || !o) return set_err(COMDGB_ERR_ARG, "null argument");
-  if (s->nboxes < 1 || !s->natoms || !s->r)
-    return set_err(COMDGB_ERR_ARG, "simflat_t has no allocated domains");
-  if ((long)s->nboxes * CG_MAXATOMS >= (1L << 31))
+  if (!sims || !o || nrep < 1) return set_err(COMDGB_ERR_ARG, "null argument");
+  long nbt = 0, ntt = 0;
+  for (int r = 0; r < nrep; r++) {
+    const simflat_t *q = sims[r];
+    if (!q) return set_err(COMDGB_ERR_ARG, "null replica %d", r);
+    if (q->nboxes < 1 || !q->natoms || !q->r)
+      return set_err(COMDGB_ERR_ARG, "simflat_t has no allocated domains");
+    for (int j = 0; j < 3; j++)
+      if (q->nbx[j] > 1023) return set_err(COMDGB_ERR_UNSUPPORTED, "more than 1023 boxes per axis");
+    if (r > 0 && q->pot != sims[0]->pot &&
+        (!q->pot || !sims[0]->pot || q->pot->cutoff != sims[0]->pot->cutoff))
+      return set_err(COMDGB_ERR_ARG, "replica %d has another potential", r);
+    nbt += q->nboxes;
+    ntt += q->ntot;
+  }
+  if (nbt * CG_MAXATOMS >= (1L << 31) || ntt >= (1L << 31))
     return set_err(COMDGB_ERR_UNSUPPORTED, "too many boxes");
-  for (int j = 0; j < 3; j++)
-    if (s->nbx[j] > 1023) return set_err(COMDGB_ERR_UNSUPPORTED, "more than 1023 boxes per axis");
+  const simflat_t *s = sims[0];
   comdgb_sim *h = new comdgb_sim();
   h->opts = *o;
   h->device = o->device;
@@ -787,19 +858,53 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
     delete h;
     return set_err(COMDGB_ERR_CUDA, "cudaStreamCreate failed");
   }
-  for (int j = 0; j < 3; j++) {
-    h->g.nbx[j] = s->nbx[j];
-    h->g.bounds[j] = s->bounds[j];
-    h->g.boxsize[j] = s->boxsize[j];
-    h->g.half[j] = 0.5 * s->boxsize[j];
+  h->nrep = nrep;
+  h->reps.resize(nrep);
+  h->atom0.assign(nrep + 1, 0);
+  h->volumes.assign(nrep, 0.0);
+  int box0 = 0;
+  for (int r = 0; r < nrep; r++) {
+    const simflat_t *q = sims[r];
+    RepGeo &R = h->reps[r];
+    R = RepGeo{};
+    for (int j = 0; j < 3; j++) {
+      R.nbx[j] = q->nbx[j];
+      R.bounds[j] = q->bounds[j];
+      R.boxsize[j] = q->boxsize[j];
+      R.half[j] = 0.5 * q->boxsize[j];
+      R.hi[j] = (float)q->boxsize[j];
+      R.lo[j] = (float)(q->boxsize[j] - (double)R.hi[j]);
+    }
+    R.box0 = box0;
+    R.nb = q->nboxes;
+    box0 += q->nboxes;
+    h->atom0[r + 1] = h->atom0[r] + q->ntot;
+    R.a0 = h->atom0[r];
+    R.na = q->ntot;
+    h->volumes[r] = q->bounds[0] * q->bounds[1] * q->bounds[2];
   }
-  h->g.nboxes = s->nboxes;
+  h->g.nboxes = (int)nbt;
   h->g.periodic = o->periodic;
-  h->ntot = s->ntot;
-  h->nslots = s->nboxes * CG_MAXATOMS;
-  h->volume = s->bounds[0] * s->bounds[1] * s->bounds[2];
+  h->g.nrep = nrep;
+  h->ntot = (int)ntt;
+  h->nslots = (int)nbt * CG_MAXATOMS;
+  h->volume = h->volumes[0];
   int err = 0;
-  size_t nb = (size_t)s->nboxes, ns = (size_t)h->nslots;
+  size_t nb = (size_t)nbt, ns = (size_t)h->nslots;
+  h->rep_d = track(h, dalloc<RepGeo>(nrep, &err));
+  h->g.rep = h->rep_d;
+  h->g.box_rep = nullptr;
+  if (nrep > 1) {
+    int *br = track(h, dalloc<int>(nb, &err));
+    std::vector<int> hb(nb);
+    for (int r = 0; r < nrep; r++)
+      for (int b = 0; b < h->reps[r].nb; b++) hb[h->reps[r].box0 + b] = r;
+    if (br) cudaMemcpy(br, hb.data(), nb * sizeof(int), cudaMemcpyHostToDevice);
+    h->g.box_rep = br;
+    h->rep_out = track(h, dalloc<double>(2 * (size_t)nrep, &err));
+  }
+  if (h->rep_d)
+    cudaMemcpy(h->rep_d, h->reps.data(), sizeof(RepGeo) * nrep, cudaMemcpyHostToDevice);
   alloc_slots(h, h->s, true, &err);
   alloc_slots(h, h->w.stage, false, &err);
   h->w.dest = track(h, dalloc<int>(ns, &err));
@@ -820,13 +925,16 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   h->g.boxc = h->boxc;
   h->box_start = track(h, dalloc<int>(nb + 1, &err));
   h->atom_slot = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
-  h->ncpart = compact_partials(s->nboxes);
+  h->ncpart = compact_partials((int)nbt);
   h->cpart = track(h, dalloc<int>(h->ncpart, &err));
   double rc = s->pot ? s->pot->cutoff : 1.0;
-  h->cap = neighbor_capacity(s, rc);
+  h->cap = 0;
+  for (int r = 0; r < nrep; r++) h->cap = std::max(h->cap, neighbor_capacity(sims[r], rc));
   h->cutoff = rc;
-  if (use_persistent_lists(h, s, o)) {
-    const int vcap = neighbor_capacity(s, rc + h->skin);
+  if (use_persistent_lists(h, sims, nrep, o)) {
+    int vcap = 0;
+    for (int r = 0; r < nrep; r++)
+      vcap = std::max(vcap, neighbor_capacity(sims[r], rc + h->skin));
     const size_t n1 = (size_t)h->ntot + 1;
     h->pl.slot_of = track(h, dalloc<int>(n1, &err));
     if (h->mixed && h->ntot < (1 << 27)) {
@@ -841,10 +949,6 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
       h->fo.pos = track(h, dalloc<float4>(n1, &err));
       h->fo.slot = track(h, dalloc<int>(n1, &err));
       h->fo.pf = track(h, dalloc<float4>(n1, &err));
-      for (int k = 0; k < 3; k++) {
-        h->fo.hi[k] = (float)s->boxsize[k];
-        h->fo.lo[k] = (float)(s->boxsize[k] - (double)h->fo.hi[k]);
-      }
       const double hs = 0.5 * h->skin - 1e-5;  // FP32 displacements err by < 1e-6 A
       h->fo.half_skin2 = (float)(hs * hs);
     } else {
@@ -883,11 +987,13 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
     err = 1;
   cudaMemsetAsync(h->nbr_n, 0, sizeof(int) * ((size_t)h->ntot + 1), h->stream);
   cudaMemsetAsync(h->atom_stress, 0, sizeof(double) * ((size_t)h->ntot + 1), h->stream);
-  cudaMemcpyAsync(h->dcenter, s->dcenter, nb * 3 * sizeof(double), cudaMemcpyHostToDevice,
-                  h->stream);
+  for (int r = 0; r < nrep; r++)
+    cudaMemcpyAsync(h->dcenter + 3 * (size_t)h->reps[r].box0, sims[r]->dcenter,
+                    (size_t)h->reps[r].nb * 3 * sizeof(double), cudaMemcpyHostToDevice, h->stream);
   launch_entry_table(h->g, h->dcenter, h->et, h->boxc, h->stream);
   int rc2 = setup_potential(h, s);
-  if (!rc2) rc2 = upload(h, s);
+  for (int r = 0; r < nrep && !rc2; r++) rc2 = upload_rep(h, r, sims[r]);
+  if (!rc2) rc2 = upload_done(h);
   if (!rc2) {
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) rc2 = set_err(COMDGB_ERR_CUDA, "setup: %s", cudaGetErrorString(e));
@@ -899,6 +1005,10 @@ int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   }
   *out = h;
   return 0;
+}
+
+int create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
+  return create(&s, 1, o, out);
 }
 
 comdgb_sim *find_attached(const void *s) {
@@ -1011,6 +1121,44 @@ const char *comdgb_version(void) { return "comdgb 0.1 sm_103a"; }
 
 int comdgb_sim_create(const simflat_t *s, const comdgb_opts *o, comdgb_sim **out) {
   return create(s, o, out);
+}
+
+// ---------------------------------------------------------------- batches
+
+int comdgb_batch_create(const simflat_t *const *sims, int n, const comdgb_opts *o,
+                        comdgb_sim **out) {
+  if (!out) return set_err(COMDGB_ERR_ARG, "null argument");
+  return create(sims, n, o, out);
+}
+
+int comdgb_batch_replicas(comdgb_sim *h) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  return h->nrep;
+}
+
+int comdgb_batch_upload(comdgb_sim *h, int r, const simflat_t *s) {
+  if (!h || !s || r < 0 || r >= h->nrep) return set_err(COMDGB_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  int rc = upload_rep(h, r, s);
+  if (!rc) rc = upload_done(h);
+  if (!rc) CK(cudaStreamSynchronize(h->stream));
+  return rc ? rc : check_status(h);
+}
+
+int comdgb_batch_download(comdgb_sim *h, int r, simflat_t *s) {
+  if (!h || !s || r < 0 || r >= h->nrep) return set_err(COMDGB_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  return download_rep(h, r, s);
+}
+
+int comdgb_batch_energies(comdgb_sim *h, double *e, double *stress) {
+  if (!h || !e) return set_err(COMDGB_ERR_ARG, "null argument");
+  for (int r = 0; r < h->nrep; r++) {
+    const bool one = h->nrep == 1;
+    e[r] = one ? h->e : (r < (int)h->rep_e.size() ? h->rep_e[r] : 0.0);
+    if (stress) stress[r] = one ? h->stress : (r < (int)h->rep_stress.size() ? h->rep_stress[r] : 0.0);
+  }
+  return 0;
 }
 
 void comdgb_sim_destroy(comdgb_sim *h) {

@@ -27,15 +27,33 @@ namespace cg {
 // 32-byte aligned double4 (CUDA 13 deprecates the 16-byte aligned one)
 typedef double4_32a d4;
 
-struct Geom {
+// The box grid of one replica (one reference simflat_t).  A simulation is
+// one replica; a batch packs several, each with its own grid, one after the
+// other in the global box, slot and atom numbering.
+struct RepGeo {
   int nbx[3];
-  int nboxes;
-  int periodic;
-  double bounds[3];
-  double boxsize[3];
-  double half[3];   // boxsize / 2: the box centre of the FP32 positions
-  const int *boxc;  // [nboxes] packed box coordinates ix | iy << 10 | iz << 20
+  int box0;            // first global box of the replica
+  int nb;              // boxes of the replica
+  int a0, na;          // first atom (compacted order) and atoms of the replica
+  int pad;
+  double bounds[3], boxsize[3];
+  double half[3];      // boxsize / 2: the box centre of the FP32 positions
+  float hi[3], lo[3];  // boxsize as FP32 hi + lo
 };
+
+struct Geom {
+  int nboxes;            // all replicas
+  int periodic;
+  int nrep;
+  const RepGeo *rep;     // [nrep]
+  const int *box_rep;    // [nboxes] replica of each box (null: one replica)
+  const int *boxc;       // [nboxes] packed box coordinates (within the replica) ix | iy << 10 | iz << 20
+};
+
+// the grid of the replica box b belongs to
+__device__ __forceinline__ const RepGeo &rep_of(const Geom &g, int b) {
+  return g.rep[g.box_rep ? __ldg(g.box_rep + b) : 0];
+}
 
 // RN(x) to FP32 from the IEEE bits with integer operations (the FP64 pipe of
 // this part issues two operations per SM per clock); results that are not
@@ -65,8 +83,8 @@ __host__ __device__ __forceinline__ float d2f_rn(double x) {
 
 // FP32 position relative to the box centre, RN(x - boxsize/2): one FP64
 // subtraction and the integer rounding per coordinate
-__device__ __forceinline__ float4 centred32(const Geom &g, double x, double y, double z) {
-  return make_float4(d2f_rn(x - g.half[0]), d2f_rn(y - g.half[1]), d2f_rn(z - g.half[2]), 0.f);
+__device__ __forceinline__ float4 centred32(const RepGeo &R, double x, double y, double z) {
+  return make_float4(d2f_rn(x - R.half[0]), d2f_rn(y - R.half[1]), d2f_rn(z - R.half[2]), 0.f);
 }
 
 // which side of [0, hi) x lies on (-1: x < 0, +1: x >= hi, 0: inside or NaN)
@@ -161,7 +179,6 @@ struct ForceOrder {
   float4 *pos;       // [ntot] FP32 position relative to the build box centre
   int *slot;         // [ntot] current slot of a (kept by the rebin)
   float4 *pf;        // [ntot] EAM: pos with w = F'(rho) of a (written by pass 1 for pass 2)
-  float hi[3], lo[3];  // box size as FP32 hi + lo
   float half_skin2;    // rebuild when an atom moved more than this squared
 };
 
@@ -184,25 +201,26 @@ struct SlotMap {
 // for the skin test
 __device__ __forceinline__ float4 world32(const Geom &g, int b, const float4 *pos32, long slot,
                                           const d4 &r) {
+  const RepGeo &R = rep_of(g, b);
   int ix[3];
   box_ixyz_tab(g, b, ix);
   if (pos32) {
     const float4 p = pos32[slot];
-    return make_float4(fmaf((float)ix[0] + 0.5f, (float)g.boxsize[0], p.x),
-                       fmaf((float)ix[1] + 0.5f, (float)g.boxsize[1], p.y),
-                       fmaf((float)ix[2] + 0.5f, (float)g.boxsize[2], p.z), 0.f);
+    return make_float4(fmaf((float)ix[0] + 0.5f, (float)R.boxsize[0], p.x),
+                       fmaf((float)ix[1] + 0.5f, (float)R.boxsize[1], p.y),
+                       fmaf((float)ix[2] + 0.5f, (float)R.boxsize[2], p.z), 0.f);
   }
-  return make_float4((float)(g.boxsize[0] * (double)ix[0] + r.x),
-                     (float)(g.boxsize[1] * (double)ix[1] + r.y),
-                     (float)(g.boxsize[2] * (double)ix[2] + r.z), 0.f);
+  return make_float4((float)(R.boxsize[0] * (double)ix[0] + r.x),
+                     (float)(R.boxsize[1] * (double)ix[1] + r.y),
+                     (float)(R.boxsize[2] * (double)ix[2] + r.z), 0.f);
 }
 
 // squared minimum-image distance between two FP32 world positions
-__device__ __forceinline__ float disp2(const Geom &g, float4 a, float4 b) {
+__device__ __forceinline__ float disp2(const RepGeo &R, float4 a, float4 b) {
   float d[3] = {a.x - b.x, a.y - b.y, a.z - b.z};
   float s = 0.f;
   for (int k = 0; k < 3; k++) {
-    const float L = (float)g.bounds[k];
+    const float L = (float)R.bounds[k];
     if (d[k] > 0.5f * L) d[k] -= L;
     else if (d[k] < -0.5f * L) d[k] += L;
     s = fmaf(d[k], d[k], s);
@@ -266,23 +284,25 @@ __device__ __forceinline__ float seg_dcubic(float4 c, float t) {
   return fmaf(fmaf(3.0f * c.w, t, 2.0f * c.z), t, c.y);
 }
 
-__host__ __device__ inline void box_ixyz(const Geom &g, int b, int *ix) {
-  ix[0] = b % g.nbx[0];
-  ix[1] = (b / g.nbx[0]) % g.nbx[1];
-  ix[2] = (b / g.nbx[0] / g.nbx[1]) % g.nbx[2];
+// coordinates of global box b within its replica's grid R
+__host__ __device__ inline void box_ixyz(const RepGeo &R, int b, int *ix) {
+  const int l = b - R.box0;
+  ix[0] = l % R.nbx[0];
+  ix[1] = (l / R.nbx[0]) % R.nbx[1];
+  ix[2] = (l / R.nbx[0] / R.nbx[1]) % R.nbx[2];
 }
 
 // getIBoxFromIxyz3NP (domains.c:297-325): -1 outside a non-periodic grid,
-// else wrap by one period
-__host__ __device__ inline int box_from_ixyz(const Geom &g, int *ix) {
-  if (!g.periodic)
+// else wrap by one period; the global box of the replica's coordinates ix
+__host__ __device__ inline int box_from_ixyz(const RepGeo &R, int periodic, int *ix) {
+  if (!periodic)
     for (int j = 0; j < 3; j++)
-      if (ix[j] < 0 || ix[j] >= g.nbx[j]) return -1;
+      if (ix[j] < 0 || ix[j] >= R.nbx[j]) return -1;
   for (int j = 0; j < 3; j++) {
-    if (ix[j] < 0) ix[j] += g.nbx[j];
-    else if (ix[j] >= g.nbx[j]) ix[j] -= g.nbx[j];
+    if (ix[j] < 0) ix[j] += R.nbx[j];
+    else if (ix[j] >= R.nbx[j]) ix[j] -= R.nbx[j];
   }
-  return ix[0] + ix[1] * g.nbx[0] + ix[2] * g.nbx[0] * g.nbx[1];
+  return R.box0 + ix[0] + ix[1] * R.nbx[0] + ix[2] * R.nbx[0] * R.nbx[1];
 }
 
 // Kahan-compensated FP32 accumulator

@@ -50,12 +50,13 @@ struct ForceArgs {
 // beyond the cutoff).
 __device__ __forceinline__ int stencil_entry(const Geom &g, int b, int jb) {
   const int ci = __ldg(g.boxc + b), cj = __ldg(g.boxc + jb);
+  const RepGeo &R = rep_of(g, b);
   int e = 0;
 #pragma unroll
   for (int ax = 0; ax < 3; ax++) {
     int d = ((cj >> (10 * ax)) & 1023) - ((ci >> (10 * ax)) & 1023);
-    if (d > 1) d -= g.nbx[ax];
-    else if (d < -1) d += g.nbx[ax];
+    if (d > 1) d -= R.nbx[ax];
+    else if (d < -1) d += R.nbx[ax];
     if (d > 1 || d < -1) return -1;
     e = e * 3 + d + 1;
   }
@@ -884,8 +885,9 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
                         });
     return;
   }
-  const float hx = A.fo.hi[0], hy = A.fo.hi[1], hz = A.fo.hi[2];
-  const float lx = A.fo.lo[0], ly = A.fo.lo[1], lz = A.fo.lo[2];
+  const RepGeo &R = rep_of(A.g, slot >> 6);
+  const float hx = R.hi[0], hy = R.hi[1], hz = R.hi[2];
+  const float lx = R.lo[0], ly = R.lo[1], lz = R.lo[2];
   const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
   // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1

@@ -60,6 +60,9 @@ int reduce_partials(int ntot);
 void launch_kinetic(const Geom &g, Slots s, const int *atom_slot, int ntot, double rmass,
                     double *partials, int npart, double *out, cudaStream_t st);
 void launch_unpack3(const double *src3, d4 *dst, long n, cudaStream_t st);
+void launch_add_offset(int *v, long n, int off, cudaStream_t st);
+// per replica: out[2r] energy sum, out[2r+1] stress sum
+void launch_rep_reduce(const ForceArgs &A, double *out, cudaStream_t st);
 void launch_pack3(const d4 *src, double *dst3, long n, cudaStream_t st);
 void launch_pos32(const Geom &g, Slots s, cudaStream_t st);
 void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, const double *xyz,

@@ -21,8 +21,9 @@ __global__ void entry_table_kernel(Geom g, const double *dcenter, EntryTab et) {
   if (b >= g.nboxes) return;
   int base = b * CG_NNBR;
   int cnt = 0;
-  if (g.nboxes == 1) {
-    et.box[base] = 0;
+  const RepGeo &R = rep_of(g, b);
+  if (R.nb == 1) {
+    et.box[base] = b;
     et.dr64[base] = d4{0.0, 0.0, 0.0, 0.0};
     et.dr32[2 * base] = make_float4(0.f, 0.f, 0.f, 0.f);
     et.dr32[2 * base + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -30,19 +31,19 @@ __global__ void entry_table_kernel(Geom g, const double *dcenter, EntryTab et) {
     return;
   }
   int ix[3];
-  box_ixyz(g, b, ix);
+  box_ixyz(R, b, ix);
   for (int i = ix[0] - 1; i <= ix[0] + 1; i++)
     for (int j = ix[1] - 1; j <= ix[1] + 1; j++)
       for (int k = ix[2] - 1; k <= ix[2] + 1; k++) {
         int t[3] = {i, j, k};
-        int nb = box_from_ixyz(g, t);
+        int nb = box_from_ixyz(R, g.periodic, t);
         if (nb < 0) continue;
         double dr[3];
         for (int d = 0; d < 3; d++) {
           dr[d] = dcenter[3 * b + d] - dcenter[3 * nb + d];
           if (g.periodic) {
-            if (dr[d] < -0.5 * g.bounds[d]) dr[d] += g.bounds[d];
-            else if (dr[d] > 0.5 * g.bounds[d]) dr[d] -= g.bounds[d];
+            if (dr[d] < -0.5 * R.bounds[d]) dr[d] += R.bounds[d];
+            else if (dr[d] > 0.5 * R.bounds[d]) dr[d] -= R.bounds[d];
           }
         }
         et.box[base + cnt] = nb;
@@ -63,7 +64,7 @@ __global__ void box_coord_kernel(Geom g, int *boxc) {
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= g.nboxes) return;
   int ix[3];
-  box_ixyz(g, b, ix);
+  box_ixyz(rep_of(g, b), b, ix);
   boxc[b] = ix[0] | (ix[1] << 10) | (ix[2] << 20);
 }
 
@@ -114,18 +115,19 @@ __device__ __forceinline__ void copy_record(const Slots &dst, int ds, const Slot
 __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int slot, d4 r,
                                               bool mixed, const RebinWork &w, int *status) {
   const int b = slot >> 6;
+  const RepGeo &R = rep_of(g, b);
   int ixo[3], ixn[3];
-  box_ixyz_tab(g, b, ixo);
-  const int sd[3] = {side_of(r.x, g.boxsize[0]), side_of(r.y, g.boxsize[1]),
-                      side_of(r.z, g.boxsize[2])};
+  const int sd[3] = {side_of(r.x, R.boxsize[0]), side_of(r.y, R.boxsize[1]),
+                      side_of(r.z, R.boxsize[2])};
   if ((sd[0] | sd[1] | sd[2]) == 0) return;  // stays (the common case: no FP64 work)
+  box_ixyz_tab(g, b, ixo);
   double rn[3] = {r.x, r.y, r.z};
   for (int k = 0; k < 3; k++) {
     ixn[k] = ixo[k] + sd[k];
-    if (sd[k] < 0) rn[k] += g.boxsize[k];
-    else if (sd[k] > 0) rn[k] -= g.boxsize[k];
+    if (sd[k] < 0) rn[k] += R.boxsize[k];
+    else if (sd[k] > 0) rn[k] -= R.boxsize[k];
   }
-  const int jb = box_from_ixyz(g, ixn);
+  const int jb = box_from_ixyz(R, g.periodic, ixn);
   if (jb < 0 || jb == b) return;
   atomicOr(w.depmask + (slot >> 5), 1u << (slot & 31));
   atomicAdd(b < jb ? w.arr_lo + jb : w.arr_hi + jb, 1);
@@ -139,17 +141,17 @@ __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int
   st.f[slot] = s.f[slot];
   st.rho[slot] = s.rho[slot];
   st.fi[slot] = s.fi[slot];
-  if (mixed) st.pos32[slot] = centred32(g, rn[0], rn[1], rn[2]);
+  if (mixed) st.pos32[slot] = centred32(R, rn[0], rn[1], rn[2]);
   if (jb > b) {
     // re-examined in jb's scan: must stay there
     int ix2[3], ix3[3];
     box_ixyz_tab(g, jb, ix2);
     for (int k = 0; k < 3; k++) {
       if (rn[k] < 0.0) ix3[k] = ix2[k] - 1;
-      else if (rn[k] >= g.boxsize[k]) ix3[k] = ix2[k] + 1;
+      else if (rn[k] >= R.boxsize[k]) ix3[k] = ix2[k] + 1;
       else ix3[k] = ix2[k];
     }
-    const int jb2 = box_from_ixyz(g, ix3);
+    const int jb2 = box_from_ixyz(R, g.periodic, ix3);
     if (jb2 >= 0 && jb2 != jb) atomicExch(status + ST_REBIN_SERIAL, 1);
   }
 }
@@ -171,6 +173,7 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
   const int af = fo.of_id[id];
   if (af < 0) return;
   const float4 q = fo.ref[af];
+  const RepGeo &R = rep_of(g, b);
   int ixn[3], ixb[3];
   box_ixyz_tab(g, b, ixn);
   box_ixyz_tab(g, __float_as_int(q.w), ixb);
@@ -181,11 +184,11 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
   for (int k = 0; k < 3; k++) {
     int db = ixn[k] - ixb[k];
     if (g.periodic) {
-      if (db > 1) db -= g.nbx[k];
-      else if (db < -1) db += g.nbx[k];
+      if (db > 1) db -= R.nbx[k];
+      else if (db < -1) db += R.nbx[k];
     }
     far |= db > 1 || db < -1;
-    if (db != 0) pv[k] = d2f_rn(fma((double)db, g.boxsize[k], rv[k] - g.half[k]));
+    if (db != 0) pv[k] = d2f_rn(fma((double)db, R.boxsize[k], rv[k] - R.half[k]));
     const float d = pv[k] - qv[k];
     d2 = fmaf(d, d, d2);
   }
@@ -249,7 +252,7 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
   }
   if (POS) {
     if (mixed && write32) {
-      const float4 p32 = centred32(g, r.x, r.y, r.z);
+      const float4 p32 = centred32(rep_of(g, b), r.x, r.y, r.z);
       s.pos32[slot] = p32;
       if (w.fo.of_id) fo_track(g, w.fo, b, s.id[slot], r, p32, status);
     }
@@ -257,7 +260,7 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
       // persistent lists: the half step before a force call decides
       // whether the lists are rebuilt (an atom moved more than skin/2)
       const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
-      if (disp2(g, wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
+      if (disp2(rep_of(g, b), wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
         atomicExch(status + ST_REBUILD, 1);
     }
   }
@@ -333,14 +336,15 @@ void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, boo
 // distinct stencil boxes of b other than b, ascending
 __device__ int source_boxes(const Geom &g, int b, int *src) {
   int n = 0;
-  if (g.nboxes == 1) return 0;
+  const RepGeo &R = rep_of(g, b);
+  if (R.nb == 1) return 0;
   int ix[3];
-  box_ixyz(g, b, ix);
+  box_ixyz(R, b, ix);
   for (int i = -1; i <= 1; i++)
     for (int j = -1; j <= 1; j++)
       for (int k = -1; k <= 1; k++) {
         int t[3] = {ix[0] + i, ix[1] + j, ix[2] + k};
-        int nb = box_from_ixyz(g, t);
+        int nb = box_from_ixyz(R, g.periodic, t);
         if (nb < 0 || nb == b) continue;
         bool dup = false;
         for (int q = 0; q < n; q++) dup |= (src[q] == nb);
@@ -472,8 +476,9 @@ __global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, Sl
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   status[ST_SERIAL_RUNS] += 1;
   for (int b = 0; b < g.nboxes; b++) {
+    const RepGeo &R = rep_of(g, b);
     int ixo[3];
-    box_ixyz(g, b, ixo);
+    box_ixyz(R, b, ixo);
     int i = 0;
     while (i < s.natoms[b]) {
       int off = b * CG_MAXATOMS + i;
@@ -483,21 +488,21 @@ __global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, Sl
       for (int k = 0; k < 3; k++) {
         if (rc[k] < 0.0) {
           ixn[k] = ixo[k] - 1;
-          rn[k] += g.boxsize[k];
-        } else if (rc[k] >= g.boxsize[k]) {
+          rn[k] += R.boxsize[k];
+        } else if (rc[k] >= R.boxsize[k]) {
           ixn[k] = ixo[k] + 1;
-          rn[k] -= g.boxsize[k];
+          rn[k] -= R.boxsize[k];
         } else {
           ixn[k] = ixo[k];
         }
       }
-      int jb = box_from_ixyz(g, ixn);
+      int jb = box_from_ixyz(R, g.periodic, ixn);
       if (jb < 0 || jb == b) {
         i++;
         continue;
       }
       s.r[off] = d4{rn[0], rn[1], rn[2], 0.0};
-      if (mixed) s.pos32[off] = centred32(g, rn[0], rn[1], rn[2]);
+      if (mixed) s.pos32[off] = centred32(R, rn[0], rn[1], rn[2]);
       int nj = s.natoms[jb];
       if (nj >= CG_MAXATOMS - 1) {  // reaching 64 aborts (domains.c:229)
         set_error(status, -11);
@@ -573,7 +578,8 @@ __global__ void skin_check_kernel(Geom g, Slots s, Persist pl, bool mixed, int *
   const int b = (int)(slot >> 6), k = (int)(slot & 63);
   if (k >= s.natoms[b]) return;
   const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, s.r[slot]);
-  if (disp2(g, wp, pl.rref[s.id[slot]]) > pl.half_skin2) atomicExch(status + ST_REBUILD, 1);
+  if (disp2(rep_of(g, b), wp, pl.rref[s.id[slot]]) > pl.half_skin2)
+    atomicExch(status + ST_REBUILD, 1);
 }
 
 void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *status,
@@ -691,6 +697,15 @@ void launch_compact(const Geom &g, const int *natoms, int *box_start, int *atom_
                                                      atom_slot, ntot);
 }
 
+// ids of a replica's slots, offset by its first atom
+__global__ void add_offset_kernel(int *v, long n, int off) {
+  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) v[q] += off;
+}
+void launch_add_offset(int *v, long n, int off, cudaStream_t st) {
+  if (n > 0) add_offset_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(v, n, off);
+}
+
 // ---------------------------------------------------------------------------
 // deterministic reductions: energy (sum of f[3]), stress share, pair count
 // ---------------------------------------------------------------------------
@@ -772,6 +787,27 @@ void launch_reduce(const ForceArgs &A, double *partials, long long *ipartials, i
   reduce_final_kernel<<<1, 32, 0, st>>>(partials, ipartials, npart, out, iout);
 }
 
+// per replica (one block each, fixed order): energy sum f.w and stress share
+__global__ void __launch_bounds__(RD_THREADS) rep_reduce_kernel(ForceArgs A, double *out) {
+  __shared__ double shd[RD_THREADS / 32];
+  const RepGeo &R = A.g.rep[blockIdx.x];
+  double e = 0.0, sx = 0.0;
+  for (int a = R.a0 + threadIdx.x; a < R.a0 + R.na; a += RD_THREADS) {
+    e += A.s.f[A.atom_slot[a]].w;
+    sx += A.atom_stress[a];
+  }
+  e = block_sum_d(e, shd);
+  sx = block_sum_d(sx, shd);
+  if (threadIdx.x == 0) {
+    out[2 * blockIdx.x] = e;
+    out[2 * blockIdx.x + 1] = sx;
+  }
+}
+
+void launch_rep_reduce(const ForceArgs &A, double *out, cudaStream_t st) {
+  rep_reduce_kernel<<<A.g.nrep, RD_THREADS, 0, st>>>(A, out);
+}
+
 __global__ void __launch_bounds__(RD_THREADS) kinetic_kernel(Slots s, const int *atom_slot,
                                                              int ntot, double *partials) {
   __shared__ double shd[RD_THREADS / 32];
@@ -833,7 +869,7 @@ __global__ void pos32_kernel(Geom g, Slots s) {
   long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
   d4 r = s.r[slot];
-  s.pos32[slot] = centred32(g, r.x, r.y, r.z);
+  s.pos32[slot] = centred32(rep_of(g, (int)(slot >> 6)), r.x, r.y, r.z);
 }
 
 void launch_pos32(const Geom &g, Slots s, cudaStream_t st) {
@@ -844,19 +880,21 @@ void launch_pos32(const Geom &g, Slots s, cudaStream_t st) {
 // initial binning: n putAtomInBox calls (domains.c:237-291) as a counting
 // sort that keeps call order within each box
 // ---------------------------------------------------------------------------
+// (one replica: the initial binning of a single simulation)
 __device__ __forceinline__ int world_box(const Geom &g, const double *xyz_in, double *xyz,
                                          bool &ok) {
+  const RepGeo &R = g.rep[0];
   int ib[3];
   ok = true;
   for (int m = 0; m < 3; m++) {
     double x = xyz_in[m];
-    if (x < 0.0) x += g.bounds[m];
-    else if (x >= g.bounds[m]) x -= g.bounds[m];
+    if (x < 0.0) x += R.bounds[m];
+    else if (x >= R.bounds[m]) x -= R.bounds[m];
     xyz[m] = x;
-    ib[m] = (int)floor(x / g.boxsize[m]);
-    if (ib[m] < 0 || ib[m] >= g.nbx[m]) ok = false;
+    ib[m] = (int)floor(x / R.boxsize[m]);
+    if (ib[m] < 0 || ib[m] >= R.nbx[m]) ok = false;
   }
-  return ib[0] + g.nbx[0] * ib[1] + g.nbx[0] * g.nbx[1] * ib[2];
+  return ib[0] + R.nbx[0] * ib[1] + R.nbx[0] * R.nbx[1] * ib[2];
 }
 
 __global__ void bin_count_kernel(Geom g, Slots s, int n, const double *xyz, int *tmp_index,

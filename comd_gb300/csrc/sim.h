@@ -48,6 +48,14 @@ struct comdgb_sim {
   bool mixed = false;
   cudaStream_t stream = nullptr;
   cg::Geom g{};
+  // replicas (a plain simulation is one): grids, first atom of each (+ total)
+  int nrep = 1;
+  std::vector<cg::RepGeo> reps;
+  std::vector<int> atom0;
+  std::vector<double> volumes;
+  cg::RepGeo *rep_d = nullptr;
+  double *rep_out = nullptr;                 // [2*nrep] energy, stress sums (batch)
+  std::vector<double> rep_e, rep_stress;     // per replica, after a force call
   int ntot = 0, nslots = 0;
   double rmass = 1.0, cutoff = 0.0;
   double volume = 1.0;

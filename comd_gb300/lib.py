@@ -82,6 +82,12 @@ def _bind(lib):
     L.comdgb_sim_energy_grad.argtypes = [C.c_void_p, D, D]
     L.comdgb_sim_force_loss_grad.argtypes = [C.c_void_p, D, D, D]
     L.comdgb_sim_traj_energy_grad.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, D, D]
+    L.comdgb_batch_create.argtypes = [C.POINTER(P_SIM), C.c_int, C.c_void_p,
+                                      C.POINTER(C.c_void_p)]
+    L.comdgb_batch_replicas.argtypes = [C.c_void_p]
+    L.comdgb_batch_upload.argtypes = [C.c_void_p, C.c_int, P_SIM]
+    L.comdgb_batch_download.argtypes = [C.c_void_p, C.c_int, P_SIM]
+    L.comdgb_batch_energies.argtypes = [C.c_void_p, D, D]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p
@@ -348,3 +354,29 @@ class DeviceSim:
         nk = check(self.L.comdgb_sim_timed_steps(self.h, n, dt, step, kern, max_kernels))
         names = [self.L.comdgb_kernel_name(self.h, k).decode() for k in range(nk)]
         return list(step)[:n], step[n], dict(zip(names, list(kern)[:nk]))
+
+
+class Batch(DeviceSim):
+    """Replicas advanced together (comdgb_batch_*): the DeviceSim calls act on
+    all of them; uploads, downloads and energies go per replica."""
+
+    def __init__(self, host_sims, o):
+        self.L = load()
+        self.h = C.c_void_p()
+        self._pot = o.potential
+        self.n = len(host_sims)
+        arr = (P_SIM * self.n)(*host_sims)
+        check(self.L.comdgb_batch_create(arr, self.n, C.byref(o), C.byref(self.h)))
+
+    def upload_rep(self, r, s):
+        check(self.L.comdgb_batch_upload(self.h, r, s))
+
+    def download_rep(self, r, s):
+        check(self.L.comdgb_batch_download(self.h, r, s))
+
+    def energies(self):
+        e = np.zeros(self.n)
+        st = np.zeros(self.n)
+        P = C.POINTER(C.c_double)
+        check(self.L.comdgb_batch_energies(self.h, e.ctypes.data_as(P), st.ctypes.data_as(P)))
+        return e, st

@@ -148,6 +148,21 @@ int comdgb_fp32_fma_peak(int device, double *tflops);
  * the mixed-precision kernels use for positions; runs on the host */
 int comdgb_round_f32(const double *x, float *y, long n);
 
+/* ---------------- batched replicas ---------------- */
+/* n independent simulations (uneven sizes allowed) with one potential (that
+ * of sims[0]) and the same options, advanced together: every kernel of a
+ * step runs once over all replicas' boxes and atoms, each replica on its own
+ * box grid and rebinned exactly as reBoxAll rebins it alone.  The handle
+ * takes every comdgb_sim_* call (energy: the sum over replicas); uploads and
+ * downloads go per replica. */
+int comdgb_batch_create(const simflat_t *const *sims, int n, const comdgb_opts *o,
+                        comdgb_sim **out);
+int comdgb_batch_replicas(comdgb_sim *h);
+int comdgb_batch_upload(comdgb_sim *h, int r, const simflat_t *s);
+int comdgb_batch_download(comdgb_sim *h, int r, simflat_t *s);
+/* per-replica total energy and scalar stress of the last force call */
+int comdgb_batch_energies(comdgb_sim *h, double *e, double *stress);
+
 /* ---------------- gradients and adjoint (FP64 simulations) ---------------- */
 /* Parameters.  EAM Chebyshev: the base series phi, rho, F -- coef[32*q + k],
  * q = 0 phi, 1 rho, 2 F, on [x0[q], xn[q]] -- whose derivative series follow

@@ -1,0 +1,80 @@
+"""Batched replicas: several independent simulations of uneven sizes advanced
+by one set of launches (comdgb_batch_*).  Each replica must come out exactly
+as if it had run alone: with per-step lists the FP64 trajectories, slot
+layouts and energies are bit-identical to single-simulation runs; with the
+default skin lists (one rebuild flag for the whole batch) mixed precision
+agrees to rounding."""
+import numpy as np
+import pytest
+
+import comd_gb300 as cg
+from helpers import slots_equal
+
+REPLICAS = [((5, 5, 5), 1.0, 11, 300.0), ((7, 6, 5), 1.0, 12, 900.0), ((6, 6, 6), 1.25, 13, 600.0),
+            ((4, 5, 6), 1.0, 14, 1200.0)]
+
+
+def make_replicas(pot):
+    sims = []
+    for (n, bf, seed, temp) in REPLICAS:
+        s = cg.fcc(n[0], n[1], n[2], pot.ptr.contents.lat, 1.0, bf, pot)
+        cg.seed(s, seed, cg.DISP_GAUSSIAN, 0.03, temp, pot.ptr.contents.mass)
+        sims.append(s)
+    return sims
+
+
+def single_run(s, o, nsteps):
+    d = cg.DeviceSim(s, o)
+    try:
+        e = d.steps(nsteps)[0]
+        d.download(s)
+    finally:
+        d.close()
+    return e
+
+
+@pytest.mark.gpu
+def test_batch_fp64_bit_identical_to_single_runs():
+    pot = cg.eam_potential("cu")
+    o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, True, per_step_lists=True)
+    batch_sims, single_sims = make_replicas(pot), make_replicas(pot)
+    try:
+        b = cg.Batch(batch_sims, o)
+        try:
+            assert b.n == len(REPLICAS)
+            b.steps(10)
+            e_b, _ = b.energies()
+            for r, s in enumerate(batch_sims):
+                b.download_rep(r, s)
+        finally:
+            b.close()
+        for r, s in enumerate(single_sims):
+            e = single_run(s, o, 10)
+            assert slots_equal(batch_sims[r], s, ("id", "iType", "mass", "r", "p")), r
+            assert abs(e_b[r] - e) <= 1e-12 * abs(e), r
+    finally:
+        for s in batch_sims + single_sims:
+            cg.free_host(s)
+
+
+@pytest.mark.gpu
+def test_batch_mixed_matches_single_runs():
+    pot = cg.eam_potential("cu")
+    o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, True)
+    batch_sims, single_sims = make_replicas(pot), make_replicas(pot)
+    try:
+        b = cg.Batch(batch_sims, o)
+        try:
+            b.steps(20)
+            e_b, st_b = b.energies()
+            for r, s in enumerate(batch_sims):
+                b.download_rep(r, s)
+        finally:
+            b.close()
+        for r, s in enumerate(single_sims):
+            e = single_run(s, o, 20)
+            assert abs(e_b[r] - e) <= 1e-7 * abs(e), (r, e_b[r], e)
+            assert np.isfinite(st_b[r])
+    finally:
+        for s in batch_sims + single_sims:
+            cg.free_host(s)
