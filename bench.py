@@ -441,6 +441,239 @@ def gpu_arm(args):
     return 0
 
 
+# ------------------------------------------------------------ C4: batches
+BATCH = {"replicas": 64, "edge": (8, 24), "temp_k": (100.0, 1200.0), "seed": 4242, "steps": 50,
+         "bf": (1.0, 1.25, 1.5), "skin": (0.2, 0.3, 0.4)}
+
+
+def batch_arm(args):
+    """64 EAM Cu Chebyshev replicas (mixed precision) of seeded uneven size,
+    edge U{8..24} unit cells, temperature U(100, 1200) K, advanced together:
+    a 50-step loop captured as one CUDA graph over all replicas.  The box
+    factor and the skin are chosen by timing every candidate on the batch
+    itself (autotuner); the result is set against the same 64 systems run one
+    after another, each with its own 50-step graph."""
+    import comd_gb300 as cg
+    rng = np.random.default_rng(BATCH["seed"])
+    R = BATCH["replicas"]
+    edges = rng.integers(BATCH["edge"][0], BATCH["edge"][1] + 1, R)
+    temps = rng.uniform(BATCH["temp_k"][0], BATCH["temp_k"][1], R)
+    pot = cg.eam_potential("cu")
+    lat, mass = pot.ptr.contents.lat, pot.ptr.contents.mass
+    natoms = int(sum(4 * int(n) ** 3 for n in edges))
+    nsteps = BATCH["steps"]
+
+    def build(bf):
+        sims = []
+        for r in range(R):
+            n = int(edges[r])
+            s = cg.fcc(n, n, n, lat, 1.0, bf, pot)
+            cg.seed(s, BATCH["seed"] + r, cg.DISP_NONE, 0.0, float(temps[r]), mass)
+            sims.append(s)
+        return sims
+
+    def free(sims):
+        for s in sims:
+            cg.free_host(s)
+
+    def o(skin):
+        return cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, skin=skin)
+
+    tried = []
+    for bf in BATCH["bf"]:
+        sims = build(bf)
+        for skin in BATCH["skin"]:
+            b = cg.Batch(sims, o(skin))
+            try:
+                b.graph_steps(5)
+                ms = b.graph_steps(20)
+            finally:
+                b.close()
+            tried.append({"bf": bf, "skin_A": skin, "ms_per_step": ms / 20,
+                          "atom_steps_per_s": natoms * 20 / (ms * 1e-3)})
+        free(sims)
+    best = max(tried, key=lambda t: t["atom_steps_per_s"])
+    sims = build(best["bf"])
+    try:
+        b = cg.Batch(sims, o(best["skin_A"]))
+        try:
+            b.graph_steps(nsteps)  # capture + warm
+            clk = ClockSampler(0)
+            clk.start()
+            times = [b.graph_steps(nsteps) for _ in range(max(args.steps // nsteps, 3))]
+            clocks = clk.stop()
+            e, _ = b.energies()
+        finally:
+            b.close()
+        t_batch = statistics.median(times)
+        # the same systems one after another
+        t_seq = 0.0
+        for r in range(R):
+            d = cg.DeviceSim(sims[r], o(best["skin_A"]))
+            try:
+                d.graph_steps(nsteps)
+                t_seq += d.graph_steps(nsteps)
+            finally:
+                d.close()
+    finally:
+        free(sims)
+    value = natoms * nsteps / (t_batch * 1e-3)
+    seq = natoms * nsteps / (t_seq * 1e-3)
+    print(json.dumps({
+        "metric": "EAM atom-steps/s, 64 uneven replicas in one launch per kernel, 1 GB300",
+        "value": value, "unit": UNIT, "n_gpus": 1, "steps": nsteps, "higher_is_better": True,
+        "dtype": "f32+f64", "data": "synthetic (seeded FCC Cu replicas)",
+        "config": {"workload": "eam_cu_chebyshev_64_replicas_edge8-24_100-1200K",
+                   "replicas": R, "atoms": natoms, "edges_min_max": [int(edges.min()),
+                                                                    int(edges.max())],
+                   "loop": f"{nsteps} steps captured as one CUDA graph"},
+        "ms_per_loop": t_batch, "sequential_64": {"value": seq, "ms_total": t_seq},
+        "speedup_vs_sequential": value / seq,
+        "autotune": {"chosen": best, "candidates": tried},
+        "energy_per_atom_ha": {"min": float(min(e / (4 * edges ** 3))),
+                               "max": float(max(e / (4 * edges ** 3)))},
+        "clocks": clocks}))
+    return 0
+
+
+# ---------------------------------------------------------- C5: adjoint
+def adjoint_arm(args):
+    """Gradients on 10 seeded FCC 40^3 EAM Cu configurations (256,000 atoms,
+    Gaussian displacements sigma 0.05*sqrt(T/300 K) A and momenta at
+    300/600/900 K): force-matching loss against forces of +-2 % seeded
+    perturbed Chebyshev coefficients, its gradient in the 96 coefficients
+    (timed), central differences (h = 1e-6 relative) on config 0, LJ
+    epsilon/sigma gradients on config 0's lattice, and the energy gradient
+    through 200 velocity-Verlet steps (checkpoints every 20) on a 20^3 lattice
+    against central differences of whole trajectories."""
+    import comd_gb300 as cg
+    from comd_gb300.abi import by_id
+    pot = cg.eam_potential("cu")
+    lat, mass = pot.ptr.contents.lat, pot.ptr.contents.mass
+    rng = np.random.default_rng(515)
+    temps = [300.0, 600.0, 900.0]
+    rows = []
+    fd_report = {}
+
+    def lattice(n, temp, seed, p=pot, m=mass):
+        s = cg.fcc(n, n, n, lat, 1.0, 1.0, p)
+        cg.seed(s, seed, cg.DISP_GAUSSIAN, 0.05 * (temp / 300.0) ** 0.5, temp, m)
+        return s
+
+    for k in range(10):
+        temp = temps[k % 3]
+        s = lattice(40, temp, 700 + k)
+        d = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64))
+        try:
+            c, x0, xn = d.get_cheby()
+            d.set_cheby(c * (1 + 0.02 * rng.uniform(-1, 1, c.size)), x0, xn)
+            d.force()
+            d.download(s)
+            target = by_id(s, "f")[:, :3].copy()
+            d.set_cheby(c, x0, xn)
+            d.force_loss_grad(target)  # warm
+            t0 = time.perf_counter()
+            loss, g = d.force_loss_grad(target)
+            t_grad = time.perf_counter() - t0
+            rows.append({"temp_k": temp, "loss": loss, "grad_norm": float(np.linalg.norm(g)),
+                         "grad_ms": t_grad * 1e3})
+            if k == 0:
+                errs = []
+                for q in range(3):
+                    j = int(np.argmax(np.abs(g[32 * q:32 * q + 32]))) + 32 * q
+                    for jj in (j, 32 * q + 7):
+                        h = 1e-6 * max(abs(c[jj]), 1e-3 * np.abs(c[32 * q:32 * q + 32]).max())
+                        v = []
+                        for sg in (1, -1):
+                            cc = c.copy()
+                            cc[jj] += sg * h
+                            d.set_cheby(cc, x0, xn)
+                            v.append(d.force_loss_grad(target)[0])
+                        fd = (v[0] - v[1]) / (2 * h)
+                        errs.append(abs(g[jj] - fd) / max(abs(fd), 1e-3 * np.abs(g).max()))
+                d.set_cheby(c, x0, xn)
+                fd_report["eam_force_loss_fd_max_rel_err"] = float(max(errs))
+                fd_report["eam_force_loss_fd_components"] = len(errs)
+        finally:
+            d.close()
+            if k:
+                cg.free_host(s)
+            else:
+                s0 = s
+    # LJ epsilon / sigma on config 0's lattice (BASELINE LJ parameters)
+    ev = cg.lib.EV_TO_HA
+    sig, eps = 2.315, 0.167 * ev
+    ljp = cg.lj_potential(sig, eps, 2.5 * sig, 63.55)
+    sl = cg.fcc(40, 40, 40, lat, 1.0, 1.0, ljp)
+    cg.seed(sl, 700, cg.DISP_GAUSSIAN, 0.05, 300.0, 63.55)
+    d = cg.DeviceSim(sl, cg.opts(cg.POT_LJ, cg.PREC_FP64))
+    try:
+        d.set_lj(eps * 1.02, sig * 0.99)
+        d.force()
+        d.download(sl)
+        tl = by_id(sl, "f")[:, :3].copy()
+        d.set_lj(eps, sig)
+        U, gu = d.energy_grad()
+        L, gl = d.force_loss_grad(tl)
+        errs = []
+        for i, (de, ds) in enumerate([(1, 0), (0, 1)]):
+            h = 1e-6 * (eps if de else sig)
+            v = []
+            for sg in (1, -1):
+                d.set_lj(eps + sg * de * h, sig + sg * ds * h)
+                v.append(d.force_loss_grad(tl)[0])
+            errs.append(abs(gl[i] - (v[0] - v[1]) / (2 * h)) / abs(gl[i]))
+        fd_report["lj_force_loss_fd_max_rel_err"] = float(max(errs))
+        fd_report["lj_grad_energy"] = [float(x) for x in gu]
+        fd_report["lj_grad_loss"] = [float(x) for x in gl]
+    finally:
+        d.close()
+        cg.free_host(sl)
+        cg.free_host(s0)
+    # trajectory adjoint
+    st = lattice(20, 600.0, 900)
+    d = cg.DeviceSim(st, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, per_step_lists=True))
+    try:
+        c, x0, xn = d.get_cheby()
+        t0 = time.perf_counter()
+        J, g = d.traj_energy_grad(200, 1e-15, 20)
+        t_traj = time.perf_counter() - t0
+        errs, skipped = [], 0
+        for q in range(3):
+            jj = int(np.argmax(np.abs(g[32 * q:32 * q + 32]))) + 32 * q
+            h = 1e-6 * max(abs(c[jj]), 1e-3 * np.abs(c[32 * q:32 * q + 32]).max())
+            fds = []
+            for hh in (h, h / 4):
+                v = []
+                for sg in (1, -1):
+                    cc = c.copy()
+                    cc[jj] += sg * hh
+                    d.set_cheby(cc, x0, xn)
+                    d.upload(st)
+                    v.append(d.steps(200)[0])
+                fds.append((v[0] - v[1]) / (2 * hh))
+            scale = max(abs(fds[0]), 1e-3 * np.abs(g).max())
+            if abs(fds[0] - fds[1]) > 1e-6 * scale:
+                skipped += 1  # a cutoff crossing inside the difference bracket
+                continue
+            errs.append(abs(g[jj] - fds[0]) / scale)
+        fd_report["trajectory"] = {"atoms": st.contents.ntot, "steps": 200, "every": 20,
+                                   "J_ha": J, "seconds": t_traj,
+                                   "fd_max_rel_err": float(max(errs)) if errs else None,
+                                   "fd_components": len(errs), "fd_skipped_crossing": skipped}
+    finally:
+        d.close()
+        cg.free_host(st)
+    print(json.dumps({
+        "metric": "adjoint: force-matching gradient (96 Chebyshev coefficients) per 256k-atom "
+                  "EAM Cu configuration, FP64, 1 GB300",
+        "value": statistics.median(r["grad_ms"] for r in rows), "unit": "ms",
+        "higher_is_better": False, "dtype": "f64", "data": "synthetic (seeded FCC Cu)",
+        "config": {"workload": "eam_cu_chebyshev_fcc40_x10_300-900K_adjoint"},
+        "configs": rows, "checks": fd_report}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -456,6 +689,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="step", choices=["step", "batch", "adjoint"],
+                    help="step: the headline 4M-atom step; batch: 64 replicas (C4); "
+                         "adjoint: gradients (C5)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -464,6 +700,10 @@ def main():
                         name=WORKLOAD["name"].replace("fcc100", f"fcc{args.cells}"))
     if args.impl == "reference":
         return reference_arm(args)
+    if args.workload == "batch":
+        return batch_arm(args)
+    if args.workload == "adjoint":
+        return adjoint_arm(args)
     return gpu_arm(args)
 
 

@@ -86,6 +86,7 @@ int alloc_slots(comdgb_sim *h, Slots &s, bool with_natoms, int *err) {
 }
 
 void free_all(comdgb_sim *h) {
+  if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
@@ -363,6 +364,8 @@ int setup_potential(comdgb_sim *h, const simflat_t *s) {
 
 // the captured graphs hold the potentials by value
 void cgapi::drop_graphs(comdgb_sim *h) {
+  if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
+  h->loop_exec = nullptr;
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
@@ -607,6 +610,42 @@ int do_force(comdgb_sim *h) {
   }
   CK(cudaGraphLaunch(h->force_exec, h->stream));
   return finish_force(h);
+}
+
+// n steps as one captured graph (captured once per n and dt), launched once
+// between two events; *ms = the graph's device time.  Then the force call
+// that ends nTimeSteps.
+int do_steps_graph(comdgb_sim *h, int n, double dt, float *ms) {
+  if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
+  const double dt_atu = dt * kBohrPerAtu;
+  if (!h->loop_exec || h->loop_n != n || h->loop_dt != dt_atu) {
+    if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
+    h->loop_exec = nullptr;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < n; i++) enqueue_step(h, dt_atu, nullptr);
+    CK(cudaStreamEndCapture(h->stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&h->loop_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+      return set_err(COMDGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    h->loop_n = n;
+    h->loop_dt = dt_atu;
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, h->stream));
+  CK(cudaGraphLaunch(h->loop_exec, h->stream));
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ms) *ms = t;
+  int rc = check_status(h);
+  return rc ? rc : do_force(h);
 }
 
 int do_steps(comdgb_sim *h, int n, double dt) {
@@ -1194,6 +1233,12 @@ int comdgb_sim_steps(comdgb_sim *h, int n, double dt) {
   if (!h || n < 0) return set_err(COMDGB_ERR_ARG, "bad argument");
   CK(cudaSetDevice(h->device));
   return do_steps(h, n, dt);
+}
+
+int comdgb_sim_graph_steps(comdgb_sim *h, int n, double dt, float *ms) {
+  if (!h || n < 1) return set_err(COMDGB_ERR_ARG, "bad argument");
+  CK(cudaSetDevice(h->device));
+  return do_steps_graph(h, n, dt, ms);
 }
 
 int comdgb_sim_rebox(comdgb_sim *h) {

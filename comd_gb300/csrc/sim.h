@@ -108,6 +108,10 @@ struct comdgb_sim {
   cudaGraphExec_t step_exec = nullptr;
   cudaGraphExec_t force_exec = nullptr;
   double graph_dt = NAN;
+  // n steps captured as one graph (comdgb_sim_graph_steps)
+  cudaGraphExec_t loop_exec = nullptr;
+  int loop_n = 0;
+  double loop_dt = NAN;
   // timing graph (event record nodes between kernel groups)
   cudaGraphExec_t timed_exec = nullptr;
   cudaGraph_t timed_graph = nullptr;

@@ -82,6 +82,8 @@ def _bind(lib):
     L.comdgb_sim_energy_grad.argtypes = [C.c_void_p, D, D]
     L.comdgb_sim_force_loss_grad.argtypes = [C.c_void_p, D, D, D]
     L.comdgb_sim_traj_energy_grad.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, D, D]
+    L.comdgb_sim_graph_steps.argtypes = [C.c_void_p, C.c_int, C.c_double,
+                                         C.POINTER(C.c_float)]
     L.comdgb_batch_create.argtypes = [C.POINTER(P_SIM), C.c_int, C.c_void_p,
                                       C.POINTER(C.c_void_p)]
     L.comdgb_batch_replicas.argtypes = [C.c_void_p]
@@ -308,6 +310,12 @@ class DeviceSim:
         j = C.c_double()
         check(self.L.comdgb_sim_traj_energy_grad(self.h, n, dt, every, C.byref(j), pg))
         return j.value, g
+
+    def graph_steps(self, n, dt=1e-15):
+        """n steps as one CUDA graph launch; returns its device time in ms"""
+        ms = C.c_float()
+        check(self.L.comdgb_sim_graph_steps(self.h, n, dt, C.byref(ms)))
+        return ms.value
 
     def advance_velocity(self, dt):
         check(self.L.comdgb_sim_advance_velocity(self.h, dt))

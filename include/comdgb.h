@@ -136,6 +136,10 @@ int comdgb_sim_synchronize(comdgb_sim *h);
 int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms,
                            float *kernel_ms, int max_kernels);
 const char *comdgb_kernel_name(comdgb_sim *h, int k);
+/* nTimeSteps(n, ., dt) with the n steps captured as ONE CUDA graph (captured
+ * at the first call for this n and dt, then replayed), launched once; *ms
+ * (optional) = that launch's device time.  Ends with the force call. */
+int comdgb_sim_graph_steps(comdgb_sim *h, int n, double dt, float *ms);
 /* kernels launched per replay of the captured step graph / force graph */
 int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
 /* list mode in use (1 persistent, 0 per step), its skin, and the number of

@@ -78,3 +78,36 @@ def test_batch_mixed_matches_single_runs():
     finally:
         for s in batch_sims + single_sims:
             cg.free_host(s)
+
+
+@pytest.mark.gpu
+def test_graph_steps_loop_equals_step_replays():
+    """n steps captured as one graph give the same FP64 state as n replays of
+    the one-step graph (single simulation and batch)"""
+    pot = cg.eam_potential("cu")
+    o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, True, per_step_lists=True)
+    a, b = make_replicas(pot), make_replicas(pot)
+    try:
+        da, db = cg.DeviceSim(a[0], o), cg.DeviceSim(b[0], o)
+        try:
+            ea = da.steps(12)[0]
+            ms = db.graph_steps(12)
+            eb = db.energy()[0]
+            da.download(a[0])
+            db.download(b[0])
+        finally:
+            da.close()
+            db.close()
+        assert ms > 0 and ea == eb
+        assert slots_equal(a[0], b[0])
+        ba, bb = cg.Batch(a[1:], o), cg.Batch(b[1:], o)
+        try:
+            ba.steps(8)
+            bb.graph_steps(8)
+            assert np.array_equal(ba.energies()[0], bb.energies()[0])
+        finally:
+            ba.close()
+            bb.close()
+    finally:
+        for s in a + b:
+            cg.free_host(s)
