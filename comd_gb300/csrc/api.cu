@@ -925,6 +925,10 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
   h->g.nboxes = (int)nbt;
   h->g.periodic = o->periodic;
   h->g.nrep = nrep;
+  for (int j = 0; j < 3; j++) {
+    h->g.hi0[j] = h->reps[0].hi[j];
+    h->g.lo0[j] = h->reps[0].lo[j];
+  }
   h->ntot = (int)ntt;
   h->nslots = (int)nbt * CG_MAXATOMS;
   h->volume = h->volumes[0];

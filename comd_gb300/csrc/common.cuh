@@ -48,6 +48,7 @@ struct Geom {
   const RepGeo *rep;     // [nrep]
   const int *box_rep;    // [nboxes] replica of each box (null: one replica)
   const int *boxc;       // [nboxes] packed box coordinates (within the replica) ix | iy << 10 | iz << 20
+  float hi0[3], lo0[3];  // replica 0's boxsize as FP32 hi + lo (kernel-parameter copies)
 };
 
 // the grid of the replica box b belongs to

@@ -873,7 +873,9 @@ __device__ __forceinline__ float small_int_minus1(int k) {
 // dz, r2) for every entry; with NEED_FI positions come from fo.pf and fj is
 // F'(rho_j) (its w), else fj is unspecified.  An overflowed list scans the
 // stencil of the atom's current slot instead.
-template <bool NEED_FI, class F>
+// MULTI: a batch of replicas (the box size comes from the atom's replica);
+// else replica 0's sizes are kernel-parameter constants (no registers held)
+template <bool NEED_FI, bool MULTI, class F>
 __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot, float4 pi,
                                             float rc2, F &&fn) {
   const int n = A.fo.n[a];
@@ -885,9 +887,13 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
                         });
     return;
   }
-  const RepGeo &R = rep_of(A.g, slot >> 6);
-  const float hx = R.hi[0], hy = R.hi[1], hz = R.hi[2];
-  const float lx = R.lo[0], ly = R.lo[1], lz = R.lo[2];
+  float hx = A.g.hi0[0], hy = A.g.hi0[1], hz = A.g.hi0[2];
+  float lx = A.g.lo0[0], ly = A.g.lo0[1], lz = A.g.lo0[2];
+  if (MULTI) {
+    const RepGeo &R = rep_of(A.g, slot >> 6);
+    hx = R.hi[0], hy = R.hi[1], hz = R.hi[2];
+    lx = R.lo[0], ly = R.lo[1], lz = R.lo[2];
+  }
   const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
   // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1
@@ -910,7 +916,7 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   }
 }
 
-template <int EVAL>
+template <int EVAL, bool MULTI>
 __global__ void __launch_bounds__(FO1_THREADS, 2)
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
@@ -921,14 +927,14 @@ __global__ void __launch_bounds__(FO1_THREADS, 2)
     Pass1Acc<float> acc;
     acc.zero();
     eam_pass1_sum(P, seg_sm, acc,
-                  [&](auto &&fn) { fo_for_each<false>(A, a, slot, pi, P.rc2, fn); });
+                  [&](auto &&fn) { fo_for_each<false, MULTI>(A, a, slot, pi, P.rc2, fn); });
     const float dF = eam_pass1_store(A, P, acc, slot);
     A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
     A.nbr_n[a] = acc.cnt;
   }
 }
 
-template <int EVAL>
+template <int EVAL, bool MULTI>
 __global__ void __launch_bounds__(PASS_THREADS)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
@@ -939,7 +945,7 @@ __global__ void __launch_bounds__(PASS_THREADS)
     Pass2Acc<float> acc;
     acc.zero();
     eam_pass2_sum(P, seg_sm, pi.w, acc,
-                  [&](auto &&fn) { fo_for_each<true>(A, a, slot, pi, P.rc2, fn); });
+                  [&](auto &&fn) { fo_for_each<true, MULTI>(A, a, slot, pi, P.rc2, fn); });
     eam_pass2_store(A, acc, slot, a);
   }
 }
@@ -992,7 +998,8 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
 }
 
 // LJ in force order (mixed precision, persistent lists)
-static __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<float> P) {
+template <bool MULTI>
+__global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<float> P) {
   const float s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6, rc2 = P.rc2;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
@@ -1012,7 +1019,7 @@ static __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A,
       fz.add(dz * fr);
       sx.add(fr * dx * dx);
     };
-    fo_for_each<false>(A, a, slot, A.fo.pos[a], rc2, fn);
+    fo_for_each<false, MULTI>(A, a, slot, A.fo.pos[a], rc2, fn);
     int ne = A.et.n[b], nonempty = 0;
     for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
     d4 p = A.s.p[slot];

@@ -50,17 +50,29 @@ cudaError_t prepare_force_kernels<FT>() {
   if (e != cudaSuccess) return e;
 #if COMDGB_FT_FLOAT
   {
-    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[0][EVAL_TABLE],
+    // resident CTAs of the single-replica variants (the batch variants take
+    // the same grids; they are grid-stride loops)
+    int dummy = 0;
+    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[0][EVAL_TABLE],
                        FO1_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY>, pass_smem(0, EVAL_CHEBY),
+      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, false>, pass_smem(0, EVAL_CHEBY),
                          &g_fo_per_sm[0][EVAL_CHEBY], FO1_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE>, 0, &g_fo_per_sm[1][EVAL_TABLE]);
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[1][EVAL_TABLE]);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY>, pass_smem(1, EVAL_CHEBY),
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, false>, pass_smem(1, EVAL_CHEBY),
                          &g_fo_per_sm[1][EVAL_CHEBY]);
-    if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel, 0, &g_fo_per_sm[2][0]);
+    if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<false>, 0, &g_fo_per_sm[2][0]);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, true>, 0, &dummy, FO1_THREADS);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, true>, pass_smem(0, EVAL_CHEBY), &dummy,
+                         FO1_THREADS);
+    if (e == cudaSuccess) e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, true>, 0, &dummy);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, true>, pass_smem(1, EVAL_CHEBY), &dummy);
+    if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<true>, 0, &dummy);
     return e;
   }
 #endif
@@ -100,11 +112,15 @@ template <int EVAL>
 void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st) {
   if (A.ntot <= 0) return;
   const size_t smem = P.seg.n > 0 ? pass_smem(pass, EVAL) : 0;
-  if (pass == 0)
-    fo_eam_pass1_kernel<EVAL><<<pass_grid(0, EVAL, A.ntot, true, FO1_THREADS), FO1_THREADS, smem,
-                                st>>>(A, P);
-  else
-    fo_eam_pass2_kernel<EVAL><<<pass_grid(1, EVAL, A.ntot, true), PASS_THREADS, smem, st>>>(A, P);
+  const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS), g1 = pass_grid(1, EVAL, A.ntot, true);
+  const bool multi = A.g.nrep > 1;
+  if (pass == 0) {
+    if (multi) fo_eam_pass1_kernel<EVAL, true><<<g0, FO1_THREADS, smem, st>>>(A, P);
+    else fo_eam_pass1_kernel<EVAL, false><<<g0, FO1_THREADS, smem, st>>>(A, P);
+  } else {
+    if (multi) fo_eam_pass2_kernel<EVAL, true><<<g1, PASS_THREADS, smem, st>>>(A, P);
+    else fo_eam_pass2_kernel<EVAL, false><<<g1, PASS_THREADS, smem, st>>>(A, P);
+  }
 }
 template void launch_fo_eam<EVAL_TABLE>(const ForceArgs &, const EamPot<float, EVAL_TABLE> &,
                                         int, cudaStream_t);
@@ -112,7 +128,10 @@ template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, E
                                         int, cudaStream_t);
 
 void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st) {
-  if (A.ntot > 0) fo_lj_kernel<<<pass_grid(2, 0, A.ntot, true), PASS_THREADS, 0, st>>>(A, P);
+  if (A.ntot <= 0) return;
+  const int grid = pass_grid(2, 0, A.ntot, true);
+  if (A.g.nrep > 1) fo_lj_kernel<true><<<grid, PASS_THREADS, 0, st>>>(A, P);
+  else fo_lj_kernel<false><<<grid, PASS_THREADS, 0, st>>>(A, P);
 }
 #endif
 
