@@ -9,8 +9,8 @@ package only builds and binds the library for tests and benchmarks.
 from . import abi
 from .lib import (Batch, DISP_GAUSSIAN, DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY,
                   POT_EAM_TABLE, POT_LJ, PREC_FP64, PREC_MIXED, ComdgbError, DeviceSim,
-                  eam_potential, fcc, free_host, lj_potential, load, opts, round_f32, seed)
+                  eam_potential, fcc, free_host, read_clsman, DATA_DIR, lj_potential, load, opts, round_f32, seed)
 
 __all__ = ["abi", "load", "Batch", "opts", "DeviceSim", "ComdgbError", "eam_potential", "lj_potential",
-           "fcc", "seed", "free_host", "round_f32", "POT_DIR", "POT_EAM_TABLE", "POT_EAM_CHEBY", "POT_LJ",
+           "fcc", "read_clsman", "DATA_DIR", "seed", "free_host", "round_f32", "POT_DIR", "POT_EAM_TABLE", "POT_EAM_CHEBY", "POT_LJ",
            "PREC_FP64", "PREC_MIXED", "DISP_NONE", "DISP_UNIFORM", "DISP_GAUSSIAN"]

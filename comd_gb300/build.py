@@ -56,6 +56,16 @@ def _run(cmd):
     return r.stdout + r.stderr
 
 
+def _have_zlib():
+    """zlib headers and library present (gzip clsman input); probed by a test link"""
+    src = os.path.join(OBJDIR, "zprobe.c")
+    with open(src, "w") as f:
+        f.write("#include <zlib.h>\nint main(void) { return zlibVersion() == 0; }\n")
+    r = subprocess.run(["gcc", src, "-o", os.path.join(OBJDIR, "zprobe"), "-lz"],
+                       capture_output=True, text=True)
+    return r.returncode == 0
+
+
 def build(force=False, verbose=False):
     """Compile (if sources are newer than the library) and return its path."""
     if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= _deps():
@@ -66,10 +76,12 @@ def build(force=False, verbose=False):
     for src, extra in UNITS:
         obj = os.path.join(OBJDIR, src.replace(".cu", ".o"))
         jobs.append(([nvcc] + NVFLAGS + extra + ["-c", os.path.join(CSRC, src), "-o", obj], obj))
+    zlib = _have_zlib()
     for src in CUNITS:
         obj = os.path.join(OBJDIR, src.replace(".c", ".o"))
-        jobs.append((["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-I", INCLUDE, "-c",
-                      os.path.join(CSRC, src), "-o", obj], obj))
+        jobs.append((["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-I", INCLUDE]
+                     + (["-DCOMDGB_HAVE_ZLIB"] if zlib else [])
+                     + ["-c", os.path.join(CSRC, src), "-o", obj], obj))
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(lambda j: _run(j[0]), jobs))
     if verbose:
@@ -77,7 +89,8 @@ def build(force=False, verbose=False):
             if log.strip():
                 print(log)
     tmp = OUT + ".tmp"
-    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs] + ["-lm"])
+    _run([nvcc] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs] + ["-lm"]
+         + (["-lz"] if zlib else []))
     os.replace(tmp, OUT)
     return OUT
 

@@ -11,6 +11,9 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#ifdef COMDGB_HAVE_ZLIB
+#include <zlib.h>
+#endif
 
 #include "comdgb.h"
 #include "comdgb_seed.h"
@@ -176,8 +179,10 @@ static int alloc_domains(simflat_t *s) {
   return 0;
 }
 
-/* putAtomInBox (domains.c:237-291) for one atom at world position x */
-static int put_atom(simflat_t *s, int id, int itype, double mass, const double *x) {
+/* putAtomInBox (domains.c:237-291) for one atom at world position x with
+ * momenta p (NULL: zero) */
+static int put_atom(simflat_t *s, int id, int itype, double mass, const double *x,
+                    const double *p) {
   double w[3];
   int ib[3];
   for (int m = 0; m < 3; m++) {
@@ -194,7 +199,10 @@ static int put_atom(simflat_t *s, int id, int itype, double mass, const double *
   s->id[off] = id;
   s->iType[off] = itype;
   s->mass[off] = mass;
-  for (int m = 0; m < 3; m++) s->r[off][m] = w[m] - s->dcenter[b][m];
+  for (int m = 0; m < 3; m++) {
+    s->r[off][m] = w[m] - s->dcenter[b][m];
+    s->p[off][m] = p ? p[m] : 0.0;
+  }
   return 0;
 }
 
@@ -220,12 +228,185 @@ simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double
       for (pt[1] = lat / 4.0; pt[1] < s->bounds[1] && !st; pt[1] += half, cj++)
         for (pt[0] = lat * defgrad / 4.0; pt[0] < s->bounds[0] && !st;
              pt[0] += half * defgrad, ci++)
-          if ((ci + cj + ck) % 2) st = put_atom(s, nid++, 1, pot->mass, pt);
+          if ((ci + cj + ck) % 2) st = put_atom(s, nid++, 1, pot->mass, pt, NULL);
   }
   if (status) *status = st;
   if (st) {
     comdgb_sim_free_host(s);
     return NULL;
+  }
+  return s;
+}
+
+/* The whole file into memory (gzip through zlib when the library was built
+ * with it); NUL-terminated.  Returns NULL on failure with *st set. */
+static char *read_all(const char *path, int *st) {
+  FILE *fp = fopen(path, "rb");
+  if (!fp) {
+    *st = COMDGB_ERR_IO;
+    return NULL;
+  }
+  unsigned char magic[2] = {0, 0};
+  size_t got = fread(magic, 1, 2, fp);
+  fclose(fp);
+  int gz = got == 2 && magic[0] == 0x1f && magic[1] == 0x8b;
+  size_t cap = 1 << 20, len = 0;
+  char *buf = (char *)malloc(cap + 1);
+  if (!buf) {
+    *st = COMDGB_ERR_NOMEM;
+    return NULL;
+  }
+  if (gz) {
+#ifdef COMDGB_HAVE_ZLIB
+    gzFile g = gzopen(path, "rb");
+    if (!g) {
+      free(buf);
+      *st = COMDGB_ERR_IO;
+      return NULL;
+    }
+    for (;;) {
+      if (len == cap) {
+        char *nb = (char *)realloc(buf, 2 * cap + 1);
+        if (!nb) {
+          gzclose(g);
+          free(buf);
+          *st = COMDGB_ERR_NOMEM;
+          return NULL;
+        }
+        buf = nb;
+        cap *= 2;
+      }
+      int n = gzread(g, buf + len, (unsigned)(cap - len));
+      if (n <= 0) break;
+      len += (size_t)n;
+    }
+    gzclose(g);
+#else
+    free(buf);
+    *st = COMDGB_ERR_UNSUPPORTED;  /* built without zlib: pass the decompressed text */
+    return NULL;
+#endif
+  } else {
+    fp = fopen(path, "rb");
+    if (!fp) {
+      free(buf);
+      *st = COMDGB_ERR_IO;
+      return NULL;
+    }
+    for (;;) {
+      if (len == cap) {
+        char *nb = (char *)realloc(buf, 2 * cap + 1);
+        if (!nb) {
+          fclose(fp);
+          free(buf);
+          *st = COMDGB_ERR_NOMEM;
+          return NULL;
+        }
+        buf = nb;
+        cap *= 2;
+      }
+      size_t n = fread(buf + len, 1, cap - len, fp);
+      if (n == 0) break;
+      len += n;
+    }
+    fclose(fp);
+  }
+  buf[len] = 0;
+  return buf;
+}
+
+/* next line of the buffer (as gzgets: up to and including '\n') */
+static const char *next_line(const char **cur) {
+  const char *l = *cur;
+  if (!*l) return NULL;
+  const char *e = strchr(l, '\n');
+  *cur = e ? e + 1 : l + strlen(l);
+  return l;
+}
+
+/* fromFileGzip / fromFileASCII (read.c:155-241): a clsman file -- "natoms
+ * nmove", a comment line, the periodic bounds, then one line "x y z itype px
+ * py pz" per atom -- into a new simflat_t with allocDomains' grid for box
+ * factor bf; atom i gets id i, type 0 and the potential's mass, placed as n
+ * successive putAtomInBox calls (on the GPU `device`, or on the host for
+ * device < 0). */
+simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, double bf, int device,
+                              int *status) {
+  int st = 0;
+  simflat_t *s = NULL;
+  double *xyz = NULL, *pxyz = NULL, *masses = NULL;
+  int *ids = NULL, *types = NULL;
+  if (!path || !pot) {
+    if (status) *status = COMDGB_ERR_ARG;
+    return NULL;
+  }
+  char *buf = read_all(path, &st);
+  if (!buf) goto done;
+  const char *cur = buf, *l;
+  int natoms = 0, nmove = 0;
+  if (!(l = next_line(&cur)) || sscanf(l, "%d%d", &natoms, &nmove) < 1 || natoms < 0) {
+    st = COMDGB_ERR_IO;
+    goto done;
+  }
+  s = (simflat_t *)zalloc(sizeof *s);
+  if (!s) {
+    st = COMDGB_ERR_NOMEM;
+    goto done;
+  }
+  s->pot = pot;
+  s->bf = bf;
+  s->defgrad = 0.0; /* blankSimulation's; allocDomains then takes strain 1 */
+  s->comment = (char *)zalloc(1024);
+  if ((l = next_line(&cur)) && s->comment) {
+    size_t n = (size_t)(cur - l);
+    memcpy(s->comment, l, n < 1023 ? n : 1023);
+  }
+  if (!(l = next_line(&cur)) ||
+      sscanf(l, "%lg %lg %lg", &s->bounds[0], &s->bounds[1], &s->bounds[2]) != 3) {
+    st = COMDGB_ERR_IO;
+    goto done;
+  }
+  if ((st = alloc_domains(s))) goto done;
+  size_t n = (size_t)natoms;
+  xyz = (double *)malloc(3 * n * sizeof(double) + 8);
+  pxyz = (double *)malloc(3 * n * sizeof(double) + 8);
+  masses = (double *)malloc(n * sizeof(double) + 8);
+  ids = (int *)malloc(n * sizeof(int) + 4);
+  types = (int *)malloc(n * sizeof(int) + 4);
+  if (!xyz || !pxyz || !masses || !ids || !types) {
+    st = COMDGB_ERR_NOMEM;
+    goto done;
+  }
+  for (int i = 0; i < natoms; i++) {
+    int itype = 0;
+    double *x = xyz + 3 * (size_t)i, *p = pxyz + 3 * (size_t)i;
+    if (!(l = next_line(&cur)) ||
+        sscanf(l, "%lg %lg %lg %d %lg %lg %lg", &x[0], &x[1], &x[2], &itype, &p[0], &p[1],
+               &p[2]) != 7) {
+      st = COMDGB_ERR_IO;
+      goto done;
+    }
+    ids[i] = i;
+    types[i] = 0; /* read.c:236: putAtomInBox(s, i, 1, 0, mass, ...) */
+    masses[i] = pot->mass;
+  }
+  if (device >= 0) {
+    st = comdgb_put_atoms(s, natoms, xyz, pxyz, ids, types, masses, device);
+  } else {
+    for (int i = 0; i < natoms && !st; i++)
+      st = put_atom(s, ids[i], types[i], masses[i], xyz + 3 * (size_t)i, pxyz + 3 * (size_t)i);
+  }
+done:
+  free(buf);
+  free(xyz);
+  free(pxyz);
+  free(masses);
+  free(ids);
+  free(types);
+  if (status) *status = st;
+  if (st && s) {
+    comdgb_sim_free_host(s);
+    s = NULL;
   }
   return s;
 }

@@ -103,6 +103,9 @@ def _bind(lib):
     L.comdgb_lj_make.restype = C.POINTER(LjPotential)
     L.comdgb_lj_make.argtypes = [C.c_double] * 4
     L.comdgb_lj_free.argtypes = [C.c_void_p]
+    L.comdgb_read_clsman.restype = P_SIM
+    L.comdgb_read_clsman.argtypes = [C.c_char_p, C.c_void_p, C.c_double, C.c_int,
+                                     C.POINTER(C.c_int)]
     L.comdgb_fcc.restype = P_SIM
     L.comdgb_fcc.argtypes = [C.c_int, C.c_int, C.c_int, C.c_double, C.c_double, C.c_double,
                              C.c_void_p, C.POINTER(C.c_int)]
@@ -208,6 +211,20 @@ def eam_potential(name="cu", potdir=POT_DIR):
 def lj_potential(sigma, epsilon, cutoff, mass):
     L = load()
     return Potential(L.comdgb_lj_make(sigma, epsilon, cutoff, mass), "lj", L.comdgb_lj_free)
+
+
+DATA_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+
+
+def read_clsman(path, pot, bf=1.0, device=0):
+    """comdgb_read_clsman: a clsman file into a new host simflat_t (atoms
+    binned on the GPU `device`, or on the host for device < 0)"""
+    L = load()
+    st = C.c_int(0)
+    s = L.comdgb_read_clsman(path.encode(), pot.base, bf, device, C.byref(st))
+    if not s:
+        raise ComdgbError(st.value, "comdgb_read_clsman failed: " + last_error())
+    return s
 
 
 def fcc(nx, ny, nz, lat, defgrad, bf, pot):

@@ -202,6 +202,14 @@ void comdgb_lj_free(ljpotential_t *p);
 /* create_fcc_lattice (ic_fcc.c:63-141) into a new host simflat_t */
 simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double bf,
                       pmd_base_potential_t *pot, int *status);
+/* fromFileGzip / fromFileASCII (read.c:155-241): a clsman file (gzip when
+ * the library was built with zlib, else plain text; COMDGB_ERR_UNSUPPORTED
+ * for gzip without zlib) into a new host simflat_t: allocDomains' grid for
+ * box factor bf, atom i with id i, type 0 and the potential's mass, binned as
+ * successive putAtomInBox calls on the GPU `device` (device < 0: on the
+ * host).  The caller reboxes, as initSimFromCmdLine does. */
+simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, double bf, int device,
+                              int *status);
 /* seeded displacement / momenta (include/comdgb_seed.h) followed by nothing;
  * the caller reboxes */
 void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,

@@ -564,6 +564,52 @@ static void box_offset(const simflat_t *s, int ib, int jb, double *drbox) {
   }
 }
 
+/* fromFileGzip (src-flat/read.c:155-241) on an uncompressed clsman file:
+ * "natoms nmove", a comment line, the bounds, then "x y z itype px py pz"
+ * per atom; atom i goes in by putAtomInBox(s, i, 1, 0, mass, ...), line by
+ * line as gzgets reads it */
+simflat_t *orc_read_clsman(const char *path, pmd_base_potential_t *pot, double bf,
+                           int *status) {
+  char line[16348];
+  *status = 0;
+  FILE *fp = fopen(path, "r");
+  if (!fp) {
+    *status = -3; /* "Input file does not exist", docompute.c:126 */
+    return NULL;
+  }
+  simflat_t *s = (simflat_t *)orc_calloc(sizeof(simflat_t));
+  s->pot = pot;
+  s->bf = bf;
+  s->comment = (char *)orc_calloc(1024);
+  int natoms = 0, nmove = 0, rc = 0;
+  if (!fgets(line, sizeof line, fp) || sscanf(line, "%d%d", &natoms, &nmove) < 1) rc = -33;
+  if (!rc && fgets(line, sizeof line, fp)) {
+    size_t n = strlen(line);
+    memcpy(s->comment, line, n < 1023 ? n : 1023);
+  }
+  if (!rc && (!fgets(line, sizeof line, fp) ||
+              sscanf(line, "%lg %lg %lg", s->bounds, s->bounds + 1, s->bounds + 2) != 3))
+    rc = -33;
+  if (!rc) rc = orc_alloc_domains(s);
+  for (int i = 0; i < natoms && !rc; i++) {
+    double x, y, z, px, py, pz;
+    int itype;
+    if (!fgets(line, sizeof line, fp) ||
+        sscanf(line, "%lg %lg %lg %d %lg %lg %lg", &x, &y, &z, &itype, &px, &py, &pz) != 7) {
+      rc = -33;
+      break;
+    }
+    rc = orc_put_atom(s, i, 0, pot->mass, x, y, z, px, py, pz);
+  }
+  fclose(fp);
+  if (rc) {
+    *status = rc;
+    orc_sim_free(s);
+    return NULL;
+  }
+  return s;
+}
+
 /* ------------------------------------------------------------------ */
 /* forces                                                              */
 /* ------------------------------------------------------------------ */

@@ -65,6 +65,8 @@ def _bind(lib):
     f.orc_lj_make.restype = C.POINTER(LjPotential)
     f.orc_lj_make.argtypes = [C.c_double] * 4
     f.orc_free.argtypes = [C.c_void_p]
+    f.orc_read_clsman.restype = P_SIM
+    f.orc_read_clsman.argtypes = [C.c_char_p, C.c_void_p, C.c_double, C.POINTER(C.c_int)]
     D = C.POINTER(C.c_double)
     f.orc_cheb_set.argtypes = [C.c_void_p, D, D, D]
     f.orc_eam_cheb_grad.argtypes = [P_SIM, D, D, D, D, D]
@@ -97,6 +99,14 @@ class Oracle:
 
     def cheby(self, pot, n=32):
         return self.lib.orc_cheb_make(pot, n)
+
+    def read_clsman(self, path, pot, bf=1.0):
+        """fromFileGzip's arithmetic on an uncompressed clsman file"""
+        st = C.c_int(0)
+        s = self.lib.orc_read_clsman(path.encode(), C.cast(pot, C.c_void_p), bf, C.byref(st))
+        if not s:
+            raise IOError(f"oracle clsman read failed: {st.value}")
+        return s
 
     def cheb_set(self, ch, coef, x0, xn):
         """replace the base series (phi, rho, F) and derive the derivative series"""
@@ -177,6 +187,8 @@ class RefLib:
         lib.refh_ntimesteps.restype = C.c_double
         lib.refh_ntimesteps.argtypes = [C.c_int, P_SIM, C.c_double]
         lib.refh_set_periodic.argtypes = [C.c_int]
+        lib.refh_read_clsman.restype = P_SIM
+        lib.refh_read_clsman.argtypes = [C.c_char_p, C.c_double, C.c_void_p, C.c_int]
         self.lib = lib
         self.cheby = cheby
 

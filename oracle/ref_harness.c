@@ -16,6 +16,7 @@
 #include "pmd.h"
 #include "cheby.h"
 #include "ic_fcc.h"
+#include "read.h"
 
 extern int PERIODIC;
 extern void reBoxAll(simflat_t *s);
@@ -64,6 +65,19 @@ void *refh_fcc(int nx, int ny, int nz, double lat, double defgrad, double bf, vo
   cmd.doeam = is_eam;
   simflat_t *s = create_fcc_lattice(cmd, (struct pmd_base_potential_t *)pot);
   if (is_eam) s->ch_pot = setChebPot((eampotential_t *)pot, 32);
+  return s;
+}
+
+/* the reference's own clsman reader (fromFileASCII -> fromFileGzip in a
+ * GZIPSUPPORT build), then setChebPot for EAM as initSimFromCmdLine does */
+void *refh_read_clsman(const char *path, double bf, void *pot, int is_eam) {
+  command_t cmd;
+  memset(&cmd, 0, sizeof cmd);
+  strncpy(cmd.filename, path, sizeof cmd.filename - 1);
+  cmd.bf = bf;
+  cmd.doeam = is_eam;
+  simflat_t *s = fromFileASCII(cmd, (struct pmd_base_potential_t *)pot);
+  if (s && is_eam) s->ch_pot = setChebPot((eampotential_t *)pot, 32);
   return s;
 }
 

@@ -1,0 +1,157 @@
+"""clsman input (fromFileGzip, read.c:155-241) on the bundled Ag structures.
+
+Known answers from runs of the reference on data/8k.inp.gz with the Ag
+potential, box factor 1 (`comd_dbl -e -p ag -f data/8k.inp.gz` and the
+Chebyshev build): E0 (after the first force call), E10 (after nTimeSteps(10),
+dt = 1 fs, table) and E200 (after 20 x nTimeSteps(10), Chebyshev)."""
+import gzip
+import os
+
+import numpy as np
+import pytest
+
+import comd_gb300 as cg
+from comd_gb300.abi import by_id
+from helpers import slots_equal
+from oracle import KIND_EAM_CHEBY, KIND_EAM_TABLE
+
+E0_TABLE = -852.31072722864178
+E10_TABLE = -852.67331452789108
+E0_CHEBY = -852.27037691173302
+E200_CHEBY = -854.77081758005625
+E0_TWO_ATOMS = -0.007229952672898890681
+GZ = os.path.join(cg.DATA_DIR, "8k.inp.gz")
+
+
+@pytest.fixture(scope="module")
+def text_file(tmp_path_factory):
+    """the 8k file decompressed (the oracle reads text)"""
+    p = tmp_path_factory.mktemp("clsman") / "8k.inp"
+    p.write_bytes(gzip.open(GZ).read())
+    return str(p)
+
+
+def zlib_built():
+    pot = cg.eam_potential("ag")
+    try:
+        s = cg.read_clsman(GZ, pot, 1.0, -1)
+    except cg.ComdgbError as e:
+        if e.code == -34:
+            return False
+        raise
+    cg.free_host(s)
+    return True
+
+
+def host_read(text_file, pot):
+    return cg.read_clsman(GZ if zlib_built() else text_file, pot, 1.0, -1)
+
+
+def test_oracle_clsman_known_answers(oracle, pots_dir, text_file):
+    opot = oracle.eam(pots_dir, "ag")
+    for kind, e0 in [(KIND_EAM_TABLE, E0_TABLE), (KIND_EAM_CHEBY, E0_CHEBY)]:
+        so = oracle.read_clsman(text_file, opot, 1.0)
+        try:
+            assert so.contents.ntot == 8192
+            if kind == KIND_EAM_CHEBY:
+                so.contents.ch_pot = oracle.cheby(opot, 32)
+            assert oracle.rebox(so) == 0
+            assert oracle.force(so, kind) == 0
+            assert so.contents.e == pytest.approx(e0, rel=1e-15, abs=0)
+        finally:
+            oracle.free(so)
+
+
+def test_oracle_two_atom_file(oracle, pots_dir, tmp_path):
+    p = tmp_path / "2.inp"
+    p.write_bytes(gzip.open(os.path.join(cg.DATA_DIR, "2.inp.gz")).read())
+    so = oracle.read_clsman(str(p), oracle.eam(pots_dir, "ag"), 1.0)
+    try:
+        assert so.contents.ntot == 2
+        assert oracle.rebox(so) == 0
+        assert oracle.force(so, KIND_EAM_TABLE) == 0
+        assert so.contents.e == pytest.approx(E0_TWO_ATOMS, rel=1e-14, abs=0)
+    finally:
+        oracle.free(so)
+
+
+def test_host_reader_matches_oracle_and_reference(oracle, pots_dir, text_file):
+    pot = cg.eam_potential("ag")
+    sh = host_read(text_file, pot)
+    so = oracle.read_clsman(text_file, oracle.eam(pots_dir, "ag"), 1.0)
+    try:
+        assert sh.contents.ntot == 8192
+        assert list(sh.contents.nbx) == [11, 11, 5]
+        assert slots_equal(sh, so, ("id", "iType", "mass", "r", "p"))
+        try:
+            from oracle import ref_lib
+            ref = ref_lib(False)
+        except (FileNotFoundError, OSError):
+            return  # the reference sources are not on this machine
+        ep = ref.lib.refh_eam_load(pots_dir.encode(), b"ag")
+        sr = ref.lib.refh_read_clsman(GZ.encode(), 1.0, ep, 0)
+        assert slots_equal(sh, sr, ("id", "iType", "mass", "r", "p"))
+    finally:
+        cg.free_host(sh)
+        oracle.free(so)
+
+
+@pytest.mark.gpu
+def test_gpu_binning_of_clsman_file_matches_host(text_file):
+    pot = cg.eam_potential("ag")
+    src = GZ if zlib_built() else text_file
+    sd = cg.read_clsman(src, pot, 1.0, 0)
+    sh = cg.read_clsman(src, pot, 1.0, -1)
+    try:
+        assert slots_equal(sd, sh, ("id", "iType", "mass", "r", "p"))
+    finally:
+        cg.free_host(sd)
+        cg.free_host(sh)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("potential", [cg.POT_EAM_TABLE, cg.POT_EAM_CHEBY])
+def test_gpu_clsman_known_answers(text_file, potential):
+    pot = cg.eam_potential("ag")
+    s = host_read(text_file, pot)
+    try:
+        assert cg.load().comdgb_rebox_host(s, 1, 0) == 0
+        d = cg.DeviceSim(s, cg.opts(potential, cg.PREC_FP64))
+        try:
+            e0 = d.force()[0]
+            if potential == cg.POT_EAM_TABLE:
+                assert e0 == pytest.approx(E0_TABLE, rel=1e-13, abs=0)
+                assert d.steps(10)[0] == pytest.approx(E10_TABLE, rel=1e-10, abs=0)
+            else:
+                assert e0 == pytest.approx(E0_CHEBY, rel=1e-12, abs=0)
+                for _ in range(20):
+                    e = d.steps(10)[0]
+                assert e == pytest.approx(E200_CHEBY, rel=1e-8, abs=0)
+        finally:
+            d.close()
+    finally:
+        cg.free_host(s)
+
+
+@pytest.mark.gpu
+def test_gpu_mixed_forces_on_clsman_structure(text_file):
+    """mixed precision on the real Ag structure: force error vs FP64 < 1e-5"""
+    pot = cg.eam_potential("ag")
+    s64, s32 = host_read(text_file, pot), host_read(text_file, pot)
+    try:
+        for s in (s64, s32):
+            assert cg.load().comdgb_rebox_host(s, 1, 0) == 0
+        for s, prec in ((s64, cg.PREC_FP64), (s32, cg.PREC_MIXED)):
+            d = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY, prec))
+            try:
+                d.force()
+                d.download(s)
+            finally:
+                d.close()
+        f64 = by_id(s64, "f")[:, :3]
+        f32 = by_id(s32, "f")[:, :3]
+        err = np.sqrt(((f32 - f64) ** 2).sum() / (f64 ** 2).sum())
+        assert err < 1e-5
+    finally:
+        cg.free_host(s64)
+        cg.free_host(s32)
