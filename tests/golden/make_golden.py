@@ -92,6 +92,24 @@ def lj_case(n, sigma, eps, rc, mass, lat, seed, amp, steps):
     return out
 
 
+def clsman_case(cheby, fname, steps):
+    """a bundled Ag structure read by the reference's fromFileGzip, reboxed as
+    initSimFromCmdLine does, then the force call and `steps` steps"""
+    R = ref_lib(cheby)
+    L = R.lib
+    pot = L.refh_eam_load(POTDIR, b"ag")
+    path = os.path.join(ROOT, "comd_gb300", "data", fname).encode()
+    s = L.refh_read_clsman(path, 1.0, pot, 1)
+    L.refh_rebox(s)
+    L.refh_force(s)
+    out = {"force": snapshot(s)}
+    if steps:
+        L.refh_ntimesteps(steps, s, 1e-15)
+        out["steps"] = steps
+        out["after"] = snapshot(s)
+    return out
+
+
 def main():
     if ref_lib(False) is None or ref_lib(True) is None:
         sys.exit("oracle/_ref is not built (run make -C oracle with the reference sources)")
@@ -108,6 +126,11 @@ def main():
     fx["cu3_table_small_grid"] = eam_case(False, 3, 1.0, 1.0, 4, 2, 0.05, 600.0, 3)
     fx["lj8_baseline_params"] = lj_case(8, 2.315, 0.167 * EV, 2.5 * 2.315, 63.55, 3.615, 5,
                                         0.01 * 2.315, 10)
+    # the bundled Ag structures (clsman files)
+    fx["ag8k_table_file"] = clsman_case(False, "8k.inp.gz", 10)
+    fx["ag8k_cheby_file"] = clsman_case(True, "8k.inp.gz", 10)
+    fx["ag262k_table_file"] = clsman_case(False, "262k.inp.gz", 0)
+    fx["ag262k_cheby_file"] = clsman_case(True, "262k.inp.gz", 0)
     with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
         json.dump(fx, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_fixtures.json"))

@@ -2,8 +2,12 @@
 library's host setup and cloned for the oracle, so both sides start from
 identical bytes."""
 import ctypes as C
+import hashlib
+import json
+import os
 
 import numpy as np
+import pytest
 
 import comd_gb300 as cg
 from comd_gb300.abi import by_id, occupied_mask, slot_views
@@ -95,3 +99,44 @@ def slots_equal(sa, sb, fields=("id", "iType", "mass", "r", "p")):
     if not np.array_equal(va["natoms"], vb["natoms"]):
         return False
     return all(np.array_equal(va[f][m], vb[f][m]) for f in fields)
+
+
+# ------------------------------------------------ reference fixtures ----
+
+FIX = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                  "reference_fixtures.json")))
+
+
+def layout_hash(s):
+    """sha256 of the box occupancies and the ids in slot order"""
+    v = slot_views(s)
+    m = occupied_mask(s)
+    h = hashlib.sha256()
+    h.update(v["natoms"].astype(np.int32).tobytes())
+    h.update(v["id"][m].astype(np.int32).tobytes())
+    return h.hexdigest()
+
+
+def snapshot(s):
+    f = by_id(s, "f")
+    return {"e": s.contents.e, "stress": s.contents.stress, "ntot": s.contents.ntot,
+            "f_first": f[:12], "f_abs_sum": float(np.abs(f[:, :3]).sum()),
+            "rho_first": by_id(s, "rho")[:12], "fi_first": by_id(s, "fi")[:12],
+            "r_first": by_id(s, "r")[:12], "p_first": by_id(s, "p")[:12],
+            "layout": layout_hash(s)}
+
+
+def match(snap, ref, rtol=1e-12, vrtol=1e-12):
+    """a snapshot against a reference fixture: layout exact, energy to rtol,
+    the per-atom vectors of the first ids to vrtol (absolute floor 1e-3 of
+    that relative bound times the largest entry)"""
+    assert snap["ntot"] == ref["ntot"]
+    assert snap["layout"] == ref["layout"]
+    assert snap["e"] == pytest.approx(ref["e"], rel=rtol)
+    assert snap["stress"] == pytest.approx(ref["stress"], rel=1e-10, abs=1e-18)
+    scale = max(np.abs(np.array(ref["f_first"])[:, :3]).max(), 1e-12)
+    assert np.allclose(snap["f_first"], ref["f_first"], rtol=0, atol=1e-11 * scale)
+    assert snap["f_abs_sum"] == pytest.approx(ref["f_abs_sum"], rel=1e-9, abs=1e-12)
+    for k in ("rho_first", "fi_first", "r_first", "p_first"):
+        r = np.array(ref[k])
+        assert np.allclose(snap[k], r, rtol=vrtol, atol=1e-3 * vrtol * np.abs(r).max()), k

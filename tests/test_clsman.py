@@ -12,7 +12,7 @@ import pytest
 
 import comd_gb300 as cg
 from comd_gb300.abi import by_id
-from helpers import slots_equal
+from helpers import FIX, match, slots_equal, snapshot
 from oracle import KIND_EAM_CHEBY, KIND_EAM_TABLE
 
 E0_TABLE = -852.31072722864178
@@ -23,12 +23,25 @@ E0_TWO_ATOMS = -0.007229952672898890681
 GZ = os.path.join(cg.DATA_DIR, "8k.inp.gz")
 
 
+# fixture name -> (file, Chebyshev?, steps after the force call)
+FILE_CASES = {"ag8k_table_file": ("8k.inp.gz", False, 10),
+              "ag8k_cheby_file": ("8k.inp.gz", True, 10),
+              "ag262k_table_file": ("262k.inp.gz", False, 0),
+              "ag262k_cheby_file": ("262k.inp.gz", True, 0)}
+
+
 @pytest.fixture(scope="module")
-def text_file(tmp_path_factory):
-    """the 8k file decompressed (the oracle reads text)"""
-    p = tmp_path_factory.mktemp("clsman") / "8k.inp"
-    p.write_bytes(gzip.open(GZ).read())
-    return str(p)
+def text_dir(tmp_path_factory):
+    """the bundled files decompressed (the oracle reads text)"""
+    d = tmp_path_factory.mktemp("clsman")
+    for f in ("8k.inp.gz", "262k.inp.gz", "2.inp.gz"):
+        (d / f[:-3]).write_bytes(gzip.open(os.path.join(cg.DATA_DIR, f)).read())
+    return d
+
+
+@pytest.fixture(scope="module")
+def text_file(text_dir):
+    return str(text_dir / "8k.inp")
 
 
 def zlib_built():
@@ -62,15 +75,35 @@ def test_oracle_clsman_known_answers(oracle, pots_dir, text_file):
             oracle.free(so)
 
 
-def test_oracle_two_atom_file(oracle, pots_dir, tmp_path):
-    p = tmp_path / "2.inp"
-    p.write_bytes(gzip.open(os.path.join(cg.DATA_DIR, "2.inp.gz")).read())
-    so = oracle.read_clsman(str(p), oracle.eam(pots_dir, "ag"), 1.0)
+def test_oracle_two_atom_file(oracle, pots_dir, text_dir):
+    so = oracle.read_clsman(str(text_dir / "2.inp"), oracle.eam(pots_dir, "ag"), 1.0)
     try:
         assert so.contents.ntot == 2
         assert oracle.rebox(so) == 0
         assert oracle.force(so, KIND_EAM_TABLE) == 0
         assert so.contents.e == pytest.approx(E0_TWO_ATOMS, rel=1e-14, abs=0)
+    finally:
+        oracle.free(so)
+
+
+@pytest.mark.parametrize("name", sorted(FILE_CASES))
+def test_oracle_matches_reference_fixture_files(oracle, pots_dir, text_dir, name):
+    """the oracle on the bundled structures against the reference's own runs
+    (tests/golden/make_golden.py): layout, energy, stress, forces, and the
+    state after 10 steps for the 8k file"""
+    fname, cheby, steps = FILE_CASES[name]
+    opot = oracle.eam(pots_dir, "ag")
+    so = oracle.read_clsman(str(text_dir / fname[:-3]), opot, 1.0)
+    kind = KIND_EAM_CHEBY if cheby else KIND_EAM_TABLE
+    try:
+        if cheby:
+            so.contents.ch_pot = oracle.cheby(opot, 32)
+        assert oracle.rebox(so) == 0
+        assert oracle.force(so, kind) == 0
+        match(snapshot(so), FIX[name]["force"])
+        if steps:
+            assert oracle.steps(so, steps, 1e-15, kind) == 0
+            match(snapshot(so), FIX[name]["after"], rtol=1e-11)
     finally:
         oracle.free(so)
 
@@ -127,6 +160,33 @@ def test_gpu_clsman_known_answers(text_file, potential):
                 for _ in range(20):
                     e = d.steps(10)[0]
                 assert e == pytest.approx(E200_CHEBY, rel=1e-8, abs=0)
+        finally:
+            d.close()
+    finally:
+        cg.free_host(s)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(FILE_CASES))
+def test_gpu_matches_reference_fixture_files(text_dir, name):
+    """device-binned read, FP64 force (and 10 steps on the 8k file) against
+    the reference's own runs on the same files"""
+    fname, cheby, steps = FILE_CASES[name]
+    pot = cg.eam_potential("ag")
+    src = os.path.join(cg.DATA_DIR, fname) if zlib_built() else str(text_dir / fname[:-3])
+    s = cg.read_clsman(src, pot, 1.0, 0)
+    try:
+        assert cg.load().comdgb_rebox_host(s, 1, 0) == 0
+        d = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY if cheby else cg.POT_EAM_TABLE,
+                                    cg.PREC_FP64, True, per_step_lists=True))
+        try:
+            d.force()
+            d.download(s)
+            match(snapshot(s), FIX[name]["force"])
+            if steps:
+                d.steps(steps, 1e-15)
+                d.download(s)
+                match(snapshot(s), FIX[name]["after"], rtol=1e-10, vrtol=1e-10)
         finally:
             d.close()
     finally:

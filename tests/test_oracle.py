@@ -7,28 +7,14 @@
    byte-for-byte comparison of every slot array after force, reBoxAll and
    several timesteps.
 """
-import hashlib
-import json
-import os
-
 import numpy as np
 import pytest
 
 from comd_gb300.abi import by_id, occupied_mask, slot_views
+from helpers import FIX, match, snapshot
 from oracle import KIND_EAM_CHEBY, KIND_EAM_TABLE, KIND_LJ, ref_lib
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-FIX = json.load(open(os.path.join(HERE, "golden", "reference_fixtures.json")))
 EV = 1.0 / 27.211386245988
-
-
-def layout_hash(s):
-    v = slot_views(s)
-    m = occupied_mask(s)
-    h = hashlib.sha256()
-    h.update(v["natoms"].astype(np.int32).tobytes())
-    h.update(v["id"][m].astype(np.int32).tobytes())
-    return h.hexdigest()
 
 
 def eam_run(oracle, pots_dir, cheby, n, defgrad, bf, seed, kind, amp, temp, steps):
@@ -63,27 +49,6 @@ def lj_run(oracle, n, sigma, eps, rc, mass, lat, seed, amp, steps):
         after = snapshot(s)
     oracle.free(s)
     return snap, after
-
-
-def snapshot(s):
-    f = by_id(s, "f")
-    return {"e": s.contents.e, "stress": s.contents.stress, "ntot": s.contents.ntot,
-            "f_first": f[:12], "f_abs_sum": float(np.abs(f[:, :3]).sum()),
-            "rho_first": by_id(s, "rho")[:12], "fi_first": by_id(s, "fi")[:12],
-            "r_first": by_id(s, "r")[:12], "p_first": by_id(s, "p")[:12],
-            "layout": layout_hash(s)}
-
-
-def match(snap, ref, rtol=1e-12):
-    assert snap["ntot"] == ref["ntot"]
-    assert snap["layout"] == ref["layout"]
-    assert snap["e"] == pytest.approx(ref["e"], rel=rtol)
-    assert snap["stress"] == pytest.approx(ref["stress"], rel=1e-10, abs=1e-18)
-    scale = max(np.abs(np.array(ref["f_first"])[:, :3]).max(), 1e-12)
-    assert np.allclose(snap["f_first"], ref["f_first"], rtol=0, atol=1e-11 * scale)
-    assert snap["f_abs_sum"] == pytest.approx(ref["f_abs_sum"], rel=1e-9, abs=1e-12)
-    for k in ("rho_first", "fi_first", "r_first", "p_first"):
-        assert np.allclose(snap[k], ref[k], rtol=1e-12, atol=1e-300), k
 
 
 def test_known_answer_cu_table_10(oracle, pots_dir):
