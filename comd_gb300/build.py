@@ -31,6 +31,7 @@ UNITS = [
     ("api.cu", []),
     ("noalloc.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
+    ("virial.cu", []),
 ]
 CUNITS = ["host_setup.c"]
 

@@ -104,6 +104,10 @@ struct comdgb_sim {
     int nblk = 0;
     std::vector<void *> snaps;  // Snapshot* (checkpoints, mid-step states, final)
   } adj;
+  // virial (virial.cu): per-slot virial / per-atom stress, partial sums,
+  // per-replica sums (device) and their host copy, W then K per replica
+  double *vir_slot = nullptr, *vir_part = nullptr, *vir_out = nullptr;
+  std::vector<double> vir_sums;
   // graphs
   cudaGraphExec_t step_exec = nullptr;
   cudaGraphExec_t force_exec = nullptr;

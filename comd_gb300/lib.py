@@ -90,6 +90,9 @@ def _bind(lib):
     L.comdgb_batch_upload.argtypes = [C.c_void_p, C.c_int, P_SIM]
     L.comdgb_batch_download.argtypes = [C.c_void_p, C.c_int, P_SIM]
     L.comdgb_batch_energies.argtypes = [C.c_void_p, D, D]
+    L.comdgb_sim_virial.argtypes = [C.c_void_p, D, D, D]
+    L.comdgb_batch_virial.argtypes = [C.c_void_p, C.c_int, D, D, D]
+    L.comdgb_sim_atom_stress.argtypes = [C.c_void_p, C.c_int, D]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p
@@ -252,6 +255,7 @@ class DeviceSim:
         self.L = load()
         self.h = C.c_void_p()
         self._pot = o.potential
+        self._nboxes = [host_sim.contents.nboxes]
         check(self.L.comdgb_sim_create(host_sim, C.byref(o), C.byref(self.h)))
 
     def close(self):
@@ -328,6 +332,23 @@ class DeviceSim:
         check(self.L.comdgb_sim_traj_energy_grad(self.h, n, dt, every, C.byref(j), pg))
         return j.value, g
 
+    # ---- virial tensor and per-atom stress ----
+    def virial(self):
+        """force call and virial of every replica: (W[6], K[6], volume) of
+        replica 0, Voigt order xx yy zz yz xz xy, Hartree (Angstrom^3)"""
+        P = C.POINTER(C.c_double)
+        w, k, v = np.zeros(6), np.zeros(6), C.c_double()
+        check(self.L.comdgb_sim_virial(self.h, w.ctypes.data_as(P), k.ctypes.data_as(P),
+                                       C.byref(v)))
+        return w, k, v.value
+
+    def atom_stress(self, r=0):
+        """per-atom stress x volume of the last virial() call, replica r's slot
+        layout: array [nboxes * 64, 6] (empty slots 0)"""
+        a = np.zeros((self._nboxes[r] * 64, 6))
+        check(self.L.comdgb_sim_atom_stress(self.h, r, a.ctypes.data_as(C.POINTER(C.c_double))))
+        return a
+
     def graph_steps(self, n, dt=1e-15):
         """n steps as one CUDA graph launch; returns its device time in ms"""
         ms = C.c_float()
@@ -390,6 +411,7 @@ class Batch(DeviceSim):
         self.h = C.c_void_p()
         self._pot = o.potential
         self.n = len(host_sims)
+        self._nboxes = [q.contents.nboxes for q in host_sims]
         arr = (P_SIM * self.n)(*host_sims)
         check(self.L.comdgb_batch_create(arr, self.n, C.byref(o), C.byref(self.h)))
 
@@ -405,3 +427,11 @@ class Batch(DeviceSim):
         P = C.POINTER(C.c_double)
         check(self.L.comdgb_batch_energies(self.h, e.ctypes.data_as(P), st.ctypes.data_as(P)))
         return e, st
+
+    def virial_rep(self, r):
+        """replica r's (W, K, volume) of the last virial() call"""
+        P = C.POINTER(C.c_double)
+        w, k, v = np.zeros(6), np.zeros(6), C.c_double()
+        check(self.L.comdgb_batch_virial(self.h, r, w.ctypes.data_as(P), k.ctypes.data_as(P),
+                                         C.byref(v)))
+        return w, k, v.value

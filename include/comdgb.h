@@ -188,6 +188,26 @@ int comdgb_sim_force_loss_grad(comdgb_sim *h, const double *target, double *loss
 int comdgb_sim_traj_energy_grad(comdgb_sim *h, int n, double dt, int every, double *j,
                                 double *grad);
 
+/* ---------------- virial tensor and per-atom stress ---------------- */
+/* The reference reports one scalar, s->stress (eam.c:649: x-x of the
+ * embedding term only; ljForce.c:175,210: x-x with the kinetic term added
+ * once per neighbour box); force calls keep that value as it is.  These
+ * calls give the physical tensors next to it.  Voigt order xx yy zz yz xz
+ * xy, energy units (Hartree; lengths in Angstrom):
+ *   w = sum over pairs of dr_ij (x) F_ij   F_ij the force on i from j,
+ *                                          dr_ij = r_i - r_j
+ *   k = sum over atoms of p (x) p / M      M = mass x amu_to_m_e
+ * The pressure tensor is (k + w) / volume.  comdgb_sim_virial runs a force
+ * call on the current state, then the virial of every replica, and reports
+ * replica 0 (a batch: comdgb_batch_virial for the others). */
+int comdgb_sim_virial(comdgb_sim *h, double w[6], double k[6], double *volume);
+/* replica r's tensors and volume from the last comdgb_sim_virial call */
+int comdgb_batch_virial(comdgb_sim *h, int r, double w[6], double k[6], double *volume);
+/* per-atom stress x volume from the last comdgb_sim_virial call,
+ * -(p (x) p / M + 1/2 sum_j dr_ij (x) F_ij), in replica r's slot layout:
+ * out[6 * (box * 64 + i) + c] for the replica's boxes (empty slots 0) */
+int comdgb_sim_atom_stress(comdgb_sim *h, int r, double *out);
+
 /* ---------------- host-side setup (reference setup routines) ---------------- */
 
 /* setEamPot / eamReadASCII (eam.c:102-109, 347-398): reads <dir>/<name>.{phi,rho,f,doc} */

@@ -68,6 +68,9 @@ def _bind(lib):
     f.orc_read_clsman.restype = P_SIM
     f.orc_read_clsman.argtypes = [C.c_char_p, C.c_void_p, C.c_double, C.POINTER(C.c_int)]
     D = C.POINTER(C.c_double)
+    f.orc_virial.argtypes = [P_SIM, C.c_int, D, D, D]
+    f.orc_strained.restype = P_SIM
+    f.orc_strained.argtypes = [P_SIM, D]
     f.orc_cheb_set.argtypes = [C.c_void_p, D, D, D]
     f.orc_eam_cheb_grad.argtypes = [P_SIM, D, D, D, D, D]
     f.orc_lj_grad.argtypes = [P_SIM, D, D, D, D, D]
@@ -130,6 +133,26 @@ class Oracle:
         if rc:
             raise RuntimeError(f"oracle gradient failed: {rc}")
         return e.value, gu, loss.value, gl
+
+    def virial(self, s, kind, atoms=False):
+        """(W[6], K[6], per-slot stress [nslots, 6] or None) of the state after
+        a force call; Voigt order xx yy zz yz xz xy"""
+        P = C.POINTER(C.c_double)
+        w, k = np.zeros(6), np.zeros(6)
+        a = np.zeros((s.contents.nboxes * 64, 6)) if atoms else None
+        rc = self.lib.orc_virial(s, kind, w.ctypes.data_as(P), k.ctypes.data_as(P),
+                                 a.ctypes.data_as(P) if atoms else None)
+        if rc:
+            raise RuntimeError(f"oracle virial failed: {rc}")
+        return w, k, a
+
+    def strained(self, s, scale):
+        """copy of s under x_a -> scale[a] x_a (bounds and positions)"""
+        sc = np.ascontiguousarray(scale, dtype=np.float64)
+        t = self.lib.orc_strained(s, sc.ctypes.data_as(C.POINTER(C.c_double)))
+        if not t:
+            raise RuntimeError("oracle strained copy failed")
+        return t
 
     def lj(self, sigma, epsilon, cutoff, mass):
         return self.lib.orc_lj_make(sigma, epsilon, cutoff, mass)
