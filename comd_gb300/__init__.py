@@ -7,10 +7,14 @@ reference's ``simflat_t`` / ``pot->force`` / ``nTimeSteps``.  This Python
 package only builds and binds the library for tests and benchmarks.
 """
 from . import abi
-from .lib import (Batch, DISP_GAUSSIAN, DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY,
-                  POT_EAM_TABLE, POT_LJ, PREC_FP64, PREC_MIXED, ComdgbError, DeviceSim,
-                  eam_potential, fcc, free_host, read_clsman, DATA_DIR, lj_potential, load, opts, round_f32, seed)
+from .lib import (CLSMAN_BINARY, CLSMAN_TEXT, CLSMAN_TEXT_GZ, DATA_DIR, DISP_GAUSSIAN,
+                  DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY, POT_EAM_TABLE, POT_LJ,
+                  PREC_FP64, PREC_MIXED, Batch, ComdgbError, DeviceSim, eam_potential, fcc,
+                  free_host, lj_potential, load, opts, print_it, read_clsman, round_f32, seed,
+                  set_comment, write_clsman_host)
 
-__all__ = ["abi", "load", "Batch", "opts", "DeviceSim", "ComdgbError", "eam_potential", "lj_potential",
-           "fcc", "read_clsman", "DATA_DIR", "seed", "free_host", "round_f32", "POT_DIR", "POT_EAM_TABLE", "POT_EAM_CHEBY", "POT_LJ",
-           "PREC_FP64", "PREC_MIXED", "DISP_NONE", "DISP_UNIFORM", "DISP_GAUSSIAN"]
+__all__ = ["abi", "load", "Batch", "opts", "DeviceSim", "ComdgbError", "eam_potential",
+           "lj_potential", "fcc", "read_clsman", "write_clsman_host", "set_comment", "print_it",
+           "DATA_DIR", "seed", "free_host", "round_f32", "POT_DIR", "POT_EAM_TABLE",
+           "POT_EAM_CHEBY", "POT_LJ", "PREC_FP64", "PREC_MIXED", "DISP_NONE", "DISP_UNIFORM",
+           "DISP_GAUSSIAN", "CLSMAN_BINARY", "CLSMAN_TEXT_GZ", "CLSMAN_TEXT"]

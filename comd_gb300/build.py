@@ -32,6 +32,7 @@ UNITS = [
     ("noalloc.cu", ["-fmad=false"]),
     ("adjoint.cu", []),
     ("virial.cu", []),
+    ("clsman_io.cu", []),
 ]
 CUNITS = ["host_setup.c"]
 
@@ -73,15 +74,17 @@ def build(force=False, verbose=False):
         return OUT
     os.makedirs(OBJDIR, exist_ok=True)
     nvcc = _nvcc()
+    zlib = _have_zlib()
+    zdef = ["-DCOMDGB_HAVE_ZLIB"] if zlib else []
     jobs = []
     for src, extra in UNITS:
         obj = os.path.join(OBJDIR, src.replace(".cu", ".o"))
-        jobs.append(([nvcc] + NVFLAGS + extra + ["-c", os.path.join(CSRC, src), "-o", obj], obj))
-    zlib = _have_zlib()
+        jobs.append(([nvcc] + NVFLAGS + extra + zdef + ["-c", os.path.join(CSRC, src), "-o", obj],
+                     obj))
     for src in CUNITS:
         obj = os.path.join(OBJDIR, src.replace(".c", ".o"))
         jobs.append((["gcc", "-O2", "-fPIC", "-std=c11", "-Wall", "-I", INCLUDE]
-                     + (["-DCOMDGB_HAVE_ZLIB"] if zlib else [])
+                     + zdef
                      + ["-c", os.path.join(CSRC, src), "-o", obj], obj))
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         logs = list(ex.map(lambda j: _run(j[0]), jobs))

@@ -411,6 +411,19 @@ done:
   return s;
 }
 
+/* printIt (write.c:89-110): box, id + 1, box-relative position, momentum
+ * and force of the atoms with id < 10, in slot order */
+void comdgb_printIt(const simflat_t *s, FILE *fp) {
+  for (int b = 0; b < s->nboxes; b++)
+    for (int i = 0, o = b * COMDGB_MAXATOMS; i < s->natoms[b]; i++, o++)
+      if (s->id[o] < 10)
+        fprintf(fp,
+                "%02d, %02d, X=(%+020.12e %+020.12e %+020.12e) 1 "
+                "P=(%+020.12e %+020.12e %+020.12e) F=(%+020.12e %+020.12e %+020.12e)\n",
+                b, s->id[o] + 1, s->r[o][0], s->r[o][1], s->r[o][2], s->p[o][0], s->p[o][1],
+                s->p[o][2], s->f[o][0], s->f[o][1], s->f[o][2]);
+}
+
 void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,
                  double mass_amu) {
   comdgb_seed_apply(s, seed, disp_kind, amp, temp_k, mass_amu);

@@ -138,6 +138,7 @@ T *track(comdgb_sim *h, T *p) {
   return p;
 }
 cg::ForceArgs force_args(comdgb_sim *h);
+comdgb_sim *find_attached(const void *s);  // the handle of an attached simflat_t
 int do_force(comdgb_sim *h);       // force call (graph), energy and stress to the host
 int check_status(comdgb_sim *h);
 double cheb_host(const double *c, double a, double b, double x);  // eamCheb on the host

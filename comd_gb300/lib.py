@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(HERE, "libcomdgb.so")
 POT_DIR = os.path.join(HERE, "pots")
 
 POT_EAM_TABLE, POT_EAM_CHEBY, POT_LJ = 0, 1, 2
+CLSMAN_BINARY, CLSMAN_TEXT_GZ, CLSMAN_TEXT = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 DISP_NONE, DISP_UNIFORM, DISP_GAUSSIAN = 0, 1, 2
 ERR_MAXATOMS, ERR_BOXRANGE, ERR_NOBOX = -11, -12, -3
@@ -91,6 +92,11 @@ def _bind(lib):
     L.comdgb_batch_download.argtypes = [C.c_void_p, C.c_int, P_SIM]
     L.comdgb_batch_energies.argtypes = [C.c_void_p, D, D]
     L.comdgb_sim_virial.argtypes = [C.c_void_p, D, D, D]
+    L.comdgb_sim_gather.argtypes = [C.c_void_p, C.c_int, D]
+    L.comdgb_sim_write_clsman.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int, C.c_char_p]
+    L.comdgb_writeClsman.argtypes = [P_SIM, C.c_char_p]
+    L.comdgb_gzASCIIWrite.argtypes = [P_SIM, C.c_char_p]
+    L.comdgb_printIt.argtypes = [P_SIM, C.c_void_p]
     L.comdgb_batch_virial.argtypes = [C.c_void_p, C.c_int, D, D, D]
     L.comdgb_sim_atom_stress.argtypes = [C.c_void_p, C.c_int, D]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
@@ -230,6 +236,39 @@ def read_clsman(path, pot, bf=1.0, device=0):
     return s
 
 
+def write_clsman_host(s, path, binary=True):
+    """the drop-ins comdgb_writeClsman / comdgb_gzASCIIWrite on a host
+    simflat_t (gathered on the device when it is attached, else on the host)"""
+    L = load()
+    fn = L.comdgb_writeClsman if binary else L.comdgb_gzASCIIWrite
+    check(fn(s, path.encode()))
+
+
+def set_comment(s, text):
+    """the simflat_t's comment line (a 1024-byte buffer)"""
+    b = text.encode()[:1023] + b"\0"
+    field = C.addressof(s.contents) + type(s.contents).comment.offset
+    buf = C.c_void_p.from_address(field).value  # the char* itself, not a copy
+    if not buf:
+        raise ValueError("simflat_t has no comment buffer")
+    C.memmove(buf, b, len(b))
+
+
+def print_it(s, path):
+    """comdgb_printIt (printIt, write.c:89-110) into a file"""
+    libc = C.CDLL(None)
+    libc.fopen.restype = C.c_void_p
+    libc.fopen.argtypes = [C.c_char_p, C.c_char_p]
+    libc.fclose.argtypes = [C.c_void_p]
+    fp = libc.fopen(path.encode(), b"w")
+    if not fp:
+        raise OSError(f"cannot open {path}")
+    try:
+        load().comdgb_printIt(s, fp)
+    finally:
+        libc.fclose(fp)
+
+
 def fcc(nx, ny, nz, lat, defgrad, bf, pot):
     """create_fcc_lattice on the host; returns a SimFlat pointer (caller frees)."""
     L = load()
@@ -256,6 +295,7 @@ class DeviceSim:
         self.h = C.c_void_p()
         self._pot = o.potential
         self._nboxes = [host_sim.contents.nboxes]
+        self._ntot = [host_sim.contents.ntot]
         check(self.L.comdgb_sim_create(host_sim, C.byref(o), C.byref(self.h)))
 
     def close(self):
@@ -349,6 +389,18 @@ class DeviceSim:
         check(self.L.comdgb_sim_atom_stress(self.h, r, a.ctypes.data_as(C.POINTER(C.c_double))))
         return a
 
+    # ---- clsman output ----
+    def gather(self, r=0):
+        """replica r's atoms in id order: [ntot, 6] = position (box corner + r),
+        momentum"""
+        a = np.zeros((self._ntot[r], 6))
+        check(self.L.comdgb_sim_gather(self.h, r, a.ctypes.data_as(C.POINTER(C.c_double))))
+        return a
+
+    def write_clsman(self, path, fmt=CLSMAN_BINARY, comment=None, r=0):
+        check(self.L.comdgb_sim_write_clsman(self.h, r, path.encode(), fmt,
+                                             None if comment is None else comment.encode()))
+
     def graph_steps(self, n, dt=1e-15):
         """n steps as one CUDA graph launch; returns its device time in ms"""
         ms = C.c_float()
@@ -412,6 +464,7 @@ class Batch(DeviceSim):
         self._pot = o.potential
         self.n = len(host_sims)
         self._nboxes = [q.contents.nboxes for q in host_sims]
+        self._ntot = [q.contents.ntot for q in host_sims]
         arr = (P_SIM * self.n)(*host_sims)
         check(self.L.comdgb_batch_create(arr, self.n, C.byref(o), C.byref(self.h)))
 

@@ -23,6 +23,7 @@
 #define COMDGB_H
 
 #include <stddef.h>
+#include <stdio.h>
 #include <stdint.h>
 
 #include "comdgb_simflat.h"
@@ -230,6 +231,27 @@ simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double
  * host).  The caller reboxes, as initSimFromCmdLine does. */
 simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, double bf, int device,
                               int *status);
+
+/* ---------------- clsman output (write.c) ---------------- */
+enum {
+  COMDGB_CLSMAN_BINARY = 0,  /* writeClsman (write.c:112-167), byte for byte */
+  COMDGB_CLSMAN_TEXT_GZ = 1, /* gzASCIIWrite (write.c:175-220); gzip members, one per chunk */
+  COMDGB_CLSMAN_TEXT = 2     /* the same text, uncompressed (fromFileASCII reads it) */
+};
+/* replica r's atoms in id order, gathered on the device (getRL, write.c:58-87):
+ * out[6 * id + 0..2] = box corner + r (write.c:157), [3..5] = p; ids must be
+ * 0..ntot-1, each once (else COMDGB_ERR_ARG, nothing written) */
+int comdgb_sim_gather(comdgb_sim *h, int r, double *out);
+/* replica r's current state to `path` in `format`; `comment` is the text
+ * file's comment line (a newline is added when it has none; NULL: empty) */
+int comdgb_sim_write_clsman(comdgb_sim *h, int r, const char *path, int format,
+                            const char *comment);
+/* drop-ins for writeClsman(s, fname) and gzASCIIWrite(s, fname): an attached
+ * simflat_t is gathered from the device, any other on the host */
+int comdgb_writeClsman(simflat_t *s, const char *fname);
+int comdgb_gzASCIIWrite(simflat_t *s, const char *fname);
+/* printIt (write.c:89-110): the atoms with id < 10, box by box */
+void comdgb_printIt(const simflat_t *s, FILE *fp);
 /* seeded displacement / momenta (include/comdgb_seed.h) followed by nothing;
  * the caller reboxes */
 void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,

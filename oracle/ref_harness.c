@@ -81,6 +81,32 @@ void *refh_read_clsman(const char *path, double bf, void *pot, int is_eam) {
   return s;
 }
 
+/* the reference's clsman writers (write.c:112-167 binary, :175-220 gzip
+ * text) and its debug print (write.c:89-110) into a file */
+extern void writeClsman(simflat_t *s, char *fname);
+extern void gzASCIIWrite(simflat_t *s, char *fname);
+extern void printIt(simflat_t *s, FILE *fp);
+
+/* the simulation's comment line (gzASCIIWrite writes it verbatim) */
+void refh_set_comment(void *s, const char *text) {
+  simflat_t *q = (simflat_t *)s;
+  strncpy(q->comment, text, 1023);
+}
+
+void refh_write_clsman(void *s, const char *path) { writeClsman((simflat_t *)s, (char *)path); }
+
+void refh_gz_ascii_write(void *s, const char *path) {
+  gzASCIIWrite((simflat_t *)s, (char *)path);
+}
+
+int refh_print_it(void *s, const char *path) {
+  FILE *fp = fopen(path, "w");
+  if (!fp) return -1;
+  printIt((simflat_t *)s, fp);
+  fclose(fp);
+  return 0;
+}
+
 void refh_seed_apply(void *s, uint64_t seed, int kind, double amp, double temp_k,
                      double mass_amu) {
   refh_seed_apply_impl(s, seed, kind, amp, temp_k, mass_amu);

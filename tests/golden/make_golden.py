@@ -110,6 +110,48 @@ def clsman_case(cheby, fname, steps):
     return out
 
 
+def file_digests(L, s, tmp):
+    """sha256 of the reference's writeClsman bytes, of its gzASCIIWrite text
+    (decompressed) and of printIt's output for the state s"""
+    import gzip
+    out = {}
+    L.refh_write_clsman(s, (tmp + ".bin").encode())
+    L.refh_gz_ascii_write(s, (tmp + ".txt.gz").encode())
+    L.refh_print_it(s, (tmp + ".print").encode())
+    b = open(tmp + ".bin", "rb").read()
+    t = gzip.open(tmp + ".txt.gz").read()
+    pr = open(tmp + ".print", "rb").read()
+    out["binary_sha256"] = hashlib.sha256(b).hexdigest()
+    out["binary_bytes"] = len(b)
+    out["text_sha256"] = hashlib.sha256(t).hexdigest()
+    out["text_bytes"] = len(t)
+    out["print_sha256"] = hashlib.sha256(pr).hexdigest()
+    for ext in (".bin", ".txt.gz", ".print"):
+        os.remove(tmp + ext)
+    return out
+
+
+def writer_cases(tmpdir):
+    """clsman output of (1) the Ag 8k file as read and reboxed, (2) a seeded
+    Cu lattice (displacements and momenta from the shared seed routine) with
+    its forces computed, under a set comment"""
+    L = ref_lib(False).lib
+    pot = L.refh_eam_load(POTDIR, b"ag")
+    s = L.refh_read_clsman(os.path.join(ROOT, "comd_gb300", "data", "8k.inp.gz").encode(),
+                           1.0, pot, 1)
+    L.refh_rebox(s)
+    w1 = file_digests(L, s, os.path.join(tmpdir, "w1"))
+    pot = L.refh_eam_load(POTDIR, b"cu")
+    lat = C.cast(pot, C.POINTER(C.c_double * 8)).contents[7]
+    s = L.refh_fcc(6, 6, 6, lat, 1.0, 1.0, pot, 1)
+    L.refh_seed_apply(s, 21, 2, 0.05, 600.0, 63.55)
+    L.refh_rebox(s)
+    L.refh_force(s)
+    L.refh_set_comment(s, b"seeded Cu lattice 6x6x6\n")
+    w2 = file_digests(L, s, os.path.join(tmpdir, "w2"))
+    return {"ag8k_read": w1, "cu6_seeded_forced": w2}
+
+
 def main():
     if ref_lib(False) is None or ref_lib(True) is None:
         sys.exit("oracle/_ref is not built (run make -C oracle with the reference sources)")
@@ -131,6 +173,9 @@ def main():
     fx["ag8k_cheby_file"] = clsman_case(True, "8k.inp.gz", 10)
     fx["ag262k_table_file"] = clsman_case(False, "262k.inp.gz", 0)
     fx["ag262k_cheby_file"] = clsman_case(True, "262k.inp.gz", 0)
+    import tempfile
+    with tempfile.TemporaryDirectory() as td:
+        fx["clsman_writers"] = writer_cases(td)
     with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
         json.dump(fx, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_fixtures.json"))
