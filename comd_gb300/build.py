@@ -33,6 +33,7 @@ UNITS = [
     ("adjoint.cu", []),
     ("virial.cu", []),
     ("clsman_io.cu", []),
+    ("centro.cu", ["-fmad=false"]),
 ]
 CUNITS = ["host_setup.c"]
 

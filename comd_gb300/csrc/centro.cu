@@ -1,0 +1,280 @@
+// centro.cu -- centrosymmetry parameter of every atom
+// (AtomVisualize::computeCentrosymmetry, src-viz/AtomVisualize.c:399-672), a
+// headless kernel over the link cells.
+//
+// One CTA per box, one thread per atom of the box.  The neighbour scan
+// visits the atom's own box (box-relative differences), then the 26 adjacent
+// boxes in x-outer, z-inner order, wrapped once per axis with the periodic
+// offset rounded to float (AtomVisualize.c:458-505), and keeps up to 12
+// candidates: the next free entry while fewer than 12 are held, then the
+// first entry of largest r^2 is replaced unless the candidate's r^2 is
+// larger.  All of it in FP64 with the reference's operation order (this
+// translation unit is built without FMA contraction); r^2 values are
+// compared as the integer images of non-negative doubles.
+//
+// The parameter is the minimum over the 10395 pairings of the 12 vectors of
+// the sum of |r_a + r_b|^2, accumulated in a float over the pairs in the
+// order of their lower index (testCentro, :560-664).  Each thread first
+// scans every pairing with the 66 pair terms rounded to FP32 and plain FP32
+// sums, keeping the least; a second scan recomputes exactly (double terms,
+// each partial sum rounded to float as testCentro does) only the pairings
+// whose FP32 sum lies within 4e-6 of that least.  Both sums round at most
+// six float additions of non-negative terms, so each is within 12 units of
+// 2^-24 of the exact sum; a pairing outside the window cannot be the
+// reference's minimum, and the result is the reference's value bit for bit.
+// The pairings are a constant table (6 pair indices each, lower index first).
+// APPROX_CENTROSYM's greedy pairing (:528-557) is the `approx` variant.
+#include <vector>
+
+#include "sim.h"
+
+using namespace cg;
+using namespace cgapi;
+
+namespace {
+
+constexpr int NPAIR = 66;
+constexpr int NMATCH = 10395;  // 11 * 9 * 7 * 5 * 3
+constexpr int CT = CG_MAXATOMS;  // threads per CTA: one per slot
+
+__constant__ uint8_t c_match[NMATCH * 6];  // pair indices, lower index first
+__constant__ uint8_t c_pa[NPAIR], c_pb[NPAIR];
+
+// pairings of 12 entries, the lowest unpaired entry paired first
+void enumerate(std::vector<uint8_t> &out, int *pair_of, int used, std::vector<int> &cur) {
+  int n = 0;
+  while (n < 12 && (used >> n & 1)) n++;
+  if (n == 12) {
+    for (int k : cur) out.push_back((uint8_t)k);
+    return;
+  }
+  for (int p = n + 1; p < 12; p++) {
+    if (used >> p & 1) continue;
+    cur.push_back(pair_of[n * 12 + p]);
+    enumerate(out, pair_of, used | 1 << n | 1 << p, cur);
+    cur.pop_back();
+  }
+}
+
+int upload_tables(int device) {
+  static bool done[64] = {};
+  if (device >= 0 && device < 64 && done[device]) return 0;
+  int pair_of[144];
+  uint8_t pa[NPAIR], pb[NPAIR];
+  int k = 0;
+  for (int a = 0; a < 12; a++)
+    for (int b = a + 1; b < 12; b++) {
+      pair_of[a * 12 + b] = k;
+      pa[k] = (uint8_t)a;
+      pb[k] = (uint8_t)b;
+      k++;
+    }
+  std::vector<uint8_t> m;
+  std::vector<int> cur;
+  m.reserve(NMATCH * 6);
+  enumerate(m, pair_of, 0, cur);
+  if ((int)m.size() != NMATCH * 6) return set_err(COMDGB_ERR_ARG, "pairing table size");
+  CK(cudaMemcpyToSymbol(c_match, m.data(), m.size()));
+  CK(cudaMemcpyToSymbol(c_pa, pa, sizeof pa));
+  CK(cudaMemcpyToSymbol(c_pb, pb, sizeof pb));
+  if (device >= 0 && device < 64) done[device] = true;
+  return 0;
+}
+
+__device__ __forceinline__ long long key(double rsq) { return __double_as_longlong(rsq); }
+
+// |a + b|^2 of two held vectors, the reference's order
+__device__ __forceinline__ double pair_term(const double (*v)[3][CT], int a, int b, int t) {
+  const double x = __dadd_rn(v[a][0][t], v[b][0][t]);
+  const double y = __dadd_rn(v[a][1][t], v[b][1][t]);
+  const double z = __dadd_rn(v[a][2][t], v[b][2][t]);
+  return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
+}
+
+__global__ void __launch_bounds__(CT) centro_kernel(Geom g, Slots s, const double *dcenter,
+                                                    int approx, double *out) {
+  __shared__ double v[12][3][CT];      // held vectors
+  __shared__ long long vk[12][CT];     // their r^2 (integer images)
+  __shared__ float p32[NPAIR][CT];     // pair terms rounded to FP32
+  const int b = blockIdx.x, t = threadIdx.x;
+  const int ni = s.natoms[b];
+  if (t >= ni) return;
+  const RepGeo &R = rep_of(g, b);
+  const int nx = R.nbx[0], ny = R.nbx[1], nz = R.nbx[2];
+  const int lb = b - R.box0;
+  const int bz = lb / (nx * ny), by = (lb - bz * nx * ny) / nx, bx = lb - bz * nx * ny - by * nx;
+  const int io = b * CG_MAXATOMS + t;
+  const d4 ri = s.r[io];
+  int nb = 0, kmax = 0;
+  long long rmax = 0;
+  auto offer = [&](double dx, double dy, double dz) {
+    const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const long long kk = key(rsq);
+    int i1;
+    if (nb < 12) {
+      i1 = nb++;
+    } else {
+      if (kk > rmax) return;
+      i1 = kmax;
+    }
+    v[i1][0][t] = dx;
+    v[i1][1][t] = dy;
+    v[i1][2][t] = dz;
+    vk[i1][t] = kk;
+    if (nb == 12) {  // first entry of largest r^2
+      kmax = 0;
+      rmax = vk[0][t];
+      for (int k = 1; k < 12; k++)
+        if (vk[k][t] > rmax) {
+          kmax = k;
+          rmax = vk[k][t];
+        }
+    }
+  };
+  // own box: box-relative differences
+  for (int j = 0; j < ni; j++) {
+    if (j == t) continue;
+    const d4 rj = s.r[b * CG_MAXATOMS + j];
+    offer(__dsub_rn(rj.x, ri.x), __dsub_rn(rj.y, ri.y), __dsub_rn(rj.z, ri.z));
+  }
+  const double cxi = __dadd_rn(dcenter[3 * b + 0], ri.x);
+  const double cyi = __dadd_rn(dcenter[3 * b + 1], ri.y);
+  const double czi = __dadd_rn(dcenter[3 * b + 2], ri.z);
+  for (int cx = bx - 1; cx <= bx + 1; cx++)
+    for (int cy = by - 1; cy <= by + 1; cy++)
+      for (int cz = bz - 1; cz <= bz + 1; cz++) {
+        if (cx == bx && cy == by && cz == bz) continue;
+        float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+        int qx = cx, qy = cy, qz = cz;
+        if (qx < 0) { qx = nx - 1; ox = __double2float_rn(-R.bounds[0]); }
+        if (qx >= nx) { qx = 0; ox = __double2float_rn(R.bounds[0]); }
+        if (qy < 0) { qy = ny - 1; oy = __double2float_rn(-R.bounds[1]); }
+        if (qy >= ny) { qy = 0; oy = __double2float_rn(R.bounds[1]); }
+        if (qz < 0) { qz = nz - 1; oz = __double2float_rn(-R.bounds[2]); }
+        if (qz >= nz) { qz = 0; oz = __double2float_rn(R.bounds[2]); }
+        const int b2 = R.box0 + qz * nx * ny + qy * nx + qx;
+        const double ex = __dadd_rn((double)ox, dcenter[3 * b2 + 0]);
+        const double ey = __dadd_rn((double)oy, dcenter[3 * b2 + 1]);
+        const double ez = __dadd_rn((double)oz, dcenter[3 * b2 + 2]);
+        const int nj = s.natoms[b2];
+        for (int j = 0; j < nj; j++) {
+          const d4 rj = s.r[b2 * CG_MAXATOMS + j];
+          offer(__dsub_rn(__dadd_rn(ex, rj.x), cxi), __dsub_rn(__dadd_rn(ey, rj.y), cyi),
+                __dsub_rn(__dadd_rn(ez, rj.z), czi));
+        }
+      }
+  double c = 1000.0;
+  if (nb >= 12) {
+    if (approx) {
+      // greedy pairing; a vector with r^2 = 0 counts as paired
+      bool paired[12];
+      for (int q = 0; q < 12; q++) paired[q] = !(vk[q][t] > 0);
+      c = 0.0;
+      for (int j = 0; j < 11; j++) {
+        if (paired[j]) continue;
+        double summin = 1000.0;
+        int kmin = -1;
+        for (int k = j + 1; k < 12; k++) {
+          if (paired[k]) continue;
+          const double sum = pair_term(v, j, k, t);
+          if (sum < summin) {
+            kmin = k;
+            summin = sum;
+          }
+        }
+        c = __dadd_rn(c, summin);
+        paired[j] = true;
+        if (kmin >= 0) paired[kmin] = true;
+      }
+    } else {
+      for (int k = 0; k < NPAIR; k++)
+        p32[k][t] = __double2float_rn(pair_term(v, c_pa[k], c_pb[k], t));
+      float best = 3.0e38f;
+      for (int m = 0; m < NMATCH; m++) {
+        const uint8_t *q = c_match + 6 * m;
+        float acc = p32[q[0]][t];
+#pragma unroll
+        for (int u = 1; u < 6; u++) acc = __fadd_rn(acc, p32[q[u]][t]);
+        best = fminf(best, acc);
+      }
+      const float window = __fadd_rn(best, __fmul_rn(best, 4e-6f)) + 1e-37f;
+      for (int m = 0; m < NMATCH; m++) {
+        const uint8_t *q = c_match + 6 * m;
+        float acc = p32[q[0]][t];
+#pragma unroll
+        for (int u = 1; u < 6; u++) acc = __fadd_rn(acc, p32[q[u]][t]);
+        if (acc > window) continue;
+        float e = 0.0f;  // testCentro
+#pragma unroll
+        for (int u = 0; u < 6; u++)
+          e = __double2float_rn(__dadd_rn((double)e, pair_term(v, c_pa[q[u]], c_pb[q[u]], t)));
+        if ((double)e < c) c = (double)e;
+      }
+    }
+  }
+  out[io] = c;
+}
+
+// min / max over the replica's atoms (minCentro from 1000, maxCentro from 0)
+__global__ void centro_range_kernel(Geom g, const int *natoms, const double *c, int r,
+                                    double *range) {
+  __shared__ double lo_s[256], hi_s[256];
+  const RepGeo &R = g.rep[r];
+  double lo = 1000.0, hi = 0.0;
+  for (int b = R.box0 + threadIdx.x; b < R.box0 + R.nb; b += blockDim.x)
+    for (int i = 0; i < natoms[b]; i++) {
+      const double x = c[b * CG_MAXATOMS + i];
+      lo = x < lo ? x : lo;
+      hi = x > hi ? x : hi;
+    }
+  lo_s[threadIdx.x] = lo;
+  hi_s[threadIdx.x] = hi;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) {
+      lo_s[threadIdx.x] = fmin(lo_s[threadIdx.x], lo_s[threadIdx.x + o]);
+      hi_s[threadIdx.x] = fmax(hi_s[threadIdx.x], hi_s[threadIdx.x + o]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    range[0] = lo_s[0];
+    range[1] = hi_s[0];
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int comdgb_sim_centrosymmetry(comdgb_sim *h, int r, int approx, double *out, double *cmin,
+                              double *cmax) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  if (r < 0 || r >= h->nrep) return set_err(COMDGB_ERR_ARG, "replica %d of %d", r, h->nrep);
+  CK(cudaSetDevice(h->device));
+  int rc = upload_tables(h->device);
+  if (rc) return rc;
+  int err = 0;
+  if (!h->centro) {
+    h->centro = track(h, dalloc<double>((size_t)h->nslots + 2, &err));
+    if (err) return set_err(COMDGB_ERR_NOMEM, "centrosymmetry buffer");
+  }
+  cudaStream_t st = h->stream;
+  CK(cudaMemsetAsync(h->centro, 0, sizeof(double) * (size_t)h->nslots, st));  // empty slots 0
+  centro_kernel<<<h->g.nboxes, CT, 0, st>>>(h->g, h->s, h->dcenter, approx, h->centro);
+  centro_range_kernel<<<1, 256, 0, st>>>(h->g, h->s.natoms, h->centro, r,
+                                         h->centro + h->nslots);
+  CK(cudaGetLastError());
+  const RepGeo &R = h->reps[r];
+  if (out)
+    CK(cudaMemcpyAsync(out, h->centro + (size_t)R.box0 * CG_MAXATOMS,
+                       sizeof(double) * (size_t)R.nb * CG_MAXATOMS, cudaMemcpyDeviceToHost, st));
+  double range[2];
+  CK(cudaMemcpyAsync(range, h->centro + h->nslots, sizeof range, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (cmin) *cmin = range[0];
+  if (cmax) *cmax = range[1];
+  return 0;
+}
+
+}  // extern "C"

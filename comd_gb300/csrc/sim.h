@@ -108,6 +108,9 @@ struct comdgb_sim {
   // per-replica sums (device) and their host copy, W then K per replica
   double *vir_slot = nullptr, *vir_part = nullptr, *vir_out = nullptr;
   std::vector<double> vir_sums;
+  // centrosymmetry (centro.cu): one value per slot, then the range of the
+  // last replica asked for
+  double *centro = nullptr;
   // graphs
   cudaGraphExec_t step_exec = nullptr;
   cudaGraphExec_t force_exec = nullptr;

@@ -93,6 +93,7 @@ def _bind(lib):
     L.comdgb_batch_energies.argtypes = [C.c_void_p, D, D]
     L.comdgb_sim_virial.argtypes = [C.c_void_p, D, D, D]
     L.comdgb_sim_gather.argtypes = [C.c_void_p, C.c_int, D]
+    L.comdgb_sim_centrosymmetry.argtypes = [C.c_void_p, C.c_int, C.c_int, D, D, D]
     L.comdgb_sim_write_clsman.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int, C.c_char_p]
     L.comdgb_writeClsman.argtypes = [P_SIM, C.c_char_p]
     L.comdgb_gzASCIIWrite.argtypes = [P_SIM, C.c_char_p]
@@ -388,6 +389,15 @@ class DeviceSim:
         a = np.zeros((self._nboxes[r] * 64, 6))
         check(self.L.comdgb_sim_atom_stress(self.h, r, a.ctypes.data_as(C.POINTER(C.c_double))))
         return a
+
+    def centrosymmetry(self, r=0, approx=False):
+        """(per-slot centrosymmetry of replica r [nboxes * 64], min, max)"""
+        P = C.POINTER(C.c_double)
+        out = np.zeros(self._nboxes[r] * 64)
+        lo, hi = C.c_double(), C.c_double()
+        check(self.L.comdgb_sim_centrosymmetry(self.h, r, int(approx), out.ctypes.data_as(P),
+                                               C.byref(lo), C.byref(hi)))
+        return out, lo.value, hi.value
 
     # ---- clsman output ----
     def gather(self, r=0):

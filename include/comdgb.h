@@ -209,6 +209,19 @@ int comdgb_batch_virial(comdgb_sim *h, int r, double w[6], double k[6], double *
  * out[6 * (box * 64 + i) + c] for the replica's boxes (empty slots 0) */
 int comdgb_sim_atom_stress(comdgb_sim *h, int r, double *out);
 
+/* ---------------- centrosymmetry ---------------- */
+/* The visualiser's centrosymmetry parameter (src-viz/AtomVisualize.c:399-672)
+ * of every atom of replica r, from the 12 nearest candidates in the 27
+ * boxes around its own: the least sum of |r_a + r_b|^2 over the pairings of
+ * the 12 (approx = 0, the default build) or the greedy pairing
+ * (approx = 1, APPROX_CENTROSYM); 1000 for fewer than 12 candidates.
+ * out (optional): one double per slot of the replica's boxes (empty slots
+ * 0), the layout of the visualiser's sim->centro; *cmin / *cmax (optional):
+ * the range over the replica's atoms (minCentro, maxCentro before the
+ * visualiser clamps the latter to 100). */
+int comdgb_sim_centrosymmetry(comdgb_sim *h, int r, int approx, double *out, double *cmin,
+                              double *cmax);
+
 /* ---------------- host-side setup (reference setup routines) ---------------- */
 
 /* setEamPot / eamReadASCII (eam.c:102-109, 347-398): reads <dir>/<name>.{phi,rho,f,doc} */

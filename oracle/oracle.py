@@ -71,6 +71,7 @@ def _bind(lib):
     f.orc_virial.argtypes = [P_SIM, C.c_int, D, D, D]
     f.orc_strained.restype = P_SIM
     f.orc_strained.argtypes = [P_SIM, D]
+    f.orc_centro.argtypes = [P_SIM, C.c_int, D, D, D]
     f.orc_cheb_set.argtypes = [C.c_void_p, D, D, D]
     f.orc_eam_cheb_grad.argtypes = [P_SIM, D, D, D, D, D]
     f.orc_lj_grad.argtypes = [P_SIM, D, D, D, D, D]
@@ -145,6 +146,14 @@ class Oracle:
         if rc:
             raise RuntimeError(f"oracle virial failed: {rc}")
         return w, k, a
+
+    def centro(self, s, approx=False):
+        """(per-slot centrosymmetry [nslots], min, max)"""
+        P = C.POINTER(C.c_double)
+        out = np.zeros(s.contents.nboxes * 64)
+        lo, hi = C.c_double(), C.c_double()
+        self.lib.orc_centro(s, int(approx), out.ctypes.data_as(P), C.byref(lo), C.byref(hi))
+        return out, lo.value, hi.value
 
     def strained(self, s, scale):
         """copy of s under x_a -> scale[a] x_a (bounds and positions)"""

@@ -1,0 +1,167 @@
+"""Centrosymmetry parameter (comdgb_sim_centrosymmetry) against the oracle's
+restatement of the visualiser's computeCentrosymmetry
+(src-viz/AtomVisualize.c:399-672; the visualiser itself cannot be built
+here: it needs the VTK and OpenGL headers).  The restatement is checked by
+known answers of the physics: ~0 on a perfect lattice (the periodic offsets
+the visualiser rounds to float leave ~1e-12), and for the 12 neighbours of a
+vacancy the least pairing of its 11 remaining nearest neighbours and one
+second-shell atom at distance a, which is a^2/2, a^2 or 3a^2/2 depending on
+which second-shell atom is among the 12 (found by enumerating the six).
+The GPU values must equal the oracle's bit for bit."""
+import os
+
+import numpy as np
+import pytest
+
+import comd_gb300 as cg
+from comd_gb300.abi import occupied_mask, slot_views
+from helpers import Case
+
+LAT = 3.615
+
+
+def perfect(n=6, bf=1.0):
+    pot = cg.eam_potential("cu")
+    return cg.fcc(n, n, n, pot.ptr.contents.lat, 1.0, bf, pot), pot
+
+
+def remove_atom(s, atom_id):
+    """take atom `atom_id` out of its box (the box's last atom takes its
+    slot, as the reference's moveAtom does); returns its world position"""
+    v = slot_views(s)
+    occ = occupied_mask(s)
+    slot = int(np.nonzero((v["id"] == atom_id) & occ)[0][0])
+    b = slot // 64
+    pos = v["dcenter"][b] + v["r"][slot]
+    last = b * 64 + v["natoms"][b] - 1
+    for f in ("id", "iType", "mass", "r", "p"):
+        v[f][slot] = v[f][last]
+    v["natoms"][b] -= 1
+    s.contents.ntot -= 1
+    return pos
+
+
+def world(s):
+    v = slot_views(s)
+    return np.repeat(v["dcenter"], 64, axis=0) + v["r"]
+
+
+# ---------------------------------------------------------------- CPU ----
+
+def test_oracle_perfect_lattice_is_centrosymmetric(oracle):
+    s, _pot = perfect()
+    try:
+        c, lo, hi = oracle.centro(s)
+        m = occupied_mask(s)
+        assert np.all(c[m] < 1e-10)
+        assert lo == c[m].min() and hi == c[m].max()
+        ca, _, _ = oracle.centro(s, approx=True)
+        assert np.all(ca[m] < 1e-10)
+    finally:
+        cg.free_host(s)
+
+
+def test_oracle_vacancy_neighbours(oracle):
+    s, _pot = perfect()
+    try:
+        hole = remove_atom(s, 100)
+        c, _, _ = oracle.centro(s)
+        m = occupied_mask(s)
+        b = np.array(list(s.contents.bounds))
+        d = world(s) - hole
+        d -= b * np.round(d / b)
+        dist = np.sqrt((d ** 2).sum(axis=1))
+        nn = m & (np.abs(dist - LAT / np.sqrt(2)) < 1e-6)
+        assert nn.sum() == 12
+        allowed = np.array([0.5, 1.0, 1.5]) * LAT ** 2
+        for x in c[nn]:
+            assert np.min(np.abs(allowed - x)) < 1e-4, x
+        far = m & (dist > 2.0 * LAT)
+        assert np.all(c[far] < 1e-10)
+    finally:
+        cg.free_host(s)
+
+
+def test_oracle_greedy_bounds_the_optimum(oracle):
+    """the greedy pairing is a pairing, so never below the least one"""
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(6, 6, 6), amp=0.05, temp=600.0)
+    try:
+        ce, _, _ = oracle.centro(c.s)
+        ca, _, _ = oracle.centro(c.s, approx=True)
+        m = occupied_mask(c.s)
+        assert np.all(ca[m] >= ce[m] * (1 - 1e-5))
+        assert ce[m].max() > 0.01
+    finally:
+        c.close()
+
+
+# ---------------------------------------------------------------- GPU ----
+
+def gpu_centro(s, approx=False):
+    d = cg.DeviceSim(s, cg.opts(cg.POT_EAM_TABLE, cg.PREC_FP64))
+    try:
+        return d.centrosymmetry(0, approx)
+    finally:
+        d.close()
+
+
+def cases(oracle):
+    """[(name, host simulation)] for the comparisons, and the Case objects
+    that own some of them"""
+    out = []
+    s, _ = perfect()
+    out.append(("perfect", s))
+    s, _ = perfect()
+    remove_atom(s, 100)
+    remove_atom(s, 101)
+    out.append(("vacancies", s))
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(6, 6, 6), amp=0.05, temp=600.0)
+    out.append(("thermal", c.s))
+    c2 = Case(oracle, cg.POT_EAM_TABLE, n=(4, 4, 4), amp=0.05, temp=600.0)  # 2 boxes per axis
+    out.append(("small grid", c2.s))
+    c3 = Case(oracle, cg.POT_EAM_TABLE, n=(6, 7, 5), bf=1.5, amp=0.08, temp=1200.0)
+    out.append(("bf 1.5", c3.s))
+    ag = cg.read_clsman(os.path.join(cg.DATA_DIR, "8k.inp.gz"), cg.eam_potential("ag"), 1.0, -1)
+    out.append(("Ag 8k", ag))
+    return out, [c, c2, c3]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("approx", [False, True])
+def test_gpu_centro_matches_oracle_bitwise(oracle, approx):
+    sims, keep = cases(oracle)
+    try:
+        for name, s in sims:
+            co, lo, hi = oracle.centro(s, approx)
+            cgpu, glo, ghi = gpu_centro(s, approx)
+            m = occupied_mask(s)
+            assert np.array_equal(cgpu[m], co[m]), name
+            assert np.all(cgpu[~m] == 0), name
+            assert (glo, ghi) == (lo, hi), name
+    finally:
+        for name, s in sims:
+            if name in ("perfect", "vacancies", "Ag 8k"):
+                cg.free_host(s)
+        for c in keep:
+            c.close()
+
+
+@pytest.mark.gpu
+def test_gpu_batch_centro_equals_single(oracle):
+    from test_batch import make_replicas
+    pot = cg.eam_potential("cu")
+    bs = make_replicas(pot)
+    try:
+        b = cg.Batch(bs, cg.opts(cg.POT_EAM_TABLE, cg.PREC_FP64))
+        try:
+            got = [b.centrosymmetry(r) for r in range(b.n)]
+        finally:
+            b.close()
+        for r, s in enumerate(bs):
+            co, lo, hi = oracle.centro(s)
+            m = occupied_mask(s)
+            assert np.array_equal(got[r][0][m], co[m]), r
+            assert (got[r][1], got[r][2]) == (lo, hi), r
+    finally:
+        for s in bs:
+            cg.free_host(s)
