@@ -109,9 +109,9 @@ def cases(oracle):
     """[(name, host simulation)] for the comparisons, and the Case objects
     that own some of them"""
     out = []
-    s, _ = perfect()
+    s, p1 = perfect()
     out.append(("perfect", s))
-    s, _ = perfect()
+    s, p2 = perfect()
     remove_atom(s, 100)
     remove_atom(s, 101)
     out.append(("vacancies", s))
@@ -119,11 +119,12 @@ def cases(oracle):
     out.append(("thermal", c.s))
     c2 = Case(oracle, cg.POT_EAM_TABLE, n=(4, 4, 4), amp=0.05, temp=600.0)  # 2 boxes per axis
     out.append(("small grid", c2.s))
-    c3 = Case(oracle, cg.POT_EAM_TABLE, n=(6, 7, 5), bf=1.5, amp=0.08, temp=1200.0)
-    out.append(("bf 1.5", c3.s))
-    ag = cg.read_clsman(os.path.join(cg.DATA_DIR, "8k.inp.gz"), cg.eam_potential("ag"), 1.0, -1)
+    c3 = Case(oracle, cg.POT_EAM_TABLE, n=(6, 7, 6), bf=1.2, amp=0.08, temp=1200.0)
+    out.append(("bf 1.2", c3.s))
+    ag_pot = cg.eam_potential("ag")
+    ag = cg.read_clsman(os.path.join(cg.DATA_DIR, "8k.inp.gz"), ag_pot, 1.0, -1)
     out.append(("Ag 8k", ag))
-    return out, [c, c2, c3]
+    return out, [c, c2, c3, ag_pot, p1, p2]
 
 
 @pytest.mark.gpu
@@ -143,7 +144,8 @@ def test_gpu_centro_matches_oracle_bitwise(oracle, approx):
             if name in ("perfect", "vacancies", "Ag 8k"):
                 cg.free_host(s)
         for c in keep:
-            c.close()
+            if isinstance(c, Case):
+                c.close()
 
 
 @pytest.mark.gpu

@@ -32,10 +32,15 @@ def digests(binary_path, text_gz_path):
     return sha(open(binary_path, "rb").read()), sha(gzip.open(text_gz_path).read())
 
 
+AG = {}
+
+
 def ag8k_host():
     """the Ag 8k file as read (its atoms are already in their boxes, so the
-    reBoxAll of initSimFromCmdLine moves nothing)"""
-    return cg.read_clsman(os.path.join(cg.DATA_DIR, "8k.inp.gz"), cg.eam_potential("ag"), 1.0, -1)
+    reBoxAll of initSimFromCmdLine moves nothing); the potential is kept for
+    the module's lifetime (the simulation points at it)"""
+    pot = AG.setdefault("pot", cg.eam_potential("ag"))
+    return cg.read_clsman(os.path.join(cg.DATA_DIR, "8k.inp.gz"), pot, 1.0, -1)
 
 
 def seeded_cu_host(oracle):
