@@ -2,30 +2,31 @@
 // (AtomVisualize::computeCentrosymmetry, src-viz/AtomVisualize.c:399-672), a
 // headless kernel over the link cells.
 //
-// One CTA per box, one thread per atom of the box.  The neighbour scan
-// visits the atom's own box (box-relative differences), then the 26 adjacent
-// boxes in x-outer, z-inner order, wrapped once per axis with the periodic
-// offset rounded to float (AtomVisualize.c:458-505), and keeps up to 12
-// candidates: the next free entry while fewer than 12 are held, then the
-// first entry of largest r^2 is replaced unless the candidate's r^2 is
+// One thread per atom of the compacted atom list (64 per CTA).  The
+// neighbour scan visits the atom's own box (box-relative differences), then
+// the 26 adjacent boxes in x-outer, z-inner order, wrapped once per axis with
+// the periodic offset rounded to float (AtomVisualize.c:458-505), and keeps
+// up to 12 candidates: the next free entry while fewer than 12 are held, then
+// the first entry of largest r^2 is replaced unless the candidate's r^2 is
 // larger.  All of it in FP64 with the reference's operation order (this
 // translation unit is built without FMA contraction); r^2 values are
 // compared as the integer images of non-negative doubles.
 //
 // The parameter is the minimum over the 10395 pairings of the 12 vectors of
 // the sum of |r_a + r_b|^2, accumulated in a float over the pairs in the
-// order of their lower index (testCentro, :560-664).  Each thread first
-// scans every pairing with the 66 pair terms rounded to FP32 and plain FP32
-// sums, keeping the least; a second scan recomputes exactly (double terms,
-// each partial sum rounded to float as testCentro does) only the pairings
-// whose FP32 sum lies within 4e-6 of that least.  Both sums round at most
-// six float additions of non-negative terms, so each is within 12 units of
-// 2^-24 of the exact sum; a pairing outside the window cannot be the
-// reference's minimum, and the result is the reference's value bit for bit.
-// The pairings are a constant table (6 pair indices each, lower index first).
+// order of their lower index (testCentro, :560-664).  The 66 pair terms are
+// rounded to FP32 once; a depth-first search over the pairings (the lowest
+// unpaired vector paired first, as the visualiser's loops pair them) finds
+// the least plain-FP32 sum, cutting every branch whose partial sum already
+// reaches the best complete one (partial sums of non-negative terms never
+// decrease, so the cut loses nothing; the greedy pairing gives the first
+// bound).  A second search visits the pairings whose FP32 sum lies within
+// 4e-6 of that least and sums them exactly as testCentro does (double terms,
+// each partial sum rounded to float).  Both sums round at most six float
+// additions of non-negative terms, so each is within 12 units of 2^-24 of
+// the exact sum: a pairing outside the window cannot be the reference's
+// minimum, and the result is the reference's value bit for bit.
 // APPROX_CENTROSYM's greedy pairing (:528-557) is the `approx` variant.
-#include <vector>
-
 #include "sim.h"
 
 using namespace cg;
@@ -34,52 +35,10 @@ using namespace cgapi;
 namespace {
 
 constexpr int NPAIR = 66;
-constexpr int NMATCH = 10395;  // 11 * 9 * 7 * 5 * 3
-constexpr int CT = CG_MAXATOMS;  // threads per CTA: one per slot
+constexpr int CT = 64;  // threads (atoms) per CTA
 
-__constant__ uint8_t c_match[NMATCH * 6];  // pair indices, lower index first
-__constant__ uint8_t c_pa[NPAIR], c_pb[NPAIR];
-
-// pairings of 12 entries, the lowest unpaired entry paired first
-void enumerate(std::vector<uint8_t> &out, int *pair_of, int used, std::vector<int> &cur) {
-  int n = 0;
-  while (n < 12 && (used >> n & 1)) n++;
-  if (n == 12) {
-    for (int k : cur) out.push_back((uint8_t)k);
-    return;
-  }
-  for (int p = n + 1; p < 12; p++) {
-    if (used >> p & 1) continue;
-    cur.push_back(pair_of[n * 12 + p]);
-    enumerate(out, pair_of, used | 1 << n | 1 << p, cur);
-    cur.pop_back();
-  }
-}
-
-int upload_tables(int device) {
-  static bool done[64] = {};
-  if (device >= 0 && device < 64 && done[device]) return 0;
-  int pair_of[144];
-  uint8_t pa[NPAIR], pb[NPAIR];
-  int k = 0;
-  for (int a = 0; a < 12; a++)
-    for (int b = a + 1; b < 12; b++) {
-      pair_of[a * 12 + b] = k;
-      pa[k] = (uint8_t)a;
-      pb[k] = (uint8_t)b;
-      k++;
-    }
-  std::vector<uint8_t> m;
-  std::vector<int> cur;
-  m.reserve(NMATCH * 6);
-  enumerate(m, pair_of, 0, cur);
-  if ((int)m.size() != NMATCH * 6) return set_err(COMDGB_ERR_ARG, "pairing table size");
-  CK(cudaMemcpyToSymbol(c_match, m.data(), m.size()));
-  CK(cudaMemcpyToSymbol(c_pa, pa, sizeof pa));
-  CK(cudaMemcpyToSymbol(c_pb, pb, sizeof pb));
-  if (device >= 0 && device < 64) done[device] = true;
-  return 0;
-}
+// index of the pair a < b among the 66, row by row
+__device__ __forceinline__ int pidx(int a, int b) { return 11 * a - (a * (a - 1)) / 2 + b - a - 1; }
 
 __device__ __forceinline__ long long key(double rsq) { return __double_as_longlong(rsq); }
 
@@ -91,24 +50,71 @@ __device__ __forceinline__ double pair_term(const double (*v)[3][CT], int a, int
   return __dadd_rn(__dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y)), __dmul_rn(z, z));
 }
 
+// Depth-first over the pairings: the lowest unpaired entry is paired next,
+// with its partners in index order.  A branch whose partial FP32 sum reaches
+// `bound` (STRICT) or exceeds it is cut.  leaf(sum, nn, pp) gets every
+// pairing kept; its pairs are (nn[l], pp[l]), l = 0..5, lower index first.
+template <bool STRICT, class Leaf>
+__device__ __forceinline__ void pairing_dfs(const float (*p)[CT], int t, const float &bound,
+                                            Leaf &&leaf) {
+  int nn[6], pp[6];
+  float acc[6];
+  int used = 1, lvl = 0;
+  nn[0] = 0;
+  pp[0] = 0;
+  acc[0] = 0.0f;
+  while (true) {
+    int q = pp[lvl] + 1;
+    while (q < 12 && (used >> q & 1)) q++;
+    if (q >= 12) {  // this level's partners are done
+      used &= ~(1 << nn[lvl]);
+      if (lvl == 0) break;
+      lvl--;
+      used &= ~(1 << pp[lvl]);
+      continue;
+    }
+    pp[lvl] = q;
+    const float a = __fadd_rn(acc[lvl], p[pidx(nn[lvl], q)][t]);
+    if (STRICT ? a >= bound : a > bound) continue;
+    if (lvl == 5) {
+      leaf(a, nn, pp);
+      continue;
+    }
+    used |= 1 << q;
+    lvl++;
+    acc[lvl] = a;
+    const int n = __ffs(~used) - 1;
+    nn[lvl] = n;
+    pp[lvl] = n;
+    used |= 1 << n;
+  }
+}
+
 __global__ void __launch_bounds__(CT) centro_kernel(Geom g, Slots s, const double *dcenter,
-                                                    int approx, double *out) {
-  __shared__ double v[12][3][CT];      // held vectors
-  __shared__ long long vk[12][CT];     // their r^2 (integer images)
-  __shared__ float p32[NPAIR][CT];     // pair terms rounded to FP32
-  const int b = blockIdx.x, t = threadIdx.x;
+                                                    const int *atom_slot, int ntot, int approx,
+                                                    double *out) {
+  __shared__ double v[12][3][CT];  // held vectors
+  // r^2 of the held vectors (integer images) during the scan, then the
+  // pair terms rounded to FP32
+  __shared__ __align__(8) float scratch[NPAIR][CT];
+  long long (*vk)[CT] = reinterpret_cast<long long (*)[CT]>(&scratch[0][0]);
+  float (*p32)[CT] = scratch;
+  const int t = threadIdx.x;
+  const int a = blockIdx.x * CT + t;
+  if (a >= ntot) return;
+  const int io = atom_slot[a];
+  const int b = io >> 6, i = io & 63;
   const int ni = s.natoms[b];
-  if (t >= ni) return;
   const RepGeo &R = rep_of(g, b);
   const int nx = R.nbx[0], ny = R.nbx[1], nz = R.nbx[2];
   const int lb = b - R.box0;
   const int bz = lb / (nx * ny), by = (lb - bz * nx * ny) / nx, bx = lb - bz * nx * ny - by * nx;
-  const int io = b * CG_MAXATOMS + t;
   const d4 ri = s.r[io];
   int nb = 0, kmax = 0;
   long long rmax = 0;
   auto offer = [&](double dx, double dy, double dz) {
-    const double rsq = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    const double rsq =
+        __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     const long long kk = key(rsq);
     int i1;
     if (nb < 12) {
@@ -133,7 +139,7 @@ __global__ void __launch_bounds__(CT) centro_kernel(Geom g, Slots s, const doubl
   };
   // own box: box-relative differences
   for (int j = 0; j < ni; j++) {
-    if (j == t) continue;
+    if (j == i) continue;
     const d4 rj = s.r[b * CG_MAXATOMS + j];
     offer(__dsub_rn(rj.x, ri.x), __dsub_rn(rj.y, ri.y), __dsub_rn(rj.z, ri.z));
   }
@@ -167,15 +173,15 @@ __global__ void __launch_bounds__(CT) centro_kernel(Geom g, Slots s, const doubl
   if (nb >= 12) {
     if (approx) {
       // greedy pairing; a vector with r^2 = 0 counts as paired
-      bool paired[12];
-      for (int q = 0; q < 12; q++) paired[q] = !(vk[q][t] > 0);
+      int paired = 0;
+      for (int q = 0; q < 12; q++) paired |= (vk[q][t] > 0 ? 0 : 1) << q;
       c = 0.0;
       for (int j = 0; j < 11; j++) {
-        if (paired[j]) continue;
+        if (paired >> j & 1) continue;
         double summin = 1000.0;
         int kmin = -1;
         for (int k = j + 1; k < 12; k++) {
-          if (paired[k]) continue;
+          if (paired >> k & 1) continue;
           const double sum = pair_term(v, j, k, t);
           if (sum < summin) {
             kmin = k;
@@ -183,33 +189,35 @@ __global__ void __launch_bounds__(CT) centro_kernel(Geom g, Slots s, const doubl
           }
         }
         c = __dadd_rn(c, summin);
-        paired[j] = true;
-        if (kmin >= 0) paired[kmin] = true;
+        paired |= 1 << j;
+        if (kmin >= 0) paired |= 1 << kmin;
       }
     } else {
-      for (int k = 0; k < NPAIR; k++)
-        p32[k][t] = __double2float_rn(pair_term(v, c_pa[k], c_pb[k], t));
-      float best = 3.0e38f;
-      for (int m = 0; m < NMATCH; m++) {
-        const uint8_t *q = c_match + 6 * m;
-        float acc = p32[q[0]][t];
-#pragma unroll
-        for (int u = 1; u < 6; u++) acc = __fadd_rn(acc, p32[q[u]][t]);
-        best = fminf(best, acc);
+      for (int x = 0, k = 0; x < 12; x++)
+        for (int y = x + 1; y < 12; y++, k++) p32[k][t] = __double2float_rn(pair_term(v, x, y, t));
+      // first bound: the greedy pairing's FP32 sum (a complete pairing)
+      float best = 0.0f;
+      for (int used = 0, step = 0; step < 6; step++) {
+        const int n = __ffs(~used) - 1;
+        used |= 1 << n;
+        int qb = -1;
+        float pb = 0.0f;
+        for (int q = n + 1; q < 12; q++)
+          if (!(used >> q & 1) && (qb < 0 || p32[pidx(n, q)][t] < pb)) {
+            qb = q;
+            pb = p32[pidx(n, q)][t];
+          }
+        used |= 1 << qb;
+        best = __fadd_rn(best, pb);
       }
+      pairing_dfs<true>(p32, t, best, [&](float sum, const int *, const int *) { best = sum; });
       const float window = __fadd_rn(best, __fmul_rn(best, 4e-6f)) + 1e-37f;
-      for (int m = 0; m < NMATCH; m++) {
-        const uint8_t *q = c_match + 6 * m;
-        float acc = p32[q[0]][t];
-#pragma unroll
-        for (int u = 1; u < 6; u++) acc = __fadd_rn(acc, p32[q[u]][t]);
-        if (acc > window) continue;
+      pairing_dfs<false>(p32, t, window, [&](float, const int *nn, const int *pp) {
         float e = 0.0f;  // testCentro
-#pragma unroll
-        for (int u = 0; u < 6; u++)
-          e = __double2float_rn(__dadd_rn((double)e, pair_term(v, c_pa[q[u]], c_pb[q[u]], t)));
+        for (int l = 0; l < 6; l++)
+          e = __double2float_rn(__dadd_rn((double)e, pair_term(v, nn[l], pp[l], t)));
         if ((double)e < c) c = (double)e;
-      }
+      });
     }
   }
   out[io] = c;
@@ -252,8 +260,6 @@ int comdgb_sim_centrosymmetry(comdgb_sim *h, int r, int approx, double *out, dou
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   if (r < 0 || r >= h->nrep) return set_err(COMDGB_ERR_ARG, "replica %d of %d", r, h->nrep);
   CK(cudaSetDevice(h->device));
-  int rc = upload_tables(h->device);
-  if (rc) return rc;
   int err = 0;
   if (!h->centro) {
     h->centro = track(h, dalloc<double>((size_t)h->nslots + 2, &err));
@@ -261,7 +267,11 @@ int comdgb_sim_centrosymmetry(comdgb_sim *h, int r, int approx, double *out, dou
   }
   cudaStream_t st = h->stream;
   CK(cudaMemsetAsync(h->centro, 0, sizeof(double) * (size_t)h->nslots, st));  // empty slots 0
-  centro_kernel<<<h->g.nboxes, CT, 0, st>>>(h->g, h->s, h->dcenter, approx, h->centro);
+  // the atom list of the current layout
+  launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart, st);
+  if (h->ntot > 0)
+    centro_kernel<<<(h->ntot + CT - 1) / CT, CT, 0, st>>>(h->g, h->s, h->dcenter, h->atom_slot,
+                                                           h->ntot, approx, h->centro);
   centro_range_kernel<<<1, 256, 0, st>>>(h->g, h->s.natoms, h->centro, r,
                                          h->centro + h->nslots);
   CK(cudaGetLastError());
