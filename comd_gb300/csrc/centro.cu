@@ -93,12 +93,13 @@ __device__ __forceinline__ void pairing_dfs(const float (*p)[CT], int t, const f
 __global__ void __launch_bounds__(CT) centro_kernel(Geom g, Slots s, const double *dcenter,
                                                     const int *atom_slot, int ntot, int approx,
                                                     double *out) {
-  __shared__ double v[12][3][CT];  // held vectors
-  // r^2 of the held vectors (integer images) during the scan, then the
-  // pair terms rounded to FP32
-  __shared__ __align__(8) float scratch[NPAIR][CT];
-  long long (*vk)[CT] = reinterpret_cast<long long (*)[CT]>(&scratch[0][0]);
-  float (*p32)[CT] = scratch;
+  // per thread (column t): held vectors, their r^2 (integer images) and the
+  // pair terms rounded to FP32.  Warps run the scan and the pairing phases
+  // at different times with no barrier between them, so no array is shared
+  // between the phases.
+  __shared__ double v[12][3][CT];
+  __shared__ long long vk[12][CT];
+  __shared__ float p32[NPAIR][CT];
   const int t = threadIdx.x;
   const int a = blockIdx.x * CT + t;
   if (a >= ntot) return;
