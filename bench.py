@@ -694,6 +694,98 @@ def adjoint_arm(args):
     return 0
 
 
+def analysis_arm(args):
+    """The analyses beside the step, on the bundled 262,144-atom Ag structure
+    (the reference's data/262k.inp.gz, EAM Ag Chebyshev, box factor 1):
+    reading the clsman file (host parse + device binning), the virial tensor
+    (force call + virial pass, mixed precision), the centrosymmetry
+    parameter (exact pairing minimum and the greedy variant), the id-order
+    gather and the three clsman writers.  Each op is timed as its C ABI call
+    (wall clock, the call synchronises), median of K calls after one warm-up.
+    CPU baseline: the oracle's restatements of the virial and the exact
+    centrosymmetry on the 8,192-atom Ag file, one core."""
+    import gzip
+    import tempfile
+    import comd_gb300 as cg
+    pot = cg.eam_potential("ag")
+    path = os.path.join(cg.DATA_DIR, "262k.inp.gz")
+    k = max(3, min(args.steps, 10))
+    ops = {}
+
+    def timed(name, fn, atoms):
+        fn()
+        ts = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            fn()
+            ts.append(time.perf_counter() - t0)
+        ms = statistics.median(ts) * 1e3
+        ops[name] = {"ms": ms, "atoms_per_s": atoms / (ms * 1e-3)}
+
+    sims = []
+
+    def read():
+        s = cg.read_clsman(path, pot, 1.0, 0)
+        sims.append(s)
+    timed("read_clsman_gz_device_binning", read, 262144)
+    s = sims.pop()
+    for q in sims:
+        cg.free_host(q)
+    assert cg.load().comdgb_rebox_host(s, 1, 0) == 0
+    n = s.contents.ntot
+    d = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED))
+    tmp = tempfile.mkdtemp(prefix="comdgb_")
+    try:
+        timed("force_mixed", lambda: d.force(), n)
+        timed("virial_mixed", lambda: d.virial(), n)
+        timed("centrosymmetry_exact", lambda: d.centrosymmetry(), n)
+        timed("centrosymmetry_greedy", lambda: d.centrosymmetry(0, True), n)
+        timed("gather_by_id", lambda: d.gather(), n)
+        timed("write_binary", lambda: d.write_clsman(os.path.join(tmp, "a.bin")), n)
+        timed("write_text_gz", lambda: d.write_clsman(os.path.join(tmp, "a.txt.gz"),
+                                                      cg.CLSMAN_TEXT_GZ, "bench\n"), n)
+        timed("write_text", lambda: d.write_clsman(os.path.join(tmp, "a.txt"),
+                                                   cg.CLSMAN_TEXT, "bench\n"), n)
+        for f in ("a.bin", "a.txt.gz", "a.txt"):
+            ops["write_" + f.replace(".", "_") + "_bytes"] = os.path.getsize(os.path.join(tmp, f))
+            os.remove(os.path.join(tmp, f))
+    finally:
+        d.close()
+        cg.free_host(s)
+        os.rmdir(tmp)
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        O = oracle.Oracle()
+        with tempfile.NamedTemporaryFile(suffix=".inp") as f:
+            f.write(gzip.open(os.path.join(cg.DATA_DIR, "8k.inp.gz")).read())
+            f.flush()
+            op = O.eam(os.path.join(ROOT, "comd_gb300", "pots"), "ag")
+            so = O.read_clsman(f.name, op, 1.0)
+        so.contents.ch_pot = O.cheby(op, 32)
+        O.rebox(so)
+        O.force(so, oracle.KIND_EAM_CHEBY)
+        t0 = time.perf_counter()
+        O.virial(so, oracle.KIND_EAM_CHEBY, atoms=True)
+        t_vir = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.centro(so)
+        t_cen = time.perf_counter() - t0
+        na = so.contents.ntot
+        O.free(so)
+        cpu = {"value": na / t_cen, "unit": "atoms/s", "cores": 1, "kind": "port",
+               "sample": f"oracle centrosymmetry (exact) of the {na}-atom Ag file, {t_cen:.2f} s",
+               "virial_atoms_per_s": na / t_vir}
+    line = {"metric": "analysis: centrosymmetry (exact) throughput, 262,144-atom Ag structure, "
+                      "1 GB300",
+            "value": ops["centrosymmetry_exact"]["atoms_per_s"], "unit": "atoms/s",
+            "higher_is_better": True, "dtype": "f64", "data": "bundled Ag structure (262k)",
+            "config": {"workload": "ag262k_clsman_analysis"}, "ops": ops, "cpu_baseline": cpu,
+            "vs_baseline": None}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -709,9 +801,11 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="step", choices=["step", "batch", "adjoint"],
+    ap.add_argument("--workload", default="step",
+                    choices=["step", "batch", "adjoint", "analysis"],
                     help="step: the headline 4M-atom step; batch: 64 replicas (C4); "
-                         "adjoint: gradients (C5)")
+                         "adjoint: gradients (C5); analysis: virial, centrosymmetry and "
+                         "clsman IO on the 262k Ag structure")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -724,6 +818,8 @@ def main():
         return batch_arm(args)
     if args.workload == "adjoint":
         return adjoint_arm(args)
+    if args.workload == "analysis":
+        return analysis_arm(args)
     return gpu_arm(args)
 
 
