@@ -315,12 +315,22 @@ static char *read_all(const char *path, int *st) {
   return buf;
 }
 
-/* next line of the buffer (as gzgets: up to and including '\n') */
-static const char *next_line(const char **cur) {
-  const char *l = *cur;
+/* next line of the buffer, as gzgets reads it: *len = its length with the
+ * '\n'.  The line is cut off with a NUL in place of the '\n' (the buffer is
+ * ours), so that sscanf sees one line and not the rest of the file: glibc's
+ * sscanf measures its whole input string on every call. */
+static char *next_line(char **cur, size_t *len) {
+  char *l = *cur;
   if (!*l) return NULL;
-  const char *e = strchr(l, '\n');
-  *cur = e ? e + 1 : l + strlen(l);
+  char *e = strchr(l, '\n');
+  if (e) {
+    *e = 0;
+    *cur = e + 1;
+    if (len) *len = (size_t)(e - l) + 1;
+  } else {
+    *cur = l + strlen(l);
+    if (len) *len = (size_t)(*cur - l);
+  }
   return l;
 }
 
@@ -342,9 +352,10 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   }
   char *buf = read_all(path, &st);
   if (!buf) goto done;
-  const char *cur = buf, *l;
+  char *cur = buf, *l;
+  size_t llen = 0;
   int natoms = 0, nmove = 0;
-  if (!(l = next_line(&cur)) || sscanf(l, "%d%d", &natoms, &nmove) < 1 || natoms < 0) {
+  if (!(l = next_line(&cur, NULL)) || sscanf(l, "%d%d", &natoms, &nmove) < 1 || natoms < 0) {
     st = COMDGB_ERR_IO;
     goto done;
   }
@@ -357,11 +368,13 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   s->bf = bf;
   s->defgrad = 0.0; /* blankSimulation's; allocDomains then takes strain 1 */
   s->comment = (char *)zalloc(1024);
-  if ((l = next_line(&cur)) && s->comment) {
-    size_t n = (size_t)(cur - l);
-    memcpy(s->comment, l, n < 1023 ? n : 1023);
+  if ((l = next_line(&cur, &llen)) && s->comment) {
+    /* the comment as the reference keeps it: the line with its '\n' */
+    size_t n = llen < 1023 ? llen : 1023;
+    memcpy(s->comment, l, n);
+    if (n && l[n - 1] == 0) s->comment[n - 1] = '\n';
   }
-  if (!(l = next_line(&cur)) ||
+  if (!(l = next_line(&cur, NULL)) ||
       sscanf(l, "%lg %lg %lg", &s->bounds[0], &s->bounds[1], &s->bounds[2]) != 3) {
     st = COMDGB_ERR_IO;
     goto done;
@@ -380,7 +393,7 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   for (int i = 0; i < natoms; i++) {
     int itype = 0;
     double *x = xyz + 3 * (size_t)i, *p = pxyz + 3 * (size_t)i;
-    if (!(l = next_line(&cur)) ||
+    if (!(l = next_line(&cur, NULL)) ||
         sscanf(l, "%lg %lg %lg %d %lg %lg %lg", &x[0], &x[1], &x[2], &itype, &p[0], &p[1],
                &p[2]) != 7) {
       st = COMDGB_ERR_IO;
