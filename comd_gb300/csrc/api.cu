@@ -998,9 +998,9 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
       h->pl.vcap = vcap;
       h->pl.vlist = track(h, dalloc<int>((size_t)h->ntot * vcap + 4, &err));
       h->pl.vcount = track(h, dalloc<int>(n1, &err));
-      h->pl.rref = track(h, dalloc<float4>(n1, &err));
+      h->pl.rref = track(h, dalloc<d4>(n1, &err));
       const double hs = 0.5 * h->skin - 2e-4;
-      h->pl.half_skin2 = (float)(hs * hs);
+      h->pl.half_skin2 = hs * hs;
     }
     h->w.pl = h->pl;
     if (h->fo.list) {

@@ -156,8 +156,8 @@ struct Persist {
   int *vcount;       // [ntot] true neighbour count
   int vcap;
   int *slot_of;      // [ntot] current slot of atom id (kept by the rebin)
-  float4 *rref;      // [ntot] position (world frame, FP32) at the last build
-  float half_skin2;  // (skin/2 - 2e-4 A)^2: FP32 world coordinates err by < 1e-4 A
+  d4 *rref;          // [ntot] position (world frame, FP64) at the last build
+  double half_skin2; // (skin/2 - 2e-4 A)^2
 };
 
 // Force order (mixed precision with persistent lists): each list build
@@ -200,33 +200,41 @@ struct SlotMap {
 // world-frame position in FP32 from the FP32 box-centred position (mixed
 // precision) or from the FP64 box-relative one; good to ~1e-4 A, used only
 // for the skin test
-__device__ __forceinline__ float4 world32(const Geom &g, int b, const float4 *pos32, long slot,
-                                          const d4 &r) {
+// FP64 world position of the atom in slot r of box b: the box corner plus
+// the box-relative position
+__device__ __forceinline__ d4 world64(const Geom &g, int b, const d4 &r) {
   const RepGeo &R = rep_of(g, b);
   int ix[3];
   box_ixyz_tab(g, b, ix);
-  if (pos32) {
-    const float4 p = pos32[slot];
-    return make_float4(fmaf((float)ix[0] + 0.5f, (float)R.boxsize[0], p.x),
-                       fmaf((float)ix[1] + 0.5f, (float)R.boxsize[1], p.y),
-                       fmaf((float)ix[2] + 0.5f, (float)R.boxsize[2], p.z), 0.f);
-  }
-  return make_float4((float)(R.boxsize[0] * (double)ix[0] + r.x),
-                     (float)(R.boxsize[1] * (double)ix[1] + r.y),
-                     (float)(R.boxsize[2] * (double)ix[2] + r.z), 0.f);
+  d4 w;
+  w.x = R.boxsize[0] * (double)ix[0] + r.x;
+  w.y = R.boxsize[1] * (double)ix[1] + r.y;
+  w.z = R.boxsize[2] * (double)ix[2] + r.z;
+  w.w = 0.0;
+  return w;
 }
 
-// squared minimum-image distance between two FP32 world positions
-__device__ __forceinline__ float disp2(const RepGeo &R, float4 a, float4 b) {
-  float d[3] = {a.x - b.x, a.y - b.y, a.z - b.z};
-  float s = 0.f;
+// Persistent lists of an atom at box-relative r in box b are stale when it
+// moved more than skin/2 since the build (FP64 minimum-image distance to
+// its build position ref), when that distance is not a number, or when the
+// atom sits more than a box width outside its box -- a state only a runaway
+// step makes, in which a distance measured through one periodic image says
+// nothing.
+__device__ __forceinline__ bool persist_stale(const Geom &g, int b, const d4 &r, const d4 &ref,
+                                              double half_skin2) {
+  const RepGeo &R = rep_of(g, b);
+  const double rv[3] = {r.x, r.y, r.z};
+  for (int k = 0; k < 3; k++)
+    if (!(rv[k] >= -R.boxsize[k] && rv[k] <= 2.0 * R.boxsize[k])) return true;
+  const d4 w = world64(g, b, r);
+  double d[3] = {w.x - ref.x, w.y - ref.y, w.z - ref.z}, s2 = 0.0;
   for (int k = 0; k < 3; k++) {
-    const float L = (float)R.bounds[k];
-    if (d[k] > 0.5f * L) d[k] -= L;
-    else if (d[k] < -0.5f * L) d[k] += L;
-    s = fmaf(d[k], d[k], s);
+    const double L = R.bounds[k];
+    if (d[k] > 0.5 * L) d[k] -= L;
+    else if (d[k] < -0.5 * L) d[k] += L;
+    s2 += d[k] * d[k];
   }
-  return s;
+  return !(s2 <= half_skin2);
 }
 
 // tabulated function (potentialarray_t): v points at element 0, guards at

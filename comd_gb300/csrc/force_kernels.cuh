@@ -303,11 +303,11 @@ __device__ __forceinline__ bool build_skipped(const ForceArgs &A) {
 
 // row of atom i of box b: list storage, count slot and capacity
 template <int MODE>
-__device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i, bool mixed) {
+__device__ __forceinline__ int build_row(const ForceArgs &A, int b, int i) {
   const int slot = b * CG_MAXATOMS + i;
   if (MODE == LIST_ID) {
     const int idi = A.s.id[slot];
-    A.pl.rref[idi] = world32(A.g, b, mixed ? A.s.pos32 : nullptr, slot, A.s.r[slot]);
+    A.pl.rref[idi] = world64(A.g, b, A.s.r[slot]);
     return idi;
   }
   const int a = A.box_start[b] + i;
@@ -405,7 +405,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
     for (int t = 0; t < na; t++) {
       const uint32_t *ms = s_mask[warp][t];
       if (MODE != LIST_ID && A.box_start[b] + i0 + t >= A.ntot) break;  // only after an overflow
-      const int row = (lane == 0) ? build_row<MODE>(A, b, i0 + t, true) : 0;
+      const int row = (lane == 0) ? build_row<MODE>(A, b, i0 + t) : 0;
       const int a = __shfl_sync(0xffffffffu, row, 0);
       const int cap = build_cap<MODE>(A);
       // chunk words in candidate order: word w is held by lane w & 31 (w < 32
@@ -486,7 +486,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build64_kernel(ForceArg
     double xi, yi, zi;
     PrecT<double>::pos(A.s, b * CG_MAXATOMS + i, xi, yi, zi);
     if (MODE != LIST_ID && A.box_start[b] + i >= A.ntot) break;  // only after an overflow
-    const int row = (lane == 0) ? build_row<MODE>(A, b, i, false) : 0;
+    const int row = (lane == 0) ? build_row<MODE>(A, b, i) : 0;
     const int a = __shfl_sync(0xffffffffu, row, 0);
     const int cap = build_cap<MODE>(A);
     int cnt = 0;

@@ -188,6 +188,8 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
       else if (db < -1) db += R.nbx[k];
     }
     far |= db > 1 || db < -1;
+    // more than a box width outside its box: only a runaway step does that
+    far |= !(fabs(rv[k] - R.half[k]) <= 1.5 * R.boxsize[k]);
     if (db != 0) pv[k] = d2f_rn(fma((double)db, R.boxsize[k], rv[k] - R.half[k]));
     const float d = pv[k] - qv[k];
     d2 = fmaf(d, d, d2);
@@ -259,8 +261,7 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
     if (!VEL && w.pl.rref) {
       // persistent lists: the half step before a force call decides
       // whether the lists are rebuilt (an atom moved more than skin/2)
-      const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, r);
-      if (disp2(rep_of(g, b), wp, w.pl.rref[s.id[slot]]) > w.pl.half_skin2)
+      if (persist_stale(g, b, r, w.pl.rref[s.id[slot]], w.pl.half_skin2))
         atomicExch(status + ST_REBUILD, 1);
     }
   }
@@ -577,8 +578,7 @@ __global__ void skin_check_kernel(Geom g, Slots s, Persist pl, bool mixed, int *
   if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
   const int b = (int)(slot >> 6), k = (int)(slot & 63);
   if (k >= s.natoms[b]) return;
-  const float4 wp = world32(g, b, mixed ? s.pos32 : nullptr, slot, s.r[slot]);
-  if (disp2(rep_of(g, b), wp, pl.rref[s.id[slot]]) > pl.half_skin2)
+  if (persist_stale(g, b, s.r[slot], pl.rref[s.id[slot]], pl.half_skin2))
     atomicExch(status + ST_REBUILD, 1);
 }
 
