@@ -513,7 +513,11 @@ __global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, Sl
       s.natoms[jb] = nj + 1;
       int ni = s.natoms[b] - 1;
       s.natoms[b] = ni;
-      if (ni) copy_record(s, off, s, b * CG_MAXATOMS + ni, mixed, slot_of);
+      // the box's last atom fills the hole; when the departed atom was the
+      // last one the reference's copy is onto itself, a no-op that must not
+      // re-point the departed atom's id at its old slot
+      if (ni && off != b * CG_MAXATOMS + ni)
+        copy_record(s, off, s, b * CG_MAXATOMS + ni, mixed, slot_of);
     }
   }
 }

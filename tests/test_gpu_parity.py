@@ -13,7 +13,7 @@ import numpy as np
 import pytest
 
 import comd_gb300 as cg
-from comd_gb300.abi import by_id, slot_views
+from comd_gb300.abi import by_id, occupied_mask, slot_views
 from helpers import Case, compare_forces, layout_equal, rel_rms, slots_equal
 
 pytestmark = pytest.mark.gpu
@@ -162,6 +162,59 @@ def test_rebox_serial_fallback(oracle):
         d.close()
         assert slots_equal(c.s, o2)
         c.oracle.free(o2)
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("precision", [cg.PREC_FP64, cg.PREC_MIXED])
+def test_persistent_lists_after_serial_rebin(oracle, precision):
+    """Persistent lists read neighbours through the id -> slot map the rebin
+    keeps.  Moves of more than one box (here 1.7 boxes in x for every fifth
+    atom, -1.3 in y for the next) go through the serial replay of reBoxAll,
+    which also empties boxes by moving their last atom; the force call after
+    it must equal a fresh build's on the same state, and the oracle's."""
+    c = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=300.0)
+    try:
+        v = slot_views(c.s)
+        m = occupied_mask(c.s)
+        ids = v["id"]
+        rmass = c.pot.ptr.contents.mass * cg.lib.AMU_TO_ME
+        bs = list(c.s.contents.boxsize)
+        dt = 10.0  # internal time units
+        sel = m & (ids % 5 == 0)
+        v["p"][sel, 0] = 1.7 * bs[0] * rmass / dt
+        sel = m & (ids % 5 == 1)
+        v["p"][sel, 1] = -1.3 * bs[1] * rmass / dt
+        slot_views(c.o)["p"][:] = v["p"]  # the oracle clone has the same layout
+        d = cg.DeviceSim(c.s, cg.opts(cg.POT_EAM_CHEBY, precision, True, cheby_from_host=True))
+        try:
+            assert d.list_info()[0]
+            d.force()
+            d.advance_positions(dt)
+            e1 = d.force()[0]
+            d.download(c.s)
+        finally:
+            d.close()
+        f1 = by_id(c.s, "f")[:, :3].copy()
+        fresh = cg.DeviceSim(c.s, cg.opts(cg.POT_EAM_CHEBY, precision, True,
+                                          cheby_from_host=True))
+        try:
+            e2 = fresh.force()[0]
+            fresh.download(c.s)
+        finally:
+            fresh.close()
+        f2 = by_id(c.s, "f")[:, :3]
+        assert abs(e1 - e2) <= 1e-12 * abs(e2), (e1, e2)
+        assert np.abs(f1 - f2).max() <= 1e-9 * np.abs(f2).max()
+        c.oracle.lib.orc_advance_positions(c.o, dt)
+        assert c.oracle.rebox(c.o) == 0
+        assert layout_equal(c.s, c.o)
+        c.oracle_force()
+        eo = c.o.contents.e
+        if precision == cg.PREC_FP64:
+            assert abs(e1 - eo) <= FP64_E_TOL * abs(eo), (e1, eo)
+        else:
+            assert abs(e1 - eo) / c.s.contents.ntot < 1e-7, (e1, eo)
     finally:
         c.close()
 
