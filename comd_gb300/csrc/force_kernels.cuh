@@ -270,6 +270,50 @@ __device__ __forceinline__ int stage_entries(const ForceArgs &A, int b, int *s_b
   return ne;
 }
 
+// FP32 lists: the staged entries sorted by neighbour box (ties by entry),
+// so that every list comes out in ascending neighbour slot -- atoms in force
+// order are in box order, and lanes of a warp then walk the position array
+// together.  s_code keeps each entry's stencil index (the passes take the
+// box offset from it); s_off is rebuilt in the new order.
+__device__ __forceinline__ void order_entries_by_box(int ne, int *s_box, int *s_off,
+                                                     BoxOff<float> *s_dr, int *s_code) {
+  if (threadIdx.x < 32) {
+    const int e = threadIdx.x;
+    const int jb = e < ne ? s_box[e] : 0x7fffffff;
+    BoxOff<float> dr{};
+    int n = 0;
+    if (e < ne) {
+      dr = s_dr[e];
+      n = s_off[e + 1] - s_off[e];
+    }
+    int rank = 0;
+    for (int q = 0; q < ne; q++) {
+      const int jq = __shfl_sync(0xffffffffu, jb, q);
+      rank += (jq < jb) || (jq == jb && q < e);
+    }
+    // n of the entry at each rank, for the new prefix
+    int x = 0;
+    for (int q = 0; q < ne; q++) {
+      const int rq = __shfl_sync(0xffffffffu, rank, q);
+      const int nq = __shfl_sync(0xffffffffu, n, q);
+      if (rq == e) x = nq;
+    }
+    __syncwarp();
+    if (e < ne) {
+      s_box[rank] = jb;
+      s_dr[rank] = dr;
+      s_code[rank] = e;
+    }
+    for (int o = 1; o < 32; o <<= 1) {  // inclusive scan over ranks
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (e >= o) x += y;
+    }
+    if (e < ne) s_off[e + 1] = x;
+    if (e == 0) s_off[0] = 0;
+  }
+  __syncthreads();
+}
+
 __device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
   int lo = 0, hi = ne - 1;  // last e with s_off[e] <= c
   while (lo < hi) {
@@ -348,13 +392,14 @@ template <int MODE>
 static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
   __shared__ __align__(16) float4 cand[NB_MAXC];
   __shared__ uint32_t s_mask[NB_THREADS / 32][NB_ATOMS][NB_CHUNKS];
-  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1];
+  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1], s_code[CG_NNBR];
   __shared__ BoxOff<float> s_dr[CG_NNBR];
   if (build_skipped<MODE>(A)) return;
   const int b = blockIdx.x;
   const int ni = A.s.natoms[b];
   if (ni == 0) return;
   const int ne = stage_entries<float>(A, b, s_box, s_off, s_dr);
+  if (MODE != LIST_ID) order_entries_by_box(ne, s_box, s_off, s_dr, s_code);
   const int ncand = s_off[ne];
   const int nchunk = (ncand + 31) >> 5;
   for (int c = threadIdx.x; c < (nchunk << 5); c += NB_THREADS) {
@@ -365,8 +410,9 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
       BoxOff<float> o = s_dr[e];
       // force order: with periodic nbx >= 3 the entry index is the code
       const int tag = MODE == LIST_ID   ? A.s.id[s_box[e] * CG_MAXATOMS + k]
-                      : MODE == LIST_FO ? (int)(((unsigned)(A.box_start[s_box[e]] + k) << 5) | e)
-                                        : ((e << 6) | k);
+                      : MODE == LIST_FO ? (int)(((unsigned)(A.box_start[s_box[e]] + k) << 5) |
+                                                s_code[e])
+                                        : ((s_code[e] << 6) | k);
       cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
                             __int_as_float(tag));
     } else {

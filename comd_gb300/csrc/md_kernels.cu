@@ -188,8 +188,9 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
       else if (db < -1) db += R.nbx[k];
     }
     far |= db > 1 || db < -1;
-    // more than a box width outside its box: only a runaway step does that
-    far |= !(fabs(rv[k] - R.half[k]) <= 1.5 * R.boxsize[k]);
+    // more than a box width outside its box (only a runaway step does that):
+    // the box-centred FP32 position says so without FP64 work
+    far |= !(fabsf(pv[k]) <= 1.5f * R.hi[k]);
     if (db != 0) pv[k] = d2f_rn(fma((double)db, R.boxsize[k], rv[k] - R.half[k]));
     const float d = pv[k] - qv[k];
     d2 = fmaf(d, d, d2);
