@@ -980,7 +980,7 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
       vcap = std::max(vcap, neighbor_capacity(sims[r], rc + h->skin));
     const size_t n1 = (size_t)h->ntot + 1;
     h->pl.slot_of = track(h, dalloc<int>(n1, &err));
-    if (h->mixed && h->ntot < (1 << 27)) {
+    if (h->mixed && h->ntot < (1 << 26)) {  // entries hold the neighbour in 26 bits
       // force order: rows padded to whole warps of 32 atoms
       const size_t rows = ((size_t)h->ntot + 31) / 32 * 32;
       h->fo.vcap = vcap;

@@ -165,9 +165,9 @@ struct Persist {
 // and the passes work in that numbering until the next build.  The list of
 // atom a is stored transposed per warp of 32 atoms -- entry t of atom a at
 // ((a / 32) * vcap + t) * 32 + a % 32, so the 32 lanes of a warp read entry
-// t as one 128-byte line -- each entry (neighbour number << 5) | code, the
-// code (dx+1)*9 + (dy+1)*3 + (dz+1) of the neighbour's build box relative
-// to a's.  Positions are FP32 relative to the centre of the atom's build
+// t as one 128-byte line -- each entry (neighbour number << 6) | code, the
+// code the neighbour's build box relative to a's as three 2-bit fields
+// (dx+1) | (dy+1) << 2 | (dz+1) << 4 (so at most 2^26 atoms).  Positions are FP32 relative to the centre of the atom's build
 // box, refreshed every step from the FP64 slot data, so a pair's dr is
 // (pos_a - pos_j) - d * boxsize with d the code's box difference.
 struct ForceOrder {

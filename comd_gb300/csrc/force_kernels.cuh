@@ -314,6 +314,13 @@ __device__ __forceinline__ void order_entries_by_box(int ne, int *s_box, int *s_
   __syncthreads();
 }
 
+// force-order entry code of stencil entry e = (dx+1)*9 + (dy+1)*3 + (dz+1)
+// (periodic, nbx >= 3): the three box differences as 2-bit fields d+1 at
+// bits 0, 2 and 4
+__device__ __forceinline__ int fo_code(int e) {
+  return (e / 9) | (((e / 3) % 3) << 2) | ((e % 3) << 4);
+}
+
 __device__ __forceinline__ int entry_of(const int *s_off, int ne, int c) {
   int lo = 0, hi = ne - 1;  // last e with s_off[e] <= c
   while (lo < hi) {
@@ -410,8 +417,8 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
       BoxOff<float> o = s_dr[e];
       // force order: with periodic nbx >= 3 the entry index is the code
       const int tag = MODE == LIST_ID   ? A.s.id[s_box[e] * CG_MAXATOMS + k]
-                      : MODE == LIST_FO ? (int)(((unsigned)(A.box_start[s_box[e]] + k) << 5) |
-                                                s_code[e])
+                      : MODE == LIST_FO ? (int)(((unsigned)(A.box_start[s_box[e]] + k) << 6) |
+                                                fo_code(s_code[e]))
                                         : ((s_code[e] << 6) | k);
       cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
                             __int_as_float(tag));
@@ -910,11 +917,6 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
-// k - 1 as a float for 0 <= k < 2^22 (exponent-field trick: two instructions)
-__device__ __forceinline__ float small_int_minus1(int k) {
-  return __int_as_float(0x4B000000 | k) - 8388609.0f;
-}
-
 // Visit the list of force-order atom a at FP32 position pi: fn(fj, dx, dy,
 // dz, r2) for every entry; with NEED_FI positions come from fo.pf and fj is
 // F'(rho_j) (its w), else fj is unspecified.  An overflowed list scans the
@@ -940,6 +942,9 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
     hx = R.hi[0], hy = R.hi[1], hz = R.hi[2];
     lx = R.lo[0], ly = R.lo[1], lz = R.lo[2];
   }
+  // the y and z fields are read in place (x 4, x 16): their box sizes are
+  // scaled by 1/4 and 1/16, exactly
+  hy *= 0.25f, ly *= 0.25f, hz *= 0.0625f, lz *= 0.0625f;
   const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
   // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1
@@ -948,13 +953,15 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   for (int t = 0; t < n; t++) {
     if (t + FO_PREFETCH < n) prefetch_l1(lst + (size_t)(t + FO_PREFETCH) * 32);
     const uint32_t p = __ldg(lst + (size_t)t * 32);
-    const int j = (int)(p >> 5), c = (int)(p & 31u);
+    const int j = (int)(p >> 6);
     const float4 q = __ldg(pj + j);
-    // code = (dx+1)*9 + (dy+1)*3 + (dz+1); the pair offset is -d * boxsize
-    const int cx = (c * 57) >> 9, rem = c - 9 * cx;
-    const int cy = (rem * 11) >> 5, cz = rem - 3 * cy;
-    const float ex = -small_int_minus1(cx), ey = -small_int_minus1(cy),
-                ez = -small_int_minus1(cz);
+    // entry = j << 6 | (dz+1) << 4 | (dy+1) << 2 | (dx+1); the pair offset
+    // is -d * boxsize.  A field f * 2^s in place, OR-ed into the bits of
+    // 2^23, is the float 2^23 + f * 2^s: subtracted from 2^23 + 2^s it gives
+    // -d * 2^s exactly.
+    const float ex = 8388609.0f - __int_as_float(0x4B000000 | (int)(p & 0x3u));
+    const float ey = 8388612.0f - __int_as_float(0x4B000000 | (int)(p & 0xCu));
+    const float ez = 8388624.0f - __int_as_float(0x4B000000 | (int)(p & 0x30u));
     const float dx = fmaf(ex, lx, fmaf(ex, hx, pi.x - q.x));
     const float dy = fmaf(ey, ly, fmaf(ey, hy, pi.y - q.y));
     const float dz = fmaf(ez, lz, fmaf(ez, hz, pi.z - q.z));
