@@ -450,9 +450,11 @@ def batch_arm(args):
     """64 EAM Cu Chebyshev replicas (mixed precision) of seeded uneven size,
     edge U{8..24} unit cells, temperature U(100, 1200) K, advanced together:
     a 50-step loop captured as one CUDA graph over all replicas.  The box
-    factor and the skin are chosen by timing every candidate on the batch
-    itself (autotuner); the result is set against the same 64 systems run one
-    after another, each with its own 50-step graph."""
+    factor and the skin, then the launch shapes (the list build's threads per
+    box and atoms per candidate load, pass 2's threads per CTA), are chosen by
+    timing every candidate on the batch itself (autotuner); the result is set
+    against the same 64 systems run one after another, each with its own
+    50-step graph and the same settings."""
     import comd_gb300 as cg
     rng = np.random.default_rng(BATCH["seed"])
     R = BATCH["replicas"]
@@ -503,9 +505,36 @@ def batch_arm(args):
         free(sims)
     best = max((t for t in tried if "atom_steps_per_s" in t), key=lambda t: t["atom_steps_per_s"])
     sims = build(best["bf"])
+    # second stage: launch shapes at the chosen box factor and skin -- the
+    # list build's threads per box (threads per cell) and atoms per candidate
+    # load (cell tile), then pass 2's threads per CTA
+    shapes = []
+
+    def time_shape(bt, ba, pt):
+        b = cg.Batch(sims, o(best["skin_A"]))
+        try:
+            b.set_launch(bt, ba, pt)
+            b.graph_steps(5)
+            ms = b.graph_steps(30)
+        finally:
+            b.close()
+        rec = {"build_threads": bt, "build_atoms": ba, "pass2_threads": pt,
+               "ms_per_step": ms / 30, "atom_steps_per_s": natoms * 30 / (ms * 1e-3)}
+        shapes.append(rec)
+        return rec
+
+    for bt in (64, 128, 256):
+        for ba in (2, 4, 8):
+            time_shape(bt, ba, 256)
+    sb = max(shapes, key=lambda t: t["atom_steps_per_s"])
+    for pt in (128, 512):
+        time_shape(sb["build_threads"], sb["build_atoms"], pt)
+    shape = max(shapes, key=lambda t: t["atom_steps_per_s"])
+    launch = (shape["build_threads"], shape["build_atoms"], shape["pass2_threads"])
     try:
         b = cg.Batch(sims, o(best["skin_A"]))
         try:
+            b.set_launch(*launch)
             b.graph_steps(nsteps)  # capture + warm
             clk = ClockSampler(0)
             clk.start()
@@ -520,6 +549,8 @@ def batch_arm(args):
         for r in range(R):
             d = cg.DeviceSim(sims[r], o(best["skin_A"]))
             try:
+                if d.list_info()[0]:
+                    d.set_launch(*launch)
                 d.graph_steps(nsteps)
                 t_seq += d.graph_steps(nsteps)
             finally:
@@ -538,7 +569,8 @@ def batch_arm(args):
                    "loop": f"{nsteps} steps captured as one CUDA graph"},
         "ms_per_loop": t_batch, "sequential_64": {"value": seq, "ms_total": t_seq},
         "speedup_vs_sequential": value / seq,
-        "autotune": {"chosen": best, "candidates": tried},
+        "autotune": {"chosen": dict(best, launch_shape=shape), "candidates": tried,
+                     "launch_shapes": shapes},
         "energy_per_atom_ha": {"min": float(min(e / (4 * edges ** 3))),
                                "max": float(max(e / (4 * edges ** 3)))},
         "clocks": clocks}))

@@ -446,7 +446,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
   if (h->fo.list) {
     // force order (positions were placed by the half step before, or by
     // fo_track): the list build if due, then the passes
-    launch_nbr_build<float>(A, (float)(rcl * rcl), st);
+    launch_nbr_build<float>(A, (float)(rcl * rcl), st, &h->tune);
     launch_rebuild_done(h->status, st);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     if (pot == COMDGB_POT_LJ) {
@@ -455,11 +455,11 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
     } else if (pot == COMDGB_POT_EAM_TABLE) {
       launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 0, st);
       if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 1, st);
+      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 1, st, &h->tune);
     } else {
       launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 0, st);
       if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 1, st);
+      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 1, st, &h->tune);
     }
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     return;
@@ -1289,6 +1289,31 @@ int comdgb_sim_kinetic(comdgb_sim *h, double *ek) {
                  h->stream);
   CK(cudaMemcpyAsync(ek, h->d_out + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
+  return 0;
+}
+
+int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int pass2_threads) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  if (build_threads == 0) build_threads = 128;
+  if (build_atoms == 0) build_atoms = 4;
+  if (pass2_threads == 0) pass2_threads = 256;
+  if ((build_threads != 64 && build_threads != 128 && build_threads != 256) ||
+      (build_atoms != 2 && build_atoms != 4 && build_atoms != 8) ||
+      (pass2_threads != 128 && pass2_threads != 256 && pass2_threads != 512))
+    return set_err(COMDGB_ERR_ARG, "launch shape %d/%d/%d: build threads 64, 128 or 256, "
+                   "atoms per load 2, 4 or 8, pass 2 threads 128, 256 or 512",
+                   build_threads, build_atoms, pass2_threads);
+  CK(cudaSetDevice(h->device));
+  h->tune.build_threads = build_threads;
+  h->tune.build_atoms = build_atoms;
+  h->tune.pass2_threads = pass2_threads;
+  h->tune.pass2_blocks =
+      h->mixed && h->opts.potential != COMDGB_POT_LJ
+          ? fo_pass2_blocks(h->opts.potential == COMDGB_POT_EAM_CHEBY ? EVAL_CHEBY : EVAL_TABLE,
+                            h->nrep > 1, pass2_threads)
+          : 0;
+  CK(cudaGetLastError());
+  drop_graphs(h);  // recaptured with the new shapes at the next call
   return 0;
 }
 

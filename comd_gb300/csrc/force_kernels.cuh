@@ -395,10 +395,11 @@ __device__ __forceinline__ void build_count(const ForceArgs &A, int row, int tot
   if (total > build_cap<MODE>(A)) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
 }
 
-template <int MODE>
-static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArgs A, float rc2) {
+// NT threads per box (CTA), NA atoms tested per candidate load
+template <int MODE, int NT = NB_THREADS, int NA = NB_ATOMS>
+static __global__ void __launch_bounds__(NT) nbr_build32_kernel(ForceArgs A, float rc2) {
   __shared__ __align__(16) float4 cand[NB_MAXC];
-  __shared__ uint32_t s_mask[NB_THREADS / 32][NB_ATOMS][NB_CHUNKS];
+  __shared__ uint32_t s_mask[NT / 32][NA][NB_CHUNKS];
   __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1], s_code[CG_NNBR];
   __shared__ BoxOff<float> s_dr[CG_NNBR];
   if (build_skipped<MODE>(A)) return;
@@ -409,7 +410,7 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
   if (MODE != LIST_ID) order_entries_by_box(ne, s_box, s_off, s_dr, s_code);
   const int ncand = s_off[ne];
   const int nchunk = (ncand + 31) >> 5;
-  for (int c = threadIdx.x; c < (nchunk << 5); c += NB_THREADS) {
+  for (int c = threadIdx.x; c < (nchunk << 5); c += NT) {
     if (c < ncand) {
       int e = entry_of(s_off, ne, c);
       int k = c - s_off[e];
@@ -429,16 +430,16 @@ static __global__ void __launch_bounds__(NB_THREADS) nbr_build32_kernel(ForceArg
   __syncthreads();
   const float rc2b = rc2 * (1.0f + 4e-6f);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int i0 = NB_ATOMS * warp; i0 < ni; i0 += NB_ATOMS * (NB_THREADS / 32)) {
-    const int na = min(NB_ATOMS, ni - i0);
-    float4 pa[NB_ATOMS];
+  for (int i0 = NA * warp; i0 < ni; i0 += NA * (NT / 32)) {
+    const int na = min(NA, ni - i0);
+    float4 pa[NA];
 #pragma unroll
-    for (int t = 0; t < NB_ATOMS; t++)
+    for (int t = 0; t < NA; t++)
       pa[t] = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0 + (t < na ? t : 0));
     for (int q = 0; q < nchunk; q++) {
       const float4 cq = cand[(q << 5) + lane];
 #pragma unroll
-      for (int t = 0; t < NB_ATOMS; t++) {
+      for (int t = 0; t < NA; t++) {
         const float dx = pa[t].x - cq.x, dy = pa[t].y - cq.y, dz = pa[t].z - cq.z;
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const uint32_t m = __ballot_sync(0xffffffffu, r2 <= rc2b);
@@ -987,8 +988,10 @@ __global__ void __launch_bounds__(FO1_THREADS, 2)
   }
 }
 
+constexpr int FO2_MAX_THREADS = 512;  // pass 2 runs with 128, 256 (default) or 512
+
 template <int EVAL, bool MULTI>
-__global__ void __launch_bounds__(PASS_THREADS)
+__global__ void __launch_bounds__(FO2_MAX_THREADS)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);

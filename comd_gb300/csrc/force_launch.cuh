@@ -91,11 +91,33 @@ static int pass_grid(int pass, int eval, int ntot, bool fo = false,
   return (int)(need < cap ? need : cap);
 }
 
+#if COMDGB_FT_FLOAT
+// the force-order build at the tuned shape (threads per box x atoms per load)
+template <int NT>
+static void launch_fo_build_nt(const ForceArgs &A, float rc2, int na, cudaStream_t st) {
+  if (na == 2) nbr_build32_kernel<LIST_FO, NT, 2><<<A.g.nboxes, NT, 0, st>>>(A, rc2);
+  else if (na == 8) nbr_build32_kernel<LIST_FO, NT, 8><<<A.g.nboxes, NT, 0, st>>>(A, rc2);
+  else nbr_build32_kernel<LIST_FO, NT, 4><<<A.g.nboxes, NT, 0, st>>>(A, rc2);
+}
+static void launch_fo_build(const ForceArgs &A, float rc2, cudaStream_t st, const Tune *t) {
+  const int nt = t ? t->build_threads : NB_THREADS, na = t ? t->build_atoms : NB_ATOMS;
+  if (nt == 64) launch_fo_build_nt<64>(A, rc2, na, st);
+  else if (nt == 256) launch_fo_build_nt<256>(A, rc2, na, st);
+  else launch_fo_build_nt<128>(A, rc2, na, st);
+}
+#endif
+
 template <>
-void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
+void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st, const Tune *tune) {
+  (void)tune;
   if (sizeof(FT) == 4) {
-    if (A.fo.list) nbr_build32_kernel<LIST_FO><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
-    else if (A.pl.vlist)
+#if COMDGB_FT_FLOAT
+    if (A.fo.list) {
+      launch_fo_build(A, (float)rc2, st, tune);
+      return;
+    }
+#endif
+    if (A.pl.vlist)
       nbr_build32_kernel<LIST_ID><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
     else nbr_build32_kernel<LIST_STEP><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
   } else {
@@ -109,23 +131,50 @@ void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st) {
 
 #if COMDGB_FT_FLOAT
 template <int EVAL>
-void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st) {
+void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st,
+                   const Tune *tune) {
   if (A.ntot <= 0) return;
   const size_t smem = P.seg.n > 0 ? pass_smem(pass, EVAL) : 0;
-  const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS), g1 = pass_grid(1, EVAL, A.ntot, true);
   const bool multi = A.g.nrep > 1;
   if (pass == 0) {
+    const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS);
     if (multi) fo_eam_pass1_kernel<EVAL, true><<<g0, FO1_THREADS, smem, st>>>(A, P);
     else fo_eam_pass1_kernel<EVAL, false><<<g0, FO1_THREADS, smem, st>>>(A, P);
   } else {
-    if (multi) fo_eam_pass2_kernel<EVAL, true><<<g1, PASS_THREADS, smem, st>>>(A, P);
-    else fo_eam_pass2_kernel<EVAL, false><<<g1, PASS_THREADS, smem, st>>>(A, P);
+    const int threads = tune ? tune->pass2_threads : PASS_THREADS;
+    int g1;
+    if (tune && tune->pass2_blocks > 0) {
+      const long need = ((long)A.ntot + threads - 1) / threads;
+      g1 = (int)(need < tune->pass2_blocks ? need : tune->pass2_blocks);
+    } else {
+      g1 = pass_grid(1, EVAL, A.ntot, true, threads);
+    }
+    if (multi) fo_eam_pass2_kernel<EVAL, true><<<g1, threads, smem, st>>>(A, P);
+    else fo_eam_pass2_kernel<EVAL, false><<<g1, threads, smem, st>>>(A, P);
   }
 }
 template void launch_fo_eam<EVAL_TABLE>(const ForceArgs &, const EamPot<float, EVAL_TABLE> &,
-                                        int, cudaStream_t);
+                                        int, cudaStream_t, const Tune *);
 template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, EVAL_CHEBY> &,
-                                        int, cudaStream_t);
+                                        int, cudaStream_t, const Tune *);
+
+int fo_pass2_blocks(int eval, bool multi, int threads) {
+  int per_sm = 0;
+  const size_t smem = pass_smem(1, eval);
+  cudaError_t e;
+  if (eval == EVAL_CHEBY)
+    e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, fo_eam_pass2_kernel<EVAL_CHEBY, true>, threads, smem)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, fo_eam_pass2_kernel<EVAL_CHEBY, false>, threads, smem);
+  else
+    e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, fo_eam_pass2_kernel<EVAL_TABLE, true>, threads, 0)
+              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                    &per_sm, fo_eam_pass2_kernel<EVAL_TABLE, false>, threads, 0);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  return per_sm * g_num_sms;
+}
 
 void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st) {
   if (A.ntot <= 0) return;

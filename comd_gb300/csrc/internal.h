@@ -81,11 +81,20 @@ void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *stat
 void launch_fo_track(const Geom &g, Slots s, const ForceOrder &fo, const int *atom_slot,
                      int ntot, int *status, cudaStream_t st);
 
+// Launch shapes of the mixed-precision force-order kernels (results do not
+// depend on them): the list build's threads per box and atoms tested per
+// candidate load, pass 2's threads per CTA and its grid cap (0: the resident
+// CTAs of the default shape)
+struct Tune {
+  int build_threads = 128, build_atoms = 4;
+  int pass2_threads = 256, pass2_blocks = 0;
+};
+
 // ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----
 template <class T>
 cudaError_t prepare_force_kernels();
 template <class T>
-void launch_nbr_build(const ForceArgs &A, T rc2, cudaStream_t st);
+void launch_nbr_build(const ForceArgs &A, T rc2, cudaStream_t st, const Tune *tune = nullptr);
 template <class T, int EVAL>
 void launch_eam_pass1(const ForceArgs &A, const EamPot<T, EVAL> &P, cudaStream_t st);
 template <class T, int EVAL>
@@ -94,7 +103,11 @@ template <class T>
 void launch_lj(const ForceArgs &A, const LjPot<T> &P, cudaStream_t st);
 // force order (mixed precision only, force_mixed.cu); pass 0 or 1
 template <int EVAL>
-void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st);
+void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st,
+                   const Tune *tune = nullptr);
+// resident-CTA grid cap of pass 2 at `threads` per CTA (SMs x CTAs per SM);
+// call outside stream capture
+int fo_pass2_blocks(int eval, bool multi, int threads);
 void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st);
 
 }  // namespace cg

@@ -111,6 +111,7 @@ struct comdgb_sim {
   // centrosymmetry (centro.cu): one value per slot, then the range of the
   // last replica asked for
   double *centro = nullptr;
+  cg::Tune tune;  // launch shapes of the force-order kernels (comdgb_sim_set_launch)
   // graphs
   cudaGraphExec_t step_exec = nullptr;
   cudaGraphExec_t force_exec = nullptr;

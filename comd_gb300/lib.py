@@ -100,6 +100,7 @@ def _bind(lib):
     L.comdgb_printIt.argtypes = [P_SIM, C.c_void_p]
     L.comdgb_batch_virial.argtypes = [C.c_void_p, C.c_int, D, D, D]
     L.comdgb_sim_atom_stress.argtypes = [C.c_void_p, C.c_int, D]
+    L.comdgb_sim_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p
@@ -443,6 +444,10 @@ class DeviceSim:
 
     def synchronize(self):
         check(self.L.comdgb_sim_synchronize(self.h))
+
+    def set_launch(self, build_threads=0, build_atoms=0, pass2_threads=0):
+        """launch shapes of the force-order kernels (0: default)"""
+        check(self.L.comdgb_sim_set_launch(self.h, build_threads, build_atoms, pass2_threads))
 
     def list_info(self):
         """(persistent lists in use, skin in A, persistent-list builds since upload)"""

@@ -143,6 +143,13 @@ const char *comdgb_kernel_name(comdgb_sim *h, int k);
 int comdgb_sim_graph_steps(comdgb_sim *h, int n, double dt, float *ms);
 /* kernels launched per replay of the captured step graph / force graph */
 int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
+/* Launch shapes of the mixed-precision force-order kernels, for autotuning
+ * (0 keeps the default): the skin-list build's threads per box -- the
+ * threads per cell -- (64, 128 or 256; default 128) and atoms tested per
+ * candidate load (2, 4 or 8; default 4), and pass 2's threads per CTA (128,
+ * 256 or 512; default 256).  Results do not depend on them (the lists and
+ * every per-atom sum keep their order); the graphs are recaptured. */
+int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int pass2_threads);
 /* list mode in use (1 persistent, 0 per step), its skin, and the number of
  * persistent-list builds since the last upload */
 int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long *builds);

@@ -111,3 +111,57 @@ def test_graph_steps_loop_equals_step_replays():
     finally:
         for s in a + b:
             cg.free_host(s)
+
+
+@pytest.mark.gpu
+def test_launch_shapes_do_not_change_results():
+    """every launch shape of the force-order kernels gives the same state,
+    bit for bit (lists and per-atom sums keep their order), single and batch"""
+    pot = cg.eam_potential("cu")
+    o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, True)
+    ref = make_replicas(pot)
+    try:
+        d = cg.DeviceSim(ref[0], o)
+        try:
+            e_ref = d.steps(12)[0]
+            d.download(ref[0])
+        finally:
+            d.close()
+        b = cg.Batch(ref[1:], o)
+        try:
+            b.steps(12)
+            eb_ref = b.energies()[0]
+        finally:
+            b.close()
+        for shape in [(64, 2, 128), (256, 8, 512), (128, 4, 256), (64, 8, 256)]:
+            sims = make_replicas(pot)
+            try:
+                d = cg.DeviceSim(sims[0], o)
+                try:
+                    assert d.list_info()[0]
+                    d.set_launch(*shape)
+                    e = d.steps(12)[0]
+                    d.download(sims[0])
+                finally:
+                    d.close()
+                assert e == e_ref, shape
+                assert slots_equal(sims[0], ref[0], ("id", "r", "p")), shape
+                b = cg.Batch(sims[1:], o)
+                try:
+                    b.set_launch(*shape)
+                    b.steps(12)
+                    assert np.array_equal(b.energies()[0], eb_ref), shape
+                finally:
+                    b.close()
+            finally:
+                for s in sims:
+                    cg.free_host(s)
+        with pytest.raises(cg.ComdgbError):
+            d = cg.DeviceSim(ref[0], o)
+            try:
+                d.set_launch(96, 4, 256)
+            finally:
+                d.close()
+    finally:
+        for s in ref:
+            cg.free_host(s)
