@@ -1452,6 +1452,9 @@ int comdgb_attach(simflat_t *s, const comdgb_opts *o) {
 int comdgb_detach(simflat_t *s) {
   comdgb_sim *h = find_attached(s);
   if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  cudaSetDevice(h->device);
+  // lazy mode: the host gets the device state before the mirror goes away
+  const int rc = h->host_stale ? download(h, s) : 0;
   {
     std::lock_guard<std::mutex> lk(g_reg_mu);
     for (size_t i = 0; i < g_attached.size(); i++)
@@ -1460,20 +1463,41 @@ int comdgb_detach(simflat_t *s) {
         break;
       }
   }
-  cudaSetDevice(h->device);
   unpin_host(h, s);
   comdgb_sim_destroy(h);
-  return 0;
+  return rc;
+}
+
+// Before a drop-in call: the device state is current (eager mode uploads
+// every call; lazy mode only while the host holds the newer state).
+static int drop_in_enter(comdgb_sim *h, simflat_t *s) {
+  CK(cudaSetDevice(h->device));
+  if (h->lazy && h->dev_valid) return 0;
+  int rc = upload(h, s);
+  if (!rc) h->dev_valid = true;
+  return rc;
+}
+
+// After it: eager mode copies the results back (`full`: the whole state,
+// else the force outputs); lazy mode only e and stress, and marks the
+// host's arrays stale until comdgb_sync_to_host.
+static int drop_in_leave(comdgb_sim *h, simflat_t *s, bool full) {
+  if (h->lazy) {
+    s->e = h->e;
+    s->stress = h->stress;
+    h->host_stale = true;
+    return 0;
+  }
+  return full ? download(h, s) : download_forces(h, s);
 }
 
 int comdgb_force(void *sv) {
   simflat_t *s = (simflat_t *)sv;
   comdgb_sim *h = find_attached(s);
   if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
-  CK(cudaSetDevice(h->device));
-  int rc = upload(h, s);
+  int rc = drop_in_enter(h, s);
   if (!rc) rc = do_force(h);
-  if (!rc) rc = download_forces(h, s);
+  if (!rc) rc = drop_in_leave(h, s, false);
   return rc;
 }
 
@@ -1483,23 +1507,56 @@ double comdgb_nTimeSteps(int n, simflat_t *s, double dt) {
     set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
     return NAN;
   }
-  if (cudaSetDevice(h->device) != cudaSuccess) return NAN;
-  int rc = upload(h, s);
+  int rc = drop_in_enter(h, s);
   if (!rc) rc = do_steps(h, n, dt);
-  if (!rc) rc = download(h, s);
+  if (!rc) rc = drop_in_leave(h, s, true);
   return rc ? NAN : s->e;
 }
 
 int comdgb_reBoxAll(simflat_t *s) {
   comdgb_sim *h = find_attached(s);
   if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
-  CK(cudaSetDevice(h->device));
-  int rc = upload(h, s);
+  int rc = drop_in_enter(h, s);
   if (!rc) {
     enqueue_rebox(h);
     rc = check_status(h);
   }
-  if (!rc) rc = download(h, s);
+  if (!rc) rc = drop_in_leave(h, s, true);
+  return rc;
+}
+
+int comdgb_set_lazy(simflat_t *s, int lazy) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  CK(cudaSetDevice(h->device));
+  if (!lazy && h->host_stale) {  // leaving lazy mode: the host gets the state
+    int rc = download(h, s);
+    if (rc) return rc;
+    h->host_stale = false;
+  }
+  h->lazy = lazy != 0;
+  return 0;
+}
+
+int comdgb_sync_to_host(simflat_t *s) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  CK(cudaSetDevice(h->device));
+  if (!h->dev_valid) return 0;  // nothing ran on the device yet
+  int rc = download(h, s);
+  if (!rc) h->host_stale = false;
+  return rc;
+}
+
+int comdgb_sync_to_device(simflat_t *s) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  CK(cudaSetDevice(h->device));
+  int rc = upload(h, s);
+  if (!rc) {
+    h->dev_valid = true;
+    h->host_stale = false;
+  }
   return rc;
 }
 

@@ -268,12 +268,12 @@ int comdgb_sim_write_clsman(comdgb_sim *h, int r, const char *path, int format,
   return write_atoms(path, format, comment, h->reps[r].bounds, v.data(), h->reps[r].na);
 }
 
-// the drop-ins: an attached simflat_t is gathered from the device, any other
-// on the host
+// the drop-ins: a simflat_t attached in lazy mode (the device holds the
+// current state) is gathered on the device, any other on the host
 static int write_simflat(simflat_t *s, const char *fname, int format) {
   if (!s || !fname) return set_err(COMDGB_ERR_ARG, "null argument");
   comdgb_sim *h = find_attached(s);
-  if (h) return comdgb_sim_write_clsman(h, 0, fname, format, s->comment);
+  if (h && h->lazy) return comdgb_sim_write_clsman(h, 0, fname, format, s->comment);
   std::vector<double> v(6 * (size_t)s->ntot + 6);
   int rc = host_gather(s, v.data());
   if (rc) return rc;

@@ -101,6 +101,9 @@ def _bind(lib):
     L.comdgb_batch_virial.argtypes = [C.c_void_p, C.c_int, D, D, D]
     L.comdgb_sim_atom_stress.argtypes = [C.c_void_p, C.c_int, D]
     L.comdgb_sim_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+    L.comdgb_set_lazy.argtypes = [P_SIM, C.c_int]
+    L.comdgb_sync_to_host.argtypes = [P_SIM]
+    L.comdgb_sync_to_device.argtypes = [P_SIM]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p

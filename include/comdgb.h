@@ -98,7 +98,17 @@ int comdgb_force(void *s);
 double comdgb_nTimeSteps(int n, simflat_t *s, double dt);
 /* Drop-in for reBoxAll (domains.c:347-389) on the GPU. */
 int comdgb_reBoxAll(simflat_t *s);
+/* Releases the mirror; in lazy mode the host first gets the device state. */
 int comdgb_detach(simflat_t *s);
+/* Lazy mode (off by default).  The drop-in calls above keep the state on the
+ * GPU between calls and write back only s->e and s->stress.  The host's slot
+ * arrays are brought up to date by comdgb_sync_to_host (and by
+ * comdgb_detach, or by leaving lazy mode).  After the host changes them,
+ * comdgb_sync_to_device makes the GPU take them.  With lazy mode off, every
+ * call copies the state up and its results back. */
+int comdgb_set_lazy(simflat_t *s, int lazy);
+int comdgb_sync_to_host(simflat_t *s);
+int comdgb_sync_to_device(simflat_t *s);
 
 /* ---------------- device-resident handles ---------------- */
 
@@ -266,8 +276,9 @@ int comdgb_sim_gather(comdgb_sim *h, int r, double *out);
  * file's comment line (a newline is added when it has none; NULL: empty) */
 int comdgb_sim_write_clsman(comdgb_sim *h, int r, const char *path, int format,
                             const char *comment);
-/* drop-ins for writeClsman(s, fname) and gzASCIIWrite(s, fname): an attached
- * simflat_t is gathered from the device, any other on the host */
+/* drop-ins for writeClsman(s, fname) and gzASCIIWrite(s, fname): a simflat_t
+ * attached in lazy mode is gathered on the device (it holds the current
+ * state), any other on the host */
 int comdgb_writeClsman(simflat_t *s, const char *fname);
 int comdgb_gzASCIIWrite(simflat_t *s, const char *fname);
 /* printIt (write.c:89-110): the atoms with id < 10, box by box */

@@ -247,6 +247,7 @@ def test_attached_dropin_writes_device_state(oracle, tmp_path):
         o = cg.opts(cg.POT_EAM_TABLE, cg.PREC_FP64)
         assert L.comdgb_attach(s, C.byref(o)) == 0
         try:
+            assert L.comdgb_set_lazy(s, 1) == 0  # the device holds the state
             assert L.comdgb_writeClsman(s, str(tmp_path / "a.bin").encode()) == 0
             assert L.comdgb_gzASCIIWrite(s, str(tmp_path / "a.txt.gz").encode()) == 0
         finally:

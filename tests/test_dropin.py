@@ -1,0 +1,80 @@
+"""The drop-in calls on a host simflat_t (comdgb_attach, comdgb_force,
+comdgb_nTimeSteps, comdgb_reBoxAll), eager and lazy.
+
+Eager (the default): every call copies the host state up and the results
+back.  Lazy: the state stays on the GPU between calls; the host sees e and
+stress after each call and the slot arrays after comdgb_sync_to_host (or
+comdgb_detach); comdgb_sync_to_device hands host changes to the GPU.  With
+per-step FP64 lists the two modes give the same trajectory bit for bit."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import comd_gb300 as cg
+from comd_gb300.abi import slot_views
+from helpers import Case, slots_equal
+
+
+def opts():
+    return cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, True, cheby_from_host=True,
+                   per_step_lists=True)
+
+
+@pytest.mark.gpu
+def test_lazy_equals_eager(oracle):
+    a = Case(oracle, cg.POT_EAM_CHEBY, n=(6, 6, 6), amp=0.05, temp=600.0)
+    b = Case(oracle, cg.POT_EAM_CHEBY, n=(6, 6, 6), amp=0.05, temp=600.0)
+    L = cg.load()
+    L.comdgb_set_lazy.argtypes = [C.c_void_p, C.c_int]
+    try:
+        r0 = slot_views(a.s)["r"].copy()
+        o = opts()
+        assert L.comdgb_attach(a.s, C.byref(o)) == 0
+        assert L.comdgb_attach(b.s, C.byref(o)) == 0
+        try:
+            assert L.comdgb_set_lazy(a.s, 1) == 0
+            ea = [L.comdgb_nTimeSteps(5, a.s, 1e-15) for _ in range(3)]
+            eb = [L.comdgb_nTimeSteps(5, b.s, 1e-15) for _ in range(3)]
+            assert ea == eb
+            assert a.s.contents.e == b.s.contents.e
+            # lazy: the host's arrays are still the initial ones ...
+            assert np.array_equal(slot_views(a.s)["r"], r0)
+            # ... until they are synced
+            assert L.comdgb_sync_to_host(a.s) == 0
+            assert slots_equal(a.s, b.s, ("id", "r", "p", "f", "rho", "fi"))
+            # host changes reach the device by sync_to_device
+            for s in (a.s, b.s):
+                slot_views(s)["p"][:] *= 0.5
+            assert L.comdgb_sync_to_device(a.s) == 0
+            assert L.comdgb_nTimeSteps(3, a.s, 1e-15) == L.comdgb_nTimeSteps(3, b.s, 1e-15)
+            assert L.comdgb_force(C.cast(a.s, C.c_void_p)) == 0
+            assert L.comdgb_force(C.cast(b.s, C.c_void_p)) == 0
+            assert a.s.contents.e == b.s.contents.e
+        finally:
+            assert L.comdgb_detach(a.s) == 0  # lazy: brings the state home first
+            assert L.comdgb_detach(b.s) == 0
+        assert slots_equal(a.s, b.s, ("id", "r", "p", "f", "rho", "fi"))
+    finally:
+        a.close()
+        b.close()
+
+
+@pytest.mark.gpu
+def test_eager_force_matches_oracle(oracle):
+    """comdgb_force installed as the potential's force pointer computes what
+    the reference's computeForce computes (FP64)"""
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(6, 6, 6), amp=0.05, temp=600.0)
+    L = cg.load()
+    try:
+        o = cg.opts(cg.POT_EAM_TABLE, cg.PREC_FP64)
+        assert L.comdgb_attach(c.s, C.byref(o)) == 0
+        try:
+            assert L.comdgb_force(C.cast(c.s, C.c_void_p)) == 0
+        finally:
+            L.comdgb_detach(c.s)
+        c.oracle_force()
+        assert abs(c.s.contents.e - c.o.contents.e) <= 1e-12 * abs(c.o.contents.e)
+        assert abs(c.s.contents.stress - c.o.contents.stress) <= 1e-10 * abs(c.o.contents.stress)
+    finally:
+        c.close()
