@@ -354,6 +354,8 @@ def gpu_arm(args):
         cg.lib.check(L.comdgb_attach(s, C.byref(o)))
         calls, per_call = args.e2e_calls, 10
         L.comdgb_nTimeSteps(per_call, s, dt)  # warm-up: graph capture, pinning
+        b0 = (C.c_longlong(), C.c_longlong())
+        cg.lib.check(L.comdgb_transfer_bytes(s, C.byref(b0[0]), C.byref(b0[1])))
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(calls):
@@ -363,12 +365,14 @@ def gpu_arm(args):
         t1 = time.perf_counter()
         dist.barrier()
         e2e_s = dist.max(t1 - t0)
+        b1 = (C.c_longlong(), C.c_longlong())
+        cg.lib.check(L.comdgb_transfer_bytes(s, C.byref(b1[0]), C.byref(b1[1])))
         L.comdgb_detach(s)
-        ns = s.contents.nboxes * 64
-        nb = s.contents.nboxes
-        # bytes copied per call: natoms, id, iType, mass, r, p, f, rho, fi
-        h2d = nb * 4 + ns * (4 + 4 + 8 + 24 + 24 + 32 + 8 + 8)
-        d2h = h2d
+        # bytes the library copied in the timed calls (each box's slots up to
+        # the largest occupancy; the upload carries the state, the download
+        # the state and the forces)
+        h2d = (b1[0].value - b0[0].value) // calls
+        d2h = (b1[1].value - b0[1].value) // calls
         e2e = {"value": dist.sum(natoms * calls * per_call) / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": h2d // per_call, "d2h_bytes_per_step": d2h // per_call,
                "call": f"comdgb_nTimeSteps({per_call}) on a host simflat_t (pinned), "

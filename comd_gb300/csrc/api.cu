@@ -664,27 +664,58 @@ int do_steps(comdgb_sim *h, int n, double dt) {
 
 // the host arrays of replica r into its box and slot range (ids offset by
 // the replica's first atom)
-int upload_rep(comdgb_sim *h, int r, const simflat_t *s) {
+// Host <-> device copies of slot arrays cover the first `w` slots of every box
+// (w = the largest box occupancy): a 2D copy with the 64-slot pitch, or one
+// plain copy when w = 64.  Slots past a box's occupancy are never read.
+static cudaError_t slots_copy(void *dst, const void *src, size_t elem, size_t nb, int w,
+                              cudaMemcpyKind kind, cudaStream_t st) {
+  const size_t pitch = elem * CG_MAXATOMS;
+  if (w >= CG_MAXATOMS) return cudaMemcpyAsync(dst, src, pitch * nb, kind, st);
+  if (w <= 0) return cudaSuccess;
+  return cudaMemcpy2DAsync(dst, pitch, src, pitch, elem * (size_t)w, nb, kind, st);
+}
+
+static int max_occupancy(const int *natoms, size_t nb) {
+  int w = 0;
+  for (size_t b = 0; b < nb; b++) w = natoms[b] > w ? natoms[b] : w;
+  return w;
+}
+
+#define CKX(call, bytes, counter)  \
+  do {                             \
+    CK(call);                      \
+    h->counter += (bytes);         \
+  } while (0)
+
+// forces: also f, rho and fi (a force call or nTimeSteps recomputes them
+// before reading them; reBoxAll and the handle API carry them)
+int upload_rep(comdgb_sim *h, int r, const simflat_t *s, bool forces = true) {
   cudaStream_t st = h->stream;
   const RepGeo &R = h->reps[r];
   if (s->nboxes != R.nb) return set_err(COMDGB_ERR_ARG, "box count changed");
   if (s->ntot != h->atom0[r + 1] - h->atom0[r]) return set_err(COMDGB_ERR_ARG, "atom count changed");
   const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
   const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
-  CK(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.id + s0, s->id, ns * sizeof(int), cudaMemcpyHostToDevice, st));
+  const int w = max_occupancy(s->natoms, nb);
+  const size_t rows = nb * (size_t)w;
+  const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
+  CKX(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), H2D, st),
+      nb * sizeof(int), xfer_h2d);
+  CKX(slots_copy(h->s.id + s0, s->id, sizeof(int), nb, w, H2D, st), rows * 4, xfer_h2d);
   if (h->atom0[r]) launch_add_offset(h->s.id + s0, (long)ns, h->atom0[r], st);
-  CK(cudaMemcpyAsync(h->s.itype + s0, s->iType, ns * sizeof(int), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.mass + s0, s->mass, ns * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->stage3 + 3 * s0, s->r, ns * 3 * sizeof(double), cudaMemcpyHostToDevice,
-                     st));
+  CKX(slots_copy(h->s.itype + s0, s->iType, sizeof(int), nb, w, H2D, st), rows * 4, xfer_h2d);
+  CKX(slots_copy(h->s.mass + s0, s->mass, sizeof(double), nb, w, H2D, st), rows * 8, xfer_h2d);
+  CKX(slots_copy(h->stage3 + 3 * s0, s->r, 3 * sizeof(double), nb, w, H2D, st), rows * 24,
+      xfer_h2d);
   launch_unpack3(h->stage3 + 3 * s0, h->s.r + s0, (long)ns, st);
-  CK(cudaMemcpyAsync(h->stage3 + 3 * (NS + s0), s->p, ns * 3 * sizeof(double),
-                     cudaMemcpyHostToDevice, st));
+  CKX(slots_copy(h->stage3 + 3 * (NS + s0), s->p, 3 * sizeof(double), nb, w, H2D, st),
+      rows * 24, xfer_h2d);
   launch_unpack3(h->stage3 + 3 * (NS + s0), h->s.p + s0, (long)ns, st);
-  CK(cudaMemcpyAsync(h->s.f + s0, s->f, ns * 4 * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.rho + s0, s->rho, ns * sizeof(double), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(h->s.fi + s0, s->fi, ns * sizeof(double), cudaMemcpyHostToDevice, st));
+  if (forces) {
+    CKX(slots_copy(h->s.f + s0, s->f, 4 * sizeof(double), nb, w, H2D, st), rows * 32, xfer_h2d);
+    CKX(slots_copy(h->s.rho + s0, s->rho, sizeof(double), nb, w, H2D, st), rows * 8, xfer_h2d);
+    CKX(slots_copy(h->s.fi + s0, s->fi, sizeof(double), nb, w, H2D, st), rows * 8, xfer_h2d);
+  }
   return 0;
 }
 
@@ -704,9 +735,9 @@ int upload_done(comdgb_sim *h) {
   return 0;
 }
 
-int upload(comdgb_sim *h, const simflat_t *s) {
+int upload(comdgb_sim *h, const simflat_t *s, bool forces = true) {
   if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_upload");
-  int rc = upload_rep(h, 0, s);
+  int rc = upload_rep(h, 0, s, forces);
   return rc ? rc : upload_done(h);
 }
 
@@ -782,13 +813,28 @@ int snapshot_copy(comdgb_sim *h, const Snapshot &q, bool save) {
 }
 
 // f, rho, fi (and e, stress) of replica r
-int download_forces_rep(comdgb_sim *h, int r, simflat_t *s) {
+// w: the largest box occupancy of the replica's current layout (-1: read it)
+static int replica_width(comdgb_sim *h, int r, int w) {
+  if (w >= 0) return w;
+  const RepGeo &R = h->reps[r];
+  std::vector<int> n((size_t)R.nb);
+  if (cudaMemcpyAsync(n.data(), h->s.natoms + R.box0, sizeof(int) * n.size(),
+                      cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return CG_MAXATOMS;
+  return max_occupancy(n.data(), n.size());
+}
+
+int download_forces_rep(comdgb_sim *h, int r, simflat_t *s, int w = -1) {
   cudaStream_t st = h->stream;
   const RepGeo &R = h->reps[r];
-  const size_t ns = (size_t)R.nb * CG_MAXATOMS, s0 = (size_t)R.box0 * CG_MAXATOMS;
-  CK(cudaMemcpyAsync(s->f, h->s.f + s0, ns * 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->rho, h->s.rho + s0, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->fi, h->s.fi + s0, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const size_t nb = (size_t)R.nb, s0 = (size_t)R.box0 * CG_MAXATOMS;
+  w = replica_width(h, r, w);
+  const size_t rows = nb * (size_t)w;
+  const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+  CKX(slots_copy(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, st), rows * 32, xfer_d2h);
+  CKX(slots_copy(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, st), rows * 8, xfer_d2h);
+  CKX(slots_copy(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, st), rows * 8, xfer_d2h);
   CK(cudaStreamSynchronize(st));
   if (h->nrep == 1) {
     s->e = h->e;
@@ -806,17 +852,22 @@ int download_rep(comdgb_sim *h, int r, simflat_t *s) {
   if (s->nboxes != R.nb) return set_err(COMDGB_ERR_ARG, "box count differs");
   const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
   const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
-  CK(cudaMemcpyAsync(s->natoms, h->s.natoms + b0, nb * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->id, h->s.id + s0, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->iType, h->s.itype + s0, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(s->mass, h->s.mass + s0, ns * sizeof(double), cudaMemcpyDeviceToHost, st));
+  const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+  CKX(cudaMemcpyAsync(s->natoms, h->s.natoms + b0, nb * sizeof(int), D2H, st),
+      nb * sizeof(int), xfer_d2h);
+  CK(cudaStreamSynchronize(st));
+  const int w = max_occupancy(s->natoms, nb);
+  const size_t rows = nb * (size_t)w;
+  CKX(slots_copy(s->id, h->s.id + s0, sizeof(int), nb, w, D2H, st), rows * 4, xfer_d2h);
+  CKX(slots_copy(s->iType, h->s.itype + s0, sizeof(int), nb, w, D2H, st), rows * 4, xfer_d2h);
+  CKX(slots_copy(s->mass, h->s.mass + s0, sizeof(double), nb, w, D2H, st), rows * 8, xfer_d2h);
   launch_pack3(h->s.r + s0, h->stage3 + 3 * s0, (long)ns, st);
-  CK(cudaMemcpyAsync(s->r, h->stage3 + 3 * s0, ns * 3 * sizeof(double), cudaMemcpyDeviceToHost,
-                     st));
+  CKX(slots_copy(s->r, h->stage3 + 3 * s0, 3 * sizeof(double), nb, w, D2H, st), rows * 24,
+      xfer_d2h);
   launch_pack3(h->s.p + s0, h->stage3 + 3 * (NS + s0), (long)ns, st);
-  CK(cudaMemcpyAsync(s->p, h->stage3 + 3 * (NS + s0), ns * 3 * sizeof(double),
-                     cudaMemcpyDeviceToHost, st));
-  int rc = download_forces_rep(h, r, s);
+  CKX(slots_copy(s->p, h->stage3 + 3 * (NS + s0), 3 * sizeof(double), nb, w, D2H, st),
+      rows * 24, xfer_d2h);
+  int rc = download_forces_rep(h, r, s, w);
   if (rc) return rc;
   const int off = h->atom0[r];
   if (off)
@@ -825,7 +876,7 @@ int download_rep(comdgb_sim *h, int r, simflat_t *s) {
   return 0;
 }
 
-int download_forces(comdgb_sim *h, simflat_t *s) { return download_forces_rep(h, 0, s); }
+int download_forces(comdgb_sim *h, simflat_t *s) { return download_forces_rep(h, 0, s, -1); }
 int download(comdgb_sim *h, simflat_t *s) {
   if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_download");
   return download_rep(h, 0, s);
@@ -1470,10 +1521,12 @@ int comdgb_detach(simflat_t *s) {
 
 // Before a drop-in call: the device state is current (eager mode uploads
 // every call; lazy mode only while the host holds the newer state).
-static int drop_in_enter(comdgb_sim *h, simflat_t *s) {
+// forces: the call reads f, rho and fi as input (reBoxAll carries them; a
+// force call and nTimeSteps compute them before reading them)
+static int drop_in_enter(comdgb_sim *h, simflat_t *s, bool forces) {
   CK(cudaSetDevice(h->device));
   if (h->lazy && h->dev_valid) return 0;
-  int rc = upload(h, s);
+  int rc = upload(h, s, forces);
   if (!rc) h->dev_valid = true;
   return rc;
 }
@@ -1495,7 +1548,7 @@ int comdgb_force(void *sv) {
   simflat_t *s = (simflat_t *)sv;
   comdgb_sim *h = find_attached(s);
   if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
-  int rc = drop_in_enter(h, s);
+  int rc = drop_in_enter(h, s, false);
   if (!rc) rc = do_force(h);
   if (!rc) rc = drop_in_leave(h, s, false);
   return rc;
@@ -1507,7 +1560,7 @@ double comdgb_nTimeSteps(int n, simflat_t *s, double dt) {
     set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
     return NAN;
   }
-  int rc = drop_in_enter(h, s);
+  int rc = drop_in_enter(h, s, false);
   if (!rc) rc = do_steps(h, n, dt);
   if (!rc) rc = drop_in_leave(h, s, true);
   return rc ? NAN : s->e;
@@ -1516,7 +1569,7 @@ double comdgb_nTimeSteps(int n, simflat_t *s, double dt) {
 int comdgb_reBoxAll(simflat_t *s) {
   comdgb_sim *h = find_attached(s);
   if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
-  int rc = drop_in_enter(h, s);
+  int rc = drop_in_enter(h, s, true);
   if (!rc) {
     enqueue_rebox(h);
     rc = check_status(h);
@@ -1535,6 +1588,14 @@ int comdgb_set_lazy(simflat_t *s, int lazy) {
     h->host_stale = false;
   }
   h->lazy = lazy != 0;
+  return 0;
+}
+
+int comdgb_transfer_bytes(simflat_t *s, long long *h2d, long long *d2h) {
+  comdgb_sim *h = find_attached(s);
+  if (!h) return set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
+  if (h2d) *h2d = h->xfer_h2d;
+  if (d2h) *d2h = h->xfer_d2h;
   return 0;
 }
 

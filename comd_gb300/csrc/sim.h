@@ -134,6 +134,7 @@ struct comdgb_sim {
   // drop-in lazy mode: the device keeps the state between calls (dev_valid:
   // it holds the current state; host_stale: the host's arrays are older)
   bool lazy = false, dev_valid = false, host_stale = false;
+  long long xfer_h2d = 0, xfer_d2h = 0;  // bytes copied by uploads / downloads
 };
 
 

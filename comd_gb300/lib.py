@@ -104,6 +104,7 @@ def _bind(lib):
     L.comdgb_set_lazy.argtypes = [P_SIM, C.c_int]
     L.comdgb_sync_to_host.argtypes = [P_SIM]
     L.comdgb_sync_to_device.argtypes = [P_SIM]
+    L.comdgb_transfer_bytes.argtypes = [P_SIM, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.comdgb_sim_list_info.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double),
                                        C.POINTER(C.c_longlong)]
     L.comdgb_kernel_name.restype = C.c_char_p

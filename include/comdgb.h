@@ -109,6 +109,11 @@ int comdgb_detach(simflat_t *s);
 int comdgb_set_lazy(simflat_t *s, int lazy);
 int comdgb_sync_to_host(simflat_t *s);
 int comdgb_sync_to_device(simflat_t *s);
+/* Bytes copied host -> device and device -> host for s since it was
+ * attached.  Copies cover each box's slots up to the largest occupancy, and
+ * a force call or nTimeSteps does not upload f, rho and fi (it computes
+ * them before reading them). */
+int comdgb_transfer_bytes(simflat_t *s, long long *h2d, long long *d2h);
 
 /* ---------------- device-resident handles ---------------- */
 
