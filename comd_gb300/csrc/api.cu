@@ -664,14 +664,22 @@ int do_steps(comdgb_sim *h, int n, double dt) {
 
 // the host arrays of replica r into its box and slot range (ids offset by
 // the replica's first atom)
-// Host <-> device copies of slot arrays cover the first `w` slots of every box
-// (w = the largest box occupancy): a 2D copy with the 64-slot pitch, or one
-// plain copy when w = 64.  Slots past a box's occupancy are never read.
+// Host <-> device copies of slot arrays: a 2D copy with the 64-slot pitch
+// moves only the first w slots of every box (w = the largest box
+// occupancy), one plain copy when w = 64.  Slots past a box's occupancy are
+// never read.  Returns the bytes moved in *bytes.
 static cudaError_t slots_copy(void *dst, const void *src, size_t elem, size_t nb, int w,
-                              cudaMemcpyKind kind, cudaStream_t st) {
+                              cudaMemcpyKind kind, cudaStream_t st, size_t *bytes) {
   const size_t pitch = elem * CG_MAXATOMS;
-  if (w >= CG_MAXATOMS) return cudaMemcpyAsync(dst, src, pitch * nb, kind, st);
-  if (w <= 0) return cudaSuccess;
+  if (w <= 0) {
+    *bytes = 0;
+    return cudaSuccess;
+  }
+  if (w >= CG_MAXATOMS) {
+    *bytes = pitch * nb;
+    return cudaMemcpyAsync(dst, src, pitch * nb, kind, st);
+  }
+  *bytes = elem * (size_t)w * nb;
   return cudaMemcpy2DAsync(dst, pitch, src, pitch, elem * (size_t)w, nb, kind, st);
 }
 
@@ -681,10 +689,12 @@ static int max_occupancy(const int *natoms, size_t nb) {
   return w;
 }
 
-#define CKX(call, bytes, counter)  \
-  do {                             \
-    CK(call);                      \
-    h->counter += (bytes);         \
+// a slots_copy call, its bytes added to the counter
+#define CKX(dst, src, elem, nb, w, kind, counter)                                 \
+  do {                                                                            \
+    size_t moved_ = 0;                                                            \
+    CK(slots_copy(dst, src, elem, nb, w, kind, h->stream, &moved_));              \
+    h->counter += (long long)moved_;                                              \
   } while (0)
 
 // forces: also f, rho and fi (a force call or nTimeSteps recomputes them
@@ -697,24 +707,21 @@ int upload_rep(comdgb_sim *h, int r, const simflat_t *s, bool forces = true) {
   const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
   const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
   const int w = max_occupancy(s->natoms, nb);
-  const size_t rows = nb * (size_t)w;
   const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
-  CKX(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), H2D, st),
-      nb * sizeof(int), xfer_h2d);
-  CKX(slots_copy(h->s.id + s0, s->id, sizeof(int), nb, w, H2D, st), rows * 4, xfer_h2d);
+  CK(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), H2D, st));
+  h->xfer_h2d += (long long)(nb * sizeof(int));
+  CKX(h->s.id + s0, s->id, sizeof(int), nb, w, H2D, xfer_h2d);
   if (h->atom0[r]) launch_add_offset(h->s.id + s0, (long)ns, h->atom0[r], st);
-  CKX(slots_copy(h->s.itype + s0, s->iType, sizeof(int), nb, w, H2D, st), rows * 4, xfer_h2d);
-  CKX(slots_copy(h->s.mass + s0, s->mass, sizeof(double), nb, w, H2D, st), rows * 8, xfer_h2d);
-  CKX(slots_copy(h->stage3 + 3 * s0, s->r, 3 * sizeof(double), nb, w, H2D, st), rows * 24,
-      xfer_h2d);
+  CKX(h->s.itype + s0, s->iType, sizeof(int), nb, w, H2D, xfer_h2d);
+  CKX(h->s.mass + s0, s->mass, sizeof(double), nb, w, H2D, xfer_h2d);
+  CKX(h->stage3 + 3 * s0, s->r, 3 * sizeof(double), nb, w, H2D, xfer_h2d);
   launch_unpack3(h->stage3 + 3 * s0, h->s.r + s0, (long)ns, st);
-  CKX(slots_copy(h->stage3 + 3 * (NS + s0), s->p, 3 * sizeof(double), nb, w, H2D, st),
-      rows * 24, xfer_h2d);
+  CKX(h->stage3 + 3 * (NS + s0), s->p, 3 * sizeof(double), nb, w, H2D, xfer_h2d);
   launch_unpack3(h->stage3 + 3 * (NS + s0), h->s.p + s0, (long)ns, st);
   if (forces) {
-    CKX(slots_copy(h->s.f + s0, s->f, 4 * sizeof(double), nb, w, H2D, st), rows * 32, xfer_h2d);
-    CKX(slots_copy(h->s.rho + s0, s->rho, sizeof(double), nb, w, H2D, st), rows * 8, xfer_h2d);
-    CKX(slots_copy(h->s.fi + s0, s->fi, sizeof(double), nb, w, H2D, st), rows * 8, xfer_h2d);
+    CKX(h->s.f + s0, s->f, 4 * sizeof(double), nb, w, H2D, xfer_h2d);
+    CKX(h->s.rho + s0, s->rho, sizeof(double), nb, w, H2D, xfer_h2d);
+    CKX(h->s.fi + s0, s->fi, sizeof(double), nb, w, H2D, xfer_h2d);
   }
   return 0;
 }
@@ -830,11 +837,10 @@ int download_forces_rep(comdgb_sim *h, int r, simflat_t *s, int w = -1) {
   const RepGeo &R = h->reps[r];
   const size_t nb = (size_t)R.nb, s0 = (size_t)R.box0 * CG_MAXATOMS;
   w = replica_width(h, r, w);
-  const size_t rows = nb * (size_t)w;
   const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
-  CKX(slots_copy(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, st), rows * 32, xfer_d2h);
-  CKX(slots_copy(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, st), rows * 8, xfer_d2h);
-  CKX(slots_copy(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, st), rows * 8, xfer_d2h);
+  CKX(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, xfer_d2h);
+  CKX(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, xfer_d2h);
+  CKX(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, xfer_d2h);
   CK(cudaStreamSynchronize(st));
   if (h->nrep == 1) {
     s->e = h->e;
@@ -853,20 +859,17 @@ int download_rep(comdgb_sim *h, int r, simflat_t *s) {
   const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
   const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
   const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
-  CKX(cudaMemcpyAsync(s->natoms, h->s.natoms + b0, nb * sizeof(int), D2H, st),
-      nb * sizeof(int), xfer_d2h);
+  CK(cudaMemcpyAsync(s->natoms, h->s.natoms + b0, nb * sizeof(int), D2H, st));
+  h->xfer_d2h += (long long)(nb * sizeof(int));
   CK(cudaStreamSynchronize(st));
   const int w = max_occupancy(s->natoms, nb);
-  const size_t rows = nb * (size_t)w;
-  CKX(slots_copy(s->id, h->s.id + s0, sizeof(int), nb, w, D2H, st), rows * 4, xfer_d2h);
-  CKX(slots_copy(s->iType, h->s.itype + s0, sizeof(int), nb, w, D2H, st), rows * 4, xfer_d2h);
-  CKX(slots_copy(s->mass, h->s.mass + s0, sizeof(double), nb, w, D2H, st), rows * 8, xfer_d2h);
+  CKX(s->id, h->s.id + s0, sizeof(int), nb, w, D2H, xfer_d2h);
+  CKX(s->iType, h->s.itype + s0, sizeof(int), nb, w, D2H, xfer_d2h);
+  CKX(s->mass, h->s.mass + s0, sizeof(double), nb, w, D2H, xfer_d2h);
   launch_pack3(h->s.r + s0, h->stage3 + 3 * s0, (long)ns, st);
-  CKX(slots_copy(s->r, h->stage3 + 3 * s0, 3 * sizeof(double), nb, w, D2H, st), rows * 24,
-      xfer_d2h);
+  CKX(s->r, h->stage3 + 3 * s0, 3 * sizeof(double), nb, w, D2H, xfer_d2h);
   launch_pack3(h->s.p + s0, h->stage3 + 3 * (NS + s0), (long)ns, st);
-  CKX(slots_copy(s->p, h->stage3 + 3 * (NS + s0), 3 * sizeof(double), nb, w, D2H, st),
-      rows * 24, xfer_d2h);
+  CKX(s->p, h->stage3 + 3 * (NS + s0), 3 * sizeof(double), nb, w, D2H, xfer_d2h);
   int rc = download_forces_rep(h, r, s, w);
   if (rc) return rc;
   const int off = h->atom0[r];
