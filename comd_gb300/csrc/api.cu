@@ -86,6 +86,8 @@ int alloc_slots(comdgb_sim *h, Slots &s, bool with_natoms, int *err) {
 }
 
 void free_all(comdgb_sim *h) {
+  if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+  if (h->ev_state) cudaEventDestroy(h->ev_state);
   if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
@@ -689,11 +691,11 @@ static int max_occupancy(const int *natoms, size_t nb) {
   return w;
 }
 
-// a slots_copy call, its bytes added to the counter
-#define CKX(dst, src, elem, nb, w, kind, counter)                                 \
+// a slots_copy call on stream st, its bytes added to h->counter
+#define CKX(dst, src, elem, nb, w, kind, counter, st)                             \
   do {                                                                            \
     size_t moved_ = 0;                                                            \
-    CK(slots_copy(dst, src, elem, nb, w, kind, h->stream, &moved_));              \
+    CK(slots_copy(dst, src, elem, nb, w, kind, st, &moved_));                     \
     h->counter += (long long)moved_;                                              \
   } while (0)
 
@@ -710,18 +712,18 @@ int upload_rep(comdgb_sim *h, int r, const simflat_t *s, bool forces = true) {
   const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
   CK(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), H2D, st));
   h->xfer_h2d += (long long)(nb * sizeof(int));
-  CKX(h->s.id + s0, s->id, sizeof(int), nb, w, H2D, xfer_h2d);
+  CKX(h->s.id + s0, s->id, sizeof(int), nb, w, H2D, xfer_h2d, st);
   if (h->atom0[r]) launch_add_offset(h->s.id + s0, (long)ns, h->atom0[r], st);
-  CKX(h->s.itype + s0, s->iType, sizeof(int), nb, w, H2D, xfer_h2d);
-  CKX(h->s.mass + s0, s->mass, sizeof(double), nb, w, H2D, xfer_h2d);
-  CKX(h->stage3 + 3 * s0, s->r, 3 * sizeof(double), nb, w, H2D, xfer_h2d);
+  CKX(h->s.itype + s0, s->iType, sizeof(int), nb, w, H2D, xfer_h2d, st);
+  CKX(h->s.mass + s0, s->mass, sizeof(double), nb, w, H2D, xfer_h2d, st);
+  CKX(h->stage3 + 3 * s0, s->r, 3 * sizeof(double), nb, w, H2D, xfer_h2d, st);
   launch_unpack3(h->stage3 + 3 * s0, h->s.r + s0, (long)ns, st);
-  CKX(h->stage3 + 3 * (NS + s0), s->p, 3 * sizeof(double), nb, w, H2D, xfer_h2d);
+  CKX(h->stage3 + 3 * (NS + s0), s->p, 3 * sizeof(double), nb, w, H2D, xfer_h2d, st);
   launch_unpack3(h->stage3 + 3 * (NS + s0), h->s.p + s0, (long)ns, st);
   if (forces) {
-    CKX(h->s.f + s0, s->f, 4 * sizeof(double), nb, w, H2D, xfer_h2d);
-    CKX(h->s.rho + s0, s->rho, sizeof(double), nb, w, H2D, xfer_h2d);
-    CKX(h->s.fi + s0, s->fi, sizeof(double), nb, w, H2D, xfer_h2d);
+    CKX(h->s.f + s0, s->f, 4 * sizeof(double), nb, w, H2D, xfer_h2d, st);
+    CKX(h->s.rho + s0, s->rho, sizeof(double), nb, w, H2D, xfer_h2d, st);
+    CKX(h->s.fi + s0, s->fi, sizeof(double), nb, w, H2D, xfer_h2d, st);
   }
   return 0;
 }
@@ -838,9 +840,9 @@ int download_forces_rep(comdgb_sim *h, int r, simflat_t *s, int w = -1) {
   const size_t nb = (size_t)R.nb, s0 = (size_t)R.box0 * CG_MAXATOMS;
   w = replica_width(h, r, w);
   const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
-  CKX(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, xfer_d2h);
-  CKX(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, xfer_d2h);
-  CKX(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, xfer_d2h);
+  CKX(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, xfer_d2h, st);
+  CKX(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
+  CKX(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
   CK(cudaStreamSynchronize(st));
   if (h->nrep == 1) {
     s->e = h->e;
@@ -863,13 +865,13 @@ int download_rep(comdgb_sim *h, int r, simflat_t *s) {
   h->xfer_d2h += (long long)(nb * sizeof(int));
   CK(cudaStreamSynchronize(st));
   const int w = max_occupancy(s->natoms, nb);
-  CKX(s->id, h->s.id + s0, sizeof(int), nb, w, D2H, xfer_d2h);
-  CKX(s->iType, h->s.itype + s0, sizeof(int), nb, w, D2H, xfer_d2h);
-  CKX(s->mass, h->s.mass + s0, sizeof(double), nb, w, D2H, xfer_d2h);
+  CKX(s->id, h->s.id + s0, sizeof(int), nb, w, D2H, xfer_d2h, st);
+  CKX(s->iType, h->s.itype + s0, sizeof(int), nb, w, D2H, xfer_d2h, st);
+  CKX(s->mass, h->s.mass + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
   launch_pack3(h->s.r + s0, h->stage3 + 3 * s0, (long)ns, st);
-  CKX(s->r, h->stage3 + 3 * s0, 3 * sizeof(double), nb, w, D2H, xfer_d2h);
+  CKX(s->r, h->stage3 + 3 * s0, 3 * sizeof(double), nb, w, D2H, xfer_d2h, st);
   launch_pack3(h->s.p + s0, h->stage3 + 3 * (NS + s0), (long)ns, st);
-  CKX(s->p, h->stage3 + 3 * (NS + s0), 3 * sizeof(double), nb, w, D2H, xfer_d2h);
+  CKX(s->p, h->stage3 + 3 * (NS + s0), 3 * sizeof(double), nb, w, D2H, xfer_d2h, st);
   int rc = download_forces_rep(h, r, s, w);
   if (rc) return rc;
   const int off = h->atom0[r];
@@ -880,6 +882,56 @@ int download_rep(comdgb_sim *h, int r, simflat_t *s) {
 }
 
 int download_forces(comdgb_sim *h, simflat_t *s) { return download_forces_rep(h, 0, s, -1); }
+
+// nTimeSteps(n) with all results copied back (one replica).  After the last
+// step the layout, ids, types, masses, r and p are final: they stream to the
+// host on a second stream while the trailing force call runs on the first;
+// f, rho and fi follow the force call.
+int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
+  if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_download");
+  if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
+  if (s->nboxes != h->reps[0].nb) return set_err(COMDGB_ERR_ARG, "box count differs");
+  if (!h->copy_stream) {
+    CK(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&h->ev_state, cudaEventDisableTiming));
+  }
+  const double dt_atu = dt * kBohrPerAtu;  // timestep.c:126
+  if (n > 0 && (!h->step_exec || h->graph_dt != dt_atu)) {
+    int rc = capture(h, &h->step_exec, dt_atu, true, false);
+    if (rc) return rc;
+    h->graph_dt = dt_atu;
+  }
+  if (!h->force_exec) {
+    int rc = capture(h, &h->force_exec, 0.0, false, true);
+    if (rc) return rc;
+  }
+  cudaStream_t st = h->stream, cs = h->copy_stream;
+  for (int i = 0; i < n; i++) CK(cudaGraphLaunch(h->step_exec, st));
+  CK(cudaEventRecord(h->ev_state, st));
+  CK(cudaStreamWaitEvent(cs, h->ev_state, 0));
+  const size_t nb = (size_t)h->reps[0].nb, ns = nb * CG_MAXATOMS, NS = (size_t)h->nslots;
+  CK(cudaMemcpyAsync(s->natoms, h->s.natoms, nb * sizeof(int), cudaMemcpyDeviceToHost, cs));
+  h->xfer_d2h += (long long)(nb * sizeof(int));
+  CK(cudaGraphLaunch(h->force_exec, st));  // the trailing force call (timestep.c:139)
+  CK(cudaStreamSynchronize(cs));
+  const int w = max_occupancy(s->natoms, nb);
+  {
+    const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+    CKX(s->id, h->s.id, sizeof(int), nb, w, D2H, xfer_d2h, cs);
+    CKX(s->iType, h->s.itype, sizeof(int), nb, w, D2H, xfer_d2h, cs);
+    CKX(s->mass, h->s.mass, sizeof(double), nb, w, D2H, xfer_d2h, cs);
+    launch_pack3(h->s.r, h->stage3, (long)ns, cs);
+    CKX(s->r, h->stage3, 3 * sizeof(double), nb, w, D2H, xfer_d2h, cs);
+    launch_pack3(h->s.p, h->stage3 + 3 * NS, (long)ns, cs);
+    CKX(s->p, h->stage3 + 3 * NS, 3 * sizeof(double), nb, w, D2H, xfer_d2h, cs);
+  }
+  int rc = finish_force(h);
+  if (!rc) rc = download_forces_rep(h, 0, s, w);
+  const cudaError_t e = cudaStreamSynchronize(cs);
+  if (!rc && e != cudaSuccess)
+    rc = set_err(COMDGB_ERR_CUDA, "state download: %s", cudaGetErrorString(e));
+  return rc;
+}
 int download(comdgb_sim *h, simflat_t *s) {
   if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_download");
   return download_rep(h, 0, s);
@@ -1564,8 +1616,8 @@ double comdgb_nTimeSteps(int n, simflat_t *s, double dt) {
     return NAN;
   }
   int rc = drop_in_enter(h, s, false);
-  if (!rc) rc = do_steps(h, n, dt);
-  if (!rc) rc = drop_in_leave(h, s, true);
+  if (!rc) rc = h->lazy ? do_steps(h, n, dt) : steps_and_download(h, n, dt, s);
+  if (!rc && h->lazy) rc = drop_in_leave(h, s, true);
   return rc ? NAN : s->e;
 }
 

@@ -135,6 +135,9 @@ struct comdgb_sim {
   // it holds the current state; host_stale: the host's arrays are older)
   bool lazy = false, dev_valid = false, host_stale = false;
   long long xfer_h2d = 0, xfer_d2h = 0;  // bytes copied by uploads / downloads
+  // drop-in nTimeSteps: the state download overlaps the trailing force call
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_state = nullptr;
 };
 
 
