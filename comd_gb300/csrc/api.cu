@@ -601,6 +601,7 @@ int finish_force(comdgb_sim *h) {
     }
   }
   if (!std::isfinite(h->e)) return set_err(COMDGB_ERR_NONFINITE, "total energy is %g", h->e);
+  h->lists_built = h->pl.slot_of != nullptr;  // a force call builds them when due
   return 0;
 }
 
@@ -728,16 +729,25 @@ int upload_rep(comdgb_sim *h, int r, const simflat_t *s, bool forces = true) {
   return 0;
 }
 
-// after the uploads: FP32 copies, status, id maps and list rebuild, atom list
+// After the uploads: FP32 copies, status, id maps, atom list.  Persistent
+// lists built by an earlier force call stay: they are keyed by atom id (or
+// by force-order number, which the id keeps), the maps are redone for the
+// uploaded layout, and the skin tests of the next step or force call rebuild
+// them if any atom moved more than skin/2 from its build position -- as
+// after any step.  Before the first force call a build is due anyway.
 int upload_done(comdgb_sim *h) {
   cudaStream_t st = h->stream;
   if (h->mixed) launch_pos32(h->g, h->s, st);
   CK(cudaMemsetAsync(h->status, 0, sizeof(int) * ST_COUNT, st));
-  if (h->pl.slot_of) {  // new host state: map ids to slots and rebuild the lists
+  if (h->pl.slot_of) {
     launch_slot_of(h->g, h->s, h->pl, h->ntot, h->status, st);
-    if (h->fo.of_id)
-      CK(cudaMemsetAsync(h->fo.of_id, 0xff, sizeof(int) * ((size_t)h->ntot + 1), st));
-    CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
+    if (h->lists_built) {
+      if (h->fo.of_id) launch_fo_reslot(h->g, h->s, h->fo, h->ntot, st);
+    } else {
+      if (h->fo.of_id)
+        CK(cudaMemsetAsync(h->fo.of_id, 0xff, sizeof(int) * ((size_t)h->ntot + 1), st));
+      CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, st));
+    }
   }
   enqueue_compact(h);
   CK(cudaGetLastError());

@@ -80,6 +80,8 @@ void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *stat
                        cudaStream_t st);
 void launch_fo_track(const Geom &g, Slots s, const ForceOrder &fo, const int *atom_slot,
                      int ntot, int *status, cudaStream_t st);
+// after an upload that keeps the lists: force-order slots of the new layout
+void launch_fo_reslot(const Geom &g, Slots s, const ForceOrder &fo, int ntot, cudaStream_t st);
 
 // Launch shapes of the mixed-precision force-order kernels (results do not
 // depend on them): the list build's threads per box and atoms tested per

@@ -559,6 +559,23 @@ __global__ void rebuild_done_kernel(int *status) {
   }
 }
 
+// Force order after a host upload that keeps the lists: every atom's slot
+// in the uploaded layout, by id
+__global__ void fo_reslot_kernel(Geom g, Slots s, ForceOrder fo, int ntot) {
+  const long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
+  const int b = (int)(slot >> 6), k = (int)(slot & 63);
+  if (k >= s.natoms[b]) return;
+  const int id = s.id[slot];
+  if (id < 0 || id >= ntot) return;  // the id -> slot map reports it
+  const int a = fo.of_id[id];
+  if (a >= 0) fo.slot[a] = (int)slot;
+}
+
+void launch_fo_reslot(const Geom &g, Slots s, const ForceOrder &fo, int ntot, cudaStream_t st) {
+  fo_reslot_kernel<<<slot_blocks(g), 256, 0, st>>>(g, s, fo, ntot);
+}
+
 // Force order, standalone force calls: every atom's force-order position
 // from its refreshed FP32 position, and the rebuild test
 __global__ void __launch_bounds__(256) fo_track_kernel(Geom g, Slots s, ForceOrder fo,

@@ -135,6 +135,7 @@ struct comdgb_sim {
   // it holds the current state; host_stale: the host's arrays are older)
   bool lazy = false, dev_valid = false, host_stale = false;
   long long xfer_h2d = 0, xfer_d2h = 0;  // bytes copied by uploads / downloads
+  bool lists_built = false;  // persistent lists exist (a force call completed)
   // drop-in nTimeSteps: the state download overlaps the trailing force call
   cudaStream_t copy_stream = nullptr;
   cudaEvent_t ev_state = nullptr;

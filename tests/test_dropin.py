@@ -78,3 +78,35 @@ def test_eager_force_matches_oracle(oracle):
         assert abs(c.s.contents.stress - c.o.contents.stress) <= 1e-10 * abs(c.o.contents.stress)
     finally:
         c.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", [cg.PREC_FP64, cg.PREC_MIXED])
+def test_eager_calls_keep_lists(oracle, precision):
+    """Eager calls upload the host state each time; skin lists built by an
+    earlier call stay (maps redone, skin test decides), so 4 eager calls of
+    5 steps give the same state, bit for bit, as 20 steps on a handle, and
+    build the lists only when atoms moved, not once per call."""
+    a = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
+    b = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
+    L = cg.load()
+    try:
+        o = cg.opts(cg.POT_EAM_CHEBY, precision, True, cheby_from_host=True)
+        d = cg.DeviceSim(b.s, o)
+        try:
+            assert d.list_info()[0]
+            eb = d.steps(20, 1e-15)[0]
+            d.download(b.s)
+        finally:
+            d.close()
+        assert L.comdgb_attach(a.s, C.byref(o)) == 0
+        try:
+            for _ in range(4):
+                ea = L.comdgb_nTimeSteps(5, a.s, 1e-15)
+        finally:
+            L.comdgb_detach(a.s)
+        assert ea == eb
+        assert slots_equal(a.s, b.s, ("id", "r", "p", "f", "rho", "fi"))
+    finally:
+        a.close()
+        b.close()
