@@ -10,11 +10,11 @@ from . import abi
 from .lib import (CLSMAN_BINARY, CLSMAN_TEXT, CLSMAN_TEXT_GZ, DATA_DIR, DISP_GAUSSIAN,
                   DISP_NONE, DISP_UNIFORM, POT_DIR, POT_EAM_CHEBY, POT_EAM_TABLE, POT_LJ,
                   PREC_FP64, PREC_MIXED, Batch, ComdgbError, DeviceSim, eam_potential, fcc,
-                  free_host, lj_potential, load, opts, print_it, read_clsman, round_f32, seed,
+                  free_host, lj_potential, load, opts, print_it, read_clsman, read_tim, round_f32, seed,
                   set_comment, write_clsman_host)
 
 __all__ = ["abi", "load", "Batch", "opts", "DeviceSim", "ComdgbError", "eam_potential",
-           "lj_potential", "fcc", "read_clsman", "write_clsman_host", "set_comment", "print_it",
+           "lj_potential", "fcc", "read_clsman", "read_tim", "write_clsman_host", "set_comment", "print_it",
            "DATA_DIR", "seed", "free_host", "round_f32", "POT_DIR", "POT_EAM_TABLE",
            "POT_EAM_CHEBY", "POT_LJ", "PREC_FP64", "PREC_MIXED", "DISP_NONE", "DISP_UNIFORM",
            "DISP_GAUSSIAN", "CLSMAN_BINARY", "CLSMAN_TEXT_GZ", "CLSMAN_TEXT"]

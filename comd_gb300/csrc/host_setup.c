@@ -437,6 +437,89 @@ void comdgb_printIt(const simflat_t *s, FILE *fp) {
                 s->p[o][2], s->f[o][0], s->f[o][1], s->f[o][2]);
 }
 
+/* fromFileTim (read.c:248-315): a raw array of the visualiser's FileAtom
+ * records (five native floats: x, y, z, bond order, centrosymmetry; the
+ * file size gives the count) into a new simflat_t.  The reference fixes the
+ * bounds to 327.424 x 354.446877 x 3007.581486 A rounded to float (its
+ * :274, 287-289, one data set's); bounds != NULL replaces them.  Atom i gets id i, type 1 (:300),
+ * the potential's mass and zero momenta, binned as successive putAtomInBox
+ * calls on the GPU `device` (device < 0: on the host). */
+simflat_t *comdgb_read_tim(const char *path, pmd_base_potential_t *pot, double bf,
+                           const double *bounds, int device, int *status) {
+  static const double kTimBounds[3] = {327.42399999999997817, 354.44687726089500757,
+                                       3007.58148577889733133};
+  int st = 0;
+  simflat_t *s = NULL;
+  float *rec = NULL;
+  double *xyz = NULL, *pxyz = NULL, *masses = NULL;
+  int *ids = NULL, *types = NULL;
+  long n = 0;
+  if (!path || !pot) {
+    if (status) *status = COMDGB_ERR_ARG;
+    return NULL;
+  }
+  FILE *fp = fopen(path, "rb");
+  if (!fp) {
+    st = COMDGB_ERR_IO;
+    goto done;
+  }
+  if (fseek(fp, 0, SEEK_END) == 0) n = ftell(fp) / (long)(5 * sizeof(float));
+  rewind(fp);
+  rec = (float *)malloc((size_t)n * 5 * sizeof(float) + 4);
+  if (!rec || fread(rec, 5 * sizeof(float), (size_t)n, fp) != (size_t)n) {
+    fclose(fp);
+    st = rec ? COMDGB_ERR_IO : COMDGB_ERR_NOMEM;
+    goto done;
+  }
+  fclose(fp);
+  s = (simflat_t *)zalloc(sizeof *s);
+  if (!s) {
+    st = COMDGB_ERR_NOMEM;
+    goto done;
+  }
+  s->pot = pot;
+  s->bf = bf;
+  s->defgrad = 0.0; /* blankSimulation's; allocDomains then takes strain 1 */
+  s->comment = (char *)zalloc(1024);
+  /* the reference holds its fixed bounds in floats (read.c:274, 287-289) */
+  for (int m = 0; m < 3; m++) s->bounds[m] = bounds ? bounds[m] : (double)(float)kTimBounds[m];
+  if ((st = alloc_domains(s))) goto done;
+  xyz = (double *)malloc(3 * (size_t)n * sizeof(double) + 8);
+  pxyz = (double *)calloc(3 * (size_t)n + 1, sizeof(double));
+  masses = (double *)malloc((size_t)n * sizeof(double) + 8);
+  ids = (int *)malloc((size_t)n * sizeof(int) + 4);
+  types = (int *)malloc((size_t)n * sizeof(int) + 4);
+  if (!xyz || !pxyz || !masses || !ids || !types) {
+    st = COMDGB_ERR_NOMEM;
+    goto done;
+  }
+  for (long i = 0; i < n; i++) {
+    for (int m = 0; m < 3; m++) xyz[3 * i + m] = (double)rec[5 * i + m];
+    ids[i] = (int)i;
+    types[i] = 1;
+    masses[i] = pot->mass;
+  }
+  if (device >= 0) {
+    st = comdgb_put_atoms(s, (int)n, xyz, pxyz, ids, types, masses, device);
+  } else {
+    for (long i = 0; i < n && !st; i++)
+      st = put_atom(s, ids[i], types[i], masses[i], xyz + 3 * i, NULL);
+  }
+done:
+  free(rec);
+  free(xyz);
+  free(pxyz);
+  free(masses);
+  free(ids);
+  free(types);
+  if (status) *status = st;
+  if (st && s) {
+    comdgb_sim_free_host(s);
+    s = NULL;
+  }
+  return s;
+}
+
 void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,
                  double mass_amu) {
   comdgb_seed_apply(s, seed, disp_kind, amp, temp_k, mass_amu);

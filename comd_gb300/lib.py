@@ -93,6 +93,9 @@ def _bind(lib):
     L.comdgb_batch_energies.argtypes = [C.c_void_p, D, D]
     L.comdgb_sim_virial.argtypes = [C.c_void_p, D, D, D]
     L.comdgb_sim_gather.argtypes = [C.c_void_p, C.c_int, D]
+    L.comdgb_read_tim.restype = P_SIM
+    L.comdgb_read_tim.argtypes = [C.c_char_p, C.c_void_p, C.c_double, D, C.c_int,
+                                  C.POINTER(C.c_int)]
     L.comdgb_sim_centrosymmetry.argtypes = [C.c_void_p, C.c_int, C.c_int, D, D, D]
     L.comdgb_sim_write_clsman.argtypes = [C.c_void_p, C.c_int, C.c_char_p, C.c_int, C.c_char_p]
     L.comdgb_writeClsman.argtypes = [P_SIM, C.c_char_p]
@@ -239,6 +242,18 @@ def read_clsman(path, pot, bf=1.0, device=0):
     s = L.comdgb_read_clsman(path.encode(), pot.base, bf, device, C.byref(st))
     if not s:
         raise ComdgbError(st.value, "comdgb_read_clsman failed: " + last_error())
+    return s
+
+
+def read_tim(path, pot, bf=1.0, bounds=None, device=0):
+    """comdgb_read_tim: a FileAtom file into a new host simflat_t (the
+    reference's fixed bounds unless `bounds` is given)"""
+    L = load()
+    st = C.c_int(0)
+    b = None if bounds is None else (C.c_double * 3)(*bounds)
+    s = L.comdgb_read_tim(path.encode(), pot.base, bf, b, device, C.byref(st))
+    if not s:
+        raise ComdgbError(st.value, "comdgb_read_tim failed: " + last_error())
     return s
 
 

@@ -267,6 +267,15 @@ simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double
 simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, double bf, int device,
                               int *status);
 
+/* fromFileTim (read.c:248-315): a raw array of FileAtom records (five native
+ * floats x, y, z, bond order, centrosymmetry) into a new host simflat_t; the
+ * reference's fixed bounds (327.424 x 354.446877 x 3007.581486 A, rounded to
+ * float as the reference holds them) unless
+ * `bounds` is given; atom i: id i, type 1, the potential's mass, zero
+ * momenta; binned on the GPU `device` (device < 0: on the host). */
+simflat_t *comdgb_read_tim(const char *path, pmd_base_potential_t *pot, double bf,
+                           const double *bounds, int device, int *status);
+
 /* ---------------- clsman output (write.c) ---------------- */
 enum {
   COMDGB_CLSMAN_BINARY = 0,  /* writeClsman (write.c:112-167), byte for byte */

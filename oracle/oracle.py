@@ -221,6 +221,8 @@ class RefLib:
         lib.refh_set_periodic.argtypes = [C.c_int]
         lib.refh_read_clsman.restype = P_SIM
         lib.refh_write_clsman.argtypes = [P_SIM, C.c_char_p]
+        lib.refh_read_tim.restype = P_SIM
+        lib.refh_read_tim.argtypes = [C.c_char_p, C.c_double, C.c_void_p]
         lib.refh_set_comment.argtypes = [P_SIM, C.c_char_p]
         lib.refh_gz_ascii_write.argtypes = [P_SIM, C.c_char_p]
         lib.refh_print_it.argtypes = [P_SIM, C.c_char_p]

@@ -81,6 +81,15 @@ void *refh_read_clsman(const char *path, double bf, void *pot, int is_eam) {
   return s;
 }
 
+/* the reference's FileAtom reader (read.c:248-315, fixed bounds) */
+void *refh_read_tim(const char *path, double bf, void *pot) {
+  command_t cmd;
+  memset(&cmd, 0, sizeof cmd);
+  strncpy(cmd.filename, path, sizeof cmd.filename - 1);
+  cmd.bf = bf;
+  return fromFileTim(cmd, (struct pmd_base_potential_t *)pot);
+}
+
 /* the reference's clsman writers (write.c:112-167 binary, :175-220 gzip
  * text) and its debug print (write.c:89-110) into a file */
 extern void writeClsman(simflat_t *s, char *fname);

@@ -152,6 +152,35 @@ def writer_cases(tmpdir):
     return {"ag8k_read": w1, "cu6_seeded_forced": w2}
 
 
+TIM_BOUNDS = (327.42399999999997817, 354.44687726089500757, 3007.58148577889733133)
+
+
+def tim_file(path, n=400, seed=31):
+    """n FileAtom records (x, y, z, bond order, centrosymmetry as float32),
+    positions uniform in the reference's fixed bounds"""
+    rng = np.random.default_rng(seed)
+    rec = np.zeros((n, 5), dtype=np.float32)
+    rec[:, :3] = rng.uniform(0.0, 1.0, (n, 3)) * np.array(TIM_BOUNDS)
+    rec[:, 3:] = rng.uniform(0.0, 1.0, (n, 2))
+    rec.tofile(path)
+
+
+def tim_case(tmpdir):
+    """fromFileTim (read.c:248-315) on a seeded FileAtom file; an LJ potential
+    with a 50 A cutoff keeps the fixed bounds' grid small (6 x 7 x 60 boxes)"""
+    L = ref_lib(False).lib
+    pot = L.refh_lj_make(20.0, 0.01, 50.0, 63.55)
+    path = os.path.join(tmpdir, "atoms.tim")
+    tim_file(path)
+    s = L.refh_read_tim(path.encode(), 1.0, pot)
+    v = s.contents
+    out = {"ntot": v.ntot, "nbx": list(v.nbx), "layout": layout_hash(s),
+           "r_sum": float(np.abs(by_id(s, "r")).sum()), "itype": int(by_id(s, "iType")[0]),
+           "mass": float(by_id(s, "mass")[0])}
+    os.remove(path)
+    return out
+
+
 def main():
     if ref_lib(False) is None or ref_lib(True) is None:
         sys.exit("oracle/_ref is not built (run make -C oracle with the reference sources)")
@@ -176,6 +205,7 @@ def main():
     import tempfile
     with tempfile.TemporaryDirectory() as td:
         fx["clsman_writers"] = writer_cases(td)
+        fx["tim_reader"] = tim_case(td)
     with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
         json.dump(fx, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_fixtures.json"))

@@ -215,3 +215,64 @@ def test_gpu_mixed_forces_on_clsman_structure(text_file):
     finally:
         cg.free_host(s64)
         cg.free_host(s32)
+
+
+# ------------------------------------------------ FileAtom reader ----
+
+def tim_setup(tmp_path):
+    """the seeded FileAtom file of the reference fixture and its LJ potential
+    (50 A cutoff: 6 x 7 x 60 boxes over the reference's fixed bounds)"""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_golden import tim_file
+    path = str(tmp_path / "atoms.tim")
+    tim_file(path)
+    return path, cg.lj_potential(20.0, 0.01, 50.0, 63.55)
+
+
+def check_tim(s):
+    from helpers import layout_hash
+    ref = FIX["tim_reader"]
+    v = s.contents
+    assert v.ntot == ref["ntot"] and list(v.nbx) == ref["nbx"]
+    assert layout_hash(s) == ref["layout"]
+    assert float(np.abs(by_id(s, "r")).sum()) == ref["r_sum"]
+    assert np.all(by_id(s, "iType") == 1) and np.all(by_id(s, "mass") == ref["mass"])
+    assert np.all(by_id(s, "p") == 0)
+
+
+def test_tim_reader_host_matches_reference(tmp_path):
+    path, pot = tim_setup(tmp_path)
+    s = cg.read_tim(path, pot, 1.0, None, -1)
+    try:
+        check_tim(s)
+        try:
+            from oracle import ref_lib
+            ref = ref_lib(False)
+        except (FileNotFoundError, OSError):
+            return  # the reference sources are not on this machine
+        rp = ref.lib.refh_lj_make(20.0, 0.01, 50.0, 63.55)
+        sr = ref.lib.refh_read_tim(path.encode(), 1.0, rp)
+        assert slots_equal(s, sr, ("id", "iType", "mass", "r", "p"))
+    finally:
+        cg.free_host(s)
+
+
+def test_tim_reader_bounds_override(tmp_path):
+    path, pot = tim_setup(tmp_path)
+    s = cg.read_tim(path, pot, 1.0, (400.0, 400.0, 3100.0), -1)
+    try:
+        assert list(s.contents.bounds) == [400.0, 400.0, 3100.0]
+        assert s.contents.ntot == 400
+    finally:
+        cg.free_host(s)
+
+
+@pytest.mark.gpu
+def test_tim_reader_device_binning(tmp_path):
+    path, pot = tim_setup(tmp_path)
+    sd = cg.read_tim(path, pot, 1.0, None, 0)
+    try:
+        check_tim(sd)
+    finally:
+        cg.free_host(sd)
