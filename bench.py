@@ -447,7 +447,7 @@ def gpu_arm(args):
 
 # ------------------------------------------------------------ C4: batches
 BATCH = {"replicas": 64, "edge": (8, 24), "temp_k": (100.0, 1200.0), "seed": 4242, "steps": 50,
-         "bf": (1.0, 1.2, 1.4), "skin": (0.2, 0.3, 0.4)}
+         "bf": (1.0, 1.2, 1.4), "skin": (0.3, 0.4, 0.5, 0.6)}
 
 
 def batch_arm(args):

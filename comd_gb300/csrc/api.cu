@@ -968,7 +968,7 @@ bool use_persistent_lists(comdgb_sim *h, const simflat_t *const *sims, int nrep,
         seen[id] = 1;
       }
   }
-  double skin = o->skin > 0.0 ? o->skin : 0.3;
+  double skin = o->skin > 0.0 ? o->skin : 0.5;
   skin = std::min(skin, bmin - h->cutoff);
   if (!(skin >= 0.1)) return false;
   h->skin = skin;
@@ -1232,7 +1232,7 @@ void comdgb_default_opts(comdgb_opts *o) {
   o->n_cheby = CG_NCHEB;
   o->cheby_from_host = 0;
   o->list_mode = COMDGB_LIST_AUTO;
-  o->skin = 0.3;
+  o->skin = 0.5;
 }
 
 int comdgb_round_f32(const double *x, float *y, long n) {

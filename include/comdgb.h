@@ -69,7 +69,8 @@ typedef struct comdgb_opts {
   int n_cheby;     /* Chebyshev terms; only 32 is supported (NUM_CHEBY, docompute.c:56) */
   int cheby_from_host; /* 1: take the series from s->ch_pot; 0: fit them on the GPU */
   int list_mode;       /* COMDGB_LIST_AUTO (default) or COMDGB_LIST_PER_STEP */
-  double skin;         /* persistent-list skin in Angstrom (default 0.3) */
+  double skin;         /* persistent-list skin in Angstrom (default 0.5; at most the
+                          boxes' width minus the cutoff) */
 } comdgb_opts;
 
 /* Neighbour lists.  AUTO keeps lists across steps (cutoff rc + skin, keyed
