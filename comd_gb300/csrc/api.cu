@@ -1127,7 +1127,8 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
     }
   }
   // per-step list: built each step, or (persistent lists) left by pass 1
-  h->nbr = track(h, dalloc<uint16_t>((size_t)h->ntot * h->cap + 8, &err));
+  // (the force-order passes keep their own lists and never read this one)
+  h->nbr = track(h, dalloc<uint16_t>((h->fo.list ? 0 : (size_t)h->ntot * h->cap) + 8, &err));
   h->nbr_n = track(h, dalloc<int>((size_t)h->ntot + 1, &err));
   h->atom_stress = track(h, dalloc<double>((size_t)h->ntot + 1, &err));
   h->nrpart = reduce_partials(h->ntot);
