@@ -23,6 +23,8 @@ OBJDIR = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-I", INCLUDE, "-I", CSRC]
+# extra nvcc flags (e.g. -DCOMDGB_FO_PREFETCH=4 for a parameter sweep)
+NVFLAGS += os.environ.get("COMDGB_NVCC_EXTRA", "").split()
 # (source, extra flags)
 UNITS = [
     ("md_kernels.cu", ["-fmad=false"]),

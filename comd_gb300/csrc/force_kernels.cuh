@@ -912,7 +912,19 @@ __global__ void __launch_bounds__(PASS_THREADS)
 // ---------------------------------------------------------------------------
 constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
 
-constexpr int FO_PREFETCH = 8;    // list lines fetched ahead
+// list lines fetched ahead, unroll of the list walk and pass 2's minimum
+// resident CTAs per SM (chosen by measurement; -D overrides for sweeps)
+#ifndef COMDGB_FO_PREFETCH
+#define COMDGB_FO_PREFETCH 8
+#endif
+#ifndef COMDGB_FO_UNROLL
+#define COMDGB_FO_UNROLL 2
+#endif
+#ifndef COMDGB_FO2_MIN_CTAS
+#define COMDGB_FO2_MIN_CTAS 1
+#endif
+constexpr int FO_PREFETCH = COMDGB_FO_PREFETCH;
+constexpr int FO_UNROLL = COMDGB_FO_UNROLL;
 
 __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -950,7 +962,7 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
   // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1
   // while line t is used (within this atom's list only)
-#pragma unroll 2
+#pragma unroll FO_UNROLL
   for (int t = 0; t < n; t++) {
     if (t + FO_PREFETCH < n) prefetch_l1(lst + (size_t)(t + FO_PREFETCH) * 32);
     const uint32_t p = __ldg(lst + (size_t)t * 32);
@@ -991,7 +1003,7 @@ __global__ void __launch_bounds__(FO1_THREADS, 2)
 constexpr int FO2_MAX_THREADS = 512;  // pass 2 runs with 128, 256 (default) or 512
 
 template <int EVAL, bool MULTI>
-__global__ void __launch_bounds__(FO2_MAX_THREADS)
+__global__ void __launch_bounds__(FO2_MAX_THREADS, COMDGB_FO2_MIN_CTAS)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);
