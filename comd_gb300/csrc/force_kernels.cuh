@@ -912,16 +912,19 @@ __global__ void __launch_bounds__(PASS_THREADS)
 // ---------------------------------------------------------------------------
 constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
 
-// list lines fetched ahead, unroll of the list walk and pass 2's minimum
-// resident CTAs per SM (chosen by measurement; -D overrides for sweeps)
+// list lines fetched ahead, unroll of the list walk and pass 2's register
+// cap (chosen by measurement; -D overrides for sweeps).  Pass 2 runs with
+// CTAs of 128 to 512 threads; its register count follows the cap, not the
+// CTA size (a launch bound of 512 threads let the compiler take 63-88
+// registers, and pass 2 ran 7-70 % slower).
 #ifndef COMDGB_FO_PREFETCH
 #define COMDGB_FO_PREFETCH 8
 #endif
 #ifndef COMDGB_FO_UNROLL
 #define COMDGB_FO_UNROLL 2
 #endif
-#ifndef COMDGB_FO2_MIN_CTAS
-#define COMDGB_FO2_MIN_CTAS 1
+#ifndef COMDGB_FO2_MAXNREG
+#define COMDGB_FO2_MAXNREG 48
 #endif
 constexpr int FO_PREFETCH = COMDGB_FO_PREFETCH;
 constexpr int FO_UNROLL = COMDGB_FO_UNROLL;
@@ -1003,7 +1006,7 @@ __global__ void __launch_bounds__(FO1_THREADS, 2)
 constexpr int FO2_MAX_THREADS = 512;  // pass 2 runs with 128, 256 (default) or 512
 
 template <int EVAL, bool MULTI>
-__global__ void __launch_bounds__(FO2_MAX_THREADS, COMDGB_FO2_MIN_CTAS)
+__global__ void __maxnreg__(COMDGB_FO2_MAXNREG)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);
