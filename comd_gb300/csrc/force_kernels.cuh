@@ -918,16 +918,19 @@ constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
 // CTA size (a launch bound of 512 threads let the compiler take 63-88
 // registers, and pass 2 ran 7-70 % slower).
 #ifndef COMDGB_FO_PREFETCH
-#define COMDGB_FO_PREFETCH 8
+#define COMDGB_FO_PREFETCH 4
 #endif
-#ifndef COMDGB_FO_UNROLL
-#define COMDGB_FO_UNROLL 2
+#ifndef COMDGB_FO1_UNROLL
+#define COMDGB_FO1_UNROLL 4  // pass 1 (and LJ)
+#endif
+#ifndef COMDGB_FO2_UNROLL
+#define COMDGB_FO2_UNROLL 2  // pass 2
 #endif
 #ifndef COMDGB_FO2_MAXNREG
 #define COMDGB_FO2_MAXNREG 48
 #endif
 constexpr int FO_PREFETCH = COMDGB_FO_PREFETCH;
-constexpr int FO_UNROLL = COMDGB_FO_UNROLL;
+constexpr int FO1_UNROLL = COMDGB_FO1_UNROLL, FO2_UNROLL = COMDGB_FO2_UNROLL;
 
 __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
@@ -939,7 +942,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
 // stencil of the atom's current slot instead.
 // MULTI: a batch of replicas (the box size comes from the atom's replica);
 // else replica 0's sizes are kernel-parameter constants (no registers held)
-template <bool NEED_FI, bool MULTI, class F>
+template <bool NEED_FI, bool MULTI, int UNROLL = FO2_UNROLL, class F>
 __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot, float4 pi,
                                             float rc2, F &&fn) {
   const int n = A.fo.n[a];
@@ -965,7 +968,7 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
   // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1
   // while line t is used (within this atom's list only)
-#pragma unroll FO_UNROLL
+#pragma unroll UNROLL
   for (int t = 0; t < n; t++) {
     if (t + FO_PREFETCH < n) prefetch_l1(lst + (size_t)(t + FO_PREFETCH) * 32);
     const uint32_t p = __ldg(lst + (size_t)t * 32);
@@ -996,7 +999,9 @@ __global__ void __launch_bounds__(FO1_THREADS, 2)
     Pass1Acc<float> acc;
     acc.zero();
     eam_pass1_sum(P, seg_sm, acc,
-                  [&](auto &&fn) { fo_for_each<false, MULTI>(A, a, slot, pi, P.rc2, fn); });
+                  [&](auto &&fn) {
+                    fo_for_each<false, MULTI, FO1_UNROLL>(A, a, slot, pi, P.rc2, fn);
+                  });
     const float dF = eam_pass1_store(A, P, acc, slot);
     A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
     A.nbr_n[a] = acc.cnt;
@@ -1016,7 +1021,9 @@ __global__ void __maxnreg__(COMDGB_FO2_MAXNREG)
     Pass2Acc<float> acc;
     acc.zero();
     eam_pass2_sum(P, seg_sm, pi.w, acc,
-                  [&](auto &&fn) { fo_for_each<true, MULTI>(A, a, slot, pi, P.rc2, fn); });
+                  [&](auto &&fn) {
+                    fo_for_each<true, MULTI, FO2_UNROLL>(A, a, slot, pi, P.rc2, fn);
+                  });
     eam_pass2_store(A, acc, slot, a);
   }
 }
@@ -1090,7 +1097,7 @@ __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<
       fz.add(dz * fr);
       sx.add(fr * dx * dx);
     };
-    fo_for_each<false, MULTI>(A, a, slot, A.fo.pos[a], rc2, fn);
+    fo_for_each<false, MULTI, FO1_UNROLL>(A, a, slot, A.fo.pos[a], rc2, fn);
     int ne = A.et.n[b], nonempty = 0;
     for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
     d4 p = A.s.p[slot];
