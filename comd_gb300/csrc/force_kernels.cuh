@@ -988,8 +988,13 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   }
 }
 
+#ifdef COMDGB_FO1_MAXNREG  // sweep variant: a register cap instead of 2 CTAs of 64
+#define FO1_BOUNDS __maxnreg__(COMDGB_FO1_MAXNREG)
+#else
+#define FO1_BOUNDS __launch_bounds__(FO1_THREADS, 2)
+#endif
 template <int EVAL, bool MULTI>
-__global__ void __launch_bounds__(FO1_THREADS, 2)
+__global__ void FO1_BOUNDS
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);
