@@ -414,3 +414,45 @@ def test_persistent_lists_match_per_step_lists(oracle, precision):
     finally:
         c.close()
 
+
+
+@pytest.mark.parametrize("kw", [dict(periodic=False), dict(n=(4, 4, 4)), dict(n=(2, 5, 4))],
+                         ids=["nonperiodic", "two-box-grid", "mixed-grid"])
+def test_mixed_without_force_order(oracle, kw):
+    """mixed precision where force order does not apply (non-periodic, or
+    fewer than 3 boxes on an axis): per-step FP32 lists; forces and a
+    10-step trajectory against the FP64 oracle"""
+    c = Case(oracle, cg.POT_EAM_CHEBY, temp=600.0, amp=0.05, **kw)
+    try:
+        d = c.device(cg.PREC_MIXED)
+        try:
+            assert not d.list_info()[0] or kw.get("periodic", True)
+            d.force()
+            d.download(c.s)
+            c.oracle_force()
+            cmp = compare_forces(c.s, c.o)
+            assert cmp["f_rel_rms"] < MIXED_F_RMS_TOL, cmp
+            e, _ = d.steps(10, 1e-15)
+        finally:
+            d.close()
+        assert c.oracle.steps(c.o, 10, 1e-15, c.kind) == 0
+        assert abs(e - c.o.contents.e) / c.s.contents.ntot < 1e-7
+    finally:
+        c.close()
+
+
+def test_lj_mixed_trajectory(oracle):
+    """LJ in force order over 50 steps (the reference's sign, short enough to
+    stay near the lattice): energy per atom within 1e-6 of the FP64 oracle"""
+    c = Case(oracle, cg.POT_LJ, n=(8, 8, 8), disp=cg.DISP_UNIFORM, amp=0.01 * 2.315, temp=0.0)
+    try:
+        d = c.device(cg.PREC_MIXED)
+        try:
+            assert d.list_info()[0]
+            e, _ = d.steps(50, 1e-15)
+        finally:
+            d.close()
+        assert c.oracle.steps(c.o, 50, 1e-15, c.kind) == 0
+        assert abs(e - c.o.contents.e) / c.s.contents.ntot < 1e-6, (e, c.o.contents.e)
+    finally:
+        c.close()
