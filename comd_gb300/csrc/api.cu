@@ -44,6 +44,13 @@ const char *kGroupName[KG_COUNT] = {"advance_positions+classify", "rebin_plan_ap
                                     "force_pass1",                "force_pass2",
                                     "advance_velocity_positions+classify",
                                     "rebin_plan_apply_2"};
+// parts of a step (enqueue_step)
+enum { PART_NONE = -1, PART_OPEN = 0, PART_MID = 1, PART_CLOSE = 2, PART_FULL = 3 };
+// the middle part of a step sequence with the rebox merged
+enum { KGM_ADV_VPP, KGM_REBIN, KGM_COMPACT, KGM_NBR, KGM_PASS1, KGM_PASS2, KGM_COUNT };
+const char *kGroupNameMerged[KGM_COUNT] = {"advance_velocity_positions+classify",
+                                           "rebin_plan_apply", "compact_atoms", "nbr_build",
+                                           "force_pass1", "force_pass2"};
 
 }  // namespace
 
@@ -93,6 +100,8 @@ void free_all(comdgb_sim *h) {
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
   if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
+  for (cudaGraphExec_t &x : h->part_exec)
+    if (x) cudaGraphExecDestroy(x);
   for (cudaEvent_t e : h->timed_cap_events) cudaEventDestroy(e);
   for (void *p : h->allocs)
     if (p) cudaFree(p);
@@ -374,6 +383,10 @@ void cgapi::drop_graphs(comdgb_sim *h) {
   if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
   h->step_exec = h->force_exec = h->timed_exec = nullptr;
   h->timed_graph = nullptr;
+  for (cudaGraphExec_t &x : h->part_exec) {
+    if (x) cudaGraphExecDestroy(x);
+    x = nullptr;
+  }
 }
 
 // ljForce.c:75-86 parameters (sigma^6 forms of the pair terms)
@@ -519,19 +532,31 @@ void enqueue_rebox(comdgb_sim *h) {
   enqueue_compact(h);
 }
 
-// one velocity-Verlet step (timestep.c:129-132); ev: optional group events
-void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev) {
+// one velocity-Verlet step (timestep.c:129-132); ev: optional group events.
+// part: the whole step (PART_FULL), or with the rebox merged one of
+// PART_OPEN (position half step, rebox, force), PART_MID (velocity step, the
+// closing position half step and the opening one of the next step, one
+// rebox, force) and PART_CLOSE (velocity step, position half step, rebox):
+// n steps are OPEN, n-1 MID, CLOSE.
+void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
   int evi = 0;
   cudaStream_t st = h->stream;
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-  // the atom list is the one made after the previous rebin
-  cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
-  launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass, h->mixed,
-                           true, h->w, h->status, st, true);
-  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-  enqueue_classify_finish(h);
-  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-  enqueue_force_parts(h, ev, evi);  // starts with the atom list of the new layout
+  if (part != PART_CLOSE) {
+    // the atom list is the one made after the previous rebin
+    cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
+    if (part == PART_MID)
+      launch_advance_vpp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass,
+                         h->mixed, h->w, h->status, st);
+    else
+      launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass,
+                               h->mixed, true, h->w, h->status, st, true);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    enqueue_classify_finish(h);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    enqueue_force_parts(h, ev, evi);  // starts with the atom list of the new layout
+    if (part != PART_FULL) return;
+  }
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
   launch_advance_vp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass, h->mixed,
                     h->w, h->status, st);
@@ -554,10 +579,12 @@ int count_kernel_nodes(cudaGraph_t graph) {
   return k;
 }
 
-int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool force) {
+// part: the step part to capture, or PART_NONE
+int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool force) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-  if (step) enqueue_step(h, dt_atu, nullptr);
+  const bool step = part != PART_NONE;
+  if (step) enqueue_step(h, dt_atu, nullptr, part);
   if (force) {
     int evi = 0;
     // the last half step of a step leaves the FP32 copy stale
@@ -569,7 +596,7 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, bool step, bool
     enqueue_reduce(h);
   }
   CK(cudaStreamEndCapture(h->stream, &graph));
-  if (step) h->step_kernels = count_kernel_nodes(graph);
+  if (part == PART_FULL || part == PART_MID) h->step_kernels = count_kernel_nodes(graph);
   if (force) h->force_kernels = count_kernel_nodes(graph);
   if (*exec) cudaGraphExecDestroy(*exec);
   cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
@@ -608,7 +635,7 @@ int finish_force(comdgb_sim *h) {
 int do_force(comdgb_sim *h) {
   if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
   if (!h->force_exec) {
-    int rc = capture(h, &h->force_exec, 0.0, false, true);
+    int rc = capture(h, &h->force_exec, 0.0, PART_NONE, true);
     if (rc) return rc;
   }
   CK(cudaGraphLaunch(h->force_exec, h->stream));
@@ -626,7 +653,13 @@ int do_steps_graph(comdgb_sim *h, int n, double dt, float *ms) {
     h->loop_exec = nullptr;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < n; i++) enqueue_step(h, dt_atu, nullptr);
+    if (!h->merge_rebox)
+      for (int i = 0; i < n; i++) enqueue_step(h, dt_atu, nullptr, PART_FULL);
+    else if (n > 0) {
+      enqueue_step(h, dt_atu, nullptr, PART_OPEN);
+      for (int i = 1; i < n; i++) enqueue_step(h, dt_atu, nullptr, PART_MID);
+      enqueue_step(h, dt_atu, nullptr, PART_CLOSE);
+    }
     CK(cudaStreamEndCapture(h->stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&h->loop_exec, graph, 0);
     cudaGraphDestroy(graph);
@@ -651,15 +684,42 @@ int do_steps_graph(comdgb_sim *h, int n, double dt, float *ms) {
   return rc ? rc : do_force(h);
 }
 
+// the step graphs for dt_atu: one step, or the three parts with the rebox
+// merged
+int ensure_step_graphs(comdgb_sim *h, double dt_atu) {
+  const bool have = h->merge_rebox ? h->part_exec[0] && h->part_exec[1] && h->part_exec[2]
+                                   : h->step_exec != nullptr;
+  if (have && h->graph_dt == dt_atu) return 0;
+  int rc = 0;
+  if (h->merge_rebox)
+    for (int p = 0; p < 3 && !rc; p++) rc = capture(h, &h->part_exec[p], dt_atu, PART_OPEN + p, false);
+  else
+    rc = capture(h, &h->step_exec, dt_atu, PART_FULL, false);
+  if (!rc) h->graph_dt = dt_atu;
+  return rc;
+}
+
+// n steps on stream st from the graphs ensure_step_graphs made
+int launch_steps(comdgb_sim *h, int n, cudaStream_t st) {
+  if (n <= 0) return 0;
+  if (!h->merge_rebox) {
+    for (int i = 0; i < n; i++) CK(cudaGraphLaunch(h->step_exec, st));
+    return 0;
+  }
+  CK(cudaGraphLaunch(h->part_exec[0], st));
+  for (int i = 1; i < n; i++) CK(cudaGraphLaunch(h->part_exec[1], st));
+  CK(cudaGraphLaunch(h->part_exec[2], st));
+  return 0;
+}
+
 int do_steps(comdgb_sim *h, int n, double dt) {
   if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
   double dt_atu = dt * kBohrPerAtu;  // timestep.c:126
-  if (n > 0 && (!h->step_exec || h->graph_dt != dt_atu)) {
-    int rc = capture(h, &h->step_exec, dt_atu, true, false);
+  if (n > 0) {
+    int rc = ensure_step_graphs(h, dt_atu);
+    if (!rc) rc = launch_steps(h, n, h->stream);
     if (rc) return rc;
-    h->graph_dt = dt_atu;
   }
-  for (int i = 0; i < n; i++) CK(cudaGraphLaunch(h->step_exec, h->stream));
   return do_force(h);
 }
 
@@ -906,17 +966,19 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
     CK(cudaEventCreateWithFlags(&h->ev_state, cudaEventDisableTiming));
   }
   const double dt_atu = dt * kBohrPerAtu;  // timestep.c:126
-  if (n > 0 && (!h->step_exec || h->graph_dt != dt_atu)) {
-    int rc = capture(h, &h->step_exec, dt_atu, true, false);
+  if (n > 0) {
+    int rc = ensure_step_graphs(h, dt_atu);
     if (rc) return rc;
-    h->graph_dt = dt_atu;
   }
   if (!h->force_exec) {
-    int rc = capture(h, &h->force_exec, 0.0, false, true);
+    int rc = capture(h, &h->force_exec, 0.0, PART_NONE, true);
     if (rc) return rc;
   }
   cudaStream_t st = h->stream, cs = h->copy_stream;
-  for (int i = 0; i < n; i++) CK(cudaGraphLaunch(h->step_exec, st));
+  {
+    int rc = launch_steps(h, n, st);
+    if (rc) return rc;
+  }
   CK(cudaEventRecord(h->ev_state, st));
   CK(cudaStreamWaitEvent(cs, h->ev_state, 0));
   const size_t nb = (size_t)h->reps[0].nb, ns = nb * CG_MAXATOMS, NS = (size_t)h->nslots;
@@ -1004,6 +1066,7 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
   h->opts = *o;
   h->device = o->device;
   h->mixed = o->precision == COMDGB_PREC_MIXED;
+  h->merge_rebox = h->mixed;
   cudaError_t ce = cudaSetDevice(o->device);
   if (ce != cudaSuccess) {
     delete h;
@@ -1473,9 +1536,21 @@ int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force) {
 }
 
 const char *comdgb_kernel_name(comdgb_sim *h, int k) {
-  (void)h;
+  if (h && h->merge_rebox) return k < 0 || k >= KGM_COUNT ? "" : kGroupNameMerged[k];
   if (k < 0 || k >= KG_COUNT) return "";
   return kGroupName[k];
+}
+
+int comdgb_sim_set_merge_rebox(comdgb_sim *h, int on) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  if (on && !h->mixed) return set_err(COMDGB_ERR_ARG, "the rebox is merged in mixed precision only");
+  if ((bool)on != h->merge_rebox) {
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->stream));
+    drop_graphs(h);
+    h->merge_rebox = on != 0;
+  }
+  return 0;
 }
 
 int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, float *kernel_ms,
@@ -1483,14 +1558,23 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
   if (!h || n <= 0) return set_err(COMDGB_ERR_ARG, "bad argument");
   CK(cudaSetDevice(h->device));
   double dt_atu = dt * kBohrPerAtu;
-  const int NE = KG_COUNT + 1;  // events around the groups
-  if (!h->timed_exec || h->timed_dt != dt_atu) {
+  const bool merged = h->merge_rebox;
+  // events around the groups of the timed graph: one whole step, or the
+  // middle part of a merged sequence (n steps: the opening part, n-1 middle
+  // parts, the closing part; the span covers all three)
+  const int NG = merged ? (int)KGM_COUNT : (int)KG_COUNT, NE = NG + 1;
+  if (merged) {
+    int rc = ensure_step_graphs(h, dt_atu);
+    if (rc) return rc;
+  }
+  const int nt = merged ? n - 1 : n;  // launches of the timed graph
+  if (!h->timed_exec || h->timed_dt != dt_atu || (int)h->timed_cap_events.size() != NE) {
     for (cudaEvent_t e : h->timed_cap_events) cudaEventDestroy(e);
     h->timed_cap_events.assign(NE, nullptr);
     for (int i = 0; i < NE; i++) CK(cudaEventCreate(&h->timed_cap_events[i]));
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    enqueue_step(h, dt_atu, h->timed_cap_events.data());
+    enqueue_step(h, dt_atu, h->timed_cap_events.data(), merged ? PART_MID : PART_FULL);
     CK(cudaStreamEndCapture(h->stream, &graph));
     size_t nn = 0;
     CK(cudaGraphGetNodes(graph, nullptr, &nn));
@@ -1513,42 +1597,53 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
     }
     h->timed_dt = dt_atu;
   }
-  std::vector<cudaEvent_t> evs((size_t)n * NE);
+  std::vector<cudaEvent_t> evs((size_t)nt * NE);
   for (auto &e : evs) CK(cudaEventCreate(&e));
+  cudaEvent_t span0, span1;  // around everything
+  CK(cudaEventCreate(&span0));
+  CK(cudaEventCreate(&span1));
   CK(cudaStreamSynchronize(h->stream));
-  for (int s = 0; s < n; s++) {
+  CK(cudaEventRecord(span0, h->stream));
+  if (merged) CK(cudaGraphLaunch(h->part_exec[PART_OPEN], h->stream));
+  for (int s = 0; s < nt; s++) {
     for (int i = 0; i < NE; i++)
       if (h->timed_nodes[i])
         CK(cudaGraphExecEventRecordNodeSetEvent(h->timed_exec, h->timed_nodes[i],
                                                 evs[(size_t)s * NE + i]));
     CK(cudaGraphLaunch(h->timed_exec, h->stream));
   }
+  if (merged) CK(cudaGraphLaunch(h->part_exec[PART_CLOSE], h->stream));
+  CK(cudaEventRecord(span1, h->stream));
   CK(cudaStreamSynchronize(h->stream));
-  std::vector<double> ksum(KG_COUNT, 0.0);
-  if (step_ms) {
-    float span = 0.f;
-    CK(cudaEventElapsedTime(&span, evs[0], evs[(size_t)(n - 1) * NE + KG_COUNT]));
-    step_ms[n] = span;
-  }
-  for (int s = 0; s < n; s++) {
+  std::vector<double> ksum(NG, 0.0);
+  float span = 0.f, timed = 0.f;
+  CK(cudaEventElapsedTime(&span, span0, span1));
+  cudaEventDestroy(span0);
+  cudaEventDestroy(span1);
+  if (step_ms) step_ms[n] = span;
+  for (int s = 0; s < nt; s++) {
     float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, evs[(size_t)s * NE], evs[(size_t)s * NE + KG_COUNT]));
+    CK(cudaEventElapsedTime(&ms, evs[(size_t)s * NE], evs[(size_t)s * NE + NG]));
     if (step_ms) step_ms[s] = ms;
-    for (int k = 0; k < KG_COUNT; k++) {
+    timed += ms;
+    for (int k = 0; k < NG; k++) {
       float km = 0.f;
       CK(cudaEventElapsedTime(&km, evs[(size_t)s * NE + k], evs[(size_t)s * NE + k + 1]));
       ksum[k] += km;
     }
   }
+  // merged: the last entry is the opening and closing parts together
+  if (merged && step_ms) step_ms[n - 1] = span - timed;
   for (auto &e : evs) cudaEventDestroy(e);
   if (kernel_ms)
-    for (int k = 0; k < KG_COUNT && k < max_kernels; k++) kernel_ms[k] = (float)(ksum[k] / n);
+    for (int k = 0; k < NG && k < max_kernels; k++)
+      kernel_ms[k] = nt > 0 ? (float)(ksum[k] / nt) : 0.f;
   int rc = check_status(h);
   if (rc) return rc;
   // forces of the final positions, as nTimeSteps ends (timestep.c:137)
   rc = do_force(h);
   if (rc) return rc;
-  return KG_COUNT;
+  return NG;
 }
 
 // ---------------------------------------------------------------- drop-in

@@ -324,7 +324,11 @@ struct KSum {
     c = __fsub_rn(__fsub_rn(t, s), y);
     s = t;
   }
+#ifdef COMDGB_KSUM_F32  // sweep variant: combine in FP32 (one conversion, no FP64 subtraction)
+  __device__ __forceinline__ double value() const { return (double)__fsub_rn(s, c); }
+#else
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+#endif
 };
 
 struct DSum {

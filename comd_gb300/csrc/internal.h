@@ -38,10 +38,17 @@ void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int 
                               double rmass, bool mixed, bool classify, const RebinWork &w,
                               int *status, cudaStream_t st, bool use_delta = false);
 // p -= dt_v*f; r += dt_r*p/rmass; classify (the FP32 copy is not refreshed);
-// leaves the position increments in f.xyz and says so in the status word
+// FP64 leaves the position increments in f.xyz and says so in the status word
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
                        cudaStream_t st);
+// merged rebox (mixed precision): p -= dt_v*f, then the closing position
+// half step of one step and the opening one of the next with no rebox
+// between them (one update r += p*(2*dt_r/rmass)), the FP32 copy, the list
+// tracking and classify
+void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
+                        cudaStream_t st);
 // p -= dt_v*f only (advanceVelocity)
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                              cudaStream_t st);

@@ -156,10 +156,16 @@ __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int
   }
 }
 
-// division by the (constant) mass: Markstein (MARK, rinv = RN(1/rmass)) or IEEE
-template <bool MARK>
+// how a half step divides by the (constant) mass.  FP64 follows the
+// reference's roundings: (dt*p)/rmass by Markstein's correctly rounded
+// division (INT_MARK, rinv = RN(1/rmass)) or by IEEE division (INT_IEEE).
+// Mixed precision, whose forces are FP32 anyway, spends the scarce FP64
+// issue slots once per component (INT_FMA): p - dt*f and r + p*(dt/rmass)
+// as one fused multiply-add each, with dt/rmass rounded once on the host.
+enum { INT_IEEE = 0, INT_MARK = 1, INT_FMA = 2 };
+template <int MODE>
 __device__ __forceinline__ double div_mass(double a, double rmass, double rinv) {
-  return MARK ? div_markstein(a, rmass, rinv) : a / rmass;
+  return MODE == INT_MARK ? div_markstein(a, rmass, rinv) : a / rmass;
 }
 
 // Force order: the FP32 position of atom id (now in box b at box-relative
@@ -208,18 +214,34 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
 // by every force computation and upload).  Bit for bit the same positions.
 enum { DELTA_NONE = 0, DELTA_STORE = 1, DELTA_USE = 2 };
 
-template <bool POS, bool VEL, bool MARK>
+// INT_FMA: rinv is the drift coefficient, dt_r/rmass or (twice) 2*dt_r/rmass
+template <bool POS, bool VEL, int MODE>
 __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int *atom_slot,
                                                       int ntot, double dt_v, double dt_r,
                                                       double rmass, double rinv, bool mixed,
                                                       bool write32, bool classify, int delta,
-                                                      RebinWork w, int *status) {
+                                                      bool twice, RebinWork w, int *status) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= ntot) return;
   const int slot = atom_slot[a];
   const int b = slot >> 6;
   d4 r = s.r[slot];
-  if (POS && !VEL && delta == DELTA_USE && *(volatile const int *)(status + ST_DELTA)) {
+  if (MODE == INT_FMA && (POS || VEL)) {
+    d4 p = s.p[slot];
+    if (VEL) {
+      const d4 f = s.f[slot];
+      p.x = fma(-dt_v, f.x, p.x);
+      p.y = fma(-dt_v, f.y, p.y);
+      p.z = fma(-dt_v, f.z, p.z);
+      s.p[slot] = p;
+    }
+    if (POS) {
+      r.x = fma(p.x, rinv, r.x);
+      r.y = fma(p.y, rinv, r.y);
+      r.z = fma(p.z, rinv, r.z);
+      s.r[slot] = r;
+    }
+  } else if (POS && !VEL && delta == DELTA_USE && *(volatile const int *)(status + ST_DELTA)) {
     const d4 dl = s.f[slot];
     r.x = r.x + dl.x;
     r.y = r.y + dl.y;
@@ -238,12 +260,18 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
     }
     if (POS) {
       // advancePositions, timestep.c:104: r + (dt*p)/rmass
-      const double ix = div_mass<MARK>(dt_r * p.x, rmass, rinv);
-      const double iy = div_mass<MARK>(dt_r * p.y, rmass, rinv);
-      const double iz = div_mass<MARK>(dt_r * p.z, rmass, rinv);
+      const double ix = div_mass<MODE>(dt_r * p.x, rmass, rinv);
+      const double iy = div_mass<MODE>(dt_r * p.y, rmass, rinv);
+      const double iz = div_mass<MODE>(dt_r * p.z, rmass, rinv);
       r.x = r.x + ix;
       r.y = r.y + iy;
       r.z = r.z + iz;
+      if (twice) {
+        // the closing half step of one step and the opening one of the next
+        r.x = r.x + ix;
+        r.y = r.y + iy;
+        r.z = r.z + iz;
+      }
       s.r[slot] = r;
       if (VEL && delta == DELTA_STORE) {
         f.x = ix;
@@ -259,7 +287,7 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
       s.pos32[slot] = p32;
       if (w.fo.of_id) fo_track(g, w.fo, b, s.id[slot], r, p32, status);
     }
-    if (!VEL && w.pl.rref) {
+    if ((!VEL || twice) && w.pl.rref) {
       // persistent lists: the half step before a force call decides
       // whether the lists are rebuilt (an atom moved more than skin/2)
       if (persist_stale(g, b, r, w.pl.rref[s.id[slot]], w.pl.half_skin2))
@@ -285,54 +313,75 @@ double mass_reciprocal(double rmass) {
   return 1.0 / rmass;
 }
 
+// the advance kernel for the integration mode of the simulation: mixed
+// precision INT_FMA (rinv becomes the drift coefficient c), FP64 Markstein's
+// division where it is exact for rmass, else IEEE division
+template <bool POS, bool VEL>
+static void launch_advance(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                           double dt_r, double c, double rmass, bool mixed, bool write32,
+                           bool classify, int delta, bool twice, const RebinWork &w, int *status,
+                           cudaStream_t st) {
+  if (ntot <= 0) return;
+  const unsigned nb = atom_blocks(ntot);
+  const double rinv = mass_reciprocal(rmass);
+  if (mixed && POS)
+    advance_kernel<POS, VEL, INT_FMA><<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, dt_v, dt_r,
+                                                          rmass, c, mixed, write32, classify,
+                                                          DELTA_NONE, twice, w, status);
+  else if (rinv != 0.0)
+    advance_kernel<POS, VEL, INT_MARK><<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, dt_v, dt_r,
+                                                           rmass, rinv, mixed, write32, classify,
+                                                           delta, twice, w, status);
+  else
+    advance_kernel<POS, VEL, INT_IEEE><<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, dt_v, dt_r,
+                                                           rmass, rinv, mixed, write32, classify,
+                                                           delta, twice, w, status);
+}
+
 void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
                               double rmass, bool mixed, bool classify, const RebinWork &w,
                               int *status, cudaStream_t st, bool use_delta) {
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
-  if (ntot <= 0) return;
-  const double rinv = mass_reciprocal(rmass);
-  const int delta = use_delta ? DELTA_USE : DELTA_NONE;
-  if (rinv != 0.0)
-    advance_kernel<true, false, true><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, delta, w, status);
-  else
-    advance_kernel<true, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, dt, rmass, rinv, mixed, true, classify, delta, w, status);
+  launch_advance<true, false>(g, s, atom_slot, ntot, 0.0, dt, dt / rmass, rmass, mixed, true,
+                              classify, use_delta ? DELTA_USE : DELTA_NONE, false, w, status, st);
 }
 
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
                        cudaStream_t st) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
-  if (ntot > 0) {
-    const double rinv = mass_reciprocal(rmass);
-    if (rinv != 0.0)
-      advance_kernel<true, true, true><<<atom_blocks(ntot), 256, 0, st>>>(
-          g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, DELTA_STORE, w,
-          status);
-    else
-      advance_kernel<true, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
-          g, s, atom_slot, ntot, dt_v, dt_r, rmass, rinv, mixed, false, true, DELTA_STORE, w,
-          status);
-  }
-  // f.xyz now holds the increments (the next position half step reuses them)
-  cudaMemsetAsync(status + ST_DELTA, 0x01, 1, st);
+  launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, dt_r / rmass, rmass, mixed,
+                             false, true, DELTA_STORE, false, w, status, st);
+  // FP64: f.xyz now holds the increments (the next position half step
+  // reuses them); mixed precision does not keep them
+  if (!mixed) cudaMemsetAsync(status + ST_DELTA, 0x01, 1, st);
+}
+
+void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
+                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
+                        cudaStream_t st) {
+  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
+  // mixed precision: one multiply-add by 2*dt_r/rmass for the two half steps
+  launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, 2.0 * dt_r / rmass, rmass, mixed,
+                             true, true, DELTA_NONE, true, w, status, st);
 }
 
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                              cudaStream_t st) {
   RebinWork none{};
   if (ntot > 0)
-    advance_kernel<false, true, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, DELTA_NONE, none, nullptr);
+    advance_kernel<false, true, INT_IEEE><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, DELTA_NONE, false, none,
+        nullptr);
 }
 
 void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
                      const RebinWork &w, int *status, cudaStream_t st) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   if (ntot > 0)
-    advance_kernel<false, false, false><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, DELTA_NONE, w, status);
+    advance_kernel<false, false, INT_IEEE><<<atom_blocks(ntot), 256, 0, st>>>(
+        g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, DELTA_NONE, false, w,
+        status);
 }
 
 // distinct stencil boxes of b other than b, ascending

@@ -113,6 +113,12 @@ struct comdgb_sim {
   double *centro = nullptr;
   cg::Tune tune;  // launch shapes of the force-order kernels (comdgb_sim_set_launch)
   // graphs
+  // merge_rebox (mixed precision): a sequence of steps reboxes once per step
+  // -- the closing position half step of a step and the opening one of the
+  // next run back to back -- instead of after each half step; part_exec
+  // holds the opening, middle and closing parts of such a sequence
+  bool merge_rebox = false;
+  cudaGraphExec_t part_exec[3] = {nullptr, nullptr, nullptr};
   cudaGraphExec_t step_exec = nullptr;
   cudaGraphExec_t force_exec = nullptr;
   double graph_dt = NAN;

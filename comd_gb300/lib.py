@@ -104,6 +104,7 @@ def _bind(lib):
     L.comdgb_batch_virial.argtypes = [C.c_void_p, C.c_int, D, D, D]
     L.comdgb_sim_atom_stress.argtypes = [C.c_void_p, C.c_int, D]
     L.comdgb_sim_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+    L.comdgb_sim_set_merge_rebox.argtypes = [C.c_void_p, C.c_int]
     L.comdgb_set_lazy.argtypes = [P_SIM, C.c_int]
     L.comdgb_sync_to_host.argtypes = [P_SIM]
     L.comdgb_sync_to_device.argtypes = [P_SIM]
@@ -467,6 +468,11 @@ class DeviceSim:
     def set_launch(self, build_threads=0, build_atoms=0, pass2_threads=0):
         """launch shapes of the force-order kernels (0: default)"""
         check(self.L.comdgb_sim_set_launch(self.h, build_threads, build_atoms, pass2_threads))
+
+    def set_merge_rebox(self, on):
+        """mixed precision: one rebox per step in a sequence of steps (default)
+        or the reference's two (False)"""
+        check(self.L.comdgb_sim_set_merge_rebox(self.h, int(bool(on))))
 
     def list_info(self):
         """(persistent lists in use, skin in A, persistent-list builds since upload)"""

@@ -41,9 +41,12 @@ enum {
 
 /* arithmetic of the force kernels (integration is always FP64) */
 enum {
-  COMDGB_PREC_FP64 = 0,  /* every pair term in double precision */
+  COMDGB_PREC_FP64 = 0,  /* every pair term in double precision; the Verlet
+                            half steps round as the reference does */
   COMDGB_PREC_MIXED = 1  /* FP32 pair terms on box-relative coordinates,
-                            Kahan-compensated FP32 per-atom sums, FP64 totals */
+                            Kahan-compensated FP32 per-atom sums, FP64 totals;
+                            FP64 Verlet half steps as fused multiply-adds,
+                            p - dt*f and r + p*(dt/M) */
 };
 
 /* error codes; -11 and -3 keep the reference's abort codes */
@@ -149,7 +152,11 @@ int comdgb_sim_synchronize(comdgb_sim *h);
  * the library's stream; step_ms[0..n-1] gets each step's device time,
  * step_ms[n] the span from the first step's start to the last step's end,
  * and kernel_ms[k] the average device time of kernel group k of a step
- * (names via comdgb_kernel_name).  Returns the number of groups per step. */
+ * (names via comdgb_kernel_name).  Returns the number of groups per step.
+ * With the rebox merged (comdgb_sim_set_merge_rebox) the steps run as an
+ * opening part, n-1 middle parts and a closing part: step_ms[0..n-2] and
+ * kernel_ms are the middle parts', step_ms[n-1] the opening and closing
+ * parts' together, step_ms[n] the span of all of them. */
 int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms,
                            float *kernel_ms, int max_kernels);
 const char *comdgb_kernel_name(comdgb_sim *h, int k);
@@ -166,6 +173,15 @@ int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
  * 256 or 512; default 256).  Results do not depend on them (the lists and
  * every per-atom sum keep their order); the graphs are recaptured. */
 int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int pass2_threads);
+/* Mixed precision only (its default): a sequence of steps reboxes once per
+ * step instead of after each position half step (timestep.c:129-132 with
+ * reBoxAll at the end of advancePositions, timestep.c:106).  The closing
+ * half step of one step and the opening one of the next become one position
+ * update, r + p*(dt/M), and one rebox follows; the last step of a call still
+ * ends with its own rebox.  The positions differ from the unmerged ones by
+ * roundings, and atoms may sit in other slots of their boxes.  0 restores
+ * the reference's two reboxes per step (FP64 always has them). */
+int comdgb_sim_set_merge_rebox(comdgb_sim *h, int on);
 /* list mode in use (1 persistent, 0 per step), its skin, and the number of
  * persistent-list builds since the last upload */
 int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long *builds);

@@ -93,6 +93,15 @@ def layout_equal(sa, sb):
     return bool(np.array_equal(va["id"][m], vb["id"][m]))
 
 
+def world_by_id(s):
+    """world positions by atom id (box centre plus box-relative r)"""
+    v = slot_views(s)
+    m = occupied_mask(s)
+    out = np.empty((s.contents.ntot, 3))
+    out[v["id"][m]] = (np.repeat(v["dcenter"], 64, axis=0) + v["r"])[m, :3]
+    return out
+
+
 def slots_equal(sa, sb, fields=("id", "iType", "mass", "r", "p")):
     va, vb = slot_views(sa), slot_views(sb)
     m = occupied_mask(sa)

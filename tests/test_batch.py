@@ -81,6 +81,46 @@ def test_batch_mixed_matches_single_runs():
 
 
 @pytest.mark.gpu
+def test_merged_step_paths_agree():
+    """mixed precision with the rebox merged: replays of the step parts, the
+    n steps captured as one graph and the timed run give the same state bit
+    for bit (single simulation and batch)"""
+    pot = cg.eam_potential("cu")
+    o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, True)
+    sims = [make_replicas(pot) for _ in range(3)]
+    try:
+        devs = [cg.DeviceSim(s[0], o) for s in sims]
+        try:
+            e0 = devs[0].steps(12)[0]
+            devs[1].graph_steps(12)
+            e1 = devs[1].energy()[0]
+            step_ms, span, groups = devs[2].timed_steps(12)
+            e2 = devs[2].energy()[0]
+            for d, s in zip(devs, sims):
+                d.download(s[0])
+        finally:
+            for d in devs:
+                d.close()
+        assert e0 == e1 == e2
+        assert slots_equal(sims[0][0], sims[1][0]) and slots_equal(sims[0][0], sims[2][0])
+        assert len(step_ms) == 12 and span >= sum(step_ms) * 0.999
+        assert set(groups) == {"advance_velocity_positions+classify", "rebin_plan_apply",
+                               "compact_atoms", "nbr_build", "force_pass1", "force_pass2"}
+        ba, bb = cg.Batch(sims[0][1:], o), cg.Batch(sims[1][1:], o)
+        try:
+            ba.steps(8)
+            bb.graph_steps(8)
+            assert np.array_equal(ba.energies()[0], bb.energies()[0])
+        finally:
+            ba.close()
+            bb.close()
+    finally:
+        for s in sims:
+            for x in s:
+                cg.free_host(x)
+
+
+@pytest.mark.gpu
 def test_graph_steps_loop_equals_step_replays():
     """n steps captured as one graph give the same FP64 state as n replays of
     the one-step graph (single simulation and batch)"""

@@ -12,8 +12,8 @@ import numpy as np
 import pytest
 
 import comd_gb300 as cg
-from comd_gb300.abi import slot_views
-from helpers import Case, slots_equal
+from comd_gb300.abi import by_id, slot_views
+from helpers import Case, rel_rms, slots_equal, world_by_id
 
 
 def opts():
@@ -85,8 +85,12 @@ def test_eager_force_matches_oracle(oracle):
 def test_eager_calls_keep_lists(oracle, precision):
     """Eager calls upload the host state each time; skin lists built by an
     earlier call stay (maps redone, skin test decides), so 4 eager calls of
-    5 steps give the same state, bit for bit, as 20 steps on a handle, and
-    build the lists only when atoms moved, not once per call."""
+    5 steps give the same state as 20 steps on a handle, and build the lists
+    only when atoms moved, not once per call.  FP64: bit for bit.  Mixed
+    precision reboxes once per step inside a call but after the last half
+    step of each call, so the states agree to roundings: by atom id,
+    energies within 1e-12, world positions within 1e-10 A, momenta and
+    forces within 1e-10."""
     a = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
     b = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
     L = cg.load()
@@ -105,8 +109,17 @@ def test_eager_calls_keep_lists(oracle, precision):
                 ea = L.comdgb_nTimeSteps(5, a.s, 1e-15)
         finally:
             L.comdgb_detach(a.s)
-        assert ea == eb
-        assert slots_equal(a.s, b.s, ("id", "r", "p", "f", "rho", "fi"))
+        if precision == cg.PREC_FP64:
+            assert ea == eb
+            assert slots_equal(a.s, b.s, ("id", "r", "p", "f", "rho", "fi"))
+        else:
+            assert abs(ea - eb) <= 1e-12 * abs(eb), (ea, eb)
+            dw = world_by_id(a.s) - world_by_id(b.s)
+            L = np.array(list(a.s.contents.bounds))
+            dw -= L * np.round(dw / L)
+            assert np.abs(dw).max() < 1e-10
+            for f in ("p", "f"):
+                assert rel_rms(by_id(a.s, f)[:, :3], by_id(b.s, f)[:, :3]) < 1e-10, f
     finally:
         a.close()
         b.close()

@@ -14,7 +14,7 @@ import pytest
 
 import comd_gb300 as cg
 from comd_gb300.abi import by_id, occupied_mask, slot_views
-from helpers import Case, compare_forces, layout_equal, rel_rms, slots_equal
+from helpers import Case, compare_forces, layout_equal, rel_rms, slots_equal, world_by_id
 
 pytestmark = pytest.mark.gpu
 
@@ -454,5 +454,58 @@ def test_lj_mixed_trajectory(oracle):
             d.close()
         assert c.oracle.steps(c.o, 50, 1e-15, c.kind) == 0
         assert abs(e - c.o.contents.e) / c.s.contents.ntot < 1e-6, (e, c.o.contents.e)
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("periodic", [True, False], ids=["force-order", "nonperiodic"])
+def test_merged_rebox_matches_two_reboxes(oracle, periodic):
+    """Mixed precision reboxes once per step inside a sequence of steps (the
+    closing position half step of a step and the opening one of the next run
+    back to back).  Against the reference's two reboxes per step the
+    trajectory differs only by roundings: energy within 1e-9, world
+    positions within 1e-8 A and momenta within 1e-9 by id; every atom ends in
+    its box, so the oracle's reBoxAll moves nothing."""
+    c = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), temp=1200.0, amp=0.05, periodic=periodic)
+    try:
+        res = []
+        for merge, s in ((False, c.s), (True, c.o)):
+            d = cg.DeviceSim(s, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, periodic,
+                                        cheby_from_host=True))
+            try:
+                d.set_merge_rebox(merge)
+                e, _ = d.steps(20, 1e-15)
+                d.download(s)
+            finally:
+                d.close()
+            o2 = oracle.clone(s)
+            try:
+                assert oracle.rebox(o2) == 0
+                assert slots_equal(s, o2)
+            finally:
+                oracle.free(o2)
+            res.append((e, world_by_id(s), by_id(s, "p")[:, :3].copy()))
+        (e0, w0, p0), (e1, w1, p1) = res
+        assert abs(e1 - e0) <= 1e-9 * abs(e0), (e0, e1)
+        dw = w1 - w0
+        if periodic:
+            L = np.array(list(c.s.contents.bounds))
+            dw -= L * np.round(dw / L)
+        assert np.abs(dw).max() < 1e-8
+        assert rel_rms(p1, p0) < 1e-9
+    finally:
+        c.close()
+
+
+def test_merge_rebox_is_mixed_only(oracle):
+    c = Case(oracle, cg.POT_EAM_TABLE, n=(6, 6, 6))
+    try:
+        d = c.device(cg.PREC_FP64)
+        try:
+            with pytest.raises(cg.ComdgbError):
+                d.set_merge_rebox(True)
+            d.set_merge_rebox(False)
+        finally:
+            d.close()
     finally:
         c.close()
