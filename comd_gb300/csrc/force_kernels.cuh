@@ -395,17 +395,13 @@ __device__ __forceinline__ void build_count(const ForceArgs &A, int row, int tot
   if (total > build_cap<MODE>(A)) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
 }
 
-// NT threads per box (CTA), NA atoms tested per candidate load
-template <int MODE, int NT = NB_THREADS, int NA = NB_ATOMS>
-static __global__ void __launch_bounds__(NT) nbr_build32_kernel(ForceArgs A, float rc2) {
-  __shared__ __align__(16) float4 cand[NB_MAXC];
-  __shared__ uint32_t s_mask[NT / 32][NA][NB_CHUNKS];
-  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1], s_code[CG_NNBR];
-  __shared__ BoxOff<float> s_dr[CG_NNBR];
-  if (build_skipped<MODE>(A)) return;
-  const int b = blockIdx.x;
+// the lists of the atoms of box b (not empty): NT threads (the CTA), NA
+// atoms tested per candidate load, the shared arrays of the kernel
+template <int MODE, int NT, int NA>
+__device__ __forceinline__ void build_box32(const ForceArgs &A, float rc2, int b, float4 *cand,
+                                            uint32_t (*s_mask)[NA][NB_CHUNKS], int *s_box,
+                                            int *s_off, int *s_code, BoxOff<float> *s_dr) {
   const int ni = A.s.natoms[b];
-  if (ni == 0) return;
   const int ne = stage_entries<float>(A, b, s_box, s_off, s_dr);
   if (MODE != LIST_ID) order_entries_by_box(ne, s_box, s_off, s_dr, s_code);
   const int ncand = s_off[ne];
@@ -505,6 +501,24 @@ static __global__ void __launch_bounds__(NT) nbr_build32_kernel(ForceArgs A, flo
       if (lane == 0) build_count<MODE>(A, a, total);
     }
     __syncwarp();
+  }
+}
+
+// NT threads per CTA, NA atoms tested per candidate load.  A grid-stride
+// loop over the boxes, the grid sized to the resident CTAs: a launch with no
+// rebuild due (most steps, with skin lists) costs one check per resident
+// CTA instead of one CTA per box.
+template <int MODE, int NT = NB_THREADS, int NA = NB_ATOMS>
+static __global__ void __launch_bounds__(NT) nbr_build32_kernel(ForceArgs A, float rc2) {
+  __shared__ __align__(16) float4 cand[NB_MAXC];
+  __shared__ uint32_t s_mask[NT / 32][NA][NB_CHUNKS];
+  __shared__ int s_box[CG_NNBR], s_off[CG_NNBR + 1], s_code[CG_NNBR];
+  __shared__ BoxOff<float> s_dr[CG_NNBR];
+  if (build_skipped<MODE>(A)) return;
+  for (int b = blockIdx.x; b < A.g.nboxes; b += gridDim.x) {
+    if (A.s.natoms[b] == 0) continue;
+    build_box32<MODE, NT, NA>(A, rc2, b, cand, s_mask, s_box, s_off, s_code, s_dr);
+    __syncthreads();  // the next box restages the shared arrays
   }
 }
 

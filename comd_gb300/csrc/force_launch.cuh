@@ -13,6 +13,9 @@ static size_t nbr_build_smem() {
 static int g_pass_per_sm[2][2];
 static int g_fo_per_sm[3][2];  // force order: [pass 1, pass 2, LJ][eval]
 static int g_num_sms = 1;
+// resident CTAs per SM of the FP32 list builds: force order [64, 128, 256
+// threads][2, 4, 8 atoms per load], per-step and id-keyed lists
+static int g_build_per_sm[3][3], g_build_step_per_sm = 1, g_build_id_per_sm = 1;
 
 template <class K>
 static cudaError_t pass_occupancy(K kernel, size_t smem, int *out, int threads = PASS_THREADS) {
@@ -27,6 +30,30 @@ static cudaError_t pass_occupancy(K kernel, size_t smem, int *out, int threads =
 static size_t pass_smem(int pass, int eval) {
   if (sizeof(FT) != 4 || eval != EVAL_CHEBY) return 0;
   return sizeof(float4) * (pass == 0 ? 2 : 1) * SEG_N;
+}
+
+#if COMDGB_FT_FLOAT
+// resident CTAs per SM of the force-order builds with NT threads, for 2, 4
+// and 8 atoms per load
+template <int NT>
+static cudaError_t build_occupancy_nt(int *out) {
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &out[0], nbr_build32_kernel<LIST_FO, NT, 2>, NT, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out[1], nbr_build32_kernel<LIST_FO, NT, 4>,
+                                                      NT, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&out[2], nbr_build32_kernel<LIST_FO, NT, 8>,
+                                                      NT, 0);
+  for (int i = 0; i < 3; i++) out[i] = out[i] < 1 ? 1 : out[i];
+  return e;
+}
+#endif
+
+// grid of a list build: one CTA per box, capped at the resident CTAs
+static int build_grid(int nboxes, int per_sm) {
+  const long cap = (long)g_num_sms * per_sm;
+  return nboxes < cap ? nboxes : (int)cap;
 }
 
 // called on the current device before any launch or stream capture
@@ -73,6 +100,17 @@ cudaError_t prepare_force_kernels<FT>() {
     if (e == cudaSuccess)
       e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, true>, pass_smem(1, EVAL_CHEBY), &dummy);
     if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<true>, 0, &dummy);
+    if (e == cudaSuccess) e = build_occupancy_nt<64>(g_build_per_sm[0]);
+    if (e == cudaSuccess) e = build_occupancy_nt<128>(g_build_per_sm[1]);
+    if (e == cudaSuccess) e = build_occupancy_nt<256>(g_build_per_sm[2]);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &g_build_step_per_sm, nbr_build32_kernel<LIST_STEP>, NB_THREADS, 0);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &g_build_id_per_sm, nbr_build32_kernel<LIST_ID>, NB_THREADS, 0);
+    g_build_step_per_sm = g_build_step_per_sm < 1 ? 1 : g_build_step_per_sm;
+    g_build_id_per_sm = g_build_id_per_sm < 1 ? 1 : g_build_id_per_sm;
     return e;
   }
 #endif
@@ -95,9 +133,13 @@ static int pass_grid(int pass, int eval, int ntot, bool fo = false,
 // the force-order build at the tuned shape (threads per box x atoms per load)
 template <int NT>
 static void launch_fo_build_nt(const ForceArgs &A, float rc2, int na, cudaStream_t st) {
-  if (na == 2) nbr_build32_kernel<LIST_FO, NT, 2><<<A.g.nboxes, NT, 0, st>>>(A, rc2);
-  else if (na == 8) nbr_build32_kernel<LIST_FO, NT, 8><<<A.g.nboxes, NT, 0, st>>>(A, rc2);
-  else nbr_build32_kernel<LIST_FO, NT, 4><<<A.g.nboxes, NT, 0, st>>>(A, rc2);
+  const int *per_sm = g_build_per_sm[NT == 64 ? 0 : NT == 128 ? 1 : 2];
+  if (na == 2)
+    nbr_build32_kernel<LIST_FO, NT, 2><<<build_grid(A.g.nboxes, per_sm[0]), NT, 0, st>>>(A, rc2);
+  else if (na == 8)
+    nbr_build32_kernel<LIST_FO, NT, 8><<<build_grid(A.g.nboxes, per_sm[2]), NT, 0, st>>>(A, rc2);
+  else
+    nbr_build32_kernel<LIST_FO, NT, 4><<<build_grid(A.g.nboxes, per_sm[1]), NT, 0, st>>>(A, rc2);
 }
 static void launch_fo_build(const ForceArgs &A, float rc2, cudaStream_t st, const Tune *t) {
   const int nt = t ? t->build_threads : NB_THREADS, na = t ? t->build_atoms : NB_ATOMS;
@@ -118,8 +160,11 @@ void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st, const Tun
     }
 #endif
     if (A.pl.vlist)
-      nbr_build32_kernel<LIST_ID><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
-    else nbr_build32_kernel<LIST_STEP><<<A.g.nboxes, NB_THREADS, 0, st>>>(A, (float)rc2);
+      nbr_build32_kernel<LIST_ID><<<build_grid(A.g.nboxes, g_build_id_per_sm), NB_THREADS, 0,
+                                    st>>>(A, (float)rc2);
+    else
+      nbr_build32_kernel<LIST_STEP><<<build_grid(A.g.nboxes, g_build_step_per_sm), NB_THREADS,
+                                      0, st>>>(A, (float)rc2);
   } else {
     if (A.pl.vlist)
       nbr_build64_kernel<LIST_ID><<<A.g.nboxes, NB_THREADS, nbr_build_smem(), st>>>(A, (double)rc2);
