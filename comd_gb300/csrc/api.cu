@@ -1129,15 +1129,14 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
     cudaMemcpy(h->rep_d, h->reps.data(), sizeof(RepGeo) * nrep, cudaMemcpyHostToDevice);
   alloc_slots(h, h->s, true, &err);
   alloc_slots(h, h->w.stage, false, &err);
-  h->w.dest = track(h, dalloc<int>(ns, &err));
   h->w.depmask = track(h, dalloc<uint32_t>(4 * nb, &err));
   h->w.arr_lo = reinterpret_cast<int *>(h->w.depmask + 2 * nb);
   h->w.arr_hi = h->w.arr_lo + nb;
   h->w.n_lo = track(h, dalloc<int>(nb, &err));
-  h->w.n_dep = track(h, dalloc<int>(nb, &err));
   h->w.final_len = track(h, dalloc<int>(nb, &err));
   h->w.final_src = track(h, dalloc<uint8_t>(ns, &err));
-  h->w.dep_order = track(h, dalloc<uint8_t>(ns, &err));
+  h->w.dep_rank = track(h, dalloc<uint8_t>(ns, &err));
+  h->w.arr_list = track(h, dalloc<int>(2 * ns, &err));
   h->et.n = track(h, dalloc<int>(nb, &err));
   h->et.box = track(h, dalloc<int>(nb * CG_NNBR, &err));
   h->et.dr64 = track(h, dalloc<d4>(nb * CG_NNBR, &err));

@@ -9,15 +9,15 @@ namespace cg {
 
 // rebin scratch (one set per simulation)
 struct RebinWork {
-  int *dest;            // [nslots] destination box of a departing atom
   uint32_t *depmask;    // [2*nboxes] departure bits of slots 0-31 / 32-63
   int *arr_lo, *arr_hi; // [nboxes] arrivals from lower / higher boxes (same
                         // allocation as depmask, cleared with it: 4*nboxes words)
   int *n_lo;            // [nboxes] arrivals from lower-index boxes
-  int *n_dep;           // [nboxes]
   int *final_len;       // [nboxes] occupancy after the box's own scan
   uint8_t *final_src;   // [nboxes*64] slot t <- old slot (<64) or placeholder 64+p
-  uint8_t *dep_order;   // [nboxes*64] departure order (old slots)
+  uint8_t *dep_rank;    // [nboxes*64] departure rank of a departing old slot
+  int *arr_list;        // [2*nboxes*64] old slots of the arrivals of a box
+                        // from lower / higher boxes, in claim order
   Slots stage;          // full records of departing atoms, indexed by old slot
   Persist pl;           // id-keyed persistent lists: displacement check
   ForceOrder fo;        // force order: positions to track (fo.of_id null: none)

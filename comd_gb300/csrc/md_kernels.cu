@@ -83,12 +83,14 @@ void launch_entry_table(const Geom &g, const double *dcenter, EntryTab et, int *
 // higher-index boxes are appended after the scan.  Which atoms leave a box,
 // and for where, depends only on each atom's own position, so:
 //   classify  per slot: destination (+-1 box per axis, periodic wrap) and
-//             the moved position; departing records copied to a stage.
-//   plan      per box: count lower arrivals, then replay the swap-remove
-//             scan with placeholders for them -> departure order and the
-//             box's arrangement after its scan.
-//   apply     per box: move stayers, place lower arrivals into their
-//             placeholders and append higher arrivals in source order.
+//             the moved position; departing records copied to a stage, their
+//             old slots listed at the destination (lower / higher sources).
+//   plan      per box: replay the swap-remove scan with placeholders for
+//             the lower arrivals -> each departure's rank and the box's
+//             arrangement after its scan.
+//   apply     per box: move stayers, sort the box's arrival lists by
+//             (source box, departure rank), place the lower arrivals into
+//             their placeholders and append the higher ones.
 // If an arrival from a lower box would itself leave again when rescanned
 // (a move of more than one box per axis, or r+boxsize rounding to boxsize),
 // the plan is invalid and a serial replay of reBoxAll runs instead.
@@ -130,8 +132,13 @@ __device__ __forceinline__ void classify_atom(const Geom &g, const Slots &s, int
   const int jb = box_from_ixyz(R, g.periodic, ixn);
   if (jb < 0 || jb == b) return;
   atomicOr(w.depmask + (slot >> 5), 1u << (slot & 31));
-  atomicAdd(b < jb ? w.arr_lo + jb : w.arr_hi + jb, 1);
-  w.dest[slot] = jb;
+  // the destination's arrival lists (lower / higher source box), in claim
+  // order; 64 or more arrivals overflow the box, which the plan reports
+  const bool from_lo = b < jb;
+  const int k = atomicAdd(from_lo ? w.arr_lo + jb : w.arr_hi + jb, 1);
+  if (k < CG_MAXATOMS)
+    w.arr_list[(from_lo ? 0 : (size_t)g.nboxes * CG_MAXATOMS) + (size_t)jb * CG_MAXATOMS + k] =
+        slot;
   Slots st = w.stage;
   st.id[slot] = s.id[slot];
   st.itype[slot] = s.itype[slot];
@@ -384,32 +391,6 @@ void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, boo
         status);
 }
 
-// distinct stencil boxes of b other than b, ascending
-__device__ int source_boxes(const Geom &g, int b, int *src) {
-  int n = 0;
-  const RepGeo &R = rep_of(g, b);
-  if (R.nb == 1) return 0;
-  int ix[3];
-  box_ixyz(R, b, ix);
-  for (int i = -1; i <= 1; i++)
-    for (int j = -1; j <= 1; j++)
-      for (int k = -1; k <= 1; k++) {
-        int t[3] = {ix[0] + i, ix[1] + j, ix[2] + k};
-        int nb = box_from_ixyz(R, g.periodic, t);
-        if (nb < 0 || nb == b) continue;
-        bool dup = false;
-        for (int q = 0; q < n; q++) dup |= (src[q] == nb);
-        if (dup) continue;
-        int q = n++;
-        while (q > 0 && src[q - 1] > nb) {
-          src[q] = src[q - 1];
-          q--;
-        }
-        src[q] = nb;
-      }
-  return n;
-}
-
 __device__ __forceinline__ unsigned long long box_mask(const RebinWork &w, int b) {
   return (unsigned long long)w.depmask[2 * b] | ((unsigned long long)w.depmask[2 * b + 1] << 32);
 }
@@ -427,14 +408,12 @@ __global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status) {
   const int n_lo = w.arr_lo[b];  // counted by the classify step
   w.n_lo[b] = n_lo;
   if (mask == 0ull && n_lo == 0) {
-    w.n_dep[b] = 0;
     w.final_len[b] = n;
     return;
   }
   int L = n + n_lo;
   if (n_lo > 0 && L >= CG_MAXATOMS) {  // moveAtom aborts at 64 (domains.c:229)
     set_error(status, -11);
-    w.n_dep[b] = 0;
     w.final_len[b] = 0;
     return;
   }
@@ -442,11 +421,11 @@ __global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status) {
   for (int t = 0; t < n; t++) arr[t] = (uint8_t)t;
   for (int t = 0; t < n_lo; t++) arr[n + t] = (uint8_t)(CG_MAXATOMS + t);
   int i = 0, d = 0;
-  uint8_t *order = w.dep_order + (size_t)b * CG_MAXATOMS;
+  uint8_t *rank = w.dep_rank + (size_t)b * CG_MAXATOMS;
   while (i < L) {
     int e = arr[i];
     if (e < CG_MAXATOMS && ((mask >> e) & 1ull)) {
-      order[d++] = (uint8_t)e;
+      rank[e] = (uint8_t)d++;
       arr[i] = arr[--L];
     } else {
       i++;
@@ -454,8 +433,26 @@ __global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status) {
   }
   uint8_t *fs = w.final_src + (size_t)b * CG_MAXATOMS;
   for (int t = 0; t < L; t++) fs[t] = arr[t];
-  w.n_dep[b] = d;
   w.final_len[b] = L;
+}
+
+// the n (< 64) arrivals listed at list (old slots) in the order the
+// reference's scans take them: by source box, then by departure rank there
+__device__ __forceinline__ void sorted_arrivals(const RebinWork &w, const int *list, int n,
+                                                int *src_of) {
+  int key[CG_MAXATOMS];
+  for (int t = 0; t < n; t++) {
+    const int slot = list[t];
+    const int kk = ((slot >> 6) << 6) | w.dep_rank[slot];  // source box, rank
+    int q = t;
+    while (q > 0 && key[q - 1] > kk) {
+      key[q] = key[q - 1];
+      src_of[q] = src_of[q - 1];
+      q--;
+    }
+    key[q] = kk;
+    src_of[q] = slot;
+  }
 }
 
 __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int *status) {
@@ -468,8 +465,6 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
   const int n_hi = w.arr_hi[b];  // counted by the classify step
   if (mask == 0ull && n_lo == 0 && n_hi == 0) return;
   const int L = w.final_len[b];
-  int src[26];
-  const int ns = source_boxes(g, b, src);
   if (n_hi > 0 && L + n_hi >= CG_MAXATOMS) {
     set_error(status, -11);
     return;
@@ -483,41 +478,23 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
       if (e < CG_MAXATOMS && e != t)
         copy_record(s, base + t, s, base + e, mixed, w.map);
     }
+  int src_of[CG_MAXATOMS];
   // 2. lower arrivals into their placeholders, in (source, departure) order
   if (n_lo > 0) {
-    int src_of[CG_MAXATOMS];
-    int p = 0;
-    for (int q = 0; q < ns && src[q] < b; q++) {
-      int sb = src[q];
-      int nd = w.n_dep[sb];
-      const uint8_t *ord = w.dep_order + (size_t)sb * CG_MAXATOMS;
-      for (int d = 0; d < nd; d++) {
-        int j = ord[d];
-        if (w.dest[sb * CG_MAXATOMS + j] == b) src_of[p++] = sb * CG_MAXATOMS + j;
-      }
-    }
+    sorted_arrivals(w, w.arr_list + base, n_lo, src_of);
     for (int t = 0; t < L; t++) {
       int e = fs[t];
       if (e >= CG_MAXATOMS)
         copy_record(s, base + t, w.stage, src_of[e - CG_MAXATOMS], mixed, w.map);
     }
   }
-  // 3. higher arrivals appended
-  int h = 0;
-  for (int q = 0; q < ns; q++) {
-    int sb = src[q];
-    if (sb < b) continue;
-    int nd = w.n_dep[sb];
-    const uint8_t *ord = w.dep_order + (size_t)sb * CG_MAXATOMS;
-    for (int d = 0; d < nd; d++) {
-      int j = ord[d];
-      if (w.dest[sb * CG_MAXATOMS + j] == b) {
-        copy_record(s, base + L + h, w.stage, sb * CG_MAXATOMS + j, mixed, w.map);
-        h++;
-      }
-    }
+  // 3. higher arrivals appended, in (source, departure) order
+  if (n_hi > 0) {
+    sorted_arrivals(w, w.arr_list + (size_t)g.nboxes * CG_MAXATOMS + base, n_hi, src_of);
+    for (int h = 0; h < n_hi; h++)
+      copy_record(s, base + L + h, w.stage, src_of[h], mixed, w.map);
   }
-  s.natoms[b] = L + h;
+  s.natoms[b] = L + n_hi;
 }
 
 // reBoxAll replayed serially on the device (used only when the parallel plan
