@@ -324,11 +324,17 @@ struct KSum {
     c = __fsub_rn(__fsub_rn(t, s), y);
     s = t;
   }
-#ifdef COMDGB_KSUM_F32  // sweep variant: combine in FP32 (one conversion, no FP64 subtraction)
+  // combined in FP32 (one conversion, no FP64 subtraction: FP64 issue slots
+  // are scarce on this GPU); the result is good to half an FP32 ulp
   __device__ __forceinline__ double value() const { return (double)__fsub_rn(s, c); }
-#else
-  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-#endif
+};
+
+// plain FP32 sum (sums of terms of one sign, or without cancellation)
+struct PSum {
+  float s;
+  __device__ __forceinline__ void zero() { s = 0.f; }
+  __device__ __forceinline__ void add(float x) { s = __fadd_rn(s, x); }
+  __device__ __forceinline__ double value() const { return (double)s; }
 };
 
 struct DSum {
