@@ -329,14 +329,6 @@ struct KSum {
   __device__ __forceinline__ double value() const { return (double)__fsub_rn(s, c); }
 };
 
-// plain FP32 sum (sums of terms of one sign, or without cancellation)
-struct PSum {
-  float s;
-  __device__ __forceinline__ void zero() { s = 0.f; }
-  __device__ __forceinline__ void add(float x) { s = __fadd_rn(s, x); }
-  __device__ __forceinline__ double value() const { return (double)s; }
-};
-
 struct DSum {
   double s;
   __device__ __forceinline__ void zero() { s = 0.0; }

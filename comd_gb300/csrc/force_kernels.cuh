@@ -96,13 +96,9 @@ struct PrecT<double> {
 
 template <>
 struct PrecT<float> {
-  // force components cancel strongly (terms of ~1 eV/A to totals of ~0.1):
-  // compensated sums.  The density and the embedding stress are sums of
-  // terms of one sign, and the pair energy is a small part of an atom's
-  // energy: plain FP32 sums, which measured no change of the force error
-  // and the energy drift, and ~7 % less time in pass 1
+  // every per-atom sum Kahan-compensated: forces, energy, density, stress
   typedef KSum Acc;
-  typedef PSum Sca;
+  typedef KSum Sca;
   static __device__ __forceinline__ void pos(const Slots &s, int slot, float &x, float &y,
                                              float &z) {
     float4 v = __ldg(s.pos32 + slot);
