@@ -762,6 +762,14 @@ static int max_occupancy(const int *natoms, size_t nb) {
 
 // forces: also f, rho and fi (a force call or nTimeSteps recomputes them
 // before reading them; reBoxAll and the handle API carry them)
+// the attached owner's arrays move by the zero-copy kernels (one replica)
+bool zero_copy(const comdgb_sim *h, const simflat_t *s) {
+  return h->zc && h->nrep == 1 && s == h->host;
+}
+
+// bytes per occupied slot: id, itype, mass, r, p / f, rho, fi
+constexpr long long kStateBytes = 4 + 4 + 8 + 24 + 24, kForceBytes = 32 + 8 + 8;
+
 int upload_rep(comdgb_sim *h, int r, const simflat_t *s, bool forces = true) {
   cudaStream_t st = h->stream;
   const RepGeo &R = h->reps[r];
@@ -769,10 +777,15 @@ int upload_rep(comdgb_sim *h, int r, const simflat_t *s, bool forces = true) {
   if (s->ntot != h->atom0[r + 1] - h->atom0[r]) return set_err(COMDGB_ERR_ARG, "atom count changed");
   const size_t nb = (size_t)R.nb, ns = nb * CG_MAXATOMS, b0 = (size_t)R.box0;
   const size_t s0 = b0 * CG_MAXATOMS, NS = (size_t)h->nslots;
-  const int w = max_occupancy(s->natoms, nb);
   const cudaMemcpyKind H2D = cudaMemcpyHostToDevice;
   CK(cudaMemcpyAsync(h->s.natoms + b0, s->natoms, nb * sizeof(int), H2D, st));
   h->xfer_h2d += (long long)(nb * sizeof(int));
+  if (zero_copy(h, s)) {
+    launch_zc_upload(h->hs, h->s, (int)nb, forces, st);
+    h->xfer_h2d += (long long)s->ntot * (kStateBytes + (forces ? kForceBytes : 0));
+    return 0;
+  }
+  const int w = max_occupancy(s->natoms, nb);
   CKX(h->s.id + s0, s->id, sizeof(int), nb, w, H2D, xfer_h2d, st);
   if (h->atom0[r]) launch_add_offset(h->s.id + s0, (long)ns, h->atom0[r], st);
   CKX(h->s.itype + s0, s->iType, sizeof(int), nb, w, H2D, xfer_h2d, st);
@@ -908,11 +921,16 @@ int download_forces_rep(comdgb_sim *h, int r, simflat_t *s, int w = -1) {
   cudaStream_t st = h->stream;
   const RepGeo &R = h->reps[r];
   const size_t nb = (size_t)R.nb, s0 = (size_t)R.box0 * CG_MAXATOMS;
-  w = replica_width(h, r, w);
-  const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
-  CKX(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, xfer_d2h, st);
-  CKX(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
-  CKX(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
+  if (zero_copy(h, s)) {
+    launch_zc_download(h->hs, h->s, (int)nb, false, true, st);
+    h->xfer_d2h += (long long)h->ntot * kForceBytes;
+  } else {
+    w = replica_width(h, r, w);
+    const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
+    CKX(s->f, h->s.f + s0, 4 * sizeof(double), nb, w, D2H, xfer_d2h, st);
+    CKX(s->rho, h->s.rho + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
+    CKX(s->fi, h->s.fi + s0, sizeof(double), nb, w, D2H, xfer_d2h, st);
+  }
   CK(cudaStreamSynchronize(st));
   if (h->nrep == 1) {
     s->e = h->e;
@@ -933,6 +951,11 @@ int download_rep(comdgb_sim *h, int r, simflat_t *s) {
   const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
   CK(cudaMemcpyAsync(s->natoms, h->s.natoms + b0, nb * sizeof(int), D2H, st));
   h->xfer_d2h += (long long)(nb * sizeof(int));
+  if (zero_copy(h, s)) {
+    launch_zc_download(h->hs, h->s, (int)nb, true, false, st);
+    h->xfer_d2h += (long long)h->ntot * kStateBytes;
+    return download_forces_rep(h, r, s, -1);
+  }
   CK(cudaStreamSynchronize(st));
   const int w = max_occupancy(s->natoms, nb);
   CKX(s->id, h->s.id + s0, sizeof(int), nb, w, D2H, xfer_d2h, st);
@@ -955,7 +978,8 @@ int download_forces(comdgb_sim *h, simflat_t *s) { return download_forces_rep(h,
 
 // nTimeSteps(n) with all results copied back (one replica).  After the last
 // step the layout, ids, types, masses, r and p are final: they stream to the
-// host on a second stream while the trailing force call runs on the first;
+// host by the copy engines on a second stream while the trailing force call
+// runs on the first (a kernel there would wait for the force kernels' SMs);
 // f, rho and fi follow the force call.
 int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
   if (h->nrep != 1) return set_err(COMDGB_ERR_ARG, "a batch takes comdgb_batch_download");
@@ -1252,9 +1276,21 @@ void pin_host(comdgb_sim *h, simflat_t *s) {
   for (auto &r : regs) ok &= cudaHostRegister(r.p, r.n, cudaHostRegisterDefault) == cudaSuccess;
   cudaGetLastError();
   h->host_pinned = ok;
+  // device addresses of the registered arrays (registration maps them)
+  void *dp[9] = {};
+  bool mapped = ok;
+  for (int i = 1; i < 9 && mapped; i++)
+    mapped = cudaHostGetDevicePointer(&dp[i], regs[i].p, 0) == cudaSuccess && dp[i];
+  cudaGetLastError();
+  if (mapped)
+    h->hs = HostSlots{(int *)dp[1],    (int *)dp[2],    (double *)dp[3],
+                      (double *)dp[4], (double *)dp[5], (double *)dp[6],
+                      (double *)dp[7], (double *)dp[8]};
+  h->zc = mapped && h->nrep == 1;
 }
 
 void unpin_host(comdgb_sim *h, simflat_t *s) {
+  h->zc = false;
   if (!h->host_pinned) return;
   void *ptrs[] = {s->natoms, s->id, s->iType, s->mass, s->r, s->p, s->f, s->rho, s->fi};
   for (void *p : ptrs) cudaHostUnregister(p);

@@ -71,6 +71,22 @@ void launch_add_offset(int *v, long n, int off, cudaStream_t st);
 // per replica: out[2r] energy sum, out[2r+1] stress sum
 void launch_rep_reduce(const ForceArgs &A, double *out, cudaStream_t st);
 void launch_pack3(const d4 *src, double *dst3, long n, cudaStream_t st);
+// A host simflat_t's registered slot arrays as the device addresses them
+// (r, p: 3 doubles per slot; f: 4).
+struct HostSlots {
+  int *id, *itype;
+  double *mass, *r, *p, *f, *rho, *fi;
+};
+// Transfers of the occupied slots only (k < natoms[b]; the device natoms
+// must hold the layout), one warp per box, the kernel reading or writing
+// host memory directly in whole lines: no staging copy, no bytes for empty
+// slots.
+// upload: id, itype, mass, r, p (and f, rho, fi when forces)
+void launch_zc_upload(const HostSlots &hs, Slots s, int nboxes, bool forces, cudaStream_t st);
+// download of the state (id, itype, mass, r, p) or of the force results
+// (f, rho, fi)
+void launch_zc_download(const HostSlots &hs, Slots s, int nboxes, bool state, bool forces,
+                        cudaStream_t st);
 void launch_pos32(const Geom &g, Slots s, cudaStream_t st);
 void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, const double *xyz,
                       const double *pxyz, const int *ids, const int *types, const double *masses,

@@ -905,6 +905,98 @@ __global__ void pack3_kernel(const d4 *src, double *dst3, long n) {
   dst3[3 * i + 2] = v.z;
 }
 
+// One warp per box.  Host memory is written and read in whole lines: the
+// lanes walk each array's occupied range element by element (3 or 4 doubles
+// per slot for r, p, f), so one warp instruction covers 256 contiguous bytes
+// of the host array; the device side gathers or scatters the components of
+// the 32-byte records.
+__device__ __forceinline__ int zc_box(const Slots &s, int nboxes, int &lane) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  lane = threadIdx.x & 31;
+  const long b = t >> 5;
+  if (b >= nboxes) return -1;
+  return (int)b;
+}
+
+__global__ void zc_upload_kernel(HostSlots hs, Slots s, int nboxes, bool forces) {
+  int lane;
+  const int b = zc_box(s, nboxes, lane);
+  if (b < 0) return;
+  const int n = min(max(s.natoms[b], 0), CG_MAXATOMS);
+  const long base = (long)b * CG_MAXATOMS;
+  for (int k = lane; k < n; k += 32) {
+    s.id[base + k] = hs.id[base + k];
+    s.itype[base + k] = hs.itype[base + k];
+    s.mass[base + k] = hs.mass[base + k];
+  }
+  double *rd = reinterpret_cast<double *>(s.r + base), *pd = reinterpret_cast<double *>(s.p + base);
+  const double *rh = hs.r + 3 * base, *ph = hs.p + 3 * base;
+  for (int q = lane; q < 3 * n; q += 32) {
+    const int k = q / 3, c = q - 3 * k;
+    rd[4 * k + c] = rh[q];
+    pd[4 * k + c] = ph[q];
+  }
+  for (int k = lane; k < n; k += 32) {
+    rd[4 * k + 3] = 0.0;
+    pd[4 * k + 3] = 0.0;
+  }
+  if (forces) {
+    double *fd = reinterpret_cast<double *>(s.f + base);
+    const double *fh = hs.f + 4 * base;
+    for (int q = lane; q < 4 * n; q += 32) fd[q] = fh[q];
+    for (int k = lane; k < n; k += 32) {
+      s.rho[base + k] = hs.rho[base + k];
+      s.fi[base + k] = hs.fi[base + k];
+    }
+  }
+}
+
+__global__ void zc_download_kernel(HostSlots hs, Slots s, int nboxes, bool state, bool forces) {
+  int lane;
+  const int b = zc_box(s, nboxes, lane);
+  if (b < 0) return;
+  const int n = min(max(s.natoms[b], 0), CG_MAXATOMS);
+  const long base = (long)b * CG_MAXATOMS;
+  if (state) {
+    for (int k = lane; k < n; k += 32) {
+      hs.id[base + k] = s.id[base + k];
+      hs.itype[base + k] = s.itype[base + k];
+      hs.mass[base + k] = s.mass[base + k];
+    }
+    const double *rd = reinterpret_cast<const double *>(s.r + base);
+    const double *pd = reinterpret_cast<const double *>(s.p + base);
+    double *rh = hs.r + 3 * base, *ph = hs.p + 3 * base;
+    for (int q = lane; q < 3 * n; q += 32) {
+      const int k = q / 3, c = q - 3 * k;
+      rh[q] = rd[4 * k + c];
+      ph[q] = pd[4 * k + c];
+    }
+  }
+  if (forces) {
+    const double *fd = reinterpret_cast<const double *>(s.f + base);
+    double *fh = hs.f + 4 * base;
+    for (int q = lane; q < 4 * n; q += 32) fh[q] = fd[q];
+    for (int k = lane; k < n; k += 32) {
+      hs.rho[base + k] = s.rho[base + k];
+      hs.fi[base + k] = s.fi[base + k];
+    }
+  }
+}
+
+static unsigned zc_blocks(int nboxes) {
+  return (unsigned)(((long)nboxes * 32 + 255) / 256);  // one warp per box
+}
+
+void launch_zc_upload(const HostSlots &hs, Slots s, int nboxes, bool forces, cudaStream_t st) {
+  if (nboxes > 0) zc_upload_kernel<<<zc_blocks(nboxes), 256, 0, st>>>(hs, s, nboxes, forces);
+}
+
+void launch_zc_download(const HostSlots &hs, Slots s, int nboxes, bool state, bool forces,
+                        cudaStream_t st) {
+  if (nboxes > 0)
+    zc_download_kernel<<<zc_blocks(nboxes), 256, 0, st>>>(hs, s, nboxes, state, forces);
+}
+
 void launch_unpack3(const double *src3, d4 *dst, long n, cudaStream_t st) {
   if (n > 0) unpack3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src3, dst, n);
 }

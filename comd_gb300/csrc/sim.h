@@ -137,6 +137,10 @@ struct comdgb_sim {
   double e = 0.0, stress = 0.0;
   simflat_t *host = nullptr;   // drop-in owner (attach)
   bool host_pinned = false;
+  // the owner's registered slot arrays as the device addresses them: its
+  // transfers move the occupied slots only, by kernels (zc)
+  cg::HostSlots hs{};
+  bool zc = false;
   // drop-in lazy mode: the device keeps the state between calls (dev_valid:
   // it holds the current state; host_stale: the host's arrays are older)
   bool lazy = false, dev_valid = false, host_stale = false;

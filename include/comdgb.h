@@ -114,9 +114,13 @@ int comdgb_set_lazy(simflat_t *s, int lazy);
 int comdgb_sync_to_host(simflat_t *s);
 int comdgb_sync_to_device(simflat_t *s);
 /* Bytes copied host -> device and device -> host for s since it was
- * attached.  Copies cover each box's slots up to the largest occupancy, and
- * a force call or nTimeSteps does not upload f, rho and fi (it computes
- * them before reading them). */
+ * attached.  The attached arrays are registered.  Uploads and downloads of
+ * f, rho and fi are kernels that read or write the occupied slots only
+ * (the slots of the ntot atoms, after natoms).  The state after nTimeSteps
+ * streams back by the copy engines while the trailing force call runs, as
+ * 2D copies of each box's slots up to the largest occupancy (so do all
+ * copies where registration fails).  A force call or nTimeSteps does not
+ * upload f, rho and fi (it computes them before reading them). */
 int comdgb_transfer_bytes(simflat_t *s, long long *h2d, long long *d2h);
 
 /* ---------------- device-resident handles ---------------- */

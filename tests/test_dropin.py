@@ -123,3 +123,44 @@ def test_eager_calls_keep_lists(oracle, precision):
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.gpu
+def test_eager_transfers_move_occupied_slots_only(oracle):
+    """An attached simflat_t's arrays are registered; the upload and the
+    download of the force results are kernels that read or write only the
+    occupied slots.  One eager nTimeSteps call uploads natoms and the state
+    of ntot atoms (no f, rho, fi: the call computes them) and downloads
+    natoms, the state (copy engines, beside the trailing force call: each
+    box's slots up to the largest occupancy) and the force results of ntot
+    atoms, byte for byte; the results equal a device handle's."""
+    a = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
+    b = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
+    L = cg.load()
+    try:
+        o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, True, cheby_from_host=True,
+                    per_step_lists=True)
+        d = cg.DeviceSim(b.s, o)
+        try:
+            eb = d.steps(3, 1e-15)[0]
+            d.download(b.s)
+        finally:
+            d.close()
+        assert L.comdgb_attach(a.s, C.byref(o)) == 0
+        try:
+            h0, d0 = C.c_longlong(), C.c_longlong()
+            assert L.comdgb_transfer_bytes(a.s, C.byref(h0), C.byref(d0)) == 0
+            ea = L.comdgb_nTimeSteps(3, a.s, 1e-15)
+            h1, d1 = C.c_longlong(), C.c_longlong()
+            assert L.comdgb_transfer_bytes(a.s, C.byref(h1), C.byref(d1)) == 0
+        finally:
+            L.comdgb_detach(a.s)
+        nb, ntot = a.s.contents.nboxes, a.s.contents.ntot
+        w = int(slot_views(a.s)["natoms"].max())
+        assert h1.value - h0.value == 4 * nb + 64 * ntot
+        assert d1.value - d0.value == 4 * nb + 64 * nb * w + 48 * ntot
+        assert ea == eb
+        assert slots_equal(a.s, b.s, ("id", "iType", "mass", "r", "p", "f", "rho", "fi"))
+    finally:
+        a.close()
+        b.close()
