@@ -301,7 +301,6 @@ def gpu_arm(args):
     h0 = h0_e + mixed.kinetic()
     mixed.steps(args.warmup, dt)
     mixed.synchronize()
-    per_step_kernels, _ = mixed.graph_kernels()
 
     persistent, skin, builds0 = mixed.list_info()
     clocks = ClockSampler(dev)
@@ -435,7 +434,7 @@ def gpu_arm(args):
         "energy_drift_ha_per_atom": drift, "drift_steps": args.drift_steps,
         "neighbour_lists": lists, "pairs_per_step": pairs, "pair_evals_per_s": pairs * args.steps / (span_ms / 1e3),
         "kernel_groups": groups, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": per_step_kernels * args.steps, "clocks": clk,
+        "gpu_launches": mixed.step_launches(args.steps), "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -597,6 +597,7 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool 
   }
   CK(cudaStreamEndCapture(h->stream, &graph));
   if (part == PART_FULL || part == PART_MID) h->step_kernels = count_kernel_nodes(graph);
+  if (part >= PART_OPEN && part <= PART_CLOSE) h->part_kernels[part] = count_kernel_nodes(graph);
   if (force) h->force_kernels = count_kernel_nodes(graph);
   if (*exec) cudaGraphExecDestroy(*exec);
   cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
@@ -1567,6 +1568,20 @@ int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force) {
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   if (per_step) *per_step = h->step_kernels;
   if (per_force) *per_force = h->force_kernels;
+  return 0;
+}
+
+int comdgb_sim_step_launches(comdgb_sim *h, int n, long long *launches) {
+  if (!h || !launches || n < 0) return set_err(COMDGB_ERR_ARG, "bad argument");
+  if (n == 0) {
+    *launches = 0;
+  } else if (h->merge_rebox) {
+    if (!h->part_exec[0]) return set_err(COMDGB_ERR_ARG, "no step has run yet");
+    *launches = h->part_kernels[0] + (long long)(n - 1) * h->part_kernels[1] + h->part_kernels[2];
+  } else {
+    if (!h->step_exec) return set_err(COMDGB_ERR_ARG, "no step has run yet");
+    *launches = (long long)n * h->step_kernels;
+  }
   return 0;
 }
 

@@ -133,6 +133,7 @@ struct comdgb_sim {
   std::vector<cudaGraphNode_t> timed_nodes;  // event record nodes, group order
   std::vector<cudaEvent_t> timed_cap_events;
   int step_kernels = 0, force_kernels = 0;  // kernel nodes per captured graph
+  int part_kernels[3] = {0, 0, 0};           // opening, middle, closing parts
   // host last results
   double e = 0.0, stress = 0.0;
   simflat_t *host = nullptr;   // drop-in owner (attach)

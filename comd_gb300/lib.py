@@ -74,6 +74,7 @@ def _bind(lib):
     L.comdgb_sim_timed_steps.argtypes = [C.c_void_p, C.c_int, C.c_double,
                                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.comdgb_sim_graph_kernels.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.comdgb_sim_step_launches.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]
     L.comdgb_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.comdgb_round_f32.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_long]
     D = C.POINTER(C.c_double)
@@ -479,6 +480,12 @@ class DeviceSim:
         p, sk, n = C.c_int(), C.c_double(), C.c_longlong()
         check(self.L.comdgb_sim_list_info(self.h, C.byref(p), C.byref(sk), C.byref(n)))
         return bool(p.value), sk.value, n.value
+
+    def step_launches(self, n):
+        """kernels a sequence of n steps launches"""
+        v = C.c_longlong()
+        check(self.L.comdgb_sim_step_launches(self.h, n, C.byref(v)))
+        return v.value
 
     def graph_kernels(self):
         a, b = C.c_int(), C.c_int()

@@ -168,7 +168,12 @@ const char *comdgb_kernel_name(comdgb_sim *h, int k);
  * at the first call for this n and dt, then replayed), launched once; *ms
  * (optional) = that launch's device time.  Ends with the force call. */
 int comdgb_sim_graph_steps(comdgb_sim *h, int n, double dt, float *ms);
-/* kernels launched per replay of the captured step graph / force graph */
+/* kernels a sequence of n steps launches (after a step has run): n times
+ * the step graph's, or with the rebox merged the opening part's, n-1 middle
+ * parts' and the closing part's */
+int comdgb_sim_step_launches(comdgb_sim *h, int n, long long *launches);
+/* kernels launched per replay of the captured step graph / force graph
+ * (with the rebox merged: per middle part) */
 int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
 /* Launch shapes of the mixed-precision force-order kernels, for autotuning
  * (0 keeps the default): the skin-list build's threads per box -- the

@@ -96,6 +96,8 @@ def test_merged_step_paths_agree():
             e1 = devs[1].energy()[0]
             step_ms, span, groups = devs[2].timed_steps(12)
             e2 = devs[2].energy()[0]
+            per_step = devs[0].graph_kernels()[0]
+            assert devs[0].step_launches(12) - devs[0].step_launches(11) == per_step > 0
             for d, s in zip(devs, sims):
                 d.download(s[0])
         finally:
