@@ -81,7 +81,6 @@ struct PrecT;
 template <>
 struct PrecT<double> {
   typedef DSum Acc;
-  typedef DSum Sca;
   static __device__ __forceinline__ void pos(const Slots &s, int slot, double &x, double &y,
                                              double &z) {
     d4 v = s.r[slot];
@@ -98,7 +97,6 @@ template <>
 struct PrecT<float> {
   // every per-atom sum Kahan-compensated: forces, energy, density, stress
   typedef KSum Acc;
-  typedef KSum Sca;
   static __device__ __forceinline__ void pos(const Slots &s, int slot, float &x, float &y,
                                              float &z) {
     float4 v = __ldg(s.pos32 + slot);
@@ -774,8 +772,7 @@ __device__ __forceinline__ void stage_seg(float4 *sm, const float4 *src, int nre
 // ---------------------------------------------------------------------------
 template <class T>
 struct Pass1Acc {
-  typename PrecT<T>::Acc fx, fy, fz;
-  typename PrecT<T>::Sca ep, rh;
+  typename PrecT<T>::Acc fx, fy, fz, ep, rh;
   int cnt;
   __device__ __forceinline__ void zero() {
     fx.zero(); fy.zero(); fz.zero(); ep.zero(); rh.zero();
@@ -860,8 +857,7 @@ __global__ void __launch_bounds__(PASS_THREADS)
 // ---------------------------------------------------------------------------
 template <class T>
 struct Pass2Acc {
-  typename PrecT<T>::Acc fx, fy, fz;
-  typename PrecT<T>::Sca sx;
+  typename PrecT<T>::Acc fx, fy, fz, sx;
   __device__ __forceinline__ void zero() { fx.zero(); fy.zero(); fz.zero(); sx.zero(); }
   __device__ __forceinline__ void add(T wr, T dx, T dy, T dz) {
     fx.add(wr * dx);
