@@ -763,9 +763,14 @@ static int max_occupancy(const int *natoms, size_t nb) {
 
 // forces: also f, rho and fi (a force call or nTimeSteps recomputes them
 // before reading them; reBoxAll and the handle API carry them)
-// the attached owner's arrays move by the zero-copy kernels (one replica)
+// the attached owner's arrays move by the zero-copy kernels (one replica),
+// as long as they are still the arrays registered at attach
 bool zero_copy(const comdgb_sim *h, const simflat_t *s) {
-  return h->zc && h->nrep == 1 && s == h->host;
+  if (!h->zc || h->nrep != 1 || s != h->host) return false;
+  const void *now[9] = {s->natoms, s->id, s->iType, s->mass, s->r, s->p, s->f, s->rho, s->fi};
+  for (int i = 0; i < 9; i++)
+    if (now[i] != h->pinned[i]) return false;
+  return true;
 }
 
 // bytes per occupied slot: id, itype, mass, r, p / f, rho, fi
@@ -1273,10 +1278,18 @@ void pin_host(comdgb_sim *h, simflat_t *s) {
   } regs[] = {{s->natoms, nb * 4},     {s->id, ns * 4}, {s->iType, ns * 4}, {s->mass, ns * 8},
               {s->r, ns * 24},         {s->p, ns * 24}, {s->f, ns * 32},    {s->rho, ns * 8},
               {s->fi, ns * 8}};
-  bool ok = true;
-  for (auto &r : regs) ok &= cudaHostRegister(r.p, r.n, cudaHostRegisterDefault) == cudaSuccess;
+  bool ok = true, done[9] = {};
+  for (int i = 0; i < 9; i++) {
+    done[i] = cudaHostRegister(regs[i].p, regs[i].n, cudaHostRegisterDefault) == cudaSuccess;
+    ok &= done[i];
+  }
   cudaGetLastError();
   h->host_pinned = ok;
+  for (int i = 0; i < 9; i++) {
+    if (!ok && done[i]) cudaHostUnregister(regs[i].p);  // all or none stay registered
+    h->pinned[i] = ok ? regs[i].p : nullptr;
+  }
+  cudaGetLastError();
   // device addresses of the registered arrays (registration maps them)
   void *dp[9] = {};
   bool mapped = ok;
@@ -1291,10 +1304,11 @@ void pin_host(comdgb_sim *h, simflat_t *s) {
 }
 
 void unpin_host(comdgb_sim *h, simflat_t *s) {
+  (void)s;
   h->zc = false;
   if (!h->host_pinned) return;
-  void *ptrs[] = {s->natoms, s->id, s->iType, s->mass, s->r, s->p, s->f, s->rho, s->fi};
-  for (void *p : ptrs) cudaHostUnregister(p);
+  for (void *p : h->pinned)  // the arrays registered at attach
+    if (p) cudaHostUnregister(p);
   cudaGetLastError();
   h->host_pinned = false;
 }

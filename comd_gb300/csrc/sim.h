@@ -142,6 +142,7 @@ struct comdgb_sim {
   // transfers move the occupied slots only, by kernels (zc)
   cg::HostSlots hs{};
   bool zc = false;
+  void *pinned[9] = {};  // the host arrays registered at attach (natoms .. fi)
   // drop-in lazy mode: the device keeps the state between calls (dev_valid:
   // it holds the current state; host_stale: the host's arrays are older)
   bool lazy = false, dev_valid = false, host_stale = false;

@@ -164,3 +164,40 @@ def test_eager_transfers_move_occupied_slots_only(oracle):
     finally:
         a.close()
         b.close()
+
+
+@pytest.mark.gpu
+def test_eager_call_after_host_array_moved(oracle):
+    """The transfer kernels address the arrays registered at attach; when the
+    caller moves one (here r to a new buffer) the call copies from the
+    current pointers instead, with the same results as a device handle."""
+    a = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
+    b = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), amp=0.05, temp=600.0)
+    L = cg.load()
+    try:
+        o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, True, cheby_from_host=True,
+                    per_step_lists=True)
+        d = cg.DeviceSim(b.s, o)
+        try:
+            eb = d.steps(3, 1e-15)[0]
+            d.download(b.s)
+        finally:
+            d.close()
+        assert L.comdgb_attach(a.s, C.byref(o)) == 0
+        # the address itself: a pointer field read from a ctypes structure
+        # is a view of the field and would follow the reassignment
+        orig = C.cast(a.s.contents.r, C.c_void_p).value
+        moved = np.array(slot_views(a.s)["r"], copy=True)
+        try:
+            a.s.contents.r = moved.ctypes.data_as(C.POINTER(C.c_double))
+            ea = L.comdgb_nTimeSteps(3, a.s, 1e-15)
+        finally:
+            a.s.contents.r = C.cast(orig, C.POINTER(C.c_double))
+            L.comdgb_detach(a.s)
+        assert C.cast(a.s.contents.r, C.c_void_p).value == orig
+        slot_views(a.s)["r"][:] = moved
+        assert ea == eb
+        assert slots_equal(a.s, b.s, ("id", "iType", "mass", "r", "p", "f", "rho", "fi"))
+    finally:
+        a.close()
+        b.close()
