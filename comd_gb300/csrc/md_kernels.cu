@@ -643,7 +643,10 @@ void launch_rebuild_done(int *status, cudaStream_t st) {
 // compaction: box_start = exclusive scan of natoms; atom_slot[a] = slot
 // ---------------------------------------------------------------------------
 #define CP_THREADS 256
-#define CP_PER 2
+#ifndef COMDGB_CP_PER
+#define COMDGB_CP_PER 1  // boxes per thread in the compaction scans (1: 20 us at 110,592 boxes, 2: 27, 4: 37)
+#endif
+#define CP_PER COMDGB_CP_PER
 #define CP_CHUNK (CP_THREADS * CP_PER)
 
 int compact_partials(int nboxes) { return (nboxes + CP_CHUNK - 1) / CP_CHUNK; }
