@@ -357,8 +357,11 @@ def gpu_arm(args):
         cg.lib.check(L.comdgb_transfer_bytes(s, C.byref(b0[0]), C.byref(b0[1])))
         dist.barrier()
         t0 = time.perf_counter()
+        call_ms = []
         for _ in range(calls):
+            tc = time.perf_counter()
             e = L.comdgb_nTimeSteps(per_call, s, dt)
+            call_ms.append((time.perf_counter() - tc) * 1e3)
             if e != e:
                 raise cg.ComdgbError(-30, cg.lib.last_error())
         t1 = time.perf_counter()
@@ -375,7 +378,8 @@ def gpu_arm(args):
         e2e = {"value": dist.sum(natoms * calls * per_call) / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": h2d // per_call, "d2h_bytes_per_step": d2h // per_call,
                "call": f"comdgb_nTimeSteps({per_call}) on a host simflat_t (pinned), "
-                       "full state copied up and back every call"}
+                       "full state copied up and back every call",
+               "call_ms": [round(x, 2) for x in call_ms]}
 
     # roofline of the dominant kernel group
     peaks = measured_peaks()
