@@ -7,6 +7,7 @@
  */
 #define _POSIX_C_SOURCE 200112L
 #include <math.h>
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -334,6 +335,48 @@ static char *next_line(char **cur, size_t *len) {
   return l;
 }
 
+/* The atom lines of a clsman file, parsed by up to 16 threads: each takes a
+ * contiguous range of lines (already cut off with NULs) and reads them with
+ * the reference's format. */
+struct clsman_job {
+  char **lines;
+  double *xyz, *pxyz;
+  int lo, hi, bad;
+};
+
+static void *clsman_parse(void *arg) {
+  struct clsman_job *j = (struct clsman_job *)arg;
+  for (int i = j->lo; i < j->hi && !j->bad; i++) {
+    int itype = 0;
+    double *x = j->xyz + 3 * (size_t)i, *p = j->pxyz + 3 * (size_t)i;
+    if (sscanf(j->lines[i], "%lg %lg %lg %d %lg %lg %lg", &x[0], &x[1], &x[2], &itype, &p[0],
+               &p[1], &p[2]) != 7)
+      j->bad = 1;
+  }
+  return NULL;
+}
+
+static int clsman_parse_all(char **lines, int natoms, double *xyz, double *pxyz) {
+  int nt = natoms / 8192;
+  nt = nt < 1 ? 1 : nt > 16 ? 16 : nt;
+  struct clsman_job job[16];
+  pthread_t tid[16];
+  int started[16] = {0};
+  for (int t = 0; t < nt; t++) {
+    job[t] = (struct clsman_job){lines, xyz, pxyz, (int)((long)natoms * t / nt),
+                                 (int)((long)natoms * (t + 1) / nt), 0};
+    started[t] = t > 0 && pthread_create(&tid[t], NULL, clsman_parse, &job[t]) == 0;
+  }
+  for (int t = 0; t < nt; t++)
+    if (!started[t]) clsman_parse(&job[t]);  /* range 0, or a thread that did not start */
+  int bad = 0;
+  for (int t = 0; t < nt; t++) {
+    if (started[t]) pthread_join(tid[t], NULL);
+    bad |= job[t].bad;
+  }
+  return bad ? COMDGB_ERR_IO : 0;
+}
+
 /* fromFileGzip / fromFileASCII (read.c:155-241): a clsman file -- "natoms
  * nmove", a comment line, the periodic bounds, then one line "x y z itype px
  * py pz" per atom -- into a new simflat_t with allocDomains' grid for box
@@ -346,6 +389,7 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   simflat_t *s = NULL;
   double *xyz = NULL, *pxyz = NULL, *masses = NULL;
   int *ids = NULL, *types = NULL;
+  char **lines = NULL;
   if (!path || !pot) {
     if (status) *status = COMDGB_ERR_ARG;
     return NULL;
@@ -386,16 +430,13 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   masses = (double *)malloc(n * sizeof(double) + 8);
   ids = (int *)malloc(n * sizeof(int) + 4);
   types = (int *)malloc(n * sizeof(int) + 4);
-  if (!xyz || !pxyz || !masses || !ids || !types) {
+  lines = (char **)malloc(n * sizeof(char *) + 8);
+  if (!xyz || !pxyz || !masses || !ids || !types || !lines) {
     st = COMDGB_ERR_NOMEM;
     goto done;
   }
   for (int i = 0; i < natoms; i++) {
-    int itype = 0;
-    double *x = xyz + 3 * (size_t)i, *p = pxyz + 3 * (size_t)i;
-    if (!(l = next_line(&cur, NULL)) ||
-        sscanf(l, "%lg %lg %lg %d %lg %lg %lg", &x[0], &x[1], &x[2], &itype, &p[0], &p[1],
-               &p[2]) != 7) {
+    if (!(lines[i] = next_line(&cur, NULL))) {
       st = COMDGB_ERR_IO;
       goto done;
     }
@@ -403,6 +444,7 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
     types[i] = 0; /* read.c:236: putAtomInBox(s, i, 1, 0, mass, ...) */
     masses[i] = pot->mass;
   }
+  if ((st = clsman_parse_all(lines, natoms, xyz, pxyz))) goto done;
   if (device >= 0) {
     st = comdgb_put_atoms(s, natoms, xyz, pxyz, ids, types, masses, device);
   } else {
@@ -411,6 +453,7 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   }
 done:
   free(buf);
+  free(lines);
   free(xyz);
   free(pxyz);
   free(masses);

@@ -129,6 +129,39 @@ def test_host_reader_matches_oracle_and_reference(oracle, pots_dir, text_file):
         oracle.free(so)
 
 
+def test_host_reader_262k_matches_oracle(oracle, pots_dir, text_dir):
+    """the 262,144-atom file, whose atom lines the library parses on 16
+    threads: the same slots as the oracle's serial reader"""
+    pot = cg.eam_potential("ag")
+    path = str(text_dir / "262k.inp")
+    sh = cg.read_clsman(path, pot, 1.0, -1)
+    so = oracle.read_clsman(path, oracle.eam(pots_dir, "ag"), 1.0)
+    try:
+        assert sh.contents.ntot == 262144
+        assert slots_equal(sh, so, ("id", "iType", "mass", "r", "p"))
+    finally:
+        cg.free_host(sh)
+        oracle.free(so)
+
+
+def test_host_reader_reports_a_bad_atom_line(oracle, tmp_path, text_dir):
+    """a malformed atom line in the middle of a large file is an I/O error
+    (-33), as a short file is, whichever thread parses it"""
+    pot = cg.eam_potential("ag")
+    lines = (text_dir / "262k.inp").read_text().split("\n")
+    lines[3 + 200000] = "1.0 2.0 x"
+    bad = tmp_path / "bad.inp"
+    bad.write_text("\n".join(lines))
+    with pytest.raises(cg.ComdgbError) as ei:
+        cg.read_clsman(str(bad), pot, 1.0, -1)
+    assert ei.value.code == -33  # COMDGB_ERR_IO
+    short = tmp_path / "short.inp"
+    short.write_text("\n".join(lines[:3 + 1000]))
+    with pytest.raises(cg.ComdgbError) as ei:
+        cg.read_clsman(str(short), pot, 1.0, -1)
+    assert ei.value.code == -33
+
+
 @pytest.mark.gpu
 def test_gpu_binning_of_clsman_file_matches_host(text_file):
     pot = cg.eam_potential("ag")
