@@ -455,10 +455,18 @@ __device__ __forceinline__ void sorted_arrivals(const RebinWork &w, const int *l
   }
 }
 
+__device__ void rebin_serial(const Geom &g, const Slots &s, bool mixed, int *status,
+                             const SlotMap &slot_of);
+
+// the plan stood down (a move of more than one box): thread 0 replays
+// reBoxAll serially instead
 __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int *status) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (*(volatile int *)(status + ST_REBIN_SERIAL)) {
+    if (b == 0) rebin_serial(g, s, mixed, status, w.map);
+    return;
+  }
   if (b >= g.nboxes) return;
-  if (*(volatile int *)(status + ST_REBIN_SERIAL)) return;
   if (*(volatile int *)(status + ST_ERROR)) return;
   const unsigned long long mask = box_mask(w, b);
   const int n_lo = w.n_lo[b];
@@ -499,9 +507,8 @@ __global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int
 
 // reBoxAll replayed serially on the device (used only when the parallel plan
 // cannot reproduce it); the reference algorithm, statement for statement
-__global__ void rebin_serial_kernel(Geom g, Slots s, bool mixed, int *status, SlotMap slot_of) {
-  if (!*(volatile int *)(status + ST_REBIN_SERIAL)) return;
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void rebin_serial(const Geom &g, const Slots &s, bool mixed, int *status,
+                             const SlotMap &slot_of) {
   status[ST_SERIAL_RUNS] += 1;
   for (int b = 0; b < g.nboxes; b++) {
     const RepGeo &R = rep_of(g, b);
@@ -554,7 +561,6 @@ void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w,
   unsigned nb = (unsigned)((g.nboxes + 127) / 128);
   rebin_plan_kernel<<<nb, 128, 0, st>>>(g, s, w, status);
   rebin_apply_kernel<<<nb, 128, 0, st>>>(g, s, mixed, w, status);
-  rebin_serial_kernel<<<1, 32, 0, st>>>(g, s, mixed, status, w.map);
 }
 
 // ---------------------------------------------------------------------------
