@@ -919,7 +919,7 @@ __global__ void pack3_kernel(const d4 *src, double *dst3, long n) {
 // per slot for r, p, f), so one warp instruction covers 256 contiguous bytes
 // of the host array; the device side gathers or scatters the components of
 // the 32-byte records.
-__device__ __forceinline__ int zc_box(const Slots &s, int nboxes, int &lane) {
+__device__ __forceinline__ int zc_box(int nboxes, int &lane) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   lane = threadIdx.x & 31;
   const long b = t >> 5;
@@ -929,7 +929,7 @@ __device__ __forceinline__ int zc_box(const Slots &s, int nboxes, int &lane) {
 
 __global__ void zc_upload_kernel(HostSlots hs, Slots s, int nboxes, bool forces) {
   int lane;
-  const int b = zc_box(s, nboxes, lane);
+  const int b = zc_box(nboxes, lane);
   if (b < 0) return;
   const int n = min(max(s.natoms[b], 0), CG_MAXATOMS);
   const long base = (long)b * CG_MAXATOMS;
@@ -962,7 +962,7 @@ __global__ void zc_upload_kernel(HostSlots hs, Slots s, int nboxes, bool forces)
 
 __global__ void zc_download_kernel(HostSlots hs, Slots s, int nboxes, bool state, bool forces) {
   int lane;
-  const int b = zc_box(s, nboxes, lane);
+  const int b = zc_box(nboxes, lane);
   if (b < 0) return;
   const int n = min(max(s.natoms[b], 0), CG_MAXATOMS);
   const long base = (long)b * CG_MAXATOMS;
