@@ -833,7 +833,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--drift-steps", type=int, default=1000)
-    ap.add_argument("--e2e-calls", type=int, default=10)
+    ap.add_argument("--e2e-calls", type=int, default=20)
     ap.add_argument("--cpu-cells", type=int, default=30)
     ap.add_argument("--cells", type=int, default=0,
                     help="override the lattice to N^3 unit cells (profiling captures only)")

@@ -443,17 +443,19 @@ int check_status(comdgb_sim *h) {
 
 // ---- kernel groups of one step --------------------------------------------
 
-void enqueue_classify_finish(comdgb_sim *h) {
-  launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, h->stream);
+// lazy: the rebox only when a list rebuild is due (see enqueue_step)
+void enqueue_classify_finish(comdgb_sim *h, bool lazy = false) {
+  launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, h->stream,
+                      lazy ? h->status + ST_REBUILD : nullptr);
 }
 
-void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
+void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_rebox = false) {
   // ev (optional) records after each group: compact, nbr, pass1, pass2
   ForceArgs A = force_args(h);
   cudaStream_t st = h->stream;
   cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
-                 st);
+                 st, lazy_rebox ? h->status + ST_REBUILD : nullptr);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   const int pot = h->opts.potential;
   // persistent lists are built with rc + skin, and only when a rebuild is due
@@ -538,23 +540,34 @@ void enqueue_rebox(comdgb_sim *h) {
 // closing position half step and the opening one of the next step, one
 // rebox, force) and PART_CLOSE (velocity step, position half step, rebox):
 // n steps are OPEN, n-1 MID, CLOSE.
+// Force order (mixed precision, skin lists) reads no layout between list
+// builds -- the passes walk the lists with positions relative to the build
+// boxes -- so the OPEN and MID parts rebox (and recompact) only when a
+// rebuild is due; until then atoms keep their boxes and slots, a little
+// outside them.  The CLOSE part always reboxes, so a call ends boxed.
 void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
   int evi = 0;
   cudaStream_t st = h->stream;
+  const bool lazy = h->fo.list && (part == PART_OPEN || part == PART_MID);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   if (part != PART_CLOSE) {
     // the atom list is the one made after the previous rebin
     cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
     if (part == PART_MID)
       launch_advance_vpp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass,
-                         h->mixed, h->w, h->status, st);
+                         h->mixed, h->w, h->status, st, !lazy);
     else
       launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass,
-                               h->mixed, true, h->w, h->status, st, true);
+                               h->mixed, !lazy, h->w, h->status, st, true);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-    enqueue_classify_finish(h);
+    // lazily: classify too only when the rebuild is due (the half step above
+    // has decided that)
+    if (lazy)
+      launch_classify(h->g, h->s, h->atom_slot, h->ntot, h->mixed, h->w, h->status, st,
+                      h->status + ST_REBUILD);
+    enqueue_classify_finish(h, lazy);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-    enqueue_force_parts(h, ev, evi);  // starts with the atom list of the new layout
+    enqueue_force_parts(h, ev, evi, lazy);  // starts with the atom list of the new layout
     if (part != PART_FULL) return;
   }
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);

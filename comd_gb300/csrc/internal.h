@@ -48,18 +48,24 @@ void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, d
 // tracking and classify
 void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                         double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
-                        cudaStream_t st);
+                        cudaStream_t st, bool classify = true);
 // p -= dt_v*f only (advanceVelocity)
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                              cudaStream_t st);
-// classify only (reBoxAll without a position update)
+// classify only (reBoxAll without a position update); only_if (optional):
+// a status word, nothing is classified while it is 0
 void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
-                     const RebinWork &w, int *status, cudaStream_t st);
-// plan + apply + serial fallback; must follow a classify launch
+                     const RebinWork &w, int *status, cudaStream_t st,
+                     const int *only_if = nullptr);
+// plan + apply + serial fallback; must follow a classify launch.  only_if
+// (optional): a status word; while it is 0 the launches do nothing (the
+// atoms stay in the boxes they had, their box-relative positions as the
+// half steps left them)
 void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
-                         cudaStream_t st);
+                         cudaStream_t st, const int *only_if = nullptr);
+// the atom list of the layout; only_if as above (the layout did not change)
 void launch_compact(const Geom &g, const int *natoms, int *box_start, int *atom_slot, int ntot,
-                    int *partials, int npart, cudaStream_t st);
+                    int *partials, int npart, cudaStream_t st, const int *only_if = nullptr);
 int compact_partials(int nboxes);
 void launch_reduce(const ForceArgs &A, double *partials, long long *ipartials, int npart,
                    double *out, long long *iout, cudaStream_t st);

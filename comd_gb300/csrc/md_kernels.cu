@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstring>
 
+#include <algorithm>
+
 #include "internal.h"
 
 namespace cg {
@@ -366,11 +368,11 @@ void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, d
 
 void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                         double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
-                        cudaStream_t st) {
-  cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
+                        cudaStream_t st, bool classify) {
+  if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   // mixed precision: one multiply-add by 2*dt_r/rmass for the two half steps
   launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, 2.0 * dt_r / rmass, rmass, mixed,
-                             true, true, DELTA_NONE, true, w, status, st);
+                             true, classify, DELTA_NONE, true, w, status, st);
 }
 
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
@@ -382,13 +384,30 @@ void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int n
         nullptr);
 }
 
+// only_if (optional): a status word; the launch does nothing while it is 0
+__device__ __forceinline__ bool stood_down(const int *only_if) {
+  return only_if && !*(volatile const int *)only_if;
+}
+
+// classify only, grid-stride over the atoms (a stood-down launch costs one
+// check per CTA)
+__global__ void __launch_bounds__(256) classify_kernel(Geom g, Slots s, const int *atom_slot,
+                                                       int ntot, bool mixed, RebinWork w,
+                                                       int *status, const int *only_if) {
+  if (stood_down(only_if)) return;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < ntot; a += gridDim.x * blockDim.x) {
+    const int slot = atom_slot[a];
+    classify_atom(g, s, slot, s.r[slot], mixed, w, status);
+  }
+}
+
 void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
-                     const RebinWork &w, int *status, cudaStream_t st) {
+                     const RebinWork &w, int *status, cudaStream_t st, const int *only_if) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
-  if (ntot > 0)
-    advance_kernel<false, false, INT_IEEE><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, 0.0, 0.0, 1.0, 0.0, mixed, false, true, DELTA_NONE, false, w,
-        status);
+  if (ntot > 0) {
+    const unsigned nb = std::min(atom_blocks(ntot), 4096u);
+    classify_kernel<<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, mixed, w, status, only_if);
+  }
 }
 
 __device__ __forceinline__ unsigned long long box_mask(const RebinWork &w, int b) {
@@ -399,9 +418,9 @@ __device__ __forceinline__ void set_error(int *status, int code) {
   atomicCAS(status + ST_ERROR, 0, code);
 }
 
-__global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status) {
+__global__ void rebin_plan_kernel(Geom g, Slots s, RebinWork w, int *status, const int *only_if) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= g.nboxes) return;
+  if (b >= g.nboxes || stood_down(only_if)) return;
   if (*(volatile int *)(status + ST_REBIN_SERIAL)) return;
   const unsigned long long mask = box_mask(w, b);
   const int n = s.natoms[b];
@@ -460,8 +479,10 @@ __device__ void rebin_serial(const Geom &g, const Slots &s, bool mixed, int *sta
 
 // the plan stood down (a move of more than one box): thread 0 replays
 // reBoxAll serially instead
-__global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int *status) {
+__global__ void rebin_apply_kernel(Geom g, Slots s, bool mixed, RebinWork w, int *status,
+                                   const int *only_if) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (stood_down(only_if)) return;
   if (*(volatile int *)(status + ST_REBIN_SERIAL)) {
     if (b == 0) rebin_serial(g, s, mixed, status, w.map);
     return;
@@ -557,10 +578,10 @@ __device__ void rebin_serial(const Geom &g, const Slots &s, bool mixed, int *sta
 }
 
 void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
-                         cudaStream_t st) {
+                         cudaStream_t st, const int *only_if) {
   unsigned nb = (unsigned)((g.nboxes + 127) / 128);
-  rebin_plan_kernel<<<nb, 128, 0, st>>>(g, s, w, status);
-  rebin_apply_kernel<<<nb, 128, 0, st>>>(g, s, mixed, w, status);
+  rebin_plan_kernel<<<nb, 128, 0, st>>>(g, s, w, status, only_if);
+  rebin_apply_kernel<<<nb, 128, 0, st>>>(g, s, mixed, w, status, only_if);
 }
 
 // ---------------------------------------------------------------------------
@@ -683,8 +704,10 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh, int &total) {
 }
 
 __global__ void __launch_bounds__(CP_THREADS) compact_sum_kernel(const int *natoms, int nboxes,
-                                                                 int *partials) {
+                                                                 int *partials,
+                                                                 const int *only_if) {
   __shared__ int sh[CP_THREADS / 32];
+  if (stood_down(only_if)) return;
   int base = blockIdx.x * CP_CHUNK + threadIdx.x * CP_PER;
   int v = 0;
   for (int q = 0; q < CP_PER; q++)
@@ -695,7 +718,9 @@ __global__ void __launch_bounds__(CP_THREADS) compact_sum_kernel(const int *nato
 }
 
 __global__ void __launch_bounds__(CP_THREADS) compact_scan_partials_kernel(int *partials,
-                                                                           int npart) {
+                                                                           int npart,
+                                                                           const int *only_if) {
+  if (stood_down(only_if)) return;
   __shared__ int sh[CP_THREADS / 32];
   int carry = 0;
   for (int base = 0; base < npart; base += CP_THREADS) {
@@ -713,9 +738,11 @@ __global__ void __launch_bounds__(CP_THREADS) compact_scan_partials_kernel(int *
 __global__ void __launch_bounds__(CP_THREADS) compact_write_kernel(const int *natoms, int nboxes,
                                                                    const int *partials,
                                                                    int *box_start,
-                                                                   int *atom_slot, int ntot) {
+                                                                   int *atom_slot, int ntot,
+                                                                   const int *only_if) {
   __shared__ int sh[CP_THREADS / 32];
   __shared__ int s_off[CP_CHUNK], s_n[CP_CHUNK];
+  if (stood_down(only_if)) return;
   const int b0 = blockIdx.x * CP_CHUNK;
   int loc[CP_PER];
   int v = 0;
@@ -747,11 +774,11 @@ __global__ void __launch_bounds__(CP_THREADS) compact_write_kernel(const int *na
 }
 
 void launch_compact(const Geom &g, const int *natoms, int *box_start, int *atom_slot, int ntot,
-                    int *partials, int npart, cudaStream_t st) {
-  compact_sum_kernel<<<npart, CP_THREADS, 0, st>>>(natoms, g.nboxes, partials);
-  compact_scan_partials_kernel<<<1, CP_THREADS, 0, st>>>(partials, npart);
+                    int *partials, int npart, cudaStream_t st, const int *only_if) {
+  compact_sum_kernel<<<npart, CP_THREADS, 0, st>>>(natoms, g.nboxes, partials, only_if);
+  compact_scan_partials_kernel<<<1, CP_THREADS, 0, st>>>(partials, npart, only_if);
   compact_write_kernel<<<npart, CP_THREADS, 0, st>>>(natoms, g.nboxes, partials, box_start,
-                                                     atom_slot, ntot);
+                                                     atom_slot, ntot, only_if);
 }
 
 // ids of a replica's slots, offset by its first atom
