@@ -186,8 +186,10 @@ int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int
  * step instead of after each position half step (timestep.c:129-132 with
  * reBoxAll at the end of advancePositions, timestep.c:106).  The closing
  * half step of one step and the opening one of the next become one position
- * update, r + p*(dt/M), and one rebox follows; the last step of a call still
- * ends with its own rebox.  The positions differ from the unmerged ones by
+ * update, r + p*(dt/M), and one rebox follows; with skin lists in force
+ * order that rebox (and the atom list) waits until a list rebuild is due,
+ * the force passes reading no layout in between.  The last step of a call
+ * still ends with its own rebox.  The positions differ from the unmerged ones by
  * roundings, and atoms may sit in other slots of their boxes.  0 restores
  * the reference's two reboxes per step (FP64 always has them). */
 int comdgb_sim_set_merge_rebox(comdgb_sim *h, int on);
