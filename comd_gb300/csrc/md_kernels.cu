@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
                                                       int ntot, double dt_v, double dt_r,
                                                       double rmass, double rinv, bool mixed,
                                                       bool write32, bool classify, int delta,
-                                                      bool twice, RebinWork w, int *status) {
+                                                      bool twice, bool lazy32, RebinWork w,
+                                                      int *status) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= ntot) return;
   const int slot = atom_slot[a];
@@ -293,7 +294,10 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
   if (POS) {
     if (mixed && write32) {
       const float4 p32 = centred32(rep_of(g, b), r.x, r.y, r.z);
-      s.pos32[slot] = p32;
+      // lazy32: between list rebuilds only the stencil scan of an overflowed
+      // list reads the slot-order copy (the classification before a rebuild
+      // rewrites it for every atom)
+      if (!lazy32 || *(volatile const int *)(status + ST_NBR_OVERFLOW)) s.pos32[slot] = p32;
       if (w.fo.of_id) fo_track(g, w.fo, b, s.id[slot], r, p32, status);
     }
     if ((!VEL || twice) && w.pl.rref) {
@@ -329,22 +333,22 @@ template <bool POS, bool VEL>
 static void launch_advance(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                            double dt_r, double c, double rmass, bool mixed, bool write32,
                            bool classify, int delta, bool twice, const RebinWork &w, int *status,
-                           cudaStream_t st) {
+                           cudaStream_t st, bool lazy32 = false) {
   if (ntot <= 0) return;
   const unsigned nb = atom_blocks(ntot);
   const double rinv = mass_reciprocal(rmass);
   if (mixed && POS)
     advance_kernel<POS, VEL, INT_FMA><<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, dt_v, dt_r,
                                                           rmass, c, mixed, write32, classify,
-                                                          DELTA_NONE, twice, w, status);
+                                                          DELTA_NONE, twice, lazy32, w, status);
   else if (rinv != 0.0)
     advance_kernel<POS, VEL, INT_MARK><<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, dt_v, dt_r,
                                                            rmass, rinv, mixed, write32, classify,
-                                                           delta, twice, w, status);
+                                                           delta, twice, false, w, status);
   else
     advance_kernel<POS, VEL, INT_IEEE><<<nb, 256, 0, st>>>(g, s, atom_slot, ntot, dt_v, dt_r,
                                                            rmass, rinv, mixed, write32, classify,
-                                                           delta, twice, w, status);
+                                                           delta, twice, false, w, status);
 }
 
 void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt,
@@ -352,7 +356,8 @@ void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int 
                               int *status, cudaStream_t st, bool use_delta) {
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   launch_advance<true, false>(g, s, atom_slot, ntot, 0.0, dt, dt / rmass, rmass, mixed, true,
-                              classify, use_delta ? DELTA_USE : DELTA_NONE, false, w, status, st);
+                              classify, use_delta ? DELTA_USE : DELTA_NONE, false, w, status, st,
+                              !classify && w.fo.of_id);
 }
 
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
@@ -372,7 +377,8 @@ void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, 
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   // mixed precision: one multiply-add by 2*dt_r/rmass for the two half steps
   launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, 2.0 * dt_r / rmass, rmass, mixed,
-                             true, classify, DELTA_NONE, true, w, status, st);
+                             true, classify, DELTA_NONE, true, w, status, st,
+                             !classify && w.fo.of_id);
 }
 
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
@@ -380,8 +386,8 @@ void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int n
   RebinWork none{};
   if (ntot > 0)
     advance_kernel<false, true, INT_IEEE><<<atom_blocks(ntot), 256, 0, st>>>(
-        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, DELTA_NONE, false, none,
-        nullptr);
+        g, s, atom_slot, ntot, dt_v, 0.0, 1.0, 0.0, false, false, false, DELTA_NONE, false, false,
+        none, nullptr);
 }
 
 // only_if (optional): a status word; the launch does nothing while it is 0
@@ -397,7 +403,9 @@ __global__ void __launch_bounds__(256) classify_kernel(Geom g, Slots s, const in
   if (stood_down(only_if)) return;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < ntot; a += gridDim.x * blockDim.x) {
     const int slot = atom_slot[a];
-    classify_atom(g, s, slot, s.r[slot], mixed, w, status);
+    const d4 r = s.r[slot];
+    if (mixed) s.pos32[slot] = centred32(rep_of(g, slot >> 6), r.x, r.y, r.z);
+    classify_atom(g, s, slot, r, mixed, w, status);
   }
 }
 
