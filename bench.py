@@ -648,7 +648,7 @@ def adjoint_arm(args):
                 cg.free_host(s)
             else:
                 s0 = s
-    # LJ epsilon / sigma on config 0's lattice (BASELINE LJ parameters)
+    # LJ epsilon / sigma on configuration 0's lattice (the default LJ run's parameters)
     ev = cg.lib.EV_TO_HA
     sig, eps = 2.315, 0.167 * ev
     ljp = cg.lj_potential(sig, eps, 2.5 * sig, 63.55)

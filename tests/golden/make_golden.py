@@ -195,7 +195,7 @@ def main():
     fx["cu6_cheby_600K"] = eam_case(True, 6, 1.0, 1.0, 1, 2, 0.05, 600.0, 10)
     fx["cu13_cheby_stretch_bf15"] = eam_case(True, 13, 1.05, 1.5, 3, 2, 0.05, 300.0, 5)
     fx["cu3_table_small_grid"] = eam_case(False, 3, 1.0, 1.0, 4, 2, 0.05, 600.0, 3)
-    fx["lj8_baseline_params"] = lj_case(8, 2.315, 0.167 * EV, 2.5 * 2.315, 63.55, 3.615, 5,
+    fx["lj8_default_run_params"] = lj_case(8, 2.315, 0.167 * EV, 2.5 * 2.315, 63.55, 3.615, 5,
                                         0.01 * 2.315, 10)
     # the bundled Ag structures (clsman files)
     fx["ag8k_table_file"] = clsman_case(False, "8k.inp.gz", 10)

@@ -14,7 +14,7 @@ from comd_gb300.abi import by_id, occupied_mask, slot_views
 from oracle import KIND_EAM_CHEBY, KIND_EAM_TABLE, KIND_LJ
 
 EV = cg.lib.EV_TO_HA
-# BASELINE LJ parameters: eps 0.167 eV, sigma 2.315 A, rc 2.5 sigma, Cu mass
+# the reference's default LJ run: eps 0.167 eV, sigma 2.315 A, rc 2.5 sigma, Cu mass
 LJ_SIGMA, LJ_EPS, LJ_MASS = 2.315, 0.167 * EV, 63.55
 LJ_RC = 2.5 * LJ_SIGMA
 

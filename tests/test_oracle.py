@@ -94,8 +94,8 @@ def test_oracle_matches_reference_fixture_eam(oracle, pots_dir, name):
 def test_oracle_matches_reference_fixture_lj(oracle):
     snap, after = lj_run(oracle, 8, 2.315, 0.167 * EV, 2.5 * 2.315, 63.55, 3.615, 5,
                          0.01 * 2.315, 10)
-    match(snap, FIX["lj8_baseline_params"]["force"])
-    match(after, FIX["lj8_baseline_params"]["after"], rtol=1e-11)
+    match(snap, FIX["lj8_default_run_params"]["force"])
+    match(after, FIX["lj8_default_run_params"]["after"], rtol=1e-11)
 
 
 @pytest.mark.parametrize("cheby", [False, True])
