@@ -45,6 +45,17 @@ FLOPS_PASS2_PER_PAIR = 132    # rho' by Clenshaw + embedding force
 FLOPS_EMBED_PER_ATOM = 208    # F, F' per atom (fused into pass 1)
 BYTES_VERLET_PER_ATOM = 120   # read r, p, f; write r, p (FP64)
 BYTES_ADVPOS_PER_ATOM = 72    # read r, p; write r (FP64)
+# CPU baselines (both arms): one process per host core, each an independent
+# periodic sample of CPU_CELLS^3 FCC unit cells of the workload
+CPU_CELLS = 30
+CPU_COUNTING = ("atom-steps counted as the reference's own us/atom print counts them "
+                "(src-flat/docompute.c:203-204): N * (n+1) force calls per nTimeSteps(n)")
+# tolerances of the mixed path against the FP64 oracle (relative to the
+# oracle's largest magnitude unless stated); tests/test_mixed_vs_oracle.py
+# asserts the same values at 256,000 atoms
+ORACLE_TOL = {"f_rel_rms": 1e-5, "f_max_rel": 1e-4, "e_atom_max_rel": 1e-6, "rho_max_rel": 1e-6,
+              "fi_max_rel": 1e-5, "e_per_atom_abs": 1e-8, "stress_rel": 1e-5,
+              "virial_max_rel": 1e-5}
 
 
 def env_rank():
@@ -250,12 +261,13 @@ def reference_arm(args):
         return 0
     threads = cpu_threads()
     w = WORKLOAD
-    # each step: one nTimeSteps(1) per thread on an independent sample; the
-    # sample is sized so the whole run stays within a few minutes
+    # each step: one nTimeSteps(1) per thread on an independent sample of
+    # CPU_CELLS^3 cells (the GPU arm's cpu_baseline sample), about 3 s; only a
+    # run of more than 60 steps shrinks it to stay within a few minutes
     total_steps = args.steps + args.warmup
-    per_step_s = min(12.0, 150.0 / max(total_steps, 1))
-    cells = int(round((per_step_s / 2 / 25e-6 / 4) ** (1 / 3)))
-    cells = max(8, min(cells, 40))
+    cells = CPU_CELLS
+    if total_steps > 60:
+        cells = max(8, int(CPU_CELLS * (60.0 / total_steps) ** (1 / 3)))
     for _ in range(args.warmup):
         cpu_sample(threads, cells, 1, w, True)
     vals = []
@@ -271,7 +283,7 @@ def reference_arm(args):
             "config": {"workload": w["name"], "atoms": 4_000_000, "potential": "EAM Cu Chebyshev",
                        "sample": desc},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": desc},
+                             "sample": desc, "counting": CPU_COUNTING},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -279,9 +291,56 @@ def reference_arm(args):
 
 
 # ------------------------------------------------------------------ GPU arm
+def per_atom(s):
+    """by-id copies of the force-call outputs of a host simflat_t"""
+    from comd_gb300.abi import by_id
+    f = by_id(s, "f")
+    return {"f": f[:, :3].copy(), "e": f[:, 3].copy(), "rho": by_id(s, "rho").copy(),
+            "fi": by_id(s, "fi").copy()}
+
+
+def oracle_check(s, pot, mix, e_mix, st_mix, w_mix):
+    """The FP64 oracle's force call and virial on the positions of host
+    simflat_t s (one core), against the mixed-precision results: relative
+    RMS and maximum errors of every output (eam.c:534-545, 586-594, 644-657)
+    with the tolerances they are held to."""
+    import oracle
+    O = oracle.Oracle()
+    t0 = time.perf_counter()
+    so = O.clone(s)
+    try:
+        so.contents.ch_pot = O.cheby(pot.ptr, 32)
+        if O.force(so, oracle.KIND_EAM_CHEBY):
+            raise RuntimeError("oracle force call failed")
+        orc = per_atom(so)
+        w_orc, _, _ = O.virial(so, oracle.KIND_EAM_CHEBY)
+        e_orc, st_orc = so.contents.e, so.contents.stress
+    finally:
+        O.free(so)
+    n = len(orc["f"])
+
+    def rms(a, b):
+        return float(np.sqrt(np.mean((a - b) ** 2)) / np.sqrt(np.mean(b ** 2)))
+
+    def mx(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    rec = {"f_rel_rms": rms(mix["f"], orc["f"]), "f_max_rel": mx(mix["f"], orc["f"]),
+           "e_atom_rel_rms": rms(mix["e"], orc["e"]), "e_atom_max_rel": mx(mix["e"], orc["e"]),
+           "rho_rel_rms": rms(mix["rho"], orc["rho"]), "rho_max_rel": mx(mix["rho"], orc["rho"]),
+           "fi_rel_rms": rms(mix["fi"], orc["fi"]), "fi_max_rel": mx(mix["fi"], orc["fi"]),
+           "e_per_atom_abs": abs(e_mix - e_orc) / n, "e_total_oracle_ha": e_orc,
+           "stress_rel": abs(st_mix - st_orc) / abs(st_orc),
+           "virial_max_rel": mx(w_mix, w_orc), "virial_oracle_ha": [float(x) for x in w_orc]}
+    rec["within_tolerance"] = all(rec[k] <= v for k, v in ORACLE_TOL.items())
+    rec["tolerances"] = ORACLE_TOL
+    rec["atoms"] = n
+    rec["oracle_seconds"] = time.perf_counter() - t0
+    return rec
+
+
 def gpu_arm(args):
     import comd_gb300 as cg
-    from comd_gb300.abi import slot_views, occupied_mask
 
     rank, world, local = env_rank()
     dist = Dist(world)
@@ -325,9 +384,13 @@ def gpu_arm(args):
         e1, _ = mixed.force()
         drift = abs(e1 + mixed.kinetic() - h0) / natoms
 
-    # force error of mixed vs the FP64 kernel on the same (thermalised) state
+    # accuracy on the same (thermalised) state: the mixed force call and
+    # virial, the plain FP64 GPU kernel, and the FP64 oracle (the reference's
+    # double-precision force call restated on the CPU)
+    e_mix, st_mix = mixed.force()
+    w_mix, _, _ = mixed.virial()
     mixed.download(s)
-    f_mixed = slot_views(s)["f"][occupied_mask(s)][:, :3].copy()
+    mix = per_atom(s)
     fp64_value = fp64_ms = None
     ferr = None
     if not args.no_fp64:
@@ -335,14 +398,29 @@ def gpu_arm(args):
                                        cheby_from_host=False))
         fp64.force()
         fp64.download(s)
-        f64 = slot_views(s)["f"][occupied_mask(s)][:, :3].copy()
-        ferr = float(np.sqrt(np.mean((f_mixed - f64) ** 2)) / np.sqrt(np.mean(f64 ** 2)))
+        f64 = per_atom(s)["f"]
+        ferr = float(np.sqrt(np.mean((mix["f"] - f64) ** 2)) / np.sqrt(np.mean(f64 ** 2)))
         fp64.steps(1, dt)
         fp64.synchronize()
         st64, span64, _ = fp64.timed_steps(args.fp64_steps, dt)
         fp64_ms = span64 / args.fp64_steps
         fp64_value = natoms / (fp64_ms / 1e3)
         fp64.close()
+    vs_oracle = None
+    if rank == 0 and not args.no_oracle:
+        vs_oracle = oracle_check(s, pot, mix, e_mix, st_mix, w_mix)
+
+    # mixed precision with the reference's series evaluated in FP32 for every
+    # pair (no segment table): the same algorithm as the FP64 kernel, so
+    # against it the speed-up of precision alone
+    series_ms = None
+    if args.series_steps > 0:
+        mixed.set_pair_table(False)
+        mixed.steps(2, dt)
+        mixed.synchronize()
+        _, span_s, _ = mixed.timed_steps(args.series_steps, dt)
+        series_ms = span_s / args.series_steps
+        mixed.set_pair_table(True)
 
     # e2e through the drop-in C ABI on the host simflat_t
     e2e = None
@@ -419,7 +497,8 @@ def gpu_arm(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, kind, desc = cpu_sample(cpu_threads(), args.cpu_cells, 1, w, True)
-        cpu = {"value": v, "unit": UNIT, "cores": cpu_threads(), "kind": kind, "sample": desc}
+        cpu = {"value": v, "unit": UNIT, "cores": cpu_threads(), "kind": kind, "sample": desc,
+               "counting": CPU_COUNTING}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -434,7 +513,20 @@ def gpu_arm(args):
                    "dt_fs": 1.0},
         "fp64_gpu": {"value": fp64_value, "ms_per_step": fp64_ms, "steps": args.fp64_steps},
         "mixed_vs_fp64": (value / world / fp64_value) if fp64_value else None,
+        "mixed_series_gpu": {"ms_per_step": series_ms, "steps": args.series_steps,
+                             "value": natoms / (series_ms / 1e3) if series_ms else None,
+                             "what": "mixed precision, the 32-term series in FP32 for every "
+                                     "pair (segment table off)"},
+        "speedup_split": {
+            "precision_only": (fp64_ms / series_ms) if fp64_ms and series_ms else None,
+            "algorithm_only": (series_ms / (elapsed_s * 1e3 / args.steps))
+                              if series_ms else None,
+            "what": "precision_only = FP64 kernel / mixed with the series (both sum the "
+                    "series per pair); algorithm_only = mixed with the series / mixed with "
+                    "the segment table; their product is mixed_vs_fp64"},
         "force_rel_rms_mixed_vs_fp64": ferr,
+        "force_rel_rms_mixed_vs_oracle": vs_oracle["f_rel_rms"] if vs_oracle else None,
+        "accuracy_vs_oracle": vs_oracle,
         "energy_drift_ha_per_atom": drift, "drift_steps": args.drift_steps,
         "neighbour_lists": lists, "pairs_per_step": pairs, "pair_evals_per_s": pairs * args.steps / (span_ms / 1e3),
         "kernel_groups": groups, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
@@ -831,10 +923,14 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--series-steps", type=int, default=20,
+                    help="steps of the mixed-precision run with the series evaluator")
+    ap.add_argument("--no-oracle", action="store_true",
+                    help="skip the FP64 oracle force call on the full-size state")
     ap.add_argument("--drift-steps", type=int, default=1000)
     ap.add_argument("--e2e-calls", type=int, default=20)
-    ap.add_argument("--cpu-cells", type=int, default=30)
+    ap.add_argument("--cpu-cells", type=int, default=CPU_CELLS)
     ap.add_argument("--cells", type=int, default=0,
                     help="override the lattice to N^3 unit cells (profiling captures only)")
     ap.add_argument("--no-fp64", action="store_true")

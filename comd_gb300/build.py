@@ -6,6 +6,11 @@ integrator/rebinning kernels are compiled with ``-fmad=false`` so their
 double-precision arithmetic rounds operation by operation like the
 reference; the mixed-precision force kernels and the host API keep FMA.
 
+The C host ``comd_gb300/comdgb_run`` (``host/comdgb_run.c``: the
+reference's do_compute_work loop on the drop-in boundary) is linked
+against the library with gcc, as a maintainer would link the reference's
+own host.
+
 Usage: ``python -m comd_gb300.build [--force]``.
 """
 import os
@@ -18,6 +23,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "libcomdgb.so")
+HOST_SRC = os.path.join(HERE, "host", "comdgb_run.c")
+HOST_OUT = os.path.join(HERE, "comdgb_run")
 OBJDIR = os.path.join(HERE, "_build")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -48,7 +55,7 @@ def _nvcc():
 
 
 def _deps():
-    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [HOST_SRC]
     files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     files.append(os.path.abspath(__file__))
     return max(os.path.getmtime(f) for f in files)
@@ -71,9 +78,19 @@ def _have_zlib():
     return r.returncode == 0
 
 
+def build_host():
+    """the C host, linked with -lcomdgb (rpath: the library beside it)"""
+    tmp = HOST_OUT + ".tmp"
+    _run(["gcc", "-O2", "-std=c11", "-Wall", "-I", INCLUDE, HOST_SRC, "-o", tmp, "-L", HERE,
+          "-lcomdgb", "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, HOST_OUT)
+    return HOST_OUT
+
+
 def build(force=False, verbose=False):
     """Compile (if sources are newer than the library) and return its path."""
-    if not force and os.path.exists(OUT) and os.path.getmtime(OUT) >= _deps():
+    if not force and all(os.path.exists(f) and os.path.getmtime(f) >= _deps()
+                         for f in (OUT, HOST_OUT)):
         return OUT
     os.makedirs(OBJDIR, exist_ok=True)
     nvcc = _nvcc()
@@ -99,6 +116,7 @@ def build(force=False, verbose=False):
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + [o for _, o in jobs] + ["-lm"]
          + (["-lz"] if zlib else []))
     os.replace(tmp, OUT)
+    build_host()
     return OUT
 
 

@@ -407,8 +407,10 @@ void cgapi::install_lj(comdgb_sim *h, double eps, double sigma, double cutoff) {
 int cgapi::install_cheby(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
                          const double b[6]) {
   fill_cheb(h->eam64c.ch, h->eam32c.ch, h->eam32c.chlo, coef, a, b, h->pair_lo);
-  if (build_pair_seg(h, coef, a, b, h->pair_lo, h->cutoff, &h->eam32c.seg))
+  if (build_pair_seg(h, coef, a, b, h->pair_lo, h->cutoff, &h->seg_built))
     return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for the pair segment table");
+  h->eam32c.seg = h->seg_built;
+  if (h->pair_table_off) h->eam32c.seg.n = 0;  // the series for every pair
   for (int q = 0; q < 6; q++) {
     for (int j = 0; j < CG_NCHEB; j++) h->cheb_coef[q][j] = coef[q][j];
     h->cheb_a[q] = a[q];
@@ -446,7 +448,7 @@ int check_status(comdgb_sim *h) {
 // lazy: the rebox only when a list rebuild is due (see enqueue_step)
 void enqueue_classify_finish(comdgb_sim *h, bool lazy = false) {
   launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, h->stream,
-                      lazy ? h->status + ST_REBUILD : nullptr);
+                      lazy ? h->status : nullptr);
 }
 
 void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_rebox = false) {
@@ -455,7 +457,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_reb
   cudaStream_t st = h->stream;
   cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
-                 st, lazy_rebox ? h->status + ST_REBUILD : nullptr);
+                 st, lazy_rebox ? h->status : nullptr);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   const int pot = h->opts.potential;
   // persistent lists are built with rc + skin, and only when a rebuild is due
@@ -564,7 +566,7 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
     // has decided that)
     if (lazy)
       launch_classify(h->g, h->s, h->atom_slot, h->ntot, h->mixed, h->w, h->status, st,
-                      h->status + ST_REBUILD);
+                      h->status);
     enqueue_classify_finish(h, lazy);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     enqueue_force_parts(h, ev, evi, lazy);  // starts with the atom list of the new layout
@@ -1231,6 +1233,9 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
       h->w.map = SlotMap{h->pl.slot_of, nullptr, nullptr};
     }
   }
+  h->cap_alloc = h->cap;
+  h->pl_vcap_alloc = h->pl.vcap;
+  h->fo_vcap_alloc = h->fo.vcap;
   // per-step list: built each step, or (persistent lists) left by pass 1
   // (the force-order passes keep their own lists and never read this one)
   h->nbr = track(h, dalloc<uint16_t>((h->fo.list ? 0 : (size_t)h->ntot * h->cap) + 8, &err));
@@ -1557,6 +1562,39 @@ int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int
           : 0;
   CK(cudaGetLastError());
   drop_graphs(h);  // recaptured with the new shapes at the next call
+  return 0;
+}
+
+int comdgb_sim_set_pair_table(comdgb_sim *h, int on) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  h->pair_table_off = !on;
+  h->eam32c.seg = h->seg_built;
+  if (h->pair_table_off) h->eam32c.seg.n = 0;
+  drop_graphs(h);  // the captured kernels hold the table by value
+  return 0;
+}
+
+int comdgb_sim_set_list_capacity(comdgb_sim *h, int cap) {
+  if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
+  const bool fo = h->fo.list != nullptr, pl = h->pl.vlist != nullptr;
+  const int alloc = fo ? h->fo_vcap_alloc : pl ? h->pl_vcap_alloc : h->cap_alloc;
+  if (cap == 0) cap = alloc;
+  if (cap < 1 || cap > alloc)
+    return set_err(COMDGB_ERR_ARG, "list capacity %d: 1..%d (0 restores %d)", cap, alloc, alloc);
+  CK(cudaSetDevice(h->device));
+  if (fo) {
+    h->fo.vcap = cap;
+    h->w.fo = h->fo;
+  } else if (pl) {
+    h->pl.vcap = cap;
+    h->w.pl = h->pl;
+  } else {
+    h->cap = cap;
+  }
+  // the lists in use were laid out for the old capacity: rebuild them
+  if (fo || pl) CK(cudaMemsetAsync(h->status + ST_REBUILD, 0x01, 1, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  drop_graphs(h);  // the captured kernels hold the capacity by value
   return 0;
 }
 

@@ -140,11 +140,13 @@ struct EntryTab {
 enum {
   ST_ERROR = 0,       // first error code (COMDGB_ERR_*), 0 if none
   ST_REBIN_SERIAL = 1,// set when the parallel rebin cannot reproduce reBoxAll
-  ST_NBR_OVERFLOW = 2,// atoms whose neighbour list overflowed (handled)
+  ST_NBR_OVERFLOW = 2,// atoms whose neighbour list overflowed (handled); with
+                      // persistent lists: the overflows of the current lists
   ST_SERIAL_RUNS = 3, // number of serial rebin fallbacks taken
   ST_REBUILD = 4,     // persistent lists: an atom moved more than skin/2
   ST_REBUILDS = 5,    // persistent lists: number of list builds
   ST_DELTA = 6,       // f.xyz holds the half-step position increments (see advance_kernel)
+  ST_OVF_BUILD = 7,   // persistent lists: overflows counted by the build in progress
   ST_COUNT = 8
 };
 

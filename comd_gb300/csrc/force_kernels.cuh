@@ -393,7 +393,10 @@ __device__ __forceinline__ void build_count(const ForceArgs &A, int row, int tot
   if (MODE == LIST_ID) A.pl.vcount[row] = total;
   else if (MODE == LIST_FO) A.fo.n[row] = total;
   else A.nbr_n[row] = total;
-  if (total > build_cap<MODE>(A)) atomicAdd(A.status + ST_NBR_OVERFLOW, 1);
+  // persistent lists: counted for the lists being built (rebuild_done makes
+  // it the current lists' count)
+  if (total > build_cap<MODE>(A))
+    atomicAdd(A.status + (MODE == LIST_STEP ? ST_NBR_OVERFLOW : ST_OVF_BUILD), 1);
 }
 
 // the lists of the atoms of box b (not empty): NT threads (the CTA), NA

@@ -53,14 +53,15 @@ void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, 
 void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                              cudaStream_t st);
 // classify only (reBoxAll without a position update); only_if (optional):
-// a status word, nothing is classified while it is 0
+// the status words of a force-order simulation whose rebox waits for list
+// rebuilds: nothing is classified unless a rebuild is due (ST_REBUILD)
 void launch_classify(const Geom &g, Slots s, const int *atom_slot, int ntot, bool mixed,
                      const RebinWork &w, int *status, cudaStream_t st,
                      const int *only_if = nullptr);
 // plan + apply + serial fallback; must follow a classify launch.  only_if
-// (optional): a status word; while it is 0 the launches do nothing (the
-// atoms stay in the boxes they had, their box-relative positions as the
-// half steps left them)
+// (optional) as above; while it stands the launches down they do nothing
+// (the atoms stay in the boxes they had, their box-relative positions as
+// the half steps left them)
 void launch_rebin_finish(const Geom &g, Slots s, bool mixed, const RebinWork &w, int *status,
                          cudaStream_t st, const int *only_if = nullptr);
 // the atom list of the layout; only_if as above (the layout did not change)

@@ -10,6 +10,7 @@
 
 #include <algorithm>
 
+#include "binning.cuh"
 #include "internal.h"
 
 namespace cg {
@@ -390,9 +391,14 @@ void launch_advance_velocity(const Geom &g, Slots s, const int *atom_slot, int n
         none, nullptr);
 }
 
-// only_if (optional): a status word; the launch does nothing while it is 0
+// only_if (optional): the status words of a force-order simulation whose
+// rebox waits for list rebuilds; the launch does nothing unless a rebuild is
+// due (ST_REBUILD).  Between rebuilds atoms may sit up to skin/2 outside
+// their boxes; the skin is at most the box width minus the cutoff, so
+// in-cutoff pairs stay within adjacent boxes and an overflowed atom's
+// stencil scan still sees all of them.
 __device__ __forceinline__ bool stood_down(const int *only_if) {
-  return only_if && !*(volatile const int *)only_if;
+  return only_if && !*(volatile const int *)(only_if + ST_REBUILD);
 }
 
 // classify only, grid-stride over the atoms (a stood-down launch costs one
@@ -617,6 +623,9 @@ __global__ void rebuild_done_kernel(int *status) {
   if (status[ST_REBUILD]) {
     status[ST_REBUILDS] += 1;
     status[ST_REBUILD] = 0;
+    // the overflows of the lists just built are those of the current lists
+    status[ST_NBR_OVERFLOW] = status[ST_OVF_BUILD];
+    status[ST_OVF_BUILD] = 0;
   }
 }
 
@@ -1064,40 +1073,26 @@ void launch_pos32(const Geom &g, Slots s, cudaStream_t st) {
 // initial binning: n putAtomInBox calls (domains.c:237-291) as a counting
 // sort that keeps call order within each box
 // ---------------------------------------------------------------------------
-// (one replica: the initial binning of a single simulation)
-__device__ __forceinline__ int world_box(const Geom &g, const double *xyz_in, double *xyz,
-                                         bool &ok) {
+// (one replica: the initial binning of a single simulation; the bodies are
+// shared with the allocation-free entry point, binning.cuh)
+__device__ __forceinline__ BinGrid bin_grid(const Geom &g) {
   const RepGeo &R = g.rep[0];
-  int ib[3];
-  ok = true;
+  BinGrid b;
   for (int m = 0; m < 3; m++) {
-    double x = xyz_in[m];
-    if (x < 0.0) x += R.bounds[m];
-    else if (x >= R.bounds[m]) x -= R.bounds[m];
-    xyz[m] = x;
-    ib[m] = (int)floor(x / R.boxsize[m]);
-    if (ib[m] < 0 || ib[m] >= R.nbx[m]) ok = false;
+    b.nbx[m] = R.nbx[m];
+    b.bounds[m] = R.bounds[m];
+    b.boxsize[m] = R.boxsize[m];
   }
-  return ib[0] + R.nbx[0] * ib[1] + R.nbx[0] * R.nbx[1] * ib[2];
+  b.nboxes = g.nboxes;
+  return b;
 }
 
 __global__ void bin_count_kernel(Geom g, Slots s, int n, const double *xyz, int *tmp_index,
                                  int *status) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  double w[3];
-  bool ok;
-  int b = world_box(g, xyz + 3 * (long)t, w, ok);
-  if (!ok) {
-    set_error(status, -12);
-    return;
-  }
-  int pos = atomicAdd(s.natoms + b, 1);
-  if (pos >= CG_MAXATOMS) {
-    set_error(status, -11);
-    return;
-  }
-  tmp_index[b * CG_MAXATOMS + pos] = t;
+  const int err = bin_count_atom(bin_grid(g), t, xyz, s.natoms, tmp_index);
+  if (err) set_error(status, err);
 }
 
 __global__ void bin_place_kernel(Geom g, const double *dcenter, Slots s, int n,
@@ -1110,20 +1105,14 @@ __global__ void bin_place_kernel(Geom g, const double *dcenter, Slots s, int n,
   int nb = s.natoms[b];
   if (nb > CG_MAXATOMS) return;  // reported by bin_count_kernel
   int *ix = tmp_index + b * CG_MAXATOMS;
-  for (int i = 1; i < nb; i++) {  // insertion sort: call order
-    int v = ix[i], j = i - 1;
-    while (j >= 0 && ix[j] > v) {
-      ix[j + 1] = ix[j];
-      j--;
-    }
-    ix[j + 1] = v;
-  }
+  bin_sort_box(ix, nb);
+  const BinGrid bg = bin_grid(g);
   for (int k = 0; k < nb; k++) {
     int t = ix[k];
     int slot = b * CG_MAXATOMS + k;
     double w[3];
     bool ok;
-    world_box(g, xyz + 3 * (long)t, w, ok);
+    bin_world_box(bg, xyz + 3 * (long)t, w, ok);
     s.id[slot] = ids[t];
     s.itype[slot] = types[t];
     s.mass[slot] = masses[t];

@@ -3,13 +3,13 @@
 //
 // Who needs it: callers that must not allocate device memory while they run
 // -- an engine that owns all GPU memory through its own arena and forbids
-// allocations after start-up, code issuing work while a stream is being
-// captured into a CUDA graph (cudaMalloc is not permitted there), and tight
-// loops where cudaMalloc's implicit synchronisation would stall the GPU.
-// comdgb_put_atoms allocates its temporaries; this entry point takes every
-// input and output as a device pointer and keeps its scratch (one index per
-// slot plus a status word) in a file-scope device array that exists from the
-// moment the library's code is loaded on a device until the process exits.
+// allocations after start-up, and tight loops where cudaMalloc's implicit
+// synchronisation would stall the GPU.  comdgb_put_atoms allocates its
+// temporaries; this entry point takes every input and output as a device
+// pointer and keeps its scratch (one index per slot plus a status word) in a
+// file-scope device array that exists from the moment the library's code is
+// loaded on a device until the process exits.  The count and place bodies
+// are the ones comdgb_put_atoms runs (binning.cuh).
 //
 // Limits and rules (also in include/comdgb.h):
 //  * at most COMDGB_NOALLOC_MAX_BOXES boxes (16,384 boxes = 1,048,576 slots,
@@ -17,16 +17,21 @@
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it; make that
 //    first call before any stream capture;
+//  * the call makes `device` current for its work and restores the caller's
+//    current device before it returns;
 //  * every call shares the one array, so calls whose work overlaps on the
 //    GPU (different streams or host threads without ordering) race; the
 //    array keeps the previous call's contents, so each call clears the
-//    status word it reads and writes every index before it reads it.
+//    status word it reads and writes every index before it reads it;
+//  * the call reads its status back and synchronises `stream` to report
+//    errors.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
 
 #include "comdgb.h"
-#include "common.cuh"
+#include "binning.cuh"
 
 // records the message that comdgb_last_error() returns (api.cu)
 int comdgb_internal_set_error(int code, const char *msg);
@@ -44,50 +49,16 @@ int *g_scratch_ptr[64];  // device address of g_bin_scratch per device ordinal
 
 int fail(int code, const char *msg) { return comdgb_internal_set_error(code, msg); }
 
-struct NoAllocGeom {
-  int nbx[3];
-  int nboxes;
-  double bounds[3];
-  double boxsize[3];
-};
+using cg::BinGrid;
 
-// wrap once into the primary period and find the box (domains.c:255-269, 71-82)
-__device__ __forceinline__ int world_box_na(const NoAllocGeom &g, const double *in, double *w,
-                                            bool &ok) {
-  int ib[3];
-  ok = true;
-  for (int m = 0; m < 3; m++) {
-    double x = in[m];
-    if (x < 0.0) x += g.bounds[m];
-    else if (x >= g.bounds[m]) x -= g.bounds[m];
-    w[m] = x;
-    ib[m] = (int)floor(x / g.boxsize[m]);
-    if (ib[m] < 0 || ib[m] >= g.nbx[m]) ok = false;
-  }
-  return ib[0] + g.nbx[0] * ib[1] + g.nbx[0] * g.nbx[1] * ib[2];
-}
-
-__global__ void na_count_kernel(NoAllocGeom g, int n, const double *xyz, int *natoms,
-                                int *scratch) {
+__global__ void na_count_kernel(BinGrid g, int n, const double *xyz, int *natoms, int *scratch) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  double w[3];
-  bool ok;
-  int b = world_box_na(g, xyz + 3 * (long)t, w, ok);
-  int *status = scratch + kMaxSlots;
-  if (!ok) {
-    atomicCAS(status, 0, COMDGB_ERR_BOXRANGE);
-    return;
-  }
-  int pos = atomicAdd(natoms + b, 1);
-  if (pos >= CG_MAXATOMS) {
-    atomicCAS(status, 0, COMDGB_ERR_MAXATOMS);
-    return;
-  }
-  scratch[b * CG_MAXATOMS + pos] = t;
+  const int err = cg::bin_count_atom(g, t, xyz, natoms, scratch);
+  if (err) atomicCAS(scratch + kMaxSlots, 0, err);
 }
 
-__global__ void na_place_kernel(NoAllocGeom g, const double *dcenter, int n, const double *xyz,
+__global__ void na_place_kernel(BinGrid g, const double *dcenter, int n, const double *xyz,
                                 const double *pxyz, const int *ids, const int *types,
                                 const double *masses, const int *natoms, int *id, int *itype,
                                 double *mass, double *r, double *p, int *scratch) {
@@ -97,20 +68,13 @@ __global__ void na_place_kernel(NoAllocGeom g, const double *dcenter, int n, con
   int nb = natoms[b];
   if (nb > CG_MAXATOMS) return;
   int *ix = scratch + b * CG_MAXATOMS;
-  for (int i = 1; i < nb; i++) {  // insertion sort: the order of the calls
-    int v = ix[i], j = i - 1;
-    while (j >= 0 && ix[j] > v) {
-      ix[j + 1] = ix[j];
-      j--;
-    }
-    ix[j + 1] = v;
-  }
+  cg::bin_sort_box(ix, nb);
   for (int k = 0; k < nb; k++) {
     int t = ix[k];
     long slot = (long)b * CG_MAXATOMS + k;
     double w[3];
     bool ok;
-    world_box_na(g, xyz + 3 * (long)t, w, ok);
+    cg::bin_world_box(g, xyz + 3 * (long)t, w, ok);
     id[slot] = ids[t];
     itype[slot] = types[t];
     mass[slot] = masses[t];
@@ -139,42 +103,16 @@ int scratch_for(int device, int **out) {
   return 0;
 }
 
-}  // namespace
-
-extern "C" int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3],
-                                        const double boxsize[3], const double *dcenter, int n,
-                                        const double *xyz, const double *pxyz, const int *ids,
-                                        const int *itypes, const double *masses, int *natoms,
-                                        int *id, int *itype, double *mass, double *r,
-                                        double *p, int device, void *stream) {
-  if (!nbx || !bounds || !boxsize || !dcenter || !natoms || !id || !itype || !mass || !r || !p ||
-      n < 0 || (n > 0 && (!xyz || !pxyz || !ids || !itypes || !masses)))
-    return fail(COMDGB_ERR_ARG, "comdgb_put_atoms_noalloc: null pointer or negative count");
-  NoAllocGeom g;
-  long nboxes = 1;
-  for (int j = 0; j < 3; j++) {
-    if (nbx[j] < 1) return fail(COMDGB_ERR_ARG, "comdgb_put_atoms_noalloc: nbx < 1");
-    g.nbx[j] = nbx[j];
-    g.bounds[j] = bounds[j];
-    g.boxsize[j] = boxsize[j];
-    nboxes *= nbx[j];
-  }
-  if (nboxes > COMDGB_NOALLOC_MAX_BOXES) {
-    char m[200];
-    snprintf(m, sizeof m,
-             "comdgb_put_atoms_noalloc: %ld boxes exceed the allocation-free limit of %d boxes",
-             nboxes, COMDGB_NOALLOC_MAX_BOXES);
-    return fail(COMDGB_ERR_ARG, m);
-  }
-  g.nboxes = (int)nboxes;
-  cudaError_t e = cudaSetDevice(device);
-  if (e != cudaSuccess) return fail(COMDGB_ERR_CUDA, cudaGetErrorString(e));
+// the work of one call on the current device (see comdgb_put_atoms_noalloc)
+int put_atoms_noalloc(const BinGrid &g, int device, const double *dcenter, int n,
+                      const double *xyz, const double *pxyz, const int *ids, const int *itypes,
+                      const double *masses, int *natoms, int *id, int *itype, double *mass,
+                      double *r, double *p, cudaStream_t st) {
   int *scratch = nullptr;
   int rc = scratch_for(device, &scratch);
   if (rc) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
   // outputs that are accumulated and the status word start at zero
-  e = cudaMemsetAsync(natoms, 0, sizeof(int) * (size_t)nboxes, st);
+  cudaError_t e = cudaMemsetAsync(natoms, 0, sizeof(int) * (size_t)g.nboxes, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(scratch + kMaxSlots, 0, sizeof(int), st);
   if (e != cudaSuccess) return fail(COMDGB_ERR_CUDA, cudaGetErrorString(e));
   if (n > 0) na_count_kernel<<<(n + 255) / 256, 256, 0, st>>>(g, n, xyz, natoms, scratch);
@@ -190,5 +128,49 @@ extern "C" int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3]
   if (status == COMDGB_ERR_MAXATOMS)
     return fail(status, "comdgb_put_atoms_noalloc: a box received more than 64 atoms");
   if (status) return fail(status, "comdgb_put_atoms_noalloc: an atom's box fell outside the grid");
+  return 0;
+}
+
+}  // namespace
+
+extern "C" int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3],
+                                        const double boxsize[3], const double *dcenter, int n,
+                                        const double *xyz, const double *pxyz, const int *ids,
+                                        const int *itypes, const double *masses, int *natoms,
+                                        int *id, int *itype, double *mass, double *r,
+                                        double *p, int device, void *stream) {
+  if (!nbx || !bounds || !boxsize || !dcenter || !natoms || !id || !itype || !mass || !r || !p ||
+      n < 0 || (n > 0 && (!xyz || !pxyz || !ids || !itypes || !masses)))
+    return fail(COMDGB_ERR_ARG, "comdgb_put_atoms_noalloc: null pointer or negative count");
+  BinGrid g;
+  long nboxes = 1;
+  for (int j = 0; j < 3; j++) {
+    if (nbx[j] < 1) return fail(COMDGB_ERR_ARG, "comdgb_put_atoms_noalloc: nbx < 1");
+    if (!(std::isfinite(bounds[j]) && bounds[j] > 0.0 && std::isfinite(boxsize[j]) &&
+          boxsize[j] > 0.0))
+      return fail(COMDGB_ERR_ARG,
+                  "comdgb_put_atoms_noalloc: bounds and boxsize must be finite and positive");
+    g.nbx[j] = nbx[j];
+    g.bounds[j] = bounds[j];
+    g.boxsize[j] = boxsize[j];
+    nboxes *= nbx[j];
+  }
+  if (nboxes > COMDGB_NOALLOC_MAX_BOXES) {
+    char m[200];
+    snprintf(m, sizeof m,
+             "comdgb_put_atoms_noalloc: %ld boxes exceed the allocation-free limit of %d boxes",
+             nboxes, COMDGB_NOALLOC_MAX_BOXES);
+    return fail(COMDGB_ERR_ARG, m);
+  }
+  g.nboxes = (int)nboxes;
+  int prev = 0;
+  cudaError_t e = cudaGetDevice(&prev);
+  if (e == cudaSuccess) e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(COMDGB_ERR_CUDA, cudaGetErrorString(e));
+  const int rc = put_atoms_noalloc(g, device, dcenter, n, xyz, pxyz, ids, itypes, masses, natoms,
+                                   id, itype, mass, r, p, (cudaStream_t)stream);
+  e = cudaSetDevice(prev);  // the caller's current device, on every return path
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(COMDGB_ERR_CUDA, cudaGetErrorString(e));
   return 0;
 }

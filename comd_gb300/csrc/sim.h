@@ -73,6 +73,9 @@ struct comdgb_sim {
   uint16_t *nbr = nullptr;
   int *nbr_n = nullptr;
   int cap = 0;
+  // list capacities as allocated (comdgb_sim_set_list_capacity may lower the
+  // capacity in use): per-step, id-keyed and force-order lists
+  int cap_alloc = 0, pl_vcap_alloc = 0, fo_vcap_alloc = 0;
   double *atom_stress = nullptr;
   double *rpart = nullptr;
   long long *ripart = nullptr;
@@ -96,6 +99,10 @@ struct comdgb_sim {
   double cheb_a[6] = {}, cheb_b[6] = {};
   double pair_lo = 0.0;
   float4 *seg_buf = nullptr;
+  // the FP32 pair segment table as built (seg_built) and whether the mixed
+  // Chebyshev evaluator uses it (comdgb_sim_set_pair_table)
+  cg::PairSeg seg_built{};
+  bool pair_table_off = false;
   // adjoint scratch, allocated on first use (adjoint.cu)
   struct Adj {
     d4 *lam = nullptr;

@@ -106,6 +106,8 @@ def _bind(lib):
     L.comdgb_sim_atom_stress.argtypes = [C.c_void_p, C.c_int, D]
     L.comdgb_sim_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
     L.comdgb_sim_set_merge_rebox.argtypes = [C.c_void_p, C.c_int]
+    L.comdgb_sim_set_list_capacity.argtypes = [C.c_void_p, C.c_int]
+    L.comdgb_sim_set_pair_table.argtypes = [C.c_void_p, C.c_int]
     L.comdgb_set_lazy.argtypes = [P_SIM, C.c_int]
     L.comdgb_sync_to_host.argtypes = [P_SIM]
     L.comdgb_sync_to_device.argtypes = [P_SIM]
@@ -469,6 +471,16 @@ class DeviceSim:
     def set_launch(self, build_threads=0, build_atoms=0, pass2_threads=0):
         """launch shapes of the force-order kernels (0: default)"""
         check(self.L.comdgb_sim_set_launch(self.h, build_threads, build_atoms, pass2_threads))
+
+    def set_pair_table(self, on):
+        """mixed EAM Chebyshev: pair functions from the FP32 segment table
+        (True, default) or the FP32 series for every pair (False)"""
+        check(self.L.comdgb_sim_set_pair_table(self.h, int(bool(on))))
+
+    def set_list_capacity(self, cap):
+        """neighbour-list entries per atom in use (0: as allocated); atoms
+        beyond it scan their neighbour boxes"""
+        check(self.L.comdgb_sim_set_list_capacity(self.h, cap))
 
     def set_merge_rebox(self, on):
         """mixed precision: one rebox per step in a sequence of steps (default)

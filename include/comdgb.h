@@ -193,6 +193,20 @@ int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int
  * roundings, and atoms may sit in other slots of their boxes.  0 restores
  * the reference's two reboxes per step (FP64 always has them). */
 int comdgb_sim_set_merge_rebox(comdgb_sim *h, int on);
+/* Mixed precision, EAM Chebyshev: whether the pair functions come from the
+ * FP32 cubic segment table in r^2 fitted to the FP64 series (on = 1, the
+ * default) or from the reference's 32-term series evaluated in FP32 for
+ * every pair (0; no counterpart needed in the reference, whose FP64 path
+ * always sums the series, cheby.c:276-310).  Other potentials and FP64
+ * ignore it.  The graphs are recaptured. */
+int comdgb_sim_set_pair_table(comdgb_sim *h, int on);
+/* Neighbour-list capacity in use (entries per atom), at most the capacity
+ * allocated at creation (0 restores it); no counterpart in the reference,
+ * whose loops have no lists.  Atoms with more neighbours than the capacity
+ * are computed by scanning their 27 neighbour boxes instead, with the same
+ * results up to roundings, so a lower capacity exercises that path.  Lists
+ * in use are rebuilt at the next force call; the graphs are recaptured. */
+int comdgb_sim_set_list_capacity(comdgb_sim *h, int cap);
 /* list mode in use (1 persistent, 0 per step), its skin, and the number of
  * persistent-list builds since the last upload */
 int comdgb_sim_list_info(comdgb_sim *h, int *persistent, double *skin, long long *builds);
@@ -342,17 +356,21 @@ int comdgb_put_atoms(simflat_t *s, int n, const double *xyz, const double *pxyz,
 
 /* Allocation-free binning.  No counterpart in the reference: it is
  * comdgb_put_atoms for callers that cannot allocate device memory while
- * they run (an engine owning all GPU memory through its own arena, work
- * issued during CUDA graph stream capture, latency-critical loops).  All
- * arrays are device pointers in the reference's slot layout (r and p as
- * real3 rows, slot = box*64 + k); dcenter is nbx product x 3 doubles.  The
- * result equals comdgb_put_atoms: n putAtomInBox calls in array order.
- * Scratch is a library-owned device array of COMDGB_NOALLOC_MAX_BOXES*64
- * ints (4 MiB per device, held until the process exits); larger grids are
- * rejected with COMDGB_ERR_ARG.  The first call on a device looks up that
- * array's address (cudaGetSymbolAddress) -- make it before any stream
- * capture.  Calls share the array: calls that overlap on the GPU race.
- * Synchronises `stream` (a cudaStream_t, NULL = default) to report errors. */
+ * they run (an engine owning all GPU memory through its own arena,
+ * latency-critical loops where cudaMalloc's implicit synchronisation would
+ * stall the GPU).  All arrays are device pointers in the reference's slot
+ * layout (r and p as real3 rows, slot = box*64 + k); dcenter is nbx product
+ * x 3 doubles.  The result equals comdgb_put_atoms: n putAtomInBox calls in
+ * array order; an atom whose coordinates are not finite, or that lies more
+ * than one period outside, gives COMDGB_ERR_BOXRANGE, a box of more than 64
+ * atoms COMDGB_ERR_MAXATOMS.  Scratch is a library-owned device array of
+ * COMDGB_NOALLOC_MAX_BOXES*64 ints (4 MiB per device, held until the
+ * process exits); larger grids are rejected with COMDGB_ERR_ARG.  The first
+ * call on a device looks up that array's address (cudaGetSymbolAddress) --
+ * make it before any stream capture.  Calls share the array: calls that
+ * overlap on the GPU race.  The call makes `device` current for its work
+ * and restores the caller's current device; it synchronises `stream` (a
+ * cudaStream_t, NULL = default) to report errors. */
 #define COMDGB_NOALLOC_MAX_BOXES 16384
 int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3], const double boxsize[3],
                              const double *dcenter, int n, const double *xyz, const double *pxyz,

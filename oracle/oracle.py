@@ -23,10 +23,24 @@ _oracle = None
 _refs = {}
 
 
+def reference_dir():
+    """the reference source tree: $COMDGB_REFERENCE_DIR, else the directory
+    `reference` beside the repository (None when neither holds src-flat)"""
+    for d in (os.environ.get("COMDGB_REFERENCE_DIR"),
+              os.path.join(os.path.dirname(HERE), os.pardir, "reference")):
+        if d and os.path.exists(os.path.join(d, "src-flat", "eam.c")):
+            return os.path.abspath(d)
+    return None
+
+
 def build(with_ref=True):
     """make the oracle (and oracle/_ref when the reference is present)."""
     target = "all" if with_ref else os.path.join(HERE, "liboracle.so")
-    subprocess.run(["make", "-s", "-C", HERE, target], check=True)
+    cmd = ["make", "-s", "-C", HERE, target]
+    ref = reference_dir() if with_ref else None
+    if ref:
+        cmd.append("REF=" + ref)
+    subprocess.run(cmd, check=True)
 
 
 def _bind(lib):

@@ -1,0 +1,79 @@
+"""The drop-in boundary's data model is the reference's, member for member.
+
+include/comdgb_simflat.h restates the -DDOUBLE structs of the reference
+(simflat_t src-flat/include/pmdTypes.h:104-141, pmd_base_potential_t
+:74-79, potentialarray_t src-flat/include/eamTypes.h:68-74, eampotential_t
+:92-101, eam_cheby_t :104-114, ljpotential_t src-flat/include/ljTypes.h:
+72-81), so that a host built by the reference's own setup code can hand its
+pointers to the library.  This test compiles a probe against the
+reference's headers (-DDOUBLE) that prints sizeof and offsetof of every
+member, then compiles a second translation unit against the library's
+header whose _Static_asserts must hold for those numbers.  CPU only; it
+needs the reference sources and is skipped where they are absent.
+"""
+import os
+import subprocess
+
+import pytest
+
+from oracle.oracle import reference_dir
+
+# struct -> members, as declared in include/comdgb_simflat.h
+MEMBERS = {
+    "simflat_t": ["stateflag", "nbx", "nboxes", "ntot", "bounds", "boxsize", "dcenter", "natoms",
+                  "id", "iType", "mass", "r", "p", "f", "rho", "fi", "e", "nAtoms", "pot",
+                  "comment", "stress", "defgrad", "bf", "ch_pot"],
+    "pmd_base_potential_t": ["cutoff", "mass", "force", "destroy"],
+    "potentialarray_t": ["n", "x0", "xn", "invDx", "values"],
+    "eampotential_t": ["cutoff", "mass", "force", "destroy", "phi", "rho", "f", "lat"],
+    "eam_cheby_t": ["cutoff", "mass", "phi", "rho", "f", "dphi", "drho", "df", "lat"],
+    "ljpotential_t": ["cutoff", "mass", "force", "destroy", "sigma", "epsilon"],
+}
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _probe_source():
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "pmdTypes.h"',
+             '#include "ljTypes.h"',
+             # memUtils.h's inline allocators name two of the reference's
+             # functions; the probe never calls them
+             "void breakinme() {}", "int suAbort(int status, char *msg) { (void)msg; return status; }",
+             "int main(void) {"]
+    for st, mem in MEMBERS.items():
+        lines.append(f'  printf("{st} sizeof %zu\\n", sizeof({st}));')
+        for m in mem:
+            lines.append(f'  printf("{st} {m} %zu %zu\\n", offsetof({st}, {m}), '
+                         f'sizeof((({st} *)0)->{m}));')
+    lines += ["  return 0;", "}"]
+    return "\n".join(lines) + "\n"
+
+
+def test_simflat_layout_matches_reference_headers(tmp_path):
+    ref = reference_dir()
+    if ref is None:
+        pytest.skip("reference sources not present on this machine")
+    probe = tmp_path / "probe.c"
+    probe.write_text(_probe_source())
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-DDOUBLE", "-I", os.path.join(ref, "src-flat", "include"),
+                    str(probe), "-o", str(exe)], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    asserts = ["#include <stddef.h>", '#include "comdgb_simflat.h"']
+    n = 0
+    for line in out.splitlines():
+        f = line.split()
+        if f[1] == "sizeof":
+            asserts.append(f'_Static_assert(sizeof({f[0]}) == {f[2]}, "sizeof {f[0]}");')
+        else:
+            asserts.append(f'_Static_assert(offsetof({f[0]}, {f[1]}) == {f[2]}, '
+                           f'"offsetof {f[0]}.{f[1]}");')
+            asserts.append(f'_Static_assert(sizeof((({f[0]} *)0)->{f[1]}) == {f[3]}, '
+                           f'"sizeof {f[0]}.{f[1]}");')
+        n += 1
+    assert n == sum(len(m) + 1 for m in MEMBERS.values())
+    check = tmp_path / "layout_check.c"
+    check.write_text("\n".join(asserts) + "\n")
+    r = subprocess.run(["gcc", "-std=c11", "-c", "-I", os.path.join(ROOT, "include"), str(check),
+                        "-o", str(tmp_path / "layout_check.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
