@@ -375,6 +375,7 @@ def gpu_arm(args):
     elapsed_s = dist.max(span_ms / 1e3)
     value = dist.sum(natoms * args.steps) / elapsed_s
     pairs = mixed.pair_count()
+    launches = mixed.step_launches(args.steps)  # before any recapture below
 
     # energy drift over 1000 steps (warmup + timed + the rest, untimed)
     done = args.warmup + args.steps
@@ -530,7 +531,7 @@ def gpu_arm(args):
         "energy_drift_ha_per_atom": drift, "drift_steps": args.drift_steps,
         "neighbour_lists": lists, "pairs_per_step": pairs, "pair_evals_per_s": pairs * args.steps / (span_ms / 1e3),
         "kernel_groups": groups, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "gpu_launches": mixed.step_launches(args.steps), "clocks": clk,
+        "gpu_launches": launches, "clocks": clk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

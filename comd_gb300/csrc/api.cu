@@ -232,9 +232,13 @@ void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
 // function's largest magnitude on the interval -- so derivative series that
 // are not the derivatives of phi and rho drop the table (series path).
 // Returns 0, or -1 when device memory ran out.
+// no table: every pair distance lies below s_lo, so the kernels take the
+// series for every pair and never index the (absent) table
+PairSeg no_pair_seg() { return PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0}; }
+
 int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
                    const double b[6], double pair_lo, double rc, PairSeg *out) {
-  *out = PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0};
+  *out = no_pair_seg();
   double lo = pair_lo;
   for (int s : {0, 1, 3, 4}) lo = std::max(lo, a[s]);
   if (!(lo > 0.0 && lo < rc)) return 0;
@@ -409,8 +413,7 @@ int cgapi::install_cheby(comdgb_sim *h, const double coef[6][CG_NCHEB], const do
   fill_cheb(h->eam64c.ch, h->eam32c.ch, h->eam32c.chlo, coef, a, b, h->pair_lo);
   if (build_pair_seg(h, coef, a, b, h->pair_lo, h->cutoff, &h->seg_built))
     return set_err(COMDGB_ERR_NOMEM, "cudaMalloc failed for the pair segment table");
-  h->eam32c.seg = h->seg_built;
-  if (h->pair_table_off) h->eam32c.seg.n = 0;  // the series for every pair
+  h->eam32c.seg = h->pair_table_off ? no_pair_seg() : h->seg_built;
   for (int q = 0; q < 6; q++) {
     for (int j = 0; j < CG_NCHEB; j++) h->cheb_coef[q][j] = coef[q][j];
     h->cheb_a[q] = a[q];
@@ -1215,6 +1218,9 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
       h->fo.pos = track(h, dalloc<float4>(n1, &err));
       h->fo.slot = track(h, dalloc<int>(n1, &err));
       h->fo.pf = track(h, dalloc<float4>(n1, &err));
+      h->fo.cut = track(h, dalloc<uint32_t>(rows * vcap, &err));
+      h->fo.ncut = track(h, dalloc<int>(n1, &err));
+      h->fo.emb = track(h, dalloc<float>(n1, &err));
       const double hs = 0.5 * h->skin - 1e-5;  // FP32 displacements err by < 1e-6 A
       h->fo.half_skin2 = (float)(hs * hs);
     } else {
@@ -1544,7 +1550,7 @@ int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   if (build_threads == 0) build_threads = 128;
   if (build_atoms == 0) build_atoms = 4;
-  if (pass2_threads == 0) pass2_threads = 256;
+  if (pass2_threads == 0) pass2_threads = 512;
   if ((build_threads != 64 && build_threads != 128 && build_threads != 256) ||
       (build_atoms != 2 && build_atoms != 4 && build_atoms != 8) ||
       (pass2_threads != 128 && pass2_threads != 256 && pass2_threads != 512))
@@ -1568,8 +1574,7 @@ int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int
 int comdgb_sim_set_pair_table(comdgb_sim *h, int on) {
   if (!h) return set_err(COMDGB_ERR_ARG, "null handle");
   h->pair_table_off = !on;
-  h->eam32c.seg = h->seg_built;
-  if (h->pair_table_off) h->eam32c.seg.n = 0;
+  h->eam32c.seg = h->pair_table_off ? no_pair_seg() : h->seg_built;
   drop_graphs(h);  // the captured kernels hold the table by value
   return 0;
 }

@@ -183,6 +183,12 @@ struct ForceOrder {
   int *slot;         // [ntot] current slot of a (kept by the rebin)
   float4 *pf;        // [ntot] EAM: pos with w = F'(rho) of a (written by pass 1 for pass 2)
   float half_skin2;    // rebuild when an atom moved more than this squared
+  // EAM: the pairs of this force call.  The density pass (pass 1) walks the
+  // skin list and writes the entries within the cutoff, in the list's
+  // transposed layout, for the force pass (pass 2).
+  uint32_t *cut;     // [rows*vcap] entries with r^2 <= rc^2
+  int *ncut;         // [ntot] their count (> vcap: the skin list overflowed)
+  float *emb;        // [ntot] F(rho) of a, from pass 1 (the per-atom energy's embedding part)
 };
 
 // the slot of an atom moved by the rebin, in the maps the list mode keeps

@@ -928,13 +928,12 @@ __global__ void __launch_bounds__(PASS_THREADS)
 // ---------------------------------------------------------------------------
 // Force-order passes (mixed precision, persistent lists)
 // ---------------------------------------------------------------------------
-constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
+constexpr int FO1_THREADS = 512;  // pass 1 (density): 2 CTAs of 64 registers per SM
 
 // list lines fetched ahead, unroll of the list walk and pass 2's register
-// cap (chosen by measurement; -D overrides for sweeps).  Pass 2 runs with
-// CTAs of 128 to 512 threads; its register count follows the cap, not the
-// CTA size (a launch bound of 512 threads let the compiler take 63-88
-// registers, and pass 2 ran 7-70 % slower).
+// cap (chosen by measurement; -D overrides for sweeps).  Pass 2 (the force
+// pass, five compensated sums) runs with CTAs of 128 to 512 threads; its
+// register count follows the cap, not the CTA size.
 #ifndef COMDGB_FO_PREFETCH
 #define COMDGB_FO_PREFETCH 4
 #endif
@@ -945,7 +944,12 @@ constexpr int FO1_THREADS = 512;  // pass 1: 2 CTAs of 64 registers per SM
 #define COMDGB_FO2_UNROLL 2  // pass 2
 #endif
 #ifndef COMDGB_FO2_MAXNREG
-#define COMDGB_FO2_MAXNREG 48
+#define COMDGB_FO2_MAXNREG 64
+#endif
+// 1: the density pass writes the entries within the cutoff (the cut list)
+// and the force pass walks them; 0: the force pass walks the skin list
+#ifndef COMDGB_FO_CUT
+#define COMDGB_FO_CUT 1
 #endif
 constexpr int FO_PREFETCH = COMDGB_FO_PREFETCH;
 constexpr int FO1_UNROLL = COMDGB_FO1_UNROLL, FO2_UNROLL = COMDGB_FO2_UNROLL;
@@ -954,16 +958,53 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
   asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
-// Visit the list of force-order atom a at FP32 position pi: fn(fj, dx, dy,
-// dz, r2) for every entry; with NEED_FI positions come from fo.pf and fj is
-// F'(rho_j) (its w), else fj is unspecified.  An overflowed list scans the
-// stencil of the atom's current slot instead.
-// MULTI: a batch of replicas (the box size comes from the atom's replica);
-// else replica 0's sizes are kernel-parameter constants (no registers held)
-template <bool NEED_FI, bool MULTI, int UNROLL = FO2_UNROLL, class F>
-__device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot, float4 pi,
-                                            float rc2, F &&fn) {
-  const int n = A.fo.n[a];
+// The box sizes of the pair offsets of force-order atom `slot`'s replica:
+// FP32 hi + lo, the y and z ones pre-scaled by 1/4 and 1/16 (their code
+// fields are read in place, x 4 and x 16, exactly).  MULTI: a batch of
+// replicas (the box size comes from the atom's replica); else replica 0's
+// sizes are kernel-parameter constants (no registers held).
+struct FoFrame {
+  float hx, hy, hz, lx, ly, lz;
+};
+template <bool MULTI>
+__device__ __forceinline__ FoFrame fo_frame(const ForceArgs &A, int slot) {
+  FoFrame f{A.g.hi0[0], A.g.hi0[1], A.g.hi0[2], A.g.lo0[0], A.g.lo0[1], A.g.lo0[2]};
+  if (MULTI) {
+    const RepGeo &R = rep_of(A.g, slot >> 6);
+    f = FoFrame{R.hi[0], R.hi[1], R.hi[2], R.lo[0], R.lo[1], R.lo[2]};
+  }
+  f.hy *= 0.25f, f.ly *= 0.25f, f.hz *= 0.0625f, f.lz *= 0.0625f;
+  return f;
+}
+
+// dr of list entry p = j << 6 | (dz+1) << 4 | (dy+1) << 2 | (dx+1) between
+// the atom at pi and its neighbour at q: (pi - q) - d * boxsize.  A field
+// f * 2^s in place, OR-ed into the bits of 2^23, is the float 2^23 + f *
+// 2^s: subtracted from 2^23 + 2^s it gives -d * 2^s exactly.
+__device__ __forceinline__ float fo_dr(const FoFrame &f, uint32_t p, float4 pi, float4 q,
+                                       float &dx, float &dy, float &dz) {
+  const float ex = 8388609.0f - __int_as_float(0x4B000000 | (int)(p & 0x3u));
+  const float ey = 8388612.0f - __int_as_float(0x4B000000 | (int)(p & 0xCu));
+  const float ez = 8388624.0f - __int_as_float(0x4B000000 | (int)(p & 0x30u));
+  dx = fmaf(ex, f.lx, fmaf(ex, f.hx, pi.x - q.x));
+  dy = fmaf(ey, f.ly, fmaf(ey, f.hy, pi.y - q.y));
+  dz = fmaf(ez, f.lz, fmaf(ez, f.hz, pi.z - q.z));
+  return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+
+// the transposed row of force-order atom a in a list of capacity vcap
+__device__ __forceinline__ size_t fo_row(int a, int vcap) {
+  return (size_t)(a >> 5) * vcap * 32 + (a & 31);
+}
+
+// Visit n entries of the list `lst` (a force-order list: skin or cut) of
+// force-order atom a at FP32 position pi: fn(fj, dx, dy, dz, r2) for every
+// entry; with NEED_FI positions come from fo.pf and fj is F'(rho_j) (its w),
+// else fj is unspecified.  n > vcap (the skin list overflowed): the stencil
+// of the atom's current slot is scanned instead.
+template <bool NEED_FI, bool MULTI, int UNROLL, class F>
+__device__ __forceinline__ void fo_walk(const ForceArgs &A, const uint32_t *list, int n, int a,
+                                        int slot, float4 pi, float rc2, F &&fn) {
   if (n > A.fo.vcap) {
     const float4 p = __ldg(A.s.pos32 + slot);
     scan_stencil<float>(A, slot >> 6, slot & 63, p.x, p.y, p.z, rc2,
@@ -972,17 +1013,8 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
                         });
     return;
   }
-  float hx = A.g.hi0[0], hy = A.g.hi0[1], hz = A.g.hi0[2];
-  float lx = A.g.lo0[0], ly = A.g.lo0[1], lz = A.g.lo0[2];
-  if (MULTI) {
-    const RepGeo &R = rep_of(A.g, slot >> 6);
-    hx = R.hi[0], hy = R.hi[1], hz = R.hi[2];
-    lx = R.lo[0], ly = R.lo[1], lz = R.lo[2];
-  }
-  // the y and z fields are read in place (x 4, x 16): their box sizes are
-  // scaled by 1/4 and 1/16, exactly
-  hy *= 0.25f, ly *= 0.25f, hz *= 0.0625f, lz *= 0.0625f;
-  const uint32_t *lst = A.fo.list + (size_t)(a >> 5) * A.fo.vcap * 32 + (a & 31);
+  const FoFrame fr = fo_frame<MULTI>(A, slot);
+  const uint32_t *lst = list + fo_row(a, A.fo.vcap);
   const float4 *pj = NEED_FI ? A.fo.pf : A.fo.pos;
   // the warp's list lines stream from HBM: pull line t + FO_PREFETCH into L1
   // while line t is used (within this atom's list only)
@@ -990,64 +1022,257 @@ __device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot,
   for (int t = 0; t < n; t++) {
     if (t + FO_PREFETCH < n) prefetch_l1(lst + (size_t)(t + FO_PREFETCH) * 32);
     const uint32_t p = __ldg(lst + (size_t)t * 32);
-    const int j = (int)(p >> 6);
-    const float4 q = __ldg(pj + j);
-    // entry = j << 6 | (dz+1) << 4 | (dy+1) << 2 | (dx+1); the pair offset
-    // is -d * boxsize.  A field f * 2^s in place, OR-ed into the bits of
-    // 2^23, is the float 2^23 + f * 2^s: subtracted from 2^23 + 2^s it gives
-    // -d * 2^s exactly.
-    const float ex = 8388609.0f - __int_as_float(0x4B000000 | (int)(p & 0x3u));
-    const float ey = 8388612.0f - __int_as_float(0x4B000000 | (int)(p & 0xCu));
-    const float ez = 8388624.0f - __int_as_float(0x4B000000 | (int)(p & 0x30u));
-    const float dx = fmaf(ex, lx, fmaf(ex, hx, pi.x - q.x));
-    const float dy = fmaf(ey, ly, fmaf(ey, hy, pi.y - q.y));
-    const float dz = fmaf(ez, lz, fmaf(ez, hz, pi.z - q.z));
-    fn(q.w, dx, dy, dz, fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+    const float4 q = __ldg(pj + (p >> 6));
+    float dx, dy, dz;
+    const float r2 = fo_dr(fr, p, pi, q, dx, dy, dz);
+    fn(q.w, dx, dy, dz, r2);
   }
 }
 
-#ifdef COMDGB_FO1_MAXNREG  // sweep variant: a register cap instead of 2 CTAs of 64
+// the skin list of force-order atom a
+template <bool NEED_FI, bool MULTI, int UNROLL = FO2_UNROLL, class F>
+__device__ __forceinline__ void fo_for_each(const ForceArgs &A, int a, int slot, float4 pi,
+                                            float rc2, F &&fn) {
+  fo_walk<NEED_FI, MULTI, UNROLL>(A, A.fo.list, A.fo.n[a], a, slot, pi, rc2, fn);
+}
+
+// ---------------------------------------------------------------------------
+// Force-order EAM (mixed precision, persistent lists): the density pass with
+// the embedding fused in, then the force pass.  The reference's pass 1
+// (eam.c:484-549) computes phi, phi' and rho per pair and pass 3
+// (eam.c:595-653) rho'; here the density pass needs rho alone, and the
+// force pass takes phi (the pair energy), phi' and rho' together, so every
+// per-atom force component is one compensated sum.  The pass criteria stay
+// the reference's: phi, phi' and rho for r^2 <= rc^2, the embedding force
+// and stress for r^2 < rc^2.
+// ---------------------------------------------------------------------------
+
+// rho(r) of one pair distance: the rho cubics of the FP32 pair table (sm),
+// or the table evaluator.  false: below the pair table (the series, in a
+// second sweep)
+template <int EVAL>
+__device__ __forceinline__ bool fo_rho(const EamPot<float, EVAL> &P, const float4 *, float r2,
+                                       float &rho) {
+  float r, inv_r, v, d;
+  r_and_inv(r2, r, inv_r);
+  if (EVAL == EVAL_CHEBY) {
+    rho = cheb_series(P, 1, r);
+  } else {
+    table_eval(P.rho, r, v, d);
+    rho = v;
+  }
+  return true;
+}
+static __device__ __forceinline__ bool fo_rho(const EamPot<float, EVAL_CHEBY> &P,
+                                              const float4 *sm, float r2, float &rho) {
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  if (!(u >= 0.f)) return false;
+  const int k = min((int)u, P.seg.n - 1);
+  rho = seg_cubic(sm[k], u - (float)k);
+  return true;
+}
+template <int EVAL>
+__device__ __forceinline__ float fo_rho_series(const EamPot<float, EVAL> &, float) {
+  return 0.f;
+}
+static __device__ __noinline__ float fo_rho_series(const EamPot<float, EVAL_CHEBY> &P, float r2) {
+  float r, inv_r;
+  r_and_inv(r2, r, inv_r);
+  return cheb_series(P, 1, r);
+}
+
+// phi, phi'(r)/r and rho'(r)/r of one pair distance: both halves of the
+// pair table (sm), or the table evaluator.  false: below the pair table
+template <int EVAL>
+__device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL> &P, const float4 *, float r2,
+                                        float &phi, float &wphi, float &wrho) {
+  float r, inv_r, dphi, v, drho;
+  r_and_inv(r2, r, inv_r);
+  if (EVAL == EVAL_CHEBY) {
+    phi = cheb_series(P, 0, r);
+    dphi = cheb_series(P, 3, r);
+    drho = cheb_series(P, 4, r);
+  } else {
+    table_eval(P.phi, r, phi, dphi);
+    table_eval(P.rho, r, v, drho);
+  }
+  wphi = dphi * inv_r;
+  wrho = drho * inv_r;
+  return true;
+}
+static __device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL_CHEBY> &P,
+                                               const float4 *sm, float r2, float &phi,
+                                               float &wphi, float &wrho) {
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  if (!(u >= 0.f)) return false;
+  const int k = min((int)u, P.seg.n - 1);
+  const float t = u - (float)k;
+  const float4 cp = sm[k], cr = sm[P.seg.n + k];
+  phi = seg_cubic(cp, t);
+  wphi = P.seg.dscale * seg_dcubic(cp, t);
+  wrho = P.seg.dscale * seg_dcubic(cr, t);
+  return true;
+}
+// the series for a pair below the table (FP32 Chebyshev only)
+template <int EVAL>
+__device__ __forceinline__ void fo_pair_series(const EamPot<float, EVAL> &, float, float &,
+                                               float &, float &) {}
+static __device__ __noinline__ void fo_pair_series(const EamPot<float, EVAL_CHEBY> &P, float r2,
+                                                   float &phi, float &wphi, float &wrho) {
+  float r, inv_r, dphi, rho;
+  r_and_inv(r2, r, inv_r);
+  cheb_pair32(P, r, phi, dphi, rho);
+  wphi = dphi * inv_r;
+  wrho = cheb_series(P, 4, r) * inv_r;
+}
+
+// per-atom results of the density pass: F and F' fused in (eam.c:576-594)
+template <int EVAL>
+__device__ __forceinline__ void fo_density_store(const ForceArgs &A,
+                                                 const EamPot<float, EVAL> &P, const KSum &rh,
+                                                 int a, int slot, float4 pi, int cnt, int ncut) {
+  const double rho_i = rh.value();
+  float F, dF;
+  eam_embed<float, EVAL>(P, (float)rho_i, F, dF);
+  A.s.rho[slot] = rho_i;
+  A.s.fi[slot] = (double)dF;
+  A.s.fi32[slot] = dF;
+  A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
+  A.fo.emb[a] = F;
+  A.fo.ncut[a] = ncut;
+  A.nbr_n[a] = cnt;
+}
+
+#ifdef COMDGB_FO1_MAXNREG  // sweep variant: a register cap instead of the launch bound
 #define FO1_BOUNDS __maxnreg__(COMDGB_FO1_MAXNREG)
 #else
 #define FO1_BOUNDS __launch_bounds__(FO1_THREADS, 2)
 #endif
+
+// Density pass: rho_i = sum of rho(r_ij) over the skin list within the
+// cutoff, F(rho_i) and F'(rho_i); the entries within the cutoff are written
+// to the cut list for the force pass.
 template <int EVAL, bool MULTI>
 __global__ void FO1_BOUNDS
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);  // the rho cubics
+  const float rc2 = P.rc2;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
     const float4 pi = A.fo.pos[a];
-    Pass1Acc<float> acc;
-    acc.zero();
-    eam_pass1_sum(P, seg_sm, acc,
-                  [&](auto &&fn) {
-                    fo_for_each<false, MULTI, FO1_UNROLL>(A, a, slot, pi, P.rc2, fn);
-                  });
-    const float dF = eam_pass1_store(A, P, acc, slot);
-    A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
-    A.nbr_n[a] = acc.cnt;
+    const int n = A.fo.n[a];
+    KSum rh;
+    rh.zero();
+    int cnt = 0;
+    if (n > A.fo.vcap) {  // overflowed skin list: the stencil, no cut list
+      fo_walk<false, MULTI, 1>(A, A.fo.list, n, a, slot, pi, rc2,
+                               [&](float, float, float, float, float r2) {
+                                 if (r2 > rc2) return;
+                                 cnt++;
+                                 float rho;
+                                 if (!fo_rho(P, seg_sm, r2, rho)) rho = fo_rho_series(P, r2);
+                                 rh.add(rho);
+                               });
+      fo_density_store(A, P, rh, a, slot, pi, cnt, A.fo.vcap + 1);
+      continue;
+    }
+    const FoFrame fr = fo_frame<MULTI>(A, slot);
+    const size_t row = fo_row(a, A.fo.vcap);
+    const uint32_t *lst = A.fo.list + row;
+    uint32_t *cut = A.fo.cut + row;
+    bool low = false;
+#pragma unroll FO1_UNROLL
+    for (int t = 0; t < n; t++) {
+      if (t + FO_PREFETCH < n) prefetch_l1(lst + (size_t)(t + FO_PREFETCH) * 32);
+      const uint32_t p = __ldg(lst + (size_t)t * 32);
+      const float4 q = __ldg(A.fo.pos + (p >> 6));
+      float dx, dy, dz;
+      const float r2 = fo_dr(fr, p, pi, q, dx, dy, dz);
+      if (r2 > rc2) continue;
+      if (COMDGB_FO_CUT) cut[(size_t)cnt * 32] = p;
+      cnt++;
+      float rho;
+      if (fo_rho(P, seg_sm, r2, rho)) rh.add(rho);
+      else low = true;
+    }
+    if (low)  // pairs below the table: the series, in a second sweep
+      fo_walk<false, MULTI, 1>(A, A.fo.list, n, a, slot, pi, rc2,
+                               [&](float, float, float, float, float r2) {
+                                 if (r2 <= rc2 && below_seg(P, r2)) rh.add(fo_rho_series(P, r2));
+                               });
+    fo_density_store(A, P, rh, a, slot, pi, cnt, cnt);
   }
 }
 
-constexpr int FO2_MAX_THREADS = 512;  // pass 2 runs with 128, 256 (default) or 512
+// force pass: the per-atom sums
+struct ForceSums {
+  KSum fx, fy, fz, ep, sx;
+  __device__ __forceinline__ void zero() {
+    fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
+  }
+  // phi and w = phi'/r for r^2 <= rc^2; we = (F'_i + F'_j) rho'/r, zero
+  // unless r^2 < rc^2
+  __device__ __forceinline__ void add(float phi, float wphi, float we, float dx, float dy,
+                                      float dz) {
+    const float w = wphi + we;
+    fx.add(w * dx);
+    fy.add(w * dy);
+    fz.add(w * dz);
+    ep.add(phi);
+    sx.add(we * dx * dx);
+  }
+};
 
+constexpr int FO2_MAX_THREADS = 512;  // the force pass runs with 128, 256 (default) or 512
+
+// Force pass: f_i = sum over the cut list of (phi'(r) + (F'_i + F'_j)
+// rho'(r)) dr/r, the per-atom energy 1/2 sum phi + F(rho_i) and the
+// embedding x-x stress (eam.c:534-545, 644-649; f is +grad U as in the
+// reference).
 template <int EVAL, bool MULTI>
 __global__ void __maxnreg__(COMDGB_FO2_MAXNREG)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);  // phi and rho cubics
+  const float rc2 = P.rc2;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
     const float4 pi = A.fo.pf[a];
-    Pass2Acc<float> acc;
+    const float fii = pi.w;
+    const int n = COMDGB_FO_CUT ? A.fo.ncut[a] : A.fo.n[a];
+    ForceSums acc;
     acc.zero();
-    eam_pass2_sum(P, seg_sm, pi.w, acc,
-                  [&](auto &&fn) {
-                    fo_for_each<true, MULTI, FO2_UNROLL>(A, a, slot, pi, P.rc2, fn);
-                  });
-    eam_pass2_store(A, acc, slot, a);
+    bool low = false;
+    auto walk = [&](auto &&fn) {
+      fo_walk<true, MULTI, FO2_UNROLL>(A, COMDGB_FO_CUT ? A.fo.cut : A.fo.list, n, a, slot, pi,
+                                       rc2, fn);
+    };
+    walk([&](float fj, float dx, float dy, float dz, float r2) {
+      if (r2 > rc2) return;
+      float phi, wphi, wrho;
+      if (!fo_pair(P, seg_sm, r2, phi, wphi, wrho)) {
+        low = true;
+        return;
+      }
+      const float we = r2 < rc2 ? (fii + fj) * wrho : 0.f;
+      acc.add(phi, wphi, we, dx, dy, dz);
+    });
+    if (low)  // pairs below the table: the series, in a second sweep
+      walk([&](float fj, float dx, float dy, float dz, float r2) {
+        if (r2 > rc2 || !below_seg(P, r2)) return;
+        float phi, wphi, wrho;
+        fo_pair_series(P, r2, phi, wphi, wrho);
+        const float we = r2 < rc2 ? (fii + fj) * wrho : 0.f;
+        acc.add(phi, wphi, we, dx, dy, dz);
+      });
+    d4 fo;
+    fo.x = acc.fx.value();
+    fo.y = acc.fy.value();
+    fo.z = acc.fz.value();
+    fo.w = 0.5 * acc.ep.value() + (double)__ldg(A.fo.emb + a);
+    A.s.f[slot] = fo;
+    A.atom_stress[a] = acc.sx.value();
   }
 }
 

@@ -32,6 +32,13 @@ static size_t pass_smem(int pass, int eval) {
   return sizeof(float4) * (pass == 0 ? 2 : 1) * SEG_N;
 }
 
+// force order: the density pass stages the rho cubics of the pair table,
+// the force pass both halves
+static size_t fo_pass_smem(int pass, int eval) {
+  if (sizeof(FT) != 4 || eval != EVAL_CHEBY) return 0;
+  return sizeof(float4) * (pass == 0 ? 1 : 2) * SEG_N;
+}
+
 #if COMDGB_FT_FLOAT
 // resident CTAs per SM of the force-order builds with NT threads, for 2, 4
 // and 8 atoms per load
@@ -83,22 +90,25 @@ cudaError_t prepare_force_kernels<FT>() {
     e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[0][EVAL_TABLE],
                        FO1_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, false>, pass_smem(0, EVAL_CHEBY),
+      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, false>, fo_pass_smem(0, EVAL_CHEBY),
                          &g_fo_per_sm[0][EVAL_CHEBY], FO1_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[1][EVAL_TABLE]);
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[1][EVAL_TABLE],
+                         FO2_MAX_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, false>, pass_smem(1, EVAL_CHEBY),
-                         &g_fo_per_sm[1][EVAL_CHEBY]);
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, false>, fo_pass_smem(1, EVAL_CHEBY),
+                         &g_fo_per_sm[1][EVAL_CHEBY], FO2_MAX_THREADS);
     if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<false>, 0, &g_fo_per_sm[2][0]);
     if (e == cudaSuccess)
       e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, true>, 0, &dummy, FO1_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, true>, pass_smem(0, EVAL_CHEBY), &dummy,
-                         FO1_THREADS);
-    if (e == cudaSuccess) e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, true>, 0, &dummy);
+      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, true>, fo_pass_smem(0, EVAL_CHEBY),
+                         &dummy, FO1_THREADS);
     if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, true>, pass_smem(1, EVAL_CHEBY), &dummy);
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, true>, 0, &dummy, FO2_MAX_THREADS);
+    if (e == cudaSuccess)
+      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, true>, fo_pass_smem(1, EVAL_CHEBY),
+                         &dummy, FO2_MAX_THREADS);
     if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<true>, 0, &dummy);
     if (e == cudaSuccess) e = build_occupancy_nt<64>(g_build_per_sm[0]);
     if (e == cudaSuccess) e = build_occupancy_nt<128>(g_build_per_sm[1]);
@@ -179,14 +189,14 @@ template <int EVAL>
 void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st,
                    const Tune *tune) {
   if (A.ntot <= 0) return;
-  const size_t smem = P.seg.n > 0 ? pass_smem(pass, EVAL) : 0;
+  const size_t smem = P.seg.n > 0 ? fo_pass_smem(pass, EVAL) : 0;
   const bool multi = A.g.nrep > 1;
   if (pass == 0) {
     const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS);
     if (multi) fo_eam_pass1_kernel<EVAL, true><<<g0, FO1_THREADS, smem, st>>>(A, P);
     else fo_eam_pass1_kernel<EVAL, false><<<g0, FO1_THREADS, smem, st>>>(A, P);
   } else {
-    const int threads = tune ? tune->pass2_threads : PASS_THREADS;
+    const int threads = tune ? tune->pass2_threads : FO2_MAX_THREADS;
     int g1;
     if (tune && tune->pass2_blocks > 0) {
       const long need = ((long)A.ntot + threads - 1) / threads;
@@ -205,7 +215,7 @@ template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, E
 
 int fo_pass2_blocks(int eval, bool multi, int threads) {
   int per_sm = 0;
-  const size_t smem = pass_smem(1, eval);
+  const size_t smem = fo_pass_smem(1, eval);
   cudaError_t e;
   if (eval == EVAL_CHEBY)
     e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(

@@ -119,7 +119,7 @@ void launch_fo_reslot(const Geom &g, Slots s, const ForceOrder &fo, int ntot, cu
 // CTAs of the default shape)
 struct Tune {
   int build_threads = 128, build_atoms = 4;
-  int pass2_threads = 256, pass2_blocks = 0;
+  int pass2_threads = 512, pass2_blocks = 0;  // force pass: 2 CTAs of 512 per SM
 };
 
 // ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----

@@ -3,8 +3,9 @@
 An atom whose neighbour count exceeds the list capacity is computed by
 scanning its 27 neighbour boxes instead of its list (the reference's own
 loop, eam.c:484-549 and :595-653).  Capping the capacity below the real
-neighbour count (comdgb_sim_set_list_capacity) sends every atom, or about
-half of them, down that path:
+neighbour count (comdgb_sim_set_list_capacity) sends every atom (a capacity
+of 8), or the atoms with more than the 54 neighbours that a perfect lattice
+has within the list cutoff (a capacity of 54), down that path:
 
 * mixed precision, force order: a 40-step sequence across list rebuilds
   must give the trajectory of the uncapped run up to roundings.  Between
@@ -46,7 +47,7 @@ def _min_image(a, b, bounds):
     return d - np.round(d / bounds) * bounds
 
 
-@pytest.mark.parametrize("cap", [8, 57])
+@pytest.mark.parametrize("cap", [8, 54])
 def test_mixed_overflow_trajectory(oracle, cap):
     # 12^3 cells, box factor 1: 8 boxes of 5.4225 A per axis against a
     # 4.961 A cutoff, skin 0.4615 A (capped at box width minus cutoff); 600 K
@@ -96,7 +97,8 @@ def test_fp64_idkeyed_overflow_vs_oracle(oracle):
         d = cg.DeviceSim(c.s, cg.opts(cg.POT_EAM_CHEBY, cg.PREC_FP64, cheby_from_host=True))
         try:
             assert d.list_info()[0]
-            d.set_list_capacity(57)  # about half of the skin lists (~58 entries) overflow
+            # thermal atoms with more than the 54 lattice neighbours overflow
+            d.set_list_capacity(54)
             e, _ = d.steps(10, 1e-15)
             d.download(c.s)
         finally:
