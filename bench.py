@@ -39,10 +39,14 @@ WORKLOAD = {"name": "eam_cu_chebyshev_fcc100_stretch1.05_bf1.5_300K", "nx": 100,
             "nz": 100, "defgrad": 1.05, "bf": 1.5, "temp_k": 300.0, "seed": 2026, "dt_s": 1e-15}
 METRIC = "EAM atom-steps/s @4M atoms, 1 GB300: mixed vs FP64 at <=1e-5 force err"
 UNIT = "atom-steps/s"
-# algorithmic work (counted per unique in-cutoff pair / per atom; FMA = 2)
-FLOPS_PASS1_PER_PAIR = 443    # phi, phi', rho by Clenshaw (+ r, dr)
-FLOPS_PASS2_PER_PAIR = 132    # rho' by Clenshaw + embedding force
-FLOPS_EMBED_PER_ATOM = 208    # F, F' per atom (fused into pass 1)
+# algorithmic work (counted per unique in-cutoff pair / per atom; FMA = 2),
+# the reference's Chebyshev arithmetic: its pass 1 sums three series (phi,
+# phi', rho: 443 flops with r, dr and the sums) and its pass 3 one (rho': 132
+# with the embedding force).  Here the density pass sums one series (rho)
+# and the force pass three (phi, phi', rho'), so the counts swap kernels.
+FLOPS_PASS1_PER_PAIR = 132    # density pass: rho by Clenshaw (+ r, dr, the sum)
+FLOPS_PASS2_PER_PAIR = 443    # force pass: phi, phi', rho' by Clenshaw + the force
+FLOPS_EMBED_PER_ATOM = 208    # F, F' per atom (fused into the density pass)
 BYTES_VERLET_PER_ATOM = 120   # read r, p, f; write r, p (FP64)
 BYTES_ADVPOS_PER_ATOM = 72    # read r, p; write r (FP64)
 # CPU baselines (both arms): one process per host core, each an independent
@@ -492,8 +496,10 @@ def gpu_arm(args):
                 "peak_source": ("FP32 FMA throughput measured on this GPU by "
                                 "comdgb_fp32_fma_peak (no FP32 figure in MEASURED_PEAKS.json)"
                                 if dg.get("bound") == "fp32" else "MEASURED_PEAKS.json hbm_gbs"),
-                "algorithmic": f"{FLOPS_PASS1_PER_PAIR} flops/unique pair + "
-                               f"{FLOPS_EMBED_PER_ATOM}/atom, {pairs} pairs"}
+                "algorithmic": (f"{FLOPS_PASS2_PER_PAIR} flops/unique pair, {pairs} pairs"
+                                if dom == "force_pass2" else
+                                f"{FLOPS_PASS1_PER_PAIR} flops/unique pair + "
+                                f"{FLOPS_EMBED_PER_ATOM}/atom, {pairs} pairs")}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -551,10 +557,13 @@ def batch_arm(args):
     edge U{8..24} unit cells, temperature U(100, 1200) K, advanced together:
     a 50-step loop captured as one CUDA graph over all replicas.  The box
     factor and the skin, then the launch shapes (the list build's threads per
-    box and atoms per candidate load, pass 2's threads per CTA), are chosen by
-    timing every candidate on the batch itself (autotuner); the result is set
-    against the same 64 systems run one after another, each with its own
-    50-step graph and the same settings."""
+    box and atoms per candidate load, the force pass's threads per CTA), are
+    chosen by the library's autotuner (comdgb_batch_autotune, timing every
+    candidate on the batch itself, cached per GPU and system); the result is
+    set against the same 64 systems run one after another with the same
+    settings.  The launch structure is measured too: the cost of one kernel
+    node of the step graph against one grid-wide barrier of a persistent
+    kernel (comdgb_graph_node_cost, comdgb_grid_barrier_cost)."""
     import comd_gb300 as cg
     rng = np.random.default_rng(BATCH["seed"])
     R = BATCH["replicas"]
@@ -566,16 +575,10 @@ def batch_arm(args):
     nsteps = BATCH["steps"]
 
     def build(bf):
-        """the replicas at box factor bf, or None when a box of some replica
-        would pass the reference's 64 atoms (createFccLattice aborts)"""
         sims = []
         for r in range(R):
             n = int(edges[r])
-            try:
-                s = cg.fcc(n, n, n, lat, 1.0, bf, pot)
-            except cg.ComdgbError:
-                free(sims)
-                return None
+            s = cg.fcc(n, n, n, lat, 1.0, bf, pot)
             cg.seed(s, BATCH["seed"] + r, cg.DISP_NONE, 0.0, float(temps[r]), mass)
             sims.append(s)
         return sims
@@ -587,78 +590,47 @@ def batch_arm(args):
     def o(skin):
         return cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, skin=skin)
 
-    tried = []
-    for bf in BATCH["bf"]:
-        sims = build(bf)
-        if sims is None:
-            tried.append({"bf": bf, "skipped": "a replica's box would exceed 64 atoms"})
-            continue
-        for skin in BATCH["skin"]:
-            b = cg.Batch(sims, o(skin))
-            try:
-                b.graph_steps(5)
-                ms = b.graph_steps(20)
-            finally:
-                b.close()
-            tried.append({"bf": bf, "skin_A": skin, "ms_per_step": ms / 20,
-                          "atom_steps_per_s": natoms * 20 / (ms * 1e-3)})
-        free(sims)
-    best = max((t for t in tried if "atom_steps_per_s" in t), key=lambda t: t["atom_steps_per_s"])
-    sims = build(best["bf"])
-    # second stage: launch shapes at the chosen box factor and skin -- the
-    # list build's threads per box (threads per cell) and atoms per candidate
-    # load (cell tile), then pass 2's threads per CTA
-    shapes = []
-
-    def time_shape(bt, ba, pt):
-        b = cg.Batch(sims, o(best["skin_A"]))
-        try:
-            b.set_launch(bt, ba, pt)
-            b.graph_steps(5)
-            ms = b.graph_steps(30)
-        finally:
-            b.close()
-        rec = {"build_threads": bt, "build_atoms": ba, "pass2_threads": pt,
-               "ms_per_step": ms / 30, "atom_steps_per_s": natoms * 30 / (ms * 1e-3)}
-        shapes.append(rec)
-        return rec
-
-    for bt in (64, 128, 256):
-        for ba in (2, 4, 8):
-            time_shape(bt, ba, 256)
-    sb = max(shapes, key=lambda t: t["atom_steps_per_s"])
-    for pt in (128, 512):
-        time_shape(sb["build_threads"], sb["build_atoms"], pt)
-    shape = max(shapes, key=lambda t: t["atom_steps_per_s"])
-    launch = (shape["build_threads"], shape["build_atoms"], shape["pass2_threads"])
+    base = build(1.0)
     try:
-        b = cg.Batch(sims, o(best["skin_A"]))
+        t0 = time.perf_counter()
+        tune = cg.batch_autotune(base, o(None), BATCH["bf"], BATCH["skin"], steps=20,
+                                 cache_path=args.tune_cache or None)
+        tune_s = time.perf_counter() - t0
+    finally:
+        free(base)
+    sims = build(tune.box_factor)
+    try:
+        b = cg.Batch(sims, o(tune.skin))
         try:
-            b.set_launch(*launch)
+            b.apply_tune(tune)
             b.graph_steps(nsteps)  # capture + warm
             clk = ClockSampler(0)
             clk.start()
             times = [b.graph_steps(nsteps) for _ in range(max(args.steps // nsteps, 3))]
             clocks = clk.stop()
             e, _ = b.energies()
+            b.steps(2)  # the step graphs (their kernel counts), after the timed loops
+            per_step = b.step_launches(nsteps) / nsteps
         finally:
             b.close()
         t_batch = statistics.median(times)
         # the same systems one after another
         t_seq = 0.0
         for r in range(R):
-            d = cg.DeviceSim(sims[r], o(best["skin_A"]))
+            d = cg.DeviceSim(sims[r], o(tune.skin))
             try:
                 if d.list_info()[0]:
-                    d.set_launch(*launch)
+                    d.apply_tune(tune)
                 d.graph_steps(nsteps)
                 t_seq += d.graph_steps(nsteps)
             finally:
                 d.close()
     finally:
         free(sims)
+    node_us, barrier_us = cg.lib.launch_probes(0)
     value = natoms * nsteps / (t_batch * 1e-3)
     seq = natoms * nsteps / (t_seq * 1e-3)
+    ms_step = t_batch / nsteps
     print(json.dumps({
         "metric": "EAM atom-steps/s, 64 uneven replicas in one launch per kernel, 1 GB300",
         "value": value, "unit": UNIT, "n_gpus": 1, "steps": nsteps, "higher_is_better": True,
@@ -669,8 +641,18 @@ def batch_arm(args):
                    "loop": f"{nsteps} steps captured as one CUDA graph"},
         "ms_per_loop": t_batch, "sequential_64": {"value": seq, "ms_total": t_seq},
         "speedup_vs_sequential": value / seq,
-        "autotune": {"chosen": dict(best, launch_shape=shape), "candidates": tried,
-                     "launch_shapes": shapes},
+        "autotune": {"chosen": tune.as_dict(), "seconds": tune_s,
+                     "candidates": {"box_factor": BATCH["bf"], "skin_A": BATCH["skin"],
+                                    "build_threads": [64, 128, 256], "build_atoms": [2, 4, 8],
+                                    "pass2_threads": [128, 256, 512]},
+                     "cache": args.tune_cache or None},
+        "launch_structure": {
+            "kernels_per_step_graph": per_step, "graph_node_us": node_us,
+            "grid_barrier_us": barrier_us, "ms_per_step": ms_step,
+            "node_overhead_frac": per_step * node_us * 1e-3 / ms_step,
+            "what": "a persistent step kernel would save at most the graph's kernel nodes "
+                    "(kernels_per_step_graph x graph_node_us) and pay a grid-wide barrier "
+                    "per phase instead"},
         "energy_per_atom_ha": {"min": float(min(e / (4 * edges ** 3))),
                                "max": float(max(e / (4 * edges ** 3)))},
         "clocks": clocks}))
@@ -927,6 +909,8 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=20)
     ap.add_argument("--series-steps", type=int, default=20,
                     help="steps of the mixed-precision run with the series evaluator")
+    ap.add_argument("--tune-cache", default="",
+                    help="autotune cache file of the batch workload (default: none)")
     ap.add_argument("--no-oracle", action="store_true",
                     help="skip the FP64 oracle force call on the full-size state")
     ap.add_argument("--drift-steps", type=int, default=1000)

@@ -43,6 +43,8 @@ UNITS = [
     ("virial.cu", []),
     ("clsman_io.cu", []),
     ("centro.cu", ["-fmad=false"]),
+    ("autotune.cu", []),
+    ("probes.cu", []),
 ]
 CUNITS = ["host_setup.c"]
 

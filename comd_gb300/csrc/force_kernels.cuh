@@ -257,7 +257,7 @@ __device__ __forceinline__ int stage_entries(const ForceArgs &A, int b, int *s_b
       int jb = A.et.box[b * CG_NNBR + e];
       s_box[e] = jb;
       s_dr[e] = PrecT<T>::drbox(A.et, b * CG_NNBR + e);
-      n = A.s.natoms[jb];
+      n = min(A.s.natoms[jb], CG_MAXATOMS);  // (more only in a reported overflow)
     }
     int x = n;  // inclusive warp scan
     for (int o = 1; o < 32; o <<= 1) {

@@ -239,6 +239,58 @@ simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double
   return s;
 }
 
+/* A copy of s with its atoms binned on a grid of box factor bf
+ * (allocDomains, domains.c:155-200, then putAtomInBox, domains.c:237-291,
+ * once per atom in id order at its world position, box corner + r); ids,
+ * types, masses and momenta are kept, forces zero.  Fails with
+ * COMDGB_ERR_MAXATOMS when a box of the new grid would pass 64 atoms. */
+simflat_t *comdgb_rebin_host(const simflat_t *src, double bf, int *status) {
+  int st = 0;
+  if (!src || !src->pot || !(bf > 0.0)) {
+    if (status) *status = COMDGB_ERR_ARG;
+    return NULL;
+  }
+  simflat_t *s = (simflat_t *)zalloc(sizeof *s);
+  if (!s) { if (status) *status = COMDGB_ERR_NOMEM; return NULL; }
+  s->pot = src->pot;
+  s->comment = (char *)zalloc(1024);
+  s->defgrad = src->defgrad;
+  s->bf = bf;
+  s->ch_pot = src->ch_pot;
+  for (int j = 0; j < 3; j++) s->bounds[j] = src->bounds[j];
+  st = s->comment ? alloc_domains(s) : COMDGB_ERR_NOMEM;
+  /* slot of every id in the source */
+  int *slot_of = st ? NULL : (int *)malloc(sizeof(int) * (size_t)(src->ntot > 0 ? src->ntot : 1));
+  if (!st && !slot_of) st = COMDGB_ERR_NOMEM;
+  if (!st) {
+    for (int i = 0; i < src->ntot; i++) slot_of[i] = -1;
+    for (int b = 0; b < src->nboxes && !st; b++)
+      for (int k = 0; k < src->natoms[b]; k++) {
+        const int off = b * COMDGB_MAXATOMS + k, id = src->id[off];
+        if (id < 0 || id >= src->ntot || slot_of[id] >= 0) {
+          st = COMDGB_ERR_ARG;  /* ids must be 0..ntot-1, each once */
+          break;
+        }
+        slot_of[id] = off;
+      }
+    for (int id = 0; id < src->ntot && !st; id++) {
+      const int off = slot_of[id];
+      if (off < 0) { st = COMDGB_ERR_ARG; break; }
+      const int b = off / COMDGB_MAXATOMS;
+      double x[3];
+      for (int m = 0; m < 3; m++) x[m] = src->dcenter[b][m] + src->r[off][m];
+      st = put_atom(s, id, src->iType[off], src->mass[off], x, src->p[off]);
+    }
+  }
+  free(slot_of);
+  if (status) *status = st;
+  if (st) {
+    comdgb_sim_free_host(s);
+    return NULL;
+  }
+  return s;
+}
+
 /* The whole file into memory (gzip through zlib when the library was built
  * with it); NUL-terminated.  Returns NULL on failure with *st set. */
 static char *read_all(const char *path, int *st) {

@@ -37,6 +37,15 @@ class Opts(C.Structure):
                 ("list_mode", C.c_int), ("skin", C.c_double)]
 
 
+class Tune(C.Structure):
+    _fields_ = [("box_factor", C.c_double), ("skin", C.c_double), ("build_threads", C.c_int),
+                ("build_atoms", C.c_int), ("pass2_threads", C.c_int),
+                ("ms_per_step", C.c_double), ("from_cache", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class ComdgbError(RuntimeError):
     def __init__(self, code, msg):
         super().__init__(f"libcomdgb error {code}: {msg}")
@@ -107,6 +116,15 @@ def _bind(lib):
     L.comdgb_sim_set_launch.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
     L.comdgb_sim_set_merge_rebox.argtypes = [C.c_void_p, C.c_int]
     L.comdgb_sim_set_list_capacity.argtypes = [C.c_void_p, C.c_int]
+    L.comdgb_batch_autotune.argtypes = [C.POINTER(P_SIM), C.c_int, C.c_void_p,
+                                        C.POINTER(C.c_double), C.c_int,
+                                        C.POINTER(C.c_double), C.c_int, C.c_int, C.c_double,
+                                        C.c_char_p, C.POINTER(Tune)]
+    L.comdgb_sim_apply_tune.argtypes = [C.c_void_p, C.POINTER(Tune)]
+    L.comdgb_graph_node_cost.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.comdgb_grid_barrier_cost.argtypes = [C.c_int, C.POINTER(C.c_double)]
+    L.comdgb_rebin_host.restype = P_SIM
+    L.comdgb_rebin_host.argtypes = [P_SIM, C.c_double, C.POINTER(C.c_int)]
     L.comdgb_sim_set_pair_table.argtypes = [C.c_void_p, C.c_int]
     L.comdgb_set_lazy.argtypes = [P_SIM, C.c_int]
     L.comdgb_sync_to_host.argtypes = [P_SIM]
@@ -304,6 +322,39 @@ def fcc(nx, ny, nz, lat, defgrad, bf, pot):
     return s
 
 
+def launch_probes(device=0):
+    """(us per empty graph kernel node, us per grid-wide barrier)"""
+    a, b = C.c_double(), C.c_double()
+    check(load().comdgb_graph_node_cost(device, C.byref(a)))
+    check(load().comdgb_grid_barrier_cost(device, C.byref(b)))
+    return a.value, b.value
+
+
+def rebin_host(s, bf):
+    """comdgb_rebin_host: a new host simflat_t with the atoms of s binned at
+    box factor bf (caller frees)"""
+    st = C.c_int(0)
+    out = load().comdgb_rebin_host(s, bf, C.byref(st))
+    if not out:
+        raise ComdgbError(st.value, "comdgb_rebin_host failed: " + last_error())
+    return out
+
+
+def batch_autotune(host_sims, o, box_factors=(), skins=(), steps=20, dt=1e-15,
+                   cache_path=None):
+    """comdgb_batch_autotune over the replicas; returns the Tune"""
+    n = len(host_sims)
+    arr = (P_SIM * n)(*host_sims)
+    bfs = (C.c_double * max(len(box_factors), 1))(*box_factors)
+    sks = (C.c_double * max(len(skins), 1))(*skins)
+    t = Tune()
+    check(load().comdgb_batch_autotune(arr, n, C.byref(o), bfs, len(box_factors), sks,
+                                       len(skins), steps, dt,
+                                       cache_path.encode() if cache_path else None,
+                                       C.byref(t)))
+    return t
+
+
 def seed(s, seed_value, disp_kind, amp, temp_k, mass_amu):
     load().comdgb_seed(s, seed_value, disp_kind, amp, temp_k, mass_amu)
 
@@ -481,6 +532,10 @@ class DeviceSim:
         """neighbour-list entries per atom in use (0: as allocated); atoms
         beyond it scan their neighbour boxes"""
         check(self.L.comdgb_sim_set_list_capacity(self.h, cap))
+
+    def apply_tune(self, t):
+        """the launch shapes of a batch_autotune result"""
+        check(self.L.comdgb_sim_apply_tune(self.h, C.byref(t)))
 
     def set_merge_rebox(self, on):
         """mixed precision: one rebox per step in a sequence of steps (default)

@@ -232,6 +232,45 @@ int comdgb_batch_download(comdgb_sim *h, int r, simflat_t *s);
 /* per-replica total energy and scalar stress of the last force call */
 int comdgb_batch_energies(comdgb_sim *h, double *e, double *stress);
 
+/* Batch autotuner.  No counterpart in the reference (one system, no
+ * tunable launches).  Times every (box factor, skin) candidate as a batch of
+ * the replicas rebinned at that box factor (`steps` steps as one CUDA graph
+ * after a warm-up replay), then at the best pair the list build's threads
+ * per box (64, 128, 256) and atoms per candidate load (2, 4, 8), then the
+ * force pass's threads per CTA (128, 256, 512).  nbf = 0: the replicas' own
+ * box factor; nskin = 0: o->skin.  Box factors at which a box of some
+ * replica would pass 64 atoms are skipped.  cache_path (NULL: none) is a
+ * text file keyed by the GPU, the replicas' sizes and bounds, the options
+ * and the candidates: a system tuned before returns at once with
+ * from_cache = 1; a new result is appended.  The caller adopts the box
+ * factor by building its replicas at it (comdgb_rebin_host does that for a
+ * host simflat_t), the skin through comdgb_opts.skin, and the launch shapes
+ * with comdgb_sim_apply_tune. */
+typedef struct comdgb_tune {
+  double box_factor;
+  double skin;
+  int build_threads, build_atoms, pass2_threads;
+  double ms_per_step;  /* measured for the choice (the cached value when from_cache) */
+  int from_cache;
+} comdgb_tune;
+int comdgb_batch_autotune(const simflat_t *const *sims, int n, const comdgb_opts *o,
+                          const double *box_factors, int nbf, const double *skins, int nskin,
+                          int steps, double dt, const char *cache_path, comdgb_tune *out);
+int comdgb_sim_apply_tune(comdgb_sim *h, const comdgb_tune *t);
+/* A new host simflat_t with the atoms of s binned at box factor bf
+ * (allocDomains then one putAtomInBox per atom in id order, domains.c:155-200,
+ * 237-291); COMDGB_ERR_MAXATOMS in *status when a box would pass 64 atoms.
+ * Free with comdgb_sim_free_host. */
+simflat_t *comdgb_rebin_host(const simflat_t *s, double bf, int *status);
+
+/* Launch-structure probes (no counterpart in the reference): the cost of one
+ * kernel node of a CUDA graph whose kernel does nothing (4 CTAs of 256
+ * threads per SM, as the step's stood-down launches), and of one grid-wide
+ * barrier inside a cooperative kernel of every resident CTA (what a
+ * persistent step kernel would pay between phases).  Microseconds. */
+int comdgb_graph_node_cost(int device, double *us_per_node);
+int comdgb_grid_barrier_cost(int device, double *us_per_barrier);
+
 /* ---------------- gradients and adjoint (FP64 simulations) ---------------- */
 /* Parameters.  EAM Chebyshev: the base series phi, rho, F -- coef[32*q + k],
  * q = 0 phi, 1 rho, 2 F, on [x0[q], xn[q]] -- whose derivative series follow

@@ -385,7 +385,11 @@ def test_dropin_force_and_steps(oracle):
 @pytest.mark.parametrize("precision", [cg.PREC_FP64, cg.PREC_MIXED])
 def test_persistent_lists_match_per_step_lists(oracle, precision):
     """Lists kept across steps (skin) give the same forces as lists rebuilt
-    every step, and trajectories with several rebuilds track the oracle."""
+    every step, and trajectories with several rebuilds track the oracle.
+    The same pairs: equal pair counts.  FP64 sums in the same order (energy
+    to 1e-12); mixed precision's force-order lists come in sub-cell order,
+    so its compensated FP32 per-atom sums may differ in the last bits
+    (energy to 1e-8)."""
     c = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), temp=1200.0, amp=0.05)
     try:
         dp = cg.DeviceSim(c.s, cg.opts(cg.POT_EAM_CHEBY, precision, cheby_from_host=True,
@@ -395,7 +399,9 @@ def test_persistent_lists_match_per_step_lists(oracle, precision):
         assert dp.list_info()[0] and not ds.list_info()[0]
         ep, _ = dp.force()
         es, _ = ds.force()
-        assert abs(ep - es) <= 1e-12 * abs(es)
+        assert dp.pair_count() == ds.pair_count()
+        tol = 1e-12 if precision == cg.PREC_FP64 else 1e-8
+        assert abs(ep - es) <= tol * abs(es)
         n = 40
         ep, _ = dp.steps(n, 1e-15)
         es, _ = ds.steps(n, 1e-15)
