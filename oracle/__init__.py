@@ -4,8 +4,8 @@ reference (oracle/_ref) behind one ctypes interface.
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
 load this package, as the checker; the GB300 library never calls it.
 """
-from .oracle import (KIND_EAM_CHEBY, KIND_EAM_TABLE, KIND_LJ, Oracle, RefLib, build,
-                     oracle_lib, ref_lib)
+from .oracle import (KIND_EAM_CHEBY, KIND_EAM_TABLE, KIND_LJ, Oracle, RefCentro, RefLib, build,
+                     oracle_lib, ref_centro, ref_lib)
 
-__all__ = ["Oracle", "RefLib", "oracle_lib", "ref_lib", "build", "KIND_EAM_TABLE",
+__all__ = ["Oracle", "RefLib", "RefCentro", "oracle_lib", "ref_lib", "ref_centro", "build", "KIND_EAM_TABLE",
            "KIND_EAM_CHEBY", "KIND_LJ"]

@@ -245,6 +245,54 @@ class RefLib:
         self.cheby = cheby
 
 
+class RefCentro:
+    """The reference visualiser's computeCentrosymmetry, compiled from its
+    text by oracle/Makefile (exact, or the -DAPPROX_CENTROSYM greedy
+    pairing), over a simulation's slot arrays."""
+
+    def __init__(self, approx=False):
+        name = "libcomdref_centro_approx.so" if approx else "libcomdref_centro.so"
+        path = os.path.join(HERE, "_ref", name)
+        if not os.path.exists(path):
+            raise FileNotFoundError(path)
+        lib = C.CDLL(path)
+        D = C.POINTER(C.c_double)
+        lib.refc_centro.restype = C.c_int
+        lib.refc_centro.argtypes = [C.c_int, C.POINTER(C.c_int), D, D, C.POINTER(C.c_int), D, D,
+                                    C.POINTER(C.c_float)]
+        self.lib = lib
+
+    def centro(self, s):
+        """(per-slot centrosymmetry [nslots], minCentro, maxCentro as floats)"""
+        v = s.contents
+        nb = v.nboxes
+        nbx = (C.c_int * 3)(*v.nbx)
+        bounds = (C.c_double * 3)(*v.bounds)
+        out = np.zeros(nb * 64)
+        mm = (C.c_float * 2)()
+        D = C.POINTER(C.c_double)
+        stride = self.lib.refc_centro(nb, nbx, bounds, C.cast(v.dcenter, D), v.natoms,
+                                      C.cast(v.r, D), out.ctypes.data_as(D), mm)
+        if stride != 64:
+            raise RuntimeError(f"reference MAXATOMS {stride} != 64")
+        return out, mm[0], mm[1]
+
+
+_centro_refs = {}
+
+
+def ref_centro(approx=False):
+    """RefCentro or None when oracle/_ref holds no centrosymmetry build."""
+    key = bool(approx)
+    with _lock:
+        if key not in _centro_refs:
+            try:
+                _centro_refs[key] = RefCentro(approx)
+            except (FileNotFoundError, OSError):
+                _centro_refs[key] = None
+        return _centro_refs[key]
+
+
 def ref_lib(cheby=False):
     """RefLib or None when oracle/_ref was not built on this machine."""
     key = bool(cheby)

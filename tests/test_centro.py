@@ -1,14 +1,22 @@
-"""Centrosymmetry parameter (comdgb_sim_centrosymmetry) against the oracle's
-restatement of the visualiser's computeCentrosymmetry
-(src-viz/AtomVisualize.c:399-672; the visualiser itself cannot be built
-here: it needs the VTK and OpenGL headers).  The restatement is checked by
-known answers of the physics: ~0 on a perfect lattice (the periodic offsets
-the visualiser rounds to float leave ~1e-12), and for the 12 neighbours of a
-vacancy the least pairing of its 11 remaining nearest neighbours and one
-second-shell atom at distance a, which is a^2/2, a^2 or 3a^2/2 depending on
-which second-shell atom is among the 12 (found by enumerating the six).
-The GPU values must equal the oracle's bit for bit."""
+"""Centrosymmetry parameter (comdgb_sim_centrosymmetry) against the
+reference visualiser's computeCentrosymmetry (src-viz/AtomVisualize.c:
+399-672).  The visualiser itself cannot be built here (VTK and OpenGL), but
+that one routine is arithmetic on the slot arrays: oracle/Makefile compiles
+its text inside a shim without graphics (oracle/_ref/libcomdref_centro*.so)
+and tests/golden/make_centro_golden.py records its per-atom values for
+fixed inputs in tests/golden/centro_reference.json.  The chain:
+  * the oracle's restatement (oracle/centro_oracle.c) equals the reference
+    routine bit for bit, live where the shim is built and against the
+    fixtures everywhere;
+  * the GPU values equal the fixtures and the oracle bit for bit.
+Known answers of the physics check the restatement as well: ~0 on a perfect
+lattice (the periodic offsets the visualiser rounds to float leave ~1e-12),
+and for the 12 neighbours of a vacancy the least pairing of its 11 remaining
+nearest neighbours and one second-shell atom at distance a, which is a^2/2,
+a^2 or 3a^2/2 depending on which second-shell atom is among the 12."""
+import json
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -16,6 +24,12 @@ import pytest
 import comd_gb300 as cg
 from comd_gb300.abi import occupied_mask, slot_views
 from helpers import Case
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+from make_centro_golden import by_id, centro_case, digest, layout_digest  # noqa: E402
+
+FIXTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                        "centro_reference.json")
 
 LAT = 3.615
 
@@ -95,6 +109,57 @@ def test_oracle_greedy_bounds_the_optimum(oracle):
         c.close()
 
 
+def fixture_cases():
+    with open(FIXTURES) as f:
+        return json.load(f)["cases"]
+
+
+def check_against_fixture(name, fx, s, compute):
+    """compute(s, approx) -> (per-slot values, min, max), checked against the
+    reference's recorded values; the range as the routine keeps it (floats,
+    maxCentro clamped to 100)"""
+    assert layout_digest(s) == fx["input"], f"{name}: input differs from the fixture's"
+    for key, approx in (("exact", False), ("approx", True)):
+        c, lo, hi = compute(s, approx)
+        vals = by_id(s, c)
+        want = fx[key]
+        assert vals[:len(want["first"])].tolist() == want["first"], (name, key)
+        assert digest(vals) == want["sha256"], (name, key)
+        assert float(np.float32(lo)) == want["min_centro"], (name, key)
+        assert min(float(np.float32(hi)), 100.0) == want["max_centro"], (name, key)
+
+
+@pytest.mark.parametrize("name", sorted(fixture_cases()))
+def test_oracle_centro_matches_reference_fixtures(oracle, name):
+    fx = fixture_cases()[name]
+    s, _pot = centro_case(fx["spec"])
+    try:
+        assert s.contents.ntot == fx["ntot"] and list(s.contents.nbx) == fx["nbx"]
+        check_against_fixture(name, fx, s, lambda t, a: oracle.centro(t, a))
+    finally:
+        cg.free_host(s)
+
+
+@pytest.mark.parametrize("approx", [False, True])
+def test_oracle_centro_matches_reference_live(oracle, approx):
+    """vacancies, Gaussian-seeded lattices, a 2-box grid and box factor 1.2
+    against the reference routine itself, where its shim is built"""
+    from oracle import ref_centro
+    ref = ref_centro(approx)
+    if ref is None:
+        pytest.skip("oracle/_ref holds no centrosymmetry build (no reference sources)")
+    sims, keep = cases(oracle)
+    try:
+        for name, s in sims:
+            co, lo, hi = oracle.centro(s, approx)
+            cr, rlo, rhi = ref.centro(s)
+            m = occupied_mask(s)
+            assert np.array_equal(co[m].view(np.uint64), cr[m].view(np.uint64)), name
+            assert float(np.float32(lo)) == rlo and min(float(np.float32(hi)), 100.0) == rhi, name
+    finally:
+        release(sims, keep)
+
+
 # ---------------------------------------------------------------- GPU ----
 
 def gpu_centro(s, approx=False):
@@ -127,6 +192,15 @@ def cases(oracle):
     return out, [c, c2, c3, ag_pot, p1, p2]
 
 
+def release(sims, keep):
+    for name, s in sims:
+        if name in ("perfect", "vacancies", "Ag 8k"):
+            cg.free_host(s)
+    for c in keep:
+        if isinstance(c, Case):
+            c.close()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("approx", [False, True])
 def test_gpu_centro_matches_oracle_bitwise(oracle, approx):
@@ -140,12 +214,18 @@ def test_gpu_centro_matches_oracle_bitwise(oracle, approx):
             assert np.all(cgpu[~m] == 0), name
             assert (glo, ghi) == (lo, hi), name
     finally:
-        for name, s in sims:
-            if name in ("perfect", "vacancies", "Ag 8k"):
-                cg.free_host(s)
-        for c in keep:
-            if isinstance(c, Case):
-                c.close()
+        release(sims, keep)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(fixture_cases()))
+def test_gpu_centro_matches_reference_fixtures(name):
+    fx = fixture_cases()[name]
+    s, _pot = centro_case(fx["spec"])
+    try:
+        check_against_fixture(name, fx, s, gpu_centro)
+    finally:
+        cg.free_host(s)
 
 
 @pytest.mark.gpu
