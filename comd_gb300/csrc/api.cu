@@ -454,8 +454,12 @@ void enqueue_classify_finish(comdgb_sim *h, bool lazy = false) {
                       lazy ? h->status : nullptr);
 }
 
-void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_rebox = false) {
-  // ev (optional) records after each group: compact, nbr, pass1, pass2
+void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_rebox = false,
+                         bool obs = true) {
+  // ev (optional) records after each group: compact, nbr, pass1, pass2.
+  // obs = false: a force call inside a step sequence, whose energies, stress,
+  // rho and F' the next force call overwrites before the caller can read
+  // them (the force-order passes then compute forces only)
   ForceArgs A = force_args(h);
   cudaStream_t st = h->stream;
   cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
@@ -472,16 +476,16 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_reb
     launch_rebuild_done(h->status, st);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     if (pot == COMDGB_POT_LJ) {
-      launch_fo_lj(A, h->lj32, st);
+      launch_fo_lj(A, h->lj32, st, obs);
       if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     } else if (pot == COMDGB_POT_EAM_TABLE) {
-      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 0, st);
+      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 0, st, &h->tune, obs);
       if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 1, st, &h->tune);
+      launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 1, st, &h->tune, obs);
     } else {
-      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 0, st);
+      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 0, st, &h->tune, obs);
       if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 1, st, &h->tune);
+      launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 1, st, &h->tune, obs);
     }
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     return;
@@ -572,7 +576,9 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
                       h->status);
     enqueue_classify_finish(h, lazy);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-    enqueue_force_parts(h, ev, evi, lazy);  // starts with the atom list of the new layout
+    // inside the sequence (OPEN, MID): the CLOSE part and the force call
+    // that ends nTimeSteps follow, so nothing reads this call's energies
+    enqueue_force_parts(h, ev, evi, lazy, part == PART_FULL);  // the atom list of the new layout
     if (part != PART_FULL) return;
   }
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
@@ -1561,11 +1567,11 @@ int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int
   h->tune.build_threads = build_threads;
   h->tune.build_atoms = build_atoms;
   h->tune.pass2_threads = pass2_threads;
-  h->tune.pass2_blocks =
-      h->mixed && h->opts.potential != COMDGB_POT_LJ
-          ? fo_pass2_blocks(h->opts.potential == COMDGB_POT_EAM_CHEBY ? EVAL_CHEBY : EVAL_TABLE,
-                            h->nrep > 1, pass2_threads)
-          : 0;
+  const bool fo_eam = h->mixed && h->opts.potential != COMDGB_POT_LJ;
+  const int eval = h->opts.potential == COMDGB_POT_EAM_CHEBY ? EVAL_CHEBY : EVAL_TABLE;
+  h->tune.pass2_blocks = fo_eam ? fo_pass2_blocks(eval, h->nrep > 1, pass2_threads, true) : 0;
+  h->tune.pass2_blocks_fast =
+      fo_eam ? fo_pass2_blocks(eval, h->nrep > 1, pass2_threads, false) : 0;
   CK(cudaGetLastError());
   drop_graphs(h);  // recaptured with the new shapes at the next call
   return 0;

@@ -943,6 +943,9 @@ constexpr int FO1_THREADS = 512;  // pass 1 (density): 2 CTAs of 64 registers pe
 #ifndef COMDGB_FO2_UNROLL
 #define COMDGB_FO2_UNROLL 2  // pass 2
 #endif
+#ifndef COMDGB_FO2F_MAXNREG  // the force pass without energies (OBS = false)
+#define COMDGB_FO2F_MAXNREG 64
+#endif
 #ifndef COMDGB_FO2_MAXNREG
 #define COMDGB_FO2_MAXNREG 64
 #endif
@@ -1127,18 +1130,20 @@ static __device__ __noinline__ void fo_pair_series(const EamPot<float, EVAL_CHEB
 }
 
 // per-atom results of the density pass: F and F' fused in (eam.c:576-594)
-template <int EVAL>
+template <int EVAL, bool OBS>
 __device__ __forceinline__ void fo_density_store(const ForceArgs &A,
                                                  const EamPot<float, EVAL> &P, const KSum &rh,
                                                  int a, int slot, float4 pi, int cnt, int ncut) {
   const double rho_i = rh.value();
   float F, dF;
   eam_embed<float, EVAL>(P, (float)rho_i, F, dF);
-  A.s.rho[slot] = rho_i;
-  A.s.fi[slot] = (double)dF;
+  if (OBS) {  // the host-visible rho, F' and the embedding energy
+    A.s.rho[slot] = rho_i;
+    A.s.fi[slot] = (double)dF;
+    A.fo.emb[a] = F;
+  }
   A.s.fi32[slot] = dF;
   A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
-  A.fo.emb[a] = F;
   A.fo.ncut[a] = ncut;
   A.nbr_n[a] = cnt;
 }
@@ -1151,8 +1156,10 @@ __device__ __forceinline__ void fo_density_store(const ForceArgs &A,
 
 // Density pass: rho_i = sum of rho(r_ij) over the skin list within the
 // cutoff, F(rho_i) and F'(rho_i); the entries within the cutoff are written
-// to the cut list for the force pass.
-template <int EVAL, bool MULTI>
+// to the cut list for the force pass.  OBS: a force call whose results the
+// caller can read (see the force pass); otherwise only what the force pass
+// needs is stored.
+template <int EVAL, bool MULTI, bool OBS>
 __global__ void FO1_BOUNDS
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
@@ -1174,7 +1181,7 @@ __global__ void FO1_BOUNDS
                                  if (!fo_rho(P, seg_sm, r2, rho)) rho = fo_rho_series(P, r2);
                                  rh.add(rho);
                                });
-      fo_density_store(A, P, rh, a, slot, pi, cnt, A.fo.vcap + 1);
+      fo_density_store<EVAL, OBS>(A, P, rh, a, slot, pi, cnt, A.fo.vcap + 1);
       continue;
     }
     const FoFrame fr = fo_frame<MULTI>(A, slot);
@@ -1201,15 +1208,21 @@ __global__ void FO1_BOUNDS
                                [&](float, float, float, float, float r2) {
                                  if (r2 <= rc2 && below_seg(P, r2)) rh.add(fo_rho_series(P, r2));
                                });
-    fo_density_store(A, P, rh, a, slot, pi, cnt, cnt);
+    fo_density_store<EVAL, OBS>(A, P, rh, a, slot, pi, cnt, cnt);
   }
 }
 
 // force pass: the per-atom sums
+// (OBS: also the pair energy and the embedding stress)
+template <bool OBS>
 struct ForceSums {
   KSum fx, fy, fz, ep, sx;
   __device__ __forceinline__ void zero() {
-    fx.zero(); fy.zero(); fz.zero(); ep.zero(); sx.zero();
+    fx.zero(); fy.zero(); fz.zero();
+    if (OBS) {
+      ep.zero();
+      sx.zero();
+    }
   }
   // phi and w = phi'/r for r^2 <= rc^2; we = (F'_i + F'_j) rho'/r, zero
   // unless r^2 < rc^2
@@ -1219,8 +1232,10 @@ struct ForceSums {
     fx.add(w * dx);
     fy.add(w * dy);
     fz.add(w * dz);
-    ep.add(phi);
-    sx.add(we * dx * dx);
+    if (OBS) {
+      ep.add(phi);
+      sx.add(we * dx * dx);
+    }
   }
 };
 
@@ -1230,8 +1245,13 @@ constexpr int FO2_MAX_THREADS = 512;  // the force pass runs with 128, 256 (defa
 // rho'(r)) dr/r, the per-atom energy 1/2 sum phi + F(rho_i) and the
 // embedding x-x stress (eam.c:534-545, 644-649; f is +grad U as in the
 // reference).
-template <int EVAL, bool MULTI>
-__global__ void __maxnreg__(COMDGB_FO2_MAXNREG)
+// OBS = false: the force calls inside a step sequence, whose energies and
+// stress the next force call overwrites before anything can read them (the
+// reference's nTimeSteps ends with its own computeForce, timestep.c:137):
+// forces only, f.w = 0.  Every force call whose results the caller can read
+// (a force call, the one ending nTimeSteps) is OBS.
+template <int EVAL, bool MULTI, bool OBS>
+__global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);  // phi and rho cubics
@@ -1241,7 +1261,7 @@ __global__ void __maxnreg__(COMDGB_FO2_MAXNREG)
     const float4 pi = A.fo.pf[a];
     const float fii = pi.w;
     const int n = COMDGB_FO_CUT ? A.fo.ncut[a] : A.fo.n[a];
-    ForceSums acc;
+    ForceSums<OBS> acc;
     acc.zero();
     bool low = false;
     auto walk = [&](auto &&fn) {
@@ -1270,9 +1290,9 @@ __global__ void __maxnreg__(COMDGB_FO2_MAXNREG)
     fo.x = acc.fx.value();
     fo.y = acc.fy.value();
     fo.z = acc.fz.value();
-    fo.w = 0.5 * acc.ep.value() + (double)__ldg(A.fo.emb + a);
+    fo.w = OBS ? 0.5 * acc.ep.value() + (double)__ldg(A.fo.emb + a) : 0.0;
     A.s.f[slot] = fo;
-    A.atom_stress[a] = acc.sx.value();
+    if (OBS) A.atom_stress[a] = acc.sx.value();
   }
 }
 
@@ -1324,7 +1344,8 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
 }
 
 // LJ in force order (mixed precision, persistent lists)
-template <bool MULTI>
+// (OBS as in the EAM force pass: energy and stress only where readable)
+template <bool MULTI, bool OBS>
 __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<float> P) {
   const float s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6, rc2 = P.rc2;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
@@ -1338,25 +1359,27 @@ __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<
       cnt++;
       float ir2 = 1.0f / r2;
       float r6 = ir2 * ir2 * ir2;
-      ep.add(0.5f * r6 * (s6 * r6 - 1.0f));
+      if (OBS) ep.add(0.5f * r6 * (s6 * r6 - 1.0f));
       float fr = c4 * r6 * ir2 * (s12 * r6 - 6.0f);
       fx.add(dx * fr);
       fy.add(dy * fr);
       fz.add(dz * fr);
-      sx.add(fr * dx * dx);
+      if (OBS) sx.add(fr * dx * dx);
     };
     fo_for_each<false, MULTI, FO1_UNROLL>(A, a, slot, A.fo.pos[a], rc2, fn);
-    int ne = A.et.n[b], nonempty = 0;
-    for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
-    d4 p = A.s.p[slot];
-    double kin = __ddiv_rn(__dmul_rn(p.x, p.x), A.s.mass[slot]);
     d4 fo;
     fo.x = fx.value();
     fo.y = fy.value();
     fo.z = fz.value();
-    fo.w = ep.value();
+    fo.w = OBS ? ep.value() : 0.0;
     A.s.f[slot] = fo;
-    A.atom_stress[a] = sx.value() - (double)nonempty * kin;
+    if (OBS) {
+      int ne = A.et.n[b], nonempty = 0;
+      for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
+      d4 p = A.s.p[slot];
+      double kin = __ddiv_rn(__dmul_rn(p.x, p.x), A.s.mass[slot]);
+      A.atom_stress[a] = sx.value() - (double)nonempty * kin;
+    }
     A.nbr_n[a] = cnt;
   }
 }

@@ -11,7 +11,8 @@ static size_t nbr_build_smem() {
 // resident CTAs per SM of the EAM pass kernels ([pass][eval]) and the SM
 // count, found before any launch or stream capture
 static int g_pass_per_sm[2][2];
-static int g_fo_per_sm[3][2];  // force order: [pass 1, pass 2, LJ][eval]
+// force order: [without, with energies][pass 1, pass 2, LJ][eval]
+static int g_fo_per_sm[2][3][2];
 static int g_num_sms = 1;
 // resident CTAs per SM of the FP32 list builds: force order [64, 128, 256
 // threads][2, 4, 8 atoms per load], per-step and id-keyed lists
@@ -57,6 +58,39 @@ static cudaError_t build_occupancy_nt(int *out) {
 }
 #endif
 
+#if COMDGB_FT_FLOAT
+// resident CTAs per SM of the force-order passes with or without energies
+// (g_fo_per_sm[OBS]); every variant's shared-memory limit set
+template <bool OBS>
+static cudaError_t fo_occupancy() {
+  int dummy = 0;
+  int(&o)[3][2] = g_fo_per_sm[OBS];
+  const size_t s0 = fo_pass_smem(0, EVAL_CHEBY), s1 = fo_pass_smem(1, EVAL_CHEBY);
+  cudaError_t e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, false, OBS>, 0,
+                                 &o[0][EVAL_TABLE], FO1_THREADS);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, false, OBS>, s0, &o[0][EVAL_CHEBY],
+                       FO1_THREADS);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, false, OBS>, 0, &o[1][EVAL_TABLE],
+                       FO2_MAX_THREADS);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, false, OBS>, s1, &o[1][EVAL_CHEBY],
+                       FO2_MAX_THREADS);
+  if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<false, OBS>, 0, &o[2][0]);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, true, OBS>, 0, &dummy, FO1_THREADS);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, true, OBS>, s0, &dummy, FO1_THREADS);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, true, OBS>, 0, &dummy, FO2_MAX_THREADS);
+  if (e == cudaSuccess)
+    e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, true, OBS>, s1, &dummy, FO2_MAX_THREADS);
+  if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<true, OBS>, 0, &dummy);
+  return e;
+}
+#endif
+
 // grid of a list build: one CTA per box, capped at the resident CTAs
 static int build_grid(int nboxes, int per_sm) {
   const long cap = (long)g_num_sms * per_sm;
@@ -86,30 +120,8 @@ cudaError_t prepare_force_kernels<FT>() {
   {
     // resident CTAs of the single-replica variants (the batch variants take
     // the same grids; they are grid-stride loops)
-    int dummy = 0;
-    e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[0][EVAL_TABLE],
-                       FO1_THREADS);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, false>, fo_pass_smem(0, EVAL_CHEBY),
-                         &g_fo_per_sm[0][EVAL_CHEBY], FO1_THREADS);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, false>, 0, &g_fo_per_sm[1][EVAL_TABLE],
-                         FO2_MAX_THREADS);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, false>, fo_pass_smem(1, EVAL_CHEBY),
-                         &g_fo_per_sm[1][EVAL_CHEBY], FO2_MAX_THREADS);
-    if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<false>, 0, &g_fo_per_sm[2][0]);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, true>, 0, &dummy, FO1_THREADS);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass1_kernel<EVAL_CHEBY, true>, fo_pass_smem(0, EVAL_CHEBY),
-                         &dummy, FO1_THREADS);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_TABLE, true>, 0, &dummy, FO2_MAX_THREADS);
-    if (e == cudaSuccess)
-      e = pass_occupancy(fo_eam_pass2_kernel<EVAL_CHEBY, true>, fo_pass_smem(1, EVAL_CHEBY),
-                         &dummy, FO2_MAX_THREADS);
-    if (e == cudaSuccess) e = pass_occupancy(fo_lj_kernel<true>, 0, &dummy);
+    e = fo_occupancy<false>();
+    if (e == cudaSuccess) e = fo_occupancy<true>();
     if (e == cudaSuccess) e = build_occupancy_nt<64>(g_build_per_sm[0]);
     if (e == cudaSuccess) e = build_occupancy_nt<128>(g_build_per_sm[1]);
     if (e == cudaSuccess) e = build_occupancy_nt<256>(g_build_per_sm[2]);
@@ -133,9 +145,9 @@ cudaError_t prepare_force_kernels<FT>() {
 
 // grid of a pass: every atom one thread, capped at the resident CTAs
 static int pass_grid(int pass, int eval, int ntot, bool fo = false,
-                     int threads = PASS_THREADS) {
+                     int threads = PASS_THREADS, bool obs = true) {
   long need = (ntot + threads - 1) / threads;
-  long cap = (long)g_num_sms * (fo ? g_fo_per_sm[pass][eval] : g_pass_per_sm[pass][eval]);
+  long cap = (long)g_num_sms * (fo ? g_fo_per_sm[obs][pass][eval] : g_pass_per_sm[pass][eval]);
   return (int)(need < cap ? need : cap);
 }
 
@@ -185,57 +197,76 @@ void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st, const Tun
 }
 
 #if COMDGB_FT_FLOAT
-template <int EVAL>
-void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st,
-                   const Tune *tune) {
-  if (A.ntot <= 0) return;
+template <int EVAL, bool OBS>
+static void launch_fo_eam_obs(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass,
+                              cudaStream_t st, const Tune *tune) {
   const size_t smem = P.seg.n > 0 ? fo_pass_smem(pass, EVAL) : 0;
   const bool multi = A.g.nrep > 1;
   if (pass == 0) {
-    const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS);
-    if (multi) fo_eam_pass1_kernel<EVAL, true><<<g0, FO1_THREADS, smem, st>>>(A, P);
-    else fo_eam_pass1_kernel<EVAL, false><<<g0, FO1_THREADS, smem, st>>>(A, P);
+    const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS, OBS);
+    if (multi) fo_eam_pass1_kernel<EVAL, true, OBS><<<g0, FO1_THREADS, smem, st>>>(A, P);
+    else fo_eam_pass1_kernel<EVAL, false, OBS><<<g0, FO1_THREADS, smem, st>>>(A, P);
   } else {
     const int threads = tune ? tune->pass2_threads : FO2_MAX_THREADS;
+    const int tuned = tune ? (OBS ? tune->pass2_blocks : tune->pass2_blocks_fast) : 0;
     int g1;
-    if (tune && tune->pass2_blocks > 0) {
+    if (tuned > 0) {
       const long need = ((long)A.ntot + threads - 1) / threads;
-      g1 = (int)(need < tune->pass2_blocks ? need : tune->pass2_blocks);
+      g1 = (int)(need < tuned ? need : tuned);
     } else {
-      g1 = pass_grid(1, EVAL, A.ntot, true, threads);
+      g1 = pass_grid(1, EVAL, A.ntot, true, threads, OBS);
     }
-    if (multi) fo_eam_pass2_kernel<EVAL, true><<<g1, threads, smem, st>>>(A, P);
-    else fo_eam_pass2_kernel<EVAL, false><<<g1, threads, smem, st>>>(A, P);
+    if (multi) fo_eam_pass2_kernel<EVAL, true, OBS><<<g1, threads, smem, st>>>(A, P);
+    else fo_eam_pass2_kernel<EVAL, false, OBS><<<g1, threads, smem, st>>>(A, P);
   }
 }
-template void launch_fo_eam<EVAL_TABLE>(const ForceArgs &, const EamPot<float, EVAL_TABLE> &,
-                                        int, cudaStream_t, const Tune *);
-template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, EVAL_CHEBY> &,
-                                        int, cudaStream_t, const Tune *);
 
-int fo_pass2_blocks(int eval, bool multi, int threads) {
+template <int EVAL>
+void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st,
+                   const Tune *tune, bool obs) {
+  if (A.ntot <= 0) return;
+  if (obs) launch_fo_eam_obs<EVAL, true>(A, P, pass, st, tune);
+  else launch_fo_eam_obs<EVAL, false>(A, P, pass, st, tune);
+}
+template void launch_fo_eam<EVAL_TABLE>(const ForceArgs &, const EamPot<float, EVAL_TABLE> &,
+                                        int, cudaStream_t, const Tune *, bool);
+template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, EVAL_CHEBY> &,
+                                        int, cudaStream_t, const Tune *, bool);
+
+template <int EVAL, bool OBS>
+static int fo_pass2_per_sm(bool multi, int threads) {
   int per_sm = 0;
-  const size_t smem = fo_pass_smem(1, eval);
-  cudaError_t e;
+  const size_t smem = fo_pass_smem(1, EVAL);
+  const cudaError_t e =
+      multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &per_sm, fo_eam_pass2_kernel<EVAL, true, OBS>, threads, smem)
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                  &per_sm, fo_eam_pass2_kernel<EVAL, false, OBS>, threads, smem);
+  return e != cudaSuccess || per_sm < 1 ? 1 : per_sm;
+}
+
+int fo_pass2_blocks(int eval, bool multi, int threads, bool obs) {
+  int per_sm;
   if (eval == EVAL_CHEBY)
-    e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, fo_eam_pass2_kernel<EVAL_CHEBY, true>, threads, smem)
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, fo_eam_pass2_kernel<EVAL_CHEBY, false>, threads, smem);
+    per_sm = obs ? fo_pass2_per_sm<EVAL_CHEBY, true>(multi, threads)
+                 : fo_pass2_per_sm<EVAL_CHEBY, false>(multi, threads);
   else
-    e = multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, fo_eam_pass2_kernel<EVAL_TABLE, true>, threads, 0)
-              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                    &per_sm, fo_eam_pass2_kernel<EVAL_TABLE, false>, threads, 0);
-  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+    per_sm = obs ? fo_pass2_per_sm<EVAL_TABLE, true>(multi, threads)
+                 : fo_pass2_per_sm<EVAL_TABLE, false>(multi, threads);
   return per_sm * g_num_sms;
 }
 
-void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st) {
+void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st, bool obs) {
   if (A.ntot <= 0) return;
-  const int grid = pass_grid(2, 0, A.ntot, true);
-  if (A.g.nrep > 1) fo_lj_kernel<true><<<grid, PASS_THREADS, 0, st>>>(A, P);
-  else fo_lj_kernel<false><<<grid, PASS_THREADS, 0, st>>>(A, P);
+  const int grid = pass_grid(2, 0, A.ntot, true, PASS_THREADS, obs);
+  const bool multi = A.g.nrep > 1;
+  if (obs) {
+    if (multi) fo_lj_kernel<true, true><<<grid, PASS_THREADS, 0, st>>>(A, P);
+    else fo_lj_kernel<false, true><<<grid, PASS_THREADS, 0, st>>>(A, P);
+  } else {
+    if (multi) fo_lj_kernel<true, false><<<grid, PASS_THREADS, 0, st>>>(A, P);
+    else fo_lj_kernel<false, false><<<grid, PASS_THREADS, 0, st>>>(A, P);
+  }
 }
 #endif
 

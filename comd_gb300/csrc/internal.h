@@ -120,6 +120,7 @@ void launch_fo_reslot(const Geom &g, Slots s, const ForceOrder &fo, int ntot, cu
 struct Tune {
   int build_threads = 128, build_atoms = 4;
   int pass2_threads = 512, pass2_blocks = 0;  // force pass: 2 CTAs of 512 per SM
+  int pass2_blocks_fast = 0;  // the same for the force pass without energies (OBS = false)
 };
 
 // ---- force_fp64.cu (T = double) / force_mixed.cu (T = float) ----
@@ -133,13 +134,15 @@ template <class T, int EVAL>
 void launch_eam_pass2(const ForceArgs &A, const EamPot<T, EVAL> &P, cudaStream_t st);
 template <class T>
 void launch_lj(const ForceArgs &A, const LjPot<T> &P, cudaStream_t st);
-// force order (mixed precision only, force_mixed.cu); pass 0 or 1
+// force order (mixed precision only, force_mixed.cu); pass 0 or 1.  obs:
+// the caller can read this force call's energies, stress, rho and F' (else
+// forces only: the force calls inside a step sequence)
 template <int EVAL>
 void launch_fo_eam(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass, cudaStream_t st,
-                   const Tune *tune = nullptr);
-// resident-CTA grid cap of pass 2 at `threads` per CTA (SMs x CTAs per SM);
-// call outside stream capture
-int fo_pass2_blocks(int eval, bool multi, int threads);
-void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st);
+                   const Tune *tune = nullptr, bool obs = true);
+// resident-CTA grid cap of pass 2 at `threads` per CTA (SMs x CTAs per SM),
+// with or without energies; call outside stream capture
+int fo_pass2_blocks(int eval, bool multi, int threads, bool obs = true);
+void launch_fo_lj(const ForceArgs &A, const LjPot<float> &P, cudaStream_t st, bool obs = true);
 
 }  // namespace cg
