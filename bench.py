@@ -379,7 +379,10 @@ def gpu_arm(args):
     elapsed_s = dist.max(span_ms / 1e3)
     value = dist.sum(natoms * args.steps) / elapsed_s
     pairs = mixed.pair_count()
-    launches = mixed.step_launches(args.steps)  # before any recapture below
+    # before any recapture below: the step graphs' kernels, plus the
+    # conditional rebuild section's once per rebuild
+    launches = (mixed.step_launches(args.steps)
+                + lists["builds_in_timed_steps"] * mixed.rebuild_launches())
 
     # energy drift over 1000 steps (warmup + timed + the rest, untimed)
     done = args.warmup + args.steps

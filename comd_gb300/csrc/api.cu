@@ -51,6 +51,11 @@ enum { KGM_ADV_VPP, KGM_REBIN, KGM_COMPACT, KGM_NBR, KGM_PASS1, KGM_PASS2, KGM_C
 const char *kGroupNameMerged[KGM_COUNT] = {"advance_velocity_positions+classify",
                                            "rebin_plan_apply", "compact_atoms", "nbr_build",
                                            "force_pass1", "force_pass2"};
+// the middle part of a force-order sequence: the rebuild section (classify,
+// rebin, compact, list build) is one conditional graph node
+enum { KGF_ADV_VPP, KGF_REBUILD, KGF_PASS1, KGF_PASS2, KGF_COUNT };
+const char *kGroupNameFo[KGF_COUNT] = {"advance_velocity_positions", "rebuild_if_due",
+                                       "force_pass1", "force_pass2"};
 
 }  // namespace
 
@@ -108,6 +113,7 @@ void free_all(comdgb_sim *h) {
   h->allocs.clear();
   for (void *q : h->adj.snaps) delete (Snapshot *)q;  // their device arrays were in allocs
   h->adj.snaps.clear();
+  if (h->cond_stream) cudaStreamDestroy(h->cond_stream);
   if (h->stream) cudaStreamDestroy(h->stream);
 }
 
@@ -448,14 +454,20 @@ int check_status(comdgb_sim *h) {
 
 // ---- kernel groups of one step --------------------------------------------
 
+// groups of the graph comdgb_sim_timed_steps times: a whole step, the
+// middle part of a merged sequence, or that of a force-order sequence
+int group_count(const comdgb_sim *h) {
+  if (!h->merge_rebox) return KG_COUNT;
+  return h->fo.list ? KGF_COUNT : KGM_COUNT;
+}
+
 // lazy: the rebox only when a list rebuild is due (see enqueue_step)
 void enqueue_classify_finish(comdgb_sim *h, bool lazy = false) {
   launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, h->stream,
                       lazy ? h->status : nullptr);
 }
 
-void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_rebox = false,
-                         bool obs = true) {
+void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool obs = true) {
   // ev (optional) records after each group: compact, nbr, pass1, pass2.
   // obs = false: a force call inside a step sequence, whose energies, stress,
   // rho and F' the next force call overwrites before the caller can read
@@ -464,7 +476,7 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_reb
   cudaStream_t st = h->stream;
   cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
-                 st, lazy_rebox ? h->status : nullptr);
+                 st);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   const int pot = h->opts.potential;
   // persistent lists are built with rc + skin, and only when a rebuild is due
@@ -524,6 +536,96 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool lazy_reb
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
 }
 
+int count_kernel_nodes(cudaGraph_t graph);
+
+// Under stream capture of h->stream: a kernel that sets a new conditional
+// handle to "a list rebuild is due", then an IF node after it whose body
+// is captured on h->cond_stream until cond_end.  Returns that stream, or
+// nullptr when h->stream is not capturing or the node cannot be made (the
+// caller then enqueues the section on h->stream, where it stands down by
+// itself).
+cudaStream_t cond_begin(comdgb_sim *h) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t graph = nullptr;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  if (!h->cond_stream ||
+      cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &graph, &deps, nullptr, &nd) !=
+          cudaSuccess ||
+      cs != cudaStreamCaptureStatusActive)
+    return nullptr;
+  cudaGraphConditionalHandle cond;
+  if (cudaGraphConditionalHandleCreate(&cond, graph, 0, cudaGraphCondAssignDefault) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  launch_rebuild_cond(cond, h->status, h->stream);
+  if (cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &graph, &deps, nullptr, &nd) !=
+      cudaSuccess)
+    return nullptr;
+  std::vector<cudaGraphNode_t> dv(deps, deps + nd);
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = cond;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, graph, dv.data(), nullptr, dv.size(), &p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;  // the handle stays unused
+  }
+  if (cudaStreamUpdateCaptureDependencies(h->stream, &node, nullptr, 1,
+                                          cudaStreamSetCaptureDependencies) != cudaSuccess ||
+      cudaStreamBeginCaptureToGraph(h->cond_stream, p.conditional.phGraph_out[0], nullptr,
+                                    nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return nullptr;  // (an error the end of the capture of h->stream reports)
+  return h->cond_stream;
+}
+
+void cond_end(comdgb_sim *h) {
+  cudaGraph_t body = nullptr;
+  if (cudaStreamEndCapture(h->cond_stream, &body) == cudaSuccess && body)
+    h->rebuild_kernels = count_kernel_nodes(body);
+}
+
+// The force call of a force-order step part (OPEN or MID, mixed precision):
+// the rebuild section -- classify, rebin, compact and the list build, all
+// needed only when the half step before found an atom moved more than
+// skin/2 -- as the body of a conditional node, then the passes without
+// energies (nothing reads them before the next force call).  ev: events
+// after the rebuild section and after each pass.
+void enqueue_fo_step_force(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
+  ForceArgs A = force_args(h);
+  cudaStream_t st = h->stream;
+  cudaStream_t bs = cond_begin(h);
+  cudaStream_t rs = bs ? bs : st;
+  launch_classify(h->g, h->s, h->atom_slot, h->ntot, h->mixed, h->w, h->status, rs, h->status);
+  launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, rs, h->status);
+  launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
+                 rs, h->status);
+  const double rcl = h->cutoff + h->skin;
+  launch_nbr_build<float>(A, (float)(rcl * rcl), rs, &h->tune);
+  if (bs) cond_end(h);
+  cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
+  launch_rebuild_done(h->status, st);
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+  const int pot = h->opts.potential;
+  if (pot == COMDGB_POT_LJ) {
+    launch_fo_lj(A, h->lj32, st, false);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+  } else if (pot == COMDGB_POT_EAM_TABLE) {
+    launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 0, st, &h->tune, false);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    launch_fo_eam<EVAL_TABLE>(A, h->eam32t, 1, st, &h->tune, false);
+  } else {
+    launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 0, st, &h->tune, false);
+    if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+    launch_fo_eam<EVAL_CHEBY>(A, h->eam32c, 1, st, &h->tune, false);
+  }
+  if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+}
+
 void enqueue_reduce(comdgb_sim *h) {
   ForceArgs A = force_args(h);
   launch_reduce(A, h->rpart, h->ripart, h->nrpart, h->d_out, h->d_iout, h->stream);
@@ -569,16 +671,17 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
       launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass,
                                h->mixed, !lazy, h->w, h->status, st, true);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-    // lazily: classify too only when the rebuild is due (the half step above
-    // has decided that)
-    if (lazy)
-      launch_classify(h->g, h->s, h->atom_slot, h->ntot, h->mixed, h->w, h->status, st,
-                      h->status);
-    enqueue_classify_finish(h, lazy);
+    if (lazy) {
+      // the classification, rebox and list build only when the half step
+      // above found a rebuild due
+      enqueue_fo_step_force(h, ev, evi);
+      return;
+    }
+    enqueue_classify_finish(h);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     // inside the sequence (OPEN, MID): the CLOSE part and the force call
     // that ends nTimeSteps follow, so nothing reads this call's energies
-    enqueue_force_parts(h, ev, evi, lazy, part == PART_FULL);  // the atom list of the new layout
+    enqueue_force_parts(h, ev, evi, part == PART_FULL);  // the atom list of the new layout
     if (part != PART_FULL) return;
   }
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
@@ -1126,7 +1229,9 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
     delete h;
     return set_err(COMDGB_ERR_CUDA, "cudaSetDevice(%d): %s", o->device, cudaGetErrorString(ce));
   }
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->cond_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
     return set_err(COMDGB_ERR_CUDA, "cudaStreamCreate failed");
   }
@@ -1661,9 +1766,15 @@ int comdgb_sim_step_launches(comdgb_sim *h, int n, long long *launches) {
   return 0;
 }
 
+int comdgb_sim_rebuild_launches(comdgb_sim *h, int *kernels) {
+  if (!h || !kernels) return set_err(COMDGB_ERR_ARG, "bad argument");
+  *kernels = h->rebuild_kernels;
+  return 0;
+}
+
 const char *comdgb_kernel_name(comdgb_sim *h, int k) {
-  if (h && h->merge_rebox) return k < 0 || k >= KGM_COUNT ? "" : kGroupNameMerged[k];
-  if (k < 0 || k >= KG_COUNT) return "";
+  if (!h || k < 0 || k >= group_count(h)) return "";
+  if (h->merge_rebox) return h->fo.list ? kGroupNameFo[k] : kGroupNameMerged[k];
   return kGroupName[k];
 }
 
@@ -1688,7 +1799,7 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
   // events around the groups of the timed graph: one whole step, or the
   // middle part of a merged sequence (n steps: the opening part, n-1 middle
   // parts, the closing part; the span covers all three)
-  const int NG = merged ? (int)KGM_COUNT : (int)KG_COUNT, NE = NG + 1;
+  const int NG = group_count(h), NE = NG + 1;
   if (merged) {
     int rc = ensure_step_graphs(h, dt_atu);
     if (rc) return rc;

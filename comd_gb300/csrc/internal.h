@@ -106,6 +106,8 @@ void launch_cheb_fit(const double *table_v, double x0, double xn, double invdx, 
 // end of a (possible) rebuild
 void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, cudaStream_t st);
 void launch_rebuild_done(int *status, cudaStream_t st);
+// sets the conditional node `cond` to whether a list rebuild is due
+void launch_rebuild_cond(cudaGraphConditionalHandle cond, const int *status, cudaStream_t st);
 void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *status,
                        cudaStream_t st);
 void launch_fo_track(const Geom &g, Slots s, const ForceOrder &fo, const int *atom_slot,

@@ -683,6 +683,14 @@ void launch_rebuild_done(int *status, cudaStream_t st) {
   rebuild_done_kernel<<<1, 1, 0, st>>>(status);
 }
 
+// the condition of the graph's rebuild section: a rebuild is due
+__global__ void rebuild_cond_kernel(cudaGraphConditionalHandle cond, const int *status) {
+  cudaGraphSetConditional(cond, *(volatile const int *)(status + ST_REBUILD) != 0 ? 1u : 0u);
+}
+void launch_rebuild_cond(cudaGraphConditionalHandle cond, const int *status, cudaStream_t st) {
+  rebuild_cond_kernel<<<1, 1, 0, st>>>(cond, status);
+}
+
 // ---------------------------------------------------------------------------
 // compaction: box_start = exclusive scan of natoms; atom_slot[a] = slot
 // ---------------------------------------------------------------------------

@@ -141,6 +141,11 @@ struct comdgb_sim {
   std::vector<cudaEvent_t> timed_cap_events;
   int step_kernels = 0, force_kernels = 0;  // kernel nodes per captured graph
   int part_kernels[3] = {0, 0, 0};           // opening, middle, closing parts
+  // force order: the rebuild section of a step (classify, rebin, compact,
+  // list build) is the body of a conditional graph node, captured on
+  // cond_stream; its kernel nodes run only in steps that rebuild
+  cudaStream_t cond_stream = nullptr;
+  int rebuild_kernels = 0;
   // host last results
   double e = 0.0, stress = 0.0;
   simflat_t *host = nullptr;   // drop-in owner (attach)

@@ -84,6 +84,7 @@ def _bind(lib):
                                          C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.comdgb_sim_graph_kernels.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.comdgb_sim_step_launches.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_longlong)]
+    L.comdgb_sim_rebuild_launches.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
     L.comdgb_fp32_fma_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
     L.comdgb_round_f32.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_float), C.c_long]
     D = C.POINTER(C.c_double)
@@ -552,6 +553,13 @@ class DeviceSim:
         """kernels a sequence of n steps launches"""
         v = C.c_longlong()
         check(self.L.comdgb_sim_step_launches(self.h, n, C.byref(v)))
+        return v.value
+
+    def rebuild_launches(self):
+        """kernels of a step's rebuild section, launched once per list
+        rebuild (0 when the rebuild section is not a conditional node)"""
+        v = C.c_int()
+        check(self.L.comdgb_sim_rebuild_launches(self.h, C.byref(v)))
         return v.value
 
     def graph_kernels(self):

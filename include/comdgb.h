@@ -170,8 +170,13 @@ const char *comdgb_kernel_name(comdgb_sim *h, int k);
 int comdgb_sim_graph_steps(comdgb_sim *h, int n, double dt, float *ms);
 /* kernels a sequence of n steps launches (after a step has run): n times
  * the step graph's, or with the rebox merged the opening part's, n-1 middle
- * parts' and the closing part's */
+ * parts' and the closing part's.  In force order (mixed precision with skin
+ * lists) a step part's rebuild section -- classify, rebin, compact, list
+ * build -- is the body of a conditional graph node and launches only in
+ * steps that rebuild the lists: comdgb_sim_rebuild_launches gives its
+ * kernels, to be added once per rebuild (comdgb_sim_list_info counts them). */
 int comdgb_sim_step_launches(comdgb_sim *h, int n, long long *launches);
+int comdgb_sim_rebuild_launches(comdgb_sim *h, int *kernels);
 /* kernels launched per replay of the captured step graph / force graph
  * (with the rebox merged: per middle part) */
 int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
