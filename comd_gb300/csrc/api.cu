@@ -1332,6 +1332,7 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
       h->fo.cut = track(h, dalloc<uint32_t>(rows * vcap, &err));
       h->fo.ncut = track(h, dalloc<int>(n1, &err));
       h->fo.emb = track(h, dalloc<float>(n1, &err));
+      h->fo.force = track(h, dalloc<float4>(n1, &err));
       const double hs = 0.5 * h->skin - 1e-5;  // FP32 displacements err by < 1e-6 A
       h->fo.half_skin2 = (float)(hs * hs);
     } else {

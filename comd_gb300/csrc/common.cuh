@@ -189,6 +189,11 @@ struct ForceOrder {
   uint32_t *cut;     // [rows*vcap] entries with r^2 <= rc^2
   int *ncut;         // [ntot] their count (> vcap: the skin list overflowed)
   float *emb;        // [ntot] F(rho) of a, from pass 1 (the per-atom energy's embedding part)
+  // the force of a from every force-order force call, as the FP32 value its
+  // compensated sum gives (the FP64 f of the slot arrays holds the same
+  // values, written only by the force calls whose results the caller reads);
+  // the velocity steps of a step sequence read it
+  float4 *force;     // [ntot] xyz
 };
 
 // the slot of an atom moved by the rebin, in the maps the list mode keeps
@@ -335,6 +340,7 @@ struct KSum {
   // combined in FP32 (one conversion, no FP64 subtraction: FP64 issue slots
   // are scarce on this GPU); the result is good to half an FP32 ulp
   __device__ __forceinline__ double value() const { return (double)__fsub_rn(s, c); }
+  __device__ __forceinline__ float valuef() const { return __fsub_rn(s, c); }
 };
 
 struct DSum {

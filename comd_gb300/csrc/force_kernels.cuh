@@ -1245,11 +1245,13 @@ constexpr int FO2_MAX_THREADS = 512;  // the force pass runs with 128, 256 (defa
 // rho'(r)) dr/r, the per-atom energy 1/2 sum phi + F(rho_i) and the
 // embedding x-x stress (eam.c:534-545, 644-649; f is +grad U as in the
 // reference).
-// OBS = false: the force calls inside a step sequence, whose energies and
-// stress the next force call overwrites before anything can read them (the
-// reference's nTimeSteps ends with its own computeForce, timestep.c:137):
-// forces only, f.w = 0.  Every force call whose results the caller can read
-// (a force call, the one ending nTimeSteps) is OBS.
+// Every force call stores the forces in force order (fo.force, FP32: the
+// velocity steps of a sequence read them).  OBS: also the slot arrays' f
+// with the per-atom energy, and the stress -- a force call whose results the
+// caller can read (a force call, the one ending nTimeSteps).  The force
+// calls inside a step sequence are not OBS: the next force call overwrites
+// their energies and stress before anything can read them (the reference's
+// nTimeSteps ends with its own computeForce, timestep.c:137).
 template <int EVAL, bool MULTI, bool OBS>
 __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
@@ -1286,13 +1288,17 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
         const float we = r2 < rc2 ? (fii + fj) * wrho : 0.f;
         acc.add(phi, wphi, we, dx, dy, dz);
       });
-    d4 fo;
-    fo.x = acc.fx.value();
-    fo.y = acc.fy.value();
-    fo.z = acc.fz.value();
-    fo.w = OBS ? 0.5 * acc.ep.value() + (double)__ldg(A.fo.emb + a) : 0.0;
-    A.s.f[slot] = fo;
-    if (OBS) A.atom_stress[a] = acc.sx.value();
+    const float fx = acc.fx.valuef(), fy = acc.fy.valuef(), fz = acc.fz.valuef();
+    A.fo.force[a] = make_float4(fx, fy, fz, 0.f);
+    if (OBS) {
+      d4 fo;
+      fo.x = fx;
+      fo.y = fy;
+      fo.z = fz;
+      fo.w = 0.5 * acc.ep.value() + (double)__ldg(A.fo.emb + a);
+      A.s.f[slot] = fo;
+      A.atom_stress[a] = acc.sx.value();
+    }
   }
 }
 
@@ -1367,13 +1373,14 @@ __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<
       if (OBS) sx.add(fr * dx * dx);
     };
     fo_for_each<false, MULTI, FO1_UNROLL>(A, a, slot, A.fo.pos[a], rc2, fn);
-    d4 fo;
-    fo.x = fx.value();
-    fo.y = fy.value();
-    fo.z = fz.value();
-    fo.w = OBS ? ep.value() : 0.0;
-    A.s.f[slot] = fo;
+    A.fo.force[a] = make_float4(fx.valuef(), fy.valuef(), fz.valuef(), 0.f);
     if (OBS) {
+      d4 fo;
+      fo.x = fx.value();
+      fo.y = fy.value();
+      fo.z = fz.value();
+      fo.w = ep.value();
+      A.s.f[slot] = fo;
       int ne = A.et.n[b], nonempty = 0;
       for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
       d4 p = A.s.p[slot];

@@ -184,10 +184,8 @@ __device__ __forceinline__ double div_mass(double a, double rmass, double rinv) 
 // boxsize/2 + (b - build box) * boxsize), one rounding either way -- and the
 // rebuild test on its displacement since the build.  Before the first build
 // (no force-order number) a rebuild is due anyway.
-__device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, int b, int id,
-                                         const d4 &r, float4 p32, int *status) {
-  const int af = fo.of_id[id];
-  if (af < 0) return;
+__device__ __forceinline__ void fo_track_at(const Geom &g, const ForceOrder &fo, int b, int af,
+                                            const d4 &r, float4 p32, int *status) {
   const float4 q = fo.ref[af];
   const RepGeo &R = rep_of(g, b);
   int ixn[3], ixb[3];
@@ -213,6 +211,11 @@ __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, in
   }
   if (far || !(d2 <= fo.half_skin2)) atomicExch(status + ST_REBUILD, 1);
   fo.pos[af] = make_float4(pv[0], pv[1], pv[2], 0.f);
+}
+__device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, int b, int id,
+                                         const d4 &r, float4 p32, int *status) {
+  const int af = fo.of_id[id];
+  if (af >= 0) fo_track_at(g, fo, b, af, r, p32, status);
 }
 
 // delta: the two position half steps around a step boundary add the same
@@ -240,7 +243,18 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
   if (MODE == INT_FMA && (POS || VEL)) {
     d4 p = s.p[slot];
     if (VEL) {
-      const d4 f = s.f[slot];
+      // force order: the forces of the last force call are the FP32 records
+      // (the slot arrays' f holds them only after a force call the caller reads)
+      const int af = w.fo.force ? w.fo.of_id[s.id[slot]] : -1;
+      d4 f;
+      if (af >= 0) {
+        const float4 f32 = w.fo.force[af];
+        f.x = f32.x;
+        f.y = f32.y;
+        f.z = f32.z;
+      } else {
+        f = s.f[slot];
+      }
       p.x = fma(-dt_v, f.x, p.x);
       p.y = fma(-dt_v, f.y, p.y);
       p.z = fma(-dt_v, f.z, p.z);
@@ -311,6 +325,36 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
   if (classify) classify_atom(g, s, slot, r, mixed, w, status);
 }
 
+// Force order, the middle part of a step sequence (mixed precision): the
+// velocity step and both position half steps of advance_kernel<1, 1,
+// INT_FMA> with the same arithmetic, walked in force order -- a's slot from
+// the force-order map the rebin keeps, its force from the force pass's FP32
+// record, the tracking records at a -- instead of through the atom list and
+// the id map.  c = 2 dt_r / rmass.
+__global__ void __launch_bounds__(256) advance_fo_kernel(Geom g, Slots s, ForceOrder fo,
+                                                         int ntot, double dt_v, double c,
+                                                         int *status) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= ntot) return;
+  const int slot = fo.slot[a];
+  const int b = slot >> 6;
+  const float4 f = fo.force[a];
+  d4 p = s.p[slot];
+  p.x = fma(-dt_v, (double)f.x, p.x);
+  p.y = fma(-dt_v, (double)f.y, p.y);
+  p.z = fma(-dt_v, (double)f.z, p.z);
+  s.p[slot] = p;
+  d4 r = s.r[slot];
+  r.x = fma(p.x, c, r.x);
+  r.y = fma(p.y, c, r.y);
+  r.z = fma(p.z, c, r.z);
+  s.r[slot] = r;
+  const float4 p32 = centred32(rep_of(g, b), r.x, r.y, r.z);
+  // the slot-order copy only for the stencil scan of an overflowed list
+  if (*(volatile const int *)(status + ST_NBR_OVERFLOW)) s.pos32[slot] = p32;
+  fo_track_at(g, fo, b, a, r, p32, status);
+}
+
 static unsigned slot_blocks(const Geom &g) {
   long nslots = (long)g.nboxes * CG_MAXATOMS;
   return (unsigned)((nslots + 255) / 256);
@@ -377,6 +421,13 @@ void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, 
                         cudaStream_t st, bool classify) {
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   // mixed precision: one multiply-add by 2*dt_r/rmass for the two half steps
+  if (mixed && !classify && w.fo.force) {
+    // force order between rebuilds (the rebox waits for the next one)
+    if (ntot > 0)
+      advance_fo_kernel<<<atom_blocks(ntot), 256, 0, st>>>(g, s, w.fo, ntot, dt_v,
+                                                           2.0 * dt_r / rmass, status);
+    return;
+  }
   launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, 2.0 * dt_r / rmass, rmass, mixed,
                              true, classify, DELTA_NONE, true, w, status, st,
                              !classify && w.fo.of_id);
