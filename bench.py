@@ -477,7 +477,7 @@ def gpu_arm(args):
         if name == "force_pass1":
             fl = FLOPS_PASS1_PER_PAIR * pairs + FLOPS_EMBED_PER_ATOM * natoms
             g.update(bound="fp32", achieved=fl / (ms / 1e3) / 1e12, unit="TFLOP/s")
-        elif name == "force_pass2":
+        elif name.startswith("force_pass2"):  # (force order: with the step's update)
             fl = FLOPS_PASS2_PER_PAIR * pairs
             g.update(bound="fp32", achieved=fl / (ms / 1e3) / 1e12, unit="TFLOP/s")
         elif name.startswith("advance_velocity"):
@@ -500,7 +500,7 @@ def gpu_arm(args):
                                 "comdgb_fp32_fma_peak (no FP32 figure in MEASURED_PEAKS.json)"
                                 if dg.get("bound") == "fp32" else "MEASURED_PEAKS.json hbm_gbs"),
                 "algorithmic": (f"{FLOPS_PASS2_PER_PAIR} flops/unique pair, {pairs} pairs"
-                                if dom == "force_pass2" else
+                                if dom.startswith("force_pass2") else
                                 f"{FLOPS_PASS1_PER_PAIR} flops/unique pair + "
                                 f"{FLOPS_EMBED_PER_ATOM}/atom, {pairs} pairs")}
 

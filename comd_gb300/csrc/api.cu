@@ -52,10 +52,11 @@ const char *kGroupNameMerged[KGM_COUNT] = {"advance_velocity_positions+classify"
                                            "rebin_plan_apply", "compact_atoms", "nbr_build",
                                            "force_pass1", "force_pass2"};
 // the middle part of a force-order sequence: the rebuild section (classify,
-// rebin, compact, list build) is one conditional graph node
-enum { KGF_ADV_VPP, KGF_REBUILD, KGF_PASS1, KGF_PASS2, KGF_COUNT };
-const char *kGroupNameFo[KGF_COUNT] = {"advance_velocity_positions", "rebuild_if_due",
-                                       "force_pass1", "force_pass2"};
+// rebin, compact, list build) is one conditional graph node, and the force
+// pass ends with the velocity-Verlet update of the step boundary
+enum { KGF_REBUILD, KGF_PASS1, KGF_PASS2, KGF_COUNT };
+const char *kGroupNameFo[KGF_COUNT] = {"rebuild_if_due", "force_pass1",
+                                       "force_pass2+advance_velocity_positions"};
 
 }  // namespace
 
@@ -539,12 +540,12 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool obs = tr
 int count_kernel_nodes(cudaGraph_t graph);
 
 // Under stream capture of h->stream: a kernel that sets a new conditional
-// handle to "a list rebuild is due", then an IF node after it whose body
+// handle to "status word `word` is set", then an IF node after it whose body
 // is captured on h->cond_stream until cond_end.  Returns that stream, or
 // nullptr when h->stream is not capturing or the node cannot be made (the
-// caller then enqueues the section on h->stream, where it stands down by
-// itself).
-cudaStream_t cond_begin(comdgb_sim *h) {
+// caller then enqueues the body on h->stream, where its kernels stand down
+// by themselves).
+cudaStream_t cond_begin(comdgb_sim *h, int word) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t graph = nullptr;
   const cudaGraphNode_t *deps = nullptr;
@@ -560,7 +561,7 @@ cudaStream_t cond_begin(comdgb_sim *h) {
     cudaGetLastError();
     return nullptr;
   }
-  launch_rebuild_cond(cond, h->status, h->stream);
+  launch_status_cond(cond, h->status, word, h->stream);
   if (cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &graph, &deps, nullptr, &nd) !=
       cudaSuccess)
     return nullptr;
@@ -583,32 +584,53 @@ cudaStream_t cond_begin(comdgb_sim *h) {
   return h->cond_stream;
 }
 
-void cond_end(comdgb_sim *h) {
+// ends the body's capture; its kernel nodes
+int cond_end(comdgb_sim *h) {
   cudaGraph_t body = nullptr;
   if (cudaStreamEndCapture(h->cond_stream, &body) == cudaSuccess && body)
-    h->rebuild_kernels = count_kernel_nodes(body);
+    return count_kernel_nodes(body);
+  return 0;
+}
+
+// Inside a force-order step sequence the force pass makes the next step's
+// velocity step and position half steps (ST_FUSE), except in the sequence's
+// last force call: the closing part makes that step's own.  n steps: set
+// before the opening part, cleared before the last middle part.
+void set_fuse(comdgb_sim *h, bool on, cudaStream_t st = nullptr) {
+  if (h->fo.list)
+    cudaMemsetAsync(h->status + ST_FUSE, on ? 1 : 0, sizeof(int), st ? st : h->stream);
 }
 
 // The force call of a force-order step part (OPEN or MID, mixed precision):
 // the rebuild section -- classify, rebin, compact and the list build, all
-// needed only when the half step before found an atom moved more than
-// skin/2 -- as the body of a conditional node, then the passes without
-// energies (nothing reads them before the next force call).  ev: events
-// after the rebuild section and after each pass.
-void enqueue_fo_step_force(comdgb_sim *h, cudaEvent_t *ev, int &evi) {
+// needed only when an atom moved more than skin/2 since the build -- as the
+// body of a conditional node; the slot-order FP32 copy refreshed (another
+// conditional node) when a list overflowed, since only the stencil scan of
+// an overflowed list reads it and the fused update does not keep it; then
+// the passes without energies, the force pass with the update of the step
+// boundary when ST_FUSE is set (dt_atu: the step).  ev: events after the
+// rebuild section and after each pass.
+void enqueue_fo_step_force(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int &evi) {
   ForceArgs A = force_args(h);
+  A.vv_dt = dt_atu;
+  const double dt_r = dt_atu / 2.0;
+  A.vv_c = 2.0 * dt_r / h->rmass;  // both half steps, as one multiply-add
   cudaStream_t st = h->stream;
-  cudaStream_t bs = cond_begin(h);
+  cudaStream_t bs = cond_begin(h, ST_REBUILD);
   cudaStream_t rs = bs ? bs : st;
+  cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), rs);
   launch_classify(h->g, h->s, h->atom_slot, h->ntot, h->mixed, h->w, h->status, rs, h->status);
   launch_rebin_finish(h->g, h->s, h->mixed, h->w, h->status, rs, h->status);
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
                  rs, h->status);
   const double rcl = h->cutoff + h->skin;
   launch_nbr_build<float>(A, (float)(rcl * rcl), rs, &h->tune);
-  if (bs) cond_end(h);
+  if (bs) h->rebuild_kernels = cond_end(h);
   cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
   launch_rebuild_done(h->status, st);
+  cudaStream_t os = cond_begin(h, ST_NBR_OVERFLOW);
+  launch_pos32(h->g, h->s, os ? os : st, h->status);
+  if (os) h->overflow_kernels = cond_end(h);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   const int pot = h->opts.potential;
   if (pot == COMDGB_POT_LJ) {
@@ -661,22 +683,26 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
   cudaStream_t st = h->stream;
   const bool lazy = h->fo.list && (part == PART_OPEN || part == PART_MID);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
+  if (lazy) {
+    // force order: the opening position half step; a middle part's update
+    // was made by the force pass before it (ST_FUSE); the classification,
+    // rebox and list build only when a rebuild is due
+    if (part == PART_OPEN)
+      launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass,
+                               h->mixed, false, h->w, h->status, st, true);
+    enqueue_fo_step_force(h, dt_atu, ev, evi);
+    return;
+  }
   if (part != PART_CLOSE) {
     // the atom list is the one made after the previous rebin
     cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
     if (part == PART_MID)
       launch_advance_vpp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass,
-                         h->mixed, h->w, h->status, st, !lazy);
+                         h->mixed, h->w, h->status, st, true);
     else
       launch_advance_positions(h->g, h->s, h->atom_slot, h->ntot, dt_atu / 2.0, h->rmass,
-                               h->mixed, !lazy, h->w, h->status, st, true);
+                               h->mixed, true, h->w, h->status, st, true);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
-    if (lazy) {
-      // the classification, rebox and list build only when the half step
-      // above found a rebuild due
-      enqueue_fo_step_force(h, ev, evi);
-      return;
-    }
     enqueue_classify_finish(h);
     if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
     // inside the sequence (OPEN, MID): the CLOSE part and the force call
@@ -784,8 +810,12 @@ int do_steps_graph(comdgb_sim *h, int n, double dt, float *ms) {
     if (!h->merge_rebox)
       for (int i = 0; i < n; i++) enqueue_step(h, dt_atu, nullptr, PART_FULL);
     else if (n > 0) {
+      set_fuse(h, n > 1);
       enqueue_step(h, dt_atu, nullptr, PART_OPEN);
-      for (int i = 1; i < n; i++) enqueue_step(h, dt_atu, nullptr, PART_MID);
+      for (int i = 1; i < n; i++) {
+        if (i == n - 1) set_fuse(h, false);
+        enqueue_step(h, dt_atu, nullptr, PART_MID);
+      }
       enqueue_step(h, dt_atu, nullptr, PART_CLOSE);
     }
     CK(cudaStreamEndCapture(h->stream, &graph));
@@ -834,8 +864,12 @@ int launch_steps(comdgb_sim *h, int n, cudaStream_t st) {
     for (int i = 0; i < n; i++) CK(cudaGraphLaunch(h->step_exec, st));
     return 0;
   }
+  set_fuse(h, n > 1, st);
   CK(cudaGraphLaunch(h->part_exec[0], st));
-  for (int i = 1; i < n; i++) CK(cudaGraphLaunch(h->part_exec[1], st));
+  for (int i = 1; i < n; i++) {
+    if (i == n - 1) set_fuse(h, false, st);
+    CK(cudaGraphLaunch(h->part_exec[1], st));
+  }
   CK(cudaGraphLaunch(h->part_exec[2], st));
   return 0;
 }
@@ -1842,12 +1876,16 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
   CK(cudaEventCreate(&span1));
   CK(cudaStreamSynchronize(h->stream));
   CK(cudaEventRecord(span0, h->stream));
-  if (merged) CK(cudaGraphLaunch(h->part_exec[PART_OPEN], h->stream));
+  if (merged) {
+    set_fuse(h, n > 1);
+    CK(cudaGraphLaunch(h->part_exec[PART_OPEN], h->stream));
+  }
   for (int s = 0; s < nt; s++) {
     for (int i = 0; i < NE; i++)
       if (h->timed_nodes[i])
         CK(cudaGraphExecEventRecordNodeSetEvent(h->timed_exec, h->timed_nodes[i],
                                                 evs[(size_t)s * NE + i]));
+    if (merged && s == nt - 1) set_fuse(h, false);
     CK(cudaGraphLaunch(h->timed_exec, h->stream));
   }
   if (merged) CK(cudaGraphLaunch(h->part_exec[PART_CLOSE], h->stream));

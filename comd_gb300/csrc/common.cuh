@@ -147,7 +147,9 @@ enum {
   ST_REBUILDS = 5,    // persistent lists: number of list builds
   ST_DELTA = 6,       // f.xyz holds the half-step position increments (see advance_kernel)
   ST_OVF_BUILD = 7,   // persistent lists: overflows counted by the build in progress
-  ST_COUNT = 8
+  ST_FUSE = 8,        // force order: the force pass also makes the next step's velocity
+                      // step and both position half steps (see fo_eam_pass2_kernel)
+  ST_COUNT = 9
 };
 
 // Persistent (skin) neighbour lists, keyed by atom id: built with cutoff
@@ -196,6 +198,39 @@ struct ForceOrder {
   float4 *force;     // [ntot] xyz
 };
 
+// Force order: the FP32 position of force-order atom af (now in box b at
+// box-relative FP64 position r, FP32 centred position p32) relative to its
+// build box centre -- p32 itself while the atom is in its build box, else
+// RN(r - boxsize/2 + (b - build box) * boxsize), one rounding either way --
+// and the rebuild test on its displacement since the build.
+__device__ __forceinline__ void fo_track_at(const Geom &g, const ForceOrder &fo, int b, int af,
+                                            const d4 &r, float4 p32, int *status) {
+  const float4 q = fo.ref[af];
+  const RepGeo &R = rep_of(g, b);
+  int ixn[3], ixb[3];
+  box_ixyz_tab(g, b, ixn);
+  box_ixyz_tab(g, __float_as_int(q.w), ixb);
+  const double rv[3] = {r.x, r.y, r.z};
+  const float qv[3] = {q.x, q.y, q.z};
+  float pv[3] = {p32.x, p32.y, p32.z}, d2 = 0.f;
+  bool far = false;
+  for (int k = 0; k < 3; k++) {
+    int db = ixn[k] - ixb[k];
+    if (g.periodic) {
+      if (db > 1) db -= R.nbx[k];
+      else if (db < -1) db += R.nbx[k];
+    }
+    far |= db > 1 || db < -1;
+    // more than a box width outside its box (only a runaway step does that):
+    // the box-centred FP32 position says so without FP64 work
+    far |= !(fabsf(pv[k]) <= 1.5f * R.hi[k]);
+    if (db != 0) pv[k] = d2f_rn(fma((double)db, R.boxsize[k], rv[k] - R.half[k]));
+    const float d = pv[k] - qv[k];
+    d2 = fmaf(d, d, d2);
+  }
+  if (far || !(d2 <= fo.half_skin2)) atomicExch(status + ST_REBUILD, 1);
+  fo.pos[af] = make_float4(pv[0], pv[1], pv[2], 0.f);
+}
 // the slot of an atom moved by the rebin, in the maps the list mode keeps
 struct SlotMap {
   int *slot_of;        // by id (id-keyed persistent lists) or null

@@ -41,6 +41,9 @@ struct ForceArgs {
   int *status;
   Persist pl;            // persistent lists keyed by id (FP64)
   ForceOrder fo;         // persistent lists in force order (mixed; fo.list != nullptr)
+  // force order, a step sequence: the velocity-Verlet coefficients of the
+  // update the force pass makes when ST_FUSE is set (p -= vv_dt f, r += vv_c p)
+  double vv_dt, vv_c;
 };
 
 // Stencil entry of box jb seen from box b when both stencils are the full
@@ -1241,16 +1244,44 @@ struct ForceSums {
 
 constexpr int FO2_MAX_THREADS = 512;  // the force pass runs with 128, 256 (default) or 512
 
+// The end of a force-order force call inside a step sequence: with ST_FUSE
+// set (fuse), atom a's velocity step with the force just summed and the two
+// position half steps around the step boundary, as one multiply-add each
+// (the arithmetic of the mixed-precision middle-part update), and its
+// tracking record; else its FP32 force record for the velocity step that
+// follows.  Safe inside the pass: the other atoms of the pass read the
+// positions the density pass stored (pf), never r, p, fo.pos or pos32.
+__device__ __forceinline__ void fo_force_end(const ForceArgs &A, int a, int slot, bool fuse,
+                                             float fx, float fy, float fz) {
+  if (!fuse) {
+    A.fo.force[a] = make_float4(fx, fy, fz, 0.f);
+    return;
+  }
+  d4 p = A.s.p[slot];
+  p.x = fma(-A.vv_dt, (double)fx, p.x);
+  p.y = fma(-A.vv_dt, (double)fy, p.y);
+  p.z = fma(-A.vv_dt, (double)fz, p.z);
+  A.s.p[slot] = p;
+  d4 r = A.s.r[slot];
+  r.x = fma(p.x, A.vv_c, r.x);
+  r.y = fma(p.y, A.vv_c, r.y);
+  r.z = fma(p.z, A.vv_c, r.z);
+  A.s.r[slot] = r;
+  const int b = slot >> 6;
+  fo_track_at(A.g, A.fo, b, a, r, centred32(rep_of(A.g, b), r.x, r.y, r.z), A.status);
+}
+
 // Force pass: f_i = sum over the cut list of (phi'(r) + (F'_i + F'_j)
 // rho'(r)) dr/r, the per-atom energy 1/2 sum phi + F(rho_i) and the
 // embedding x-x stress (eam.c:534-545, 644-649; f is +grad U as in the
 // reference).
-// Every force call stores the forces in force order (fo.force, FP32: the
-// velocity steps of a sequence read them).  OBS: also the slot arrays' f
-// with the per-atom energy, and the stress -- a force call whose results the
-// caller can read (a force call, the one ending nTimeSteps).  The force
-// calls inside a step sequence are not OBS: the next force call overwrites
-// their energies and stress before anything can read them (the reference's
+// Every force call ends with fo_force_end: the FP32 force record in force
+// order, or inside a step sequence (ST_FUSE) the next step's velocity and
+// position update made right here.  OBS: also the slot arrays' f with the
+// per-atom energy, and the stress -- a force call whose results the caller
+// can read (a force call, the one ending nTimeSteps).  The force calls
+// inside a step sequence are not OBS: the next force call overwrites their
+// energies and stress before anything can read them (the reference's
 // nTimeSteps ends with its own computeForce, timestep.c:137).
 template <int EVAL, bool MULTI, bool OBS>
 __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
@@ -1258,6 +1289,7 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);  // phi and rho cubics
   const float rc2 = P.rc2;
+  const bool fuse = !OBS && *(volatile const int *)(A.status + ST_FUSE);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
     const float4 pi = A.fo.pf[a];
@@ -1289,7 +1321,7 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
         acc.add(phi, wphi, we, dx, dy, dz);
       });
     const float fx = acc.fx.valuef(), fy = acc.fy.valuef(), fz = acc.fz.valuef();
-    A.fo.force[a] = make_float4(fx, fy, fz, 0.f);
+    fo_force_end(A, a, slot, fuse, fx, fy, fz);
     if (OBS) {
       d4 fo;
       fo.x = fx;
@@ -1354,6 +1386,7 @@ __global__ void __launch_bounds__(128) lj_pass_kernel(ForceArgs A, LjPot<T> P) {
 template <bool MULTI, bool OBS>
 __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<float> P) {
   const float s6 = P.s6, s12 = P.s6x12, c4 = P.eps4s6, rc2 = P.rc2;
+  const bool fuse = !OBS && *(volatile const int *)(A.status + ST_FUSE);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
     const int b = slot >> 6;
@@ -1373,7 +1406,7 @@ __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<
       if (OBS) sx.add(fr * dx * dx);
     };
     fo_for_each<false, MULTI, FO1_UNROLL>(A, a, slot, A.fo.pos[a], rc2, fn);
-    A.fo.force[a] = make_float4(fx.valuef(), fy.valuef(), fz.valuef(), 0.f);
+    fo_force_end(A, a, slot, fuse, fx.valuef(), fy.valuef(), fz.valuef());
     if (OBS) {
       d4 fo;
       fo.x = fx.value();

@@ -94,7 +94,7 @@ void launch_zc_upload(const HostSlots &hs, Slots s, int nboxes, bool forces, cud
 // (f, rho, fi)
 void launch_zc_download(const HostSlots &hs, Slots s, int nboxes, bool state, bool forces,
                         cudaStream_t st);
-void launch_pos32(const Geom &g, Slots s, cudaStream_t st);
+void launch_pos32(const Geom &g, Slots s, cudaStream_t st, const int *only_if_overflow = nullptr);
 void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, const double *xyz,
                       const double *pxyz, const int *ids, const int *types, const double *masses,
                       int *tmp_index, int *status, cudaStream_t st);
@@ -106,8 +106,9 @@ void launch_cheb_fit(const double *table_v, double x0, double xn, double invdx, 
 // end of a (possible) rebuild
 void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, cudaStream_t st);
 void launch_rebuild_done(int *status, cudaStream_t st);
-// sets the conditional node `cond` to whether a list rebuild is due
-void launch_rebuild_cond(cudaGraphConditionalHandle cond, const int *status, cudaStream_t st);
+// sets the conditional node `cond` to whether status word `word` is set
+void launch_status_cond(cudaGraphConditionalHandle cond, const int *status, int word,
+                        cudaStream_t st);
 void launch_skin_check(const Geom &g, Slots s, Persist pl, bool mixed, int *status,
                        cudaStream_t st);
 void launch_fo_track(const Geom &g, Slots s, const ForceOrder &fo, const int *atom_slot,

@@ -178,40 +178,8 @@ __device__ __forceinline__ double div_mass(double a, double rmass, double rinv) 
   return MODE == INT_MARK ? div_markstein(a, rmass, rinv) : a / rmass;
 }
 
-// Force order: the FP32 position of atom id (now in box b at box-relative
-// FP64 position r, FP32 centred position p32) relative to its build box
-// centre -- p32 itself while the atom is in its build box, else RN(r -
-// boxsize/2 + (b - build box) * boxsize), one rounding either way -- and the
-// rebuild test on its displacement since the build.  Before the first build
-// (no force-order number) a rebuild is due anyway.
-__device__ __forceinline__ void fo_track_at(const Geom &g, const ForceOrder &fo, int b, int af,
-                                            const d4 &r, float4 p32, int *status) {
-  const float4 q = fo.ref[af];
-  const RepGeo &R = rep_of(g, b);
-  int ixn[3], ixb[3];
-  box_ixyz_tab(g, b, ixn);
-  box_ixyz_tab(g, __float_as_int(q.w), ixb);
-  const double rv[3] = {r.x, r.y, r.z};
-  const float qv[3] = {q.x, q.y, q.z};
-  float pv[3] = {p32.x, p32.y, p32.z}, d2 = 0.f;
-  bool far = false;
-  for (int k = 0; k < 3; k++) {
-    int db = ixn[k] - ixb[k];
-    if (g.periodic) {
-      if (db > 1) db -= R.nbx[k];
-      else if (db < -1) db += R.nbx[k];
-    }
-    far |= db > 1 || db < -1;
-    // more than a box width outside its box (only a runaway step does that):
-    // the box-centred FP32 position says so without FP64 work
-    far |= !(fabsf(pv[k]) <= 1.5f * R.hi[k]);
-    if (db != 0) pv[k] = d2f_rn(fma((double)db, R.boxsize[k], rv[k] - R.half[k]));
-    const float d = pv[k] - qv[k];
-    d2 = fmaf(d, d, d2);
-  }
-  if (far || !(d2 <= fo.half_skin2)) atomicExch(status + ST_REBUILD, 1);
-  fo.pos[af] = make_float4(pv[0], pv[1], pv[2], 0.f);
-}
+// fo_track_at for atom id (before the first build, no force-order number:
+// a rebuild is due anyway)
 __device__ __forceinline__ void fo_track(const Geom &g, const ForceOrder &fo, int b, int id,
                                          const d4 &r, float4 p32, int *status) {
   const int af = fo.of_id[id];
@@ -325,36 +293,6 @@ __global__ void __launch_bounds__(256) advance_kernel(Geom g, Slots s, const int
   if (classify) classify_atom(g, s, slot, r, mixed, w, status);
 }
 
-// Force order, the middle part of a step sequence (mixed precision): the
-// velocity step and both position half steps of advance_kernel<1, 1,
-// INT_FMA> with the same arithmetic, walked in force order -- a's slot from
-// the force-order map the rebin keeps, its force from the force pass's FP32
-// record, the tracking records at a -- instead of through the atom list and
-// the id map.  c = 2 dt_r / rmass.
-__global__ void __launch_bounds__(256) advance_fo_kernel(Geom g, Slots s, ForceOrder fo,
-                                                         int ntot, double dt_v, double c,
-                                                         int *status) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= ntot) return;
-  const int slot = fo.slot[a];
-  const int b = slot >> 6;
-  const float4 f = fo.force[a];
-  d4 p = s.p[slot];
-  p.x = fma(-dt_v, (double)f.x, p.x);
-  p.y = fma(-dt_v, (double)f.y, p.y);
-  p.z = fma(-dt_v, (double)f.z, p.z);
-  s.p[slot] = p;
-  d4 r = s.r[slot];
-  r.x = fma(p.x, c, r.x);
-  r.y = fma(p.y, c, r.y);
-  r.z = fma(p.z, c, r.z);
-  s.r[slot] = r;
-  const float4 p32 = centred32(rep_of(g, b), r.x, r.y, r.z);
-  // the slot-order copy only for the stencil scan of an overflowed list
-  if (*(volatile const int *)(status + ST_NBR_OVERFLOW)) s.pos32[slot] = p32;
-  fo_track_at(g, fo, b, a, r, p32, status);
-}
-
 static unsigned slot_blocks(const Geom &g) {
   long nslots = (long)g.nboxes * CG_MAXATOMS;
   return (unsigned)((nslots + 255) / 256);
@@ -421,13 +359,6 @@ void launch_advance_vpp(const Geom &g, Slots s, const int *atom_slot, int ntot, 
                         cudaStream_t st, bool classify) {
   if (classify) cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   // mixed precision: one multiply-add by 2*dt_r/rmass for the two half steps
-  if (mixed && !classify && w.fo.force) {
-    // force order between rebuilds (the rebox waits for the next one)
-    if (ntot > 0)
-      advance_fo_kernel<<<atom_blocks(ntot), 256, 0, st>>>(g, s, w.fo, ntot, dt_v,
-                                                           2.0 * dt_r / rmass, status);
-    return;
-  }
   launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, 2.0 * dt_r / rmass, rmass, mixed,
                              true, classify, DELTA_NONE, true, w, status, st,
                              !classify && w.fo.of_id);
@@ -734,12 +665,13 @@ void launch_rebuild_done(int *status, cudaStream_t st) {
   rebuild_done_kernel<<<1, 1, 0, st>>>(status);
 }
 
-// the condition of the graph's rebuild section: a rebuild is due
-__global__ void rebuild_cond_kernel(cudaGraphConditionalHandle cond, const int *status) {
-  cudaGraphSetConditional(cond, *(volatile const int *)(status + ST_REBUILD) != 0 ? 1u : 0u);
+// the condition of a conditional graph node: status word `word` is set
+__global__ void status_cond_kernel(cudaGraphConditionalHandle cond, const int *status, int word) {
+  cudaGraphSetConditional(cond, *(volatile const int *)(status + word) != 0 ? 1u : 0u);
 }
-void launch_rebuild_cond(cudaGraphConditionalHandle cond, const int *status, cudaStream_t st) {
-  rebuild_cond_kernel<<<1, 1, 0, st>>>(cond, status);
+void launch_status_cond(cudaGraphConditionalHandle cond, const int *status, int word,
+                        cudaStream_t st) {
+  status_cond_kernel<<<1, 1, 0, st>>>(cond, status, word);
 }
 
 // ---------------------------------------------------------------------------
@@ -1117,15 +1049,18 @@ void launch_pack3(const d4 *src, double *dst3, long n, cudaStream_t st) {
   if (n > 0) pack3_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(src, dst3, n);
 }
 
-__global__ void pos32_kernel(Geom g, Slots s) {
+// only_if_overflow (optional): status words; nothing unless some list
+// overflowed (ST_NBR_OVERFLOW), the one case the slot-order copy is read
+__global__ void pos32_kernel(Geom g, Slots s, const int *only_if_overflow) {
   long slot = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (slot >= (long)g.nboxes * CG_MAXATOMS) return;
+  if (only_if_overflow && !*(volatile const int *)(only_if_overflow + ST_NBR_OVERFLOW)) return;
   d4 r = s.r[slot];
   s.pos32[slot] = centred32(rep_of(g, (int)(slot >> 6)), r.x, r.y, r.z);
 }
 
-void launch_pos32(const Geom &g, Slots s, cudaStream_t st) {
-  pos32_kernel<<<slot_blocks(g), 256, 0, st>>>(g, s);
+void launch_pos32(const Geom &g, Slots s, cudaStream_t st, const int *only_if_overflow) {
+  pos32_kernel<<<slot_blocks(g), 256, 0, st>>>(g, s, only_if_overflow);
 }
 
 // ---------------------------------------------------------------------------

@@ -146,6 +146,7 @@ struct comdgb_sim {
   // cond_stream; its kernel nodes run only in steps that rebuild
   cudaStream_t cond_stream = nullptr;
   int rebuild_kernels = 0;
+  int overflow_kernels = 0;  // the slot-order copy's refresh after a list overflow
   // host last results
   double e = 0.0, stress = 0.0;
   simflat_t *host = nullptr;   // drop-in owner (attach)

@@ -107,10 +107,11 @@ def test_merged_step_paths_agree():
         assert slots_equal(sims[0][0], sims[1][0]) and slots_equal(sims[0][0], sims[2][0])
         assert len(step_ms) == 12 and span >= sum(step_ms) * 0.999
         # merged groups; in force order the rebuild section is one conditional node
+        # and the force pass makes the step's velocity and position update
         assert set(groups) in ({"advance_velocity_positions+classify", "rebin_plan_apply",
                                 "compact_atoms", "nbr_build", "force_pass1", "force_pass2"},
-                               {"advance_velocity_positions", "rebuild_if_due", "force_pass1",
-                                "force_pass2"})
+                               {"rebuild_if_due", "force_pass1",
+                                "force_pass2+advance_velocity_positions"})
         ba, bb = cg.Batch(sims[0][1:], o), cg.Batch(sims[1][1:], o)
         try:
             ba.steps(8)
