@@ -540,11 +540,13 @@ void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool obs = tr
 int count_kernel_nodes(cudaGraph_t graph);
 
 // Under stream capture of h->stream: a kernel that sets a new conditional
-// handle to "status word `word` is set", then an IF node after it whose body
-// is captured on h->cond_stream until cond_end.  Returns that stream, or
-// nullptr when h->stream is not capturing or the node cannot be made (the
-// caller then enqueues the body on h->stream, where its kernels stand down
-// by themselves).
+// handle to "status word `word` is set" (word < 0: the end of a possible
+// rebuild and "a current list overflowed", rebuild_done_cond_kernel), then
+// an IF node after it whose body is captured on h->cond_stream until
+// cond_end.  Returns that stream, or nullptr when h->stream is not capturing
+// or the node cannot be made (the caller then enqueues the body on
+// h->stream, where its kernels stand down by themselves; with word < 0 it
+// also launches rebuild_done itself).
 cudaStream_t cond_begin(comdgb_sim *h, int word) {
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t graph = nullptr;
@@ -561,7 +563,8 @@ cudaStream_t cond_begin(comdgb_sim *h, int word) {
     cudaGetLastError();
     return nullptr;
   }
-  launch_status_cond(cond, h->status, word, h->stream);
+  if (word < 0) launch_rebuild_done_cond(h->status, cond, h->stream);
+  else launch_status_cond(cond, h->status, word, h->stream);
   if (cudaStreamGetCaptureInfo(h->stream, &cs, nullptr, &graph, &deps, nullptr, &nd) !=
       cudaSuccess)
     return nullptr;
@@ -626,9 +629,9 @@ void enqueue_fo_step_force(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int &e
   const double rcl = h->cutoff + h->skin;
   launch_nbr_build<float>(A, (float)(rcl * rcl), rs, &h->tune);
   if (bs) h->rebuild_kernels = cond_end(h);
-  cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
-  launch_rebuild_done(h->status, st);
-  cudaStream_t os = cond_begin(h, ST_NBR_OVERFLOW);
+  // (mixed precision keeps no position increments in f: ST_DELTA stays 0)
+  cudaStream_t os = cond_begin(h, -1);
+  if (!os) launch_rebuild_done(h->status, st);
   launch_pos32(h->g, h->s, os ? os : st, h->status);
   if (os) h->overflow_kernels = cond_end(h);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);

@@ -424,29 +424,49 @@ __device__ __forceinline__ void build_box32(const ForceArgs &A, float rc2, int b
                       : MODE == LIST_FO ? (int)(((unsigned)(A.box_start[s_box[e]] + k) << 6) |
                                                 fo_code(s_code[e]))
                                         : ((s_code[e] << 6) | k);
-      cand[c] = make_float4((q.x - o.x) - o.lx, (q.y - o.y) - o.ly, (q.z - o.z) - o.lz,
+      // negated, so the test below is one packed add per axis: pa + (-c)
+      // rounds exactly as pa - c
+      cand[c] = make_float4(-((q.x - o.x) - o.lx), -((q.y - o.y) - o.ly), -((q.z - o.z) - o.lz),
                             __int_as_float(tag));
     } else {
-      cand[c] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+      cand[c] = make_float4(-1e18f, -1e18f, -1e18f, 0.f);
     }
   }
   __syncthreads();
   const float rc2b = rc2 * (1.0f + 4e-6f);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  static_assert(NA % 2 == 0, "atoms are tested in pairs");
   for (int i0 = NA * warp; i0 < ni; i0 += NA * (NT / 32)) {
     const int na = min(NA, ni - i0);
-    float4 pa[NA];
+    // the atoms in pairs, one per half of the packed FP32x2 operations (two
+    // pair tests per instruction; r^2 = dx*dx, + dy*dy, + dz*dz rounded as
+    // fmaf(dz, dz, fmaf(dy, dy, dx * dx)))
+    float2 px[NA / 2], py[NA / 2], pz[NA / 2];
 #pragma unroll
-    for (int t = 0; t < NA; t++)
-      pa[t] = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0 + (t < na ? t : 0));
+    for (int u = 0; u < NA / 2; u++) {
+      const float4 a0 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0 + (2 * u < na ? 2 * u : 0));
+      const float4 a1 = __ldg(A.s.pos32 + b * CG_MAXATOMS + i0 + (2 * u + 1 < na ? 2 * u + 1 : 0));
+      px[u] = make_float2(a0.x, a1.x);
+      py[u] = make_float2(a0.y, a1.y);
+      pz[u] = make_float2(a0.z, a1.z);
+    }
     for (int q = 0; q < nchunk; q++) {
       const float4 cq = cand[(q << 5) + lane];
+      const float2 cx = make_float2(cq.x, cq.x), cy = make_float2(cq.y, cq.y),
+                   cz = make_float2(cq.z, cq.z);
 #pragma unroll
-      for (int t = 0; t < NA; t++) {
-        const float dx = pa[t].x - cq.x, dy = pa[t].y - cq.y, dz = pa[t].z - cq.z;
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        const uint32_t m = __ballot_sync(0xffffffffu, r2 <= rc2b);
-        if (lane == 0) s_mask[warp][t][q] = m;
+      for (int u = 0; u < NA / 2; u++) {
+        const float2 dx = __fadd2_rn(px[u], cx), dy = __fadd2_rn(py[u], cy),
+                     dz = __fadd2_rn(pz[u], cz);
+        float2 r2 = __fmul2_rn(dx, dx);
+        r2 = __ffma2_rn(dy, dy, r2);
+        r2 = __ffma2_rn(dz, dz, r2);
+        const uint32_t m0 = __ballot_sync(0xffffffffu, r2.x <= rc2b);
+        const uint32_t m1 = __ballot_sync(0xffffffffu, r2.y <= rc2b);
+        if (lane == 0) {
+          s_mask[warp][2 * u][q] = m0;
+          s_mask[warp][2 * u + 1][q] = m1;
+        }
       }
     }
     __syncwarp();

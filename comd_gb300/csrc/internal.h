@@ -106,6 +106,8 @@ void launch_cheb_fit(const double *table_v, double x0, double xn, double invdx, 
 // end of a (possible) rebuild
 void launch_slot_of(const Geom &g, Slots s, Persist pl, int ntot, int *status, cudaStream_t st);
 void launch_rebuild_done(int *status, cudaStream_t st);
+// launch_rebuild_done, then sets `cond` to whether a current list overflowed
+void launch_rebuild_done_cond(int *status, cudaGraphConditionalHandle cond, cudaStream_t st);
 // sets the conditional node `cond` to whether status word `word` is set
 void launch_status_cond(cudaGraphConditionalHandle cond, const int *status, int word,
                         cudaStream_t st);

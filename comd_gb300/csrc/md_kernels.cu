@@ -665,6 +665,21 @@ void launch_rebuild_done(int *status, cudaStream_t st) {
   rebuild_done_kernel<<<1, 1, 0, st>>>(status);
 }
 
+// rebuild_done_kernel, then the condition of a conditional graph node: some
+// list of the current lists overflowed
+__global__ void rebuild_done_cond_kernel(int *status, cudaGraphConditionalHandle cond) {
+  if (status[ST_REBUILD]) {
+    status[ST_REBUILDS] += 1;
+    status[ST_REBUILD] = 0;
+    status[ST_NBR_OVERFLOW] = status[ST_OVF_BUILD];
+    status[ST_OVF_BUILD] = 0;
+  }
+  cudaGraphSetConditional(cond, status[ST_NBR_OVERFLOW] != 0 ? 1u : 0u);
+}
+void launch_rebuild_done_cond(int *status, cudaGraphConditionalHandle cond, cudaStream_t st) {
+  rebuild_done_cond_kernel<<<1, 1, 0, st>>>(status, cond);
+}
+
 // the condition of a conditional graph node: status word `word` is set
 __global__ void status_cond_kernel(cudaGraphConditionalHandle cond, const int *status, int word) {
   cudaGraphSetConditional(cond, *(volatile const int *)(status + word) != 0 ? 1u : 0u);
