@@ -548,6 +548,14 @@ int count_kernel_nodes(cudaGraph_t graph);
 // h->stream, where its kernels stand down by themselves; with word < 0 it
 // also launches rebuild_done itself).
 cudaStream_t cond_begin(comdgb_sim *h, int word) {
+  // COMDGB_GRAPH_CONDITIONALS=0: no conditional nodes (the sections stand
+  // down by themselves instead).  ncu profiles no kernel of a graph that
+  // holds a conditional node, so the launch lists are taken with this set.
+  static const bool off = [] {
+    const char *e = getenv("COMDGB_GRAPH_CONDITIONALS");
+    return e && e[0] == '0';
+  }();
+  if (off) return nullptr;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   cudaGraph_t graph = nullptr;
   const cudaGraphNode_t *deps = nullptr;
