@@ -442,6 +442,9 @@ def gpu_arm(args):
         b0 = (C.c_longlong(), C.c_longlong())
         cg.lib.check(L.comdgb_transfer_bytes(s, C.byref(b0[0]), C.byref(b0[1])))
         dist.barrier()
+        import gc
+        gc.collect()
+        gc.disable()  # no collector pause inside the host-timed loop
         t0 = time.perf_counter()
         call_ms = []
         for _ in range(calls):
@@ -451,6 +454,7 @@ def gpu_arm(args):
             if e != e:
                 raise cg.ComdgbError(-30, cg.lib.last_error())
         t1 = time.perf_counter()
+        gc.enable()
         dist.barrier()
         e2e_s = dist.max(t1 - t0)
         b1 = (C.c_longlong(), C.c_longlong())
