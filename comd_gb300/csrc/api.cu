@@ -241,7 +241,9 @@ void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
 // Returns 0, or -1 when device memory ran out.
 // no table: every pair distance lies below s_lo, so the kernels take the
 // series for every pair and never index the (absent) table
-PairSeg no_pair_seg() { return PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0}; }
+PairSeg no_pair_seg() {
+  return PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0, nullptr, 1.0f, 0, nullptr, nullptr};
+}
 
 int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
                    const double b[6], double pair_lo, double rc, PairSeg *out) {
@@ -263,6 +265,7 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
     return (q == 0 ? cheb_host(coef[3], a[3], b[3], r) : cheb_host(coef[4], a[4], b[4], r)) / r;
   };
   std::vector<float4> p1((size_t)2 * n);
+  std::vector<double> dc((size_t)6 * n);  // c1, c2, c3 of phi and rho per segment
   for (int q = 0; q < 2; q++) {
     double fmax = 0, gmax = 0, ferr = 0, gerr = 0;
     double f0 = val(q, (double)s_lo), m0 = 0.5 * hs * der(q, (double)s_lo);
@@ -272,6 +275,9 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
       const double c0 = f0, c1 = m0, c2 = 3.0 * (f1 - f0) - 2.0 * m0 - m1,
                    c3 = 2.0 * (f0 - f1) + m0 + m1;
       p1[(size_t)q * n + k] = make_float4((float)c0, (float)c1, (float)c2, (float)c3);
+      dc[(size_t)6 * k + 3 * q] = c1;
+      dc[(size_t)6 * k + 3 * q + 1] = c2;
+      dc[(size_t)6 * k + 3 * q + 2] = c3;
       for (int e = 0; e <= 8; e++) {
         const double t = e / 8.0, s = (double)s_lo + (k + t) * hs;
         const double fv = val(q, s), gv = der(q, s);
@@ -287,6 +293,45 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
     }
     if (!(ferr <= 1e-7 * fmax) || !(gerr <= 1e-6 * gmax)) return 0;
   }
+  // the density pass's rho table: n1 segments, values checked as above
+  const int n1 = SEG1_N;
+  const float inv_h1 = (float)(n1 / (rc * rc - (double)s_lo));
+  const double hs1 = 1.0 / (double)inv_h1;
+  {
+    double fmax = 0, ferr = 0;
+    double f0 = val(1, (double)s_lo), m0 = 0.5 * hs1 * der(1, (double)s_lo);
+    for (int k = 0; k < n1; k++) {
+      const double s1 = (double)s_lo + (k + 1) * hs1;
+      const double f1 = val(1, s1), m1 = 0.5 * hs1 * der(1, s1);
+      const double c0 = f0, c1 = m0, c2 = 3.0 * (f1 - f0) - 2.0 * m0 - m1,
+                   c3 = 2.0 * (f0 - f1) + m0 + m1;
+      p1.push_back(make_float4((float)c0, (float)c1, (float)c2, (float)c3));
+      for (int e = 0; e <= 8; e++) {
+        const double t = e / 8.0, s = (double)s_lo + (k + t) * hs1;
+        const double fv = val(1, s), pv = ((c3 * t + c2) * t + c1) * t + c0;
+        fmax = std::max(fmax, fabs(fv));
+        ferr = std::max(ferr, fabs(pv - fv));
+      }
+      f0 = f1;
+      m0 = m1;
+    }
+    if (!(ferr <= 1e-7 * fmax)) return 0;
+  }
+  // the force pass's derivative quadratics: d/dt of each cubic times dscale
+  const size_t off4 = p1.size();
+  const double ds = (double)dscale;
+  for (int k = 0; k < n; k++) {
+    const double *c = &dc[(size_t)6 * k];
+    p1.push_back(make_float4((float)(ds * c[0]), (float)(ds * 2.0 * c[1]), (float)(ds * 3.0 * c[2]),
+                             (float)(ds * c[3])));
+  }
+  const size_t off2 = p1.size();  // then n float2, two per float4
+  for (int k = 0; k < n; k += 2) {
+    const double *c = &dc[(size_t)6 * k];
+    const double *e = &dc[(size_t)6 * (k + 1)];
+    p1.push_back(make_float4((float)(ds * 2.0 * c[4]), (float)(ds * 3.0 * c[5]),
+                             (float)(ds * 2.0 * e[4]), (float)(ds * 3.0 * e[5])));
+  }
   int err = 0;
   float4 *d1 = h->seg_buf ? h->seg_buf : track(h, dalloc<float4>(p1.size(), &err));
   if (err) return -1;
@@ -294,7 +339,8 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
   if (cudaMemcpy(d1, p1.data(), sizeof(float4) * p1.size(), cudaMemcpyHostToDevice) !=
       cudaSuccess)
     return -1;
-  *out = PairSeg{d1, s_lo, inv_h, dscale, n};
+  *out = PairSeg{d1, s_lo, inv_h, dscale, n, d1 + 2 * (size_t)n, inv_h1, n1, d1 + off4,
+                 reinterpret_cast<const float2 *>(d1 + off2)};
   return 0;
 }
 

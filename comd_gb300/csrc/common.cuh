@@ -326,11 +326,30 @@ struct ChebLow32 {
 // derivatives of its phi and rho series (genDer), so phi'(r)/r = 2 dphi/ds
 // = dscale * dphi/dt with dscale = 2 * inv_h, and likewise rho'(r)/r.
 // s < s_lo (and n == 0: no table) takes the series instead.
-constexpr int SEG_N = 2048;  // segments of the table
+// The force-order density pass reads rho alone, no derivative: it has its
+// own rho table of SEG1_N segments over the same range (rho1, inv_h1: a
+// fourth of the shared memory, so the pass keeps more of the L1 cache).
+#ifndef COMDGB_SEG_N
+#define COMDGB_SEG_N 2048
+#endif
+#ifndef COMDGB_SEG1_N
+#define COMDGB_SEG1_N 512
+#endif
+constexpr int SEG_N = COMDGB_SEG_N;    // segments of the table
+constexpr int SEG1_N = COMDGB_SEG1_N;  // segments of the density pass's rho table
+static_assert(SEG_N % 2 == 0, "the float2 derivative records pair up into float4");
 struct PairSeg {
   const float4 *p1;
   float s_lo, inv_h, dscale;
   int n;
+  const float4 *rho1;  // [n1] rho cubics for the density pass
+  float inv_h1;
+  int n1;
+  // the force-order force pass reads derivatives: on segment k, phi'(r)/r =
+  // d4.x + d4.y t + d4.z t^2 and rho'(r)/r = d4.w + d2.x t + d2.y t^2, the
+  // derivatives of the cubics above scaled by dscale, rounded once from FP64
+  const float4 *d4;  // [n]
+  const float2 *d2;  // [n]
 };
 
 __device__ __forceinline__ float seg_cubic(float4 c, float t) {

@@ -1089,11 +1089,13 @@ __device__ __forceinline__ bool fo_rho(const EamPot<float, EVAL> &P, const float
   }
   return true;
 }
+// (sm: the density pass's rho table, n1 segments; the same lower end s_lo,
+// so "below the table" is below_seg's test)
 static __device__ __forceinline__ bool fo_rho(const EamPot<float, EVAL_CHEBY> &P,
                                               const float4 *sm, float r2, float &rho) {
-  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h1;
   if (!(u >= 0.f)) return false;
-  const int k = min((int)u, P.seg.n - 1);
+  const int k = min((int)u, P.seg.n1 - 1);
   rho = seg_cubic(sm[k], u - (float)k);
   return true;
 }
@@ -1107,9 +1109,10 @@ static __device__ __noinline__ float fo_rho_series(const EamPot<float, EVAL_CHEB
   return cheb_series(P, 1, r);
 }
 
-// phi, phi'(r)/r and rho'(r)/r of one pair distance: both halves of the
-// pair table (sm), or the table evaluator.  false: below the pair table
-template <int EVAL>
+// phi (OBS only), phi'(r)/r and rho'(r)/r of one pair distance: the force
+// pass's tables (sm, staged by stage_force_table), or the table evaluator.
+// false: below the pair table
+template <bool OBS, int EVAL>
 __device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL> &P, const float4 *, float r2,
                                         float &phi, float &wphi, float &wrho) {
   float r, inv_r, dphi, v, drho;
@@ -1126,18 +1129,36 @@ __device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL> &P, const floa
   wrho = drho * inv_r;
   return true;
 }
+// (the derivative quadratics: one 16-byte and one 8-byte shared load per
+// pair, the phi cubic a third only when the energy is summed)
+template <bool OBS>
 static __device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL_CHEBY> &P,
                                                const float4 *sm, float r2, float &phi,
                                                float &wphi, float &wrho) {
   const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
   if (!(u >= 0.f)) return false;
-  const int k = min((int)u, P.seg.n - 1);
+  const int n = P.seg.n;
+  const int k = min((int)u, n - 1);
   const float t = u - (float)k;
-  const float4 cp = sm[k], cr = sm[P.seg.n + k];
-  phi = seg_cubic(cp, t);
-  wphi = P.seg.dscale * seg_dcubic(cp, t);
-  wrho = P.seg.dscale * seg_dcubic(cr, t);
+  const float4 d = sm[k];
+  const float2 e = reinterpret_cast<const float2 *>(sm + n)[k];
+  wphi = fmaf(fmaf(d.z, t, d.y), t, d.x);
+  wrho = fmaf(fmaf(e.y, t, e.x), t, d.w);
+  if (OBS) phi = seg_cubic(sm[n + n / 2 + k], t);
   return true;
+}
+
+// the force pass's tables into shared memory, once per CTA: the derivative
+// quadratics (n float4, then n float2), and with OBS the phi cubics
+template <bool OBS>
+__device__ __forceinline__ void stage_force_table(float4 *sm, const PairSeg &S) {
+  const int n = S.n;
+  const float4 *d2 = reinterpret_cast<const float4 *>(S.d2);
+  for (int q = threadIdx.x; q < n; q += blockDim.x) sm[q] = __ldg(S.d4 + q);
+  for (int q = threadIdx.x; q < n / 2; q += blockDim.x) sm[n + q] = __ldg(d2 + q);
+  if (OBS)
+    for (int q = threadIdx.x; q < n; q += blockDim.x) sm[n + n / 2 + q] = __ldg(S.p1 + q);
+  __syncthreads();
 }
 // the series for a pair below the table (FP32 Chebyshev only)
 template <int EVAL>
@@ -1186,7 +1207,7 @@ template <int EVAL, bool MULTI, bool OBS>
 __global__ void FO1_BOUNDS
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1 + P.seg.n, P.seg.n);  // the rho cubics
+  if (uses_seg(P)) stage_seg(seg_sm, P.seg.rho1, P.seg.n1);  // the density pass's rho cubics
   const float rc2 = P.rc2;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
@@ -1307,7 +1328,7 @@ template <int EVAL, bool MULTI, bool OBS>
 __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.p1, 2 * P.seg.n);  // phi and rho cubics
+  if (uses_seg(P)) stage_force_table<OBS>(seg_sm, P.seg);
   const float rc2 = P.rc2;
   const bool fuse = !OBS && *(volatile const int *)(A.status + ST_FUSE);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
@@ -1325,7 +1346,7 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
     walk([&](float fj, float dx, float dy, float dz, float r2) {
       if (r2 > rc2) return;
       float phi, wphi, wrho;
-      if (!fo_pair(P, seg_sm, r2, phi, wphi, wrho)) {
+      if (!fo_pair<OBS>(P, seg_sm, r2, phi, wphi, wrho)) {
         low = true;
         return;
       }

@@ -33,11 +33,13 @@ static size_t pass_smem(int pass, int eval) {
   return sizeof(float4) * (pass == 0 ? 2 : 1) * SEG_N;
 }
 
-// force order: the density pass stages the rho cubics of the pair table,
-// the force pass both halves
-static size_t fo_pass_smem(int pass, int eval) {
+// force order: the density pass stages its rho table (SEG1_N cubics), the
+// force pass the derivative quadratics (SEG_N float4 + SEG_N float2) and,
+// summing energies (obs), the phi cubics
+static size_t fo_pass_smem(int pass, int eval, bool obs = true) {
   if (sizeof(FT) != 4 || eval != EVAL_CHEBY) return 0;
-  return sizeof(float4) * (pass == 0 ? 1 : 2) * SEG_N;
+  if (pass == 0) return sizeof(float4) * SEG1_N;
+  return sizeof(float4) * (SEG_N + SEG_N / 2 + (obs ? SEG_N : 0));
 }
 
 #if COMDGB_FT_FLOAT
@@ -65,7 +67,7 @@ template <bool OBS>
 static cudaError_t fo_occupancy() {
   int dummy = 0;
   int(&o)[3][2] = g_fo_per_sm[OBS];
-  const size_t s0 = fo_pass_smem(0, EVAL_CHEBY), s1 = fo_pass_smem(1, EVAL_CHEBY);
+  const size_t s0 = fo_pass_smem(0, EVAL_CHEBY), s1 = fo_pass_smem(1, EVAL_CHEBY, OBS);
   cudaError_t e = pass_occupancy(fo_eam_pass1_kernel<EVAL_TABLE, false, OBS>, 0,
                                  &o[0][EVAL_TABLE], FO1_THREADS);
   if (e == cudaSuccess)
@@ -200,7 +202,7 @@ void launch_nbr_build<FT>(const ForceArgs &A, FT rc2, cudaStream_t st, const Tun
 template <int EVAL, bool OBS>
 static void launch_fo_eam_obs(const ForceArgs &A, const EamPot<float, EVAL> &P, int pass,
                               cudaStream_t st, const Tune *tune) {
-  const size_t smem = P.seg.n > 0 ? fo_pass_smem(pass, EVAL) : 0;
+  const size_t smem = P.seg.n > 0 ? fo_pass_smem(pass, EVAL, OBS) : 0;
   const bool multi = A.g.nrep > 1;
   if (pass == 0) {
     const int g0 = pass_grid(0, EVAL, A.ntot, true, FO1_THREADS, OBS);
@@ -236,7 +238,7 @@ template void launch_fo_eam<EVAL_CHEBY>(const ForceArgs &, const EamPot<float, E
 template <int EVAL, bool OBS>
 static int fo_pass2_per_sm(bool multi, int threads) {
   int per_sm = 0;
-  const size_t smem = fo_pass_smem(1, EVAL);
+  const size_t smem = fo_pass_smem(1, EVAL, OBS);
   const cudaError_t e =
       multi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                   &per_sm, fo_eam_pass2_kernel<EVAL, true, OBS>, threads, smem)
