@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <chrono>
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
@@ -104,6 +105,7 @@ void free_all(comdgb_sim *h) {
   if (h->loop_exec) cudaGraphExecDestroy(h->loop_exec);
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
+  if (h->force_exec_tracked) cudaGraphExecDestroy(h->force_exec_tracked);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
   if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
   for (cudaGraphExec_t &x : h->part_exec)
@@ -436,9 +438,10 @@ void cgapi::drop_graphs(comdgb_sim *h) {
   h->loop_exec = nullptr;
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
+  if (h->force_exec_tracked) cudaGraphExecDestroy(h->force_exec_tracked);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
   if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
-  h->step_exec = h->force_exec = h->timed_exec = nullptr;
+  h->step_exec = h->force_exec = h->force_exec_tracked = h->timed_exec = nullptr;
   h->timed_graph = nullptr;
   for (cudaGraphExec_t &x : h->part_exec) {
     if (x) cudaGraphExecDestroy(x);
@@ -768,8 +771,10 @@ void enqueue_step(comdgb_sim *h, double dt_atu, cudaEvent_t *ev, int part) {
     if (part != PART_FULL) return;
   }
   cudaMemsetAsync(h->status + ST_REBIN_SERIAL, 0, sizeof(int), st);
+  // the closing part writes the FP32 copies and the force-order tracking for
+  // the force call that ends the sequence
   launch_advance_vp(h->g, h->s, h->atom_slot, h->ntot, dt_atu, dt_atu / 2.0, h->rmass, h->mixed,
-                    h->w, h->status, st);
+                    h->w, h->status, st, h->mixed && part == PART_CLOSE);
   if (ev) cudaEventRecordWithFlags(ev[evi++], st, cudaEventRecordExternal);
   enqueue_classify_finish(h);
   enqueue_compact(h);
@@ -789,18 +794,22 @@ int count_kernel_nodes(cudaGraph_t graph) {
   return k;
 }
 
-// part: the step part to capture, or PART_NONE
-int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool force) {
+// part: the step part to capture, or PART_NONE; force: then a force call
+// (tracked: after a closing part, which wrote the FP32 copies and the
+// force-order tracking itself)
+int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool force,
+            bool tracked = false) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   const bool step = part != PART_NONE;
   if (step) enqueue_step(h, dt_atu, nullptr, part);
   if (force) {
     int evi = 0;
-    // the last half step of a step leaves the FP32 copy stale
-    if (h->mixed) launch_pos32(h->g, h->s, h->stream);
+    // the last half step of a step leaves the FP32 copy stale (unless the
+    // closing part of a merged sequence wrote it)
+    if (h->mixed && !tracked) launch_pos32(h->g, h->s, h->stream);
     if (h->pl.vlist) launch_skin_check(h->g, h->s, h->pl, h->mixed, h->status, h->stream);
-    if (h->fo.list)
+    if (h->fo.list && !tracked)
       launch_fo_track(h->g, h->s, h->fo, h->atom_slot, h->ntot, h->status, h->stream);
     enqueue_force_parts(h, nullptr, evi);
     enqueue_reduce(h);
@@ -812,6 +821,8 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool 
   if (*exec) cudaGraphExecDestroy(*exec);
   cudaError_t e = cudaGraphInstantiate(exec, graph, 0);
   cudaGraphDestroy(graph);
+  // on the device now, conditional bodies included, not at a first launch
+  if (e == cudaSuccess) e = cudaGraphUpload(*exec, h->stream);
   if (e != cudaSuccess)
     return set_err(COMDGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
   return 0;
@@ -843,15 +854,30 @@ int finish_force(comdgb_sim *h) {
   return 0;
 }
 
-int do_force(comdgb_sim *h) {
-  if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
-  if (!h->force_exec) {
-    int rc = capture(h, &h->force_exec, 0.0, PART_NONE, true);
+// the force call graph; after_steps: the one that ends a step sequence
+// (with the rebox merged in mixed precision the closing part already wrote
+// the FP32 copies and the tracking, so that graph skips them)
+int force_graph(comdgb_sim *h, bool after_steps, cudaGraphExec_t *out) {
+  const bool tracked = after_steps && h->merge_rebox && h->mixed;
+  cudaGraphExec_t *exec = tracked ? &h->force_exec_tracked : &h->force_exec;
+  if (!*exec) {
+    int rc = capture(h, exec, 0.0, PART_NONE, true, tracked);
     if (rc) return rc;
   }
-  CK(cudaGraphLaunch(h->force_exec, h->stream));
+  *out = *exec;
+  return 0;
+}
+
+int do_force_ex(comdgb_sim *h, bool after_steps) {
+  if (h->opts.potential < 0) return set_err(COMDGB_ERR_ARG, "simulation has no potential");
+  cudaGraphExec_t exec = nullptr;
+  int rc = force_graph(h, after_steps, &exec);
+  if (rc) return rc;
+  CK(cudaGraphLaunch(exec, h->stream));
   return finish_force(h);
 }
+
+int do_force(comdgb_sim *h) { return do_force_ex(h, false); }
 
 // n steps as one captured graph (captured once per n and dt), launched once
 // between two events; *ms = the graph's device time.  Then the force call
@@ -878,6 +904,7 @@ int do_steps_graph(comdgb_sim *h, int n, double dt, float *ms) {
     CK(cudaStreamEndCapture(h->stream, &graph));
     cudaError_t e = cudaGraphInstantiate(&h->loop_exec, graph, 0);
     cudaGraphDestroy(graph);
+    if (e == cudaSuccess) e = cudaGraphUpload(h->loop_exec, h->stream);
     if (e != cudaSuccess)
       return set_err(COMDGB_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
     h->loop_n = n;
@@ -896,7 +923,7 @@ int do_steps_graph(comdgb_sim *h, int n, double dt, float *ms) {
   cudaEventDestroy(e1);
   if (ms) *ms = t;
   int rc = check_status(h);
-  return rc ? rc : do_force(h);
+  return rc ? rc : do_force_ex(h, n > 0);
 }
 
 // the step graphs for dt_atu: one step, or the three parts with the rebox
@@ -939,7 +966,7 @@ int do_steps(comdgb_sim *h, int n, double dt) {
     if (!rc) rc = launch_steps(h, n, h->stream);
     if (rc) return rc;
   }
-  return do_force(h);
+  return do_force_ex(h, n > 0);
 }
 
 // ---- host transfers ---------------------------------------------------------
@@ -1218,8 +1245,9 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
     int rc = ensure_step_graphs(h, dt_atu);
     if (rc) return rc;
   }
-  if (!h->force_exec) {
-    int rc = capture(h, &h->force_exec, 0.0, PART_NONE, true);
+  cudaGraphExec_t force_exec = nullptr;
+  {
+    int rc = force_graph(h, n > 0, &force_exec);
     if (rc) return rc;
   }
   cudaStream_t st = h->stream, cs = h->copy_stream;
@@ -1232,8 +1260,10 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
   const size_t nb = (size_t)h->reps[0].nb, ns = nb * CG_MAXATOMS, NS = (size_t)h->nslots;
   CK(cudaMemcpyAsync(s->natoms, h->s.natoms, nb * sizeof(int), cudaMemcpyDeviceToHost, cs));
   h->xfer_d2h += (long long)(nb * sizeof(int));
-  CK(cudaGraphLaunch(h->force_exec, st));  // the trailing force call (timestep.c:139)
+  CK(cudaGraphLaunch(force_exec, st));  // the trailing force call (timestep.c:139)
+  const auto ta = std::chrono::steady_clock::now();
   CK(cudaStreamSynchronize(cs));
+  const auto tb = std::chrono::steady_clock::now();
   const int w = max_occupancy(s->natoms, nb);
   {
     const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
@@ -1246,8 +1276,18 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
     CKX(s->p, h->stage3 + 3 * NS, 3 * sizeof(double), nb, w, D2H, xfer_d2h, cs);
   }
   int rc = finish_force(h);
+  const auto tc = std::chrono::steady_clock::now();
   if (!rc) rc = download_forces_rep(h, 0, s, w);
+  const auto td = std::chrono::steady_clock::now();
   const cudaError_t e = cudaStreamSynchronize(cs);
+  const auto te = std::chrono::steady_clock::now();
+  {
+    const auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+    char buf[160];
+    snprintf(buf, sizeof buf, " (steps %.2f, force %.2f, forces down %.2f, state down %.2f)",
+             ms(ta, tb), ms(tb, tc), ms(tc, td), ms(td, te));
+    h->trace_note = buf;
+  }
   if (!rc && e != cudaSuccess)
     rc = set_err(COMDGB_ERR_CUDA, "state download: %s", cudaGetErrorString(e));
   return rc;
@@ -1913,6 +1953,7 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
     if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
     h->timed_graph = graph;  // node handles below belong to it
     CK(cudaGraphInstantiate(&h->timed_exec, graph, 0));
+    CK(cudaGraphUpload(h->timed_exec, h->stream));
     // map each capture event to its record node in the instantiated graph
     h->timed_nodes.assign(NE, nullptr);
     for (cudaGraphNode_t nd : nodes) {
@@ -1974,7 +2015,7 @@ int comdgb_sim_timed_steps(comdgb_sim *h, int n, double dt, float *step_ms, floa
   int rc = check_status(h);
   if (rc) return rc;
   // forces of the final positions, as nTimeSteps ends (timestep.c:137)
-  rc = do_force(h);
+  rc = do_force_ex(h, true);
   if (rc) return rc;
   return NG;
 }
@@ -2054,9 +2095,22 @@ double comdgb_nTimeSteps(int n, simflat_t *s, double dt) {
     set_err(COMDGB_ERR_NOTATTACHED, "simflat_t is not attached");
     return NAN;
   }
+  // COMDGB_TRACE_CALLS=1: the host time of the call's phases on stderr
+  static const bool trace = [] {
+    const char *e = getenv("COMDGB_TRACE_CALLS");
+    return e && e[0] == '1';
+  }();
+  const auto t0 = std::chrono::steady_clock::now();
   int rc = drop_in_enter(h, s, false);
+  const auto t1 = std::chrono::steady_clock::now();
   if (!rc) rc = h->lazy ? do_steps(h, n, dt) : steps_and_download(h, n, dt, s);
   if (!rc && h->lazy) rc = drop_in_leave(h, s, true);
+  if (trace) {
+    const auto t2 = std::chrono::steady_clock::now();
+    const auto ms = [](auto a, auto b) { return std::chrono::duration<double, std::milli>(b - a).count(); };
+    fprintf(stderr, "comdgb_nTimeSteps(%d): upload %.2f ms, steps to download %.2f ms%s\n", n,
+            ms(t0, t1), ms(t1, t2), h->trace_note.c_str());
+  }
   return rc ? NAN : s->e;
 }
 

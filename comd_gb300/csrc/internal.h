@@ -39,9 +39,11 @@ void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int 
                               int *status, cudaStream_t st, bool use_delta = false);
 // p -= dt_v*f; r += dt_r*p/rmass; classify (the FP32 copy is not refreshed);
 // FP64 leaves the position increments in f.xyz and says so in the status word
+// write32: also the FP32 copies and the force-order tracking (the closing
+// part of a merged mixed-precision sequence)
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
-                       cudaStream_t st);
+                       cudaStream_t st, bool write32 = false);
 // merged rebox (mixed precision): p -= dt_v*f, then the closing position
 // half step of one step and the opening one of the next with no rebox
 // between them (one update r += p*(2*dt_r/rmass)), the FP32 copy, the list

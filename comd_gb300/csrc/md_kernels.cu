@@ -345,10 +345,10 @@ void launch_advance_positions(const Geom &g, Slots s, const int *atom_slot, int 
 
 void launch_advance_vp(const Geom &g, Slots s, const int *atom_slot, int ntot, double dt_v,
                        double dt_r, double rmass, bool mixed, const RebinWork &w, int *status,
-                       cudaStream_t st) {
+                       cudaStream_t st, bool write32) {
   cudaMemsetAsync(w.depmask, 0, sizeof(uint32_t) * 4 * (size_t)g.nboxes, st);
   launch_advance<true, true>(g, s, atom_slot, ntot, dt_v, dt_r, dt_r / rmass, rmass, mixed,
-                             false, true, DELTA_STORE, false, w, status, st);
+                             write32, true, DELTA_STORE, false, w, status, st);
   // FP64: f.xyz now holds the increments (the next position half step
   // reuses them); mixed precision does not keep them
   if (!mixed) cudaMemsetAsync(status + ST_DELTA, 0x01, 1, st);
@@ -873,25 +873,37 @@ __global__ void __launch_bounds__(RD_THREADS) reduce_force_kernel(ForceArgs A, d
   }
 }
 
-__global__ void reduce_final_kernel(const double *partials, const long long *ipartials, int npart,
-                                    double *out, long long *iout) {
-  if (threadIdx.x != 0) return;
+// The block partials summed by one CTA in a fixed order (thread t sums
+// partials t, t + RD_THREADS, ... in turn, then the block tree), so every
+// run gives the same bits.  (One thread summing them serially took 150 us
+// for the ~1000 partials of 4 M atoms.)
+__global__ void __launch_bounds__(RD_THREADS) reduce_final_kernel(const double *partials,
+                                                                  const long long *ipartials,
+                                                                  int npart, double *out,
+                                                                  long long *iout) {
+  __shared__ double shd[RD_THREADS / 32];
+  __shared__ long long shl[RD_THREADS / 32];
   double e = 0.0, sx = 0.0;
   long long np = 0;
-  for (int q = 0; q < npart; q++) {
+  for (int q = threadIdx.x; q < npart; q += RD_THREADS) {
     e += partials[2 * q];
     sx += partials[2 * q + 1];
     np += ipartials[q];
   }
-  out[0] = e;
-  out[1] = sx;
-  iout[0] = np;
+  e = block_sum_d(e, shd);
+  sx = block_sum_d(sx, shd);
+  np = block_sum_l(np, shl);
+  if (threadIdx.x == 0) {
+    out[0] = e;
+    out[1] = sx;
+    iout[0] = np;
+  }
 }
 
 void launch_reduce(const ForceArgs &A, double *partials, long long *ipartials, int npart,
                    double *out, long long *iout, cudaStream_t st) {
   reduce_force_kernel<<<npart, RD_THREADS, 0, st>>>(A, partials, ipartials);
-  reduce_final_kernel<<<1, 32, 0, st>>>(partials, ipartials, npart, out, iout);
+  reduce_final_kernel<<<1, RD_THREADS, 0, st>>>(partials, ipartials, npart, out, iout);
 }
 
 // per replica (one block each, fixed order): energy sum f.w and stress share
@@ -931,19 +943,22 @@ __global__ void __launch_bounds__(RD_THREADS) kinetic_kernel(Slots s, const int 
   if (threadIdx.x == 0) partials[blockIdx.x] = ek;
 }
 
-__global__ void kinetic_final_kernel(const double *partials, int npart, double rmass,
-                                     double *out) {
-  if (threadIdx.x != 0) return;
+// (the partials summed as in reduce_final_kernel)
+__global__ void __launch_bounds__(RD_THREADS) kinetic_final_kernel(const double *partials,
+                                                                   int npart, double rmass,
+                                                                   double *out) {
+  __shared__ double shd[RD_THREADS / 32];
   double ek = 0.0;
-  for (int q = 0; q < npart; q++) ek += partials[q];
-  out[0] = ek / (2.0 * rmass);
+  for (int q = threadIdx.x; q < npart; q += RD_THREADS) ek += partials[q];
+  ek = block_sum_d(ek, shd);
+  if (threadIdx.x == 0) out[0] = ek / (2.0 * rmass);
 }
 
 void launch_kinetic(const Geom &g, Slots s, const int *atom_slot, int ntot, double rmass,
                     double *partials, int npart, double *out, cudaStream_t st) {
   (void)g;
   kinetic_kernel<<<npart, RD_THREADS, 0, st>>>(s, atom_slot, ntot, partials);
-  kinetic_final_kernel<<<1, 32, 0, st>>>(partials, npart, rmass, out);
+  kinetic_final_kernel<<<1, RD_THREADS, 0, st>>>(partials, npart, rmass, out);
 }
 
 // ---------------------------------------------------------------------------

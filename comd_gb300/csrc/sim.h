@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "comdgb.h"
@@ -128,6 +129,9 @@ struct comdgb_sim {
   cudaGraphExec_t part_exec[3] = {nullptr, nullptr, nullptr};
   cudaGraphExec_t step_exec = nullptr;
   cudaGraphExec_t force_exec = nullptr;
+  // the force call that ends a merged mixed-precision sequence: the closing
+  // part has already written the FP32 copies and the force-order tracking
+  cudaGraphExec_t force_exec_tracked = nullptr;
   double graph_dt = NAN;
   // n steps captured as one graph (comdgb_sim_graph_steps)
   cudaGraphExec_t loop_exec = nullptr;
@@ -147,6 +151,7 @@ struct comdgb_sim {
   cudaStream_t cond_stream = nullptr;
   int rebuild_kernels = 0;
   int overflow_kernels = 0;  // the slot-order copy's refresh after a list overflow
+  std::string trace_note;    // phases of the last drop-in call (COMDGB_TRACE_CALLS)
   // host last results
   double e = 0.0, stress = 0.0;
   simflat_t *host = nullptr;   // drop-in owner (attach)
