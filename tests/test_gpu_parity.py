@@ -422,6 +422,39 @@ def test_persistent_lists_match_per_step_lists(oracle, precision):
 
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 7])
+def test_step_sequences_match_single_steps(oracle, n):
+    """In force order a sequence of n steps makes every step's velocity step
+    and position half steps inside the force pass before it, except the last
+    step's, which the closing part makes (the ST_FUSE flag the host sets and
+    clears).  n steps in one call against n calls of one step (where no
+    force pass makes an update) agree up to the roundings of adding the two
+    half steps at once: a misplaced update would be off by half a step."""
+    c = Case(oracle, cg.POT_EAM_CHEBY, n=(8, 8, 8), temp=900.0, amp=0.05)
+    try:
+        o = cg.opts(cg.POT_EAM_CHEBY, cg.PREC_MIXED, cheby_from_host=True)
+        res = []
+        for calls, s in ((1, c.s), (n, c.o)):
+            d = cg.DeviceSim(s, o)
+            try:
+                assert d.list_info()[0]
+                for _ in range(calls):
+                    e, _ = d.steps(n // calls, 1e-15)
+                d.download(s)
+            finally:
+                d.close()
+            res.append((e, world_by_id(s), by_id(s, "p")[:, :3].copy()))
+        (e0, w0, p0), (e1, w1, p1) = res
+        assert abs(e1 - e0) <= 1e-10 * abs(e0), (e0, e1)
+        dw = w1 - w0
+        L = np.array(list(c.s.contents.bounds))
+        dw -= L * np.round(dw / L)
+        assert np.abs(dw).max() < 1e-9
+        assert rel_rms(p1, p0) < 1e-9
+    finally:
+        c.close()
+
+
 @pytest.mark.parametrize("kw", [dict(periodic=False), dict(n=(4, 4, 4)), dict(n=(2, 5, 4))],
                          ids=["nonperiodic", "two-box-grid", "mixed-grid"])
 def test_mixed_without_force_order(oracle, kw):
