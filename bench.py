@@ -497,9 +497,12 @@ def gpu_arm(args):
         groups[name] = g
     dg = groups[dom]
     traffic = committed_traffic().get(dom)
+    limits = committed_traffic().get("limits", {})
     roofline = {"kernel": dom, "bound": dg.get("bound"), "achieved": dg.get("achieved"),
                 "peak": dg.get("peak"), "unit": dg.get("unit"), "frac": dg.get("frac"),
                 "traffic": traffic,
+                # the unit the kernel is really bound by, from the committed ncu capture
+                "measured_limit": limits.get(dom),
                 "peak_source": ("FP32 FMA throughput measured on this GPU by "
                                 "comdgb_fp32_fma_peak (no FP32 figure in MEASURED_PEAKS.json)"
                                 if dg.get("bound") == "fp32" else "MEASURED_PEAKS.json hbm_gbs"),
