@@ -80,6 +80,8 @@ ForceArgs force_args(comdgb_sim *h) {
   A.status = h->status;
   A.pl = h->pl;
   A.fo = h->fo;
+  A.vv_dt = A.vv_c = 0.0;
+  A.host_f = A.host_rho = A.host_fi = nullptr;
   return A;
 }
 
@@ -106,6 +108,7 @@ void free_all(comdgb_sim *h) {
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
   if (h->force_exec_tracked) cudaGraphExecDestroy(h->force_exec_tracked);
+  if (h->force_exec_host) cudaGraphExecDestroy(h->force_exec_host);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
   if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
   for (cudaGraphExec_t &x : h->part_exec)
@@ -439,9 +442,11 @@ void cgapi::drop_graphs(comdgb_sim *h) {
   if (h->step_exec) cudaGraphExecDestroy(h->step_exec);
   if (h->force_exec) cudaGraphExecDestroy(h->force_exec);
   if (h->force_exec_tracked) cudaGraphExecDestroy(h->force_exec_tracked);
+  if (h->force_exec_host) cudaGraphExecDestroy(h->force_exec_host);
   if (h->timed_exec) cudaGraphExecDestroy(h->timed_exec);
   if (h->timed_graph) cudaGraphDestroy(h->timed_graph);
-  h->step_exec = h->force_exec = h->force_exec_tracked = h->timed_exec = nullptr;
+  h->step_exec = h->force_exec = h->force_exec_tracked = h->force_exec_host = h->timed_exec =
+      nullptr;
   h->timed_graph = nullptr;
   for (cudaGraphExec_t &x : h->part_exec) {
     if (x) cudaGraphExecDestroy(x);
@@ -517,12 +522,20 @@ void enqueue_classify_finish(comdgb_sim *h, bool lazy = false) {
                       lazy ? h->status : nullptr);
 }
 
-void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool obs = true) {
+void enqueue_force_parts(comdgb_sim *h, cudaEvent_t *ev, int &evi, bool obs = true,
+                         bool host_out = false) {
   // ev (optional) records after each group: compact, nbr, pass1, pass2.
   // obs = false: a force call inside a step sequence, whose energies, stress,
   // rho and F' the next force call overwrites before the caller can read
-  // them (the force-order passes then compute forces only)
+  // them (the force-order passes then compute forces only).  host_out: the
+  // force-order passes also write f, rho and F' into the attached host
+  // arrays (zero-copy), so no download follows the call.
   ForceArgs A = force_args(h);
+  if (host_out && h->fo.list) {
+    A.host_f = h->hs.f;
+    A.host_rho = h->hs.rho;
+    A.host_fi = h->hs.fi;
+  }
   cudaStream_t st = h->stream;
   cudaMemsetAsync(h->status + ST_DELTA, 0, sizeof(int), st);  // f is about to hold forces
   launch_compact(h->g, h->s.natoms, h->box_start, h->atom_slot, h->ntot, h->cpart, h->ncpart,
@@ -798,7 +811,7 @@ int count_kernel_nodes(cudaGraph_t graph) {
 // (tracked: after a closing part, which wrote the FP32 copies and the
 // force-order tracking itself)
 int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool force,
-            bool tracked = false) {
+            bool tracked = false, bool host_out = false) {
   cudaGraph_t graph;
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   const bool step = part != PART_NONE;
@@ -811,7 +824,7 @@ int capture(comdgb_sim *h, cudaGraphExec_t *exec, double dt_atu, int part, bool 
     if (h->pl.vlist) launch_skin_check(h->g, h->s, h->pl, h->mixed, h->status, h->stream);
     if (h->fo.list && !tracked)
       launch_fo_track(h->g, h->s, h->fo, h->atom_slot, h->ntot, h->status, h->stream);
-    enqueue_force_parts(h, nullptr, evi);
+    enqueue_force_parts(h, nullptr, evi, true, host_out);
     enqueue_reduce(h);
   }
   CK(cudaStreamEndCapture(h->stream, &graph));
@@ -857,11 +870,16 @@ int finish_force(comdgb_sim *h) {
 // the force call graph; after_steps: the one that ends a step sequence
 // (with the rebox merged in mixed precision the closing part already wrote
 // the FP32 copies and the tracking, so that graph skips them)
-int force_graph(comdgb_sim *h, bool after_steps, cudaGraphExec_t *out) {
+// host_out: the force-order passes write f, rho and F' straight into the
+// attached host arrays (only with `tracked`, in force order)
+int force_graph(comdgb_sim *h, bool after_steps, cudaGraphExec_t *out, bool host_out = false) {
   const bool tracked = after_steps && h->merge_rebox && h->mixed;
-  cudaGraphExec_t *exec = tracked ? &h->force_exec_tracked : &h->force_exec;
+  host_out = host_out && tracked && h->fo.list;
+  cudaGraphExec_t *exec = host_out  ? &h->force_exec_host
+                          : tracked ? &h->force_exec_tracked
+                                    : &h->force_exec;
   if (!*exec) {
-    int rc = capture(h, exec, 0.0, PART_NONE, true, tracked);
+    int rc = capture(h, exec, 0.0, PART_NONE, true, tracked, host_out);
     if (rc) return rc;
   }
   *out = *exec;
@@ -1168,11 +1186,14 @@ static int replica_width(comdgb_sim *h, int r, int w) {
   return max_occupancy(n.data(), n.size());
 }
 
-int download_forces_rep(comdgb_sim *h, int r, simflat_t *s, int w = -1) {
+// written: the force call already wrote f, rho and F' into the host arrays
+int download_forces_rep(comdgb_sim *h, int r, simflat_t *s, int w = -1, bool written = false) {
   cudaStream_t st = h->stream;
   const RepGeo &R = h->reps[r];
   const size_t nb = (size_t)R.nb, s0 = (size_t)R.box0 * CG_MAXATOMS;
-  if (zero_copy(h, s)) {
+  if (written) {
+    h->xfer_d2h += (long long)h->ntot * kForceBytes;
+  } else if (zero_copy(h, s)) {
     launch_zc_download(h->hs, h->s, (int)nb, false, true, st);
     h->xfer_d2h += (long long)h->ntot * kForceBytes;
   } else {
@@ -1245,9 +1266,13 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
     int rc = ensure_step_graphs(h, dt_atu);
     if (rc) return rc;
   }
+  // the attached arrays registered at attach: the results of the trailing
+  // force call go to them from the passes themselves (force order)
+  const bool zc = zero_copy(h, s);
+  const bool host_out = zc && n > 0 && h->merge_rebox && h->mixed && h->fo.list;
   cudaGraphExec_t force_exec = nullptr;
   {
-    int rc = force_graph(h, n > 0, &force_exec);
+    int rc = force_graph(h, n > 0, &force_exec, host_out);
     if (rc) return rc;
   }
   cudaStream_t st = h->stream, cs = h->copy_stream;
@@ -1260,12 +1285,21 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
   const size_t nb = (size_t)h->reps[0].nb, ns = nb * CG_MAXATOMS, NS = (size_t)h->nslots;
   CK(cudaMemcpyAsync(s->natoms, h->s.natoms, nb * sizeof(int), cudaMemcpyDeviceToHost, cs));
   h->xfer_d2h += (long long)(nb * sizeof(int));
+  // the attached arrays: the state of the occupied slots by the zero-copy
+  // kernel on the copy stream, beside the trailing force call (it needs few
+  // of the SMs the L1-bound passes leave, and moves 64 bytes per atom where
+  // the 2D copies move 96 per slot up to the fullest box's occupancy)
+  if (zc) {
+    // (one CTA per SM: the download is bound by the host link, not the SMs)
+    launch_zc_download(h->hs, h->s, (int)nb, true, false, cs, h->sms);
+    h->xfer_d2h += (long long)h->ntot * kStateBytes;
+  }
   CK(cudaGraphLaunch(force_exec, st));  // the trailing force call (timestep.c:139)
   const auto ta = std::chrono::steady_clock::now();
   CK(cudaStreamSynchronize(cs));
   const auto tb = std::chrono::steady_clock::now();
   const int w = max_occupancy(s->natoms, nb);
-  {
+  if (!zc) {
     const cudaMemcpyKind D2H = cudaMemcpyDeviceToHost;
     CKX(s->id, h->s.id, sizeof(int), nb, w, D2H, xfer_d2h, cs);
     CKX(s->iType, h->s.itype, sizeof(int), nb, w, D2H, xfer_d2h, cs);
@@ -1277,7 +1311,7 @@ int steps_and_download(comdgb_sim *h, int n, double dt, simflat_t *s) {
   }
   int rc = finish_force(h);
   const auto tc = std::chrono::steady_clock::now();
-  if (!rc) rc = download_forces_rep(h, 0, s, w);
+  if (!rc) rc = download_forces_rep(h, 0, s, w, host_out);
   const auto td = std::chrono::steady_clock::now();
   const cudaError_t e = cudaStreamSynchronize(cs);
   const auto te = std::chrono::steady_clock::now();
@@ -1360,6 +1394,7 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
     delete h;
     return set_err(COMDGB_ERR_CUDA, "cudaSetDevice(%d): %s", o->device, cudaGetErrorString(ce));
   }
+  cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, o->device);
   if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->cond_stream, cudaStreamNonBlocking) != cudaSuccess) {
     if (h->stream) cudaStreamDestroy(h->stream);

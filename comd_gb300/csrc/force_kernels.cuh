@@ -44,6 +44,10 @@ struct ForceArgs {
   // force order, a step sequence: the velocity-Verlet coefficients of the
   // update the force pass makes when ST_FUSE is set (p -= vv_dt f, r += vv_c p)
   double vv_dt, vv_c;
+  // force order, a force call whose results go straight to an attached host
+  // simflat_t (device pointers of its registered f, rho, fi; slot-indexed),
+  // or null
+  double *host_f, *host_rho, *host_fi;
 };
 
 // Stencil entry of box jb seen from box b when both stencils are the full
@@ -1185,6 +1189,10 @@ __device__ __forceinline__ void fo_density_store(const ForceArgs &A,
     A.s.rho[slot] = rho_i;
     A.s.fi[slot] = (double)dF;
     A.fo.emb[a] = F;
+    if (A.host_rho) {
+      A.host_rho[slot] = rho_i;
+      A.host_fi[slot] = (double)dF;
+    }
   }
   A.s.fi32[slot] = dF;
   A.fo.pf[a] = make_float4(pi.x, pi.y, pi.z, dF);
@@ -1285,6 +1293,15 @@ struct ForceSums {
 
 constexpr int FO2_MAX_THREADS = 512;  // the force pass runs with 128, 256 (default) or 512
 
+// the force of slot into the attached host array (real4 per slot)
+__device__ __forceinline__ void fo_host_f(const ForceArgs &A, int slot, const d4 &f) {
+  double *h = A.host_f + 4 * (size_t)slot;
+  h[0] = f.x;
+  h[1] = f.y;
+  h[2] = f.z;
+  h[3] = f.w;
+}
+
 // The end of a force-order force call inside a step sequence: with ST_FUSE
 // set (fuse), atom a's velocity step with the force just summed and the two
 // position half steps around the step boundary, as one multiply-add each
@@ -1371,6 +1388,7 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
       fo.w = 0.5 * acc.ep.value() + (double)__ldg(A.fo.emb + a);
       A.s.f[slot] = fo;
       A.atom_stress[a] = acc.sx.value();
+      if (A.host_f) fo_host_f(A, slot, fo);
     }
   }
 }
@@ -1455,6 +1473,7 @@ __global__ void __launch_bounds__(PASS_THREADS) fo_lj_kernel(ForceArgs A, LjPot<
       fo.z = fz.value();
       fo.w = ep.value();
       A.s.f[slot] = fo;
+      if (A.host_f) fo_host_f(A, slot, fo);
       int ne = A.et.n[b], nonempty = 0;
       for (int e = 0; e < ne; e++) nonempty += A.s.natoms[A.et.box[b * CG_NNBR + e]] > 0;
       d4 p = A.s.p[slot];

@@ -95,7 +95,7 @@ void launch_zc_upload(const HostSlots &hs, Slots s, int nboxes, bool forces, cud
 // download of the state (id, itype, mass, r, p) or of the force results
 // (f, rho, fi)
 void launch_zc_download(const HostSlots &hs, Slots s, int nboxes, bool state, bool forces,
-                        cudaStream_t st);
+                        cudaStream_t st, int max_blocks = 0);
 void launch_pos32(const Geom &g, Slots s, cudaStream_t st, const int *only_if_overflow = nullptr);
 void launch_bin_atoms(const Geom &g, const double *dcenter, Slots s, int n, const double *xyz,
                       const double *pxyz, const int *ids, const int *types, const double *masses,

@@ -1025,10 +1025,8 @@ __global__ void zc_upload_kernel(HostSlots hs, Slots s, int nboxes, bool forces)
   }
 }
 
-__global__ void zc_download_kernel(HostSlots hs, Slots s, int nboxes, bool state, bool forces) {
-  int lane;
-  const int b = zc_box(nboxes, lane);
-  if (b < 0) return;
+__device__ __forceinline__ void zc_download_box(const HostSlots &hs, const Slots &s, int b,
+                                                int lane, bool state, bool forces) {
   const int n = min(max(s.natoms[b], 0), CG_MAXATOMS);
   const long base = (long)b * CG_MAXATOMS;
   if (state) {
@@ -1057,6 +1055,15 @@ __global__ void zc_download_kernel(HostSlots hs, Slots s, int nboxes, bool state
   }
 }
 
+// (a warp per box, grid-stride over the boxes: a small grid runs beside
+// other kernels)
+__global__ void zc_download_kernel(HostSlots hs, Slots s, int nboxes, bool state, bool forces) {
+  const int lane = threadIdx.x & 31;
+  const long w0 = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long nw = ((long)gridDim.x * blockDim.x) >> 5;
+  for (long bb = w0; bb < nboxes; bb += nw) zc_download_box(hs, s, (int)bb, lane, state, forces);
+}
+
 static unsigned zc_blocks(int nboxes) {
   return (unsigned)(((long)nboxes * 32 + 255) / 256);  // one warp per box
 }
@@ -1066,9 +1073,10 @@ void launch_zc_upload(const HostSlots &hs, Slots s, int nboxes, bool forces, cud
 }
 
 void launch_zc_download(const HostSlots &hs, Slots s, int nboxes, bool state, bool forces,
-                        cudaStream_t st) {
-  if (nboxes > 0)
-    zc_download_kernel<<<zc_blocks(nboxes), 256, 0, st>>>(hs, s, nboxes, state, forces);
+                        cudaStream_t st, int max_blocks) {
+  unsigned nb = zc_blocks(nboxes);
+  if (max_blocks > 0 && nb > (unsigned)max_blocks) nb = (unsigned)max_blocks;
+  if (nboxes > 0) zc_download_kernel<<<nb, 256, 0, st>>>(hs, s, nboxes, state, forces);
 }
 
 void launch_unpack3(const double *src3, d4 *dst, long n, cudaStream_t st) {

@@ -45,6 +45,7 @@ using cg::d4;
 
 struct comdgb_sim {
   int device = 0;
+  int sms = 0;  // streaming multiprocessors of the device
   comdgb_opts opts{};
   bool mixed = false;
   cudaStream_t stream = nullptr;
@@ -132,6 +133,8 @@ struct comdgb_sim {
   // the force call that ends a merged mixed-precision sequence: the closing
   // part has already written the FP32 copies and the force-order tracking
   cudaGraphExec_t force_exec_tracked = nullptr;
+  // the same writing f, rho and F' straight into the attached host arrays
+  cudaGraphExec_t force_exec_host = nullptr;
   double graph_dt = NAN;
   // n steps captured as one graph (comdgb_sim_graph_steps)
   cudaGraphExec_t loop_exec = nullptr;
