@@ -1,6 +1,6 @@
 """ctypes bindings of libcomdgb.so (the C ABI declared in include/comdgb.h).
 
-Python is only the driver here: every computation runs in the library's
+Python only calls the library here: every computation runs in the library's
 CUDA kernels.  Loading fails loudly if the library is missing; there is no
 CPU fallback.
 """
