@@ -248,11 +248,13 @@ def cpu_sample(procs, cells, steps, w, prefer_reference):
     wall = max(r[1] for r in res)
     kind = res[0][2]
     value = sum(r[0] for r in res) * (steps + 1) / wall
+    # one core: the median process's own rate (the reference is serial)
+    one_core = statistics.median(r[0] * (steps + 1) / r[1] for r in res)
     desc = (f"{procs} concurrent processes, each an independent periodic sample of {natoms} "
             f"atoms ({cells}^3 FCC cells, stretch {w['defgrad']}, box factor {w['bf']}, "
             f"{w['temp_k']} K momenta), nTimeSteps({steps}) of EAM Chebyshev FP64; "
             f"slowest sample {wall:.1f} s")
-    return value, kind, desc
+    return value, kind, desc, one_core
 
 
 def cpu_threads():
@@ -274,11 +276,12 @@ def reference_arm(args):
         cells = max(8, int(CPU_CELLS * (60.0 / total_steps) ** (1 / 3)))
     for _ in range(args.warmup):
         cpu_sample(threads, cells, 1, w, True)
-    vals = []
+    vals, ones = [], []
     kind = desc = None
     for _ in range(args.steps):
-        v, kind, desc = cpu_sample(threads, cells, 1, w, True)
+        v, kind, desc, one = cpu_sample(threads, cells, 1, w, True)
         vals.append(v)
+        ones.append(one)
     value = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -287,7 +290,8 @@ def reference_arm(args):
             "config": {"workload": w["name"], "atoms": 4_000_000, "potential": "EAM Cu Chebyshev",
                        "sample": desc},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                             "sample": desc, "counting": CPU_COUNTING},
+                             "sample": desc, "counting": CPU_COUNTING,
+                             "one_core": {"value": statistics.median(ones), "unit": UNIT}},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -513,9 +517,11 @@ def gpu_arm(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        v, kind, desc = cpu_sample(cpu_threads(), args.cpu_cells, 1, w, True)
+        v, kind, desc, one = cpu_sample(cpu_threads(), args.cpu_cells, 1, w, True)
         cpu = {"value": v, "unit": UNIT, "cores": cpu_threads(), "kind": kind, "sample": desc,
-               "counting": CPU_COUNTING}
+               "counting": CPU_COUNTING,
+               # the serial reference on one core (the median process's own rate)
+               "one_core": {"value": one, "unit": UNIT}}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
