@@ -247,7 +247,7 @@ void fill_cheb(Cheb<double> &c64, Cheb<float> &c32, ChebLow32 &lo32,
 // no table: every pair distance lies below s_lo, so the kernels take the
 // series for every pair and never index the (absent) table
 PairSeg no_pair_seg() {
-  return PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0, nullptr, 1.0f, 0, nullptr, nullptr};
+  return PairSeg{nullptr, 3.0e38f, 1.0f, 2.0f, 0, nullptr, 1.0f, 0, nullptr, 1.0f, 3.0e38f, 1.0f, 0, 0};
 }
 
 int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a[6],
@@ -270,7 +270,6 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
     return (q == 0 ? cheb_host(coef[3], a[3], b[3], r) : cheb_host(coef[4], a[4], b[4], r)) / r;
   };
   std::vector<float4> p1((size_t)2 * n);
-  std::vector<double> dc((size_t)6 * n);  // c1, c2, c3 of phi and rho per segment
   for (int q = 0; q < 2; q++) {
     double fmax = 0, gmax = 0, ferr = 0, gerr = 0;
     double f0 = val(q, (double)s_lo), m0 = 0.5 * hs * der(q, (double)s_lo);
@@ -280,9 +279,6 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
       const double c0 = f0, c1 = m0, c2 = 3.0 * (f1 - f0) - 2.0 * m0 - m1,
                    c3 = 2.0 * (f0 - f1) + m0 + m1;
       p1[(size_t)q * n + k] = make_float4((float)c0, (float)c1, (float)c2, (float)c3);
-      dc[(size_t)6 * k + 3 * q] = c1;
-      dc[(size_t)6 * k + 3 * q + 1] = c2;
-      dc[(size_t)6 * k + 3 * q + 2] = c3;
       for (int e = 0; e <= 8; e++) {
         const double t = e / 8.0, s = (double)s_lo + (k + t) * hs;
         const double fv = val(q, s), gv = der(q, s);
@@ -322,20 +318,97 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
     }
     if (!(ferr <= 1e-7 * fmax)) return 0;
   }
-  // the force pass's derivative quadratics: d/dt of each cubic times dscale
-  const size_t off4 = p1.size();
-  const double ds = (double)dscale;
-  for (int k = 0; k < n; k++) {
-    const double *c = &dc[(size_t)6 * k];
-    p1.push_back(make_float4((float)(ds * c[0]), (float)(ds * 2.0 * c[1]), (float)(ds * 3.0 * c[2]),
-                             (float)(ds * c[3])));
+  // the force pass's derivative cubics: n2 segments in two uniform runs (n2a
+  // from s_lo to s2b, the rest from s2b to rc^2), on each D(r)/r of phi and
+  // of rho interpolated at t = 0, 1/3, 2/3, 1 (Newton's forward differences
+  // in x = 3t).  The split is the candidate with the smallest interpolation
+  // error relative to each function's largest magnitude, probed where the
+  // error term t (t - 1/3) (t - 2/3) (t - 1) peaks; the table is then
+  // checked at 9 points per segment to 1e-6 of that magnitude.
+  const int n2 = SEG2_N;
+  const double span = rc * rc - (double)s_lo;
+  struct Split {
+    float inv_a, s_b, inv_b;
+    int na;
+  };
+  auto make_split = [&](double frac, int na) {
+    Split sp;
+    sp.na = na;
+    sp.inv_a = (float)(na / (span * frac));
+    sp.s_b = (float)((double)s_lo + na / (double)sp.inv_a);
+    sp.inv_b = (float)((n2 - na) / (rc * rc - (double)sp.s_b));
+    return sp;
+  };
+  auto seg_of = [&](const Split &sp, int k, double &s0, double &hh) {
+    if (k < sp.na) {
+      hh = 1.0 / (double)sp.inv_a;
+      s0 = (double)s_lo + k * hh;
+    } else {
+      hh = 1.0 / (double)sp.inv_b;
+      s0 = (double)sp.s_b + (k - sp.na) * hh;
+    }
+  };
+  auto dcubic = [&](int q, double s0, double hh, double c[4]) {
+    double g[4];
+    for (int i = 0; i < 4; i++) g[i] = der(q, s0 + (i / 3.0) * hh);
+    const double d1 = g[1] - g[0], d2 = g[2] - 2.0 * g[1] + g[0],
+                 d3 = g[3] - 3.0 * g[2] + 3.0 * g[1] - g[0];
+    c[0] = g[0];
+    c[1] = 3.0 * (d1 - 0.5 * d2 + d3 / 3.0);
+    c[2] = 4.5 * (d2 - d3);
+    c[3] = 4.5 * d3;
+  };
+  auto cubic_at = [](const double c[4], double t) {
+    return ((c[3] * t + c[2]) * t + c[1]) * t + c[0];
+  };
+  double gm[2] = {0.0, 0.0};
+  for (int q = 0; q < 2; q++)
+    for (int i = 0; i <= 4 * n2; i++)
+      gm[q] = std::max(gm[q], fabs(der(q, (double)s_lo + span * i / (4.0 * n2))));
+  if (!(gm[0] > 0.0 && gm[1] > 0.0)) return 0;
+  auto split_err = [&](const Split &sp, const double *ts, int nt) {
+    double e = 0.0;
+    for (int q = 0; q < 2; q++)
+      for (int k = 0; k < n2; k++) {
+        double s0, hh, c[4];
+        seg_of(sp, k, s0, hh);
+        dcubic(q, s0, hh, c);
+        for (int i = 0; i < nt; i++)
+          e = std::max(e, fabs(cubic_at(c, ts[i]) - der(q, s0 + ts[i] * hh)) / gm[q]);
+      }
+    return e;
+  };
+  const double probe[3] = {0.12, 0.5, 0.88};
+  Split best = make_split(0.5, n2 / 2);
+  if (COMDGB_SEG2_RUNS == 1) {  // one run: the kernel ignores the split
+    best.inv_b = best.inv_a;
+    best.s_b = 3.0e38f;
+    best.na = n2;
   }
-  const size_t off2 = p1.size();  // then n float2, two per float4
-  for (int k = 0; k < n; k += 2) {
-    const double *c = &dc[(size_t)6 * k];
-    const double *e = &dc[(size_t)6 * (k + 1)];
-    p1.push_back(make_float4((float)(ds * 2.0 * c[4]), (float)(ds * 3.0 * c[5]),
-                             (float)(ds * 2.0 * e[4]), (float)(ds * 3.0 * e[5])));
+  double best_err = split_err(best, probe, 3);
+  if (COMDGB_SEG2_RUNS > 1)
+    for (double frac : {0.1, 0.15, 0.2, 0.25, 0.3, 0.35, 0.4})
+      for (int j = 2; j <= 7; j++) {
+        const Split sp = make_split(frac, n2 * j / 8);
+        const double e = split_err(sp, probe, 3);
+        if (e < best_err) {
+          best_err = e;
+          best = sp;
+        }
+      }
+  const size_t off2 = p1.size();
+  p1.resize(off2 + 2 * (size_t)n2);
+  for (int q = 0; q < 2; q++) {
+    double gerr = 0;
+    for (int k = 0; k < n2; k++) {
+      double s0, hh, c[4];
+      seg_of(best, k, s0, hh);
+      dcubic(q, s0, hh, c);
+      p1[off2 + 2 * (size_t)k + q] = make_float4((float)c[0], (float)c[1], (float)c[2], (float)c[3]);
+      for (int e = 0; e <= 8; e++)
+        gerr = std::max(gerr, fabs(cubic_at(c, e / 8.0) - der(q, s0 + (e / 8.0) * hh)));
+    }
+    if (!(gerr <= 1e-6 * gm[q])) return 0;
   }
   int err = 0;
   float4 *d1 = h->seg_buf ? h->seg_buf : track(h, dalloc<float4>(p1.size(), &err));
@@ -344,8 +417,8 @@ int build_pair_seg(comdgb_sim *h, const double coef[6][CG_NCHEB], const double a
   if (cudaMemcpy(d1, p1.data(), sizeof(float4) * p1.size(), cudaMemcpyHostToDevice) !=
       cudaSuccess)
     return -1;
-  *out = PairSeg{d1, s_lo, inv_h, dscale, n, d1 + 2 * (size_t)n, inv_h1, n1, d1 + off4,
-                 reinterpret_cast<const float2 *>(d1 + off2)};
+  *out = PairSeg{d1, s_lo, inv_h, dscale, n, d1 + 2 * (size_t)n, inv_h1, n1,
+                 d1 + off2, best.inv_a, best.s_b, best.inv_b, best.na, n2};
   return 0;
 }
 

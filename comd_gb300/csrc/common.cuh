@@ -327,8 +327,9 @@ struct ChebLow32 {
 // = dscale * dphi/dt with dscale = 2 * inv_h, and likewise rho'(r)/r.
 // s < s_lo (and n == 0: no table) takes the series instead.
 // The force-order density pass reads rho alone, no derivative: it has its
-// own rho table of SEG1_N segments over the same range (rho1, inv_h1: a
-// fourth of the shared memory, so the pass keeps more of the L1 cache).
+// own rho table of SEG1_N segments over the same range (rho1, inv_h1; the
+// cubic's error at 512 segments is 4e-9 of rho's maximum, at 256 segments
+// 6e-8, FP32's own rounding).
 #ifndef COMDGB_SEG_N
 #define COMDGB_SEG_N 2048
 #endif
@@ -338,6 +339,53 @@ struct ChebLow32 {
 constexpr int SEG_N = COMDGB_SEG_N;    // segments of the table
 constexpr int SEG1_N = COMDGB_SEG1_N;  // segments of the density pass's rho table
 static_assert(SEG_N % 2 == 0, "the float2 derivative records pair up into float4");
+// The density pass keeps RHO_COPIES copies of its rho table in shared
+// memory, interleaved record by record (segment k of copy c at k *
+// RHO_COPIES + c), and lane l reads copy l % RHO_COPIES.  A warp's 16-byte
+// shared loads are served a quarter-warp (8 lanes, 128 bytes, all 32 banks)
+// at a time; with 8 copies the 8 lanes of a quarter read 8 different
+// 16-byte bank groups whatever segments they look up, so the lookup takes
+// its minimum of 4 wavefronts instead of about 10 for random segments of
+// one copy.  The price is shared memory taken from the L1 cache: 64 KB a
+// CTA at 8 copies.  (At 4M atoms, EAM Cu: 0.588 ms a pass with 8 copies,
+// 0.610 with 4, 0.614 with 2, 0.625 with one.)
+#ifndef COMDGB_RHO_COPIES
+#define COMDGB_RHO_COPIES 8
+#endif
+constexpr int RHO_COPIES = COMDGB_RHO_COPIES;
+static_assert(RHO_COPIES == 1 || RHO_COPIES == 2 || RHO_COPIES == 4 || RHO_COPIES == 8,
+              "copies of the rho table: 1, 2, 4 or 8");
+// The force-order force pass reads the derivatives alone (and phi when it
+// sums energies): SEG2_N segments over the same range in two uniform runs,
+// n2a of width 1/inv_h2 from s_lo to s2b and the rest of width 1/inv_h2b
+// from s2b to rc^2 (u = (s - s_lo) inv_h2, or n2a + (s - s2b) inv_h2b past
+// n2a).  On segment k phi'(r)/r = dcub[2k] and rho'(r)/r = dcub[2k + 1] as
+// cubics in t = u - k, each interpolating the reference's derivative
+// series D(r)/r at t = 0, 1/3, 2/3 and 1, rounded once from FP64.  The
+// interpolation error falls off steeply with r (for EAM Cu at 256 uniform
+// segments, 1.3e-7 of the largest magnitude at 2.0 A, 5e-9 at 2.5 A, below
+// 2e-10 past 3 A; FP32 rounding alone gives 6e-8).  By default the table
+// is one uniform run (n2a = n2); COMDGB_SEG2_RUNS=2 makes the first run
+// finer, with s2b and n2a picked by the host for the smallest error (EAM
+// Cu: 3.4e-9 everywhere), at one compare and one FMA more per pair (2.7 %
+// of the force pass).  Its shared memory holds FORCE_COPIES
+// interleaved copies, as the density pass's rho table: record (2k + h) *
+// FORCE_COPIES + c is cubic h of segment k in copy c, so a pair's two
+// lookups take 4 wavefronts each.
+#ifndef COMDGB_SEG2_N
+#define COMDGB_SEG2_N 256
+#endif
+#ifndef COMDGB_FORCE_COPIES
+#define COMDGB_FORCE_COPIES 8
+#endif
+#ifndef COMDGB_SEG2_RUNS  // 1: one uniform run, 2: a finer first run
+#define COMDGB_SEG2_RUNS 1
+#endif
+static_assert(COMDGB_SEG2_RUNS == 1 || COMDGB_SEG2_RUNS == 2, "one or two runs of segments");
+constexpr int SEG2_N = COMDGB_SEG2_N;
+constexpr int FORCE_COPIES = COMDGB_FORCE_COPIES;
+static_assert(FORCE_COPIES == 1 || FORCE_COPIES == 2 || FORCE_COPIES == 4 || FORCE_COPIES == 8,
+              "copies of the force pass's table: 1, 2, 4 or 8");
 struct PairSeg {
   const float4 *p1;
   float s_lo, inv_h, dscale;
@@ -345,11 +393,9 @@ struct PairSeg {
   const float4 *rho1;  // [n1] rho cubics for the density pass
   float inv_h1;
   int n1;
-  // the force-order force pass reads derivatives: on segment k, phi'(r)/r =
-  // d4.x + d4.y t + d4.z t^2 and rho'(r)/r = d4.w + d2.x t + d2.y t^2, the
-  // derivatives of the cubics above scaled by dscale, rounded once from FP64
-  const float4 *d4;  // [n]
-  const float2 *d2;  // [n]
+  const float4 *dcub;  // [2 * n2] phi'(r)/r and rho'(r)/r cubics for the force pass
+  float inv_h2, s2b, inv_h2b;
+  int n2a, n2;
 };
 
 __device__ __forceinline__ float seg_cubic(float4 c, float t) {

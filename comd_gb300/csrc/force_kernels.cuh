@@ -796,6 +796,14 @@ __device__ __forceinline__ void stage_seg(float4 *sm, const float4 *src, int nre
   __syncthreads();
 }
 
+// the density pass's rho table (nrec cubics from src) as RHO_COPIES
+// interleaved copies: record q of the shared array is segment q / RHO_COPIES
+__device__ __forceinline__ void stage_rho_copies(float4 *sm, const float4 *src, int nrec) {
+  for (int q = threadIdx.x; q < nrec * RHO_COPIES; q += blockDim.x)
+    sm[q] = __ldg(src + q / RHO_COPIES);
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // EAM pass 1: density, pair energy and pair force of one atom.  `visit`
 // runs the atom's neighbour traversal with a pair functor.
@@ -1093,14 +1101,15 @@ __device__ __forceinline__ bool fo_rho(const EamPot<float, EVAL> &P, const float
   }
   return true;
 }
-// (sm: the density pass's rho table, n1 segments; the same lower end s_lo,
-// so "below the table" is below_seg's test)
+// (sm: this lane's copy of the density pass's rho table, n1 segments
+// RHO_COPIES records apart; the same lower end s_lo, so "below the table"
+// is below_seg's test)
 static __device__ __forceinline__ bool fo_rho(const EamPot<float, EVAL_CHEBY> &P,
                                               const float4 *sm, float r2, float &rho) {
   const float u = (r2 - P.seg.s_lo) * P.seg.inv_h1;
   if (!(u >= 0.f)) return false;
   const int k = min((int)u, P.seg.n1 - 1);
-  rho = seg_cubic(sm[k], u - (float)k);
+  rho = seg_cubic(sm[k * RHO_COPIES], u - (float)k);
   return true;
 }
 template <int EVAL>
@@ -1114,11 +1123,13 @@ static __device__ __noinline__ float fo_rho_series(const EamPot<float, EVAL_CHEB
 }
 
 // phi (OBS only), phi'(r)/r and rho'(r)/r of one pair distance: the force
-// pass's tables (sm, staged by stage_force_table), or the table evaluator.
+// pass's tables (staged by stage_force_table: sm this lane's copy of the
+// derivative cubics, phi_sm the phi cubics), or the table evaluator.
 // false: below the pair table
 template <bool OBS, int EVAL>
-__device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL> &P, const float4 *, float r2,
-                                        float &phi, float &wphi, float &wrho) {
+__device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL> &P, const float4 *,
+                                        const float4 *, float r2, float &phi, float &wphi,
+                                        float &wrho) {
   float r, inv_r, dphi, v, drho;
   r_and_inv(r2, r, inv_r);
   if (EVAL == EVAL_CHEBY) {
@@ -1133,35 +1144,38 @@ __device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL> &P, const floa
   wrho = drho * inv_r;
   return true;
 }
-// (the derivative quadratics: one 16-byte and one 8-byte shared load per
-// pair, the phi cubic a third only when the energy is summed)
+// (two conflict-free 16-byte shared loads per pair, the phi cubic a third
+// only when the energy is summed)
 template <bool OBS>
 static __device__ __forceinline__ bool fo_pair(const EamPot<float, EVAL_CHEBY> &P,
-                                               const float4 *sm, float r2, float &phi,
-                                               float &wphi, float &wrho) {
-  const float u = (r2 - P.seg.s_lo) * P.seg.inv_h;
+                                               const float4 *sm, const float4 *phi_sm, float r2,
+                                               float &phi, float &wphi, float &wrho) {
+  const float d = r2 - P.seg.s_lo;
+  float u = d * P.seg.inv_h2;
   if (!(u >= 0.f)) return false;
-  const int n = P.seg.n;
-  const int k = min((int)u, n - 1);
+  if (COMDGB_SEG2_RUNS > 1 && u >= (float)P.seg.n2a)
+    u = fmaf(r2 - P.seg.s2b, P.seg.inv_h2b, (float)P.seg.n2a);
+  const int k = min((int)u, P.seg.n2 - 1);
   const float t = u - (float)k;
-  const float4 d = sm[k];
-  const float2 e = reinterpret_cast<const float2 *>(sm + n)[k];
-  wphi = fmaf(fmaf(d.z, t, d.y), t, d.x);
-  wrho = fmaf(fmaf(e.y, t, e.x), t, d.w);
-  if (OBS) phi = seg_cubic(sm[n + n / 2 + k], t);
+  wphi = seg_cubic(sm[(2 * k) * FORCE_COPIES], t);
+  wrho = seg_cubic(sm[(2 * k + 1) * FORCE_COPIES], t);
+  if (OBS) {
+    const float u1 = d * P.seg.inv_h;
+    const int k1 = min((int)u1, P.seg.n - 1);
+    phi = seg_cubic(phi_sm[k1], u1 - (float)k1);
+  }
   return true;
 }
 
-// the force pass's tables into shared memory, once per CTA: the derivative
-// quadratics (n float4, then n float2), and with OBS the phi cubics
+// the force pass's tables into shared memory, once per CTA: FORCE_COPIES
+// interleaved copies of the derivative cubics (2 n2 records each), then
+// with OBS the phi cubics (n records)
 template <bool OBS>
 __device__ __forceinline__ void stage_force_table(float4 *sm, const PairSeg &S) {
-  const int n = S.n;
-  const float4 *d2 = reinterpret_cast<const float4 *>(S.d2);
-  for (int q = threadIdx.x; q < n; q += blockDim.x) sm[q] = __ldg(S.d4 + q);
-  for (int q = threadIdx.x; q < n / 2; q += blockDim.x) sm[n + q] = __ldg(d2 + q);
+  const int m = 2 * S.n2 * FORCE_COPIES;
+  for (int q = threadIdx.x; q < m; q += blockDim.x) sm[q] = __ldg(S.dcub + q / FORCE_COPIES);
   if (OBS)
-    for (int q = threadIdx.x; q < n; q += blockDim.x) sm[n + n / 2 + q] = __ldg(S.p1 + q);
+    for (int q = threadIdx.x; q < S.n; q += blockDim.x) sm[m + q] = __ldg(S.p1 + q);
   __syncthreads();
 }
 // the series for a pair below the table (FP32 Chebyshev only)
@@ -1215,7 +1229,8 @@ template <int EVAL, bool MULTI, bool OBS>
 __global__ void FO1_BOUNDS
     fo_eam_pass1_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
-  if (uses_seg(P)) stage_seg(seg_sm, P.seg.rho1, P.seg.n1);  // the density pass's rho cubics
+  if (uses_seg(P)) stage_rho_copies(seg_sm, P.seg.rho1, P.seg.n1);  // the rho cubics
+  const float4 *rho_sm = seg_sm + (threadIdx.x & (RHO_COPIES - 1));  // this lane's copy
   const float rc2 = P.rc2;
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
     const int slot = A.fo.slot[a];
@@ -1230,7 +1245,7 @@ __global__ void FO1_BOUNDS
                                  if (r2 > rc2) return;
                                  cnt++;
                                  float rho;
-                                 if (!fo_rho(P, seg_sm, r2, rho)) rho = fo_rho_series(P, r2);
+                                 if (!fo_rho(P, rho_sm, r2, rho)) rho = fo_rho_series(P, r2);
                                  rh.add(rho);
                                });
       fo_density_store<EVAL, OBS>(A, P, rh, a, slot, pi, cnt, A.fo.vcap + 1);
@@ -1252,7 +1267,7 @@ __global__ void FO1_BOUNDS
       if (COMDGB_FO_CUT) cut[(size_t)cnt * 32] = p;
       cnt++;
       float rho;
-      if (fo_rho(P, seg_sm, r2, rho)) rh.add(rho);
+      if (fo_rho(P, rho_sm, r2, rho)) rh.add(rho);
       else low = true;
     }
     if (low)  // pairs below the table: the series, in a second sweep
@@ -1346,6 +1361,8 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
     fo_eam_pass2_kernel(ForceArgs A, const __grid_constant__ EamPot<float, EVAL> P) {
   extern __shared__ float4 seg_sm[];
   if (uses_seg(P)) stage_force_table<OBS>(seg_sm, P.seg);
+  const float4 *dcub_sm = seg_sm + (threadIdx.x & (FORCE_COPIES - 1));  // this lane's copy
+  const float4 *phi_sm = seg_sm + 2 * SEG2_N * FORCE_COPIES;
   const float rc2 = P.rc2;
   const bool fuse = !OBS && *(volatile const int *)(A.status + ST_FUSE);
   for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.ntot; a += gridDim.x * blockDim.x) {
@@ -1363,7 +1380,7 @@ __global__ void __maxnreg__(OBS ? COMDGB_FO2_MAXNREG : COMDGB_FO2F_MAXNREG)
     walk([&](float fj, float dx, float dy, float dz, float r2) {
       if (r2 > rc2) return;
       float phi, wphi, wrho;
-      if (!fo_pair<OBS>(P, seg_sm, r2, phi, wphi, wrho)) {
+      if (!fo_pair<OBS>(P, dcub_sm, phi_sm, r2, phi, wphi, wrho)) {
         low = true;
         return;
       }

@@ -33,13 +33,13 @@ static size_t pass_smem(int pass, int eval) {
   return sizeof(float4) * (pass == 0 ? 2 : 1) * SEG_N;
 }
 
-// force order: the density pass stages its rho table (SEG1_N cubics), the
-// force pass the derivative quadratics (SEG_N float4 + SEG_N float2) and,
-// summing energies (obs), the phi cubics
+// force order: the density pass stages its rho table (SEG1_N cubics, in
+// RHO_COPIES copies), the force pass its derivative cubics (2 SEG2_N, in
+// FORCE_COPIES copies) and, summing energies (obs), the phi cubics (SEG_N)
 static size_t fo_pass_smem(int pass, int eval, bool obs = true) {
   if (sizeof(FT) != 4 || eval != EVAL_CHEBY) return 0;
-  if (pass == 0) return sizeof(float4) * SEG1_N;
-  return sizeof(float4) * (SEG_N + SEG_N / 2 + (obs ? SEG_N : 0));
+  if (pass == 0) return sizeof(float4) * SEG1_N * RHO_COPIES;
+  return sizeof(float4) * (2 * SEG2_N * FORCE_COPIES + (obs ? SEG_N : 0));
 }
 
 #if COMDGB_FT_FLOAT
