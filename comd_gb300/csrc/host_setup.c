@@ -54,7 +54,13 @@ static potentialarray_t *read_table(const char *path) {
            read_be_or_le(fp, &xn, 8, swap) && read_be_or_le(fp, &invdx, 8, swap) &&
            read_be_or_le(fp, &iflo, 4, swap) && read_be_or_le(fp, &ifhi, 4, swap) &&
            read_be_or_le(fp, &rec, 4, swap) && read_be_or_le(fp, &rec, 4, swap);
-  if (!ok || n <= 0 || rec != n * 8) { fclose(fp); return NULL; }
+  /* a table the interpolation can index: n points on x0 < xn with a finite,
+   * positive 1/dx (the reference reads these fields unchecked) */
+  if (!ok || n <= 0 || n > (1 << 26) || rec != n * 8 || !isfinite(x0) || !isfinite(xn) ||
+      !(xn > x0) || !isfinite(invdx) || !(invdx > 0.0)) {
+    fclose(fp);
+    return NULL;
+  }
   potentialarray_t *a = (potentialarray_t *)zalloc(sizeof *a);
   double *buf = (double *)zalloc((size_t)(n + 3) * sizeof(double));
   if (!a || !buf) { free(a); free(buf); fclose(fp); return NULL; }
@@ -181,7 +187,10 @@ static int alloc_domains(simflat_t *s) {
 }
 
 /* putAtomInBox (domains.c:237-291) for one atom at world position x with
- * momenta p (NULL: zero) */
+ * momenta p (NULL: zero).  A coordinate that is not in [0, bounds) after
+ * one wrap -- more than a period outside, NaN or infinite -- is
+ * COMDGB_ERR_BOXRANGE, as in the device binning (binning.cuh): the
+ * conversion of floor(NaN) to int differs between hosts. */
 static int put_atom(simflat_t *s, int id, int itype, double mass, const double *x,
                     const double *p) {
   double w[3];
@@ -190,6 +199,7 @@ static int put_atom(simflat_t *s, int id, int itype, double mass, const double *
     w[m] = x[m];
     if (w[m] < 0.0) w[m] += s->bounds[m];
     else if (w[m] >= s->bounds[m]) w[m] -= s->bounds[m];
+    if (!(w[m] >= 0.0 && w[m] < s->bounds[m])) return COMDGB_ERR_BOXRANGE;
     ib[m] = (int)floor(w[m] / s->boxsize[m]);
     if (ib[m] < 0 || ib[m] >= s->nbx[m]) return COMDGB_ERR_BOXRANGE;
   }
@@ -475,6 +485,12 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
     st = COMDGB_ERR_IO;
     goto done;
   }
+  /* every atom line holds seven numbers: a count the rest of the file
+   * cannot hold is an I/O error before anything is allocated for it */
+  if ((size_t)natoms > strlen(cur) / 2 + 1) {
+    st = COMDGB_ERR_IO;
+    goto done;
+  }
   if ((st = alloc_domains(s))) goto done;
   size_t n = (size_t)natoms;
   xyz = (double *)malloc(3 * n * sizeof(double) + 8);
@@ -560,6 +576,11 @@ simflat_t *comdgb_read_tim(const char *path, pmd_base_potential_t *pot, double b
   }
   if (fseek(fp, 0, SEEK_END) == 0) n = ftell(fp) / (long)(5 * sizeof(float));
   rewind(fp);
+  if (n > 0x7fffffffL) {  /* atom ids and counts are int */
+    fclose(fp);
+    st = COMDGB_ERR_ARG;
+    goto done;
+  }
   rec = (float *)malloc((size_t)n * 5 * sizeof(float) + 4);
   if (!rec || fread(rec, 5 * sizeof(float), (size_t)n, fp) != (size_t)n) {
     fclose(fp);

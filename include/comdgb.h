@@ -184,7 +184,7 @@ int comdgb_sim_graph_kernels(comdgb_sim *h, int *per_step, int *per_force);
  * (0 keeps the default): the skin-list build's threads per box -- the
  * threads per cell -- (64, 128 or 256; default 128) and atoms tested per
  * candidate load (2, 4 or 8; default 4), and pass 2's threads per CTA (128,
- * 256 or 512; default 256).  Results do not depend on them (the lists and
+ * 256 or 512; default 512).  Results do not depend on them (the lists and
  * every per-atom sum keep their order); the graphs are recaptured. */
 int comdgb_sim_set_launch(comdgb_sim *h, int build_threads, int build_atoms, int pass2_threads);
 /* Mixed precision only (its default): a sequence of steps reboxes once per

@@ -146,3 +146,86 @@ def test_round_f32_matches_ieee_nearest_even():
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     nan = cg.round_f32(np.array([np.nan]))
     assert np.isnan(nan[0])
+
+
+def _write_table(path, n, x0, xn, invdx, rec=None, values=None, big_endian=True):
+    """a table file in the reference's Fortran-record layout (eam.c:156-249)"""
+    import struct
+    e = ">" if big_endian else "<"
+    vals = np.linspace(1.0, 0.0, n) if values is None else values
+    with open(path, "wb") as f:
+        f.write(struct.pack(e + "i", 36))
+        f.write(struct.pack(e + "idddii", n, x0, xn, invdx, 1, 0))
+        f.write(struct.pack(e + "ii", 36, 8 * n if rec is None else rec))
+        f.write(struct.pack(e + "%dd" % len(vals), *vals))
+        f.write(struct.pack(e + "i", 8 * n))
+
+
+@pytest.mark.parametrize("case", ["good", "good_le", "truncated", "zero_n", "bad_record",
+                                  "nan_x0", "empty_range", "zero_invdx", "inf_invdx"])
+def test_eam_read_rejects_malformed_tables(tmp_path, case):
+    """comdgb_eam_read loads a table only when the interpolation can index it:
+    n > 0 values, x0 < xn finite, 1/dx finite and positive, a data record of
+    8n bytes; a short file is rejected too.  Either byte order is read."""
+    import shutil
+    for ext in ("rho", "f", "doc"):
+        shutil.copy(os.path.join(cg.POT_DIR, "cu." + ext), tmp_path / ("t." + ext))
+    n, x0, xn = 3000, 1.0, 4.961
+    invdx = n / (xn - x0)
+    args = {"good": (n, x0, xn, invdx), "good_le": (n, x0, xn, invdx),
+            "truncated": (n, x0, xn, invdx), "zero_n": (0, x0, xn, invdx),
+            "bad_record": (n, x0, xn, invdx), "nan_x0": (n, float("nan"), xn, invdx),
+            "empty_range": (n, xn, xn, invdx), "zero_invdx": (n, x0, xn, 0.0),
+            "inf_invdx": (n, x0, xn, float("inf"))}[case]
+    phi = str(tmp_path / "t.phi")
+    _write_table(phi, *args, rec=8 * n + 8 if case == "bad_record" else None,
+                 values=np.linspace(1.0, 0.0, 0 if case == "zero_n" else n),
+                 big_endian=case != "good_le")
+    if case == "truncated":
+        with open(phi, "r+b") as f:
+            f.truncate(48 + 8 * 100)
+    L = cg.load()
+    p = L.comdgb_eam_read(str(tmp_path).encode(), b"t")
+    if case.startswith("good"):
+        assert p, case
+        a = p.contents.phi.contents
+        assert (a.n, a.xn, a.invDx) == (n, xn, invdx)
+        L.comdgb_eam_free(p)
+    else:
+        assert not p, case
+
+
+def test_host_binning_rejects_non_finite_and_far_coordinates(tmp_path):
+    """Host binning (comdgb_read_clsman with device < 0, the path of
+    putAtomInBox on the host) gives COMDGB_ERR_BOXRANGE for a NaN or
+    infinite coordinate and for an atom more than one period outside, on
+    every host (the int conversion of floor(NaN) is host-dependent), as the
+    device binning does; an atom less than one period outside is wrapped."""
+    pot = cg.eam_potential("cu")
+
+    def clsman(x):
+        p = tmp_path / "one.inp"
+        p.write_text("2 0\ncomment\n21.69 21.69 21.69\n"
+                     "1.0 1.0 1.0 0 0.0 0.0 0.0\n%s 2.0 2.0 0 0.0 0.0 0.0\n" % x)
+        return str(p)
+
+    s = cg.read_clsman(clsman("-1.5"), pot, 1.0, -1)  # wrapped into the period
+    try:
+        assert s.contents.ntot == 2
+    finally:
+        cg.free_host(s)
+    for bad in ("nan", "inf", "-inf", "-30.0", "50.0"):
+        with pytest.raises(cg.ComdgbError) as ei:
+            cg.read_clsman(clsman(bad), pot, 1.0, -1)
+        assert ei.value.code == -12, bad  # COMDGB_ERR_BOXRANGE
+
+
+def test_clsman_count_beyond_the_file_is_an_io_error(tmp_path):
+    """an atom count that the file cannot hold fails before any allocation
+    for it (no multi-gigabyte request from a corrupt header)"""
+    pot = cg.eam_potential("cu")
+    p = tmp_path / "huge.inp"
+    p.write_text("2000000000 0\ncomment\n21.69 21.69 21.69\n1.0 1.0 1.0 0 0.0 0.0 0.0\n")
+    with pytest.raises(cg.ComdgbError) as ei:
+        cg.read_clsman(str(p), pot, 1.0, -1)
+    assert ei.value.code == -33  # COMDGB_ERR_IO
