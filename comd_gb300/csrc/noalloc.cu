@@ -153,14 +153,15 @@ extern "C" int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3]
     g.nbx[j] = nbx[j];
     g.bounds[j] = bounds[j];
     g.boxsize[j] = boxsize[j];
-    nboxes *= nbx[j];
-  }
-  if (nboxes > COMDGB_NOALLOC_MAX_BOXES) {
-    char m[200];
-    snprintf(m, sizeof m,
-             "comdgb_put_atoms_noalloc: %ld boxes exceed the allocation-free limit of %d boxes",
-             nboxes, COMDGB_NOALLOC_MAX_BOXES);
-    return fail(COMDGB_ERR_ARG, m);
+    nboxes *= nbx[j];  // checked after every factor: at most 16,384 * (2^31 - 1)
+    if (nboxes > COMDGB_NOALLOC_MAX_BOXES) {
+      char m[240];
+      snprintf(m, sizeof m,
+               "comdgb_put_atoms_noalloc: a grid of %d x %d x %d boxes exceeds the "
+               "allocation-free limit of %d boxes",
+               nbx[0], nbx[1], nbx[2], COMDGB_NOALLOC_MAX_BOXES);
+      return fail(COMDGB_ERR_ARG, m);
+    }
   }
   g.nboxes = (int)nboxes;
   int prev = 0;

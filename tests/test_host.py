@@ -229,3 +229,19 @@ def test_clsman_count_beyond_the_file_is_an_io_error(tmp_path):
     with pytest.raises(cg.ComdgbError) as ei:
         cg.read_clsman(str(p), pot, 1.0, -1)
     assert ei.value.code == -33  # COMDGB_ERR_IO
+
+
+@pytest.mark.parametrize("nbx", [(64, 64, 8), (2**31 - 1,) * 3, (128, 128, 2**31 - 1)])
+def test_noalloc_binning_rejects_grids_beyond_its_scratch_without_a_gpu(nbx):
+    """comdgb_put_atoms_noalloc checks the grid against its fixed scratch
+    (16,384 boxes) before any CUDA call, with no integer overflow for the
+    largest int extents"""
+    L = cg.load()
+    n3 = (C.c_int * 3)(*nbx)
+    bounds = (C.c_double * 3)(100.0, 100.0, 100.0)
+    bs = (C.c_double * 3)(*(100.0 / k for k in nbx))
+    dummy = C.c_void_p(1)
+    rc = L.comdgb_put_atoms_noalloc(n3, bounds, bs, dummy, 0, None, None, None, None, None,
+                                    dummy, dummy, dummy, dummy, dummy, dummy, 0, None)
+    assert rc == -1  # COMDGB_ERR_ARG
+    assert "allocation-free limit" in cg.lib.last_error()
