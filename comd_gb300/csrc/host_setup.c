@@ -157,13 +157,21 @@ void comdgb_sim_free_host(simflat_t *s) {
 static int alloc_domains(simflat_t *s) {
   double strain[3] = {s->defgrad == 0.0 ? 1.0 : s->defgrad, 1.0, 1.0};
   double bf = s->bf == 0.0 ? 1.0 : s->bf;
-  s->nboxes = 1;
+  /* slot indexes (box * 64 + k) are int, as in the reference: a grid of
+   * more boxes than that allows (or a non-finite extent) is an argument
+   * error here, where the reference's int conversion would be undefined */
+  const long long max_boxes = 0x7fffffffLL / COMDGB_MAXATOMS;
+  long long nboxes = 1;
   for (int j = 0; j < 3; j++) {
-    s->nbx[j] = (int)floor(s->bounds[j] / (s->pot->cutoff * bf * strain[j]));
-    if (s->nbx[j] < 1) return COMDGB_ERR_NOBOX;
-    s->nboxes *= s->nbx[j];
+    const double q = floor(s->bounds[j] / (s->pot->cutoff * bf * strain[j]));
+    if (q != q || q > (double)max_boxes) return COMDGB_ERR_ARG;
+    if (q < 1.0) return COMDGB_ERR_NOBOX;
+    s->nbx[j] = (int)q;
+    nboxes *= s->nbx[j];
+    if (nboxes > max_boxes) return COMDGB_ERR_ARG;
     s->boxsize[j] = s->bounds[j] / (double)s->nbx[j];
   }
+  s->nboxes = (int)nboxes;
   size_t nb = (size_t)s->nboxes, ns = nb * COMDGB_MAXATOMS;
   s->dcenter = (comdgb_real3 *)zalloc(nb * sizeof(comdgb_real3));
   s->natoms = (int *)zalloc(nb * sizeof(int));

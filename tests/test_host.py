@@ -245,3 +245,20 @@ def test_noalloc_binning_rejects_grids_beyond_its_scratch_without_a_gpu(nbx):
                                     dummy, dummy, dummy, dummy, dummy, dummy, 0, None)
     assert rc == -1  # COMDGB_ERR_ARG
     assert "allocation-free limit" in cg.lib.last_error()
+
+
+def test_grid_beyond_int_slot_indexes_is_an_argument_error():
+    """allocDomains' grid (domains.c:155-200) for a lattice whose slot
+    indexes (box * 64 + k) would not fit an int is refused with
+    COMDGB_ERR_ARG before anything is allocated; a grid below one box per
+    axis keeps the reference's -3"""
+    pot = cg.eam_potential("cu")
+    # 728^3 = 386 M boxes and 72,868^3 (an int product that overflows) against
+    # the 33.5 M boxes whose slot indexes fit an int
+    for n in (1000, 100000):
+        with pytest.raises(cg.ComdgbError) as ei:
+            cg.fcc(n, n, n, 3.615, 1.0, 1.0, pot)
+        assert ei.value.code == -1, n  # COMDGB_ERR_ARG
+    with pytest.raises(cg.ComdgbError) as ei:
+        cg.fcc(1, 1, 1, 3.615, 1.0, 1.0, pot)  # 3.615 A < the 4.961 A cutoff
+    assert ei.value.code == -3  # COMDGB_ERR_NOBOX
