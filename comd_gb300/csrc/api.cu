@@ -1446,8 +1446,16 @@ int create(const simflat_t *const *sims, int nrep, const comdgb_opts *o, comdgb_
     if (!q) return set_err(COMDGB_ERR_ARG, "null replica %d", r);
     if (q->nboxes < 1 || !q->natoms || !q->r)
       return set_err(COMDGB_ERR_ARG, "simflat_t has no allocated domains");
-    for (int j = 0; j < 3; j++)
+    for (int j = 0; j < 3; j++) {
       if (q->nbx[j] > 1023) return set_err(COMDGB_ERR_UNSUPPORTED, "more than 1023 boxes per axis");
+      // the stencils index boxes by nbx, the arrays hold nboxes: they must agree
+      if (q->nbx[j] < 1 || !(q->boxsize[j] > 0.0) || !(q->bounds[j] > 0.0) ||
+          !std::isfinite(q->boxsize[j]) || !std::isfinite(q->bounds[j]))
+        return set_err(COMDGB_ERR_ARG, "replica %d: box grid (nbx, boxsize, bounds) not set", r);
+    }
+    if ((long)q->nbx[0] * q->nbx[1] * q->nbx[2] != q->nboxes)
+      return set_err(COMDGB_ERR_ARG, "replica %d: nboxes %d is not nbx[0]*nbx[1]*nbx[2]", r,
+                     q->nboxes);
     if (r > 0 && q->pot != sims[0]->pot &&
         (!q->pot || !sims[0]->pot || q->pot->cutoff != sims[0]->pot->cutoff))
       return set_err(COMDGB_ERR_ARG, "replica %d has another potential", r);

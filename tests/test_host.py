@@ -262,3 +262,27 @@ def test_grid_beyond_int_slot_indexes_is_an_argument_error():
     with pytest.raises(cg.ComdgbError) as ei:
         cg.fcc(1, 1, 1, 3.615, 1.0, 1.0, pot)  # 3.615 A < the 4.961 A cutoff
     assert ei.value.code == -3  # COMDGB_ERR_NOBOX
+
+
+def test_create_checks_the_box_grid_before_any_cuda_call():
+    """comdgb_sim_create / comdgb_attach refuse a simflat_t whose nboxes is not
+    nbx[0]*nbx[1]*nbx[2], or whose box sizes are unset, with COMDGB_ERR_ARG
+    (before touching the GPU; the stencil kernels index boxes by nbx)"""
+    L = cg.load()
+    pot = cg.eam_potential("cu")
+    s = cg.fcc(6, 6, 6, 3.615, 1.0, 1.0, pot)
+    o = cg.opts()
+    h = C.c_void_p()
+    try:
+        nb = s.contents.nboxes
+        s.contents.nboxes = nb + 1
+        assert L.comdgb_sim_create(s, C.byref(o), C.byref(h)) == -1
+        assert "nboxes" in cg.lib.last_error()
+        assert L.comdgb_attach(s, C.byref(o)) == -1
+        s.contents.nboxes = nb
+        bs = s.contents.boxsize[1]
+        s.contents.boxsize[1] = float("nan")
+        assert L.comdgb_sim_create(s, C.byref(o), C.byref(h)) == -1
+        s.contents.boxsize[1] = bs
+    finally:
+        cg.free_host(s)
