@@ -2,7 +2,7 @@
 reference (oracle/_ref) behind one ctypes interface.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg
-load this package, as the checker; the GB300 library never calls it.
+load this package, to check results; the GB300 library never calls it.
 """
 from .oracle import (KIND_EAM_CHEBY, KIND_EAM_TABLE, KIND_LJ, Oracle, RefCentro, RefLib, build,
                      oracle_lib, ref_centro, ref_lib)

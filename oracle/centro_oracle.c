@@ -3,11 +3,13 @@
  *
  * Plain serial restatement of the centrosymmetry parameter of the in-situ
  * visualiser (AtomVisualize::computeCentrosymmetry,
- * src-viz/AtomVisualize.c:399-672), the checker of the library's
- * centrosymmetry kernel.  The visualiser's source cannot be compiled here
- * (it includes the VTK and OpenGL headers), so the restatement follows its
- * loops step for step instead of being pinned against it; the tests add
- * known answers of the physics (perfect lattice, vacancy neighbours).
+ * src-viz/AtomVisualize.c:399-672), the oracle of the library's
+ * centrosymmetry kernel.  It follows the routine's loops step for step.
+ * The visualiser as a whole cannot be compiled without its VTK and OpenGL
+ * headers, so oracle/Makefile compiles that one routine's text inside
+ * oracle/centro_ref_shim.cpp, and the tests pin this restatement against
+ * it bit for bit (and against fixtures it generated); known answers of the
+ * physics (perfect lattice, vacancy neighbours) are a second check.
  *
  * Per atom: up to 12 nearest candidates, scanned from the atom's own box
  * (box-relative differences, :421-447) and then the 26 adjacent boxes in

@@ -2,9 +2,10 @@
  * comd_oracle.c -- TEST INFRASTRUCTURE ONLY.
  *
  * A CPU restatement, in plain serial C with double precision, of CoMD's
- * force-and-integrate timestep (src-flat).  It is the checker for the GB300
- * library: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
- * leg load it, and never as the thing measured on the GPU or shipped.
+ * force-and-integrate timestep (src-flat).  It is the oracle of the GB300
+ * library's tests: only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it, and never as the thing measured on the GPU or
+ * shipped.
  *
  * Every function follows the reference loop for loop and operation for
  * operation (same evaluation order, no FMA contraction: build with
