@@ -28,6 +28,8 @@
  * Output: the reference's per-iteration lines (energy, virial stress and
  * microseconds per atom and force call), then one line
  *   "comdgb_run: iterations N steps K atoms A final_energy E"
+ * and the run as one JSON record (atoms, steps, atom-steps/s over the
+ * comdgb_nTimeSteps calls, final energy and stress).
  * Exit status 0, or the library's negative error code as 1 with a message.
  */
 #define _POSIX_C_SOURCE 200809L
@@ -172,6 +174,7 @@ int main(int argc, char **argv) {
   double te = now_s();
   if (rc) return fail("computeForce", rc);
   printf("Starting timesteps\n");
+  double steps_s = 0.0; /* host time inside comdgb_nTimeSteps */
   int iter;
   for (iter = 0; iter < ro.niter; iter++) {
     const double ns = iter == 0 ? 1.0 : (double)(1 + ro.nsteps);
@@ -181,6 +184,7 @@ int main(int argc, char **argv) {
     ts = now_s();
     const double eone = comdgb_nTimeSteps(ro.nsteps, sim, dt);
     te = now_s();
+    steps_s += te - ts;
     if (eone != eone) return fail("comdgb_nTimeSteps", COMDGB_ERR_CUDA);
   }
   printf(" %3d %30.20g computed in %.3fs (%8.4f us/atom for %d atoms)\n", iter * ro.nsteps,
@@ -189,6 +193,16 @@ int main(int argc, char **argv) {
   printf("Virial stress = %.17g\n", sim->stress);
   printf("comdgb_run: iterations %d steps %d atoms %d final_energy %.17g\n", ro.niter,
          ro.nsteps, sim->ntot, sim->e);
+  /* the same run as one JSON record: atom-steps/s over the nTimeSteps calls
+   * (host clock, each call with its trailing force call and copies) */
+  const double atom_steps = (double)sim->ntot * (double)ro.niter * (double)ro.nsteps;
+  printf("{\"comdgb_run\": {\"atoms\": %d, \"iterations\": %d, \"steps_per_call\": %d, "
+         "\"potential\": \"%s\", \"precision\": \"%s\", \"lazy\": %d, "
+         "\"seconds_in_nTimeSteps\": %.6f, \"atom_steps_per_s\": %.6g, "
+         "\"final_energy\": %.17g, \"final_stress\": %.17g}}\n",
+         sim->ntot, ro.niter, ro.nsteps,
+         !ro.eam ? "lj" : ro.cheby ? "eam_cheby" : "eam_table", ro.mixed ? "mixed" : "fp64",
+         ro.lazy, steps_s, steps_s > 0.0 ? atom_steps / steps_s : 0.0, sim->e, sim->stress);
 
   rc = comdgb_detach(sim); /* brings the state home (lazy mode) */
   if (rc) return fail("comdgb_detach", rc);

@@ -9,6 +9,7 @@ prints after the initial force call and after every nTimeSteps(10) with the
 oracle running the same loop on the same state: FP64 to 1e-10 relative,
 mixed precision to 1e-7 Ha per atom.
 """
+import json
 import os
 import re
 import subprocess
@@ -64,3 +65,9 @@ def test_host_loop_matches_oracle(oracle, mixed):
             assert abs(e - eo) / ntot < 1e-7, (step, e, eo)
         else:
             assert abs(e - eo) <= 1e-10 * abs(eo), (step, e, eo)
+    # the run's JSON record agrees with the printed lines
+    rec = [json.loads(l)["comdgb_run"] for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(rec) == 1, r.stdout
+    assert rec[0]["atoms"] == ntot and rec[0]["iterations"] == niter
+    assert rec[0]["precision"] == ("mixed" if mixed else "fp64")
+    assert rec[0]["final_energy"] == got[-1][1] and rec[0]["atom_steps_per_s"] > 0
