@@ -83,8 +83,16 @@ bool cache_lookup(const char *path, const std::string &key, comdgb_tune *t) {
     *tab = 0;
     if (key != line) continue;
     comdgb_tune v{};
+    // a line that does not parse, or holds values comdgb_sim_set_launch
+    // would refuse (an edited or damaged file), is skipped: the system is
+    // tuned again
     if (sscanf(tab + 1, "%lf %lf %d %d %d %lf", &v.box_factor, &v.skin, &v.build_threads,
-               &v.build_atoms, &v.pass2_threads, &v.ms_per_step) == 6) {
+               &v.build_atoms, &v.pass2_threads, &v.ms_per_step) == 6 &&
+        v.box_factor > 0.0 && std::isfinite(v.box_factor) && v.skin > 0.0 &&
+        std::isfinite(v.skin) &&
+        (v.build_threads == 64 || v.build_threads == 128 || v.build_threads == 256) &&
+        (v.build_atoms == 2 || v.build_atoms == 4 || v.build_atoms == 8) &&
+        (v.pass2_threads == 128 || v.pass2_threads == 256 || v.pass2_threads == 512)) {
       *t = v;
       found = true;
     }
