@@ -181,9 +181,8 @@ def tim_case(tmpdir):
     return out
 
 
-def main():
-    if ref_lib(False) is None or ref_lib(True) is None:
-        sys.exit("oracle/_ref is not built (run make -C oracle with the reference sources)")
+def generate():
+    """every fixture, computed by the reference (oracle/_ref must be built)"""
     fx = {"generator": "tests/golden/make_golden.py (reference src-flat via oracle/_ref)"}
     # known answers (perfect lattices, as the reference's own runs)
     fx["cu10_table_perfect"] = eam_case(False, 10, 1.0, 1.0, None, 0, 0, 0, 0)
@@ -206,6 +205,13 @@ def main():
     with tempfile.TemporaryDirectory() as td:
         fx["clsman_writers"] = writer_cases(td)
         fx["tim_reader"] = tim_case(td)
+    return fx
+
+
+def main():
+    if ref_lib(False) is None or ref_lib(True) is None:
+        sys.exit("oracle/_ref is not built (run make -C oracle with the reference sources)")
+    fx = generate()
     with open(os.path.join(HERE, "reference_fixtures.json"), "w") as f:
         json.dump(fx, f, indent=1)
     print("wrote", os.path.join(HERE, "reference_fixtures.json"))

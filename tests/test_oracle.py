@@ -127,3 +127,24 @@ def test_oracle_bitexact_vs_compiled_reference(oracle, pots_dir, cheby):
             assert np.array_equal(va[f], vb[f]), f
         assert s.contents.e == rs.contents.e
         oracle.free(s)
+
+
+def test_committed_fixtures_regenerate_from_the_reference():
+    """tests/golden/reference_fixtures.json is exactly what the reference
+    computes today: make_golden.generate() on the reference compiled from its
+    sources reproduces every committed value (skipped where the reference
+    sources are absent)."""
+    import json
+    import os
+    import sys
+    if ref_lib(False) is None or ref_lib(True) is None:
+        pytest.skip("reference sources not present (oracle/_ref not built)")
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    sys.path.insert(0, here)
+    import make_golden
+    fresh = json.loads(json.dumps(make_golden.generate()))
+    with open(os.path.join(here, "reference_fixtures.json")) as f:
+        committed = json.load(f)
+    assert fresh.keys() == committed.keys()
+    for k in committed:
+        assert fresh[k] == committed[k], k
