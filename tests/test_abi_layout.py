@@ -77,3 +77,38 @@ def test_simflat_layout_matches_reference_headers(tmp_path):
     r = subprocess.run(["gcc", "-std=c11", "-c", "-I", os.path.join(ROOT, "include"), str(check),
                         "-o", str(tmp_path / "layout_check.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_python_binding_structs_match_the_library_header(tmp_path):
+    """The ctypes mirrors the tests and bench.py pass through the C ABI
+    (comd_gb300/abi.py, comd_gb300/lib.py) have the sizes and member offsets
+    of include/comdgb.h, as the host compiler lays the structs out."""
+    import ctypes as C
+
+    from comd_gb300 import abi
+    from comd_gb300.lib import Opts, Tune
+    mirrors = {"simflat_t": abi.SimFlat, "pmd_base_potential_t": abi.BasePotential,
+               "potentialarray_t": abi.PotentialArray, "eampotential_t": abi.EamPotential,
+               "eam_cheby_t": abi.EamCheby, "ljpotential_t": abi.LjPotential,
+               "comdgb_opts": Opts, "comdgb_tune": Tune}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "comdgb.h"',
+             "int main(void) {"]
+    for st, py in mirrors.items():
+        lines.append(f'  printf("{st} sizeof %zu\\n", sizeof({st}));')
+        for name, _ in py._fields_:
+            lines.append(f'  printf("{st} {name} %zu\\n", offsetof({st}, {name}));')
+    lines += ["  return 0;", "}"]
+    probe = tmp_path / "probe.c"
+    probe.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(probe), "-o",
+                    str(exe)], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    seen = 0
+    for line in out.splitlines():
+        st, name, val = line.split()
+        py = mirrors[st]
+        got = C.sizeof(py) if name == "sizeof" else getattr(py, name).offset
+        assert got == int(val), (st, name, got, val)
+        seen += 1
+    assert seen == sum(len(p._fields_) + 1 for p in mirrors.values())
