@@ -286,3 +286,56 @@ def test_create_checks_the_box_grid_before_any_cuda_call():
         s.contents.boxsize[1] = bs
     finally:
         cg.free_host(s)
+
+
+def _c_kind(decl):
+    """'int', 'long', 'long long', 'double', 'float', 'uint64', 'void' or
+    'ptr' for one C parameter or return declaration of include/comdgb.h"""
+    d = " ".join(decl.replace("const", " ").split())
+    if "*" in d or "[" in d:
+        return "ptr"
+    words = d.split()
+    base = " ".join(w for w in words[:-1]) if len(words) > 1 else words[0]
+    return {"int": "int", "long": "long", "long long": "long long", "double": "double",
+            "float": "float", "uint64_t": "uint64", "void": "void", "size_t": "ulong"}[base]
+
+
+def _py_kind(t):
+    if t is None:
+        return "void"
+    for ct, k in ((C.c_int, "int"), (C.c_double, "double"), (C.c_float, "float"),
+                  (C.c_uint64, "uint64"), (C.c_longlong, "long long"), (C.c_long, "long")):
+        if t is ct:
+            return k
+    if t in (C.c_void_p, C.c_char_p) or hasattr(t, "_type_") and issubclass(t, C._Pointer):
+        return "ptr"
+    raise AssertionError(f"unclassified ctypes type {t}")
+
+
+def test_binding_prototypes_match_the_header():
+    """Every entry point the Python binding declares (argtypes) takes the
+    parameters and returns the type include/comdgb.h gives it, kind for kind
+    (a double passed where the C side reads an int would not be caught by
+    ctypes), so the tests call the library as a C caller would."""
+    src = open(os.path.join(ROOT, "include", "comdgb.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][\w \*]*?)\b(comdgb_\w+)\s*\(([^)]*)\)\s*;", src):
+        ret, name, params = m.group(1), m.group(2), m.group(3).strip()
+        args = [] if params in ("", "void") else [_c_kind(p) for p in params.split(",")]
+        protos[name] = (_c_kind(ret.strip() + " x"), args)
+    lib = cg.load()
+    checked = 0
+    for name, (ret, args) in protos.items():
+        fn = getattr(lib, name)
+        if fn.argtypes is None:
+            continue
+        # long and long long are one ctypes type where they have one size
+        same = C.sizeof(C.c_long) == C.sizeof(C.c_longlong)
+        canon = (lambda k: "long long" if same and k == "long" else k)
+        assert [canon(_py_kind(t)) for t in fn.argtypes] == [canon(a) for a in args], name
+        want = "int" if fn.restype is C.c_int else _py_kind(fn.restype)
+        # a void function's ctypes default (int) result is never read
+        assert want == ret or (ret == "void" and want == "int"), (name, want, ret)
+        checked += 1
+    assert checked >= 70, checked
