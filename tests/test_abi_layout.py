@@ -112,3 +112,17 @@ def test_python_binding_structs_match_the_library_header(tmp_path):
         assert got == int(val), (st, name, got, val)
         seen += 1
     assert seen == sum(len(p._fields_) + 1 for p in mirrors.values())
+
+
+def test_public_headers_compile_cleanly_as_c99_and_cxx11(tmp_path):
+    """include/*.h compile without a warning in a C99 and a C++11 caller
+    (-pedantic -Wall -Wextra -Werror): the reference's host is C, and the
+    headers carry their own extern "C" guards"""
+    src = '#include "comdgb.h"\n#include "comdgb_seed.h"\nint main(void) { return 0; }\n'
+    for compiler, std, ext in (("gcc", "-std=c99", "c"), ("g++", "-std=c++11", "cpp")):
+        f = tmp_path / f"hdr.{ext}"
+        f.write_text(src)
+        r = subprocess.run([compiler, std, "-pedantic", "-Wall", "-Wextra", "-Werror", "-I",
+                            os.path.join(ROOT, "include"), "-c", str(f), "-o",
+                            str(tmp_path / f"hdr_{ext}.o")], capture_output=True, text=True)
+        assert r.returncode == 0, (compiler, r.stderr)
