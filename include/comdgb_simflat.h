@@ -14,9 +14,26 @@
  *   ljpotential_t        src-flat/include/ljTypes.h:72-81
  * real_t is double here (the reference's -DDOUBLE oracle build); the
  * reference's default -DSINGLE layout is not supported by this library.
+ *
+ * In a translation unit of the reference itself, include comdgb.h after the
+ * reference's pmd.h: the structs are then the reference's own definitions
+ * (its include guards are tested below) and this header adds none of its
+ * own.  That needs the reference's double layout (-DDOUBLE) and a simflat_t
+ * without the in-situ visualiser's extra member (USE_IN_SITU_VIZ); either
+ * mismatch stops the compile here.
  */
 #ifndef COMDGB_SIMFLAT_H
 #define COMDGB_SIMFLAT_H
+
+/* the reference's headers already seen (pmdTypes.h, eamTypes.h, ljTypes.h) */
+#if defined(__PMDTYPES_H_) || defined(__EAM_TYPES_H_) || defined(_LJTYPES_H_)
+#if defined(SINGLE)
+#error "libcomdgb takes the reference's double layout: build the reference with -DDOUBLE"
+#endif
+#if defined(__PMDTYPES_H_) && defined(USE_IN_SITU_VIZ)
+#error "libcomdgb takes simflat_t without the visualiser's centro member (USE_IN_SITU_VIZ)"
+#endif
+#endif
 
 #ifdef __cplusplus
 extern "C" {
@@ -31,13 +48,16 @@ typedef double comdgb_real_t;
 typedef comdgb_real_t comdgb_real3[3];
 typedef comdgb_real_t comdgb_real4[4];
 
+#ifndef __PMDTYPES_H_
 typedef struct pmd_base_potential_t {
   comdgb_real_t cutoff;          /* Angstrom */
   comdgb_real_t mass;            /* amu */
   int (*force)(void *s);         /* the force routine; takes simflat_t* */
   void (*destroy)(void *pot);
 } pmd_base_potential_t;
+#endif
 
+#ifndef __EAM_TYPES_H_
 /* Tabulated function.  values[-1], values[n] and values[n+1] are guard
  * cells; x0 is already shifted by one interval (eam.c:130-153). */
 typedef struct potentialarray_t {
@@ -71,7 +91,9 @@ typedef struct eam_cheby_t {
   potentialarray_t *df;
   comdgb_real_t lat;
 } eam_cheby_t;
+#endif
 
+#ifndef _LJTYPES_H_
 typedef struct ljpotential_t {
   comdgb_real_t cutoff;
   comdgb_real_t mass;
@@ -80,7 +102,9 @@ typedef struct ljpotential_t {
   comdgb_real_t sigma;
   comdgb_real_t epsilon;
 } ljpotential_t;
+#endif
 
+#ifndef __PMDTYPES_H_
 /* Flat link-cell simulation: slot = box*64 + k for k < natoms[box]. */
 typedef struct simflat_t {
   int stateflag;
@@ -108,6 +132,7 @@ typedef struct simflat_t {
   comdgb_real_t bf;
   eam_cheby_t *ch_pot;
 } simflat_t;
+#endif
 
 #ifdef __cplusplus
 }

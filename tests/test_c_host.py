@@ -17,7 +17,7 @@ import subprocess
 import pytest
 
 import comd_gb300 as cg
-from comd_gb300.build import HOST_OUT, build
+from comd_gb300.build import HOST_OUT, INCLUDE, OUT, build
 from helpers import Case
 
 LINE = re.compile(r"^\s*(\d+)\s+(\S+)\s+computed in")
@@ -71,3 +71,96 @@ def test_host_loop_matches_oracle(oracle, mixed):
     assert rec[0]["atoms"] == ntot and rec[0]["iterations"] == niter
     assert rec[0]["precision"] == ("mixed" if mixed else "fp64")
     assert rec[0]["final_energy"] == got[-1][1] and rec[0]["atom_steps_per_s"] > 0
+
+
+# The maintainer's edits of INTEGRATION.md, applied to copies of the
+# reference's own sources in a temporary directory (nothing of the reference
+# is kept): comdgb.h after pmd.h, the attach and the force pointer at the end
+# of initSimFromCmdLine, comdgb_nTimeSteps in do_compute_work's loop, and the
+# detach before destroySimulation.
+_ATTACH = r'''
+    {   /* libcomdgb: computeForce and nTimeSteps on the GPU */
+        extern int PERIODIC;
+        comdgb_opts o;
+        comdgb_default_opts(&o);
+#ifdef USE_CHEBY
+        o.potential = cmd.doeam ? COMDGB_POT_EAM_CHEBY : COMDGB_POT_LJ;
+#else
+        o.potential = cmd.doeam ? COMDGB_POT_EAM_TABLE : COMDGB_POT_LJ;
+#endif
+        o.precision = COMDGB_PREC_MIXED;
+        o.periodic = PERIODIC;
+        o.cheby_from_host = cmd.doeam;
+        if (comdgb_attach(sim, &o)) {
+            char m[256];
+            comdgb_last_error(m, 256);
+            fprintf(stderr, "comdgb_attach failed: %s\n", m);
+            simulationAbort(-30, m);
+        }
+        sim->pot->force = comdgb_force;
+    }
+    printf("Initialization finished\n");'''
+
+
+def _edit(text, old, new):
+    assert text.count(old) == 1, old
+    return text.replace(old, new)
+
+
+def test_reference_program_builds_with_the_documented_edits(tmp_path):
+    """The reference's own program (src-flat: pmd.c's main, initSimFromCmdLine
+    and do_compute_work) compiles and links against libcomdgb with the edits
+    INTEGRATION.md lists, with pointer types checked as errors: comdgb.h then
+    uses the reference's own struct definitions.  Run without a GPU it gets
+    through the reference's set-up and stops at comdgb_attach with the
+    library's error (there is no CPU fallback).  Skipped where the reference
+    sources are absent."""
+    from oracle.oracle import reference_dir
+    ref = reference_dir()
+    if ref is None:
+        pytest.skip("reference sources not present on this machine")
+    build()
+    flat = os.path.join(ref, "src-flat")
+    srcs = ["pmd.c", "docompute.c", "cmdLineParser.c", "domains.c", "eam.c", "ljForce.c",
+            "ic_fcc.c", "cheby.c", "mycommand.c", "read.c", "write.c", "utility.c",
+            "timestep.c"]
+    for name in srcs:
+        (tmp_path / name).write_text(open(os.path.join(flat, name)).read())
+    d = (tmp_path / "docompute.c").read_text()
+    d = _edit(d, '#include "read.h"\n', '#include "read.h"\n#include "comdgb.h"\n')
+    d = _edit(d, '    printf("Initialization finished\\n");', _ATTACH)
+    d = _edit(d, "eone = nTimeSteps(nsteps,data->sim,dt);",
+              "eone = comdgb_nTimeSteps(nsteps, data->sim, dt);")
+    (tmp_path / "docompute.c").write_text(d)
+    p = (tmp_path / "pmd.c").read_text()
+    p = _edit(p, '#include "pmd.h"\n', '#include "pmd.h"\n#include "comdgb.h"\n')
+    p = _edit(p, "    destroySimulation(&sim);", "    comdgb_detach(sim);\n    destroySimulation(&sim);")
+    (tmp_path / "pmd.c").write_text(p)
+    lib = os.path.dirname(OUT)
+    exe = tmp_path / "comd_dropin"
+    flags = ["-O1", "-DDOUBLE", "-DUSE_CHEBY", "-DGZIPSUPPORT", "-I",
+             os.path.join(flat, "include"), "-I", INCLUDE]
+    objs = []
+    for name in srcs:
+        # the edited files: the library's types must be the reference's, and
+        # every library call declared (pmd.c calls do_compute_work
+        # undeclared in the reference itself)
+        strict = {"docompute.c": ["-Werror=incompatible-pointer-types",
+                                  "-Werror=implicit-function-declaration"],
+                  "pmd.c": ["-Werror=incompatible-pointer-types"]}.get(name, ["-w"])
+        obj = str(tmp_path / (name[:-2] + ".o"))
+        r = subprocess.run(["gcc"] + flags + strict +
+                           ["-c", str(tmp_path / name), "-o", obj], capture_output=True, text=True)
+        assert r.returncode == 0, (name, r.stderr)
+        objs.append(obj)
+    r = subprocess.run(["gcc"] + objs + ["-o", str(exe), "-L", lib, "-lcomdgb",
+                                         "-Wl,-rpath," + lib, "-lz", "-lm"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe), "-e", "-p", "cu", "-d", cg.POT_DIR, "-x", "4", "-y", "4",
+                        "-z", "4"], capture_output=True, text=True, timeout=300,
+                       env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert r.returncode != 0
+    assert "total atoms is: 256" in r.stdout, r.stdout[-2000:]
+    assert "comdgb_attach failed" in r.stderr, r.stderr[-2000:]
+    assert "Starting simulation" not in r.stdout
