@@ -102,6 +102,18 @@ _ATTACH = r'''
     printf("Initialization finished\n");'''
 
 
+_READ = r'''        {   /* libcomdgb: the clsman reader, atoms binned on GPU 0 */
+            int st;
+            sim = comdgb_read_clsman(cmd.filename, pot, cmd.bf, 0, &st);
+            if (!sim) {
+                char m[256];
+                comdgb_last_error(m, 256);
+                fprintf(stderr, "comdgb_read_clsman failed (%d): %s\n", st, m);
+                simulationAbort(-3, m);
+            }
+        }'''
+
+
 def _edit(text, old, new):
     assert text.count(old) == 1, old
     return text.replace(old, new)
@@ -131,6 +143,7 @@ def test_reference_program_builds_with_the_documented_edits(tmp_path):
     d = _edit(d, '    printf("Initialization finished\\n");', _ATTACH)
     d = _edit(d, "eone = nTimeSteps(nsteps,data->sim,dt);",
               "eone = comdgb_nTimeSteps(nsteps, data->sim, dt);")
+    d = _edit(d, "        sim = fromFileASCII(cmd, pot);", _READ)
     (tmp_path / "docompute.c").write_text(d)
     p = (tmp_path / "pmd.c").read_text()
     p = _edit(p, '#include "pmd.h"\n', '#include "pmd.h"\n#include "comdgb.h"\n')
@@ -164,3 +177,9 @@ def test_reference_program_builds_with_the_documented_edits(tmp_path):
     assert "total atoms is: 256" in r.stdout, r.stdout[-2000:]
     assert "comdgb_attach failed" in r.stderr, r.stderr[-2000:]
     assert "Starting simulation" not in r.stdout
+    # a structure file: the reader bins on GPU 0, so without one it fails
+    r = subprocess.run([str(exe), "-e", "-p", "ag", "-d", cg.POT_DIR, "-f",
+                        os.path.join(cg.DATA_DIR, "8k.inp.gz")], capture_output=True, text=True,
+                       timeout=300, env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert r.returncode != 0
+    assert "comdgb_read_clsman failed" in r.stderr, r.stderr[-2000:]
