@@ -1,7 +1,6 @@
 """Shared builders for the parity tests: seeded inputs made once by the
 library's host setup and cloned for the oracle, so both sides start from
 identical bytes."""
-import ctypes as C
 import hashlib
 import json
 import os

@@ -10,7 +10,7 @@
 import numpy as np
 import pytest
 
-from comd_gb300.abi import by_id, occupied_mask, slot_views
+from comd_gb300.abi import slot_views
 from helpers import FIX, match, snapshot
 from oracle import KIND_EAM_CHEBY, KIND_EAM_TABLE, KIND_LJ, ref_lib
 
