@@ -126,3 +126,26 @@ def test_public_headers_compile_cleanly_as_c99_and_cxx11(tmp_path):
                             os.path.join(ROOT, "include"), "-c", str(f), "-o",
                             str(tmp_path / f"hdr_{ext}.o")], capture_output=True, text=True)
         assert r.returncode == 0, (compiler, r.stderr)
+
+
+def test_integration_batch_and_gradient_example_compiles(tmp_path):
+    """The C example of INTEGRATION.md's "Batches and gradients" section
+    compiles against include/comdgb.h as written (inside a function that
+    declares the handles and inputs it names), so the document keeps up
+    with the header"""
+    import re
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    sec = text.split("## Batches and gradients", 1)[1]
+    code = re.search(r"```c\n(.*?)```", sec, re.S).group(1)
+    src = ("#include <stddef.h>\n#include \"comdgb.h\"\n"
+           "void example(comdgb_opts o, comdgb_sim *h, const double *target_forces_by_id) {\n"
+           + code + "\n}\n")
+    f = tmp_path / "example.c"
+    f.write_text(src)
+    # (the example leaves reps[] to the caller's set-up: no use-before-set
+    # warnings)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wno-unused-variable", "-Wno-uninitialized",
+                        "-Wno-maybe-uninitialized", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), "-c", str(f), "-o",
+                        str(tmp_path / "example.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
