@@ -147,7 +147,8 @@ def test_reference_program_builds_with_the_documented_edits(tmp_path):
     (tmp_path / "docompute.c").write_text(d)
     p = (tmp_path / "pmd.c").read_text()
     p = _edit(p, '#include "pmd.h"\n', '#include "pmd.h"\n#include "comdgb.h"\n')
-    p = _edit(p, "    destroySimulation(&sim);", "    comdgb_detach(sim);\n    destroySimulation(&sim);")
+    p = _edit(p, "    destroySimulation(&sim);",
+              "    comdgb_detach(sim);\n    destroySimulation(&sim);")
     (tmp_path / "pmd.c").write_text(p)
     lib = os.path.dirname(OUT)
     exe = tmp_path / "comd_dropin"
