@@ -73,45 +73,20 @@ def test_host_loop_matches_oracle(oracle, mixed):
     assert rec[0]["final_energy"] == got[-1][1] and rec[0]["atom_steps_per_s"] > 0
 
 
-# The maintainer's edits of INTEGRATION.md, applied to copies of the
-# reference's own sources in a temporary directory (nothing of the reference
-# is kept): comdgb.h after pmd.h, the attach and the force pointer at the end
-# of initSimFromCmdLine, comdgb_nTimeSteps in do_compute_work's loop, and the
-# detach before destroySimulation.
-_ATTACH = r'''
-    {   /* libcomdgb: computeForce and nTimeSteps on the GPU */
-        extern int PERIODIC;
-        comdgb_opts o;
-        comdgb_default_opts(&o);
-#ifdef USE_CHEBY
-        o.potential = cmd.doeam ? COMDGB_POT_EAM_CHEBY : COMDGB_POT_LJ;
-#else
-        o.potential = cmd.doeam ? COMDGB_POT_EAM_TABLE : COMDGB_POT_LJ;
-#endif
-        o.precision = COMDGB_PREC_MIXED;
-        o.periodic = PERIODIC;
-        o.cheby_from_host = cmd.doeam;
-        if (comdgb_attach(sim, &o)) {
-            char m[256];
-            comdgb_last_error(m, 256);
-            fprintf(stderr, "comdgb_attach failed: %s\n", m);
-            simulationAbort(-30, m);
-        }
-        sim->pot->force = comdgb_force;
-    }
-    printf("Initialization finished\n");'''
-
-
-_READ = r'''        {   /* libcomdgb: the clsman reader, atoms binned on GPU 0 */
-            int st;
-            sim = comdgb_read_clsman(cmd.filename, pot, cmd.bf, 0, &st);
-            if (!sim) {
-                char m[256];
-                comdgb_last_error(m, 256);
-                fprintf(stderr, "comdgb_read_clsman failed (%d): %s\n", st, m);
-                simulationAbort(-3, m);
-            }
-        }'''
+# The maintainer's edits of INTEGRATION.md, taken from the document itself
+# and applied to copies of the reference's own sources in a temporary
+# directory (nothing of the reference is kept): comdgb.h after pmd.h, the
+# attach and the force pointer at the end of initSimFromCmdLine (item 1),
+# comdgb_nTimeSteps in do_compute_work's loop (item 2), the detach before
+# destroySimulation (item 4) and the clsman reader (item 8).
+def _integration_snippets():
+    text = open(os.path.join(os.path.dirname(INCLUDE), "INTEGRATION.md")).read()
+    sec = text.split("## What a maintainer adds to the reference", 1)[1]
+    attach = re.search(r"```c\n(.*?)```", sec, re.S).group(1)
+    read = re.search(r"```c\n(.*?)```", sec.split("8. Structure files", 1)[1], re.S).group(1)
+    includes = "".join(l + "\n" for l in attach.splitlines() if l.startswith("#include"))
+    attach = "".join(l + "\n" for l in attach.splitlines() if not l.startswith("#include"))
+    return includes, attach, read
 
 
 def _edit(text, old, new):
@@ -122,11 +97,12 @@ def _edit(text, old, new):
 def test_reference_program_builds_with_the_documented_edits(tmp_path):
     """The reference's own program (src-flat: pmd.c's main, initSimFromCmdLine
     and do_compute_work) compiles and links against libcomdgb with the edits
-    INTEGRATION.md lists, with pointer types checked as errors: comdgb.h then
-    uses the reference's own struct definitions.  Run without a GPU it gets
-    through the reference's set-up and stops at comdgb_attach with the
-    library's error (there is no CPU fallback).  Skipped where the reference
-    sources are absent."""
+    INTEGRATION.md lists, its C snippets pasted as written, with pointer
+    types checked as errors: comdgb.h then uses the reference's own struct
+    definitions.  Run without a GPU it gets through the reference's set-up
+    and stops at comdgb_attach, or at comdgb_read_clsman given a structure
+    file, through the snippets' simulationAbort (there is no CPU fallback).
+    Skipped where the reference sources are absent."""
     from oracle.oracle import reference_dir
     ref = reference_dir()
     if ref is None:
@@ -138,12 +114,16 @@ def test_reference_program_builds_with_the_documented_edits(tmp_path):
             "timestep.c"]
     for name in srcs:
         (tmp_path / name).write_text(open(os.path.join(flat, name)).read())
+    includes, attach, read = _integration_snippets()
+    assert '#include "comdgb.h"' in includes and "comdgb_attach(sim, &o)" in attach
+    assert "comdgb_read_clsman(" in read
     d = (tmp_path / "docompute.c").read_text()
-    d = _edit(d, '#include "read.h"\n', '#include "read.h"\n#include "comdgb.h"\n')
-    d = _edit(d, '    printf("Initialization finished\\n");', _ATTACH)
+    d = _edit(d, '#include "read.h"\n', '#include "read.h"\n' + includes)
+    d = _edit(d, '    printf("Initialization finished\\n");',
+              "    {\n" + attach + "    }\n    printf(\"Initialization finished\\n\");")
     d = _edit(d, "eone = nTimeSteps(nsteps,data->sim,dt);",
               "eone = comdgb_nTimeSteps(nsteps, data->sim, dt);")
-    d = _edit(d, "        sim = fromFileASCII(cmd, pot);", _READ)
+    d = _edit(d, "        sim = fromFileASCII(cmd, pot);", "        {\n" + read + "        }")
     (tmp_path / "docompute.c").write_text(d)
     p = (tmp_path / "pmd.c").read_text()
     p = _edit(p, '#include "pmd.h"\n', '#include "pmd.h"\n#include "comdgb.h"\n')
@@ -176,11 +156,12 @@ def test_reference_program_builds_with_the_documented_edits(tmp_path):
                        env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
     assert r.returncode != 0
     assert "total atoms is: 256" in r.stdout, r.stdout[-2000:]
-    assert "comdgb_attach failed" in r.stderr, r.stderr[-2000:]
+    assert "Error code: -30" in r.stderr, r.stderr[-2000:]  # the snippet's abort
     assert "Starting simulation" not in r.stdout
     # a structure file: the reader bins on GPU 0, so without one it fails
     r = subprocess.run([str(exe), "-e", "-p", "ag", "-d", cg.POT_DIR, "-f",
                         os.path.join(cg.DATA_DIR, "8k.inp.gz")], capture_output=True, text=True,
                        timeout=300, env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
     assert r.returncode != 0
-    assert "comdgb_read_clsman failed" in r.stderr, r.stderr[-2000:]
+    assert "Error code: -3\n" in r.stderr, r.stderr[-2000:]
+    assert "Initialization finished" not in r.stdout
