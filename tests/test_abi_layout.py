@@ -149,3 +149,21 @@ def test_integration_batch_and_gradient_example_compiles(tmp_path):
                         os.path.join(ROOT, "include"), "-c", str(f), "-o",
                         str(tmp_path / "example.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_integration_python_example_runs_to_the_gpu_boundary():
+    """INTEGRATION.md's ctypes example, run as written without a GPU: every
+    name it uses exists, the attach returns the library's CUDA error and
+    nTimeSteps on the unattached simulation returns NaN (no CPU fallback)"""
+    import re
+    import sys
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    sec = text.split("## Python (ctypes) binding", 1)[1]
+    code = re.search(r"```python\n(.*?)```", sec, re.S).group(1)
+    code += ("\nimport math\nassert L.comdgb_last_error(None, 0) >= 0\n"
+             "print('E', e, math.isnan(e))\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True,
+                       timeout=300, env=dict(os.environ, CUDA_VISIBLE_DEVICES="",
+                                             PYTHONPATH=ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "E nan True" in r.stdout, r.stdout
