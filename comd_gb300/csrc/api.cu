@@ -2353,26 +2353,42 @@ eam_cheby_t *comdgb_cheb_make(const eampotential_t *p, int n, int device) {
     set_err(COMDGB_ERR_UNSUPPORTED, "only %d Chebyshev terms are supported", CG_NCHEB);
     return nullptr;
   }
-  if (cudaSetDevice(device) != cudaSuccess) return nullptr;
+  cudaError_t ce = cudaSetDevice(device);
   comdgb_sim tmp;
-  cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
+  if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&tmp.stream, cudaStreamNonBlocking);
+  if (ce != cudaSuccess) {
+    set_err(COMDGB_ERR_CUDA, "comdgb_cheb_make on device %d: %s", device, cudaGetErrorString(ce));
+    return nullptr;
+  }
   double coef[6][CG_NCHEB], a[6], b[6];
   int rc = fit_cheb_gpu(&tmp, p, coef, a, b);
   cudaStreamDestroy(tmp.stream);
   tmp.stream = nullptr;
   if (rc) return nullptr;
   eam_cheby_t *c = (eam_cheby_t *)calloc(1, sizeof(eam_cheby_t));
+  if (!c) {
+    set_err(COMDGB_ERR_NOMEM, "comdgb_cheb_make: out of host memory");
+    return nullptr;
+  }
   c->cutoff = p->cutoff;
   c->mass = p->mass;
   c->lat = p->lat;
   potentialarray_t **ser[6] = {&c->phi, &c->rho, &c->f, &c->dphi, &c->drho, &c->df};
   for (int q = 0; q < 6; q++) {
     potentialarray_t *pa = (potentialarray_t *)calloc(1, sizeof(potentialarray_t));
+    double *v = (double *)malloc(sizeof(double) * n);
+    if (!pa || !v) {
+      free(pa);
+      free(v);
+      comdgb_cheb_free(c);
+      set_err(COMDGB_ERR_NOMEM, "comdgb_cheb_make: out of host memory");
+      return nullptr;
+    }
     pa->n = n;
     pa->x0 = a[q];
     pa->xn = b[q];
     pa->invDx = q >= 3 ? 1.0 : 0.0;
-    pa->values = (double *)malloc(sizeof(double) * n);
+    pa->values = v;
     for (int j = 0; j < n; j++) pa->values[j] = coef[q][j];
     *ser[q] = pa;
   }

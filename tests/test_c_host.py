@@ -37,6 +37,20 @@ def test_host_links_against_library():
     assert "usage" in r.stderr
 
 
+def test_host_without_a_gpu_fails_with_the_library_error():
+    """without a usable GPU the C host stops at its first GPU call (the
+    Chebyshev fit) with exit status 1 and the library's message; nothing is
+    computed on the CPU"""
+    build()
+    r = subprocess.run([HOST_OUT, "-e", "-c", "-p", "cu", "-d", cg.POT_DIR, "-x", "4", "-y", "4",
+                        "-z", "4", "-m"], capture_output=True, text=True, timeout=300,
+                       env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert r.returncode == 1, r.stdout + r.stderr
+    m = re.search(r"comdgb_cheb_make failed \(-30\): (.+)", r.stderr)
+    assert m and m.group(1).strip(), r.stderr
+    assert "Starting simulation" not in r.stdout
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("mixed", [False, True])
 def test_host_loop_matches_oracle(oracle, mixed):
