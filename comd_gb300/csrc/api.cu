@@ -1713,8 +1713,12 @@ __global__ void fma_probe_kernel(float *out, int iters, float a, float b) {
   if (s == 1.2345f) out[0] = s;  // keeps the chains live; practically never stores
 }
 
-// message for comdgb_last_error from other translation units
-int comdgb_internal_set_error(int code, const char *msg) { return set_err(code, "%s", msg); }
+// message for comdgb_last_error from other translation units (C and C++;
+// not exported from the library)
+extern "C" __attribute__((visibility("hidden"))) int comdgb_internal_set_error(int code,
+                                                                                const char *msg) {
+  return set_err(code, "%s", msg);
+}
 
 // ============================================================================
 // exported C ABI

@@ -28,6 +28,44 @@ static void *zalloc(size_t n) {
   return p;
 }
 
+/* the message comdgb_last_error() returns (api.cu) */
+int comdgb_internal_set_error(int code, const char *msg);
+
+/* records why a host set-up call failed: the call, the file when there is
+ * one, and the meaning of the code */
+static int host_err(int code, const char *call, const char *path) {
+  const char *why;
+  switch (code) {
+    case COMDGB_ERR_ARG:
+      why = "bad argument, or a grid whose slot indexes do not fit an int";
+      break;
+    case COMDGB_ERR_NOBOX:
+      why = "Need at least one cutoff wide domain (bounds below the cutoff)";
+      break;
+    case COMDGB_ERR_MAXATOMS:
+      why = "Increase maxatoms (a box would hold more than 64 atoms)";
+      break;
+    case COMDGB_ERR_BOXRANGE:
+      why = "an atom's coordinate is not finite or lies more than one period outside";
+      break;
+    case COMDGB_ERR_NOMEM:
+      why = "out of host memory";
+      break;
+    case COMDGB_ERR_IO:
+      why = "cannot open the file, or it is short or malformed";
+      break;
+    case COMDGB_ERR_UNSUPPORTED:
+      why = "gzip input needs the library built with zlib";
+      break;
+    default:
+      why = "failed";
+      break;
+  }
+  char m[512];
+  snprintf(m, sizeof m, "%s%s%.300s: %s", call, path ? " " : "", path ? path : "", why);
+  return comdgb_internal_set_error(code, m);
+}
+
 static int read_be_or_le(FILE *fp, void *dst, int size, int swap) {
   unsigned char b[8];
   if (fread(b, (size_t)size, 1, fp) != 1) return 0;
@@ -100,16 +138,22 @@ eampotential_t *comdgb_eam_read(const char *dir, const char *name) {
   char path[4096];
   eampotential_t *p = (eampotential_t *)zalloc(sizeof *p);
   if (!p) return NULL;
-  snprintf(path, sizeof path, "%s/%s.phi", dir, name);
-  p->phi = read_table(path);
-  snprintf(path, sizeof path, "%s/%s.rho", dir, name);
-  p->rho = read_table(path);
-  snprintf(path, sizeof path, "%s/%s.f", dir, name);
-  p->f = read_table(path);
+  static const char *ext[3] = {"phi", "rho", "f"};
+  potentialarray_t **tab[3] = {&p->phi, &p->rho, &p->f};
+  for (int q = 0; q < 3; q++) {
+    snprintf(path, sizeof path, "%s/%s.%s", dir, name, ext[q]);
+    *tab[q] = read_table(path);
+    if (!*tab[q]) {
+      host_err(COMDGB_ERR_IO, "comdgb_eam_read", path);
+      comdgb_eam_free(p);
+      return NULL;
+    }
+  }
   snprintf(path, sizeof path, "%s/%s.doc", dir, name);
   p->mass = doc_line_value(path, 2); /* mass in amu, second line */
   p->lat = doc_line_value(path, 3);  /* lattice constant, third line */
-  if (!p->phi || !p->rho || !p->f || p->mass < 0.0) {
+  if (p->mass < 0.0) {
+    host_err(COMDGB_ERR_IO, "comdgb_eam_read", path);
     comdgb_eam_free(p);
     return NULL;
   }
@@ -251,6 +295,7 @@ simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double
   }
   if (status) *status = st;
   if (st) {
+    host_err(st, "comdgb_fcc", NULL);
     comdgb_sim_free_host(s);
     return NULL;
   }
@@ -265,7 +310,7 @@ simflat_t *comdgb_fcc(int nx, int ny, int nz, double lat, double defgrad, double
 simflat_t *comdgb_rebin_host(const simflat_t *src, double bf, int *status) {
   int st = 0;
   if (!src || !src->pot || !(bf > 0.0)) {
-    if (status) *status = COMDGB_ERR_ARG;
+    if (status) *status = host_err(COMDGB_ERR_ARG, "comdgb_rebin_host", NULL);
     return NULL;
   }
   simflat_t *s = (simflat_t *)zalloc(sizeof *s);
@@ -303,6 +348,7 @@ simflat_t *comdgb_rebin_host(const simflat_t *src, double bf, int *status) {
   free(slot_of);
   if (status) *status = st;
   if (st) {
+    host_err(st, "comdgb_rebin_host", NULL);
     comdgb_sim_free_host(s);
     return NULL;
   }
@@ -455,13 +501,13 @@ static int clsman_parse_all(char **lines, int natoms, double *xyz, double *pxyz)
  * device < 0). */
 simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, double bf, int device,
                               int *status) {
-  int st = 0;
+  int st = 0, from_gpu = 0;
   simflat_t *s = NULL;
   double *xyz = NULL, *pxyz = NULL, *masses = NULL;
   int *ids = NULL, *types = NULL;
   char **lines = NULL;
   if (!path || !pot) {
-    if (status) *status = COMDGB_ERR_ARG;
+    if (status) *status = host_err(COMDGB_ERR_ARG, "comdgb_read", path);
     return NULL;
   }
   char *buf = read_all(path, &st);
@@ -523,6 +569,7 @@ simflat_t *comdgb_read_clsman(const char *path, pmd_base_potential_t *pot, doubl
   if ((st = clsman_parse_all(lines, natoms, xyz, pxyz))) goto done;
   if (device >= 0) {
     st = comdgb_put_atoms(s, natoms, xyz, pxyz, ids, types, masses, device);
+    from_gpu = st != 0;  /* comdgb_put_atoms recorded its own message */
   } else {
     for (int i = 0; i < natoms && !st; i++)
       st = put_atom(s, ids[i], types[i], masses[i], xyz + 3 * (size_t)i, pxyz + 3 * (size_t)i);
@@ -536,6 +583,7 @@ done:
   free(ids);
   free(types);
   if (status) *status = st;
+  if (st && !from_gpu) host_err(st, "comdgb_read_clsman", path);
   if (st && s) {
     comdgb_sim_free_host(s);
     s = NULL;
@@ -567,14 +615,14 @@ simflat_t *comdgb_read_tim(const char *path, pmd_base_potential_t *pot, double b
                            const double *bounds, int device, int *status) {
   static const double kTimBounds[3] = {327.42399999999997817, 354.44687726089500757,
                                        3007.58148577889733133};
-  int st = 0;
+  int st = 0, from_gpu = 0;
   simflat_t *s = NULL;
   float *rec = NULL;
   double *xyz = NULL, *pxyz = NULL, *masses = NULL;
   int *ids = NULL, *types = NULL;
   long n = 0;
   if (!path || !pot) {
-    if (status) *status = COMDGB_ERR_ARG;
+    if (status) *status = host_err(COMDGB_ERR_ARG, "comdgb_read", path);
     return NULL;
   }
   FILE *fp = fopen(path, "rb");
@@ -625,6 +673,7 @@ simflat_t *comdgb_read_tim(const char *path, pmd_base_potential_t *pot, double b
   }
   if (device >= 0) {
     st = comdgb_put_atoms(s, (int)n, xyz, pxyz, ids, types, masses, device);
+    from_gpu = st != 0;  /* comdgb_put_atoms recorded its own message */
   } else {
     for (long i = 0; i < n && !st; i++)
       st = put_atom(s, ids[i], types[i], masses[i], xyz + 3 * i, NULL);
@@ -637,6 +686,7 @@ done:
   free(ids);
   free(types);
   if (status) *status = st;
+  if (st && !from_gpu) host_err(st, "comdgb_read_tim", path);
   if (st && s) {
     comdgb_sim_free_host(s);
     s = NULL;

@@ -34,7 +34,7 @@
 #include "binning.cuh"
 
 // records the message that comdgb_last_error() returns (api.cu)
-int comdgb_internal_set_error(int code, const char *msg);
+extern "C" int comdgb_internal_set_error(int code, const char *msg);
 
 namespace {
 

@@ -319,7 +319,7 @@ def fcc(nx, ny, nz, lat, defgrad, bf, pot):
     st = C.c_int(0)
     s = L.comdgb_fcc(nx, ny, nz, lat, defgrad, bf, pot.base, C.byref(st))
     if not s:
-        raise ComdgbError(st.value, "comdgb_fcc failed")
+        raise ComdgbError(st.value, "comdgb_fcc failed: " + last_error())
     return s
 
 

@@ -193,6 +193,7 @@ def test_eam_read_rejects_malformed_tables(tmp_path, case):
         L.comdgb_eam_free(p)
     else:
         assert not p, case
+        assert "t.phi" in cg.lib.last_error(), cg.lib.last_error()
 
 
 def test_host_binning_rejects_non_finite_and_far_coordinates(tmp_path):
@@ -218,6 +219,7 @@ def test_host_binning_rejects_non_finite_and_far_coordinates(tmp_path):
         with pytest.raises(cg.ComdgbError) as ei:
             cg.read_clsman(clsman(bad), pot, 1.0, -1)
         assert ei.value.code == -12, bad  # COMDGB_ERR_BOXRANGE
+        assert "one.inp" in str(ei.value) and "not finite" in str(ei.value), str(ei.value)
 
 
 def test_clsman_count_beyond_the_file_is_an_io_error(tmp_path):
@@ -229,6 +231,7 @@ def test_clsman_count_beyond_the_file_is_an_io_error(tmp_path):
     with pytest.raises(cg.ComdgbError) as ei:
         cg.read_clsman(str(p), pot, 1.0, -1)
     assert ei.value.code == -33  # COMDGB_ERR_IO
+    assert "huge.inp" in str(ei.value), str(ei.value)
 
 
 @pytest.mark.parametrize("nbx", [(64, 64, 8), (2**31 - 1,) * 3, (128, 128, 2**31 - 1)])
@@ -259,6 +262,7 @@ def test_grid_beyond_int_slot_indexes_is_an_argument_error():
         with pytest.raises(cg.ComdgbError) as ei:
             cg.fcc(n, n, n, 3.615, 1.0, 1.0, pot)
         assert ei.value.code == -1, n  # COMDGB_ERR_ARG
+        assert "slot indexes" in cg.lib.last_error()
     with pytest.raises(cg.ComdgbError) as ei:
         cg.fcc(1, 1, 1, 3.615, 1.0, 1.0, pot)  # 3.615 A < the 4.961 A cutoff
     assert ei.value.code == -3  # COMDGB_ERR_NOBOX
