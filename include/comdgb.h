@@ -422,7 +422,11 @@ int comdgb_put_atoms_noalloc(const int nbx[3], const double bounds[3], const dou
                              int *natoms, int *id, int *itype, double *mass, double *r, double *p,
                              int device, void *stream);
 
+/* The message of the last failing call made by the calling thread (each
+ * thread has its own), copied into buf and truncated to len - 1 characters
+ * (buf may be NULL); returns the message's full length. */
 int comdgb_last_error(char *buf, int len);
+/* "comdgb <version> sm_103a" */
 const char *comdgb_version(void);
 
 #ifdef __cplusplus
