@@ -138,6 +138,7 @@ int comdgb_sim_force(comdgb_sim *h);
 /* n steps + final force on the GPU state; dt in seconds; captured in a
  * CUDA graph after the first call with the same dt */
 int comdgb_sim_steps(comdgb_sim *h, int n, double dt);
+/* reBoxAll (domains.c:347-389) on the GPU state */
 int comdgb_sim_rebox(comdgb_sim *h);
 /* advanceVelocity (timestep.c:62-74): p -= dt f; dt in the reference's
  * internal time unit (seconds * 0.529/2.418e-17, timestep.c:126) */
@@ -150,6 +151,7 @@ int comdgb_sim_energy(comdgb_sim *h, double *e, double *stress);
 int comdgb_sim_kinetic(comdgb_sim *h, double *ek);
 /* device-side counters: unique in-cutoff pairs of the last force call */
 int comdgb_sim_pair_count(comdgb_sim *h, long long *pairs);
+/* waits for the handle's queued GPU work (COMDGB_ERR_CUDA if it failed) */
 int comdgb_sim_synchronize(comdgb_sim *h);
 
 /* Timed run for benchmarks: `n` steps (graph replays), events recorded on
@@ -231,6 +233,8 @@ int comdgb_round_f32(const double *x, float *y, long n);
  * downloads go per replica. */
 int comdgb_batch_create(const simflat_t *const *sims, int n, const comdgb_opts *o,
                         comdgb_sim **out);
+/* the number of replicas; replica r's host state to the GPU (s must have
+ * the replica's grid) and back */
 int comdgb_batch_replicas(comdgb_sim *h);
 int comdgb_batch_upload(comdgb_sim *h, int r, const simflat_t *s);
 int comdgb_batch_download(comdgb_sim *h, int r, simflat_t *s);
@@ -387,6 +391,8 @@ void comdgb_printIt(const simflat_t *s, FILE *fp);
  * the caller reboxes */
 void comdgb_seed(simflat_t *s, uint64_t seed, int disp_kind, double amp, double temp_k,
                  double mass_amu);
+/* frees a host simflat_t made by comdgb_fcc, comdgb_read_clsman,
+ * comdgb_read_tim or comdgb_rebin_host (not its potential) */
 void comdgb_sim_free_host(simflat_t *s);
 /* reBoxAll on the host simflat_t via the GPU (upload, rebox, download) */
 int comdgb_rebox_host(simflat_t *s, int periodic, int device);
